@@ -1,0 +1,226 @@
+/*
+ * phys-engine-gb300 — C ABI of the GPU collision-and-contact path.
+ *
+ * Drop-in boundary for bkuangs/phys-engine's PhysicsWorld::step(dt) hot path
+ * (src/world/physics_world.cpp:518-782).  The reference exposes C++ classes
+ * only; each entry point below names the reference member it replaces.  Plain
+ * pointers and sizes only; all device memory is owned by the library.
+ *
+ * Errors: every function returns a pe_status; pe_last_error() holds the
+ * message of the calling thread's last failure.  Reference exceptions map to
+ * PE_ERR_INVALID_ARGUMENT, factory `false` returns to PE_ERR_CREATE_FAILED,
+ * and `nullptr` from getBody/getCollider to PE_ERR_STALE_HANDLE.
+ *
+ * Threading: a world is used from one host thread at a time (the reference
+ * world is not thread-safe either); each world owns one CUDA stream.
+ */
+#ifndef PHYS_GB300_H
+#define PHYS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pe_status {
+    PE_OK = 0,
+    PE_ERR_INVALID_ARGUMENT = 1, /* the reference throws std::invalid_argument */
+    PE_ERR_CREATE_FAILED = 2,    /* createSphere/createBox returned false */
+    PE_ERR_STALE_HANDLE = 3,     /* getBody/getCollider returned nullptr */
+    PE_ERR_CAPACITY = 4,         /* caller buffer too small; *count holds the size needed */
+    PE_ERR_UNSUPPORTED = 5,      /* e.g. BroadPhaseAlgorithm::DynamicTree on the GPU path */
+    PE_ERR_CUDA = 6,             /* CUDA runtime failure (no device, out of memory, ...) */
+    PE_ERR_DEVICE = 7            /* device-side failure: a bounded wait timed out, colour overflow */
+} pe_status;
+
+/* BroadPhaseAlgorithm (include/phys/collision/broadphase.hpp:8-13) */
+enum { PE_BROADPHASE_SAP = 0, PE_BROADPHASE_GRID = 1, PE_BROADPHASE_TREE = 2 };
+/* Collider shapes: Sphere, Box (include/phys/collision/collider.hpp:27) and a
+   convex hull (absent from the reference, which only forward-declares one). */
+enum { PE_SHAPE_SPHERE = 0, PE_SHAPE_BOX = 1, PE_SHAPE_HULL = 2 };
+/* Solver order: the reference's manifold order (one manifold at a time) or the
+   GPU's graph-colour order. */
+enum { PE_ORDER_MANIFOLD = 0, PE_ORDER_COLOR = 1 };
+
+/* RigidBodyHandle / ColliderHandle (include/phys/world/body_handle.hpp:6-15,
+   include/phys/collision/collider.hpp:12-16) */
+typedef struct pe_handle {
+    uint32_t index;
+    uint32_t generation;
+} pe_handle;
+
+/* Public RigidBody state (include/phys/dynamics/rigid_body.hpp:14-140). */
+typedef struct pe_body_state {
+    float position[3];
+    float rotation[4]; /* quaternion x, y, z, w */
+    float linear_velocity[3];
+    float angular_velocity[3];
+    float force[3];
+    float mass;
+    float restitution;
+    float friction;
+    int32_t is_static;
+} pe_body_state;
+
+/* ContactManifold + ContactPoint (include/phys/collision/manifold.hpp:9-34) with
+   per-point feature ids added.  216 bytes. */
+typedef struct pe_contact_manifold {
+    uint32_t body_a_index, body_a_generation;
+    uint32_t body_b_index, body_b_generation;
+    float normal[3]; /* from body A toward body B */
+    uint32_t point_count;
+    float friction;
+    float restitution;
+    float anchor_a[4][3]; /* localAnchorA per point (body A space) */
+    float anchor_b[4][3]; /* localAnchorB per point (body B space) */
+    float penetration[4];
+    float normal_impulse[4];
+    float tangent_impulse1[4];
+    float tangent_impulse2[4];
+    uint32_t feature[4]; /* (kind << 24) | (source << 16) | (face axis << 8) | (face sign << 4) | vertex */
+} pe_contact_manifold;
+
+/* StepStats with BroadPhaseStats / NarrowPhaseStats / SolverStats counters
+   (include/phys/world/step_stats.hpp:7-54, broadphase.hpp:21-42).  Stage
+   timings are replaced by the device time of the whole step. */
+typedef struct pe_step_stats {
+    uint64_t possible_pairs;
+    uint64_t candidate_pairs;
+    uint64_t contact_count;
+    uint64_t solved_contact_count;
+    uint64_t awake_body_count;
+    uint64_t sleeping_body_count;
+    uint64_t x_window_comparisons;
+    uint64_t aabb_pairs;
+    uint64_t grid_comparisons;
+    uint64_t grid_entries;
+    uint64_t grid_overflow_aabbs;
+    double grid_cell_size;
+    uint64_t np_candidates[4]; /* sphere-sphere, sphere-box, box-box, hull-any */
+    uint64_t np_contacts[4];
+    uint64_t prepared_points;
+    uint64_t warm_start_comparisons;
+    uint64_t warm_start_matches;
+    uint64_t velocity_point_visits;
+    uint64_t color_count;
+    uint64_t color_rounds;
+    uint64_t epa_failures;
+    uint64_t contact_points;
+    double total_ms; /* device time of the step */
+} pe_step_stats;
+
+typedef struct pe_world pe_world;
+
+const char *pe_last_error(void);
+/* Library / device check: number of CUDA devices visible. */
+int pe_device_count(void);
+
+/* PhysicsWorld::PhysicsWorld() / ~PhysicsWorld() (physics_world.hpp:24-25) */
+pe_status pe_world_create(int device, pe_world **out);
+void pe_world_destroy(pe_world *world);
+
+/* PhysicsWorld::gravity (physics_world.hpp:37) */
+pe_status pe_world_set_gravity(pe_world *world, float x, float y, float z);
+pe_status pe_world_get_gravity(const pe_world *world, float *xyz);
+/* PhysicsWorld::broadPhaseAlgorithm (physics_world.hpp:38); DynamicTree is
+   accepted here and rejected by pe_world_step with PE_ERR_UNSUPPORTED. */
+pe_status pe_world_set_broadphase(pe_world *world, int algorithm);
+pe_status pe_world_get_broadphase(const pe_world *world, int *algorithm);
+/* Grid cell size: <= 0 keeps the reference's median policy
+   (src/collision/broadphase.cpp:98-110); > 0 fixes it.  No reference counterpart. */
+pe_status pe_world_set_grid_cell_size(pe_world *world, double cell_size);
+/* Solver iteration count (the reference hard-codes 8,
+   src/solver/sequential_impulse_solver.cpp:235) and order (PE_ORDER_*). */
+pe_status pe_world_set_solver(pe_world *world, int iterations, int order);
+/* setNarrowPhaseWorkerCount / setSolverWorkerCount / setBroadPhaseWorkerCount
+   (physics_world.hpp:66-73): validated like the reference (0 is invalid); the
+   GPU path has no host worker threads. */
+pe_status pe_world_set_worker_counts(pe_world *world, uint64_t narrowphase, uint64_t solver, uint64_t broadphase);
+/* setSleepingEnabled (physics_world.hpp:63): only `false` is supported. */
+pe_status pe_world_set_sleeping_enabled(pe_world *world, int enabled);
+
+/* createSphere / createBox (physics_world.hpp:43-50): same validation and mass
+   properties as RigidBody::createSphere / createBox (src/dynamics/rigid_body.cpp:25-91). */
+pe_status pe_world_create_sphere(pe_world *world, float radius, const float *position, float density,
+                                 int is_static, float restitution, float friction, pe_handle *body,
+                                 pe_handle *collider);
+pe_status pe_world_create_box(pe_world *world, float width, float height, float depth, const float *position,
+                              float density, int is_static, float restitution, float friction, pe_handle *body,
+                              pe_handle *collider);
+/* Bulk creation of n sphere/box bodies, each exactly as createSphere/createBox
+   followed by setLinearVelocity(linear_velocity) and the reference's
+   orientation idiom setAngularVelocity(spin); integrateRotation(1);
+   setAngularVelocity(0) (tests/solver/sequential_impulse_solver_tests.cpp:349-351).
+   dims: radius or width/height/depth per body; linear_velocity and spin may be
+   NULL.  On a validation failure returns PE_ERR_CREATE_FAILED with the failing
+   index in *failed_index; bodies before it stay created.  No reference counterpart. */
+pe_status pe_world_create_bodies(pe_world *world, uint32_t n, const uint8_t *shape, const float *dims,
+                                 const float *position, const float *density, const uint8_t *is_static,
+                                 const float *restitution, const float *friction, const float *linear_velocity,
+                                 const float *spin, pe_handle *bodies, pe_handle *colliders, uint32_t *failed_index);
+/* Convex hull body (no reference counterpart): vertices in body space, mass and
+   diagonal inverse inertia supplied by the caller. */
+pe_status pe_world_create_hull(pe_world *world, const float *vertices, uint32_t vertex_count,
+                               const float *position, float mass, const float *inverse_inertia, int is_static,
+                               float restitution, float friction, pe_handle *body, pe_handle *collider);
+/* addCollider (physics_world.hpp:57) for an existing body, with a local transform. */
+pe_status pe_world_add_collider(pe_world *world, pe_handle body, int shape, const float *dims,
+                                const float *local_position, const float *local_rotation, pe_handle *collider);
+/* removeBody / removeCollider (physics_world.hpp:41, 58) */
+pe_status pe_world_remove_body(pe_world *world, pe_handle body);
+pe_status pe_world_remove_collider(pe_world *world, pe_handle collider);
+
+/* getBody (physics_world.hpp:54-55) read / write of the public state. */
+pe_status pe_world_get_body(pe_world *world, pe_handle body, pe_body_state *out);
+pe_status pe_world_set_body(pe_world *world, pe_handle body, const pe_body_state *state);
+/* RigidBody::integrateRotation (rigid_body.cpp:110-125) on one body; with
+   dt = 1 and an angular velocity this is the reference's orientation idiom. */
+pe_status pe_world_body_integrate_rotation(pe_world *world, pe_handle body, float dt);
+
+/* Bulk state by body slot (positions xyz, quaternions xyzw, linear and angular
+   velocity xyz); any pointer may be NULL.  No reference counterpart. */
+uint32_t pe_world_body_slot_count(pe_world *world);
+pe_status pe_world_read_bodies(pe_world *world, float *positions, float *rotations, float *linear,
+                               float *angular);
+
+/* PhysicsWorld::step (physics_world.hpp:75) */
+pe_status pe_world_step(pe_world *world, float dt);
+/* lastStepStats (physics_world.hpp:77) */
+pe_status pe_world_get_step_stats(const pe_world *world, pe_step_stats *out);
+/* contacts() (physics_world.hpp:61): manifolds of the last step in candidate
+   pair order with their solved impulses. */
+pe_status pe_world_get_contacts(pe_world *world, pe_contact_manifold *out, uint32_t capacity, uint32_t *count);
+/* Candidate collider-slot pairs of the last step (lexicographic), as the
+   broadphase + same-body filter produce them (physics_world.cpp:620-633). */
+pe_status pe_world_get_candidate_pairs(pe_world *world, uint32_t *pairs, uint32_t capacity, uint32_t *count);
+/* Solve order of the last step: order[k] = manifold index solved k-th,
+   colors[m] = colour of manifold m. */
+pe_status pe_world_get_solve_order(pe_world *world, uint32_t *order, uint32_t *colors, uint32_t capacity,
+                                   uint32_t *count);
+
+/* SequentialImpulseSolver::solve(contacts, world, dt)
+   (include/phys/solver/sequential_impulse_solver.hpp:17): solves the given
+   manifolds against the world's bodies with the world's solver settings,
+   writing impulses back into `contacts` and updating the warm-start cache. */
+pe_status pe_world_solve(pe_world *world, pe_contact_manifold *contacts, uint32_t count, float dt);
+
+/* BroadPhase::findCandidatePairs (include/phys/collision/broadphase.hpp:52-54):
+   mins/maxs are n xyz triples; pairs receives 2*count indices in lexicographic
+   order (first < second); stats may be NULL. */
+pe_status pe_broadphase_find_pairs(int device, const float *mins, const float *maxs, uint32_t n, int algorithm,
+                                   double cell_size, uint32_t *pairs, uint64_t capacity, uint64_t *count,
+                                   pe_step_stats *stats);
+/* NarrowPhase::generateContact (include/phys/collision/narrowphase.hpp:34-39)
+   for sphere/box colliders given world transforms (position xyz, rotation
+   xyzw); dims = radius or half extents.  *hit = 1 when a manifold is produced. */
+pe_status pe_generate_contact(int device, int shape_a, const float *dims_a, const float *pos_a, const float *rot_a,
+                              int shape_b, const float *dims_b, const float *pos_b, const float *rot_b,
+                              pe_contact_manifold *out, int *hit);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,580 @@
+// C ABI (include/phys_gb300.h) over the GPU world.
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+
+#include "phys_gb300.h"
+#include "world.h"
+
+struct pe_world {
+    std::unique_ptr<pe::World> w;
+    uint64_t npWorkers = 1, solverWorkers = 1, bpWorkers = 1;
+};
+
+namespace {
+
+thread_local std::string g_lastError;
+
+pe_status fail(pe_status s, const std::string &msg) {
+    g_lastError = msg;
+    return s;
+}
+
+template <class F> pe_status guarded(F &&f) {
+    try {
+        return f();
+    } catch (const std::invalid_argument &e) {
+        return fail(PE_ERR_INVALID_ARGUMENT, e.what());
+    } catch (const pe::CudaError &e) {
+        return fail(PE_ERR_CUDA, e.what());
+    } catch (const std::bad_alloc &e) {
+        return fail(PE_ERR_CUDA, e.what());
+    } catch (const std::exception &e) {
+        return fail(PE_ERR_DEVICE, e.what());
+    }
+}
+
+// Per-device world for the stateless stage entry points.
+std::mutex g_utilMutex;
+std::map<int, std::unique_ptr<pe::World>> g_util;
+pe::World &utilWorld(int device) {
+    auto &slot = g_util[device];
+    if (!slot) slot.reset(new pe::World(device));
+    return *slot;
+}
+
+void fillStats(const pe::StepCounters &c, pe_step_stats *o) {
+    std::memset(o, 0, sizeof(*o));
+    o->possible_pairs = c.possiblePairs;
+    o->candidate_pairs = c.candidatePairs;
+    o->contact_count = c.contactCount;
+    o->solved_contact_count = c.solvedContactCount;
+    o->awake_body_count = c.awakeBodyCount;
+    o->sleeping_body_count = 0;
+    o->x_window_comparisons = c.xWindow;
+    o->aabb_pairs = c.aabbPairs;
+    o->grid_comparisons = c.gridComparisons;
+    o->grid_entries = c.gridEntries;
+    o->grid_overflow_aabbs = c.gridOverflow;
+    o->grid_cell_size = c.cellSize;
+    for (int k = 0; k < 4; ++k) {
+        o->np_candidates[k] = c.npCandidates[k];
+        o->np_contacts[k] = c.npContacts[k];
+    }
+    o->prepared_points = c.preparedPoints;
+    o->warm_start_comparisons = c.warmComparisons;
+    o->warm_start_matches = c.warmMatches;
+    o->velocity_point_visits = c.velocityPointVisits;
+    o->color_count = c.colors;
+    o->color_rounds = c.colorRounds;
+    o->epa_failures = c.epaFailures;
+    o->contact_points = c.points;
+    o->total_ms = c.gpuMs;
+}
+
+// RigidBody::createSphere / createBox validation and mass properties
+// (src/dynamics/rigid_body.cpp:25-91, src/dynamics/mass_properties.cpp:5-32,
+// include/phys/core/constants.hpp:5-16).  Returns an error message or nullptr.
+const char *makeBody(int shape, const float *dims, const float *pos, float density, int isStatic, float restitution,
+                     float friction, pe::HostBody &b) {
+    const float pi = 3.14159265358979323846f;
+    const float minSize = 0.01f * 0.01f, maxSize = 64.0f * 64.0f;
+    float volume;
+    if (shape == PE_SHAPE_SPHERE) {
+        float r = dims[0];
+        volume = (4.0f / 3.0f) * pi * r * r * r;
+        if (volume < minSize) return "Sphere is too small";
+        if (volume > maxSize) return "Sphere is too large";
+    } else {
+        if (dims[0] <= 0.0f || dims[1] <= 0.0f || dims[2] <= 0.0f) return "Box dimensions must be positive";
+        volume = dims[0] * dims[1] * dims[2];
+        if (volume < minSize) return "Box is too small";
+        if (volume > maxSize) return "Box is too large";
+    }
+    if (!(density >= 0.2f && density <= 21.4f)) return "Density is out of range";
+    float rest = restitution;
+    if (rest < 0.0f) rest = 0.0f;
+    if (rest > 1.0f) rest = 1.0f;
+    const float mass = volume * density;
+    b = pe::HostBody{};
+    b.mass = mass;
+    b.restitution = rest;
+    b.friction = friction < 0.0f ? 0.0f : friction;
+    b.isStatic = isStatic != 0;
+    b.pos[0] = pos[0];
+    b.pos[1] = pos[1];
+    b.pos[2] = pos[2];
+    if (!isStatic) {
+        if (shape == PE_SHAPE_SPHERE) {
+            float r = dims[0];
+            if (mass > 0.0f && r > 0.0f) {
+                float ii = 1.0f / (0.4f * mass * r * r);
+                b.iinv[0] = b.iinv[1] = b.iinv[2] = ii;
+            }
+        } else if (mass > 0.0f) {
+            float w = dims[0], h = dims[1], d = dims[2];
+            float factor = 12.0f / mass;
+            b.iinv[0] = factor / (h * h + d * d);
+            b.iinv[1] = factor / (w * w + d * d);
+            b.iinv[2] = factor / (w * w + h * h);
+        }
+    }
+    return nullptr;
+}
+
+pe_status createBody(pe_world *world, int shape, const float *dims, const float *pos, float density, int isStatic,
+                     float restitution, float friction, pe_handle *body, pe_handle *collider) {
+    if (!world || !dims || !pos) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    pe::HostBody b;
+    if (const char *err = makeBody(shape, dims, pos, density, isStatic, restitution, friction, b))
+        return fail(PE_ERR_CREATE_FAILED, err);
+    uint32_t bg, cg;
+    uint32_t bi = world->w->addBody(b, bg);
+    pe::HostCollider c;
+    c.body = bi;
+    c.bodyGeneration = bg;
+    c.shape = (uint32_t)shape;
+    if (shape == PE_SHAPE_SPHERE) {
+        c.dims[0] = dims[0];
+    } else {
+        // PhysicsWorld::createBox stores half extents (physics_world.cpp:218)
+        c.dims[0] = dims[0] * 0.5f;
+        c.dims[1] = dims[1] * 0.5f;
+        c.dims[2] = dims[2] * 0.5f;
+    }
+    uint32_t ci = world->w->addCollider(c, cg);
+    if (body) *body = pe_handle{bi, bg};
+    if (collider) *collider = pe_handle{ci, cg};
+    return PE_OK;
+}
+
+// RigidBody::integrateRotation (src/dynamics/rigid_body.cpp:110-125).
+void integrateRotation(pe::HostBody &b, float dt) {
+    if (b.isStatic) return;
+    const float wx = b.ang[0], wy = b.ang[1], wz = b.ang[2];
+    const float x = b.rot[0], y = b.rot[1], z = b.rot[2], w = b.rot[3];
+    const float sw = 0.0f;
+    // spin * rotation (quaternion.hpp:24-31)
+    float dx = sw * x + wx * w + wy * z - wz * y;
+    float dy = sw * y - wx * z + wy * w + wz * x;
+    float dz = sw * z + wx * y - wy * x + wz * w;
+    float dw = sw * w - wx * x - wy * y - wz * z;
+    const float h2 = 0.5f * dt;
+    float q[4] = {x + h2 * dx, y + h2 * dy, z + h2 * dz, w + h2 * dw};
+    float len = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+    if (len == 0.0f) {
+        b.rot[0] = b.rot[1] = b.rot[2] = 0.0f;
+        b.rot[3] = 1.0f;
+    } else {
+        for (int k = 0; k < 4; ++k) b.rot[k] = q[k] / len;
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+const char *pe_last_error(void) { return g_lastError.c_str(); }
+
+int pe_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+pe_status pe_world_create(int device, pe_world **out) {
+    if (!out) return fail(PE_ERR_INVALID_ARGUMENT, "null output");
+    return guarded([&] {
+        auto *w = new pe_world;
+        try {
+            w->w.reset(new pe::World(device));
+        } catch (...) {
+            delete w;
+            throw;
+        }
+        *out = w;
+        return PE_OK;
+    });
+}
+
+void pe_world_destroy(pe_world *world) { delete world; }
+
+pe_status pe_world_set_gravity(pe_world *world, float x, float y, float z) {
+    if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
+    world->w->gravity[0] = x;
+    world->w->gravity[1] = y;
+    world->w->gravity[2] = z;
+    return PE_OK;
+}
+pe_status pe_world_get_gravity(const pe_world *world, float *xyz) {
+    if (!world || !xyz) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    std::memcpy(xyz, world->w->gravity, 3 * sizeof(float));
+    return PE_OK;
+}
+pe_status pe_world_set_broadphase(pe_world *world, int algorithm) {
+    if (!world || algorithm < 0 || algorithm > 2) return fail(PE_ERR_INVALID_ARGUMENT, "unknown broadphase algorithm");
+    world->w->algorithm = algorithm;
+    return PE_OK;
+}
+pe_status pe_world_get_broadphase(const pe_world *world, int *algorithm) {
+    if (!world || !algorithm) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    *algorithm = world->w->algorithm;
+    return PE_OK;
+}
+pe_status pe_world_set_grid_cell_size(pe_world *world, double cell) {
+    if (!world || !std::isfinite(cell)) return fail(PE_ERR_INVALID_ARGUMENT, "cell size must be finite");
+    world->w->cellSize = cell;
+    return PE_OK;
+}
+pe_status pe_world_set_solver(pe_world *world, int iterations, int order) {
+    if (!world || iterations < 0 || (order != PE_ORDER_MANIFOLD && order != PE_ORDER_COLOR))
+        return fail(PE_ERR_INVALID_ARGUMENT, "invalid solver settings");
+    world->w->iterations = iterations;
+    world->w->orderMode = order;
+    return PE_OK;
+}
+pe_status pe_world_set_worker_counts(pe_world *world, uint64_t np, uint64_t solver, uint64_t bp) {
+    if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
+    // physics_world.cpp:132-160
+    if (np == 0) return fail(PE_ERR_INVALID_ARGUMENT, "Narrowphase worker count must be positive");
+    if (solver == 0) return fail(PE_ERR_INVALID_ARGUMENT, "Solver worker count must be positive");
+    if (bp == 0) return fail(PE_ERR_INVALID_ARGUMENT, "Broadphase worker count must be positive");
+    world->npWorkers = np;
+    world->solverWorkers = solver;
+    world->bpWorkers = bp;
+    return PE_OK;
+}
+pe_status pe_world_set_sleeping_enabled(pe_world *world, int enabled) {
+    if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
+    if (enabled) return fail(PE_ERR_UNSUPPORTED, "sleeping islands are not part of the GPU path");
+    return PE_OK;
+}
+
+pe_status pe_world_create_sphere(pe_world *world, float radius, const float *position, float density, int is_static,
+                                 float restitution, float friction, pe_handle *body, pe_handle *collider) {
+    float dims[3] = {radius, 0.0f, 0.0f};
+    return guarded(
+        [&] { return createBody(world, PE_SHAPE_SPHERE, dims, position, density, is_static, restitution, friction, body, collider); });
+}
+
+pe_status pe_world_create_box(pe_world *world, float width, float height, float depth, const float *position,
+                              float density, int is_static, float restitution, float friction, pe_handle *body,
+                              pe_handle *collider) {
+    float dims[3] = {width, height, depth};
+    return guarded(
+        [&] { return createBody(world, PE_SHAPE_BOX, dims, position, density, is_static, restitution, friction, body, collider); });
+}
+
+pe_status pe_world_create_hull(pe_world *world, const float *vertices, uint32_t n, const float *position, float mass,
+                               const float *iinv, int is_static, float restitution, float friction, pe_handle *body,
+                               pe_handle *collider) {
+    if (!world || !vertices || n == 0 || n > 255 || !position || !iinv)
+        return fail(PE_ERR_INVALID_ARGUMENT, "hull needs 1..255 vertices, a position and an inverse inertia");
+    return guarded([&] {
+        pe::HostBody b;
+        b.mass = mass;
+        b.restitution = restitution;
+        b.friction = friction;
+        b.isStatic = is_static != 0;
+        std::memcpy(b.pos, position, 3 * sizeof(float));
+        if (!is_static) std::memcpy(b.iinv, iinv, 3 * sizeof(float));
+        uint32_t bg, cg;
+        uint32_t bi = world->w->addBody(b, bg);
+        pe::HostCollider c;
+        c.body = bi;
+        c.bodyGeneration = bg;
+        c.shape = PE_SHAPE_HULL;
+        c.hull = (uint32_t)world->w->addHull(vertices, n);
+        uint32_t ci = world->w->addCollider(c, cg);
+        if (body) *body = pe_handle{bi, bg};
+        if (collider) *collider = pe_handle{ci, cg};
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_add_collider(pe_world *world, pe_handle body, int shape, const float *dims, const float *lpos,
+                                const float *lrot, pe_handle *collider) {
+    if (!world || !dims || (shape != PE_SHAPE_SPHERE && shape != PE_SHAPE_BOX))
+        return fail(PE_ERR_INVALID_ARGUMENT, "sphere or box collider expected");
+    return guarded([&] {
+        world->w->pull();
+        // PhysicsWorld::addCollider returns an empty handle for a stale body
+        // (physics_world.cpp:276-281).
+        if (!world->w->body(body.index, body.generation)) {
+            if (collider) *collider = pe_handle{0, 0};
+            return fail(PE_ERR_STALE_HANDLE, "stale body handle");
+        }
+        pe::HostCollider c;
+        c.body = body.index;
+        c.bodyGeneration = body.generation;
+        c.shape = (uint32_t)shape;
+        std::memcpy(c.dims, dims, 3 * sizeof(float));
+        if (lpos) std::memcpy(c.lpos, lpos, 3 * sizeof(float));
+        if (lrot) std::memcpy(c.lrot, lrot, 4 * sizeof(float));
+        uint32_t g;
+        uint32_t i = world->w->addCollider(c, g);
+        if (collider) *collider = pe_handle{i, g};
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_remove_body(pe_world *world, pe_handle body) {
+    if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
+    return guarded([&] {
+        world->w->removeBody(body.index, body.generation);
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_remove_collider(pe_world *world, pe_handle collider) {
+    if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
+    return guarded([&] {
+        world->w->removeCollider(collider.index, collider.generation);
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_get_body(pe_world *world, pe_handle h, pe_body_state *out) {
+    if (!world || !out) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        world->w->pull();
+        pe::HostBody *b = world->w->body(h.index, h.generation);
+        if (!b) return fail(PE_ERR_STALE_HANDLE, "stale body handle");
+        std::memcpy(out->position, b->pos, sizeof(out->position));
+        std::memcpy(out->rotation, b->rot, sizeof(out->rotation));
+        std::memcpy(out->linear_velocity, b->lin, sizeof(out->linear_velocity));
+        std::memcpy(out->angular_velocity, b->ang, sizeof(out->angular_velocity));
+        std::memcpy(out->force, b->force, sizeof(out->force));
+        out->mass = b->mass;
+        out->restitution = b->restitution;
+        out->friction = b->friction;
+        out->is_static = b->isStatic ? 1 : 0;
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_set_body(pe_world *world, pe_handle h, const pe_body_state *in) {
+    if (!world || !in) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        world->w->pull();
+        pe::HostBody *b = world->w->body(h.index, h.generation);
+        if (!b) return fail(PE_ERR_STALE_HANDLE, "stale body handle");
+        std::memcpy(b->pos, in->position, sizeof(b->pos));
+        std::memcpy(b->rot, in->rotation, sizeof(b->rot));
+        std::memcpy(b->lin, in->linear_velocity, sizeof(b->lin));
+        std::memcpy(b->ang, in->angular_velocity, sizeof(b->ang));
+        // RigidBody::applyForce ignores static bodies (rigid_body.hpp:77-84)
+        if (!in->is_static) std::memcpy(b->force, in->force, sizeof(b->force));
+        b->mass = in->mass;
+        b->restitution = in->restitution;
+        b->friction = in->friction;
+        b->isStatic = in->is_static != 0;
+        world->w->touch();
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_body_integrate_rotation(pe_world *world, pe_handle h, float dt) {
+    if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
+    return guarded([&] {
+        world->w->pull();
+        pe::HostBody *b = world->w->body(h.index, h.generation);
+        if (!b) return fail(PE_ERR_STALE_HANDLE, "stale body handle");
+        integrateRotation(*b, dt);
+        world->w->touch();
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_create_bodies(pe_world *world, uint32_t n, const uint8_t *shape, const float *dims,
+                                 const float *position, const float *density, const uint8_t *is_static,
+                                 const float *restitution, const float *friction, const float *linear_velocity,
+                                 const float *spin, pe_handle *bodies, pe_handle *colliders, uint32_t *failed_index) {
+    if (!world || (n && (!shape || !dims || !position || !density || !is_static || !restitution || !friction)))
+        return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        for (uint32_t i = 0; i < n; ++i) {
+            if (shape[i] != PE_SHAPE_SPHERE && shape[i] != PE_SHAPE_BOX)
+                return fail(PE_ERR_INVALID_ARGUMENT, "sphere or box shapes expected");
+            pe_handle b, c;
+            pe_status st = createBody(world, shape[i], dims + 3 * (size_t)i, position + 3 * (size_t)i, density[i],
+                                      is_static[i], restitution[i], friction[i], &b, &c);
+            if (st != PE_OK) {
+                if (failed_index) *failed_index = i;
+                return st;
+            }
+            pe::HostBody *hb = world->w->body(b.index, b.generation);
+            if (linear_velocity) {
+                // RigidBody::setLinearVelocity (rigid_body.hpp:59-63)
+                hb->lin[0] = linear_velocity[3 * (size_t)i];
+                hb->lin[1] = linear_velocity[3 * (size_t)i + 1];
+                hb->lin[2] = linear_velocity[3 * (size_t)i + 2];
+            }
+            if (spin && (spin[3 * (size_t)i] != 0.0f || spin[3 * (size_t)i + 1] != 0.0f || spin[3 * (size_t)i + 2] != 0.0f)) {
+                hb->ang[0] = spin[3 * (size_t)i];
+                hb->ang[1] = spin[3 * (size_t)i + 1];
+                hb->ang[2] = spin[3 * (size_t)i + 2];
+                integrateRotation(*hb, 1.0f);
+                hb->ang[0] = hb->ang[1] = hb->ang[2] = 0.0f;
+            }
+            if (bodies) bodies[i] = b;
+            if (colliders) colliders[i] = c;
+        }
+        world->w->touch();
+        return PE_OK;
+    });
+}
+
+uint32_t pe_world_body_slot_count(pe_world *world) { return world ? (uint32_t)world->w->bodies.size() : 0u; }
+
+pe_status pe_world_read_bodies(pe_world *world, float *pos, float *rot, float *lin, float *ang) {
+    if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
+    return guarded([&] {
+        world->w->pull();
+        const auto &bs = world->w->bodies;
+        for (size_t i = 0; i < bs.size(); ++i) {
+            if (pos) std::memcpy(pos + 3 * i, bs[i].pos, 3 * sizeof(float));
+            if (rot) std::memcpy(rot + 4 * i, bs[i].rot, 4 * sizeof(float));
+            if (lin) std::memcpy(lin + 3 * i, bs[i].lin, 3 * sizeof(float));
+            if (ang) std::memcpy(ang + 3 * i, bs[i].ang, 3 * sizeof(float));
+        }
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_step(pe_world *world, float dt) {
+    if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
+    if (world->w->algorithm == PE_BROADPHASE_TREE)
+        return fail(PE_ERR_UNSUPPORTED, "DynamicTree broadphase is not part of the GPU path");
+    return guarded([&] {
+        world->w->step(dt);
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_get_step_stats(const pe_world *world, pe_step_stats *out) {
+    if (!world || !out) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    fillStats(world->w->counters(), out);
+    return PE_OK;
+}
+
+pe_status pe_world_get_contacts(pe_world *world, pe_contact_manifold *out, uint32_t capacity, uint32_t *count) {
+    if (!world || !count) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        uint32_t m = world->w->manifoldCount();
+        *count = m;
+        if (!out || capacity < m) return m == 0 ? PE_OK : fail(PE_ERR_CAPACITY, "contact buffer too small");
+        world->w->downloadManifolds(out, m);
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_get_candidate_pairs(pe_world *world, uint32_t *pairs, uint32_t capacity, uint32_t *count) {
+    if (!world || !count) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        uint32_t p = world->w->pairCount();
+        *count = p;
+        if (!pairs || capacity < p) return p == 0 ? PE_OK : fail(PE_ERR_CAPACITY, "pair buffer too small");
+        world->w->downloadPairs(pairs);
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_get_solve_order(pe_world *world, uint32_t *order, uint32_t *colors, uint32_t capacity,
+                                   uint32_t *count) {
+    if (!world || !count) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        uint32_t m = world->w->manifoldCount();
+        *count = m;
+        if (capacity < m) return m == 0 ? PE_OK : fail(PE_ERR_CAPACITY, "order buffer too small");
+        world->w->downloadOrder(order, colors);
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_solve(pe_world *world, pe_contact_manifold *contacts, uint32_t count, float dt) {
+    if (!world || (count && !contacts)) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        std::vector<float> recs(count * (sizeof(pe_contact_manifold) / sizeof(float)));
+        if (count) std::memcpy(recs.data(), contacts, count * sizeof(pe_contact_manifold));
+        world->w->solveOnly(recs, count, dt, world->w->iterations, world->w->orderMode);
+        if (count) std::memcpy(contacts, recs.data(), count * sizeof(pe_contact_manifold));
+        return PE_OK;
+    });
+}
+
+pe_status pe_broadphase_find_pairs(int device, const float *mins, const float *maxs, uint32_t n, int algorithm,
+                                   double cell, uint32_t *pairs, uint64_t capacity, uint64_t *count,
+                                   pe_step_stats *stats) {
+    if (!count || (n && (!mins || !maxs))) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    if (algorithm == PE_BROADPHASE_TREE)
+        return fail(PE_ERR_INVALID_ARGUMENT, "DynamicTree requires a persistent DynamicAabbTree instance");
+    if (algorithm != PE_BROADPHASE_SAP && algorithm != PE_BROADPHASE_GRID)
+        return fail(PE_ERR_INVALID_ARGUMENT, "unknown broadphase algorithm");
+    return guarded([&] {
+        std::lock_guard<std::mutex> lock(g_utilMutex);
+        pe::World &w = utilWorld(device);
+        std::vector<uint32_t> out;
+        pe::StepCounters c;
+        w.broadphaseOnly(mins, maxs, n, algorithm, cell, out, c);
+        *count = out.size() / 2;
+        if (stats) fillStats(c, stats);
+        if (!pairs || capacity < *count) return *count == 0 ? PE_OK : fail(PE_ERR_CAPACITY, "pair buffer too small");
+        if (!out.empty()) std::memcpy(pairs, out.data(), out.size() * sizeof(uint32_t));
+        return PE_OK;
+    });
+}
+
+pe_status pe_generate_contact(int device, int sa, const float *da, const float *pa, const float *ra, int sb,
+                              const float *db, const float *pb, const float *rb, pe_contact_manifold *out, int *hit) {
+    if (!da || !pa || !ra || !db || !pb || !rb || !out || !hit) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    if ((sa != PE_SHAPE_SPHERE && sa != PE_SHAPE_BOX) || (sb != PE_SHAPE_SPHERE && sb != PE_SHAPE_BOX))
+        return fail(PE_ERR_INVALID_ARGUMENT, "sphere or box shapes expected");
+    return guarded([&] {
+        std::lock_guard<std::mutex> lock(g_utilMutex);
+        pe::World &w = utilWorld(device);
+        PE_CHECK(cudaSetDevice(device));
+        float4 in[6] = {make_float4(da[0], da[1], da[2], (float)sa), make_float4(pa[0], pa[1], pa[2], 0),
+                        make_float4(ra[0], ra[1], ra[2], ra[3]),     make_float4(db[0], db[1], db[2], (float)sb),
+                        make_float4(pb[0], pb[1], pb[2], 0),         make_float4(rb[0], rb[1], rb[2], rb[3])};
+        float4 *dIn = nullptr, *dOut = nullptr;
+        PE_CHECK(cudaMalloc(&dIn, sizeof(in)));
+        PE_CHECK(cudaMalloc(&dOut, 11 * sizeof(float4)));
+        float4 res[11];
+        try {
+            PE_CHECK(cudaMemcpyAsync(dIn, in, sizeof(in), cudaMemcpyHostToDevice, w.stream()));
+            pe::launchGeneratePairs(dIn, dOut, 1, w.stream());
+            PE_CHECK(cudaMemcpyAsync(res, dOut, sizeof(res), cudaMemcpyDeviceToHost, w.stream()));
+            PE_CHECK(cudaStreamSynchronize(w.stream()));
+        } catch (...) {
+            cudaFree(dIn);
+            cudaFree(dOut);
+            throw;
+        }
+        cudaFree(dIn);
+        cudaFree(dOut);
+        std::memset(out, 0, sizeof(*out));
+        *hit = res[0].w >= 0.0f ? 1 : 0;
+        if (!*hit) return PE_OK;
+        out->normal[0] = res[0].x;
+        out->normal[1] = res[0].y;
+        out->normal[2] = res[0].z;
+        out->point_count = (uint32_t)res[0].w;
+        for (int k = 0; k < 4; ++k) {
+            out->anchor_a[k][0] = res[1 + k].x;
+            out->anchor_a[k][1] = res[1 + k].y;
+            out->anchor_a[k][2] = res[1 + k].z;
+            out->penetration[k] = res[1 + k].w;
+            out->anchor_b[k][0] = res[5 + k].x;
+            out->anchor_b[k][1] = res[5 + k].y;
+            out->anchor_b[k][2] = res[5 + k].z;
+        }
+        std::memcpy(out->feature, &res[9], 4 * sizeof(uint32_t));
+        return PE_OK;
+    });
+}
+
+} // extern "C"

@@ -1,0 +1,367 @@
+// Broadphase kernels.  Both algorithms emit every AABB-overlapping pair of
+// input indices exactly as BroadPhase::findCandidatePairs does
+// (src/collision/broadphase.cpp:186-291): inclusive (touching) overlap on all
+// three axes, (min, max) index order; the pair list is then put into the
+// reference's lexicographic order by a radix sort of 64-bit pair keys
+// (first << 32 | second), deduplicated, mapped to collider slots and filtered
+// of same-body pairs (src/world/physics_world.cpp:623-633).
+#include "pe_kernels.cuh"
+#include "pe_stages.h"
+
+namespace pe {
+
+__device__ __forceinline__ bool overlapYZ(const float4 &f, const float4 &s) {
+    // f, s = (min.y, max.y, min.z, max.z); broadphase.cpp:233-236
+    return f.x <= s.y && f.y >= s.x && f.z <= s.w && f.w >= s.z;
+}
+__device__ __forceinline__ bool overlaps(const float4 &amn, const float4 &amx, const float4 &bmn, const float4 &bmx) {
+    // Aabb::overlaps (include/phys/collision/aabb.hpp:15-19)
+    return amn.x <= bmx.x && amx.x >= bmn.x && amn.y <= bmx.y && amx.y >= bmn.y && amn.z <= bmx.z && amx.z >= bmn.z;
+}
+__device__ __forceinline__ void emitPair(uint32_t a, uint32_t b, unsigned long long *keys, uint32_t cap,
+                                         uint32_t *count) {
+    uint32_t lo = a < b ? a : b, hi = a < b ? b : a;
+    uint32_t slot = aggregatedAppend(count);
+    if (slot < cap) keys[slot] = ((unsigned long long)lo << 32) | hi;
+}
+
+__global__ void k_step_init(DevStats *st, uint32_t inputCount) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        memset(st, 0, sizeof(DevStats));
+        st->inputCount = inputCount;
+        for (int a = 0; a < 3; ++a) {
+            st->cellLo[a] = 0x7FFFFFFF;
+            st->cellHi[a] = (int32_t)0x80000000;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- SAP ------
+__global__ void k_sap_gather(BroadInput in, const uint32_t *sortedVals, float *sMinX, float *sMaxX, float4 *sYZ,
+                             uint32_t *sIdx) {
+    const uint32_t n = *in.d_n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t idx = sortedVals[i];
+        float4 mn = in.mn[idx], mx = in.mx[idx];
+        sMinX[i] = mn.x;
+        sMaxX[i] = mx.x;
+        sYZ[i] = make_float4(mn.y, mx.y, mn.z, mx.z);
+        sIdx[i] = idx;
+    }
+}
+
+// Window of sorted entry i: entries i+1 .. e-1 with min.x <= max.x(i), the
+// reference's sweep break (broadphase.cpp:228-231).
+__global__ void k_sap_window(const uint32_t *d_n, const float *sMinX, const float *sMaxX, uint32_t *len,
+                             DevStats *st) {
+    const uint32_t n = *d_n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float x = sMaxX[i];
+        uint32_t lo = i + 1, hi = n;
+        while (lo < hi) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (sMinX[mid] > x) hi = mid;
+            else lo = mid + 1;
+        }
+        uint32_t l = lo - i - 1;
+        len[i] = l;
+        aggregatedAdd64(&st->xWindow, l);
+    }
+}
+
+// Load-balanced sweep over the flattened windows: each thread owns kSweepChunk
+// consecutive (entry, partner) items.
+constexpr uint32_t kSweepChunk = 16;
+__global__ void k_sap_emit(const uint32_t *d_n, const uint32_t *off, const uint32_t *len, const float4 *sYZ,
+                           const uint32_t *sIdx, unsigned long long *keys, uint32_t cap, DevStats *st) {
+    const uint32_t n = *d_n;
+    const uint32_t W = st->windowWork;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * kSweepChunk;
+    for (uint64_t w0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kSweepChunk; w0 < W; w0 += stride) {
+        // i = last entry with off[i] <= w0 (it has a non-empty window)
+        uint32_t lo = 0, hi = n;
+        while (lo < hi) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (off[mid] > w0) hi = mid;
+            else lo = mid + 1;
+        }
+        uint32_t i = lo - 1;
+        uint32_t j = i + 1 + (uint32_t)(w0 - off[i]);
+        uint32_t end = i + 1 + len[i];
+        float4 f = sYZ[i];
+        uint32_t fi = sIdx[i];
+        uint64_t wEnd = w0 + kSweepChunk < W ? w0 + kSweepChunk : W;
+        for (uint64_t w = w0; w < wEnd; ++w) {
+            if (overlapYZ(f, sYZ[j])) emitPair(fi, sIdx[j], keys, cap, &st->rawPairs);
+            if (++j == end && w + 1 < wEnd) {
+                do { ++i; } while (len[i] == 0);
+                j = i + 1;
+                end = i + 1 + len[i];
+                f = sYZ[i];
+                fi = sIdx[i];
+            }
+        }
+    }
+}
+
+// --------------------------------------------------------------- grid ------
+// Widths for the median cell size (broadphase.cpp:94-110).
+__global__ void k_grid_widths(BroadInput in, unsigned long long *keys, uint32_t *count) {
+    const uint32_t n = *in.d_n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 mn = in.mn[i], mx = in.mx[i];
+        double wx = (double)mx.x - (double)mn.x, wy = (double)mx.y - (double)mn.y, wz = (double)mx.z - (double)mn.z;
+        double w = wx;
+        if (w < wy) w = wy;
+        if (w < wz) w = wz;
+        bool ok = w > 0.0 && isfinite(w);
+        keys[i] = ok ? (unsigned long long)__double_as_longlong(w) : ~0ull;
+        if (ok) aggregatedAppend(count);
+    }
+}
+
+__global__ void k_grid_cellsize(const unsigned long long *sortedWidths, const uint32_t *count, double fixedCell,
+                                DevStats *st) {
+    double cell = 1.0;
+    if (fixedCell > 0.0) cell = fixedCell;
+    else if (*count > 0) cell = __longlong_as_double((long long)sortedWidths[*count / 2]);
+    st->cellSize = cell;
+}
+
+// gridRange (broadphase.cpp:62-88) per input box.
+__global__ void k_grid_range(BroadInput in, DevStats *st, int4 *firstCell, uint32_t *cellCount, uint8_t *inGrid,
+                             uint32_t *overflow) {
+    const uint32_t n = *in.d_n;
+    const double cell = st->cellSize;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 mn = in.mn[i], mx = in.mx[i];
+        double lower[3] = {floor((double)mn.x / cell), floor((double)mn.y / cell), floor((double)mn.z / cell)};
+        double upper[3] = {floor((double)mx.x / cell), floor((double)mx.y / cell), floor((double)mx.z / cell)};
+        uint64_t total = 1;
+        int32_t first[3];
+        int counts[3];
+        bool ok = true;
+        for (int a = 0; a < 3 && ok; ++a) {
+            if (!isfinite(lower[a]) || !isfinite(upper[a]) || lower[a] < -2147483648.0 || upper[a] > 2147483647.0 ||
+                lower[a] > upper[a]) {
+                ok = false;
+                break;
+            }
+            int64_t c = (int64_t)upper[a] - (int64_t)lower[a] + 1;
+            if (c > (int64_t)(64 / total)) {
+                ok = false;
+                break;
+            }
+            first[a] = (int32_t)lower[a];
+            counts[a] = (int)c;
+            total *= (uint64_t)c;
+        }
+        if (ok) {
+            firstCell[i] = make_int4(first[0], first[1], first[2], counts[0] | (counts[1] << 8) | (counts[2] << 16));
+            cellCount[i] = (uint32_t)total;
+            inGrid[i] = 1;
+            namespace cg = cooperative_groups;
+            cg::coalesced_group g = cg::coalesced_threads();
+            for (int a = 0; a < 3; ++a) {
+                int lo = cg::reduce(g, first[a], cg::less<int>());
+                int hi = cg::reduce(g, first[a] + counts[a] - 1, cg::greater<int>());
+                if (g.thread_rank() == 0) {
+                    atomicMin(&st->cellLo[a], lo);
+                    atomicMax(&st->cellHi[a], hi);
+                }
+            }
+        } else {
+            cellCount[i] = 0;
+            inGrid[i] = 0;
+            uint32_t k = aggregatedAppend(&st->overflowCount);
+            overflow[k] = i;
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t bitsFor(uint32_t range) { return range ? 32u - __clz(range) : 0u; }
+
+// One entry per covered cell; key = packed cell offsets from the lowest cell,
+// so equal cells are adjacent after the sort (cell order is irrelevant: the
+// reference only groups entries by cell before the final pair sort).
+__global__ void k_grid_entries(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const uint32_t *entryOff,
+                               unsigned long long *keys, uint32_t *vals, uint32_t cap, DevStats *st) {
+    const uint32_t n = *in.d_n;
+    const uint32_t bx = bitsFor((uint32_t)(st->cellHi[0] - st->cellLo[0]));
+    const uint32_t by = bitsFor((uint32_t)(st->cellHi[1] - st->cellLo[1]));
+    const uint32_t bz = bitsFor((uint32_t)(st->cellHi[2] - st->cellLo[2]));
+    if (bx + by + bz > 64) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&st->err, kErrEntryCapacity);
+        return;
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!inGrid[i]) continue;
+        int4 f = firstCell[i];
+        int cx = f.w & 0xFF, cy = (f.w >> 8) & 0xFF, cz = (f.w >> 16) & 0xFF;
+        uint32_t e = entryOff[i];
+        for (int x = 0; x < cx; ++x)
+            for (int y = 0; y < cy; ++y)
+                for (int z = 0; z < cz; ++z, ++e) {
+                    if (e >= cap) continue;
+                    unsigned long long dx = (uint32_t)(f.x + x - st->cellLo[0]);
+                    unsigned long long dy = (uint32_t)(f.y + y - st->cellLo[1]);
+                    unsigned long long dz = (uint32_t)(f.z + z - st->cellLo[2]);
+                    keys[e] = (bx ? dx << (by + bz) : 0ull) | (by ? dy << bz : 0ull) | dz;
+                    vals[e] = i;
+                }
+    }
+}
+
+// Per-cell all pairs (broadphase.cpp:152-160): entry e against every later
+// entry of its cell.
+__global__ void k_grid_cell_pairs(const uint32_t *d_entries, const unsigned long long *ekeys, const uint32_t *evals,
+                                  BroadInput in, unsigned long long *pkeys, uint32_t cap, DevStats *st) {
+    const uint32_t E = *d_entries;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x) {
+        const unsigned long long key = ekeys[e];
+        const uint32_t a = evals[e];
+        const float4 amn = in.mn[a], amx = in.mx[a];
+        uint64_t cmp = 0;
+        for (uint32_t f = e + 1; f < E && ekeys[f] == key; ++f) {
+            ++cmp;
+            const uint32_t b = evals[f];
+            if (overlaps(amn, amx, in.mn[b], in.mx[b])) emitPair(a, b, pkeys, cap, &st->rawPairs);
+        }
+        if (cmp) atomicAdd(&st->gridComparisons, (unsigned long long)cmp);
+    }
+}
+
+// Overflow boxes against all others (broadphase.cpp:162-166).
+__global__ void k_grid_overflow_pairs(BroadInput in, const uint32_t *overflow, const uint8_t *inGrid,
+                                      unsigned long long *pkeys, uint32_t cap, DevStats *st) {
+    const uint32_t n = *in.d_n;
+    const uint32_t F = st->overflowCount;
+    const uint64_t total = (uint64_t)F * n;
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t k = (uint32_t)(t / n), s = (uint32_t)(t % n);
+        const uint32_t f = overflow[k];
+        if (f == s || !(inGrid[s] || f < s)) continue;
+        aggregatedAdd64(&st->gridComparisons, 1ull);
+        if (overlaps(in.mn[f], in.mx[f], in.mn[s], in.mx[s])) emitPair(f, s, pkeys, cap, &st->rawPairs);
+    }
+}
+
+// ------------------------------------------------------------ finalize -----
+__global__ void k_pairs_flags(const uint32_t *d_raw, const unsigned long long *keys, const uint32_t *inSlot,
+                              const uint32_t *cbody, const uint32_t *cbgen, uint32_t *flags, DevStats *st) {
+    const uint32_t n = *d_raw;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        unsigned long long key = keys[k];
+        bool keep = !(k > 0 && keys[k - 1] == key);
+        if (keep) {
+            aggregatedAppend(&st->uniquePairs);
+            uint32_t a = (uint32_t)(key >> 32), b = (uint32_t)key;
+            if (inSlot) {
+                a = inSlot[a];
+                b = inSlot[b];
+            }
+            if (cbody && cbody[a] == cbody[b] && cbgen[a] == cbgen[b]) keep = false;
+        }
+        flags[k] = keep ? 1u : 0u;
+    }
+}
+
+__global__ void k_pairs_scatter(const uint32_t *d_raw, const unsigned long long *keys, const uint32_t *inSlot,
+                                const uint32_t *flags, const uint32_t *pos, uint32_t *pairA, uint32_t *pairB) {
+    const uint32_t n = *d_raw;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        if (!flags[k]) continue;
+        unsigned long long key = keys[k];
+        uint32_t a = (uint32_t)(key >> 32), b = (uint32_t)key;
+        if (inSlot) {
+            a = inSlot[a];
+            b = inSlot[b];
+        }
+        pairA[pos[k]] = a;
+        pairB[pos[k]] = b;
+    }
+}
+
+static inline int gridFor(uint32_t n, int threads = 256, int maxBlocks = 152 * 8) {
+    uint32_t b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    return (int)(b < (uint32_t)maxBlocks ? b : (uint32_t)maxBlocks);
+}
+
+void launchStepInit(DevStats *st, uint32_t inputCount, cudaStream_t s) {
+    k_step_init<<<1, 32, 0, s>>>(st, inputCount);
+    PE_CHECK(cudaGetLastError());
+}
+
+__global__ void k_set_manifolds(DevStats *st, uint32_t count) { st->manifolds = count; }
+void launchSetManifoldCount(DevStats *st, uint32_t count, cudaStream_t s) {
+    k_set_manifolds<<<1, 1, 0, s>>>(st, count);
+    PE_CHECK(cudaGetLastError());
+}
+
+__global__ void k_sap_keys(BroadInput in, uint32_t *keys, uint32_t *vals) {
+    const uint32_t n = *in.d_n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        keys[i] = orderedFloatKey(in.mn[i].x);
+        vals[i] = i;
+    }
+}
+
+void launchSapKeys(const BroadInput &in, uint32_t *keys, uint32_t *vals, cudaStream_t s) {
+    k_sap_keys<<<gridFor(in.maxN), 256, 0, s>>>(in, keys, vals);
+    PE_CHECK(cudaGetLastError());
+}
+
+void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, BroadBuffers &bb, PairBuffers &pb,
+               DevStats *st, Scratch &ws, cudaStream_t s) {
+    uint32_t *err = &st->err;
+    launchRadixSort<uint32_t>(sapKeys, bb.keyTmp32, sapVals, bb.valTmp, in.d_n, in.maxN, 0, 32, ws, err, s);
+    k_sap_gather<<<gridFor(in.maxN), 256, 0, s>>>(in, sapVals, bb.sMinX, bb.sMaxX, bb.sYZ, bb.sIdx);
+    k_sap_window<<<gridFor(in.maxN), 256, 0, s>>>(in.d_n, bb.sMinX, bb.sMaxX, bb.len, st);
+    PE_CHECK(cudaGetLastError());
+    launchScanExclusive(bb.len, bb.off, in.d_n, in.maxN, &st->windowWork, ws, err, s);
+    k_sap_emit<<<152 * 8, 256, 0, s>>>(in.d_n, bb.off, bb.len, bb.sYZ, bb.sIdx, pb.keys, pb.cap, st);
+    PE_CHECK(cudaGetLastError());
+}
+
+void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBuffers &pb, DevStats *st, Scratch &ws,
+                cudaStream_t s) {
+    uint32_t *err = &st->err;
+    if (fixedCell <= 0.0) {
+        k_grid_widths<<<gridFor(in.maxN), 256, 0, s>>>(in, bb.widthKeys, &bb.counters[0]);
+        PE_CHECK(cudaGetLastError());
+        launchRadixSort<unsigned long long>(bb.widthKeys, bb.widthTmp, nullptr, nullptr, in.d_n, in.maxN, 0, 64, ws,
+                                            err, s);
+    }
+    k_grid_cellsize<<<1, 1, 0, s>>>(bb.widthKeys, &bb.counters[0], fixedCell, st);
+    k_grid_range<<<gridFor(in.maxN), 256, 0, s>>>(in, st, bb.firstCell, bb.cellCount, bb.inGrid, bb.overflow);
+    PE_CHECK(cudaGetLastError());
+    launchScanExclusive(bb.cellCount, bb.entryOff, in.d_n, in.maxN, &st->gridEntryCount, ws, err, s);
+    k_grid_entries<<<gridFor(in.maxN), 256, 0, s>>>(in, bb.firstCell, bb.inGrid, bb.entryOff, bb.entryKeys,
+                                                    bb.entryVals, bb.entryCap, st);
+    launchClamp(&st->gridEntryCount, bb.entryCap, &bb.counters[1], s);
+    PE_CHECK(cudaGetLastError());
+    launchRadixSort<unsigned long long>(bb.entryKeys, bb.entryKeysTmp, bb.entryVals, bb.entryValsTmp,
+                                        &bb.counters[1], bb.entryCap, 0, 64, ws, err, s);
+    k_grid_cell_pairs<<<gridFor(bb.entryCap), 256, 0, s>>>(&bb.counters[1], bb.entryKeys, bb.entryVals, in, pb.keys,
+                                                           pb.cap, st);
+    k_grid_overflow_pairs<<<152 * 4, 256, 0, s>>>(in, bb.overflow, bb.inGrid, pb.keys, pb.cap, st);
+    PE_CHECK(cudaGetLastError());
+}
+
+void launchPairsFinalize(const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen, PairBuffers &pb,
+                         DevStats *st, Scratch &ws, cudaStream_t s) {
+    uint32_t *err = &st->err;
+    launchClamp(&st->rawPairs, pb.cap, &pb.counters[0], s);
+    PE_CHECK(cudaGetLastError());
+    launchRadixSort<unsigned long long>(pb.keys, pb.keysTmp, nullptr, nullptr, &pb.counters[0], pb.cap, 0, 64, ws,
+                                        err, s);
+    k_pairs_flags<<<gridFor(pb.cap), 256, 0, s>>>(&pb.counters[0], pb.keys, inSlot, cbody, cbgen, pb.flags, st);
+    PE_CHECK(cudaGetLastError());
+    launchScanExclusive(pb.flags, pb.pos, &pb.counters[0], pb.cap, &st->pairs, ws, err, s);
+    k_pairs_scatter<<<gridFor(pb.cap), 256, 0, s>>>(&pb.counters[0], pb.keys, inSlot, pb.flags, pb.pos, pb.a, pb.b);
+    PE_CHECK(cudaGetLastError());
+}
+
+} // namespace pe

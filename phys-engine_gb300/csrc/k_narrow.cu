@@ -1,0 +1,191 @@
+// Narrowphase: one candidate pair per thread; manifolds are compacted in pair
+// order in the same pass (block scan of hit flags + decoupled look-back), so
+// manifold order equals the reference's (src/world/physics_world.cpp:692-736).
+// Per pair this is the world's generateContact lambda
+// (physics_world.cpp:645-691): collider world transforms, shape dispatch with
+// the box-sphere swap (src/collision/narrowphase.cpp:353-365), anchors moved
+// from collider space to body space, restitution = max, friction =
+// sqrt(max(fa,0) * max(fb,0)).
+#include "pe_kernels.cuh"
+#include "pe_narrow.cuh"
+#include "pe_stages.h"
+
+namespace pe {
+
+constexpr int kNarrowThreads = 256;
+
+__device__ __forceinline__ SupportShape supportShape(const WorldView &w, uint32_t c, const Tf &t) {
+    SupportShape s;
+    s.shape = colliderShape(w.cflags[c]);
+    float4 sh = w.cshape[c];
+    s.radius = sh.x;
+    s.he = V3{sh.x, sh.y, sh.z};
+    s.tf = t;
+    s.verts = nullptr;
+    s.nverts = 0;
+    if (s.shape == kShapeHull) {
+        uint32_t h = __float_as_uint(sh.w);
+        uint32_t b = w.hullOffset[h];
+        s.verts = w.hullVerts + b;
+        s.nverts = w.hullOffset[h + 1] - b;
+    }
+    return s;
+}
+
+__global__ void __launch_bounds__(kNarrowThreads)
+k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *__restrict__ pairB,
+              const uint32_t *d_pairs, ManifoldView out, uint32_t mcap, DevStats *st, unsigned long long *state,
+              uint32_t *counter) {
+    __shared__ uint32_t s_tile, s_scan[9], s_prefix;
+    const uint32_t tile = takeTile(counter, &s_tile);
+    const uint32_t P = *d_pairs;
+    const uint32_t ntiles = (P + kNarrowThreads - 1) / kNarrowThreads;
+    if (tile >= (ntiles > 0 ? ntiles : 1u)) return;
+    const uint32_t p = tile * kNarrowThreads + threadIdx.x;
+
+    LocalManifold lm;
+    lm.count = 0;
+    bool hit = false;
+    uint32_t ca = 0, cb = 0, ba = 0, bb = 0, category = 0;
+    float restitution = 0.0f, friction = 0.0f;
+    if (p < P) {
+        ca = pairA[p];
+        cb = pairB[p];
+        ba = w.cbody[ca];
+        bb = w.cbody[cb];
+        const uint32_t sa = colliderShape(w.cflags[ca]), sb = colliderShape(w.cflags[cb]);
+        V3 lpa = w.clpos ? f4xyz(w.clpos[ca]) : V3{0.0f, 0.0f, 0.0f};
+        Q lqa = w.clrot ? f4q(w.clrot[ca]) : qidentity();
+        V3 lpb = w.clpos ? f4xyz(w.clpos[cb]) : V3{0.0f, 0.0f, 0.0f};
+        Q lqb = w.clrot ? f4q(w.clrot[cb]) : qidentity();
+        V3 pa = f4xyz(w.cur.pos[ba]), pb = f4xyz(w.cur.pos[bb]);
+        Q qa = f4q(w.cur.rot[ba]), qb = f4q(w.cur.rot[bb]);
+        Tf tA{pa + rotate(qa, lpa), qmul(qa, lqa)};
+        Tf tB{pb + rotate(qb, lpb), qmul(qb, lqb)};
+        const float4 sha = w.cshape[ca], shb = w.cshape[cb];
+        if (sa == kShapeHull || sb == kShapeHull) {
+            category = 3;
+            bool failed;
+            hit = hullContact(supportShape(w, ca, tA), supportShape(w, cb, tB), lm, failed);
+            if (failed) atomicAdd(&st->epaFailures, 1ull);
+        } else {
+            category = sa + sb;
+            if (sa == kShapeSphere && sb == kShapeSphere) {
+                hit = sphereSphere(sha.x, tA, shb.x, tB, lm);
+            } else if (sa == kShapeSphere) {
+                hit = sphereBox(sha.x, tA, V3{shb.x, shb.y, shb.z}, tB, lm);
+            } else if (sb == kShapeSphere) {
+                hit = sphereBox(shb.x, tB, V3{sha.x, sha.y, sha.z}, tA, lm);
+                if (hit) {
+                    lm.normal = -lm.normal;
+                    for (uint32_t k = 0; k < lm.count; ++k) {
+                        V3 t = lm.anchorA[k];
+                        lm.anchorA[k] = lm.anchorB[k];
+                        lm.anchorB[k] = t;
+                    }
+                }
+            } else {
+                hit = boxBox(V3{sha.x, sha.y, sha.z}, tA, V3{shb.x, shb.y, shb.z}, tB, lm);
+            }
+        }
+        if (hit) {
+            for (uint32_t k = 0; k < lm.count; ++k) {
+                lm.anchorA[k] = lpa + rotate(lqa, lm.anchorA[k]);
+                lm.anchorB[k] = lpb + rotate(lqb, lm.anchorB[k]);
+            }
+            const float4 ma = w.mat[ba], mb = w.mat[bb];
+            restitution = smax(ma.y, mb.y);
+            friction = sqrtf(smax(ma.z, 0.0f) * smax(mb.z, 0.0f));
+        }
+        aggregatedAdd64(&st->npCandidates[category], 1ull);
+        if (hit) aggregatedAdd64(&st->npContacts[category], 1ull);
+    }
+    uint32_t total;
+    const uint32_t local = blockExclusiveScan(hit ? 1u : 0u, total, s_scan);
+    if (threadIdx.x == 0) s_prefix = lookbackExclusive(state, tile, total, &st->err);
+    __syncthreads();
+    const uint32_t m = s_prefix + local;
+    if (hit) {
+        if (m < mcap) {
+            out.bodyA[m] = ba;
+            out.genA[m] = w.cbgen[ca];
+            out.bodyB[m] = bb;
+            out.genB[m] = w.cbgen[cb];
+            out.normalFriction[m] = make4(lm.normal, friction);
+            out.restitution[m] = restitution;
+            out.pointCount[m] = lm.count;
+            for (uint32_t k = 0; k < 4; ++k) {
+                const bool live = k < lm.count;
+                out.anchorA[4 * m + k] = live ? make4(lm.anchorA[k], lm.depth[k]) : make_float4(0, 0, 0, 0);
+                out.anchorB[4 * m + k] = live ? make4(lm.anchorB[k], 0.0f) : make_float4(0, 0, 0, 0);
+                out.impulse[4 * m + k] = make_float4(0, 0, 0, 0);
+                out.feature[4 * m + k] = live ? lm.feature[k] : 0u;
+            }
+        }
+        aggregatedAppend(&st->points);
+        if (lm.count > 1) atomicAdd(&st->points, lm.count - 1);
+    }
+    if (threadIdx.x == 0 && tile + 1 >= ntiles) st->manifolds = s_prefix + total;
+}
+
+void launchNarrowphase(const WorldView &w, const PairBuffers &pb, const ManifoldView &mv, uint32_t mcap, DevStats *st,
+                       Scratch &ws, cudaStream_t s) {
+    uint32_t tiles = (pb.cap + kNarrowThreads - 1) / kNarrowThreads;
+    if (tiles == 0) tiles = 1;
+    PE_CHECK(cudaMemsetAsync(ws.scanState, 0, sizeof(unsigned long long) * tiles + 8, s));
+    k_narrowphase<<<tiles, kNarrowThreads, 0, s>>>(w, pb.a, pb.b, &st->pairs, mv, mcap, st, ws.scanState,
+                                                    (uint32_t *)(ws.scanState + tiles));
+    PE_CHECK(cudaGetLastError());
+}
+
+} // namespace pe
+
+namespace pe {
+
+// NarrowPhase::generateContact on explicit transforms (sphere / box only):
+// in[6k..6k+5] = dims A (w = shape), pos A, rot A, dims B (w = shape), pos B, rot B;
+// out[11k..] = normal (w = hit, point count in bits), 4 x anchorA (w = depth),
+// 4 x anchorB, features as uint bits in two float4.
+__global__ void k_generate_pairs(const float4 *in, float4 *out, uint32_t n) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float4 da = in[6 * k], pa = in[6 * k + 1], ra = in[6 * k + 2];
+    const float4 db = in[6 * k + 3], pb = in[6 * k + 4], rb = in[6 * k + 5];
+    const uint32_t sa = (uint32_t)da.w, sb = (uint32_t)db.w;
+    Tf tA{f4xyz(pa), f4q(ra)}, tB{f4xyz(pb), f4q(rb)};
+    LocalManifold lm;
+    lm.count = 0;
+    bool hit;
+    if (sa == kShapeSphere && sb == kShapeSphere) hit = sphereSphere(da.x, tA, db.x, tB, lm);
+    else if (sa == kShapeSphere) hit = sphereBox(da.x, tA, V3{db.x, db.y, db.z}, tB, lm);
+    else if (sb == kShapeSphere) {
+        hit = sphereBox(db.x, tB, V3{da.x, da.y, da.z}, tA, lm);
+        if (hit) {
+            lm.normal = -lm.normal;
+            for (uint32_t i = 0; i < lm.count; ++i) {
+                V3 t = lm.anchorA[i];
+                lm.anchorA[i] = lm.anchorB[i];
+                lm.anchorB[i] = t;
+            }
+        }
+    } else hit = boxBox(V3{da.x, da.y, da.z}, tA, V3{db.x, db.y, db.z}, tB, lm);
+    float4 *o = out + 11 * k;
+    o[0] = make_float4(lm.normal.x, lm.normal.y, lm.normal.z, hit ? (float)lm.count : -1.0f);
+    for (uint32_t i = 0; i < 4; ++i) {
+        bool live = hit && i < lm.count;
+        o[1 + i] = live ? make4(lm.anchorA[i], lm.depth[i]) : make_float4(0, 0, 0, 0);
+        o[5 + i] = live ? make4(lm.anchorB[i], 0.0f) : make_float4(0, 0, 0, 0);
+    }
+    uint32_t f[4];
+    for (uint32_t i = 0; i < 4; ++i) f[i] = (hit && i < lm.count) ? lm.feature[i] : 0u;
+    o[9] = make_float4(__uint_as_float(f[0]), __uint_as_float(f[1]), __uint_as_float(f[2]), __uint_as_float(f[3]));
+    o[10] = make_float4(0, 0, 0, 0);
+}
+
+void launchGeneratePairs(const float4 *in, float4 *out, uint32_t n, cudaStream_t s) {
+    if (!n) return;
+    k_generate_pairs<<<(n + 127) / 128, 128, 0, s>>>(in, out, n);
+    PE_CHECK(cudaGetLastError());
+}
+
+} // namespace pe

@@ -1,0 +1,140 @@
+// Internal declarations of the GB300 engine: device-side views of a world,
+// scratch memory, and the stage launchers used by the step pipeline.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <cuda_runtime.h>
+
+namespace pe {
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+#define PE_CHECK(expr)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (expr);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            throw ::pe::CudaError(std::string(#expr) + ": " + cudaGetErrorString(e_));             \
+    } while (0)
+
+// Error bits shared by all kernels (written to the step's status word).
+enum : uint32_t {
+    kErrTimeout = 1u,
+    kErrPairCapacity = 2u,
+    kErrManifoldCapacity = 4u,
+    kErrColors = 8u,
+    kErrEntryCapacity = 16u,
+    kErrEpa = 32u,
+};
+
+// Body flag bits (bflags) and collider flag layout (cflags).
+enum : uint32_t { kBodyAlive = 1u, kBodyStatic = 2u };
+enum : uint32_t { kColliderAlive = 1u };
+__host__ __device__ inline uint32_t colliderShape(uint32_t cflags) { return (cflags >> 8) & 0xFFu; }
+enum : uint32_t { kShapeSphere = 0, kShapeBox = 1, kShapeHull = 2 };
+
+// Feature-id kinds (bits 24-31 of a contact feature id).
+enum : uint32_t { kFeatSphereSphere = 1, kFeatSphereBox = 2, kFeatBoxFace = 3, kFeatBoxFallback = 4, kFeatHull = 5 };
+
+// One copy of the integrated body state (the step reads one and writes the
+// other, so a step can be re-run from the untouched copy).
+struct BodyState {
+    float4 *pos;  // xyz
+    float4 *rot;  // quaternion xyzw
+    float4 *lin;  // xyz
+    float4 *ang;  // xyz
+};
+
+// Device counters of one step (copied to pinned host memory after the step).
+struct DevStats {
+    unsigned long long xWindow;
+    unsigned long long aabbPairs;
+    unsigned long long gridComparisons;
+    unsigned long long gridEntries;
+    unsigned long long gridOverflow;
+    unsigned long long npCandidates[4];
+    unsigned long long npContacts[4];
+    unsigned long long preparedPoints;
+    unsigned long long warmComparisons;
+    unsigned long long warmMatches;
+    unsigned long long epaFailures;
+    double cellSize;
+    uint32_t err;
+    uint32_t inputCount;     // bounds handed to the broadphase
+    uint32_t rawPairs;       // pairs emitted before dedup (capacity check)
+    uint32_t uniquePairs;
+    uint32_t pairs;          // candidate pairs after the same-body filter
+    uint32_t manifolds;
+    uint32_t points;         // contact points over all manifolds
+    uint32_t colors;
+    uint32_t gridEntryCount; // grid entries (capacity check)
+    uint32_t overflowCount;
+    uint32_t colorRounds;
+    uint32_t sel;            // radix-sort buffer selector (device-side pass skipping)
+    uint32_t windowWork;     // SAP flattened window work
+    uint32_t solved;         // manifolds whose bodies are valid (prepared)
+    int32_t cellLo[3];
+    int32_t cellHi[3];
+};
+
+struct WorldView {
+    uint32_t nb, nc;
+    BodyState cur, nxt;
+    const float4 *force;     // nullable: all forces zero
+    const float4 *mat;       // invMass, restitution, friction, mass
+    const float4 *iinv;      // diagonal local inverse inertia (xyz)
+    const uint32_t *bflags;
+    const uint32_t *bgen;
+    const uint32_t *cbody;
+    const uint32_t *cbgen;
+    const uint32_t *cflags;
+    const float4 *cshape;    // sphere: radius in x; box: half extents; hull: hull index in w (as uint bits)
+    const float4 *clpos;     // nullable: all local positions zero
+    const float4 *clrot;     // nullable: all local rotations identity
+    const uint32_t *hullOffset;
+    const float4 *hullVerts;
+    float4 *aabbMin;
+    float4 *aabbMax;
+    float gx, gy, gz, dt;
+};
+
+// Contact manifolds (structure of arrays; manifold m owns points 4m..4m+3).
+struct ManifoldView {
+    uint32_t *bodyA, *genA, *bodyB, *genB;
+    float4 *normalFriction;  // normal xyz, friction
+    float *restitution;
+    uint32_t *pointCount;
+    float4 *anchorA;         // xyz, penetration
+    float4 *anchorB;         // xyz
+    float4 *impulse;         // normal, tangent1, tangent2
+    uint32_t *feature;
+};
+
+// Warm-start cache (sorted by (bodyA index, bodyB index); generations checked).
+struct CacheView {
+    unsigned long long *key;  // bodyA index << 32 | bodyB index
+    unsigned long long *gens; // bodyA gen << 32 | bodyB gen
+    float4 *anchorA;          // xyz, normal impulse
+    float4 *anchorB;          // xyz, tangent impulse 1
+    float *tangent2;
+};
+
+struct Scratch {
+    unsigned long long *scanState = nullptr;
+    uint32_t *sortHist = nullptr;
+    uint32_t *sortState = nullptr;
+};
+
+void launchScanExclusive(const uint32_t *in, uint32_t *out, const uint32_t *d_n, uint32_t max_n, uint32_t *d_total,
+                         Scratch &ws, uint32_t *d_err, cudaStream_t s);
+template <class K>
+void launchRadixSort(K *keys, K *keys_tmp, uint32_t *vals, uint32_t *vals_tmp, const uint32_t *d_n, uint32_t max_n,
+                    int bit_begin, int bit_end, Scratch &ws, uint32_t *d_err, cudaStream_t s);
+void launchClamp(const uint32_t *src, uint32_t cap, uint32_t *dst, cudaStream_t s);
+size_t scratchBytesScan(uint32_t max_n);
+size_t scratchBytesSort(uint32_t max_n);
+
+} // namespace pe

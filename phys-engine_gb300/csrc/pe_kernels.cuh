@@ -1,0 +1,28 @@
+// Common includes for the step kernels.
+#pragma once
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
+
+#include "pe_engine.h"
+#include "pe_math.cuh"
+#include "pe_prims.cuh"
+
+namespace pe {
+
+// Warp-aggregated append: one atomic per converged group of lanes.
+__device__ __forceinline__ uint32_t aggregatedAppend(uint32_t *counter) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    uint32_t base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(counter, g.size());
+    return g.shfl(base, 0) + g.thread_rank();
+}
+
+__device__ __forceinline__ void aggregatedAdd64(unsigned long long *counter, unsigned long long v) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long s = cg::reduce(g, v, cg::plus<unsigned long long>());
+    if (g.thread_rank() == 0 && s) atomicAdd(counter, s);
+}
+
+} // namespace pe

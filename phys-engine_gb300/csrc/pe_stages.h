@@ -1,0 +1,91 @@
+// Buffers and launchers of the step stages (broadphase, narrowphase, solver).
+#pragma once
+#include "pe_engine.h"
+
+namespace pe {
+
+struct BroadInput {
+    const float4 *mn;
+    const float4 *mx;
+    const uint32_t *d_n;  // live count on the device
+    uint32_t maxN;        // launch bound
+};
+
+struct BroadBuffers {
+    // SAP
+    uint32_t *keyTmp32, *valTmp;
+    float *sMinX, *sMaxX;
+    float4 *sYZ;
+    uint32_t *sIdx, *len, *off;
+    // grid
+    unsigned long long *widthKeys, *widthTmp;
+    int4 *firstCell;
+    uint32_t *cellCount;
+    uint8_t *inGrid;
+    uint32_t *overflow, *entryOff;
+    unsigned long long *entryKeys, *entryKeysTmp;
+    uint32_t *entryVals, *entryValsTmp;
+    uint32_t entryCap;
+    uint32_t *counters;  // [4] device scratch counters
+};
+
+struct PairBuffers {
+    unsigned long long *keys, *keysTmp;
+    uint32_t cap;
+    uint32_t *flags, *pos;
+    uint32_t *a, *b;       // candidate pairs (collider slots), lexicographic
+    uint32_t *counters;    // [4]
+};
+
+struct SolverBuffers {
+    uint32_t mcap;
+    // colouring
+    unsigned long long *bodyBest;   // [nb] round-stamped max priority
+    unsigned long long *bodyUsed;   // [2 * nb] colour masks (128 colours)
+    unsigned long long *epoch;      // [1] persistent round stamp
+    uint32_t *color;                // [mcap]
+    uint32_t *dyn;                  // [mcap] bit0 A dynamic, bit1 B dynamic
+    uint32_t *colorCount;           // [kMaxColors]
+    uint32_t *orderKeys, *orderKeysTmp, *order, *orderTmp;  // [mcap]
+    // prepared data, in solve order k (structure of arrays)
+    float4 *pm;                     // [mcap] invMassA, staticA, invMassB, staticB
+    float4 *pmInertia;              // [6 * mcap] rows of the world inverse inertia (A: 3, B: 3)
+    float4 *pp;                     // [kPreparedVec4 * 4 * mcap] prepared contact points
+    float4 *pimp;                   // [4 * mcap] normal, tangent1, tangent2 impulse, warm-start match flag
+    float4 *pn;                     // [mcap] normal, friction
+    uint2 *pbody;                   // [mcap] body A, body B
+    uint32_t *pcount;               // [mcap] point count
+    // cache rebuild
+    unsigned long long *cacheKeys, *cacheKeysTmp;
+    uint32_t *cacheVals, *cacheValsTmp;
+    uint32_t *cacheCounts, *cacheOff;
+    uint32_t *bar;                  // grid barrier [2]
+    uint32_t *counters;             // [4]
+};
+
+constexpr int kMaxColors = 128;
+constexpr int kPreparedVec4 = 10;
+
+void launchStepInit(DevStats *st, uint32_t inputCount, cudaStream_t s);
+void launchSetManifoldCount(DevStats *st, uint32_t count, cudaStream_t s);
+void launchSapKeys(const BroadInput &in, uint32_t *keys, uint32_t *vals, cudaStream_t s);
+void launchIntegrateAabb(const WorldView &w, uint32_t *sapKeys, uint32_t *sapVals, cudaStream_t s);
+void launchCollect(const WorldView &w, uint32_t *flags, uint32_t *pos, float4 *inMin, float4 *inMax, uint32_t *inSlot,
+                   uint32_t *sapKeys, uint32_t *sapVals, uint32_t *d_count, Scratch &ws, uint32_t *d_err,
+                   cudaStream_t s);
+void launchIntegratePose(const WorldView &w, cudaStream_t s);
+void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, BroadBuffers &bb, PairBuffers &pb,
+               DevStats *st, Scratch &ws, cudaStream_t s);
+void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBuffers &pb, DevStats *st, Scratch &ws,
+                cudaStream_t s);
+void launchPairsFinalize(const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen, PairBuffers &pb,
+                         DevStats *st, Scratch &ws, cudaStream_t s);
+void launchNarrowphase(const WorldView &w, const PairBuffers &pb, const ManifoldView &mv, uint32_t mcap, DevStats *st,
+                       Scratch &ws, cudaStream_t s);
+void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &oldCache, const uint32_t *oldCacheCount,
+                  const CacheView &newCache, uint32_t *newCacheCount, uint32_t cacheCap, SolverBuffers &sb,
+                  int iterations, int orderMode, int coopBlocks, DevStats *st, Scratch &ws, cudaStream_t s);
+int maxCooperativeBlocks(int smCount);
+void launchGeneratePairs(const float4 *in, float4 *out, uint32_t n, cudaStream_t s);
+
+} // namespace pe

@@ -1,0 +1,795 @@
+// GPU world: host mirror, device state and the step pipeline
+// (PhysicsWorld::step, src/world/physics_world.cpp:518-782, sleeping off).
+#include "world.h"
+
+#include <algorithm>
+#include <cstring>
+
+namespace pe {
+
+namespace {
+template <class T> void upload(DeviceArray<T> &d, const std::vector<T> &h, cudaStream_t s) {
+    d.reserve(h.size());
+    if (!h.empty()) PE_CHECK(cudaMemcpyAsync(d.ptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+inline uint32_t grow(uint32_t need, uint32_t have) {
+    uint64_t n = std::max<uint64_t>(need, have);
+    n = n + n / 2 + 1024;
+    return (uint32_t)std::min<uint64_t>(n, 0xFFFFFFF0u);
+}
+} // namespace
+
+World::World(int device) : device_(device) {
+    PE_CHECK(cudaSetDevice(device_));
+    PE_CHECK(cudaDeviceGetAttribute(&smCount_, cudaDevAttrMultiProcessorCount, device_));
+    PE_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    PE_CHECK(cudaEventCreate(&evStart_));
+    PE_CHECK(cudaEventCreate(&evEnd_));
+    PE_CHECK(cudaMallocHost(&hostStats_, sizeof(DevStats)));
+    std::memset(hostStats_, 0, sizeof(DevStats));
+    stats_.reserve(1);
+    cCount_.reserve(2);
+    sEpoch_.reserve(1);
+}
+
+World::~World() {
+    if (stream_) cudaStreamSynchronize(stream_);
+    if (hostStats_) cudaFreeHost(hostStats_);
+    if (evStart_) cudaEventDestroy(evStart_);
+    if (evEnd_) cudaEventDestroy(evEnd_);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+void World::syncDevice() { PE_CHECK(cudaStreamSynchronize(stream_)); }
+
+// ---------------------------------------------------------------- slots ----
+uint32_t World::addBody(const HostBody &b, uint32_t &generation) {
+    pull();
+    hostDirty_ = true;
+    if (!freeBodies.empty()) {
+        uint32_t idx = freeBodies.back();
+        freeBodies.pop_back();
+        uint32_t g = bodies[idx].generation;
+        bodies[idx] = b;
+        bodies[idx].generation = g;
+        bodies[idx].alive = true;
+        generation = g;
+        return idx;
+    }
+    bodies.push_back(b);
+    bodies.back().generation = 0;
+    bodies.back().alive = true;
+    generation = 0;
+    return (uint32_t)bodies.size() - 1;
+}
+
+uint32_t World::addCollider(const HostCollider &c, uint32_t &generation) {
+    pull();
+    hostDirty_ = true;
+    if (!freeColliders.empty()) {
+        uint32_t idx = freeColliders.back();
+        freeColliders.pop_back();
+        uint32_t g = colliders[idx].generation;
+        colliders[idx] = c;
+        colliders[idx].generation = g;
+        colliders[idx].alive = true;
+        generation = g;
+        return idx;
+    }
+    colliders.push_back(c);
+    colliders.back().generation = 0;
+    colliders.back().alive = true;
+    generation = 0;
+    return (uint32_t)colliders.size() - 1;
+}
+
+void World::removeBody(uint32_t index, uint32_t generation) {
+    pull();
+    if (index >= bodies.size()) return;
+    HostBody &b = bodies[index];
+    if (!b.alive || b.generation != generation) return;
+    hostDirty_ = true;
+    b.alive = false;
+    b.generation++;
+    freeBodies.push_back(index);
+    for (uint32_t i = 0; i < colliders.size(); ++i) {
+        HostCollider &c = colliders[i];
+        if (c.alive && c.body == index && c.bodyGeneration == generation) {
+            c.alive = false;
+            c.generation++;
+            freeColliders.push_back(i);
+        }
+    }
+}
+
+void World::removeCollider(uint32_t index, uint32_t generation) {
+    pull();
+    if (index >= colliders.size()) return;
+    HostCollider &c = colliders[index];
+    if (!c.alive || c.generation != generation) return;
+    hostDirty_ = true;
+    c.alive = false;
+    c.generation++;
+    freeColliders.push_back(index);
+}
+
+HostBody *World::body(uint32_t index, uint32_t generation) {
+    if (index >= bodies.size()) return nullptr;
+    HostBody &b = bodies[index];
+    if (!b.alive || b.generation != generation) return nullptr;
+    return &b;
+}
+
+HostCollider *World::collider(uint32_t index, uint32_t generation) {
+    if (index >= colliders.size()) return nullptr;
+    HostCollider &c = colliders[index];
+    if (!c.alive || c.generation != generation) return nullptr;
+    return &c;
+}
+
+int World::addHull(const float *verts, uint32_t count) {
+    hostDirty_ = true;
+    hullVerts.insert(hullVerts.end(), verts, verts + 3 * (size_t)count);
+    hullOffsets.push_back((uint32_t)(hullVerts.size() / 3));
+    return (int)hullOffsets.size() - 2;
+}
+
+// ---------------------------------------------------------- host/device ----
+void World::pull() {
+    if (!deviceNewer_) return;
+    PE_CHECK(cudaSetDevice(device_));
+    std::vector<float4> p(nb_), q(nb_), l(nb_), a(nb_);
+    if (nb_) {
+        PE_CHECK(cudaMemcpyAsync(p.data(), pos_[cur_].ptr, nb_ * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
+        PE_CHECK(cudaMemcpyAsync(q.data(), rot_[cur_].ptr, nb_ * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
+        PE_CHECK(cudaMemcpyAsync(l.data(), lin_[cur_].ptr, nb_ * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
+        PE_CHECK(cudaMemcpyAsync(a.data(), ang_[cur_].ptr, nb_ * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
+        PE_CHECK(cudaStreamSynchronize(stream_));
+    }
+    for (uint32_t i = 0; i < nb_ && i < bodies.size(); ++i) {
+        HostBody &b = bodies[i];
+        b.pos[0] = p[i].x; b.pos[1] = p[i].y; b.pos[2] = p[i].z;
+        b.rot[0] = q[i].x; b.rot[1] = q[i].y; b.rot[2] = q[i].z; b.rot[3] = q[i].w;
+        b.lin[0] = l[i].x; b.lin[1] = l[i].y; b.lin[2] = l[i].z;
+        b.ang[0] = a[i].x; b.ang[1] = a[i].y; b.ang[2] = a[i].z;
+        // PhysicsWorld::step clears forces of live bodies (physics_world.cpp:766)
+        if (b.alive) b.force[0] = b.force[1] = b.force[2] = 0.0f;
+    }
+    deviceNewer_ = false;
+}
+
+void World::computePossiblePairs() {
+    // physics_world.cpp:568-581
+    std::vector<uint64_t> perBody(bodies.size(), 0);
+    uint64_t total = 0, count = 0;
+    for (const HostCollider &c : colliders) {
+        if (!c.alive || c.body >= bodies.size() || !bodies[c.body].alive || bodies[c.body].generation != c.bodyGeneration)
+            continue;
+        total += count - perBody[c.body];
+        ++perBody[c.body];
+        ++count;
+    }
+    possiblePairs_ = total;
+    dynamicAlive_ = 0;
+    for (const HostBody &b : bodies)
+        if (b.alive && !b.isStatic) ++dynamicAlive_;
+}
+
+void World::push() {
+    PE_CHECK(cudaSetDevice(device_));
+    nb_ = (uint32_t)bodies.size();
+    nc_ = (uint32_t)colliders.size();
+    ensureCapacity();
+    std::vector<float4> p(nb_), q(nb_), l(nb_), a(nb_), f(nb_), mat(nb_), ii(nb_);
+    std::vector<uint32_t> flags(nb_), gen(nb_);
+    forces_ = false;
+    for (uint32_t i = 0; i < nb_; ++i) {
+        const HostBody &b = bodies[i];
+        p[i] = make_float4(b.pos[0], b.pos[1], b.pos[2], 0.0f);
+        q[i] = make_float4(b.rot[0], b.rot[1], b.rot[2], b.rot[3]);
+        l[i] = make_float4(b.lin[0], b.lin[1], b.lin[2], 0.0f);
+        a[i] = make_float4(b.ang[0], b.ang[1], b.ang[2], 0.0f);
+        f[i] = make_float4(b.force[0], b.force[1], b.force[2], 0.0f);
+        if (b.alive && (b.force[0] != 0.0f || b.force[1] != 0.0f || b.force[2] != 0.0f)) forces_ = true;
+        // RigidBody::getInverseMass (rigid_body.hpp:72-75)
+        float invMass = b.isStatic || b.mass <= 0.0f ? 0.0f : 1.0f / b.mass;
+        mat[i] = make_float4(invMass, b.restitution, b.friction, b.mass);
+        ii[i] = make_float4(b.iinv[0], b.iinv[1], b.iinv[2], 0.0f);
+        flags[i] = (b.alive ? kBodyAlive : 0u) | (b.isStatic ? kBodyStatic : 0u);
+        gen[i] = b.generation;
+    }
+    upload(pos_[cur_], p, stream_);
+    upload(rot_[cur_], q, stream_);
+    upload(lin_[cur_], l, stream_);
+    upload(ang_[cur_], a, stream_);
+    upload(force_, f, stream_);
+    upload(mat_, mat, stream_);
+    upload(iinv_, ii, stream_);
+    upload(bflags_, flags, stream_);
+    upload(bgen_, gen, stream_);
+
+    std::vector<uint32_t> cb(nc_), cg(nc_), cf(nc_);
+    std::vector<float4> cs(nc_), lp(nc_), lr(nc_);
+    dense_ = true;
+    localIdentity_ = true;
+    for (uint32_t i = 0; i < nc_; ++i) {
+        const HostCollider &c = colliders[i];
+        cb[i] = c.body;
+        cg[i] = c.bodyGeneration;
+        cf[i] = (c.alive ? kColliderAlive : 0u) | (c.shape << 8);
+        float hw;
+        uint32_t hb = c.hull;
+        std::memcpy(&hw, &hb, 4);
+        cs[i] = make_float4(c.dims[0], c.dims[1], c.dims[2], hw);
+        lp[i] = make_float4(c.lpos[0], c.lpos[1], c.lpos[2], 0.0f);
+        lr[i] = make_float4(c.lrot[0], c.lrot[1], c.lrot[2], c.lrot[3]);
+        if (c.lpos[0] != 0.0f || c.lpos[1] != 0.0f || c.lpos[2] != 0.0f || c.lrot[0] != 0.0f || c.lrot[1] != 0.0f ||
+            c.lrot[2] != 0.0f || c.lrot[3] != 1.0f)
+            localIdentity_ = false;
+        bool valid = c.alive && c.body < nb_ && bodies[c.body].alive && bodies[c.body].generation == c.bodyGeneration;
+        if (!valid) dense_ = false;
+    }
+    upload(cbody_, cb, stream_);
+    upload(cbgen_, cg, stream_);
+    upload(cflags_, cf, stream_);
+    upload(cshape_, cs, stream_);
+    upload(clpos_, lp, stream_);
+    upload(clrot_, lr, stream_);
+    std::vector<uint32_t> ho(hullOffsets.begin(), hullOffsets.end());
+    std::vector<float4> hv(hullVerts.size() / 3);
+    for (size_t k = 0; k < hv.size(); ++k)
+        hv[k] = make_float4(hullVerts[3 * k], hullVerts[3 * k + 1], hullVerts[3 * k + 2], 0.0f);
+    upload(hullOffset_, ho, stream_);
+    upload(hullVerts_, hv, stream_);
+    computePossiblePairs();
+    PE_CHECK(cudaStreamSynchronize(stream_));
+    hostDirty_ = false;
+}
+
+void World::ensureScratch(uint32_t maxN) {
+    if (maxN <= scratchN_ && wsScan_.ptr) return;
+    scratchN_ = maxN;
+    // The narrowphase uses 256-item tiles for its look-back.
+    wsScan_.reserve((maxN + 255) / 256 + 16);
+    wsSortHist_.reserve(256 * 8 + 16);
+    wsSortState_.reserve(scratchBytesSort(maxN) / sizeof(uint32_t) + 16);
+    ws_.scanState = wsScan_.ptr;
+    ws_.sortHist = wsSortHist_.ptr;
+    ws_.sortState = wsSortState_.ptr;
+}
+
+void World::ensureCapacity() {
+    const uint32_t nb = std::max<uint32_t>(nb_, 1), nc = std::max<uint32_t>(nc_, 1);
+    for (int k = 0; k < 2; ++k) {
+        pos_[k].reserve(nb);
+        rot_[k].reserve(nb);
+        lin_[k].reserve(nb);
+        ang_[k].reserve(nb);
+    }
+    aabbMin_.reserve(nc);
+    aabbMax_.reserve(nc);
+    collectFlags_.reserve(nc);
+    collectPos_.reserve(nc);
+    inSlot_.reserve(nc);
+    inMin_.reserve(nc);
+    inMax_.reserve(nc);
+    sapKeys_.reserve(nc);
+    sapVals_.reserve(nc);
+    bbKeyTmp32_.reserve(nc);
+    bbValTmp_.reserve(nc);
+    bbMinX_.reserve(nc);
+    bbMaxX_.reserve(nc);
+    bbYZ_.reserve(nc);
+    bbIdx_.reserve(nc);
+    bbLen_.reserve(nc);
+    bbOff_.reserve(nc);
+    bbWidth_.reserve(nc);
+    bbWidthTmp_.reserve(nc);
+    bbFirst_.reserve(nc);
+    bbCellCount_.reserve(nc);
+    bbInGrid_.reserve(nc);
+    bbOverflow_.reserve(nc);
+    bbEntryOff_.reserve(nc);
+    bbCounters_.reserve(4);
+    if (entryCap_ < 8u * nc) entryCap_ = std::max<uint32_t>(65536, 8u * nc);
+    bbEntryKeys_.reserve(entryCap_);
+    bbEntryKeysTmp_.reserve(entryCap_);
+    bbEntryVals_.reserve(entryCap_);
+    bbEntryValsTmp_.reserve(entryCap_);
+    bb_ = BroadBuffers{bbKeyTmp32_.ptr, bbValTmp_.ptr, bbMinX_.ptr, bbMaxX_.ptr, bbYZ_.ptr, bbIdx_.ptr, bbLen_.ptr,
+                       bbOff_.ptr, bbWidth_.ptr, bbWidthTmp_.ptr, bbFirst_.ptr, bbCellCount_.ptr, bbInGrid_.ptr,
+                       bbOverflow_.ptr, bbEntryOff_.ptr, bbEntryKeys_.ptr, bbEntryKeysTmp_.ptr, bbEntryVals_.ptr,
+                       bbEntryValsTmp_.ptr, entryCap_, bbCounters_.ptr};
+
+    if (pairCap_ < 4u * nc) pairCap_ = std::max<uint32_t>(65536, 4u * nc);
+    pairKeys_.reserve(pairCap_);
+    pairKeysTmp_.reserve(pairCap_);
+    pairFlags_.reserve(pairCap_);
+    pairPos_.reserve(pairCap_);
+    pairA_.reserve(pairCap_);
+    pairB_.reserve(pairCap_);
+    pairCounters_.reserve(4);
+    pb_ = PairBuffers{pairKeys_.ptr, pairKeysTmp_.ptr, pairCap_, pairFlags_.ptr, pairPos_.ptr, pairA_.ptr, pairB_.ptr,
+                      pairCounters_.ptr};
+
+    if (mcap_ < pairCap_) mcap_ = pairCap_;
+    const uint32_t m = mcap_;
+    mBodyA_.reserve(m);
+    mGenA_.reserve(m);
+    mBodyB_.reserve(m);
+    mGenB_.reserve(m);
+    mCount_.reserve(m);
+    mRest_.reserve(m);
+    mNormal_.reserve(m);
+    mAnchorA_.reserve(4 * (size_t)m);
+    mAnchorB_.reserve(4 * (size_t)m);
+    mImpulse_.reserve(4 * (size_t)m);
+    mFeature_.reserve(4 * (size_t)m);
+
+    sBest_.reserve(nb);
+    sUsed_.reserve(2 * (size_t)nb);
+    sColor_.reserve(m);
+    sDyn_.reserve(m);
+    sColorCount_.reserve(kMaxColors);
+    sOrderKeys_.reserve(m);
+    sOrderKeysTmp_.reserve(m);
+    sOrder_.reserve(m);
+    sOrderTmp_.reserve(m);
+    sPm_.reserve(m);
+    sPmI_.reserve(6 * (size_t)m);
+    sPp_.reserve((size_t)kPreparedVec4 * 4 * m);
+    sPimp_.reserve(4 * (size_t)m);
+    sPn_.reserve(m);
+    sPbody_.reserve(m);
+    sPcount_.reserve(m);
+    sCacheKeys_.reserve(m);
+    sCacheKeysTmp_.reserve(m);
+    sCacheVals_.reserve(m);
+    sCacheValsTmp_.reserve(m);
+    sCacheCounts_.reserve(m);
+    sCacheOff_.reserve(m);
+    sBar_.reserve(2);
+    sCounters_.reserve(4);
+    sb_ = SolverBuffers{m,
+                        sBest_.ptr,
+                        sUsed_.ptr,
+                        sEpoch_.ptr,
+                        sColor_.ptr,
+                        sDyn_.ptr,
+                        sColorCount_.ptr,
+                        sOrderKeys_.ptr,
+                        sOrderKeysTmp_.ptr,
+                        sOrder_.ptr,
+                        sOrderTmp_.ptr,
+                        sPm_.ptr,
+                        sPmI_.ptr,
+                        sPp_.ptr,
+                        sPimp_.ptr,
+                        sPn_.ptr,
+                        sPbody_.ptr,
+                        sPcount_.ptr,
+                        sCacheKeys_.ptr,
+                        sCacheKeysTmp_.ptr,
+                        sCacheVals_.ptr,
+                        sCacheValsTmp_.ptr,
+                        sCacheCounts_.ptr,
+                        sCacheOff_.ptr,
+                        sBar_.ptr,
+                        sCounters_.ptr};
+
+    // Warm-start caches keep their contents when they grow.
+    const uint32_t needCache = 4 * m;
+    if (cacheCap_ < needCache) {
+        for (int k = 0; k < 2; ++k) {
+            DeviceArray<unsigned long long> nk, ng;
+            DeviceArray<float4> na, nbb;
+            DeviceArray<float> nt;
+            nk.reserve(needCache);
+            ng.reserve(needCache);
+            na.reserve(needCache);
+            nbb.reserve(needCache);
+            nt.reserve(needCache);
+            if (cacheCap_) {
+                PE_CHECK(cudaMemcpy(nk.ptr, cKey_[k].ptr, cacheCap_ * sizeof(unsigned long long), cudaMemcpyDeviceToDevice));
+                PE_CHECK(cudaMemcpy(ng.ptr, cGens_[k].ptr, cacheCap_ * sizeof(unsigned long long), cudaMemcpyDeviceToDevice));
+                PE_CHECK(cudaMemcpy(na.ptr, cA_[k].ptr, cacheCap_ * sizeof(float4), cudaMemcpyDeviceToDevice));
+                PE_CHECK(cudaMemcpy(nbb.ptr, cB_[k].ptr, cacheCap_ * sizeof(float4), cudaMemcpyDeviceToDevice));
+                PE_CHECK(cudaMemcpy(nt.ptr, cT2_[k].ptr, cacheCap_ * sizeof(float), cudaMemcpyDeviceToDevice));
+            }
+            std::swap(cKey_[k].ptr, nk.ptr);
+            std::swap(cKey_[k].count, nk.count);
+            std::swap(cGens_[k].ptr, ng.ptr);
+            std::swap(cGens_[k].count, ng.count);
+            std::swap(cA_[k].ptr, na.ptr);
+            std::swap(cA_[k].count, na.count);
+            std::swap(cB_[k].ptr, nbb.ptr);
+            std::swap(cB_[k].count, nbb.count);
+            std::swap(cT2_[k].ptr, nt.ptr);
+            std::swap(cT2_[k].count, nt.count);
+        }
+        cacheCap_ = needCache;
+    }
+    ensureScratch(std::max({nc, pairCap_, entryCap_, m}));
+}
+
+WorldView World::view(float dt) {
+    WorldView w;
+    w.nb = nb_;
+    w.nc = nc_;
+    w.cur = BodyState{pos_[cur_].ptr, rot_[cur_].ptr, lin_[cur_].ptr, ang_[cur_].ptr};
+    w.nxt = BodyState{pos_[1 - cur_].ptr, rot_[1 - cur_].ptr, lin_[1 - cur_].ptr, ang_[1 - cur_].ptr};
+    w.force = forces_ ? force_.ptr : nullptr;
+    w.mat = mat_.ptr;
+    w.iinv = iinv_.ptr;
+    w.bflags = bflags_.ptr;
+    w.bgen = bgen_.ptr;
+    w.cbody = cbody_.ptr;
+    w.cbgen = cbgen_.ptr;
+    w.cflags = cflags_.ptr;
+    w.cshape = cshape_.ptr;
+    w.clpos = localIdentity_ ? nullptr : clpos_.ptr;
+    w.clrot = localIdentity_ ? nullptr : clrot_.ptr;
+    w.hullOffset = hullOffset_.ptr;
+    w.hullVerts = hullVerts_.ptr;
+    w.aabbMin = aabbMin_.ptr;
+    w.aabbMax = aabbMax_.ptr;
+    w.gx = gravity[0];
+    w.gy = gravity[1];
+    w.gz = gravity[2];
+    w.dt = dt;
+    return w;
+}
+
+ManifoldView World::manifoldView() {
+    return ManifoldView{mBodyA_.ptr, mGenA_.ptr,     mBodyB_.ptr,   mGenB_.ptr,    mNormal_.ptr, mRest_.ptr,
+                        mCount_.ptr, mAnchorA_.ptr, mAnchorB_.ptr, mImpulse_.ptr, mFeature_.ptr};
+}
+
+CacheView World::cacheView(int which) {
+    return CacheView{cKey_[which].ptr, cGens_[which].ptr, cA_[which].ptr, cB_[which].ptr, cT2_[which].ptr};
+}
+
+void World::runPipeline(float dt) {
+    cudaStream_t s = stream_;
+    WorldView w = view(dt);
+    DevStats *st = stats_.ptr;
+    launchStepInit(st, dense_ ? nc_ : 0u, s);
+    const bool sap = algorithm == 0;
+    if (dense_) {
+        launchIntegrateAabb(w, sap ? sapKeys_.ptr : nullptr, sapVals_.ptr, s);
+    } else {
+        launchIntegrateAabb(w, nullptr, nullptr, s);
+        launchCollect(w, collectFlags_.ptr, collectPos_.ptr, inMin_.ptr, inMax_.ptr, inSlot_.ptr,
+                      sap ? sapKeys_.ptr : nullptr, sapVals_.ptr, &st->inputCount, ws_, &st->err, s);
+    }
+    BroadInput in{dense_ ? aabbMin_.ptr : inMin_.ptr, dense_ ? aabbMax_.ptr : inMax_.ptr, &st->inputCount, nc_};
+    if (sap) launchSap(in, sapKeys_.ptr, sapVals_.ptr, bb_, pb_, st, ws_, s);
+    else launchGrid(in, cellSize, bb_, pb_, st, ws_, s);
+    launchPairsFinalize(dense_ ? nullptr : inSlot_.ptr, cbody_.ptr, cbgen_.ptr, pb_, st, ws_, s);
+    ManifoldView mv = manifoldView();
+    launchNarrowphase(w, pb_, mv, mcap_, st, ws_, s);
+    int blocks = (int)std::min<uint32_t>((lastMEstimate_ + 1023) / 1024, (uint32_t)maxCooperativeBlocks(smCount_));
+    if (blocks < 1) blocks = 1;
+    launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], cacheView(1 - cache_), &cCount_.ptr[1 - cache_],
+                 cacheCap_, sb_, iterations, orderMode, blocks, st, ws_, s);
+    launchIntegratePose(w, s);
+    PE_CHECK(cudaMemcpyAsync(hostStats_, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
+}
+
+bool World::finishStep() {
+    PE_CHECK(cudaStreamSynchronize(stream_));
+    const DevStats &h = *hostStats_;
+    lastErr_ = h.err;
+    if (h.err & (kErrTimeout | kErrColors | kErrEntryCapacity)) {
+        throw std::runtime_error(std::string("step failed on the device: ") +
+                                 ((h.err & kErrTimeout) ? "a bounded wait timed out" :
+                                  (h.err & kErrColors) ? "more than 128 solver colours" :
+                                                         "grid cell range exceeds 64 key bits"));
+    }
+    bool retry = false;
+    if (h.rawPairs > pairCap_) {
+        pairCap_ = grow(h.rawPairs, pairCap_);
+        retry = true;
+    }
+    if (h.gridEntryCount > entryCap_) {
+        entryCap_ = grow(h.gridEntryCount, entryCap_);
+        retry = true;
+    }
+    if (h.manifolds > mcap_ || h.pairs > mcap_) {
+        mcap_ = grow(std::max(h.manifolds, h.pairs), mcap_);
+        retry = true;
+    }
+    if (retry) {
+        ensureCapacity();
+        return false;
+    }
+    StepCounters &c = counters_;
+    c = StepCounters{};
+    c.possiblePairs = possiblePairs_;
+    c.candidatePairs = h.pairs;
+    c.contactCount = h.manifolds;
+    c.solvedContactCount = h.solved;
+    c.awakeBodyCount = dynamicAlive_;
+    c.xWindow = h.xWindow;
+    c.aabbPairs = h.uniquePairs;
+    c.gridComparisons = h.gridComparisons;
+    c.gridEntries = algorithm == 1 ? h.gridEntryCount : 0;
+    c.gridOverflow = algorithm == 1 ? h.overflowCount : 0;
+    c.cellSize = algorithm == 1 ? h.cellSize : 0.0;
+    for (int k = 0; k < 4; ++k) {
+        c.npCandidates[k] = h.npCandidates[k];
+        c.npContacts[k] = h.npContacts[k];
+    }
+    c.preparedPoints = h.preparedPoints;
+    c.warmComparisons = h.warmComparisons;
+    c.warmMatches = h.warmMatches;
+    c.velocityPointVisits = h.preparedPoints * (uint64_t)iterations;
+    c.colors = orderMode == 0 ? h.manifolds : h.colors;
+    c.colorRounds = h.colorRounds;
+    c.epaFailures = h.epaFailures;
+    c.points = h.points;
+    lastPairs_ = h.pairs;
+    lastManifolds_ = h.manifolds;
+    lastMEstimate_ = h.manifolds;
+    cur_ = 1 - cur_;
+    cache_ = 1 - cache_;
+    deviceNewer_ = true;
+    ++steps_;
+    return true;
+}
+
+void World::step(float dt) {
+    PE_CHECK(cudaSetDevice(device_));
+    if (algorithm == 2) throw std::invalid_argument("DynamicTree requires a persistent DynamicAabbTree instance");
+    if (hostDirty_) {
+        pull();
+        push();
+    }
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        PE_CHECK(cudaEventRecord(evStart_, stream_));
+        runPipeline(dt);
+        PE_CHECK(cudaEventRecord(evEnd_, stream_));
+        if (finishStep()) {
+            float ms = 0;
+            PE_CHECK(cudaEventElapsedTime(&ms, evStart_, evEnd_));
+            counters_.gpuMs = ms;
+            return;
+        }
+    }
+    throw std::runtime_error("step buffers kept overflowing");
+}
+
+// ------------------------------------------------------------- downloads ---
+void World::downloadPairs(uint32_t *pairs) {
+    std::vector<uint32_t> a(lastPairs_), b(lastPairs_);
+    if (lastPairs_) {
+        PE_CHECK(cudaMemcpy(a.data(), pairA_.ptr, lastPairs_ * 4, cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(b.data(), pairB_.ptr, lastPairs_ * 4, cudaMemcpyDeviceToHost));
+    }
+    for (uint32_t i = 0; i < lastPairs_; ++i) {
+        pairs[2 * i] = a[i];
+        pairs[2 * i + 1] = b[i];
+    }
+}
+
+struct ManifoldRecord {
+    uint32_t aIdx, aGen, bIdx, bGen;
+    float normal[3];
+    uint32_t pointCount;
+    float friction, restitution;
+    float anchorA[4][3];
+    float anchorB[4][3];
+    float penetration[4];
+    float normalImpulse[4];
+    float tangentImpulse1[4];
+    float tangentImpulse2[4];
+    uint32_t feature[4];
+};
+static_assert(sizeof(ManifoldRecord) == 216, "manifold record layout");
+
+void World::downloadManifolds(void *records, uint32_t count) {
+    const uint32_t M = std::min(count, lastManifolds_);
+    std::vector<uint32_t> ba(M), ga(M), bbv(M), gb(M), cnt(M), feat(4 * (size_t)M);
+    std::vector<float4> nf(M), aa(4 * (size_t)M), ab(4 * (size_t)M), im(4 * (size_t)M);
+    std::vector<float> rest(M);
+    if (M) {
+        PE_CHECK(cudaMemcpy(ba.data(), mBodyA_.ptr, M * 4, cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(ga.data(), mGenA_.ptr, M * 4, cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(bbv.data(), mBodyB_.ptr, M * 4, cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(gb.data(), mGenB_.ptr, M * 4, cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(cnt.data(), mCount_.ptr, M * 4, cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(feat.data(), mFeature_.ptr, 4 * (size_t)M * 4, cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(nf.data(), mNormal_.ptr, M * sizeof(float4), cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(aa.data(), mAnchorA_.ptr, 4 * (size_t)M * sizeof(float4), cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(ab.data(), mAnchorB_.ptr, 4 * (size_t)M * sizeof(float4), cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(im.data(), mImpulse_.ptr, 4 * (size_t)M * sizeof(float4), cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(rest.data(), mRest_.ptr, M * 4, cudaMemcpyDeviceToHost));
+    }
+    ManifoldRecord *out = (ManifoldRecord *)records;
+    for (uint32_t m = 0; m < M; ++m) {
+        ManifoldRecord &r = out[m];
+        std::memset(&r, 0, sizeof(r));
+        r.aIdx = ba[m];
+        r.aGen = ga[m];
+        r.bIdx = bbv[m];
+        r.bGen = gb[m];
+        r.normal[0] = nf[m].x;
+        r.normal[1] = nf[m].y;
+        r.normal[2] = nf[m].z;
+        r.friction = nf[m].w;
+        r.restitution = rest[m];
+        r.pointCount = cnt[m];
+        for (int k = 0; k < 4; ++k) {
+            const float4 &A = aa[4 * m + k], &B = ab[4 * m + k], &I = im[4 * m + k];
+            r.anchorA[k][0] = A.x; r.anchorA[k][1] = A.y; r.anchorA[k][2] = A.z;
+            r.anchorB[k][0] = B.x; r.anchorB[k][1] = B.y; r.anchorB[k][2] = B.z;
+            r.penetration[k] = A.w;
+            r.normalImpulse[k] = I.x;
+            r.tangentImpulse1[k] = I.y;
+            r.tangentImpulse2[k] = I.z;
+            r.feature[k] = feat[4 * m + k];
+        }
+    }
+}
+
+void World::downloadOrder(uint32_t *order, uint32_t *colors) {
+    const uint32_t M = lastManifolds_;
+    if (!M) return;
+    if (order) PE_CHECK(cudaMemcpy(order, sOrder_.ptr, M * 4, cudaMemcpyDeviceToHost));
+    if (colors) {
+        if (orderMode == 0)
+            for (uint32_t m = 0; m < M; ++m) colors[m] = m;
+        else
+            PE_CHECK(cudaMemcpy(colors, sColor_.ptr, M * 4, cudaMemcpyDeviceToHost));
+    }
+}
+
+// --------------------------------------------------------------- stages ----
+void World::broadphaseOnly(const float *mins, const float *maxs, uint32_t n, int algo, double cell,
+                           std::vector<uint32_t> &pairs, StepCounters &c) {
+    PE_CHECK(cudaSetDevice(device_));
+    if (algo == 2) throw std::invalid_argument("DynamicTree requires a persistent DynamicAabbTree instance");
+    uint32_t saveNc = nc_;
+    nc_ = std::max(nc_, n);
+    ensureCapacity();
+    nc_ = saveNc;
+    std::vector<float4> mn(n), mx(n);
+    std::vector<uint32_t> keys(n), vals(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        mn[i] = make_float4(mins[3 * i], mins[3 * i + 1], mins[3 * i + 2], 0.0f);
+        mx[i] = make_float4(maxs[3 * i], maxs[3 * i + 1], maxs[3 * i + 2], 0.0f);
+    }
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        cudaStream_t s = stream_;
+        DevStats *st = stats_.ptr;
+        if (n) {
+            PE_CHECK(cudaMemcpyAsync(inMin_.ptr, mn.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s));
+            PE_CHECK(cudaMemcpyAsync(inMax_.ptr, mx.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s));
+        }
+        launchStepInit(st, n, s);
+        BroadInput in{inMin_.ptr, inMax_.ptr, &st->inputCount, std::max<uint32_t>(n, 1)};
+        if (algo == 0) {
+            launchSapKeys(in, sapKeys_.ptr, sapVals_.ptr, s);
+            launchSap(in, sapKeys_.ptr, sapVals_.ptr, bb_, pb_, st, ws_, s);
+        } else {
+            launchGrid(in, cell, bb_, pb_, st, ws_, s);
+        }
+        launchPairsFinalize(nullptr, nullptr, nullptr, pb_, st, ws_, s);
+        PE_CHECK(cudaMemcpyAsync(hostStats_, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
+        PE_CHECK(cudaStreamSynchronize(s));
+        const DevStats &h = *hostStats_;
+        if (h.err & (kErrTimeout | kErrEntryCapacity)) throw std::runtime_error("broadphase failed on the device");
+        bool retry = false;
+        if (h.rawPairs > pairCap_) {
+            pairCap_ = grow(h.rawPairs, pairCap_);
+            retry = true;
+        }
+        if (h.gridEntryCount > entryCap_) {
+            entryCap_ = grow(h.gridEntryCount, entryCap_);
+            retry = true;
+        }
+        if (retry) {
+            uint32_t save = nc_;
+            nc_ = std::max(nc_, n);
+            ensureCapacity();
+            nc_ = save;
+            continue;
+        }
+        c = StepCounters{};
+        c.xWindow = algo == 0 ? h.xWindow : 0;
+        c.aabbPairs = h.uniquePairs;
+        c.gridComparisons = h.gridComparisons;
+        c.gridEntries = algo == 1 ? h.gridEntryCount : 0;
+        c.gridOverflow = algo == 1 ? h.overflowCount : 0;
+        c.cellSize = algo == 1 ? h.cellSize : 0.0;
+        pairs.resize(2 * (size_t)h.pairs);
+        std::vector<uint32_t> a(h.pairs), b(h.pairs);
+        if (h.pairs) {
+            PE_CHECK(cudaMemcpy(a.data(), pairA_.ptr, h.pairs * 4, cudaMemcpyDeviceToHost));
+            PE_CHECK(cudaMemcpy(b.data(), pairB_.ptr, h.pairs * 4, cudaMemcpyDeviceToHost));
+        }
+        for (uint32_t i = 0; i < h.pairs; ++i) {
+            pairs[2 * i] = a[i];
+            pairs[2 * i + 1] = b[i];
+        }
+        return;
+    }
+    throw std::runtime_error("broadphase buffers kept overflowing");
+}
+
+void World::solveOnly(std::vector<float> &recs, uint32_t count, float dt, int iters, int mode) {
+    PE_CHECK(cudaSetDevice(device_));
+    if (hostDirty_) {
+        pull();
+        push();
+    }
+    if (count > mcap_) {
+        mcap_ = grow(count, mcap_);
+        ensureCapacity();
+    }
+    ManifoldRecord *r = (ManifoldRecord *)recs.data();
+    std::vector<uint32_t> ba(count), ga(count), bbv(count), gb(count), cnt(count), feat(4 * (size_t)count);
+    std::vector<float4> nf(count), aa(4 * (size_t)count), ab(4 * (size_t)count), im(4 * (size_t)count);
+    std::vector<float> rest(count);
+    for (uint32_t m = 0; m < count; ++m) {
+        ba[m] = r[m].aIdx;
+        ga[m] = r[m].aGen;
+        bbv[m] = r[m].bIdx;
+        gb[m] = r[m].bGen;
+        cnt[m] = r[m].pointCount;
+        nf[m] = make_float4(r[m].normal[0], r[m].normal[1], r[m].normal[2], r[m].friction);
+        rest[m] = r[m].restitution;
+        for (int k = 0; k < 4; ++k) {
+            aa[4 * m + k] = make_float4(r[m].anchorA[k][0], r[m].anchorA[k][1], r[m].anchorA[k][2], r[m].penetration[k]);
+            ab[4 * m + k] = make_float4(r[m].anchorB[k][0], r[m].anchorB[k][1], r[m].anchorB[k][2], 0.0f);
+            im[4 * m + k] = make_float4(r[m].normalImpulse[k], r[m].tangentImpulse1[k], r[m].tangentImpulse2[k], 0.0f);
+            feat[4 * m + k] = r[m].feature[k];
+        }
+    }
+    cudaStream_t s = stream_;
+    auto up = [&](void *d, const void *h, size_t bytes) {
+        if (bytes) PE_CHECK(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s));
+    };
+    up(mBodyA_.ptr, ba.data(), count * 4);
+    up(mGenA_.ptr, ga.data(), count * 4);
+    up(mBodyB_.ptr, bbv.data(), count * 4);
+    up(mGenB_.ptr, gb.data(), count * 4);
+    up(mCount_.ptr, cnt.data(), count * 4);
+    up(mFeature_.ptr, feat.data(), 4 * (size_t)count * 4);
+    up(mNormal_.ptr, nf.data(), count * sizeof(float4));
+    up(mAnchorA_.ptr, aa.data(), 4 * (size_t)count * sizeof(float4));
+    up(mAnchorB_.ptr, ab.data(), 4 * (size_t)count * sizeof(float4));
+    up(mImpulse_.ptr, im.data(), 4 * (size_t)count * sizeof(float4));
+    up(mRest_.ptr, rest.data(), count * 4);
+    DevStats *st = stats_.ptr;
+    launchStepInit(st, 0, s);
+    launchSetManifoldCount(st, count, s);
+    const size_t bytes = (size_t)std::max<uint32_t>(nb_, 1) * sizeof(float4);
+    PE_CHECK(cudaMemcpyAsync(pos_[1 - cur_].ptr, pos_[cur_].ptr, bytes, cudaMemcpyDeviceToDevice, s));
+    PE_CHECK(cudaMemcpyAsync(rot_[1 - cur_].ptr, rot_[cur_].ptr, bytes, cudaMemcpyDeviceToDevice, s));
+    PE_CHECK(cudaMemcpyAsync(lin_[1 - cur_].ptr, lin_[cur_].ptr, bytes, cudaMemcpyDeviceToDevice, s));
+    PE_CHECK(cudaMemcpyAsync(ang_[1 - cur_].ptr, ang_[cur_].ptr, bytes, cudaMemcpyDeviceToDevice, s));
+    WorldView w = view(dt);
+    ManifoldView mv = manifoldView();
+    int blocks = (int)std::min<uint32_t>((count + 1023) / 1024, (uint32_t)maxCooperativeBlocks(smCount_));
+    if (blocks < 1) blocks = 1;
+    launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], cacheView(1 - cache_), &cCount_.ptr[1 - cache_],
+                 cacheCap_, sb_, iters, mode, blocks, st, ws_, s);
+    PE_CHECK(cudaMemcpyAsync(hostStats_, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
+    PE_CHECK(cudaStreamSynchronize(s));
+    if (hostStats_->err & (kErrTimeout | kErrColors)) throw std::runtime_error("solve failed on the device");
+    counters_ = StepCounters{};
+    counters_.solvedContactCount = hostStats_->solved;
+    counters_.preparedPoints = hostStats_->preparedPoints;
+    counters_.warmComparisons = hostStats_->warmComparisons;
+    counters_.warmMatches = hostStats_->warmMatches;
+    counters_.velocityPointVisits = hostStats_->preparedPoints * (uint64_t)iters;
+    counters_.colors = mode == 0 ? count : hostStats_->colors;
+    cur_ = 1 - cur_;
+    cache_ = 1 - cache_;
+    deviceNewer_ = true;
+    lastManifolds_ = count;
+    downloadManifolds(recs.data(), count);
+}
+
+} // namespace pe

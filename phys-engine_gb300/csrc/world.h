@@ -1,0 +1,210 @@
+// Host side of a GPU world: the reference's slot/generation storage
+// (src/world/physics_world.cpp:162-339) kept as a host mirror, device
+// structure-of-arrays state, and the step pipeline.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "pe_engine.h"
+#include "pe_stages.h"
+
+namespace pe {
+
+template <class T> struct DeviceArray {
+    T *ptr = nullptr;
+    size_t count = 0;
+    DeviceArray() = default;
+    DeviceArray(const DeviceArray &) = delete;
+    DeviceArray &operator=(const DeviceArray &) = delete;
+    ~DeviceArray() { release(); }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        count = 0;
+    }
+    // Grows to at least n elements (contents are not kept); zero-filled.
+    void reserve(size_t n) {
+        if (n <= count && ptr) return;
+        release();
+        size_t c = n ? n : 1;
+        PE_CHECK(cudaMalloc(&ptr, c * sizeof(T)));
+        PE_CHECK(cudaMemset(ptr, 0, c * sizeof(T)));
+        PE_CHECK(cudaDeviceSynchronize());
+        count = c;
+    }
+};
+
+struct HostBody {
+    float mass = 0, restitution = 0, friction = 0;
+    bool isStatic = false;
+    float pos[3] = {0, 0, 0};
+    float rot[4] = {0, 0, 0, 1};
+    float lin[3] = {0, 0, 0};
+    float ang[3] = {0, 0, 0};
+    float force[3] = {0, 0, 0};
+    float iinv[3] = {0, 0, 0};  // diagonal local inverse inertia
+    uint32_t generation = 0;
+    bool alive = false;
+};
+
+struct HostCollider {
+    uint32_t body = 0, bodyGeneration = 0;
+    float lpos[3] = {0, 0, 0};
+    float lrot[4] = {0, 0, 0, 1};
+    uint32_t shape = 0;
+    float dims[3] = {0, 0, 0};  // radius or half extents
+    uint32_t hull = 0;
+    uint32_t generation = 0;
+    bool alive = false;
+};
+
+struct StepCounters {
+    uint64_t possiblePairs = 0, candidatePairs = 0, contactCount = 0, solvedContactCount = 0;
+    uint64_t awakeBodyCount = 0, xWindow = 0, aabbPairs = 0, gridComparisons = 0, gridEntries = 0,
+             gridOverflow = 0;
+    double cellSize = 0;
+    uint64_t npCandidates[4] = {0, 0, 0, 0}, npContacts[4] = {0, 0, 0, 0};
+    uint64_t preparedPoints = 0, warmComparisons = 0, warmMatches = 0, velocityPointVisits = 0;
+    uint64_t colors = 0, colorRounds = 0, epaFailures = 0, points = 0;
+    double gpuMs = 0;
+};
+
+class World {
+  public:
+    explicit World(int device);
+    ~World();
+    World(const World &) = delete;
+    World &operator=(const World &) = delete;
+
+    // configuration (PhysicsWorld::gravity, broadPhaseAlgorithm; solver
+    // iteration count and order are additions)
+    float gravity[3] = {0.0f, -9.81f, 0.0f};
+    int algorithm = 0;        // 0 SAP, 1 uniform grid, 2 dynamic tree (unsupported)
+    double cellSize = 0.0;    // grid: <= 0 median (reference), > 0 fixed
+    int iterations = 8;
+    int orderMode = 1;        // 0 manifold order (serial), 1 graph-colour order
+
+    // host mirror (bodies / colliders by slot)
+    std::vector<HostBody> bodies;
+    std::vector<uint32_t> freeBodies;
+    std::vector<HostCollider> colliders;
+    std::vector<uint32_t> freeColliders;
+    std::vector<float> hullVerts;          // xyz per vertex
+    std::vector<uint32_t> hullOffsets{0};
+
+    uint32_t addBody(const HostBody &b, uint32_t &generation);
+    uint32_t addCollider(const HostCollider &c, uint32_t &generation);
+    void removeBody(uint32_t index, uint32_t generation);
+    void removeCollider(uint32_t index, uint32_t generation);
+    HostBody *body(uint32_t index, uint32_t generation);
+    HostCollider *collider(uint32_t index, uint32_t generation);
+    int addHull(const float *verts, uint32_t count);
+
+    // Host-mirror access: pull() refreshes it from the device, touch() marks it
+    // modified so the next step uploads it.
+    void pull();
+    void touch() { hostDirty_ = true; }
+
+    void step(float dt);
+    // Standalone stages (BroadPhase::findCandidatePairs, solve on explicit manifolds).
+    void broadphaseOnly(const float *mins, const float *maxs, uint32_t n, int algo, double cell,
+                        std::vector<uint32_t> &pairs, StepCounters &c);
+    void solveOnly(std::vector<float> &manifoldRecords, uint32_t count, float dt, int iterations, int mode);
+
+    const StepCounters &counters() const { return counters_; }
+    uint32_t manifoldCount() const { return lastManifolds_; }
+    uint32_t pairCount() const { return lastPairs_; }
+    void downloadPairs(uint32_t *pairs);
+    // Manifold fields in the pe_contact_manifold layout (see capi).
+    void downloadManifolds(void *records, uint32_t count);
+    void downloadOrder(uint32_t *order, uint32_t *colors);
+    uint32_t statusBits() const { return lastErr_; }
+    int device() const { return device_; }
+    cudaStream_t stream() const { return stream_; }
+    uint64_t stepsTaken() const { return steps_; }
+    void syncDevice();
+
+  private:
+    void push();
+    void ensureCapacity();
+    void ensureScratch(uint32_t maxN);
+    WorldView view(float dt);
+    ManifoldView manifoldView();
+    CacheView cacheView(int which);
+    void runPipeline(float dt);
+    bool finishStep();
+    void computePossiblePairs();
+
+    int device_;
+    int smCount_ = 152;
+    cudaStream_t stream_ = nullptr;
+    bool hostDirty_ = true;
+    bool deviceNewer_ = false;
+    bool dense_ = true;
+    bool forces_ = false;
+    bool localIdentity_ = true;
+    uint32_t nb_ = 0, nc_ = 0, nin_ = 0;
+    int cur_ = 0;
+    int cache_ = 0;
+    uint64_t steps_ = 0;
+    uint32_t lastErr_ = 0;
+    uint32_t lastPairs_ = 0, lastManifolds_ = 0, lastMEstimate_ = 0;
+    uint64_t possiblePairs_ = 0, dynamicAlive_ = 0;
+    StepCounters counters_;
+
+    // body state (two copies), static body data, colliders
+    DeviceArray<float4> pos_[2], rot_[2], lin_[2], ang_[2];
+    DeviceArray<float4> force_, mat_, iinv_;
+    DeviceArray<uint32_t> bflags_, bgen_;
+    DeviceArray<uint32_t> cbody_, cbgen_, cflags_;
+    DeviceArray<float4> cshape_, clpos_, clrot_, aabbMin_, aabbMax_;
+    DeviceArray<uint32_t> hullOffset_;
+    DeviceArray<float4> hullVerts_;
+    // broadphase input compaction
+    DeviceArray<uint32_t> collectFlags_, collectPos_, inSlot_;
+    DeviceArray<float4> inMin_, inMax_;
+    DeviceArray<uint32_t> sapKeys_, sapVals_;
+    // broadphase / pairs
+    BroadBuffers bb_{};
+    DeviceArray<uint32_t> bbKeyTmp32_, bbValTmp_, bbIdx_, bbLen_, bbOff_, bbCellCount_, bbOverflow_, bbEntryOff_,
+        bbEntryVals_, bbEntryValsTmp_, bbCounters_;
+    DeviceArray<float> bbMinX_, bbMaxX_;
+    DeviceArray<float4> bbYZ_;
+    DeviceArray<unsigned long long> bbWidth_, bbWidthTmp_, bbEntryKeys_, bbEntryKeysTmp_;
+    DeviceArray<int4> bbFirst_;
+    DeviceArray<uint8_t> bbInGrid_;
+    uint32_t entryCap_ = 0;
+    PairBuffers pb_{};
+    DeviceArray<unsigned long long> pairKeys_, pairKeysTmp_;
+    DeviceArray<uint32_t> pairFlags_, pairPos_, pairA_, pairB_, pairCounters_;
+    uint32_t pairCap_ = 0;
+    // manifolds
+    uint32_t mcap_ = 0;
+    DeviceArray<uint32_t> mBodyA_, mGenA_, mBodyB_, mGenB_, mCount_, mFeature_;
+    DeviceArray<float4> mNormal_, mAnchorA_, mAnchorB_, mImpulse_;
+    DeviceArray<float> mRest_;
+    // solver
+    SolverBuffers sb_{};
+    DeviceArray<unsigned long long> sBest_, sUsed_, sEpoch_, sCacheKeys_, sCacheKeysTmp_;
+    DeviceArray<uint32_t> sColor_, sDyn_, sColorCount_, sOrderKeys_, sOrderKeysTmp_, sOrder_, sOrderTmp_, sPcount_,
+        sCacheVals_, sCacheValsTmp_, sCacheCounts_, sCacheOff_, sBar_, sCounters_;
+    DeviceArray<float4> sPm_, sPmI_, sPp_, sPimp_, sPn_;
+    DeviceArray<uint2> sPbody_;
+    // warm-start caches (two copies)
+    DeviceArray<unsigned long long> cKey_[2], cGens_[2];
+    DeviceArray<float4> cA_[2], cB_[2];
+    DeviceArray<float> cT2_[2];
+    DeviceArray<uint32_t> cCount_;  // [2]
+    uint32_t cacheCap_ = 0;
+    // scratch and stats
+    Scratch ws_{};
+    DeviceArray<unsigned long long> wsScan_;
+    DeviceArray<uint32_t> wsSortHist_, wsSortState_;
+    uint32_t scratchN_ = 0;
+    DeviceArray<DevStats> stats_;
+    DevStats *hostStats_ = nullptr;
+    cudaEvent_t evStart_ = nullptr, evEnd_ = nullptr;
+};
+
+} // namespace pe

@@ -1,0 +1,328 @@
+"""ctypes binding of the GPU engine's C ABI (include/phys_gb300.h).
+
+:class:`GpuWorld` mirrors ``phys::PhysicsWorld`` (include/phys/world/physics_world.hpp
+of bkuangs/phys-engine): bodies are created through the same factories with the
+same validation, ``step(dt)`` runs the whole collision-and-contact path on the
+GPU, and contacts / stats / candidate pairs can be read back.  Every call goes
+through ``libphys_gb300.so``; there is no host fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native
+
+_P = ctypes.c_void_p
+_u32 = ctypes.c_uint32
+
+
+class Handle(ctypes.Structure):
+    _fields_ = [("index", ctypes.c_uint32), ("generation", ctypes.c_uint32)]
+
+
+class BodyState(ctypes.Structure):
+    _fields_ = [("position", ctypes.c_float * 3), ("rotation", ctypes.c_float * 4),
+                ("linear_velocity", ctypes.c_float * 3), ("angular_velocity", ctypes.c_float * 3),
+                ("force", ctypes.c_float * 3), ("mass", ctypes.c_float), ("restitution", ctypes.c_float),
+                ("friction", ctypes.c_float), ("is_static", ctypes.c_int32)]
+
+
+MANIFOLD_DTYPE = np.dtype([
+    ("body_a_index", "<u4"), ("body_a_generation", "<u4"),
+    ("body_b_index", "<u4"), ("body_b_generation", "<u4"),
+    ("normal", "<f4", (3,)), ("point_count", "<u4"),
+    ("friction", "<f4"), ("restitution", "<f4"),
+    ("anchor_a", "<f4", (4, 3)), ("anchor_b", "<f4", (4, 3)),
+    ("penetration", "<f4", (4,)), ("normal_impulse", "<f4", (4,)),
+    ("tangent_impulse1", "<f4", (4,)), ("tangent_impulse2", "<f4", (4,)),
+    ("feature", "<u4", (4,)),
+])
+assert MANIFOLD_DTYPE.itemsize == 216
+
+STATS_DTYPE = np.dtype([
+    ("possible_pairs", "<u8"), ("candidate_pairs", "<u8"), ("contact_count", "<u8"),
+    ("solved_contact_count", "<u8"), ("awake_body_count", "<u8"), ("sleeping_body_count", "<u8"),
+    ("x_window_comparisons", "<u8"), ("aabb_pairs", "<u8"), ("grid_comparisons", "<u8"),
+    ("grid_entries", "<u8"), ("grid_overflow_aabbs", "<u8"), ("grid_cell_size", "<f8"),
+    ("np_candidates", "<u8", (4,)), ("np_contacts", "<u8", (4,)),
+    ("prepared_points", "<u8"), ("warm_start_comparisons", "<u8"), ("warm_start_matches", "<u8"),
+    ("velocity_point_visits", "<u8"), ("color_count", "<u8"), ("color_rounds", "<u8"),
+    ("epa_failures", "<u8"), ("contact_points", "<u8"), ("total_ms", "<f8"),
+])
+
+SAP, GRID, TREE = 0, 1, 2
+ORDER_MANIFOLD, ORDER_COLOR = 0, 1
+
+PE_OK = 0
+_STATUS = {1: ValueError, 2: ValueError, 3: LookupError, 4: OverflowError, 5: NotImplementedError,
+           6: RuntimeError, 7: RuntimeError}
+
+# Every entry point declared in include/phys_gb300.h: name -> (restype, argtypes).
+SIGNATURES = {
+    "pe_last_error": (ctypes.c_char_p, []),
+    "pe_device_count": (ctypes.c_int, []),
+    "pe_world_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_P)]),
+    "pe_world_destroy": (None, [_P]),
+    "pe_world_set_gravity": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float]),
+    "pe_world_get_gravity": (ctypes.c_int, [_P, _P]),
+    "pe_world_set_broadphase": (ctypes.c_int, [_P, ctypes.c_int]),
+    "pe_world_get_broadphase": (ctypes.c_int, [_P, _P]),
+    "pe_world_set_grid_cell_size": (ctypes.c_int, [_P, ctypes.c_double]),
+    "pe_world_set_solver": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
+    "pe_world_set_worker_counts": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]),
+    "pe_world_set_sleeping_enabled": (ctypes.c_int, [_P, ctypes.c_int]),
+    "pe_world_create_sphere": (ctypes.c_int, [_P, ctypes.c_float, _P, ctypes.c_float, ctypes.c_int,
+                                              ctypes.c_float, ctypes.c_float, _P, _P]),
+    "pe_world_create_box": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, _P,
+                                           ctypes.c_float, ctypes.c_int, ctypes.c_float, ctypes.c_float, _P, _P]),
+    "pe_world_create_bodies": (ctypes.c_int, [_P, _u32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "pe_world_create_hull": (ctypes.c_int, [_P, _P, _u32, _P, ctypes.c_float, _P, ctypes.c_int, ctypes.c_float,
+                                            ctypes.c_float, _P, _P]),
+    "pe_world_add_collider": (ctypes.c_int, [_P, Handle, ctypes.c_int, _P, _P, _P, _P]),
+    "pe_world_remove_body": (ctypes.c_int, [_P, Handle]),
+    "pe_world_remove_collider": (ctypes.c_int, [_P, Handle]),
+    "pe_world_get_body": (ctypes.c_int, [_P, Handle, _P]),
+    "pe_world_set_body": (ctypes.c_int, [_P, Handle, _P]),
+    "pe_world_body_integrate_rotation": (ctypes.c_int, [_P, Handle, ctypes.c_float]),
+    "pe_world_body_slot_count": (_u32, [_P]),
+    "pe_world_read_bodies": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "pe_world_step": (ctypes.c_int, [_P, ctypes.c_float]),
+    "pe_world_get_step_stats": (ctypes.c_int, [_P, _P]),
+    "pe_world_get_contacts": (ctypes.c_int, [_P, _P, _u32, _P]),
+    "pe_world_get_candidate_pairs": (ctypes.c_int, [_P, _P, _u32, _P]),
+    "pe_world_get_solve_order": (ctypes.c_int, [_P, _P, _P, _u32, _P]),
+    "pe_world_solve": (ctypes.c_int, [_P, _P, _u32, ctypes.c_float]),
+    "pe_broadphase_find_pairs": (ctypes.c_int, [ctypes.c_int, _P, _P, _u32, ctypes.c_int, ctypes.c_double, _P,
+                                                ctypes.c_uint64, _P, _P]),
+    "pe_generate_contact": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _P, _P, _P, ctypes.c_int, _P, _P, _P, _P,
+                                           _P]),
+}
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        l = _native.engine_lib()
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(l, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_P)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def check(rc: int):
+    if rc != PE_OK:
+        msg = lib().pe_last_error().decode()
+        raise _STATUS.get(rc, RuntimeError)(f"phys_gb300 status {rc}: {msg}")
+
+
+class GpuWorld:
+    """GPU-resident world with the reference PhysicsWorld's creation API."""
+
+    def __init__(self, device=0, algo=SAP, cell_size=0.0, iterations=8, order=ORDER_COLOR):
+        self.lib = lib()
+        h = _P()
+        check(self.lib.pe_world_create(int(device), ctypes.byref(h)))
+        self.h = h
+        self.device = device
+        self.set_broadphase(algo, cell_size)
+        self.set_solver(iterations, order)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pe_world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # configuration -------------------------------------------------------
+    def set_gravity(self, g):
+        check(self.lib.pe_world_set_gravity(self.h, float(g[0]), float(g[1]), float(g[2])))
+
+    def set_broadphase(self, algo, cell_size=0.0):
+        check(self.lib.pe_world_set_broadphase(self.h, int(algo)))
+        check(self.lib.pe_world_set_grid_cell_size(self.h, float(cell_size)))
+
+    def set_solver(self, iterations, order):
+        check(self.lib.pe_world_set_solver(self.h, int(iterations), int(order)))
+
+    # bodies --------------------------------------------------------------
+    def create_body(self, shape, dims, pos, density, is_static, restitution, friction):
+        b, c = Handle(), Handle()
+        p = _f32(pos)
+        if int(shape) == 0:
+            rc = self.lib.pe_world_create_sphere(self.h, float(dims[0]), _ptr(p), float(density), int(is_static),
+                                                 float(restitution), float(friction), ctypes.byref(b), ctypes.byref(c))
+        else:
+            rc = self.lib.pe_world_create_box(self.h, float(dims[0]), float(dims[1]), float(dims[2]), _ptr(p),
+                                              float(density), int(is_static), float(restitution), float(friction),
+                                              ctypes.byref(b), ctypes.byref(c))
+        check(rc)
+        return np.array([b.index, b.generation, c.index, c.generation], np.uint32)
+
+    def create_hull(self, vertices, pos, mass, inv_inertia, is_static, restitution, friction):
+        b, c = Handle(), Handle()
+        v = _f32(vertices)
+        check(self.lib.pe_world_create_hull(self.h, _ptr(v), len(v), _ptr(_f32(pos)), float(mass),
+                                            _ptr(_f32(inv_inertia)), int(is_static), float(restitution),
+                                            float(friction), ctypes.byref(b), ctypes.byref(c)))
+        return np.array([b.index, b.generation, c.index, c.generation], np.uint32)
+
+    def load_scene(self, scene):
+        """Creates the scene's bodies in order (spheres/boxes in one bulk call per
+        run, hulls one by one) and returns [n, 4] handles (body idx, gen,
+        collider idx, gen)."""
+        n = scene.count
+        handles = np.zeros((n, 4), np.uint32)
+        i = 0
+        while i < n:
+            if scene.shape[i] == 2:
+                handles[i] = self.create_hull(scene.hull(scene.hull_id[i]), scene.pos[i], scene.mass[i],
+                                              scene.inv_inertia[i], scene.is_static[i], scene.restitution[i],
+                                              scene.friction[i])
+                h = Handle(int(handles[i, 0]), int(handles[i, 1]))
+                if np.any(scene.spin[i] != 0) and not scene.is_static[i]:
+                    self.apply_spin(h, scene.spin[i])
+                if np.any(scene.linvel[i] != 0):
+                    st = self.get_body(h)
+                    st.linear_velocity[:] = [float(x) for x in scene.linvel[i]]
+                    self.set_body(h, st)
+                i += 1
+                continue
+            j = i
+            while j < n and scene.shape[j] != 2:
+                j += 1
+            sl = slice(i, j)
+            m = j - i
+            bh = (Handle * m)()
+            ch = (Handle * m)()
+            failed = _u32()
+            rc = self.lib.pe_world_create_bodies(
+                self.h, m, _ptr(np.ascontiguousarray(scene.shape[sl], np.uint8)), _ptr(_f32(scene.dims[sl])),
+                _ptr(_f32(scene.pos[sl])), _ptr(_f32(scene.density[sl])),
+                _ptr(np.ascontiguousarray(scene.is_static[sl], np.uint8)), _ptr(_f32(scene.restitution[sl])),
+                _ptr(_f32(scene.friction[sl])), _ptr(_f32(scene.linvel[sl])), _ptr(_f32(scene.spin[sl])),
+                ctypes.cast(bh, _P), ctypes.cast(ch, _P), ctypes.byref(failed))
+            check(rc)
+            raw_b = np.ctypeslib.as_array(ctypes.cast(bh, ctypes.POINTER(ctypes.c_uint32)), shape=(2 * m,))
+            raw_c = np.ctypeslib.as_array(ctypes.cast(ch, ctypes.POINTER(ctypes.c_uint32)), shape=(2 * m,))
+            handles[sl, 0:2] = raw_b.reshape(m, 2)
+            handles[sl, 2:4] = raw_c.reshape(m, 2)
+            i = j
+        return handles
+
+    def get_body(self, h) -> BodyState:
+        st = BodyState()
+        check(self.lib.pe_world_get_body(self.h, h, ctypes.byref(st)))
+        return st
+
+    def set_body(self, h, st: BodyState):
+        check(self.lib.pe_world_set_body(self.h, h, ctypes.byref(st)))
+
+    def apply_spin(self, h, spin):
+        """setAngularVelocity(spin); integrateRotation(1); setAngularVelocity(0)."""
+        st = self.get_body(h)
+        st.angular_velocity[:] = [float(x) for x in spin]
+        self.set_body(h, st)
+        check(self.lib.pe_world_body_integrate_rotation(self.h, h, 1.0))
+        st = self.get_body(h)
+        st.angular_velocity[:] = [0.0, 0.0, 0.0]
+        self.set_body(h, st)
+
+    def remove_body(self, idx, gen):
+        check(self.lib.pe_world_remove_body(self.h, Handle(int(idx), int(gen))))
+
+    def body_count(self):
+        return int(self.lib.pe_world_body_slot_count(self.h))
+
+    def bodies(self):
+        n = self.body_count()
+        pos = np.zeros((n, 3), np.float32)
+        quat = np.zeros((n, 4), np.float32)
+        lin = np.zeros((n, 3), np.float32)
+        ang = np.zeros((n, 3), np.float32)
+        check(self.lib.pe_world_read_bodies(self.h, _ptr(pos), _ptr(quat), _ptr(lin), _ptr(ang)))
+        return {"pos": pos, "quat": quat, "lin": lin, "ang": ang}
+
+    # stepping ------------------------------------------------------------
+    def step(self, dt):
+        check(self.lib.pe_world_step(self.h, float(dt)))
+
+    def stats(self):
+        s = np.zeros(1, STATS_DTYPE)
+        check(self.lib.pe_world_get_step_stats(self.h, _ptr(s)))
+        return s[0]
+
+    def contacts(self):
+        n = _u32()
+        check(self.lib.pe_world_get_contacts(self.h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, MANIFOLD_DTYPE)
+        if n.value:
+            check(self.lib.pe_world_get_contacts(self.h, _ptr(out), n.value, ctypes.byref(n)))
+        return out
+
+    def pairs(self):
+        n = _u32()
+        check(self.lib.pe_world_get_candidate_pairs(self.h, None, 0, ctypes.byref(n)))
+        out = np.zeros((n.value, 2), np.uint32)
+        if n.value:
+            check(self.lib.pe_world_get_candidate_pairs(self.h, _ptr(out), n.value, ctypes.byref(n)))
+        return out
+
+    def solve_order(self):
+        n = _u32()
+        check(self.lib.pe_world_get_solve_order(self.h, None, None, 0, ctypes.byref(n)))
+        order = np.zeros(n.value, np.uint32)
+        colors = np.zeros(n.value, np.uint32)
+        if n.value:
+            check(self.lib.pe_world_get_solve_order(self.h, _ptr(order), _ptr(colors), n.value, ctypes.byref(n)))
+        return order, colors
+
+    def solve(self, manifolds, dt):
+        m = np.ascontiguousarray(manifolds.copy())
+        check(self.lib.pe_world_solve(self.h, _ptr(m), len(m), float(dt)))
+        return m
+
+
+def broadphase(mins, maxs, algo=SAP, cell_size=0.0, device=0):
+    """BroadPhase::findCandidatePairs on the GPU; returns (pairs[n,2], stats)."""
+    l = lib()
+    mins, maxs = _f32(mins).reshape(-1, 3), _f32(maxs).reshape(-1, 3)
+    n = len(mins)
+    cnt = ctypes.c_uint64()
+    st = np.zeros(1, STATS_DTYPE)
+    check(l.pe_broadphase_find_pairs(int(device), _ptr(mins), _ptr(maxs), n, int(algo), float(cell_size), None, 0,
+                                     ctypes.byref(cnt), _ptr(st)))
+    pairs = np.zeros((cnt.value, 2), np.uint32)
+    if cnt.value:
+        check(l.pe_broadphase_find_pairs(int(device), _ptr(mins), _ptr(maxs), n, int(algo), float(cell_size),
+                                         _ptr(pairs), cnt.value, ctypes.byref(cnt), _ptr(st)))
+    return pairs, st[0]
+
+
+def generate_contact(shape_a, dims_a, pos_a, quat_a, shape_b, dims_b, pos_b, quat_b, device=0):
+    """NarrowPhase::generateContact on the GPU for one sphere/box pair (dims =
+    radius or half extents)."""
+    out = np.zeros(1, MANIFOLD_DTYPE)
+    hit = ctypes.c_int()
+    check(lib().pe_generate_contact(int(device), int(shape_a), _ptr(_f32(dims_a)), _ptr(_f32(pos_a)),
+                                    _ptr(_f32(quat_a)), int(shape_b), _ptr(_f32(dims_b)), _ptr(_f32(pos_b)),
+                                    _ptr(_f32(quat_b)), _ptr(out), ctypes.byref(hit)))
+    return bool(hit.value), out[0]

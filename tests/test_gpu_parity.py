@@ -1,0 +1,265 @@
+"""GPU parity: the CUDA path through the C ABI against the reference's golden
+fixtures and the oracle, bit for bit (integers and floats alike; the device
+code mirrors the reference's operation order with contraction off)."""
+import numpy as np
+import pytest
+
+from helpers import assert_bit_equal, assert_manifolds_equal, colors_valid
+from oracle import cpu
+from phys_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+WORLD_RUNS = ["spheres_floor_sap", "spheres_floor_grid", "mixed_volume_sap", "mixed_volume_grid", "pyramid_sap",
+              "boxes_plane_sap"]
+
+
+def scene_from(g):
+    n = len(g["shape"])
+    return scenes.Scene(g["shape"], g["is_static"], g["dims"], g["pos"], g["density"], g["restitution"],
+                        g["friction"], g["linvel"], g["spin"], np.full(n, -1, np.int32), np.zeros(n, np.float32),
+                        np.zeros((n, 3), np.float32))
+
+
+def compare_worlds(gw, ow, what, features=True):
+    gb, ob = gw.bodies(), ow.bodies()
+    for k in ("pos", "quat", "lin", "ang"):
+        assert_bit_equal(gb[k], ob[k], f"{what} {k}")
+    assert_bit_equal(gw.pairs(), ow.pairs(), f"{what} pairs")
+    assert_manifolds_equal(gw.contacts(), ow.contacts(), features=features, what=what)
+
+
+# ------------------------------------------------------------- broadphase ---
+@pytest.mark.parametrize("algo", [0, 1])
+def test_broadphase_golden(gpu, golden, algo):
+    g = golden("broadphase")
+    for k in range(int(g["count"])):
+        c = g[f"aabb_{k}"]
+        pairs, st = gpu.broadphase(c[:, 0], c[:, 1], algo)
+        assert_bit_equal(pairs, g[f"pairs_{k}_{algo}"], f"case {k} pairs")
+        got = np.array([st["x_window_comparisons"], st["aabb_pairs"], st["grid_comparisons"], st["grid_entries"],
+                        st["grid_overflow_aabbs"]], np.uint64)
+        assert np.array_equal(got, g[f"stats_{k}_{algo}"]), f"case {k}: {got} != {g[f'stats_{k}_{algo}']}"
+        assert st["grid_cell_size"] == g[f"cell_{k}_{algo}"]
+
+
+@pytest.mark.parametrize("algo", [0, 1])
+def test_broadphase_random_large(gpu, algo):
+    rng = np.random.default_rng(3)
+    for n in (5000, 40000):
+        c = rng.uniform(-60, 60, (n, 3)).astype(np.float32)
+        h = rng.uniform(0.05, 1.5, (n, 3)).astype(np.float32)
+        pairs, st = gpu.broadphase(c - h, c + h, algo)
+        ref, rst = cpu.broadphase("oracle", c - h, c + h, algo)
+        assert_bit_equal(pairs, ref, f"n={n}")
+        assert st["aabb_pairs"] == rst["aabb_pairs"] and st["x_window_comparisons"] == rst["x_window_comparisons"]
+        assert st["grid_comparisons"] == rst["grid_comparisons"] and st["grid_entries"] == rst["grid_entries"]
+
+
+def test_broadphase_fixed_cell_same_pairs(gpu):
+    rng = np.random.default_rng(4)
+    c = rng.uniform(-30, 30, (20000, 3)).astype(np.float32)
+    h = rng.uniform(0.1, 0.6, (20000, 3)).astype(np.float32)
+    base, _ = gpu.broadphase(c - h, c + h, 0)
+    for cell in (1.2, 2.5, 7.0):
+        pairs, st = gpu.broadphase(c - h, c + h, 1, cell)
+        assert_bit_equal(pairs, base, f"cell {cell}")
+        assert st["grid_cell_size"] == cell
+
+
+def test_broadphase_tree_rejected(gpu):
+    with pytest.raises(ValueError):
+        gpu.broadphase(np.zeros((2, 3)), np.ones((2, 3)), 2)
+
+
+# ------------------------------------------------------------ narrowphase ---
+def test_narrowphase_golden(gpu, golden):
+    g = golden("narrowphase")
+    for k in range(len(g["hits"])):
+        args = (g["shapes"][k, 0], g["dims"][k, 0], g["pos"][k, 0], g["quat"][k, 0], g["shapes"][k, 1],
+                g["dims"][k, 1], g["pos"][k, 1], g["quat"][k, 1])
+        hit, m = gpu.generate_contact(*args)
+        assert hit == bool(g["hits"][k]), f"case {k} hit"
+        if hit:
+            assert_manifolds_equal(np.array([m]), g["manifolds"][k:k + 1], features=False, what=f"case {k}")
+            ohit, om = cpu.generate_contact("oracle", *args)
+            assert_bit_equal(m["feature"], om["feature"], f"case {k} feature ids")
+
+
+# ------------------------------------------------------------------ world ---
+@pytest.mark.parametrize("run", WORLD_RUNS)
+def test_world_manifold_order_matches_reference(gpu, golden, run):
+    """In the reference's own manifold order the GPU step equals the reference
+    PhysicsWorld::step, bit for bit, over the whole run."""
+    g = golden(f"world_{run}")
+    w = gpu.GpuWorld(algo=int(g["algo"]), order=gpu.ORDER_MANIFOLD)
+    w.load_scene(scene_from(g))
+    counts = []
+    for _ in range(int(g["steps"])):
+        w.step(g["dt"])
+        counts.append(len(w.contacts()))
+    b = w.bodies()
+    for k in ("pos", "quat", "lin", "ang"):
+        assert_bit_equal(b[k], g[f"final_{k}"], f"{run} {k}")
+    assert_manifolds_equal(w.contacts(), g["contacts"], features=False, what=run)
+    assert np.array_equal(np.array(counts, np.uint32), g["contacts_per_step"])
+    assert_bit_equal(w.pairs(), g["last_pairs"], f"{run} pairs")
+    st, ref = w.stats(), g["stats"][0]
+    for f in ("possible_pairs", "candidate_pairs", "contact_count", "solved_contact_count", "x_window_comparisons",
+              "aabb_pairs", "grid_comparisons", "grid_entries", "grid_overflow_aabbs", "prepared_points",
+              "warm_start_comparisons", "warm_start_matches", "velocity_point_visits"):
+        assert st[f] == ref[f], f"{run} {f}: {st[f]} != {ref[f]}"
+
+
+@pytest.mark.parametrize("kind,n,algo,cell,iters,steps", [
+    (scenes.SPHERES_ON_FLOOR, 1000, 0, 0.0, 10, 60),
+    (scenes.MIXED_VOLUME, 6000, 1, 2.2, 10, 40),
+    (scenes.MIXED_VOLUME, 6000, 0, 0.0, 10, 20),
+    (scenes.PYRAMIDS_BOXES_ONLY, 2, 0, 0.0, 20, 40),
+    (scenes.BOXES_ON_PLANE, 64, 1, 0.0, 8, 60),
+])
+def test_world_color_order_matches_oracle_every_step(gpu, kind, n, algo, cell, iters, steps):
+    sc = scenes.generate(kind, n, 42)
+    gw = gpu.GpuWorld(algo=algo, cell_size=cell, iterations=iters, order=gpu.ORDER_COLOR)
+    ow = cpu.OracleWorld(algo=algo, cell_size=cell, iterations=iters, order_mode=1)
+    gw.load_scene(sc)
+    ow.load_scene(sc)
+    statics = sc.is_static.astype(bool)
+    for s in range(steps):
+        gw.step(1 / 60)
+        ow.step(1 / 60)
+        compare_worlds(gw, ow, f"step {s}")
+        order, colors = gw.solve_order()
+        oorder, ocolors = ow.solve_order()
+        assert np.array_equal(order, oorder) and np.array_equal(colors, ocolors), f"step {s} colour order"
+        assert colors_valid(gw.contacts(), colors, statics)
+    st, ost = gw.stats(), ow.stats()
+    for f in ("candidate_pairs", "contact_count", "prepared_points", "warm_start_matches", "np_candidates",
+              "np_contacts", "color_count"):
+        assert np.array_equal(st[f], ost[f]), f
+
+
+def test_world_hulls_match_oracle(gpu):
+    sc = scenes.generate(scenes.PYRAMIDS, 1, 9)
+    # lower the hulls onto the pyramid so they collide within the run
+    sc.pos[sc.shape == 2, 1] -= 20.0
+    gw = gpu.GpuWorld(iterations=20, order=gpu.ORDER_COLOR)
+    ow = cpu.OracleWorld(iterations=20, order_mode=1)
+    gw.load_scene(sc)
+    ow.load_scene(sc)
+    hull_contacts = 0
+    for s in range(120):
+        gw.step(1 / 60)
+        ow.step(1 / 60)
+        compare_worlds(gw, ow, f"step {s}")
+        hull_contacts += int(gw.stats()["np_contacts"][3])
+    assert hull_contacts > 0
+
+
+# ----------------------------------------------------------------- solver ---
+def test_solver_known_answers(gpu, golden):
+    g = golden("solver")
+    for name in ("offcenter", "restitution"):
+        w = gpu.GpuWorld(order=gpu.ORDER_MANIFOLD)
+        w.create_body(1, [2, 2, 2], [0, 0, 0], 1.0, 1, 0.0, 0.0)
+        h = w.create_body(1, [2, 2, 2], [0, 0, 0], 1.0, 0, float(g[f"{name}_rest"]), 0.0)
+        st = w.get_body(gpu.Handle(int(h[0]), int(h[1])))
+        st.linear_velocity[:] = [0.0, float(g[f"{name}_vel"]), 0.0]
+        w.set_body(gpu.Handle(int(h[0]), int(h[1])), st)
+        solved = w.solve(g[f"{name}_in"], 1 / 60)
+        b = w.bodies()
+        assert_manifolds_equal(solved, g[f"{name}_out"], features=False, what=name)
+        assert_bit_equal(b["lin"], g[f"{name}_lin"], name)
+        assert_bit_equal(b["ang"], g[f"{name}_ang"], name)
+
+
+def test_standalone_solve_matches_oracle_with_stale_handles(gpu):
+    sc = scenes.generate(scenes.PYRAMIDS_BOXES_ONLY, 1, 42)
+    gw = gpu.GpuWorld(order=gpu.ORDER_COLOR)
+    ow = cpu.OracleWorld(order_mode=1)
+    gw.load_scene(sc)
+    ow.load_scene(sc)
+    gw.step(1 / 60)
+    ow.step(1 / 60)
+    cs = ow.contacts().copy()
+    cs["normal_impulse"] = 0
+    stale = cs[:3].copy()
+    stale["body_b_generation"] += 1
+    mixed = np.concatenate([stale, cs])
+    order, _, _ = ow.color(mixed)
+    got = gw.solve(mixed, 1 / 60)
+    exp, est = ow.solve(mixed, 1 / 60, 8, order)
+    assert_manifolds_equal(got, exp, features=False)
+    for k in ("lin", "ang"):
+        assert_bit_equal(gw.bodies()[k], ow.bodies()[k], k)
+    assert gw.stats()["solved_contact_count"] == est["solved_contact_count"] == len(cs)
+
+
+# ------------------------------------------------------------- edge cases ---
+def test_empty_and_single_body_worlds(gpu):
+    w = gpu.GpuWorld()
+    w.step(1 / 60)
+    assert len(w.contacts()) == 0 and w.stats()["candidate_pairs"] == 0
+    h = w.create_body(0, [0.5, 0, 0], [0, 3, 0], 1.0, 0, 0.0, 0.5)
+    for _ in range(10):
+        w.step(1 / 60)
+    o = cpu.OracleWorld()
+    o.create_body(0, [0.5, 0, 0], [0, 3, 0], 1.0, 0, 0.0, 0.5)
+    for _ in range(10):
+        o.step(1 / 60)
+    assert_bit_equal(w.bodies()["pos"], o.bodies()["pos"], "free fall")
+    assert h[0] == 0
+
+
+def test_removal_slot_reuse_and_stale_handles(gpu):
+    sc = scenes.generate(scenes.SPHERES_ON_FLOOR, 120, 5)
+    gw, ow = gpu.GpuWorld(order=gpu.ORDER_COLOR), cpu.OracleWorld(order_mode=1)
+    hg, ho = gw.load_scene(sc), ow.load_scene(sc)
+    assert np.array_equal(hg, ho)
+    for s in range(40):
+        gw.step(1 / 60)
+        ow.step(1 / 60)
+        if s == 10:
+            for i in (5, 17, 60):
+                gw.remove_body(hg[i, 0], hg[i, 1])
+                ow.remove_body(ho[i, 0], ho[i, 1])
+        if s == 20:
+            a = gw.create_body(1, [0.6, 0.6, 0.6], [0.5, 4.0, 0.2], 1.0, 0, 0.0, 0.5)
+            b = ow.create_body(1, [0.6, 0.6, 0.6], [0.5, 4.0, 0.2], 1.0, 0, 0.0, 0.5)
+            assert np.array_equal(a, b) and a[1] == 1  # reused slot, bumped generation
+        compare_worlds(gw, ow, f"step {s}")
+    with pytest.raises(LookupError):
+        gw.get_body(gpu.Handle(int(hg[5, 0]), int(hg[5, 1])))
+
+
+def test_invalid_arguments_and_unsupported(gpu):
+    w = gpu.GpuWorld()
+    with pytest.raises(ValueError):
+        w.create_body(0, [0.001, 0, 0], [0, 0, 0], 1.0, 0, 0, 0)  # Sphere is too small
+    with pytest.raises(ValueError):
+        w.create_body(1, [1, 1, 1], [0, 0, 0], 50.0, 0, 0, 0)  # Density is out of range
+    with pytest.raises(ValueError):
+        w.create_body(1, [100, 100, 1], [0, 0, 0], 1.0, 1, 0, 0)  # Box is too large
+    w.set_broadphase(gpu.TREE)
+    w.create_body(0, [0.5, 0, 0], [0, 0, 0], 1.0, 0, 0, 0)
+    with pytest.raises(NotImplementedError):
+        w.step(1 / 60)
+    with pytest.raises(ValueError):
+        gpu.check(w.lib.pe_world_set_worker_counts(w.h, 0, 1, 1))
+
+
+def test_pair_buffer_growth(gpu):
+    """A dense pile overflows the initial pair capacity; the step is re-run
+    from the untouched state with larger buffers and still matches."""
+    n = 9000
+    rng = np.random.default_rng(1)
+    sc = scenes.generate(scenes.SPHERES_ON_FLOOR, n, 2)
+    sc.pos[1:] = rng.uniform(-5, 5, (n, 3)).astype(np.float32) + np.float32([0, 6, 0])
+    gw, ow = gpu.GpuWorld(order=gpu.ORDER_COLOR), cpu.OracleWorld(order_mode=1)
+    gw.load_scene(sc)
+    ow.load_scene(sc)
+    for s in range(3):
+        gw.step(1 / 60)
+        ow.step(1 / 60)
+        compare_worlds(gw, ow, f"step {s}")
+    assert gw.stats()["candidate_pairs"] > 65536

@@ -1,0 +1,205 @@
+"""CPU tests of the oracle (the checker): pinned to the reference's golden
+fixtures everywhere, and to the live reference where its sources are present."""
+import numpy as np
+import pytest
+
+from helpers import assert_bit_equal, assert_manifolds_equal, colors_valid
+from oracle import cpu
+from phys_gb300 import scenes
+
+WORLD_RUNS = ["spheres_floor_sap", "spheres_floor_grid", "mixed_volume_sap", "mixed_volume_grid", "pyramid_sap",
+              "boxes_plane_sap"]
+
+
+def scene_from(g):
+    n = len(g["shape"])
+    return scenes.Scene(g["shape"], g["is_static"], g["dims"], g["pos"], g["density"], g["restitution"],
+                        g["friction"], g["linvel"], g["spin"], np.full(n, -1, np.int32), np.zeros(n, np.float32),
+                        np.zeros((n, 3), np.float32))
+
+
+@pytest.mark.parametrize("algo", [0, 1])
+def test_broadphase_golden(golden, algo):
+    g = golden("broadphase")
+    for k in range(int(g["count"])):
+        c = g[f"aabb_{k}"]
+        pairs, st = cpu.broadphase("oracle", c[:, 0], c[:, 1], algo)
+        assert_bit_equal(pairs, g[f"pairs_{k}_{algo}"], f"case {k} pairs")
+        got = np.array([st["x_window_comparisons"], st["aabb_pairs"], st["grid_comparisons"], st["grid_entries"],
+                        st["grid_overflow_aabbs"]], np.uint64)
+        assert np.array_equal(got, g[f"stats_{k}_{algo}"]), f"case {k} counters {got} != {g[f'stats_{k}_{algo}']}"
+        assert st["grid_cell_size"] == g[f"cell_{k}_{algo}"]
+
+
+def test_narrowphase_golden(golden):
+    g = golden("narrowphase")
+    for k in range(len(g["hits"])):
+        hit, m = cpu.generate_contact("oracle", g["shapes"][k, 0], g["dims"][k, 0], g["pos"][k, 0], g["quat"][k, 0],
+                                      g["shapes"][k, 1], g["dims"][k, 1], g["pos"][k, 1], g["quat"][k, 1])
+        assert hit == bool(g["hits"][k]), f"case {k} hit"
+        if hit:
+            assert_manifolds_equal(np.array([m]), g["manifolds"][k:k + 1], features=False, what=f"case {k}")
+
+
+def test_narrowphase_known_answers(golden):
+    """Values stated by the reference's narrowphase tests (tol 1e-5)."""
+    g = golden("narrowphase")
+    m = g["manifolds"]
+    np.testing.assert_allclose(m[0]["anchor_a"][0], [0.75, 0, 0], atol=1e-5)
+    np.testing.assert_allclose(m[0]["anchor_b"][0], [-0.75, 0, 0], atol=1e-5)
+    np.testing.assert_allclose(m[1]["anchor_a"][0], [0.75, 0, 0], atol=1e-5)
+    np.testing.assert_allclose(m[1]["anchor_b"][0], [0, -0.75, 0], atol=1e-5)
+    assert abs(np.linalg.norm(m[2]["normal"]) - 1.0) <= 1e-5
+    for k, sign in ((3, 1), (4, -1), (5, 1), (6, -1)):
+        np.testing.assert_allclose(m[k]["normal"], [0, sign, 0], atol=1e-5)
+
+
+def test_solver_known_answers(golden):
+    g = golden("solver")
+    dt = np.float32(1.0 / 60.0)
+    for name, lin_y, ang_z in (("offcenter", -0.6, 0.6), ("restitution", 1.0, 0.0)):
+        w = cpu.OracleWorld()
+        w.create_body(1, [2, 2, 2], [0, 0, 0], 1.0, 1, 0.0, 0.0)
+        w.create_body(1, [2, 2, 2], [0, 0, 0], 1.0, 0, float(g[f"{name}_rest"]), 0.0)
+        w.set_velocity(1, [0, float(g[f"{name}_vel"]), 0], None)
+        solved, _ = w.solve(g[f"{name}_in"], dt)
+        b = w.bodies()
+        assert_manifolds_equal(solved, g[f"{name}_out"], features=False, what=name)
+        assert_bit_equal(b["lin"], g[f"{name}_lin"], name)
+        assert_bit_equal(b["ang"], g[f"{name}_ang"], name)
+        assert abs(b["lin"][1, 1] - lin_y) <= 1e-5 and abs(b["ang"][1, 2] - ang_z) <= 1e-5
+
+
+@pytest.mark.parametrize("run", WORLD_RUNS)
+def test_world_golden(golden, run):
+    g = golden(f"world_{run}")
+    w = cpu.OracleWorld(algo=int(g["algo"]))
+    w.load_scene(scene_from(g))
+    counts = []
+    for _ in range(int(g["steps"])):
+        w.step(g["dt"])
+        counts.append(len(w.contacts()))
+    b = w.bodies()
+    for k in ("pos", "quat", "lin", "ang"):
+        assert_bit_equal(b[k], g[f"final_{k}"], f"{run} {k}")
+    assert_manifolds_equal(w.contacts(), g["contacts"], features=False, what=run)
+    assert np.array_equal(np.array(counts, np.uint32), g["contacts_per_step"])
+    assert_bit_equal(w.pairs(), g["last_pairs"], f"{run} pairs")
+    st, ref = w.stats(), g["stats"][0]
+    for f in ("possible_pairs", "candidate_pairs", "contact_count", "solved_contact_count", "x_window_comparisons",
+              "aabb_pairs", "grid_comparisons", "grid_entries", "grid_overflow_aabbs", "prepared_points",
+              "warm_start_comparisons", "warm_start_matches", "velocity_point_visits"):
+        assert st[f] == ref[f], f"{run} {f}: {st[f]} != {ref[f]}"
+
+
+def test_color_order_is_valid_and_greedy():
+    sc = scenes.generate(scenes.PYRAMIDS_BOXES_ONLY, 1, 42)
+    w = cpu.OracleWorld(order_mode=1)
+    w.load_scene(sc)
+    for _ in range(3):
+        w.step(1 / 60)
+    cs = w.contacts()
+    order, colors = w.solve_order()
+    assert colors_valid(cs, colors, sc.is_static.astype(bool))
+    assert sorted(order.tolist()) == list(range(len(cs)))
+    assert np.all(np.diff(colors[order].astype(np.int64)) >= 0)
+    # stable within a colour
+    for c in np.unique(colors):
+        idx = order[colors[order] == c]
+        assert np.all(np.diff(idx.astype(np.int64)) > 0)
+
+
+def test_color_order_equals_permuted_manifold_order():
+    """Solving in colour order is the reference solve fed the permuted list."""
+    sc = scenes.generate(scenes.PYRAMIDS_BOXES_ONLY, 1, 42)
+    w = cpu.OracleWorld(order_mode=0)
+    w.load_scene(sc)
+    w.step(1 / 60)
+    cs = w.contacts()
+    a, b = w.clone(), w.clone()
+    order, _, _ = a.color(cs)
+    sa, _ = a.solve(cs, 1 / 60, 8, order)
+    sb, _ = b.solve(cs[order], 1 / 60, 8, None)
+    assert_manifolds_equal(sa[order], sb, features=False)
+    for k in ("lin", "ang"):
+        assert_bit_equal(a.bodies()[k], b.bodies()[k], k)
+
+
+def test_iterations_parameter_changes_result():
+    sc = scenes.generate(scenes.PYRAMIDS_BOXES_ONLY, 1, 42)
+    res = []
+    for it in (8, 10, 20):
+        w = cpu.OracleWorld(iterations=it)
+        w.load_scene(sc)
+        for _ in range(5):
+            w.step(1 / 60)
+        res.append(w.bodies()["lin"])
+    assert not np.array_equal(res[0], res[1]) and not np.array_equal(res[1], res[2])
+
+
+def test_fp64_instance_tracks_fp32():
+    sc = scenes.generate(scenes.BOXES_ON_PLANE, 16, 3)
+    w32, w64 = cpu.OracleWorld(), cpu.OracleWorld(fp64=True)
+    w32.load_scene(sc)
+    w64.load_scene(sc)
+    for _ in range(30):
+        w32.step(1 / 120)
+        w64.step(1 / 120)
+    np.testing.assert_allclose(w64.bodies_f64()["pos"], w32.bodies()["pos"], atol=1e-3)
+
+
+# ---------------------------------------------------------------- live reference
+needs_ref = pytest.mark.skipif(not cpu.reference_available(), reason="reference sources not present")
+
+
+@needs_ref
+@pytest.mark.parametrize("kind,n,algo,steps", [(scenes.SPHERES_ON_FLOOR, 300, 0, 150),
+                                                (scenes.MIXED_VOLUME, 2500, 1, 40),
+                                                (scenes.PYRAMIDS_BOXES_ONLY, 1, 0, 80),
+                                                (scenes.BOXES_ON_PLANE, 64, 1, 60)])
+def test_oracle_matches_reference_every_step(kind, n, algo, steps):
+    sc = scenes.generate(kind, n, 11)
+    ref, ow = cpu.RefWorld(algo=algo), cpu.OracleWorld(algo=algo)
+    ref.load_scene(sc)
+    ow.load_scene(sc)
+    for s in range(steps):
+        ref.step(1 / 60)
+        ow.step(1 / 60)
+        rb, ob = ref.bodies(), ow.bodies()
+        for k in rb:
+            assert_bit_equal(ob[k], rb[k], f"step {s} {k}")
+        assert_manifolds_equal(ow.contacts(), ref.contacts(), features=False, what=f"step {s}")
+
+
+@needs_ref
+def test_oracle_solve_matches_reference_in_color_order():
+    sc = scenes.generate(scenes.PYRAMIDS_BOXES_ONLY, 1, 42)
+    ref, ow = cpu.RefWorld(), cpu.OracleWorld()
+    ref.load_scene(sc)
+    ow.load_scene(sc)
+    ref.step(1 / 60)
+    ow.step(1 / 60)
+    cs = ow.contacts()
+    order, _, _ = ow.color(cs)
+    rs, _ = ref.solve(cs, 1 / 60, order)
+    os_, _ = ow.solve(cs, 1 / 60, 8, order)
+    assert_manifolds_equal(os_, rs, features=False)
+    for k in ("lin", "ang"):
+        assert_bit_equal(ow.bodies()[k], ref.bodies()[k], k)
+
+
+@needs_ref
+def test_gjk_epa_matches_reference():
+    rng = np.random.default_rng(5)
+    agree = 0
+    for _ in range(300):
+        a = rng.normal(size=(24, 3)).astype(np.float32) * rng.uniform(0.3, 0.8, 3).astype(np.float32)
+        b = (rng.normal(size=(24, 3)) * rng.uniform(0.3, 0.8, 3) + rng.uniform(-1.2, 1.2, 3)).astype(np.float32)
+        r = cpu.gjk_epa("ref", a, b)
+        o = cpu.gjk_epa("oracle", a, b)
+        assert r[0] == o[0] and r[3] == o[3]
+        if r[0] == 1:
+            assert_bit_equal(o[1], r[1], "epa normal")
+            assert np.float32(o[2]) == np.float32(r[2])
+        agree += 1
+    assert agree == 300
