@@ -1,0 +1,336 @@
+"""Benchmark: body-steps/s of the GPU collision-and-contact step on the 100k
+mixed-body workload (50% spheres r~U[0.2,0.6], 50% oriented boxes with half
+extents U[0.2,0.6], positions uniform in 200x100x200 m without overlap,
+velocities N(0,1), dt = 1/60, 10 solver iterations, uniform-grid broadphase
+with cell = 2x the largest collider extent).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line (rank 0).  `value` is device-timed: CUDA events on the
+world's own stream around each step, L2 flushed before every timed step.  `e2e`
+is the same metric through the C ABI with host buffers: every step writes the
+per-body forces from pinned host memory, steps, and reads all poses back.  The
+CPU baseline is the oracle port (the reference algorithm restated) timed on the
+host cores for a bounded sample of the same workload.  With N > 1 (torchrun)
+each rank steps an independent replica of the world ("replicas only": a single
+world does not shard) and `value` aggregates all ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = pathlib.Path(__file__).resolve().parent
+for _p in (REPO, REPO / "phys-engine_gb300"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+METRIC = "body-steps/s at 100k mixed bodies"
+UNIT = "body-steps/s"
+BODIES = 100_000
+DT = 1.0 / 60.0
+ITERATIONS = 10
+SEED = 42
+
+
+def workload_scene():
+    from phys_gb300 import scenes
+
+    return scenes.generate(scenes.MIXED_VOLUME, BODIES, SEED)
+
+
+def cell_size(scene):
+    """2 x the largest collider extent (sphere radius, box half diagonal)."""
+    sph = scene.shape == 0
+    ext = np.where(sph, scene.dims[:, 0], np.linalg.norm(scene.dims * 0.5, axis=1))
+    return float(2.0 * ext.max())
+
+
+def workload_config(scene, order):
+    return {
+        "workload": "mixed_100k",
+        "bodies": scene.count,
+        "shapes": "50% spheres r~U[0.2,0.6], 50% boxes half-extents~U[0.2,0.6]^3, uniform random orientation",
+        "volume_m": [200, 100, 200],
+        "velocity": "N(0,1) m/s",
+        "density_g_cm3": 1.0,
+        "broadphase": "uniform grid",
+        "grid_cell_m": round(cell_size(scene), 6),
+        "solver_iterations": ITERATIONS,
+        "solver_order": order,
+        "dt": DT,
+        "steps_of_reference_run": 600,
+        "l2": "flushed before every timed step (512 MiB write)",
+    }
+
+
+# ----------------------------------------------------------------- helpers
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def stage_bytes(stats, bodies, iterations):
+    """Algorithmic bytes per step by stage (minimum each stage must move, SoA
+    FP32; sort and scratch traffic excluded)."""
+    P = int(stats["candidate_pairs"])
+    M = int(stats["contact_count"])
+    K = int(stats["contact_points"])
+    I = iterations
+    return {
+        "integrate": 92 * bodies,                  # velocity + AABB: read 56, write 36
+        "broadphase": 24 * bodies + 8 * P,         # AABB read, pair write
+        "narrowphase": 112 * P + 32 * M + 32 * K,  # pair + two bodies' pose/shape/material; manifold writes
+        "solver": (32 + 112 + 48 + 96 * I) * M + (32 + 36 + 152 + 36 + 176 * I) * K,
+        "pose": 80 * bodies,                       # read 52, write 28
+    }
+
+
+# ------------------------------------------------------------ CPU legs
+def cpu_port_rate(scene, budget_s: float, max_steps: int, threads: int):
+    """Oracle port (reference algorithm, reference order) on the host cores."""
+    from oracle import cpu
+
+    w = cpu.OracleWorld(algo=1, iterations=ITERATIONS, order_mode=0, threads=threads)
+    t0 = time.perf_counter()
+    w.load_scene(scene)
+    load_s = time.perf_counter() - t0
+    w.step(DT)  # warm-up
+    steps, t0 = 0, time.perf_counter()
+    while steps < max_steps:
+        w.step(DT)
+        steps += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return scene.count * steps / el, steps, el, load_s
+
+
+def run_reference(args, rank, world_size):
+    if rank != 0:
+        return
+    from oracle import cpu
+
+    cpu.build_oracle()
+    scene = workload_scene()
+    threads = os.cpu_count() or 1
+    budget = 150.0
+    rate, steps, el, _ = cpu_port_rate(scene, budget, max(args.steps, 1), threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world_size,
+        "steps": steps, "warmup": 1, "ms_per_step": 1000.0 * el / max(steps, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": f"synthetic (scene generator, seed {SEED})",
+        "config": workload_config(scene, "manifold order (the reference's)"),
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{steps} consecutive steps (after 1 warm-up step) of the full 100k-body world; "
+                                   f"the reference's own build is not available on this host, so the oracle "
+                                   f"restatement of its algorithm (bit-identical to it) is timed"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------- GPU leg
+def run_gpu(args, rank, world_size, local_rank):
+    import torch
+
+    from phys_gb300 import engine
+
+    torch.cuda.set_device(local_rank)
+    scene = workload_scene()
+    w = engine.GpuWorld(device=local_rank, algo=engine.GRID, cell_size=cell_size(scene), iterations=ITERATIONS,
+                        order=engine.ORDER_COLOR)
+    w.load_scene(scene)
+    stream = torch.cuda.ExternalStream(w.stream(), device=torch.device("cuda", local_rank))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
+
+    for _ in range(args.warmup):
+        w.step(DT)
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    acc = {"integrate_ms": 0.0, "broadphase_ms": 0.0, "narrowphase_ms": 0.0, "solver_ms": 0.0, "pose_ms": 0.0}
+    stage_b = {k: 0 for k in ("integrate", "broadphase", "narrowphase", "solver", "pose")}
+    launches = 0
+    totals = {"pairs": 0, "manifolds": 0, "points": 0}
+    if world_size > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clocks:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.add_(1.0)
+            starts[k].record(stream)
+            w.step(DT)
+            ends[k].record(stream)
+            st = w.stats()
+            for key in acc:
+                acc[key] += float(st[key])
+            for key, v in stage_bytes(st, scene.count, ITERATIONS).items():
+                stage_b[key] += v
+            launches += int(st["kernel_launches"])
+            totals["pairs"] += int(st["candidate_pairs"])
+            totals["manifolds"] += int(st["contact_count"])
+            totals["points"] += int(st["contact_points"])
+        torch.cuda.synchronize()
+    elapsed_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    t = torch.tensor([elapsed_ms], dtype=torch.float64, device=f"cuda:{local_rank}")
+    if world_size > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    max_ms = float(t.item())
+    value = world_size * scene.count * args.steps / (max_ms / 1000.0)
+
+    # e2e: forces in from pinned host memory, step, poses out, every step
+    forces = torch.zeros((scene.count, 3), dtype=torch.float32).pin_memory().numpy()
+    poses_p = torch.empty((scene.count, 3), dtype=torch.float32).pin_memory().numpy()
+    poses_q = torch.empty((scene.count, 4), dtype=torch.float32).pin_memory().numpy()
+    e2e_steps = max(1, min(args.steps, 200))
+    e2e_s = 0.0
+    for k in range(e2e_steps):
+        with torch.cuda.stream(stream):
+            flush.add_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        w.write_forces(forces)
+        w.step(DT)
+        w.read_poses(poses_p, poses_q)
+        e2e_s += time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{local_rank}")
+    if world_size > 1:
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = world_size * scene.count * e2e_steps / float(te.item())
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    stage_ms = {k[:-3]: v for k, v in acc.items()}
+    dominant = max(stage_ms, key=stage_ms.get)
+    achieved = stage_b[dominant] / (stage_ms[dominant] / 1000.0) / 1e9 if stage_ms[dominant] > 0 else 0.0
+    step_bytes = sum(stage_b.values())
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": f"synthetic (scene generator, seed {SEED})",
+        "config": workload_config(scene, "graph colour"),
+        "roofline": {
+            "bound": "hbm", "stage": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": None,
+            "algorithmic_bytes_per_step": stage_b[dominant] / args.steps,
+            "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()},
+            "whole_step": {"algorithmic_bytes_per_step": step_bytes / args.steps,
+                           "achieved_gbs": step_bytes / (max_ms / 1000.0) / 1e9 / world_size,
+                           "frac": step_bytes / (max_ms / 1000.0) / 1e9 / world_size / peak},
+        },
+        "workload_per_step": {k: v / args.steps for k, v in totals.items()},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 16 * scene.count,
+                "d2h_bytes_per_step": 32 * scene.count, "steps": e2e_steps},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+    }
+    if world_size == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, steps, el, _ = cpu_port_rate(scene, 20.0, 60, threads)
+        line["cpu_baseline"] = {
+            "value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} steps (after 1 warm-up step) of the same 100k-body world, {el:.1f} s; oracle "
+                      f"restatement of the reference algorithm (reference order, grid, {ITERATIONS} iterations)"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=600)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+
+    world_size = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world_size)
+        return
+    if world_size > 1:
+        import torch
+
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    try:
+        run_gpu(args, rank, world_size, local_rank)
+    finally:
+        if world_size > 1:
+            import torch
+
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -109,6 +109,14 @@ typedef struct pe_step_stats {
     uint64_t epa_failures;
     uint64_t contact_points;
     double total_ms; /* device time of the step */
+    /* device time per stage, the GPU counterpart of StepStats::integrateVelocityMs,
+       broadPhaseMs, narrowPhaseMs, solverMs, integratePoseMs */
+    double integrate_ms;
+    double broadphase_ms;
+    double narrowphase_ms;
+    double solver_ms;
+    double pose_ms;
+    uint64_t kernel_launches; /* engine kernels launched by the step */
 } pe_step_stats;
 
 typedef struct pe_world pe_world;
@@ -184,6 +192,17 @@ pe_status pe_world_body_integrate_rotation(pe_world *world, pe_handle body, floa
 uint32_t pe_world_body_slot_count(pe_world *world);
 pe_status pe_world_read_bodies(pe_world *world, float *positions, float *rotations, float *linear,
                                float *angular);
+
+/* Per-step host I/O without the host mirror (no reference counterpart; the
+   reference's equivalents are RigidBody::applyForce and getPosition/getRotation
+   per body): set the accumulated force of body slots [0, n) from xyz triples
+   (static bodies ignore it, like applyForce), and copy all current positions
+   (xyz) / rotations (xyzw) out.  Either output pointer may be NULL. */
+pe_status pe_world_write_forces(pe_world *world, const float *forces, uint32_t n);
+pe_status pe_world_read_poses(pe_world *world, float *positions, float *rotations);
+/* The CUDA stream (cudaStream_t) the world's kernels run on, for event timing
+   by the caller. */
+pe_status pe_world_get_stream(pe_world *world, void **stream);
 
 /* PhysicsWorld::step (physics_world.hpp:75) */
 pe_status pe_world_step(pe_world *world, float dt);

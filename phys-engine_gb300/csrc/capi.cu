@@ -73,6 +73,12 @@ void fillStats(const pe::StepCounters &c, pe_step_stats *o) {
     o->epa_failures = c.epaFailures;
     o->contact_points = c.points;
     o->total_ms = c.gpuMs;
+    o->integrate_ms = c.integrateMs;
+    o->broadphase_ms = c.broadphaseMs;
+    o->narrowphase_ms = c.narrowphaseMs;
+    o->solver_ms = c.solverMs;
+    o->pose_ms = c.poseMs;
+    o->kernel_launches = c.kernelLaunches;
 }
 
 // RigidBody::createSphere / createBox validation and mass properties
@@ -443,6 +449,28 @@ pe_status pe_world_read_bodies(pe_world *world, float *pos, float *rot, float *l
         }
         return PE_OK;
     });
+}
+
+pe_status pe_world_write_forces(pe_world *world, const float *forces, uint32_t n) {
+    if (!world || (n && !forces)) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        world->w->writeForces(forces, n);
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_read_poses(pe_world *world, float *positions, float *rotations) {
+    if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
+    return guarded([&] {
+        world->w->readPoses(positions, rotations);
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_get_stream(pe_world *world, void **stream) {
+    if (!world || !stream) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    *stream = (void *)world->w->stream();
+    return PE_OK;
 }
 
 pe_status pe_world_step(pe_world *world, float dt) {

@@ -132,7 +132,7 @@ void launchIntegrateAabb(const WorldView &w, uint32_t *sapKeys, uint32_t *sapVal
     uint32_t n = w.nb > w.nc ? w.nb : w.nc;
     if (!n) return;
     k_integrate_aabb<<<(n + 255) / 256, 256, 0, s>>>(w, sapKeys, sapVals);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
 }
 
 void launchCollect(const WorldView &w, uint32_t *flags, uint32_t *pos, float4 *inMin, float4 *inMax, uint32_t *inSlot,
@@ -140,16 +140,16 @@ void launchCollect(const WorldView &w, uint32_t *flags, uint32_t *pos, float4 *i
                    cudaStream_t s) {
     if (!w.nc) return;
     k_collect_flags<<<(w.nc + 255) / 256, 256, 0, s>>>(w, flags);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
     launchScanExclusive(flags, pos, nullptr, w.nc, d_count, ws, d_err, s);
     k_collect_scatter<<<(w.nc + 255) / 256, 256, 0, s>>>(w, flags, pos, inMin, inMax, inSlot, sapKeys, sapVals);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
 }
 
 void launchIntegratePose(const WorldView &w, cudaStream_t s) {
     if (!w.nb) return;
     k_integrate_pose<<<(w.nb + 255) / 256, 256, 0, s>>>(w);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
 }
 
 } // namespace pe

@@ -291,13 +291,13 @@ static inline int gridFor(uint32_t n, int threads = 256, int maxBlocks = 152 * 8
 
 void launchStepInit(DevStats *st, uint32_t inputCount, cudaStream_t s) {
     k_step_init<<<1, 32, 0, s>>>(st, inputCount);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
 }
 
 __global__ void k_set_manifolds(DevStats *st, uint32_t count) { st->manifolds = count; }
 void launchSetManifoldCount(DevStats *st, uint32_t count, cudaStream_t s) {
     k_set_manifolds<<<1, 1, 0, s>>>(st, count);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
 }
 
 __global__ void k_sap_keys(BroadInput in, uint32_t *keys, uint32_t *vals) {
@@ -310,7 +310,7 @@ __global__ void k_sap_keys(BroadInput in, uint32_t *keys, uint32_t *vals) {
 
 void launchSapKeys(const BroadInput &in, uint32_t *keys, uint32_t *vals, cudaStream_t s) {
     k_sap_keys<<<gridFor(in.maxN), 256, 0, s>>>(in, keys, vals);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
 }
 
 void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, BroadBuffers &bb, PairBuffers &pb,
@@ -318,11 +318,12 @@ void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, Broad
     uint32_t *err = &st->err;
     launchRadixSort<uint32_t>(sapKeys, bb.keyTmp32, sapVals, bb.valTmp, in.d_n, in.maxN, 0, 32, ws, err, s);
     k_sap_gather<<<gridFor(in.maxN), 256, 0, s>>>(in, sapVals, bb.sMinX, bb.sMaxX, bb.sYZ, bb.sIdx);
+    PE_LAUNCHED();
     k_sap_window<<<gridFor(in.maxN), 256, 0, s>>>(in.d_n, bb.sMinX, bb.sMaxX, bb.len, st);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
     launchScanExclusive(bb.len, bb.off, in.d_n, in.maxN, &st->windowWork, ws, err, s);
     k_sap_emit<<<152 * 8, 256, 0, s>>>(in.d_n, bb.off, bb.len, bb.sYZ, bb.sIdx, pb.keys, pb.cap, st);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
 }
 
 void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBuffers &pb, DevStats *st, Scratch &ws,
@@ -330,38 +331,39 @@ void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBu
     uint32_t *err = &st->err;
     if (fixedCell <= 0.0) {
         k_grid_widths<<<gridFor(in.maxN), 256, 0, s>>>(in, bb.widthKeys, &bb.counters[0]);
-        PE_CHECK(cudaGetLastError());
+        PE_LAUNCHED();
         launchRadixSort<unsigned long long>(bb.widthKeys, bb.widthTmp, nullptr, nullptr, in.d_n, in.maxN, 0, 64, ws,
                                             err, s);
     }
     k_grid_cellsize<<<1, 1, 0, s>>>(bb.widthKeys, &bb.counters[0], fixedCell, st);
+    PE_LAUNCHED();
     k_grid_range<<<gridFor(in.maxN), 256, 0, s>>>(in, st, bb.firstCell, bb.cellCount, bb.inGrid, bb.overflow);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
     launchScanExclusive(bb.cellCount, bb.entryOff, in.d_n, in.maxN, &st->gridEntryCount, ws, err, s);
     k_grid_entries<<<gridFor(in.maxN), 256, 0, s>>>(in, bb.firstCell, bb.inGrid, bb.entryOff, bb.entryKeys,
                                                     bb.entryVals, bb.entryCap, st);
+    PE_LAUNCHED();
     launchClamp(&st->gridEntryCount, bb.entryCap, &bb.counters[1], s);
-    PE_CHECK(cudaGetLastError());
     launchRadixSort<unsigned long long>(bb.entryKeys, bb.entryKeysTmp, bb.entryVals, bb.entryValsTmp,
                                         &bb.counters[1], bb.entryCap, 0, 64, ws, err, s);
     k_grid_cell_pairs<<<gridFor(bb.entryCap), 256, 0, s>>>(&bb.counters[1], bb.entryKeys, bb.entryVals, in, pb.keys,
                                                            pb.cap, st);
+    PE_LAUNCHED();
     k_grid_overflow_pairs<<<152 * 4, 256, 0, s>>>(in, bb.overflow, bb.inGrid, pb.keys, pb.cap, st);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
 }
 
 void launchPairsFinalize(const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen, PairBuffers &pb,
                          DevStats *st, Scratch &ws, cudaStream_t s) {
     uint32_t *err = &st->err;
     launchClamp(&st->rawPairs, pb.cap, &pb.counters[0], s);
-    PE_CHECK(cudaGetLastError());
     launchRadixSort<unsigned long long>(pb.keys, pb.keysTmp, nullptr, nullptr, &pb.counters[0], pb.cap, 0, 64, ws,
                                         err, s);
     k_pairs_flags<<<gridFor(pb.cap), 256, 0, s>>>(&pb.counters[0], pb.keys, inSlot, cbody, cbgen, pb.flags, st);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
     launchScanExclusive(pb.flags, pb.pos, &pb.counters[0], pb.cap, &st->pairs, ws, err, s);
     k_pairs_scatter<<<gridFor(pb.cap), 256, 0, s>>>(&pb.counters[0], pb.keys, inSlot, pb.flags, pb.pos, pb.a, pb.b);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
 }
 
 } // namespace pe

@@ -135,7 +135,7 @@ void launchNarrowphase(const WorldView &w, const PairBuffers &pb, const Manifold
     PE_CHECK(cudaMemsetAsync(ws.scanState, 0, sizeof(unsigned long long) * tiles + 8, s));
     k_narrowphase<<<tiles, kNarrowThreads, 0, s>>>(w, pb.a, pb.b, &st->pairs, mv, mcap, st, ws.scanState,
                                                     (uint32_t *)(ws.scanState + tiles));
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
 }
 
 } // namespace pe
@@ -185,7 +185,7 @@ __global__ void k_generate_pairs(const float4 *in, float4 *out, uint32_t n) {
 void launchGeneratePairs(const float4 *in, float4 *out, uint32_t n, cudaStream_t s) {
     if (!n) return;
     k_generate_pairs<<<(n + 127) / 128, 128, 0, s>>>(in, out, n);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
 }
 
 } // namespace pe

@@ -533,6 +533,7 @@ static void launchCooperative(const void *fn, int blocks, SolveArgs &args, cudaS
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     PE_CHECK(cudaLaunchKernelExC(&cfg, fn, params));
+    ++g_kernelLaunches;
 }
 
 int maxCooperativeBlocks(int smCount) {
@@ -558,28 +559,31 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
     const bool serial = orderMode == 0;
     if (!serial) launchCooperative((const void *)k_color, coopBlocks, a, s);
     k_order_init<<<gridFor(mcap), 256, 0, s>>>(a, serial ? 1 : 0);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
     if (!serial) {
         launchClamp(&st->manifolds, mcap, &sb.counters[1], s);
         launchRadixSort<uint32_t>(sb.orderKeys, sb.orderKeysTmp, sb.order, sb.orderTmp, &sb.counters[1], mcap, 0, 8,
                                   ws, err, s);
     }
     k_prepare<<<gridFor(mcap), 256, 0, s>>>(a);
-    PE_CHECK(cudaGetLastError());
-    if (serial) k_solve_serial<<<1, 32, 0, s>>>(a);
+    PE_LAUNCHED();
+    if (serial) {
+        k_solve_serial<<<1, 32, 0, s>>>(a);
+        PE_LAUNCHED();
+    }
     else launchCooperative((const void *)k_solve_colored, coopBlocks, a, s);
-    PE_CHECK(cudaGetLastError());
     k_impulses_out<<<gridFor(mcap), 256, 0, s>>>(a);
+    PE_LAUNCHED();
     k_cache_keys<<<gridFor(mcap), 256, 0, s>>>(a);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
     launchClamp(&st->manifolds, mcap, &sb.counters[1], s);
     launchRadixSort<unsigned long long>(sb.cacheKeys, sb.cacheKeysTmp, sb.cacheVals, sb.cacheValsTmp,
                                         &sb.counters[1], mcap, 0, 64, ws, err, s);
     k_cache_counts<<<gridFor(mcap), 256, 0, s>>>(a);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
     launchScanExclusive(sb.cacheCounts, sb.cacheOff, &sb.counters[1], mcap, newCacheCount, ws, err, s);
     k_cache_write<<<gridFor(mcap), 256, 0, s>>>(a, newCache, cacheCap);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
 }
 
 } // namespace pe

@@ -20,6 +20,15 @@ struct CudaError : std::runtime_error {
             throw ::pe::CudaError(std::string(#expr) + ": " + cudaGetErrorString(e_));             \
     } while (0)
 
+// Every kernel launch of the engine is followed by PE_LAUNCHED(): it checks the
+// launch and counts it (the count is reported per step).
+extern unsigned long long g_kernelLaunches;
+#define PE_LAUNCHED()                                                                               \
+    do {                                                                                            \
+        PE_CHECK(cudaGetLastError());                                                               \
+        ++::pe::g_kernelLaunches;                                                                   \
+    } while (0)
+
 // Error bits shared by all kernels (written to the step's status word).
 enum : uint32_t {
     kErrTimeout = 1u,

@@ -6,6 +6,8 @@
 
 namespace pe {
 
+unsigned long long g_kernelLaunches = 0;
+
 // ---------------------------------------------------------------------------
 // Exclusive scan (u32), one pass with decoupled look-back.
 // ---------------------------------------------------------------------------
@@ -45,7 +47,7 @@ void launchScanExclusive(const uint32_t *in, uint32_t *out, const uint32_t *d_n,
     PE_CHECK(cudaMemsetAsync(ws.scanState, 0, sizeof(unsigned long long) * tiles + 8, s));
     k_scan_exclusive<<<tiles, kScanThreads, 0, s>>>(in, out, d_n, max_n, ws.scanState,
                                                     (uint32_t *)(ws.scanState + tiles), d_total, d_err);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
 }
 
 // ---------------------------------------------------------------------------
@@ -207,7 +209,7 @@ void launchRadixSort(K *keys, K *keys_tmp, uint32_t *vals, uint32_t *vals_tmp, c
     PE_CHECK(cudaMemsetAsync(ws.sortHist, 0, sizeof(uint32_t) * (256 * 8 + 16), s));
     int hb = (int)std::min<uint32_t>((max_n + 255) / 256, 4 * 152);
     k_radix_hist<K><<<hb, 256, 0, s>>>(keys, d_n, max_n, bit_begin, passes, ws.sortHist);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
     for (int p = 0; p < passes; ++p) {
         PE_CHECK(cudaMemsetAsync(ws.sortState, 0, sizeof(uint32_t) * (256 * (size_t)tiles + 1), s));
         uint32_t *counter = ws.sortState + 256 * (size_t)tiles;
@@ -219,11 +221,11 @@ void launchRadixSort(K *keys, K *keys_tmp, uint32_t *vals, uint32_t *vals_tmp, c
             k_radix_pass<K, false><<<tiles, kSortThreads, 0, s>>>(keys, keys_tmp, nullptr, nullptr, d_n, max_n,
                                                                   bit_begin + 8 * p, ws.sortHist + 256 * p,
                                                                   ws.sortState, counter, sel, p, d_err);
-        PE_CHECK(cudaGetLastError());
+        PE_LAUNCHED();
     }
     int fb = (int)std::min<uint32_t>((max_n + 255) / 256, 4 * 152);
     k_radix_fixup<K><<<fb, 256, 0, s>>>(keys, keys_tmp, vals, vals_tmp, d_n, max_n, sel + passes);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
 }
 
 template void launchRadixSort<uint32_t>(uint32_t *, uint32_t *, uint32_t *, uint32_t *, const uint32_t *, uint32_t,
@@ -238,7 +240,7 @@ __global__ void k_clamp_u32(const uint32_t *src, uint32_t cap, uint32_t *dst) {
 }
 void launchClamp(const uint32_t *src, uint32_t cap, uint32_t *dst, cudaStream_t s) {
     k_clamp_u32<<<1, 1, 0, s>>>(src, cap, dst);
-    PE_CHECK(cudaGetLastError());
+    PE_LAUNCHED();
 }
 
 size_t scratchBytesScan(uint32_t max_n) {

@@ -25,6 +25,7 @@ World::World(int device) : device_(device) {
     PE_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     PE_CHECK(cudaEventCreate(&evStart_));
     PE_CHECK(cudaEventCreate(&evEnd_));
+    for (auto &e : evStage_) PE_CHECK(cudaEventCreate(&e));
     PE_CHECK(cudaMallocHost(&hostStats_, sizeof(DevStats)));
     std::memset(hostStats_, 0, sizeof(DevStats));
     stats_.reserve(1);
@@ -34,7 +35,11 @@ World::World(int device) : device_(device) {
 
 World::~World() {
     if (stream_) cudaStreamSynchronize(stream_);
+    dropGraphs();
     if (hostStats_) cudaFreeHost(hostStats_);
+    for (auto &e : evStage_)
+        if (e) cudaEventDestroy(e);
+    if (pinned_) cudaFreeHost(pinned_);
     if (evStart_) cudaEventDestroy(evStart_);
     if (evEnd_) cudaEventDestroy(evEnd_);
     if (stream_) cudaStreamDestroy(stream_);
@@ -259,6 +264,7 @@ void World::ensureScratch(uint32_t maxN) {
 }
 
 void World::ensureCapacity() {
+    dropGraphs();
     const uint32_t nb = std::max<uint32_t>(nb_, 1), nc = std::max<uint32_t>(nc_, 1);
     for (int k = 0; k < 2; ++k) {
         pos_[k].reserve(nb);
@@ -453,6 +459,7 @@ void World::runPipeline(float dt) {
     cudaStream_t s = stream_;
     WorldView w = view(dt);
     DevStats *st = stats_.ptr;
+    PE_CHECK(cudaEventRecord(evStage_[0], s));
     launchStepInit(st, dense_ ? nc_ : 0u, s);
     const bool sap = algorithm == 0;
     if (dense_) {
@@ -462,17 +469,20 @@ void World::runPipeline(float dt) {
         launchCollect(w, collectFlags_.ptr, collectPos_.ptr, inMin_.ptr, inMax_.ptr, inSlot_.ptr,
                       sap ? sapKeys_.ptr : nullptr, sapVals_.ptr, &st->inputCount, ws_, &st->err, s);
     }
+    PE_CHECK(cudaEventRecord(evStage_[1], s));
     BroadInput in{dense_ ? aabbMin_.ptr : inMin_.ptr, dense_ ? aabbMax_.ptr : inMax_.ptr, &st->inputCount, nc_};
     if (sap) launchSap(in, sapKeys_.ptr, sapVals_.ptr, bb_, pb_, st, ws_, s);
     else launchGrid(in, cellSize, bb_, pb_, st, ws_, s);
     launchPairsFinalize(dense_ ? nullptr : inSlot_.ptr, cbody_.ptr, cbgen_.ptr, pb_, st, ws_, s);
+    PE_CHECK(cudaEventRecord(evStage_[2], s));
     ManifoldView mv = manifoldView();
     launchNarrowphase(w, pb_, mv, mcap_, st, ws_, s);
-    int blocks = (int)std::min<uint32_t>((lastMEstimate_ + 1023) / 1024, (uint32_t)maxCooperativeBlocks(smCount_));
-    if (blocks < 1) blocks = 1;
+    PE_CHECK(cudaEventRecord(evStage_[3], s));
     launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], cacheView(1 - cache_), &cCount_.ptr[1 - cache_],
-                 cacheCap_, sb_, iterations, orderMode, blocks, st, ws_, s);
+                 cacheCap_, sb_, iterations, orderMode, coopBlocks_, st, ws_, s);
+    PE_CHECK(cudaEventRecord(evStage_[4], s));
     launchIntegratePose(w, s);
+    PE_CHECK(cudaEventRecord(evStage_[5], s));
     PE_CHECK(cudaMemcpyAsync(hostStats_, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
 }
 
@@ -538,6 +548,99 @@ bool World::finishStep() {
     return true;
 }
 
+bool World::GraphKey::operator==(const GraphKey &o) const {
+    return nb == o.nb && nc == o.nc && pairCap == o.pairCap && entryCap == o.entryCap && mcap == o.mcap &&
+           cacheCap == o.cacheCap && dt == o.dt && gx == o.gx && gy == o.gy && gz == o.gz &&
+           algorithm == o.algorithm && iterations == o.iterations && orderMode == o.orderMode &&
+           coopBlocks == o.coopBlocks && cellSize == o.cellSize && dense == o.dense &&
+           localIdentity == o.localIdentity && forces == o.forces;
+}
+
+World::GraphKey World::currentKey(float dt) const {
+    GraphKey k{};
+    k.nb = nb_;
+    k.nc = nc_;
+    k.pairCap = pairCap_;
+    k.entryCap = entryCap_;
+    k.mcap = mcap_;
+    k.cacheCap = cacheCap_;
+    k.dt = dt;
+    k.gx = gravity[0];
+    k.gy = gravity[1];
+    k.gz = gravity[2];
+    k.algorithm = algorithm;
+    k.iterations = iterations;
+    k.orderMode = orderMode;
+    k.coopBlocks = coopBlocks_;
+    k.cellSize = cellSize;
+    k.dense = dense_;
+    k.localIdentity = localIdentity_;
+    k.forces = forces_;
+    return k;
+}
+
+void World::dropGraphs() {
+    for (int p = 0; p < 2; ++p)
+        if (graph_[p]) {
+            cudaGraphExecDestroy(graph_[p]);
+            graph_[p] = nullptr;
+        }
+}
+
+// Enqueues one step: through a captured graph when possible, else directly.
+// Returns the number of engine kernels the step launches.
+unsigned long long World::launchStep(float dt) {
+    // Cooperative solver grid from the last step's manifold count, in powers of
+    // two so the captured graph rarely changes.
+    uint32_t want = (lastMEstimate_ + 1023) / 1024, blocks = 1;
+    while (blocks < want) blocks <<= 1;
+    coopBlocks_ = (int)std::min<uint32_t>(blocks, (uint32_t)maxCooperativeBlocks(smCount_));
+    if (graphsDisabled_) {
+        const unsigned long long l0 = g_kernelLaunches;
+        runPipeline(dt);
+        return g_kernelLaunches - l0;
+    }
+    const int p = cur_;
+    const GraphKey key = currentKey(dt);
+    if (!graph_[p] || !(graphKey_[p] == key)) {
+        if (graph_[p]) {
+            cudaGraphExecDestroy(graph_[p]);
+            graph_[p] = nullptr;
+        }
+        const unsigned long long l0 = g_kernelLaunches;
+        cudaGraph_t g = nullptr;
+        PE_CHECK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        try {
+            runPipeline(dt);
+        } catch (...) {
+            cudaStreamEndCapture(stream_, &g);
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            graphsDisabled_ = true;  // capture refused: launch directly from now on
+            return launchStep(dt);
+        }
+        cudaError_t e = cudaStreamEndCapture(stream_, &g);
+        if (e != cudaSuccess || !g) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            graphsDisabled_ = true;
+            return launchStep(dt);
+        }
+        e = cudaGraphInstantiate(&graph_[p], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            graph_[p] = nullptr;
+            graphsDisabled_ = true;
+            return launchStep(dt);
+        }
+        graphKey_[p] = key;
+        graphLaunches_[p] = g_kernelLaunches - l0;
+    }
+    PE_CHECK(cudaGraphLaunch(graph_[p], stream_));
+    return graphLaunches_[p];
+}
+
 void World::step(float dt) {
     PE_CHECK(cudaSetDevice(device_));
     if (algorithm == 2) throw std::invalid_argument("DynamicTree requires a persistent DynamicAabbTree instance");
@@ -547,16 +650,80 @@ void World::step(float dt) {
     }
     for (int attempt = 0; attempt < 8; ++attempt) {
         PE_CHECK(cudaEventRecord(evStart_, stream_));
-        runPipeline(dt);
+        const unsigned long long launches = launchStep(dt);
         PE_CHECK(cudaEventRecord(evEnd_, stream_));
         if (finishStep()) {
-            float ms = 0;
+            float ms = 0, st[5] = {0, 0, 0, 0, 0};
             PE_CHECK(cudaEventElapsedTime(&ms, evStart_, evEnd_));
+            for (int k = 0; k < 5; ++k) PE_CHECK(cudaEventElapsedTime(&st[k], evStage_[k], evStage_[k + 1]));
             counters_.gpuMs = ms;
+            counters_.integrateMs = st[0];
+            counters_.broadphaseMs = st[1];
+            counters_.narrowphaseMs = st[2];
+            counters_.solverMs = st[3];
+            counters_.poseMs = st[4];
+            counters_.kernelLaunches = launches;
+            forces_ = false;  // PhysicsWorld::step clears forces (physics_world.cpp:766)
             return;
         }
     }
     throw std::runtime_error("step buffers kept overflowing");
+}
+
+float4 *World::pinnedBuffer(size_t n) {
+    if (n > pinnedCount_) {
+        if (pinned_) PE_CHECK(cudaFreeHost(pinned_));
+        pinned_ = nullptr;
+        PE_CHECK(cudaMallocHost(&pinned_, n * sizeof(float4)));
+        pinnedCount_ = n;
+    }
+    return pinned_;
+}
+
+void World::writeForces(const float *forces, uint32_t n) {
+    PE_CHECK(cudaSetDevice(device_));
+    if (hostDirty_) {
+        pull();
+        push();
+    }
+    n = std::min<uint32_t>(n, nb_);
+    float4 *stage = pinnedBuffer(std::max<uint32_t>(n, 1));
+    for (uint32_t i = 0; i < n; ++i) {
+        const bool dyn = bodies[i].alive && !bodies[i].isStatic;  // applyForce ignores static bodies
+        stage[i] = dyn ? make_float4(forces[3 * i], forces[3 * i + 1], forces[3 * i + 2], 0.0f)
+                       : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    if (n) PE_CHECK(cudaMemcpyAsync(force_.ptr, stage, n * sizeof(float4), cudaMemcpyHostToDevice, stream_));
+    PE_CHECK(cudaStreamSynchronize(stream_));
+    forces_ = true;
+}
+
+void World::readPoses(float *positions, float *rotations) {
+    PE_CHECK(cudaSetDevice(device_));
+    if (hostDirty_) {
+        pull();
+        push();
+    }
+    float4 *stage = pinnedBuffer(2 * (size_t)std::max<uint32_t>(nb_, 1));
+    if (nb_) {
+        PE_CHECK(cudaMemcpyAsync(stage, pos_[cur_].ptr, nb_ * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
+        PE_CHECK(cudaMemcpyAsync(stage + nb_, rot_[cur_].ptr, nb_ * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
+        PE_CHECK(cudaStreamSynchronize(stream_));
+    }
+    for (uint32_t i = 0; i < nb_; ++i) {
+        if (positions) {
+            positions[3 * i] = stage[i].x;
+            positions[3 * i + 1] = stage[i].y;
+            positions[3 * i + 2] = stage[i].z;
+        }
+        if (rotations) {
+            const float4 &q = stage[nb_ + i];
+            rotations[4 * i] = q.x;
+            rotations[4 * i + 1] = q.y;
+            rotations[4 * i + 2] = q.z;
+            rotations[4 * i + 3] = q.w;
+        }
+    }
 }
 
 // ------------------------------------------------------------- downloads ---
@@ -771,10 +938,11 @@ void World::solveOnly(std::vector<float> &recs, uint32_t count, float dt, int it
     PE_CHECK(cudaMemcpyAsync(ang_[1 - cur_].ptr, ang_[cur_].ptr, bytes, cudaMemcpyDeviceToDevice, s));
     WorldView w = view(dt);
     ManifoldView mv = manifoldView();
-    int blocks = (int)std::min<uint32_t>((count + 1023) / 1024, (uint32_t)maxCooperativeBlocks(smCount_));
-    if (blocks < 1) blocks = 1;
+    uint32_t want = (count + 1023) / 1024, blocks = 1;
+    while (blocks < want) blocks <<= 1;
+    blocks = std::min<uint32_t>(blocks, (uint32_t)maxCooperativeBlocks(smCount_));
     launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], cacheView(1 - cache_), &cCount_.ptr[1 - cache_],
-                 cacheCap_, sb_, iters, mode, blocks, st, ws_, s);
+                 cacheCap_, sb_, iters, mode, (int)blocks, st, ws_, s);
     PE_CHECK(cudaMemcpyAsync(hostStats_, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
     PE_CHECK(cudaStreamSynchronize(s));
     if (hostStats_->err & (kErrTimeout | kErrColors)) throw std::runtime_error("solve failed on the device");

@@ -68,6 +68,9 @@ struct StepCounters {
     uint64_t preparedPoints = 0, warmComparisons = 0, warmMatches = 0, velocityPointVisits = 0;
     uint64_t colors = 0, colorRounds = 0, epaFailures = 0, points = 0;
     double gpuMs = 0;
+    // device time per stage (CUDA events on the world's stream)
+    double integrateMs = 0, broadphaseMs = 0, narrowphaseMs = 0, solverMs = 0, poseMs = 0;
+    uint64_t kernelLaunches = 0;
 };
 
 class World {
@@ -107,6 +110,10 @@ class World {
     void touch() { hostDirty_ = true; }
 
     void step(float dt);
+    // Bulk per-step I/O: set the accumulated force of bodies [0, n) (xyz each),
+    // and read the current poses (positions xyz, rotations xyzw).
+    void writeForces(const float *forces, uint32_t n);
+    void readPoses(float *positions, float *rotations);
     // Standalone stages (BroadPhase::findCandidatePairs, solve on explicit manifolds).
     void broadphaseOnly(const float *mins, const float *maxs, uint32_t n, int algo, double cell,
                         std::vector<uint32_t> &pairs, StepCounters &c);
@@ -123,6 +130,11 @@ class World {
     int device() const { return device_; }
     cudaStream_t stream() const { return stream_; }
     uint64_t stepsTaken() const { return steps_; }
+    // CUDA graphs for the step (on by default; off runs the same launches directly).
+    void setGraphsEnabled(bool on) {
+        graphsDisabled_ = !on;
+        dropGraphs();
+    }
     void syncDevice();
 
   private:
@@ -205,6 +217,27 @@ class World {
     DeviceArray<DevStats> stats_;
     DevStats *hostStats_ = nullptr;
     cudaEvent_t evStart_ = nullptr, evEnd_ = nullptr;
+    cudaEvent_t evStage_[6] = {};
+    // Captured step pipelines, one per ping-pong parity, valid for graphKey_.
+    struct GraphKey {
+        uint32_t nb, nc, pairCap, entryCap, mcap, cacheCap;
+        float dt, gx, gy, gz;
+        int algorithm, iterations, orderMode, coopBlocks;
+        double cellSize;
+        bool dense, localIdentity, forces;
+        bool operator==(const GraphKey &o) const;
+    };
+    cudaGraphExec_t graph_[2] = {nullptr, nullptr};
+    GraphKey graphKey_[2] = {};
+    unsigned long long graphLaunches_[2] = {0, 0};
+    bool graphsDisabled_ = false;
+    int coopBlocks_ = 1;
+    GraphKey currentKey(float dt) const;
+    void dropGraphs();
+    unsigned long long launchStep(float dt);
+    float4 *pinned_ = nullptr;
+    size_t pinnedCount_ = 0;
+    float4 *pinnedBuffer(size_t n);
 };
 
 } // namespace pe

@@ -50,6 +50,8 @@ STATS_DTYPE = np.dtype([
     ("prepared_points", "<u8"), ("warm_start_comparisons", "<u8"), ("warm_start_matches", "<u8"),
     ("velocity_point_visits", "<u8"), ("color_count", "<u8"), ("color_rounds", "<u8"),
     ("epa_failures", "<u8"), ("contact_points", "<u8"), ("total_ms", "<f8"),
+    ("integrate_ms", "<f8"), ("broadphase_ms", "<f8"), ("narrowphase_ms", "<f8"), ("solver_ms", "<f8"),
+    ("pose_ms", "<f8"), ("kernel_launches", "<u8"),
 ])
 
 SAP, GRID, TREE = 0, 1, 2
@@ -88,6 +90,9 @@ SIGNATURES = {
     "pe_world_body_integrate_rotation": (ctypes.c_int, [_P, Handle, ctypes.c_float]),
     "pe_world_body_slot_count": (_u32, [_P]),
     "pe_world_read_bodies": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "pe_world_write_forces": (ctypes.c_int, [_P, _P, _u32]),
+    "pe_world_read_poses": (ctypes.c_int, [_P, _P, _P]),
+    "pe_world_get_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "pe_world_step": (ctypes.c_int, [_P, ctypes.c_float]),
     "pe_world_get_step_stats": (ctypes.c_int, [_P, _P]),
     "pe_world_get_contacts": (ctypes.c_int, [_P, _P, _u32, _P]),
@@ -121,6 +126,15 @@ def _ptr(a):
 
 def _f32(a):
     return np.ascontiguousarray(a, dtype=np.float32)
+
+
+PE_ERR_CAPACITY = 4
+
+
+def check_size(rc: int):
+    """Size query with a NULL / too-small buffer: PE_ERR_CAPACITY just reports the count."""
+    if rc not in (PE_OK, PE_ERR_CAPACITY):
+        check(rc)
 
 
 def check(rc: int):
@@ -265,6 +279,18 @@ class GpuWorld:
     def step(self, dt):
         check(self.lib.pe_world_step(self.h, float(dt)))
 
+    def write_forces(self, forces):
+        f = _f32(forces)
+        check(self.lib.pe_world_write_forces(self.h, _ptr(f), len(f)))
+
+    def read_poses(self, positions=None, rotations=None):
+        check(self.lib.pe_world_read_poses(self.h, _ptr(positions), _ptr(rotations)))
+
+    def stream(self) -> int:
+        s = _P()
+        check(self.lib.pe_world_get_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
     def stats(self):
         s = np.zeros(1, STATS_DTYPE)
         check(self.lib.pe_world_get_step_stats(self.h, _ptr(s)))
@@ -272,7 +298,7 @@ class GpuWorld:
 
     def contacts(self):
         n = _u32()
-        check(self.lib.pe_world_get_contacts(self.h, None, 0, ctypes.byref(n)))
+        check_size(self.lib.pe_world_get_contacts(self.h, None, 0, ctypes.byref(n)))
         out = np.zeros(n.value, MANIFOLD_DTYPE)
         if n.value:
             check(self.lib.pe_world_get_contacts(self.h, _ptr(out), n.value, ctypes.byref(n)))
@@ -280,7 +306,7 @@ class GpuWorld:
 
     def pairs(self):
         n = _u32()
-        check(self.lib.pe_world_get_candidate_pairs(self.h, None, 0, ctypes.byref(n)))
+        check_size(self.lib.pe_world_get_candidate_pairs(self.h, None, 0, ctypes.byref(n)))
         out = np.zeros((n.value, 2), np.uint32)
         if n.value:
             check(self.lib.pe_world_get_candidate_pairs(self.h, _ptr(out), n.value, ctypes.byref(n)))
@@ -288,7 +314,7 @@ class GpuWorld:
 
     def solve_order(self):
         n = _u32()
-        check(self.lib.pe_world_get_solve_order(self.h, None, None, 0, ctypes.byref(n)))
+        check_size(self.lib.pe_world_get_solve_order(self.h, None, None, 0, ctypes.byref(n)))
         order = np.zeros(n.value, np.uint32)
         colors = np.zeros(n.value, np.uint32)
         if n.value:
@@ -308,8 +334,8 @@ def broadphase(mins, maxs, algo=SAP, cell_size=0.0, device=0):
     n = len(mins)
     cnt = ctypes.c_uint64()
     st = np.zeros(1, STATS_DTYPE)
-    check(l.pe_broadphase_find_pairs(int(device), _ptr(mins), _ptr(maxs), n, int(algo), float(cell_size), None, 0,
-                                     ctypes.byref(cnt), _ptr(st)))
+    check_size(l.pe_broadphase_find_pairs(int(device), _ptr(mins), _ptr(maxs), n, int(algo), float(cell_size), None,
+                                          0, ctypes.byref(cnt), _ptr(st)))
     pairs = np.zeros((cnt.value, 2), np.uint32)
     if cnt.value:
         check(l.pe_broadphase_find_pairs(int(device), _ptr(mins), _ptr(maxs), n, int(algo), float(cell_size),
