@@ -117,6 +117,7 @@ typedef struct pe_step_stats {
     double solver_ms;
     double pose_ms;
     uint64_t kernel_launches; /* engine kernels launched by the step */
+    uint64_t graph_replayed;  /* 1 if the step ran from a captured CUDA graph */
 } pe_step_stats;
 
 typedef struct pe_world pe_world;
@@ -203,6 +204,12 @@ pe_status pe_world_read_poses(pe_world *world, float *positions, float *rotation
 /* The CUDA stream (cudaStream_t) the world's kernels run on, for event timing
    by the caller. */
 pe_status pe_world_get_stream(pe_world *world, void **stream);
+
+/* CUDA-graph replay of the step (default on).  Off launches the same kernels
+   one by one; results are identical.  No reference counterpart. */
+pe_status pe_world_set_graphs(pe_world *world, int enabled);
+/* Last graph capture problem of the world (empty when none), for diagnostics. */
+const char *pe_world_graph_error(pe_world *world);
 
 /* PhysicsWorld::step (physics_world.hpp:75) */
 pe_status pe_world_step(pe_world *world, float dt);

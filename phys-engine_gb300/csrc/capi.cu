@@ -79,6 +79,7 @@ void fillStats(const pe::StepCounters &c, pe_step_stats *o) {
     o->solver_ms = c.solverMs;
     o->pose_ms = c.poseMs;
     o->kernel_launches = c.kernelLaunches;
+    o->graph_replayed = c.graphed ? 1u : 0u;
 }
 
 // RigidBody::createSphere / createBox validation and mass properties
@@ -472,6 +473,14 @@ pe_status pe_world_get_stream(pe_world *world, void **stream) {
     *stream = (void *)world->w->stream();
     return PE_OK;
 }
+
+pe_status pe_world_set_graphs(pe_world *world, int enabled) {
+    if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
+    world->w->setGraphsEnabled(enabled != 0);
+    return PE_OK;
+}
+
+const char *pe_world_graph_error(pe_world *world) { return world ? world->w->graphError().c_str() : ""; }
 
 pe_status pe_world_step(pe_world *world, float dt) {
     if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");

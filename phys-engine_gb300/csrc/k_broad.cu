@@ -76,6 +76,12 @@ __global__ void k_sap_emit(const uint32_t *d_n, const uint32_t *off, const uint3
                            const uint32_t *sIdx, unsigned long long *keys, uint32_t cap, DevStats *st) {
     const uint32_t n = *d_n;
     const uint32_t W = st->windowWork;
+    // The flattened window work is indexed in 32 bits; beyond that the sweep
+    // refuses (error flag) instead of walking wrapped offsets.
+    if (st->xWindow > 0xFFFFFFFFull) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&st->err, kErrPairCapacity | kErrEntryCapacity);
+        return;
+    }
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * kSweepChunk;
     for (uint64_t w0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kSweepChunk; w0 < W; w0 += stride) {
         // i = last entry with off[i] <= w0 (it has a non-empty window)
@@ -92,9 +98,13 @@ __global__ void k_sap_emit(const uint32_t *d_n, const uint32_t *off, const uint3
         uint32_t fi = sIdx[i];
         uint64_t wEnd = w0 + kSweepChunk < W ? w0 + kSweepChunk : W;
         for (uint64_t w = w0; w < wEnd; ++w) {
+            if (j >= n) {
+                atomicOr(&st->err, kErrEntryCapacity);
+                break;
+            }
             if (overlapYZ(f, sYZ[j])) emitPair(fi, sIdx[j], keys, cap, &st->rawPairs);
             if (++j == end && w + 1 < wEnd) {
-                do { ++i; } while (len[i] == 0);
+                do { ++i; } while (i + 1 < n && len[i] == 0);
                 j = i + 1;
                 end = i + 1 + len[i];
                 f = sYZ[i];
@@ -123,8 +133,9 @@ __global__ void k_grid_widths(BroadInput in, unsigned long long *keys, uint32_t 
 __global__ void k_grid_cellsize(const unsigned long long *sortedWidths, const uint32_t *count, double fixedCell,
                                 DevStats *st) {
     double cell = 1.0;
+    const uint32_t c = *count, n = st->inputCount;
     if (fixedCell > 0.0) cell = fixedCell;
-    else if (*count > 0) cell = __longlong_as_double((long long)sortedWidths[*count / 2]);
+    else if (c > 0 && c <= n) cell = __longlong_as_double((long long)sortedWidths[c / 2]);
     st->cellSize = cell;
 }
 
@@ -187,6 +198,8 @@ __device__ __forceinline__ uint32_t bitsFor(uint32_t range) { return range ? 32u
 __global__ void k_grid_entries(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const uint32_t *entryOff,
                                unsigned long long *keys, uint32_t *vals, uint32_t cap, DevStats *st) {
     const uint32_t n = *in.d_n;
+    // No box in the grid: the bounds keep their sentinels and there is nothing to write.
+    if (st->cellLo[0] > st->cellHi[0]) return;
     const uint32_t bx = bitsFor((uint32_t)(st->cellHi[0] - st->cellLo[0]));
     const uint32_t by = bitsFor((uint32_t)(st->cellHi[1] - st->cellLo[1]));
     const uint32_t bz = bitsFor((uint32_t)(st->cellHi[2] - st->cellLo[2]));
@@ -329,6 +342,8 @@ void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, Broad
 void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBuffers &pb, DevStats *st, Scratch &ws,
                 cudaStream_t s) {
     uint32_t *err = &st->err;
+    // counters[0] counts the non-zero widths of this call; counters[1] is the clamped entry count.
+    PE_CHECK(cudaMemsetAsync(bb.counters, 0, 4 * sizeof(uint32_t), s));
     if (fixedCell <= 0.0) {
         k_grid_widths<<<gridFor(in.maxN), 256, 0, s>>>(in, bb.widthKeys, &bb.counters[0]);
         PE_LAUNCHED();

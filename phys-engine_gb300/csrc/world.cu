@@ -459,7 +459,7 @@ void World::runPipeline(float dt) {
     cudaStream_t s = stream_;
     WorldView w = view(dt);
     DevStats *st = stats_.ptr;
-    PE_CHECK(cudaEventRecord(evStage_[0], s));
+    PE_CHECK(cudaEventRecordWithFlags(evStage_[0], s, cudaEventRecordExternal));
     launchStepInit(st, dense_ ? nc_ : 0u, s);
     const bool sap = algorithm == 0;
     if (dense_) {
@@ -469,20 +469,20 @@ void World::runPipeline(float dt) {
         launchCollect(w, collectFlags_.ptr, collectPos_.ptr, inMin_.ptr, inMax_.ptr, inSlot_.ptr,
                       sap ? sapKeys_.ptr : nullptr, sapVals_.ptr, &st->inputCount, ws_, &st->err, s);
     }
-    PE_CHECK(cudaEventRecord(evStage_[1], s));
+    PE_CHECK(cudaEventRecordWithFlags(evStage_[1], s, cudaEventRecordExternal));
     BroadInput in{dense_ ? aabbMin_.ptr : inMin_.ptr, dense_ ? aabbMax_.ptr : inMax_.ptr, &st->inputCount, nc_};
     if (sap) launchSap(in, sapKeys_.ptr, sapVals_.ptr, bb_, pb_, st, ws_, s);
     else launchGrid(in, cellSize, bb_, pb_, st, ws_, s);
     launchPairsFinalize(dense_ ? nullptr : inSlot_.ptr, cbody_.ptr, cbgen_.ptr, pb_, st, ws_, s);
-    PE_CHECK(cudaEventRecord(evStage_[2], s));
+    PE_CHECK(cudaEventRecordWithFlags(evStage_[2], s, cudaEventRecordExternal));
     ManifoldView mv = manifoldView();
     launchNarrowphase(w, pb_, mv, mcap_, st, ws_, s);
-    PE_CHECK(cudaEventRecord(evStage_[3], s));
+    PE_CHECK(cudaEventRecordWithFlags(evStage_[3], s, cudaEventRecordExternal));
     launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], cacheView(1 - cache_), &cCount_.ptr[1 - cache_],
                  cacheCap_, sb_, iterations, orderMode, coopBlocks_, st, ws_, s);
-    PE_CHECK(cudaEventRecord(evStage_[4], s));
+    PE_CHECK(cudaEventRecordWithFlags(evStage_[4], s, cudaEventRecordExternal));
     launchIntegratePose(w, s);
-    PE_CHECK(cudaEventRecord(evStage_[5], s));
+    PE_CHECK(cudaEventRecordWithFlags(evStage_[5], s, cudaEventRecordExternal));
     PE_CHECK(cudaMemcpyAsync(hostStats_, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
 }
 
@@ -598,6 +598,7 @@ unsigned long long World::launchStep(float dt) {
     if (graphsDisabled_) {
         const unsigned long long l0 = g_kernelLaunches;
         runPipeline(dt);
+        lastGraphed_ = false;
         return g_kernelLaunches - l0;
     }
     const int p = cur_;
@@ -612,7 +613,8 @@ unsigned long long World::launchStep(float dt) {
         PE_CHECK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
         try {
             runPipeline(dt);
-        } catch (...) {
+        } catch (const std::exception &ex) {
+            graphError_ = std::string("capture: ") + ex.what();
             cudaStreamEndCapture(stream_, &g);
             if (g) cudaGraphDestroy(g);
             cudaGetLastError();
@@ -621,6 +623,7 @@ unsigned long long World::launchStep(float dt) {
         }
         cudaError_t e = cudaStreamEndCapture(stream_, &g);
         if (e != cudaSuccess || !g) {
+            graphError_ = std::string("capture: ") + cudaGetErrorString(e);
             if (g) cudaGraphDestroy(g);
             cudaGetLastError();
             graphsDisabled_ = true;
@@ -629,6 +632,7 @@ unsigned long long World::launchStep(float dt) {
         e = cudaGraphInstantiate(&graph_[p], g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) {
+            graphError_ = std::string("instantiate: ") + cudaGetErrorString(e);
             cudaGetLastError();
             graph_[p] = nullptr;
             graphsDisabled_ = true;
@@ -638,6 +642,7 @@ unsigned long long World::launchStep(float dt) {
         graphLaunches_[p] = g_kernelLaunches - l0;
     }
     PE_CHECK(cudaGraphLaunch(graph_[p], stream_));
+    lastGraphed_ = true;
     return graphLaunches_[p];
 }
 
@@ -663,6 +668,7 @@ void World::step(float dt) {
             counters_.solverMs = st[3];
             counters_.poseMs = st[4];
             counters_.kernelLaunches = launches;
+            counters_.graphed = lastGraphed_;
             forces_ = false;  // PhysicsWorld::step clears forces (physics_world.cpp:766)
             return;
         }

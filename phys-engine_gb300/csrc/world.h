@@ -71,6 +71,7 @@ struct StepCounters {
     // device time per stage (CUDA events on the world's stream)
     double integrateMs = 0, broadphaseMs = 0, narrowphaseMs = 0, solverMs = 0, poseMs = 0;
     uint64_t kernelLaunches = 0;
+    bool graphed = false;  // the step ran from a captured CUDA graph
 };
 
 class World {
@@ -131,6 +132,7 @@ class World {
     cudaStream_t stream() const { return stream_; }
     uint64_t stepsTaken() const { return steps_; }
     // CUDA graphs for the step (on by default; off runs the same launches directly).
+    const std::string &graphError() const { return graphError_; }
     void setGraphsEnabled(bool on) {
         graphsDisabled_ = !on;
         dropGraphs();
@@ -231,6 +233,8 @@ class World {
     GraphKey graphKey_[2] = {};
     unsigned long long graphLaunches_[2] = {0, 0};
     bool graphsDisabled_ = false;
+    bool lastGraphed_ = false;
+    std::string graphError_;
     int coopBlocks_ = 1;
     GraphKey currentKey(float dt) const;
     void dropGraphs();

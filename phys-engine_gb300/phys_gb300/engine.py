@@ -51,7 +51,7 @@ STATS_DTYPE = np.dtype([
     ("velocity_point_visits", "<u8"), ("color_count", "<u8"), ("color_rounds", "<u8"),
     ("epa_failures", "<u8"), ("contact_points", "<u8"), ("total_ms", "<f8"),
     ("integrate_ms", "<f8"), ("broadphase_ms", "<f8"), ("narrowphase_ms", "<f8"), ("solver_ms", "<f8"),
-    ("pose_ms", "<f8"), ("kernel_launches", "<u8"),
+    ("pose_ms", "<f8"), ("kernel_launches", "<u8"), ("graph_replayed", "<u8"),
 ])
 
 SAP, GRID, TREE = 0, 1, 2
@@ -93,6 +93,8 @@ SIGNATURES = {
     "pe_world_write_forces": (ctypes.c_int, [_P, _P, _u32]),
     "pe_world_read_poses": (ctypes.c_int, [_P, _P, _P]),
     "pe_world_get_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+    "pe_world_set_graphs": (ctypes.c_int, [_P, ctypes.c_int]),
+    "pe_world_graph_error": (ctypes.c_char_p, [_P]),
     "pe_world_step": (ctypes.c_int, [_P, ctypes.c_float]),
     "pe_world_get_step_stats": (ctypes.c_int, [_P, _P]),
     "pe_world_get_contacts": (ctypes.c_int, [_P, _P, _u32, _P]),
@@ -278,6 +280,12 @@ class GpuWorld:
     # stepping ------------------------------------------------------------
     def step(self, dt):
         check(self.lib.pe_world_step(self.h, float(dt)))
+
+    def set_graphs(self, enabled: bool):
+        check(self.lib.pe_world_set_graphs(self.h, 1 if enabled else 0))
+
+    def graph_error(self) -> str:
+        return self.lib.pe_world_graph_error(self.h).decode()
 
     def write_forces(self, forces):
         f = _f32(forces)
