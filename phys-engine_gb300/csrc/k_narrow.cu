@@ -97,8 +97,8 @@ k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *_
             restitution = smax(ma.y, mb.y);
             friction = sqrtf(smax(ma.z, 0.0f) * smax(mb.z, 0.0f));
         }
-        aggregatedAdd64(&st->npCandidates[category], 1ull);
-        if (hit) aggregatedAdd64(&st->npContacts[category], 1ull);
+        aggregatedCount(st->npCandidates, category);
+        if (hit) aggregatedCount(st->npContacts, category);
     }
     uint32_t total;
     const uint32_t local = blockExclusiveScan(hit ? 1u : 0u, total, s_scan);

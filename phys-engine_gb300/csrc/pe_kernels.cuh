@@ -25,4 +25,12 @@ __device__ __forceinline__ void aggregatedAdd64(unsigned long long *counter, uns
     if (g.thread_rank() == 0 && s) atomicAdd(counter, s);
 }
 
+// Adds 1 to counters[key] once per group of converged lanes sharing the key.
+__device__ __forceinline__ void aggregatedCount(unsigned long long *counters, uint32_t key) {
+    const uint32_t active = __activemask();
+    const uint32_t peers = __match_any_sync(active, key);
+    const int leader = __ffs(peers) - 1;
+    if ((int)(threadIdx.x & 31) == leader) atomicAdd(&counters[key], (unsigned long long)__popc(peers));
+}
+
 } // namespace pe

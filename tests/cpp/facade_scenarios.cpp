@@ -1,0 +1,94 @@
+// Scenarios of the reference's solver tests
+// (tests/solver/sequential_impulse_solver_tests.cpp:293-378 of bkuangs/phys-engine)
+// written against the phys_gb300 facade the way a caller of phys::PhysicsWorld
+// writes them; links libphys_gb300.so and runs on the GPU.  Exit code 0 = pass.
+#include <cmath>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+#include "phys_gb300_world.hpp"
+
+using namespace phys_gb300;
+
+static bool boxLandsOnStaticFloor() {
+    PhysicsWorld world;
+    world.gravity = {0.0f, -9.81f, 0.0f};
+    RigidBodyHandle floorBody, boxBody;
+    ColliderHandle floorCollider, boxCollider;
+    std::string error;
+    if (!world.createBox(18.0f, 1.0f, 8.0f, {0.0f, -0.5f, 0.0f}, 1.0f, true, 0.1f, 0.6f, floorBody, floorCollider,
+                         error) ||
+        !world.createBox(1.4f, 1.4f, 1.4f, {-1.5f, 3.0f, 0.0f}, 1.0f, false, 0.2f, 0.5f, boxBody, boxCollider,
+                         error)) {
+        std::fprintf(stderr, "creation failed: %s\n", error.c_str());
+        return false;
+    }
+    for (int step = 0; step < 180; ++step) world.step(1.0f / 60.0f);
+    BodyRef body = world.getBody(boxBody);
+    auto contacts = world.contacts();
+    bool ok = body && body.getPosition().y >= 0.68f && body.getPosition().y <= 0.72f &&
+              std::fabs(body.getPosition().x + 1.5f) <= 0.02f && std::fabs(body.getLinearVelocity().x) <= 0.02f &&
+              std::fabs(body.getAngularVelocity().z) <= 0.02f && !contacts.empty() && contacts.front().pointCount >= 2;
+    if (!ok) std::fprintf(stderr, "box did not land: y=%f contacts=%zu\n", body.getPosition().y, contacts.size());
+    return ok;
+}
+
+static bool tiltedBoxSettlesFlat(float dt, float angle, Vec3 axis) {
+    PhysicsWorld world(0, 8, PE_ORDER_COLOR);
+    RigidBodyHandle floorBody, boxBody;
+    ColliderHandle floorCollider, boxCollider;
+    std::string error;
+    if (!world.createBox(18.0f, 1.0f, 8.0f, {0.0f, -0.5f, 0.0f}, 1.0f, true, 0.0f, 0.6f, floorBody, floorCollider,
+                         error) ||
+        !world.createBox(1.0f, 1.0f, 1.0f, {0.0f, 2.0f, 0.0f}, 1.0f, false, 0.0f, 0.55f, boxBody, boxCollider, error))
+        return false;
+    BodyRef body = world.getBody(boxBody);
+    float s = 2.0f * std::tan(angle * 0.5f);
+    body.setAngularVelocity({axis.x * s, axis.y * s, axis.z * s});
+    body.integrateRotation(1.0f);
+    body.setAngularVelocity({});
+    for (int step = 0; step < 600; ++step) world.step(dt);
+    body = world.getBody(boxBody);
+    Quaternion q = body.getRotation();
+    // y of the rotated unit axes: the box is flat when one of them is ~vertical
+    float ax = std::fabs(2.0f * (q.x * q.y + q.w * q.z));
+    float ay = std::fabs(1.0f - 2.0f * (q.x * q.x + q.z * q.z));
+    float az = std::fabs(2.0f * (q.y * q.z - q.w * q.x));
+    float alignment = std::fmax(ax, std::fmax(ay, az));
+    Vec3 v = body.getLinearVelocity(), w = body.getAngularVelocity();
+    bool ok = alignment >= 0.995f && std::fabs(body.getPosition().y - 0.5f) <= 0.03f &&
+              std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z) <= 0.08f &&
+              std::sqrt(w.x * w.x + w.y * w.y + w.z * w.z) <= 0.1f;
+    if (!ok) std::fprintf(stderr, "tilted box: alignment=%f y=%f\n", alignment, body.getPosition().y);
+    return ok;
+}
+
+static bool invalidInputs() {
+    PhysicsWorld world;
+    RigidBodyHandle b;
+    ColliderHandle c;
+    std::string error;
+    if (world.createSphere(0.001f, {}, 1.0f, false, 0, 0, b, c, error) || error != "Sphere is too small") return false;
+    if (world.createBox(1, 1, 1, {}, 30.0f, false, 0, 0, b, c, error) || error != "Density is out of range") return false;
+    try {
+        world.setSolverWorkerCount(0);
+        return false;
+    } catch (const std::invalid_argument &) {
+    }
+    world.broadPhaseAlgorithm = BroadPhaseAlgorithm::DynamicTree;
+    try {
+        world.step(1.0f / 60.0f);
+        return false;
+    } catch (const std::invalid_argument &) {
+    }
+    if (world.getBody(RigidBodyHandle{7, 3})) return false;  // stale handle -> "nullptr"
+    return true;
+}
+
+int main() {
+    bool ok = boxLandsOnStaticFloor() && tiltedBoxSettlesFlat(1.0f / 60.0f, 0.6f, {0.0f, 0.0f, 1.0f}) &&
+              tiltedBoxSettlesFlat(1.0f / 120.0f, 0.9f, {0.6f, 0.0f, 0.8f}) && invalidInputs();
+    std::printf("%s\n", ok ? "facade scenarios ok" : "facade scenarios FAILED");
+    return ok ? 0 : 1;
+}
