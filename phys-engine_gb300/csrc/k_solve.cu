@@ -13,6 +13,7 @@
 // dynamic bodies (greedy in decreasing priority), computed in parallel rounds
 // (Jones-Plassmann): a manifold is coloured once it holds the highest priority
 // among the uncoloured manifolds at both its bodies.
+#include "pe_block.cuh"
 #include "pe_kernels.cuh"
 #include "pe_stages.h"
 
@@ -21,6 +22,7 @@ namespace pe {
 constexpr uint32_t kUncolored = 0xFFFFFFFFu;
 constexpr uint32_t kMaxRounds = 4096;
 constexpr int kSolveThreads = 256;
+constexpr int kBlockSolveThreads = 512;
 
 __device__ __forceinline__ uint32_t colorPriority(uint32_t m) {
     uint32_t h = m;
@@ -135,14 +137,13 @@ __global__ void k_order_init(SolveArgs a, int serial) {
 // --------------------------------------------------------------- prepare ---
 // prepareBody (:275-287) + prepareContactPoints (:101-214) + the cache lookup
 // of warmStartPrepared (:448-490).  Data are written in solve order k.
-__global__ void k_prepare(SolveArgs a) {
-    const uint32_t M = min(a.st->manifolds, a.mcap);
+__device__ void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t stride, uint32_t M) {
     const uint32_t mcap = a.mcap;
     const WorldView &w = a.w;
     const float inverseDt = 1.0f / smax(w.dt, 1e-6f);
     const uint32_t cacheN = *a.oldCount;
     uint64_t prepared = 0, comparisons = 0, matches = 0;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < M; k += gridDim.x * blockDim.x) {
+    for (uint32_t k = begin; k < M; k += stride) {
         const uint32_t m = a.sb.order[k];
         const uint32_t ia = a.mv.bodyA[m], ib = a.mv.bodyB[m];
         const float4 nf = a.mv.normalFriction[m];
@@ -281,6 +282,10 @@ __global__ void k_prepare(SolveArgs a) {
     aggregatedAdd64(&a.st->preparedPoints, prepared);
     aggregatedAdd64(&a.st->warmComparisons, comparisons);
     aggregatedAdd64(&a.st->warmMatches, matches);
+}
+
+__global__ void k_prepare(SolveArgs a) {
+    prepareRange(a, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, min(a.st->manifolds, a.mcap));
 }
 
 // ---------------------------------------------------------- solve sweeps ---
@@ -493,6 +498,24 @@ __global__ void k_cache_counts(SolveArgs a) {
         a.sb.cacheCounts[k] = valid ? a.mv.pointCount[m] : 0u;
     }
 }
+// Writes the cache entries of manifold m (npts points) starting at entry base.
+__device__ __forceinline__ void cacheWriteManifold(const SolveArgs &a, const CacheView &nc, uint32_t cacheCap,
+                                                   uint32_t m, uint32_t base, uint32_t npts) {
+    const unsigned long long key = ((unsigned long long)a.mv.bodyA[m] << 32) | a.mv.bodyB[m];
+    const unsigned long long gens = ((unsigned long long)a.mv.genA[m] << 32) | a.mv.genB[m];
+    for (uint32_t p = 0; p < npts; ++p) {
+        const uint32_t e = base + p;
+        if (e >= cacheCap) break;
+        const float4 aa = a.mv.anchorA[4 * m + p], ab = a.mv.anchorB[4 * m + p];
+        const float4 imp = a.mv.impulse[4 * m + p];
+        nc.key[e] = key;
+        nc.gens[e] = gens;
+        nc.anchorA[e] = make_float4(aa.x, aa.y, aa.z, imp.x);
+        nc.anchorB[e] = make_float4(ab.x, ab.y, ab.z, imp.y);
+        nc.tangent2[e] = imp.z;
+    }
+}
+
 __global__ void k_cache_write(SolveArgs a, CacheView nc, uint32_t cacheCap) {
     const uint32_t M = min(a.st->manifolds, a.mcap);
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < M; k += gridDim.x * blockDim.x) {
@@ -513,6 +536,187 @@ __global__ void k_cache_write(SolveArgs a, CacheView nc, uint32_t cacheCap) {
             nc.tangent2[e] = imp.z;
         }
     }
+}
+
+
+// ------------------------------------------------------ single-block path ---
+// The whole solver for up to kBlockMaxManifolds manifolds in one thread block:
+// the same colouring, order, prepare, sweeps and cache rebuild as the
+// multi-kernel path, separated by __syncthreads instead of kernel boundaries
+// and grid barriers.  If the live manifold count exceeds the block capacity the
+// kernel only flags kErrSmallPath; the step is then re-run on the multi-kernel
+// path.
+__global__ void __launch_bounds__(kBlockSolveThreads)
+k_solve_block(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount, int serial) {
+    extern __shared__ unsigned long long s_sort[];  // kBlockMaxManifolds u64
+    uint32_t *s_dyn = reinterpret_cast<uint32_t *>(s_sort + kBlockMaxManifolds);
+    __shared__ uint32_t s_start[kMaxColors + 1], s_count[kMaxColors], s_colored, s_colors, s_scan[40];
+    const uint32_t M = min(a.st->manifolds, a.mcap);
+    if (M > kBlockMaxManifolds) {
+        if (threadIdx.x == 0) atomicOr(&a.st->err, kErrSmallPath);
+        return;
+    }
+    const WorldView &w = a.w;
+    SolverBuffers &sb = a.sb;
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    uint32_t C = 0;
+    if (serial) {
+        for (uint32_t k = tid; k < M; k += nt) sb.order[k] = k;
+        __syncthreads();
+    } else {
+        // --- colouring (Jones-Plassmann rounds, as k_color) ---
+        for (uint32_t c = tid; c < kMaxColors; c += nt) s_count[c] = 0;
+        if (tid == 0) {
+            s_colored = 0;
+            s_colors = 0;
+        }
+        uint32_t *s_color = reinterpret_cast<uint32_t *>(s_sort);  // reused before the order sort
+        for (uint32_t m = tid; m < M; m += nt) {
+            uint32_t ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
+            bool da = ba < w.nb && (w.bflags[ba] & kBodyAlive) && w.bgen[ba] == a.mv.genA[m] && !(w.bflags[ba] & kBodyStatic);
+            bool db = bb < w.nb && (w.bflags[bb] & kBodyAlive) && w.bgen[bb] == a.mv.genB[m] && !(w.bflags[bb] & kBodyStatic);
+            s_dyn[m] = (da ? 1u : 0u) | (db ? 2u : 0u);
+            s_color[m] = kUncolored;
+            if (da) {
+                __stcg(&sb.bodyUsed[2 * ba], 0ull);
+                __stcg(&sb.bodyUsed[2 * ba + 1], 0ull);
+            }
+            if (db) {
+                __stcg(&sb.bodyUsed[2 * bb], 0ull);
+                __stcg(&sb.bodyUsed[2 * bb + 1], 0ull);
+            }
+        }
+        __syncthreads();
+        const unsigned long long epoch0 = __ldcg(sb.epoch);
+        uint32_t round = 0;
+        for (; round < kMaxRounds; ++round) {
+            const unsigned long long stamp = (epoch0 + round + 1) << 32;
+            for (uint32_t m = tid; m < M; m += nt) {
+                if (s_color[m] != kUncolored) continue;
+                const unsigned long long p = stamp | colorPriority(m);
+                if (s_dyn[m] & 1u) atomicMax(&sb.bodyBest[a.mv.bodyA[m]], p);
+                if (s_dyn[m] & 2u) atomicMax(&sb.bodyBest[a.mv.bodyB[m]], p);
+            }
+            __syncthreads();
+            for (uint32_t m = tid; m < M; m += nt) {
+                if (s_color[m] != kUncolored) continue;
+                const unsigned long long p = stamp | colorPriority(m);
+                const uint32_t d = s_dyn[m], ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
+                // Atomics resolve in L2; read past L1 so no stale line is seen.
+                if ((d & 1u) && __ldcg(&sb.bodyBest[ba]) != p) continue;
+                if ((d & 2u) && __ldcg(&sb.bodyBest[bb]) != p) continue;
+                unsigned long long u0 = 0, u1 = 0;
+                if (d & 1u) {
+                    u0 |= __ldcg(&sb.bodyUsed[2 * ba]);
+                    u1 |= __ldcg(&sb.bodyUsed[2 * ba + 1]);
+                }
+                if (d & 2u) {
+                    u0 |= __ldcg(&sb.bodyUsed[2 * bb]);
+                    u1 |= __ldcg(&sb.bodyUsed[2 * bb + 1]);
+                }
+                uint32_t c;
+                if (~u0) c = __ffsll((long long)~u0) - 1;
+                else if (~u1) c = 64 + __ffsll((long long)~u1) - 1;
+                else {
+                    atomicOr(&a.st->err, kErrColors);
+                    c = kMaxColors - 1;
+                }
+                s_color[m] = c;
+                const unsigned long long bit = 1ull << (c & 63);
+                if (d & 1u) __stcg(&sb.bodyUsed[2 * ba + (c >> 6)], __ldcg(&sb.bodyUsed[2 * ba + (c >> 6)]) | bit);
+                if (d & 2u) __stcg(&sb.bodyUsed[2 * bb + (c >> 6)], __ldcg(&sb.bodyUsed[2 * bb + (c >> 6)]) | bit);
+                atomicAdd(&s_count[c], 1u);
+                atomicMax(&s_colors, c + 1);
+                atomicAdd(&s_colored, 1u);
+            }
+            __syncthreads();
+            if (s_colored >= M) break;
+            __syncthreads();
+        }
+        if (tid == 0) {
+            *sb.epoch = epoch0 + round + 2;
+            a.st->colorRounds = round + 1;
+            a.st->colors = s_colors;
+            if (round >= kMaxRounds) atomicOr(&a.st->err, kErrColors);
+            uint32_t acc = 0;
+            for (uint32_t c = 0; c < s_colors; ++c) {
+                s_start[c] = acc;
+                sb.colorCount[c] = s_count[c];
+                acc += s_count[c];
+            }
+            s_start[s_colors] = acc;
+        }
+        // colours to global (pair order) and the (colour, index) order
+        for (uint32_t m = tid; m < M; m += nt) sb.color[m] = s_color[m];
+        __syncthreads();
+        const uint32_t n2 = nextPow2(M > 0 ? M : 1);
+        uint32_t *keys = reinterpret_cast<uint32_t *>(s_sort);
+        for (uint32_t i = tid; i < n2; i += nt) keys[i] = i < M ? ((sb.color[i] << 12) | i) : 0xFFFFFFFFu;
+        __syncthreads();
+        blockBitonicSort<uint32_t>(keys, n2);
+        for (uint32_t k = tid; k < M; k += nt) sb.order[k] = keys[k] & 0xFFFu;
+        C = s_colors;
+        __syncthreads();
+    }
+    // --- prepare + warm-start matching ---
+    prepareRange(a, tid, nt, M);
+    __syncthreads();
+    // --- warm start and velocity iterations ---
+    if (serial) {
+        if (tid == 0) {
+            for (uint32_t k = 0; k < M; ++k) warmStartOne(a, k);
+            for (int it = 0; it < a.iterations; ++it)
+                for (uint32_t k = 0; k < M; ++k) solveOne(a, k);
+        }
+    } else {
+        for (uint32_t c = 0; c < C; ++c) {
+            for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) warmStartOne(a, k);
+            __syncthreads();
+        }
+        for (int it = 0; it < a.iterations; ++it)
+            for (uint32_t c = 0; c < C; ++c) {
+                for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) solveOne(a, k);
+                __syncthreads();
+            }
+    }
+    __syncthreads();
+    // --- impulses back to the manifolds ---
+    for (uint32_t k = tid; k < M; k += nt) {
+        const uint32_t m = sb.order[k];
+        for (uint32_t p = 0; p < 4; ++p) {
+            float4 imp = sb.pimp[(size_t)p * a.mcap + k];
+            imp.w = 0.0f;
+            a.mv.impulse[4 * m + p] = imp;
+        }
+    }
+    __syncthreads();
+    // --- cache rebuild: stable sort by (body A, body B) over solve order ---
+    const uint32_t n2 = nextPow2(M > 0 ? M : 1);
+    for (uint32_t i = tid; i < n2; i += nt) {
+        unsigned long long key = ~0ull;
+        if (i < M) {
+            const uint32_t m = sb.order[i];
+            key = ((unsigned long long)a.mv.bodyA[m] << 44) | ((unsigned long long)a.mv.bodyB[m] << 24) | i;
+        }
+        s_sort[i] = key;
+    }
+    __syncthreads();
+    blockBitonicSort<unsigned long long>(s_sort, n2);
+    for (uint32_t i = tid; i < M; i += nt) {
+        const uint32_t m = sb.order[(uint32_t)(s_sort[i] & 0xFFFu)];
+        const uint32_t ia = a.mv.bodyA[m], ib = a.mv.bodyB[m];
+        const bool valid = ia < w.nb && ib < w.nb && (w.bflags[ia] & kBodyAlive) && (w.bflags[ib] & kBodyAlive) &&
+                           w.bgen[ia] == a.mv.genA[m] && w.bgen[ib] == a.mv.genB[m];
+        s_dyn[i] = valid ? a.mv.pointCount[m] : 0u;
+    }
+    __syncthreads();
+    const uint32_t total = blockExclusiveScanArray(s_dyn, M, s_scan);
+    for (uint32_t i = tid; i < M; i += nt) {
+        const uint32_t m = sb.order[(uint32_t)(s_sort[i] & 0xFFFu)];
+        const uint32_t cnt = (i + 1 < M ? s_dyn[i + 1] : total) - s_dyn[i];
+        cacheWriteManifold(a, nc, cacheCap, m, s_dyn[i], cnt);
+    }
+    if (tid == 0) *newCount = total;
 }
 
 static int gridFor(uint32_t n, int threads = 256, int maxBlocks = 152 * 8) {
@@ -550,10 +754,22 @@ int maxCooperativeBlocks(int smCount) {
 
 void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &oldCache, const uint32_t *oldCacheCount,
                   const CacheView &newCache, uint32_t *newCacheCount, uint32_t cacheCap, SolverBuffers &sb,
-                  int iterations, int orderMode, int coopBlocks, DevStats *st, Scratch &ws, cudaStream_t s) {
+                  int iterations, int orderMode, int coopBlocks, bool blockPath, DevStats *st, Scratch &ws,
+                  cudaStream_t s) {
     SolveArgs a{w, mv, sb, oldCache, oldCacheCount, st, sb.mcap, iterations};
     uint32_t *err = &st->err;
     const uint32_t mcap = sb.mcap;
+    if (blockPath) {
+        static bool configured = false;
+        const size_t smem = kBlockMaxManifolds * (sizeof(unsigned long long) + sizeof(uint32_t));
+        if (!configured) {
+            PE_CHECK(cudaFuncSetAttribute(k_solve_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            configured = true;
+        }
+        k_solve_block<<<1, kBlockSolveThreads, smem, s>>>(a, newCache, cacheCap, newCacheCount, orderMode == 0 ? 1 : 0);
+        PE_LAUNCHED();
+        return;
+    }
     PE_CHECK(cudaMemsetAsync(sb.counters, 0, 4 * sizeof(uint32_t), s));
     PE_CHECK(cudaMemsetAsync(sb.bar, 0, 2 * sizeof(uint32_t), s));
     const bool serial = orderMode == 0;

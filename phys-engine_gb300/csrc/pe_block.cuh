@@ -1,0 +1,72 @@
+// Block-level primitives for work that fits one thread block (shared-memory
+// bitonic sort, block-wide exclusive scan over many items).
+#pragma once
+#include <cstdint>
+
+namespace pe {
+
+// Sorts s[0, n) ascending in shared memory; n is a power of two (pad the tail
+// with the key type's maximum).  All threads of the block call it.
+template <class K> __device__ void blockBitonicSort(K *s, uint32_t n) {
+    for (uint32_t k = 2; k <= n; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+                const uint32_t ixj = i ^ j;
+                if (ixj > i) {
+                    const K a = s[i], b = s[ixj];
+                    const bool ascending = (i & k) == 0;
+                    if ((a > b) == ascending) {
+                        s[i] = b;
+                        s[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t nextPow2(uint32_t v) {
+    uint32_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+// In-place exclusive scan of s[0, n) (u32) by one block; returns the total.
+// scratch needs blockDim.x / 32 + 1 entries.  All threads call it.
+__device__ uint32_t blockExclusiveScanArray(uint32_t *s, uint32_t n, uint32_t *scratch) {
+    const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+    const uint32_t b = threadIdx.x * per, e = min(n, b + per);
+    uint32_t sum = 0;
+    for (uint32_t i = b; i < e; ++i) sum += s[i];
+    // warp-level inclusive scan of the per-thread sums
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = (blockDim.x + 31) >> 5;
+    uint32_t incl = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) scratch[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (int w = 0; w < warps; ++w) {
+            uint32_t t = scratch[w];
+            scratch[w] = acc;
+            acc += t;
+        }
+        scratch[warps] = acc;
+    }
+    __syncthreads();
+    uint32_t run = scratch[warp] + incl - sum;
+    for (uint32_t i = b; i < e; ++i) {
+        uint32_t t = s[i];
+        s[i] = run;
+        run += t;
+    }
+    const uint32_t total = scratch[warps];
+    __syncthreads();
+    return total;
+}
+
+} // namespace pe

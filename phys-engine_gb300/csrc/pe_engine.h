@@ -37,6 +37,7 @@ enum : uint32_t {
     kErrColors = 8u,
     kErrEntryCapacity = 16u,
     kErrEpa = 32u,
+    kErrSmallPath = 64u,  // a single-block path saw more work than it holds: re-run on the full path
 };
 
 // Body flag bits (bflags) and collider flag layout (cflags).

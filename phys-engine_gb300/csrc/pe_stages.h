@@ -84,7 +84,12 @@ void launchNarrowphase(const WorldView &w, const PairBuffers &pb, const Manifold
                        Scratch &ws, cudaStream_t s);
 void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &oldCache, const uint32_t *oldCacheCount,
                   const CacheView &newCache, uint32_t *newCacheCount, uint32_t cacheCap, SolverBuffers &sb,
-                  int iterations, int orderMode, int coopBlocks, DevStats *st, Scratch &ws, cudaStream_t s);
+                  int iterations, int orderMode, int coopBlocks, bool blockPath, DevStats *st, Scratch &ws,
+                  cudaStream_t s);
+// Largest manifold count the single-block solver handles, and the largest
+// body index it can key (bodies < 2^20).
+constexpr uint32_t kBlockMaxManifolds = 4096;
+constexpr uint32_t kBlockMaxBodies = 1u << 20;
 int maxCooperativeBlocks(int smCount);
 void launchGeneratePairs(const float4 *in, float4 *out, uint32_t n, cudaStream_t s);
 

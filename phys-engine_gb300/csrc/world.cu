@@ -479,7 +479,7 @@ void World::runPipeline(float dt) {
     launchNarrowphase(w, pb_, mv, mcap_, st, ws_, s);
     PE_CHECK(cudaEventRecordWithFlags(evStage_[3], s, cudaEventRecordExternal));
     launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], cacheView(1 - cache_), &cCount_.ptr[1 - cache_],
-                 cacheCap_, sb_, iterations, orderMode, coopBlocks_, st, ws_, s);
+                 cacheCap_, sb_, iterations, orderMode, coopBlocks_, blockSolver_, st, ws_, s);
     PE_CHECK(cudaEventRecordWithFlags(evStage_[4], s, cudaEventRecordExternal));
     launchIntegratePose(w, s);
     PE_CHECK(cudaEventRecordWithFlags(evStage_[5], s, cudaEventRecordExternal));
@@ -496,21 +496,25 @@ bool World::finishStep() {
                                   (h.err & kErrColors) ? "more than 128 solver colours" :
                                                          "grid cell range exceeds 64 key bits"));
     }
-    bool retry = false;
+    bool retry = false, grew = false;
+    if (h.err & kErrSmallPath) {
+        lastMEstimate_ = h.manifolds;  // the single-block path was too small: full path
+        retry = true;
+    }
     if (h.rawPairs > pairCap_) {
         pairCap_ = grow(h.rawPairs, pairCap_);
-        retry = true;
+        retry = grew = true;
     }
     if (h.gridEntryCount > entryCap_) {
         entryCap_ = grow(h.gridEntryCount, entryCap_);
-        retry = true;
+        retry = grew = true;
     }
     if (h.manifolds > mcap_ || h.pairs > mcap_) {
         mcap_ = grow(std::max(h.manifolds, h.pairs), mcap_);
-        retry = true;
+        retry = grew = true;
     }
     if (retry) {
-        ensureCapacity();
+        if (grew) ensureCapacity();
         return false;
     }
     StepCounters &c = counters_;
@@ -552,7 +556,7 @@ bool World::GraphKey::operator==(const GraphKey &o) const {
     return nb == o.nb && nc == o.nc && pairCap == o.pairCap && entryCap == o.entryCap && mcap == o.mcap &&
            cacheCap == o.cacheCap && dt == o.dt && gx == o.gx && gy == o.gy && gz == o.gz &&
            algorithm == o.algorithm && iterations == o.iterations && orderMode == o.orderMode &&
-           coopBlocks == o.coopBlocks && cellSize == o.cellSize && dense == o.dense &&
+           coopBlocks == o.coopBlocks && blockSolver == o.blockSolver && cellSize == o.cellSize && dense == o.dense &&
            localIdentity == o.localIdentity && forces == o.forces;
 }
 
@@ -572,6 +576,7 @@ World::GraphKey World::currentKey(float dt) const {
     k.iterations = iterations;
     k.orderMode = orderMode;
     k.coopBlocks = coopBlocks_;
+    k.blockSolver = blockSolver_;
     k.cellSize = cellSize;
     k.dense = dense_;
     k.localIdentity = localIdentity_;
@@ -595,6 +600,9 @@ unsigned long long World::launchStep(float dt) {
     uint32_t want = (lastMEstimate_ + 1023) / 1024, blocks = 1;
     while (blocks < want) blocks <<= 1;
     coopBlocks_ = (int)std::min<uint32_t>(blocks, (uint32_t)maxCooperativeBlocks(smCount_));
+    // Small manifold counts run the single-block solver (with headroom over
+    // the last step's count; an overflow re-runs the step on the full path).
+    blockSolver_ = lastMEstimate_ + lastMEstimate_ / 4 + 64 <= kBlockMaxManifolds && nb_ <= kBlockMaxBodies;
     if (graphsDisabled_) {
         const unsigned long long l0 = g_kernelLaunches;
         runPipeline(dt);
@@ -947,8 +955,9 @@ void World::solveOnly(std::vector<float> &recs, uint32_t count, float dt, int it
     uint32_t want = (count + 1023) / 1024, blocks = 1;
     while (blocks < want) blocks <<= 1;
     blocks = std::min<uint32_t>(blocks, (uint32_t)maxCooperativeBlocks(smCount_));
+    const bool block = count <= kBlockMaxManifolds && nb_ <= kBlockMaxBodies;
     launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], cacheView(1 - cache_), &cCount_.ptr[1 - cache_],
-                 cacheCap_, sb_, iters, mode, (int)blocks, st, ws_, s);
+                 cacheCap_, sb_, iters, mode, (int)blocks, block, st, ws_, s);
     PE_CHECK(cudaMemcpyAsync(hostStats_, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
     PE_CHECK(cudaStreamSynchronize(s));
     if (hostStats_->err & (kErrTimeout | kErrColors)) throw std::runtime_error("solve failed on the device");

@@ -225,6 +225,7 @@ class World {
         uint32_t nb, nc, pairCap, entryCap, mcap, cacheCap;
         float dt, gx, gy, gz;
         int algorithm, iterations, orderMode, coopBlocks;
+        bool blockSolver;
         double cellSize;
         bool dense, localIdentity, forces;
         bool operator==(const GraphKey &o) const;
@@ -236,6 +237,7 @@ class World {
     bool lastGraphed_ = false;
     std::string graphError_;
     int coopBlocks_ = 1;
+    bool blockSolver_ = true;
     GraphKey currentKey(float dt) const;
     void dropGraphs();
     unsigned long long launchStep(float dt);
