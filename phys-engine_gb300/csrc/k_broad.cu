@@ -5,6 +5,7 @@
 // reference's lexicographic order by a radix sort of 64-bit pair keys
 // (first << 32 | second), deduplicated, mapped to collider slots and filtered
 // of same-body pairs (src/world/physics_world.cpp:623-633).
+#include "pe_block.cuh"
 #include "pe_kernels.cuh"
 #include "pe_stages.h"
 
@@ -18,11 +19,13 @@ __device__ __forceinline__ bool overlaps(const float4 &amn, const float4 &amx, c
     // Aabb::overlaps (include/phys/collision/aabb.hpp:15-19)
     return amn.x <= bmx.x && amx.x >= bmn.x && amn.y <= bmx.y && amx.y >= bmn.y && amn.z <= bmx.z && amx.z >= bmn.z;
 }
+// Pair key = (first << bits) | second with first < second, so a plain integer
+// sort gives the reference's lexicographic order (broadphase.cpp:18-60).
 __device__ __forceinline__ void emitPair(uint32_t a, uint32_t b, unsigned long long *keys, uint32_t cap,
-                                         uint32_t *count) {
+                                         uint32_t *count, uint32_t bits) {
     uint32_t lo = a < b ? a : b, hi = a < b ? b : a;
     uint32_t slot = aggregatedAppend(count);
-    if (slot < cap) keys[slot] = ((unsigned long long)lo << 32) | hi;
+    if (slot < cap) keys[slot] = ((unsigned long long)lo << bits) | hi;
 }
 
 __global__ void k_step_init(DevStats *st, uint32_t inputCount) {
@@ -73,7 +76,8 @@ __global__ void k_sap_window(const uint32_t *d_n, const float *sMinX, const floa
 // consecutive (entry, partner) items.
 constexpr uint32_t kSweepChunk = 16;
 __global__ void k_sap_emit(const uint32_t *d_n, const uint32_t *off, const uint32_t *len, const float4 *sYZ,
-                           const uint32_t *sIdx, unsigned long long *keys, uint32_t cap, DevStats *st) {
+                           const uint32_t *sIdx, unsigned long long *keys, uint32_t cap, uint32_t bits,
+                           DevStats *st) {
     const uint32_t n = *d_n;
     const uint32_t W = st->windowWork;
     // The flattened window work is indexed in 32 bits; beyond that the sweep
@@ -102,7 +106,7 @@ __global__ void k_sap_emit(const uint32_t *d_n, const uint32_t *off, const uint3
                 atomicOr(&st->err, kErrEntryCapacity);
                 break;
             }
-            if (overlapYZ(f, sYZ[j])) emitPair(fi, sIdx[j], keys, cap, &st->rawPairs);
+            if (overlapYZ(f, sYZ[j])) emitPair(fi, sIdx[j], keys, cap, &st->rawPairs, bits);
             if (++j == end && w + 1 < wEnd) {
                 do { ++i; } while (i + 1 < n && len[i] == 0);
                 j = i + 1;
@@ -139,15 +143,28 @@ __global__ void k_grid_cellsize(const unsigned long long *sortedWidths, const ui
     st->cellSize = cell;
 }
 
+// floor((double)x / cell) exactly as the reference computes it
+// (broadphase.cpp:66-71).  x * (1/cell) is within a few ulps of the rounded
+// quotient; away from integer boundaries both floor to the same value, so the
+// division only runs when the product lies within 1e-9 (relative) of one.
+__device__ __forceinline__ double cellFloor(float x, double cell, double inv) {
+    const double q = (double)x * inv;
+    const double f = floor(q);
+    const double tol = 1e-9 * fmax(1.0, fabs(q));
+    if (q - f > tol && (f + 1.0) - q > tol && isfinite(q)) return f;
+    return floor((double)x / cell);
+}
+
 // gridRange (broadphase.cpp:62-88) per input box.
 __global__ void k_grid_range(BroadInput in, DevStats *st, int4 *firstCell, uint32_t *cellCount, uint8_t *inGrid,
                              uint32_t *overflow) {
     const uint32_t n = *in.d_n;
     const double cell = st->cellSize;
+    const double inv = 1.0 / cell;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 mn = in.mn[i], mx = in.mx[i];
-        double lower[3] = {floor((double)mn.x / cell), floor((double)mn.y / cell), floor((double)mn.z / cell)};
-        double upper[3] = {floor((double)mx.x / cell), floor((double)mx.y / cell), floor((double)mx.z / cell)};
+        double lower[3] = {cellFloor(mn.x, cell, inv), cellFloor(mn.y, cell, inv), cellFloor(mn.z, cell, inv)};
+        double upper[3] = {cellFloor(mx.x, cell, inv), cellFloor(mx.y, cell, inv), cellFloor(mx.z, cell, inv)};
         uint64_t total = 1;
         int32_t first[3];
         int counts[3];
@@ -192,19 +209,31 @@ __global__ void k_grid_range(BroadInput in, DevStats *st, int4 *firstCell, uint3
 
 __device__ __forceinline__ uint32_t bitsFor(uint32_t range) { return range ? 32u - __clz(range) : 0u; }
 
+// Cell (x, y, z) as offsets from the lowest cell, packed x | y | z.
+__device__ __forceinline__ unsigned long long packCell(int x, int y, int z, const DevStats *st, uint32_t by,
+                                                       uint32_t bz) {
+    const unsigned long long dx = (uint32_t)(x - st->cellLo[0]);
+    const unsigned long long dy = (uint32_t)(y - st->cellLo[1]);
+    const unsigned long long dz = (uint32_t)(z - st->cellLo[2]);
+    return (dx << (by + bz)) | (dy << bz) | dz;
+}
+
 // One entry per covered cell; key = packed cell offsets from the lowest cell,
 // so equal cells are adjacent after the sort (cell order is irrelevant: the
 // reference only groups entries by cell before the final pair sort).
 __global__ void k_grid_entries(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const uint32_t *entryOff,
-                               unsigned long long *keys, uint32_t *vals, uint32_t cap, DevStats *st) {
+                               unsigned long long *keys, uint32_t *vals, uint32_t cap, uint32_t sortBits,
+                               DevStats *st) {
     const uint32_t n = *in.d_n;
     // No box in the grid: the bounds keep their sentinels and there is nothing to write.
     if (st->cellLo[0] > st->cellHi[0]) return;
     const uint32_t bx = bitsFor((uint32_t)(st->cellHi[0] - st->cellLo[0]));
     const uint32_t by = bitsFor((uint32_t)(st->cellHi[1] - st->cellLo[1]));
     const uint32_t bz = bitsFor((uint32_t)(st->cellHi[2] - st->cellLo[2]));
-    if (bx + by + bz > 64) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&st->err, kErrEntryCapacity);
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->cellKeyBits = bx + by + bz;
+    if (bx + by + bz > sortBits) {
+        // Wider than this launch sorts: the host re-runs the step with the width recorded above.
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&st->err, bx + by + bz > 64 ? kErrEntryCapacity : kErrSmallPath);
         return;
     }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -216,10 +245,7 @@ __global__ void k_grid_entries(BroadInput in, const int4 *firstCell, const uint8
             for (int y = 0; y < cy; ++y)
                 for (int z = 0; z < cz; ++z, ++e) {
                     if (e >= cap) continue;
-                    unsigned long long dx = (uint32_t)(f.x + x - st->cellLo[0]);
-                    unsigned long long dy = (uint32_t)(f.y + y - st->cellLo[1]);
-                    unsigned long long dz = (uint32_t)(f.z + z - st->cellLo[2]);
-                    keys[e] = (bx ? dx << (by + bz) : 0ull) | (by ? dy << bz : 0ull) | dz;
+                    keys[e] = packCell(f.x + x, f.y + y, f.z + z, st, by, bz);
                     vals[e] = i;
                 }
     }
@@ -227,26 +253,38 @@ __global__ void k_grid_entries(BroadInput in, const int4 *firstCell, const uint8
 
 // Per-cell all pairs (broadphase.cpp:152-160): entry e against every later
 // entry of its cell.
-__global__ void k_grid_cell_pairs(const uint32_t *d_entries, const unsigned long long *ekeys, const uint32_t *evals,
-                                  BroadInput in, unsigned long long *pkeys, uint32_t cap, DevStats *st) {
-    const uint32_t E = *d_entries;
+// An overlapping pair is emitted only from the lowest cell both boxes cover, so
+// the list is already free of the duplicates the reference removes with
+// sort + unique (broadphase.cpp:169-172); every check is still counted.
+__global__ void k_grid_cell_pairs(const uint32_t *d_entries, uint32_t ecap, const unsigned long long *ekeys,
+                                  const uint32_t *evals, const int4 *firstCell, BroadInput in,
+                                  unsigned long long *pkeys, uint32_t cap, uint32_t bits, DevStats *st) {
+    // Entries were not written this attempt (key width refused): nothing to scan.
+    if (st->err & (kErrSmallPath | kErrEntryCapacity)) return;
+    const uint32_t E = min(*d_entries, ecap);
+    const uint32_t by = bitsFor((uint32_t)(st->cellHi[1] - st->cellLo[1]));
+    const uint32_t bz = bitsFor((uint32_t)(st->cellHi[2] - st->cellLo[2]));
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x) {
         const unsigned long long key = ekeys[e];
         const uint32_t a = evals[e];
         const float4 amn = in.mn[a], amx = in.mx[a];
+        const int4 fa = firstCell[a];
         uint64_t cmp = 0;
         for (uint32_t f = e + 1; f < E && ekeys[f] == key; ++f) {
             ++cmp;
             const uint32_t b = evals[f];
-            if (overlaps(amn, amx, in.mn[b], in.mx[b])) emitPair(a, b, pkeys, cap, &st->rawPairs);
+            if (!overlaps(amn, amx, in.mn[b], in.mx[b])) continue;
+            const int4 fb = firstCell[b];
+            const unsigned long long low = packCell(max(fa.x, fb.x), max(fa.y, fb.y), max(fa.z, fb.z), st, by, bz);
+            if (low == key) emitPair(a, b, pkeys, cap, &st->rawPairs, bits);
         }
-        if (cmp) atomicAdd(&st->gridComparisons, (unsigned long long)cmp);
+        aggregatedAdd64(&st->gridComparisons, cmp);
     }
 }
 
 // Overflow boxes against all others (broadphase.cpp:162-166).
 __global__ void k_grid_overflow_pairs(BroadInput in, const uint32_t *overflow, const uint8_t *inGrid,
-                                      unsigned long long *pkeys, uint32_t cap, DevStats *st) {
+                                      unsigned long long *pkeys, uint32_t cap, uint32_t bits, DevStats *st) {
     const uint32_t n = *in.d_n;
     const uint32_t F = st->overflowCount;
     const uint64_t total = (uint64_t)F * n;
@@ -256,20 +294,22 @@ __global__ void k_grid_overflow_pairs(BroadInput in, const uint32_t *overflow, c
         const uint32_t f = overflow[k];
         if (f == s || !(inGrid[s] || f < s)) continue;
         aggregatedAdd64(&st->gridComparisons, 1ull);
-        if (overlaps(in.mn[f], in.mx[f], in.mn[s], in.mx[s])) emitPair(f, s, pkeys, cap, &st->rawPairs);
+        if (overlaps(in.mn[f], in.mx[f], in.mn[s], in.mx[s])) emitPair(f, s, pkeys, cap, &st->rawPairs, bits);
     }
 }
 
 // ------------------------------------------------------------ finalize -----
-__global__ void k_pairs_flags(const uint32_t *d_raw, const unsigned long long *keys, const uint32_t *inSlot,
-                              const uint32_t *cbody, const uint32_t *cbgen, uint32_t *flags, DevStats *st) {
-    const uint32_t n = *d_raw;
+__global__ void k_pairs_flags(const uint32_t *d_raw, uint32_t cap, uint32_t bits, const unsigned long long *keys,
+                              const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen, uint32_t *flags,
+                              DevStats *st) {
+    const uint32_t n = min(*d_raw, cap);
+    const unsigned long long mask = (1ull << bits) - 1ull;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         unsigned long long key = keys[k];
         bool keep = !(k > 0 && keys[k - 1] == key);
         if (keep) {
             aggregatedAppend(&st->uniquePairs);
-            uint32_t a = (uint32_t)(key >> 32), b = (uint32_t)key;
+            uint32_t a = (uint32_t)(key >> bits), b = (uint32_t)(key & mask);
             if (inSlot) {
                 a = inSlot[a];
                 b = inSlot[b];
@@ -280,13 +320,15 @@ __global__ void k_pairs_flags(const uint32_t *d_raw, const unsigned long long *k
     }
 }
 
-__global__ void k_pairs_scatter(const uint32_t *d_raw, const unsigned long long *keys, const uint32_t *inSlot,
-                                const uint32_t *flags, const uint32_t *pos, uint32_t *pairA, uint32_t *pairB) {
-    const uint32_t n = *d_raw;
+__global__ void k_pairs_scatter(const uint32_t *d_raw, uint32_t cap, uint32_t bits, const unsigned long long *keys,
+                                const uint32_t *inSlot, const uint32_t *flags, const uint32_t *pos, uint32_t *pairA,
+                                uint32_t *pairB) {
+    const uint32_t n = min(*d_raw, cap);
+    const unsigned long long mask = (1ull << bits) - 1ull;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         if (!flags[k]) continue;
         unsigned long long key = keys[k];
-        uint32_t a = (uint32_t)(key >> 32), b = (uint32_t)key;
+        uint32_t a = (uint32_t)(key >> bits), b = (uint32_t)(key & mask);
         if (inSlot) {
             a = inSlot[a];
             b = inSlot[b];
@@ -335,14 +377,14 @@ void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, Broad
     k_sap_window<<<gridFor(in.maxN), 256, 0, s>>>(in.d_n, bb.sMinX, bb.sMaxX, bb.len, st);
     PE_LAUNCHED();
     launchScanExclusive(bb.len, bb.off, in.d_n, in.maxN, &st->windowWork, ws, err, s);
-    k_sap_emit<<<152 * 8, 256, 0, s>>>(in.d_n, bb.off, bb.len, bb.sYZ, bb.sIdx, pb.keys, pb.cap, st);
+    k_sap_emit<<<152 * 8, 256, 0, s>>>(in.d_n, bb.off, bb.len, bb.sYZ, bb.sIdx, pb.keys, pb.cap, pb.bits, st);
     PE_LAUNCHED();
 }
 
 void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBuffers &pb, DevStats *st, Scratch &ws,
                 cudaStream_t s) {
     uint32_t *err = &st->err;
-    // counters[0] counts the non-zero widths of this call; counters[1] is the clamped entry count.
+    // counters[0] counts the non-zero widths of this call.
     PE_CHECK(cudaMemsetAsync(bb.counters, 0, 4 * sizeof(uint32_t), s));
     if (fixedCell <= 0.0) {
         k_grid_widths<<<gridFor(in.maxN), 256, 0, s>>>(in, bb.widthKeys, &bb.counters[0]);
@@ -356,28 +398,91 @@ void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBu
     PE_LAUNCHED();
     launchScanExclusive(bb.cellCount, bb.entryOff, in.d_n, in.maxN, &st->gridEntryCount, ws, err, s);
     k_grid_entries<<<gridFor(in.maxN), 256, 0, s>>>(in, bb.firstCell, bb.inGrid, bb.entryOff, bb.entryKeys,
-                                                    bb.entryVals, bb.entryCap, st);
+                                                    bb.entryVals, bb.entryCap, bb.keyBits, st);
     PE_LAUNCHED();
-    launchClamp(&st->gridEntryCount, bb.entryCap, &bb.counters[1], s);
     launchRadixSort<unsigned long long>(bb.entryKeys, bb.entryKeysTmp, bb.entryVals, bb.entryValsTmp,
-                                        &bb.counters[1], bb.entryCap, 0, 64, ws, err, s);
-    k_grid_cell_pairs<<<gridFor(bb.entryCap), 256, 0, s>>>(&bb.counters[1], bb.entryKeys, bb.entryVals, in, pb.keys,
-                                                           pb.cap, st);
+                                        &st->gridEntryCount, bb.entryCap, 0, (int)bb.keyBits, ws, err, s);
+    k_grid_cell_pairs<<<gridFor(bb.entryCap), 256, 0, s>>>(&st->gridEntryCount, bb.entryCap, bb.entryKeys,
+                                                           bb.entryVals, bb.firstCell, in, pb.keys, pb.cap, pb.bits,
+                                                           st);
     PE_LAUNCHED();
-    k_grid_overflow_pairs<<<152 * 4, 256, 0, s>>>(in, bb.overflow, bb.inGrid, pb.keys, pb.cap, st);
+    k_grid_overflow_pairs<<<152 * 4, 256, 0, s>>>(in, bb.overflow, bb.inGrid, pb.keys, pb.cap, pb.bits, st);
     PE_LAUNCHED();
+}
+
+// Single-block finalize for up to kBlockMaxPairs raw pairs: sort, dedup, slot
+// mapping, same-body filter and order-preserving compaction in shared memory.
+__global__ void __launch_bounds__(1024)
+k_pairs_block(const unsigned long long *keys, uint32_t bits, const uint32_t *inSlot, const uint32_t *cbody,
+              const uint32_t *cbgen, uint32_t *pairA, uint32_t *pairB, DevStats *st) {
+    extern __shared__ unsigned long long s_keys[];  // kBlockMaxPairs
+    uint32_t *s_flag = reinterpret_cast<uint32_t *>(s_keys + kBlockMaxPairs);
+    __shared__ uint32_t s_scan[40];
+    const uint32_t n = st->rawPairs;
+    if (n > kBlockMaxPairs) {
+        if (threadIdx.x == 0) atomicOr(&st->err, kErrSmallPath);
+        return;
+    }
+    const uint32_t n2 = nextPow2(n > 0 ? n : 1);
+    for (uint32_t i = threadIdx.x; i < n2; i += blockDim.x) s_keys[i] = i < n ? keys[i] : ~0ull;
+    __syncthreads();
+    blockBitonicSort<unsigned long long>(s_keys, n2);
+    const unsigned long long mask = (1ull << bits) - 1ull;
+    uint32_t unique = 0;
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+        const unsigned long long key = s_keys[k];
+        bool keep = !(k > 0 && s_keys[k - 1] == key);
+        if (keep) {
+            ++unique;
+            uint32_t a = (uint32_t)(key >> bits), b = (uint32_t)(key & mask);
+            if (inSlot) {
+                a = inSlot[a];
+                b = inSlot[b];
+            }
+            if (cbody && cbody[a] == cbody[b] && cbgen[a] == cbgen[b]) keep = false;
+        }
+        s_flag[k] = keep ? 1u : 0u;
+    }
+    if (unique) atomicAdd(&st->uniquePairs, unique);
+    __syncthreads();
+    const uint32_t total = blockExclusiveScanArray(s_flag, n, s_scan);
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+        const uint32_t next = k + 1 < n ? s_flag[k + 1] : total;
+        if (next == s_flag[k]) continue;
+        const unsigned long long key = s_keys[k];
+        uint32_t a = (uint32_t)(key >> bits), b = (uint32_t)(key & mask);
+        if (inSlot) {
+            a = inSlot[a];
+            b = inSlot[b];
+        }
+        pairA[s_flag[k]] = a;
+        pairB[s_flag[k]] = b;
+    }
+    if (threadIdx.x == 0) st->pairs = total;
 }
 
 void launchPairsFinalize(const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen, PairBuffers &pb,
                          DevStats *st, Scratch &ws, cudaStream_t s) {
     uint32_t *err = &st->err;
-    launchClamp(&st->rawPairs, pb.cap, &pb.counters[0], s);
-    launchRadixSort<unsigned long long>(pb.keys, pb.keysTmp, nullptr, nullptr, &pb.counters[0], pb.cap, 0, 64, ws,
-                                        err, s);
-    k_pairs_flags<<<gridFor(pb.cap), 256, 0, s>>>(&pb.counters[0], pb.keys, inSlot, cbody, cbgen, pb.flags, st);
+    if (pb.blockPath) {
+        static bool configured = false;
+        const size_t smem = kBlockMaxPairs * (sizeof(unsigned long long) + sizeof(uint32_t));
+        if (!configured) {
+            PE_CHECK(cudaFuncSetAttribute(k_pairs_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            configured = true;
+        }
+        k_pairs_block<<<1, 1024, smem, s>>>(pb.keys, pb.bits, inSlot, cbody, cbgen, pb.a, pb.b, st);
+        PE_LAUNCHED();
+        return;
+    }
+    launchRadixSort<unsigned long long>(pb.keys, pb.keysTmp, nullptr, nullptr, &st->rawPairs, pb.cap, 0,
+                                        2 * (int)pb.bits, ws, err, s);
+    k_pairs_flags<<<gridFor(pb.cap), 256, 0, s>>>(&st->rawPairs, pb.cap, pb.bits, pb.keys, inSlot, cbody, cbgen,
+                                                  pb.flags, st);
     PE_LAUNCHED();
-    launchScanExclusive(pb.flags, pb.pos, &pb.counters[0], pb.cap, &st->pairs, ws, err, s);
-    k_pairs_scatter<<<gridFor(pb.cap), 256, 0, s>>>(&pb.counters[0], pb.keys, inSlot, pb.flags, pb.pos, pb.a, pb.b);
+    launchScanExclusive(pb.flags, pb.pos, &st->rawPairs, pb.cap, &st->pairs, ws, err, s);
+    k_pairs_scatter<<<gridFor(pb.cap), 256, 0, s>>>(&st->rawPairs, pb.cap, pb.bits, pb.keys, inSlot, pb.flags,
+                                                    pb.pos, pb.a, pb.b);
     PE_LAUNCHED();
 }
 

@@ -37,10 +37,11 @@ k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *_
               const uint32_t *d_pairs, ManifoldView out, uint32_t mcap, DevStats *st, unsigned long long *state,
               uint32_t *counter) {
     __shared__ uint32_t s_tile, s_scan[9], s_prefix;
+    const uint32_t P = min(*d_pairs, mcap);
+    const uint32_t ntiles = max((P + kNarrowThreads - 1) / kNarrowThreads, 1u);
+    for (;;) {
     const uint32_t tile = takeTile(counter, &s_tile);
-    const uint32_t P = *d_pairs;
-    const uint32_t ntiles = (P + kNarrowThreads - 1) / kNarrowThreads;
-    if (tile >= (ntiles > 0 ? ntiles : 1u)) return;
+    if (tile >= ntiles) return;
     const uint32_t p = tile * kNarrowThreads + threadIdx.x;
 
     LocalManifold lm;
@@ -125,16 +126,19 @@ k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *_
         aggregatedAppend(&st->points);
         if (lm.count > 1) atomicAdd(&st->points, lm.count - 1);
     }
-    if (threadIdx.x == 0 && tile + 1 >= ntiles) st->manifolds = s_prefix + total;
+    if (threadIdx.x == 0 && tile + 1 == ntiles) st->manifolds = s_prefix + total;
+    __syncthreads();
+    }
 }
 
 void launchNarrowphase(const WorldView &w, const PairBuffers &pb, const ManifoldView &mv, uint32_t mcap, DevStats *st,
                        Scratch &ws, cudaStream_t s) {
     uint32_t tiles = (pb.cap + kNarrowThreads - 1) / kNarrowThreads;
     if (tiles == 0) tiles = 1;
-    PE_CHECK(cudaMemsetAsync(ws.scanState, 0, sizeof(unsigned long long) * tiles + 8, s));
-    k_narrowphase<<<tiles, kNarrowThreads, 0, s>>>(w, pb.a, pb.b, &st->pairs, mv, mcap, st, ws.scanState,
-                                                    (uint32_t *)(ws.scanState + tiles));
+    PE_CHECK(cudaMemsetAsync(ws.scanState, 0, sizeof(unsigned long long) * (tiles + 1), s));
+    const uint32_t grid = tiles < 152u * 8u ? tiles : 152u * 8u;
+    k_narrowphase<<<grid, kNarrowThreads, 0, s>>>(w, pb.a, pb.b, &st->pairs, mv, mcap, st, ws.scanState,
+                                                   (uint32_t *)(ws.scanState + tiles));
     PE_LAUNCHED();
 }
 

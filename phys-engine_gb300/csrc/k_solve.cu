@@ -479,11 +479,12 @@ __global__ void k_impulses_out(SolveArgs a) {
 // ---------------------------------------------------------- cache rebuild --
 // Next cache (:623-681): every point of every solved manifold, sorted by body
 // pair, stable with respect to solve order.
-__global__ void k_cache_keys(SolveArgs a) {
+// Sort key (bodyA << bits) | bodyB: the (bodyA, bodyB) order of the cache.
+__global__ void k_cache_keys(SolveArgs a, uint32_t bits) {
     const uint32_t M = min(a.st->manifolds, a.mcap);
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < M; k += gridDim.x * blockDim.x) {
         const uint32_t m = a.sb.order[k];
-        a.sb.cacheKeys[k] = ((unsigned long long)a.mv.bodyA[m] << 32) | a.mv.bodyB[m];
+        a.sb.cacheKeys[k] = ((unsigned long long)a.mv.bodyA[m] << bits) | a.mv.bodyB[m];
         a.sb.cacheVals[k] = m;
     }
 }
@@ -518,24 +519,8 @@ __device__ __forceinline__ void cacheWriteManifold(const SolveArgs &a, const Cac
 
 __global__ void k_cache_write(SolveArgs a, CacheView nc, uint32_t cacheCap) {
     const uint32_t M = min(a.st->manifolds, a.mcap);
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < M; k += gridDim.x * blockDim.x) {
-        const uint32_t m = a.sb.cacheVals[k];
-        const unsigned long long key = a.sb.cacheKeys[k];
-        const unsigned long long gens = ((unsigned long long)a.mv.genA[m] << 32) | a.mv.genB[m];
-        const uint32_t base = a.sb.cacheOff[k];
-        const uint32_t npts = a.sb.cacheCounts[k];
-        for (uint32_t p = 0; p < npts; ++p) {
-            const uint32_t e = base + p;
-            if (e >= cacheCap) break;
-            const float4 aa = a.mv.anchorA[4 * m + p], ab = a.mv.anchorB[4 * m + p];
-            const float4 imp = a.mv.impulse[4 * m + p];
-            nc.key[e] = key;
-            nc.gens[e] = gens;
-            nc.anchorA[e] = make_float4(aa.x, aa.y, aa.z, imp.x);
-            nc.anchorB[e] = make_float4(ab.x, ab.y, ab.z, imp.y);
-            nc.tangent2[e] = imp.z;
-        }
-    }
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < M; k += gridDim.x * blockDim.x)
+        cacheWriteManifold(a, nc, cacheCap, a.sb.cacheVals[k], a.sb.cacheOff[k], a.sb.cacheCounts[k]);
 }
 
 
@@ -776,11 +761,9 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
     if (!serial) launchCooperative((const void *)k_color, coopBlocks, a, s);
     k_order_init<<<gridFor(mcap), 256, 0, s>>>(a, serial ? 1 : 0);
     PE_LAUNCHED();
-    if (!serial) {
-        launchClamp(&st->manifolds, mcap, &sb.counters[1], s);
-        launchRadixSort<uint32_t>(sb.orderKeys, sb.orderKeysTmp, sb.order, sb.orderTmp, &sb.counters[1], mcap, 0, 8,
+    if (!serial)
+        launchRadixSort<uint32_t>(sb.orderKeys, sb.orderKeysTmp, sb.order, sb.orderTmp, &st->manifolds, mcap, 0, 8,
                                   ws, err, s);
-    }
     k_prepare<<<gridFor(mcap), 256, 0, s>>>(a);
     PE_LAUNCHED();
     if (serial) {
@@ -790,14 +773,17 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
     else launchCooperative((const void *)k_solve_colored, coopBlocks, a, s);
     k_impulses_out<<<gridFor(mcap), 256, 0, s>>>(a);
     PE_LAUNCHED();
-    k_cache_keys<<<gridFor(mcap), 256, 0, s>>>(a);
+    uint32_t keyBits = 1;
+    while (keyBits < 32 && (1ull << keyBits) < (unsigned long long)(w.nb > 2 ? w.nb : 2)) ++keyBits;
+    k_cache_keys<<<gridFor(mcap), 256, 0, s>>>(a, keyBits);
     PE_LAUNCHED();
-    launchClamp(&st->manifolds, mcap, &sb.counters[1], s);
+    uint32_t bodyBits = 1;
+    while (bodyBits < 32 && (1ull << bodyBits) < (unsigned long long)(w.nb > 2 ? w.nb : 2)) ++bodyBits;
     launchRadixSort<unsigned long long>(sb.cacheKeys, sb.cacheKeysTmp, sb.cacheVals, sb.cacheValsTmp,
-                                        &sb.counters[1], mcap, 0, 64, ws, err, s);
+                                        &st->manifolds, mcap, 0, 2 * (int)bodyBits, ws, err, s);
     k_cache_counts<<<gridFor(mcap), 256, 0, s>>>(a);
     PE_LAUNCHED();
-    launchScanExclusive(sb.cacheCounts, sb.cacheOff, &sb.counters[1], mcap, newCacheCount, ws, err, s);
+    launchScanExclusive(sb.cacheCounts, sb.cacheOff, &st->manifolds, mcap, newCacheCount, ws, err, s);
     k_cache_write<<<gridFor(mcap), 256, 0, s>>>(a, newCache, cacheCap);
     PE_LAUNCHED();
 }

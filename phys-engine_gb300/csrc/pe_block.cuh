@@ -7,7 +7,7 @@ namespace pe {
 
 // Sorts s[0, n) ascending in shared memory; n is a power of two (pad the tail
 // with the key type's maximum).  All threads of the block call it.
-template <class K> __device__ void blockBitonicSort(K *s, uint32_t n) {
+template <class K> __device__ __forceinline__ void blockBitonicSort(K *s, uint32_t n) {
     for (uint32_t k = 2; k <= n; k <<= 1) {
         for (uint32_t j = k >> 1; j > 0; j >>= 1) {
             for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
@@ -34,7 +34,7 @@ __device__ __forceinline__ uint32_t nextPow2(uint32_t v) {
 
 // In-place exclusive scan of s[0, n) (u32) by one block; returns the total.
 // scratch needs blockDim.x / 32 + 1 entries.  All threads call it.
-__device__ uint32_t blockExclusiveScanArray(uint32_t *s, uint32_t n, uint32_t *scratch) {
+__device__ __forceinline__ uint32_t blockExclusiveScanArray(uint32_t *s, uint32_t n, uint32_t *scratch) {
     const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
     const uint32_t b = threadIdx.x * per, e = min(n, b + per);
     uint32_t sum = 0;

@@ -86,6 +86,7 @@ struct DevStats {
     uint32_t sel;            // radix-sort buffer selector (device-side pass skipping)
     uint32_t windowWork;     // SAP flattened window work
     uint32_t solved;         // manifolds whose bodies are valid (prepared)
+    uint32_t cellKeyBits;    // bits of the packed grid cell key this step needed
     int32_t cellLo[3];
     int32_t cellHi[3];
 };

@@ -26,12 +26,15 @@ struct BroadBuffers {
     unsigned long long *entryKeys, *entryKeysTmp;
     uint32_t *entryVals, *entryValsTmp;
     uint32_t entryCap;
+    uint32_t keyBits;    // cell-key bits sorted this step (from the previous step's cell range)
     uint32_t *counters;  // [4] device scratch counters
 };
 
 struct PairBuffers {
     unsigned long long *keys, *keysTmp;
     uint32_t cap;
+    uint32_t bits;         // pair key = (first << bits) | second
+    bool blockPath;        // single-block finalize (raw pairs <= kBlockMaxPairs)
     uint32_t *flags, *pos;
     uint32_t *a, *b;       // candidate pairs (collider slots), lexicographic
     uint32_t *counters;    // [4]
@@ -64,6 +67,7 @@ struct SolverBuffers {
 };
 
 constexpr int kMaxColors = 128;
+constexpr uint32_t kBlockMaxPairs = 16384;
 constexpr int kPreparedVec4 = 10;
 
 void launchStepInit(DevStats *st, uint32_t inputCount, cudaStream_t s);

@@ -1,4 +1,10 @@
 // Scan and radix-sort kernels (see pe_prims.cuh) and their stream launchers.
+//
+// Both run as persistent grids: a fixed number of blocks (independent of the
+// buffer capacity) loop over tiles taken from an atomic counter, so a launch
+// sized for a large buffer costs nothing when the live count is small.  Tile
+// ids are taken in launch order by running blocks, so the decoupled look-back
+// of a tile only ever waits on tiles that are being processed.
 #include <algorithm>
 
 #include "pe_engine.h"
@@ -8,60 +14,80 @@ namespace pe {
 
 unsigned long long g_kernelLaunches = 0;
 
+namespace {
+constexpr uint32_t kPersistentBlocks = 152 * 4;
+inline uint32_t persistentGrid(uint32_t tiles) { return std::max<uint32_t>(1, std::min(tiles, kPersistentBlocks)); }
+__device__ __forceinline__ uint32_t liveCount(const uint32_t *d_n, uint32_t cap) {
+    if (!d_n) return cap;
+    const uint32_t n = *d_n;
+    return n < cap ? n : cap;
+}
+} // namespace
+
 // ---------------------------------------------------------------------------
 // Exclusive scan (u32), one pass with decoupled look-back.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kScanThreads)
-k_scan_exclusive(const uint32_t *in, uint32_t *out, const uint32_t *d_n, uint32_t n_host,
-                 unsigned long long *state, uint32_t *counter, uint32_t *total, uint32_t *err) {
+k_scan_exclusive(const uint32_t *in, uint32_t *out, const uint32_t *d_n, uint32_t cap, unsigned long long *state,
+                 uint32_t *counter, uint32_t *total, uint32_t *err) {
     __shared__ uint32_t s_tile, s_scan[9], s_prefix;
-    uint32_t tile = takeTile(counter, &s_tile);
-    const uint32_t n = d_n ? *d_n : n_host;
-    const uint32_t ntiles = (n + kScanTile - 1) / kScanTile;
-    if (tile >= (ntiles > 0 ? ntiles : 1u)) return;
-    const uint32_t i0 = tile * kScanTile + threadIdx.x * kScanItems;
-    uint32_t v[kScanItems];
-    uint32_t sum = 0;
+    const uint32_t n = liveCount(d_n, cap);
+    const uint32_t ntiles = max((n + kScanTile - 1) / kScanTile, 1u);
+    for (;;) {
+        const uint32_t tile = takeTile(counter, &s_tile);
+        if (tile >= ntiles) return;
+        const uint32_t i0 = tile * kScanTile + threadIdx.x * kScanItems;
+        uint32_t v[kScanItems];
+        uint32_t sum = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        v[k] = (i0 + k < n) ? in[i0 + k] : 0u;
-        sum += v[k];
-    }
-    uint32_t agg;
-    uint32_t excl = blockExclusiveScan(sum, agg, s_scan);
-    if (threadIdx.x == 0) s_prefix = lookbackExclusive(state, tile, agg, err);
-    __syncthreads();
-    uint32_t run = s_prefix + excl;
+        for (int k = 0; k < kScanItems; ++k) {
+            v[k] = (i0 + k < n) ? in[i0 + k] : 0u;
+            sum += v[k];
+        }
+        uint32_t agg;
+        const uint32_t excl = blockExclusiveScan(sum, agg, s_scan);
+        if (threadIdx.x == 0) s_prefix = lookbackExclusive(state, tile, agg, err);
+        __syncthreads();
+        uint32_t run = s_prefix + excl;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        if (i0 + k < n) out[i0 + k] = run;
-        run += v[k];
+        for (int k = 0; k < kScanItems; ++k) {
+            if (i0 + k < n) out[i0 + k] = run;
+            run += v[k];
+        }
+        if (threadIdx.x == 0 && tile + 1 == ntiles && total) *total = s_prefix + agg;
+        __syncthreads();
     }
-    if (threadIdx.x == 0 && tile + 1 >= ntiles && total) *total = s_prefix + agg;
 }
 
 void launchScanExclusive(const uint32_t *in, uint32_t *out, const uint32_t *d_n, uint32_t max_n, uint32_t *d_total,
                          Scratch &ws, uint32_t *d_err, cudaStream_t s) {
-    uint32_t tiles = (max_n + kScanTile - 1) / kScanTile;
-    if (tiles == 0) tiles = 1;
-    PE_CHECK(cudaMemsetAsync(ws.scanState, 0, sizeof(unsigned long long) * tiles + 8, s));
-    k_scan_exclusive<<<tiles, kScanThreads, 0, s>>>(in, out, d_n, max_n, ws.scanState,
-                                                    (uint32_t *)(ws.scanState + tiles), d_total, d_err);
+    const uint32_t tiles = std::max<uint32_t>((max_n + kScanTile - 1) / kScanTile, 1);
+    PE_CHECK(cudaMemsetAsync(ws.scanState, 0, sizeof(unsigned long long) * (tiles + 1), s));
+    k_scan_exclusive<<<persistentGrid(tiles), kScanThreads, 0, s>>>(in, out, d_n, max_n, ws.scanState,
+                                                                    (uint32_t *)(ws.scanState + tiles), d_total,
+                                                                    d_err);
     PE_LAUNCHED();
 }
 
 // ---------------------------------------------------------------------------
 // Stable LSD radix sort, 8-bit digits, keys u32/u64 with optional u32 values.
 // ---------------------------------------------------------------------------
+// Histograms of every pass in one read of the keys; also clears the look-back
+// state and tile counters of all passes for the live tile count.
 template <class K>
-__global__ void k_radix_hist(const K *keys, const uint32_t *d_n, uint32_t n_host, int bit_begin, int passes,
-                             uint32_t *hist) {
+__global__ void k_radix_hist(const K *keys, const uint32_t *d_n, uint32_t cap, int bit_begin, int passes,
+                             uint32_t *hist, uint32_t *state, size_t passStride, uint32_t *counters) {
     __shared__ uint32_t sh[8 * 256];
     for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) sh[i] = 0;
+    const uint32_t n = liveCount(d_n, cap);
+    const uint32_t ntiles = (n + kSortTile - 1) / kSortTile;
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
+    for (int p = 0; p < passes; ++p)
+        for (uint32_t i = gtid; i < ntiles * 256; i += gstride) state[p * passStride + i] = 0;
+    if (gtid < (uint32_t)passes) counters[gtid] = 0;
     __syncthreads();
-    const uint32_t n = d_n ? *d_n : n_host;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        K k = keys[i];
+    for (uint32_t i = gtid; i < n; i += gstride) {
+        const K k = keys[i];
         for (int p = 0; p < passes; ++p) atomicAdd(&sh[p * 256 + (uint32_t)((k >> (bit_begin + 8 * p)) & 0xFF)], 1u);
     }
     __syncthreads();
@@ -71,21 +97,22 @@ __global__ void k_radix_hist(const K *keys, const uint32_t *d_n, uint32_t n_host
 
 // One 8-bit pass.  The pass reads from buffer sel[pass] and writes the other;
 // a pass whose digit is the same for every key is skipped on the device
-// (sel[pass + 1] = sel[pass]), so key widths need not be known on the host.
+// (sel[pass + 1] = sel[pass]), so key widths need not be exact on the host.
 template <class K, bool VALS>
 __global__ void __launch_bounds__(kSortThreads)
-k_radix_pass(K *buf0, K *buf1, uint32_t *vbuf0, uint32_t *vbuf1, const uint32_t *d_n, uint32_t n_host, int shift,
+k_radix_pass(K *buf0, K *buf1, uint32_t *vbuf0, uint32_t *vbuf1, const uint32_t *d_n, uint32_t cap, int shift,
              const uint32_t *__restrict__ hist, uint32_t *state, uint32_t *counter, uint32_t *sel, int pass,
              uint32_t *err) {
     __shared__ uint32_t s_tile, s_trivial;
     __shared__ uint32_t s_warp[kSortWarps][256];
     __shared__ uint32_t s_tileStart[256];
     __shared__ uint32_t s_base[256];
+    __shared__ uint32_t s_bucket[256];
     __shared__ uint32_t s_scan[9];
     __shared__ K s_keys[kSortTile];
     __shared__ uint32_t s_vals[VALS ? kSortTile : 1];
 
-    const uint32_t n = d_n ? *d_n : n_host;
+    const uint32_t n = liveCount(d_n, cap);
     const uint32_t from = sel[pass];
     if (threadIdx.x == 0) s_trivial = 0;
     __syncthreads();
@@ -100,97 +127,102 @@ k_radix_pass(K *buf0, K *buf1, uint32_t *vbuf0, uint32_t *vbuf1, const uint32_t 
     K *kout = from ? buf0 : buf1;
     const uint32_t *vin = from ? vbuf1 : vbuf0;
     uint32_t *vout = from ? vbuf0 : vbuf1;
-
-    const uint32_t tile = takeTile(counter, &s_tile);
+    {
+        uint32_t tot;
+        s_bucket[threadIdx.x] = blockExclusiveScan(hist[threadIdx.x], tot, s_scan);
+    }
     const uint32_t ntiles = (n + kSortTile - 1) / kSortTile;
-    if (tile >= ntiles) return;
-    const uint32_t base = tile * kSortTile;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads) (&s_warp[0][0])[i] = 0;
-    __syncthreads();
-
-    K key[kSortRounds];
-    uint32_t val[kSortRounds], dig[kSortRounds], rank[kSortRounds];
     const uint32_t lanemask_lt = (1u << lane) - 1u;
+    for (;;) {
+        const uint32_t tile = takeTile(counter, &s_tile);
+        if (tile >= ntiles) return;
+        const uint32_t base = tile * kSortTile;
+        for (int i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads) (&s_warp[0][0])[i] = 0;
+        __syncthreads();
+
+        K key[kSortRounds];
+        uint32_t val[kSortRounds], dig[kSortRounds], rank[kSortRounds];
 #pragma unroll
-    for (int r = 0; r < kSortRounds; ++r) {
-        uint32_t idx = base + warp * (32 * kSortRounds) + r * 32 + lane;
-        bool valid = idx < n;
-        key[r] = valid ? kin[idx] : (K)0;
-        if (VALS) val[r] = valid ? vin[idx] : 0u;
-        dig[r] = valid ? (uint32_t)((key[r] >> shift) & 0xFF) : 0xFFu;
-        uint32_t peers = __match_any_sync(0xffffffffu, dig[r]);
-        uint32_t lower = __popc(peers & lanemask_lt);
-        uint32_t old = s_warp[warp][dig[r]];
-        __syncwarp();
-        if (lower == 0) s_warp[warp][dig[r]] = old + __popc(peers);
-        __syncwarp();
-        rank[r] = old + lower;
-    }
-    __syncthreads();
-    const uint32_t d = threadIdx.x;
-    uint32_t cnt = 0;
+        for (int r = 0; r < kSortRounds; ++r) {
+            const uint32_t idx = base + warp * (32 * kSortRounds) + r * 32 + lane;
+            const bool valid = idx < n;
+            key[r] = valid ? kin[idx] : (K)0;
+            if (VALS) val[r] = valid ? vin[idx] : 0u;
+            dig[r] = valid ? (uint32_t)((key[r] >> shift) & 0xFF) : 0xFFu;
+            const uint32_t peers = __match_any_sync(0xffffffffu, dig[r]);
+            const uint32_t lower = __popc(peers & lanemask_lt);
+            const uint32_t old = s_warp[warp][dig[r]];
+            __syncwarp();
+            if (lower == 0) s_warp[warp][dig[r]] = old + __popc(peers);
+            __syncwarp();
+            rank[r] = old + lower;
+        }
+        __syncthreads();
+        const uint32_t d = threadIdx.x;
+        uint32_t cnt = 0;
 #pragma unroll
-    for (int w = 0; w < kSortWarps; ++w) {
-        uint32_t c = s_warp[w][d];
-        s_warp[w][d] = cnt;
-        cnt += c;
-    }
-    uint32_t tot;
-    uint32_t tileStart = blockExclusiveScan(cnt, tot, s_scan);
-    s_tileStart[d] = tileStart;
-    uint32_t bucket = blockExclusiveScan(hist[d], tot, s_scan);
-    // Look-back for this digit (flag in bits 30-31, count in bits 0-29).
-    uint32_t prefix = 0;
-    if (tile == 0) {
-        atomicExch(&state[d], (2u << 30) | cnt);
-    } else {
-        atomicExch(&state[tile * 256 + d], (1u << 30) | cnt);
-        int64_t t = (int64_t)tile - 1;
-        uint32_t spins = 0;
-        while (t >= 0) {
-            uint32_t v = ldvol(&state[t * 256 + d]);
-            uint32_t f = v >> 30;
-            if (f == 0) {
-                if (++spins > kSpinLimit) {
-                    atomicOr(err, kErrTimeout);
-                    break;
+        for (int w = 0; w < kSortWarps; ++w) {
+            const uint32_t c = s_warp[w][d];
+            s_warp[w][d] = cnt;
+            cnt += c;
+        }
+        uint32_t tot;
+        const uint32_t tileStart = blockExclusiveScan(cnt, tot, s_scan);
+        s_tileStart[d] = tileStart;
+        // Look-back for this digit (flag in bits 30-31, count in bits 0-29).
+        uint32_t prefix = 0;
+        if (tile == 0) {
+            atomicExch(&state[d], (2u << 30) | cnt);
+        } else {
+            atomicExch(&state[tile * 256 + d], (1u << 30) | cnt);
+            int64_t t = (int64_t)tile - 1;
+            uint32_t spins = 0;
+            while (t >= 0) {
+                const uint32_t v = ldvol(&state[t * 256 + d]);
+                const uint32_t f = v >> 30;
+                if (f == 0) {
+                    if (++spins > kSpinLimit) {
+                        atomicOr(err, kErrTimeout);
+                        break;
+                    }
+                    continue;
                 }
-                continue;
+                prefix += v & 0x3FFFFFFFu;
+                if (f == 2) break;
+                --t;
             }
-            prefix += v & 0x3FFFFFFFu;
-            if (f == 2) break;
-            --t;
+            atomicExch(&state[tile * 256 + d], (2u << 30) | (prefix + cnt));
         }
-        atomicExch(&state[tile * 256 + d], (2u << 30) | (prefix + cnt));
-    }
-    s_base[d] = bucket + prefix - tileStart;
-    __syncthreads();
+        s_base[d] = s_bucket[d] + prefix - tileStart;
+        __syncthreads();
 #pragma unroll
-    for (int r = 0; r < kSortRounds; ++r) {
-        uint32_t idx = base + warp * (32 * kSortRounds) + r * 32 + lane;
-        if (idx < n) {
-            uint32_t pos = s_tileStart[dig[r]] + s_warp[warp][dig[r]] + rank[r];
-            s_keys[pos] = key[r];
-            if (VALS) s_vals[pos] = val[r];
+        for (int r = 0; r < kSortRounds; ++r) {
+            const uint32_t idx = base + warp * (32 * kSortRounds) + r * 32 + lane;
+            if (idx < n) {
+                const uint32_t pos = s_tileStart[dig[r]] + s_warp[warp][dig[r]] + rank[r];
+                s_keys[pos] = key[r];
+                if (VALS) s_vals[pos] = val[r];
+            }
         }
-    }
-    __syncthreads();
-    const uint32_t live = min((uint32_t)kSortTile, n - base);
-    for (uint32_t j = threadIdx.x; j < live; j += kSortThreads) {
-        K k = s_keys[j];
-        uint32_t dst = s_base[(uint32_t)((k >> shift) & 0xFF)] + j;
-        kout[dst] = k;
-        if (VALS) vout[dst] = s_vals[j];
+        __syncthreads();
+        const uint32_t live = min((uint32_t)kSortTile, n - base);
+        for (uint32_t j = threadIdx.x; j < live; j += kSortThreads) {
+            const K k = s_keys[j];
+            const uint32_t dst = s_base[(uint32_t)((k >> shift) & 0xFF)] + j;
+            kout[dst] = k;
+            if (VALS) vout[dst] = s_vals[j];
+        }
+        __syncthreads();
     }
 }
 
 // Moves the result back into buffer 0 when an odd number of passes ran.
 template <class K>
 __global__ void k_radix_fixup(K *buf0, const K *buf1, uint32_t *v0, const uint32_t *v1, const uint32_t *d_n,
-                              uint32_t n_host, const uint32_t *sel) {
+                              uint32_t cap, const uint32_t *sel) {
     if (*sel == 0) return;
-    const uint32_t n = d_n ? *d_n : n_host;
+    const uint32_t n = liveCount(d_n, cap);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         buf0[i] = buf1[i];
         if (v0) v0[i] = v1[i];
@@ -198,33 +230,36 @@ __global__ void k_radix_fixup(K *buf0, const K *buf1, uint32_t *v0, const uint32
 }
 
 // Sorts keys (and values) in place over bits [bit_begin, bit_end); keys_tmp /
-// vals_tmp are scratch of the same size.  Stable.
+// vals_tmp are scratch of the same size.  Stable.  The live count is
+// min(*d_n, max_n) (max_n alone when d_n is null).
 template <class K>
 void launchRadixSort(K *keys, K *keys_tmp, uint32_t *vals, uint32_t *vals_tmp, const uint32_t *d_n, uint32_t max_n,
                      int bit_begin, int bit_end, Scratch &ws, uint32_t *d_err, cudaStream_t s) {
     if (max_n == 0 || bit_end <= bit_begin) return;
-    const int passes = (bit_end - bit_begin + 7) / 8;
+    const int passes = std::min((bit_end - bit_begin + 7) / 8, 8);
     const uint32_t tiles = (max_n + kSortTile - 1) / kSortTile;
+    const size_t passStride = 256 * (size_t)tiles;
     uint32_t *sel = ws.sortHist + 256 * 8;
+    uint32_t *counters = ws.sortHist + 256 * 8 + 16;
     PE_CHECK(cudaMemsetAsync(ws.sortHist, 0, sizeof(uint32_t) * (256 * 8 + 16), s));
-    int hb = (int)std::min<uint32_t>((max_n + 255) / 256, 4 * 152);
-    k_radix_hist<K><<<hb, 256, 0, s>>>(keys, d_n, max_n, bit_begin, passes, ws.sortHist);
+    const uint32_t hb = std::max<uint32_t>(1, std::min<uint32_t>((max_n + 255) / 256, 4 * 152));
+    k_radix_hist<K><<<hb, 256, 0, s>>>(keys, d_n, max_n, bit_begin, passes, ws.sortHist, ws.sortState, passStride,
+                                       counters);
     PE_LAUNCHED();
+    const uint32_t grid = persistentGrid(tiles);
     for (int p = 0; p < passes; ++p) {
-        PE_CHECK(cudaMemsetAsync(ws.sortState, 0, sizeof(uint32_t) * (256 * (size_t)tiles + 1), s));
-        uint32_t *counter = ws.sortState + 256 * (size_t)tiles;
+        uint32_t *state = ws.sortState + p * passStride;
         if (vals)
-            k_radix_pass<K, true><<<tiles, kSortThreads, 0, s>>>(keys, keys_tmp, vals, vals_tmp, d_n, max_n,
-                                                                 bit_begin + 8 * p, ws.sortHist + 256 * p,
-                                                                 ws.sortState, counter, sel, p, d_err);
+            k_radix_pass<K, true><<<grid, kSortThreads, 0, s>>>(keys, keys_tmp, vals, vals_tmp, d_n, max_n,
+                                                                bit_begin + 8 * p, ws.sortHist + 256 * p, state,
+                                                                counters + p, sel, p, d_err);
         else
-            k_radix_pass<K, false><<<tiles, kSortThreads, 0, s>>>(keys, keys_tmp, nullptr, nullptr, d_n, max_n,
-                                                                  bit_begin + 8 * p, ws.sortHist + 256 * p,
-                                                                  ws.sortState, counter, sel, p, d_err);
+            k_radix_pass<K, false><<<grid, kSortThreads, 0, s>>>(keys, keys_tmp, nullptr, nullptr, d_n, max_n,
+                                                                 bit_begin + 8 * p, ws.sortHist + 256 * p, state,
+                                                                 counters + p, sel, p, d_err);
         PE_LAUNCHED();
     }
-    int fb = (int)std::min<uint32_t>((max_n + 255) / 256, 4 * 152);
-    k_radix_fixup<K><<<fb, 256, 0, s>>>(keys, keys_tmp, vals, vals_tmp, d_n, max_n, sel + passes);
+    k_radix_fixup<K><<<hb, 256, 0, s>>>(keys, keys_tmp, vals, vals_tmp, d_n, max_n, sel + passes);
     PE_LAUNCHED();
 }
 
@@ -247,9 +282,10 @@ size_t scratchBytesScan(uint32_t max_n) {
     uint32_t tiles = (max_n + kScanTile - 1) / kScanTile + 1;
     return sizeof(unsigned long long) * tiles + 16;
 }
+// Look-back state of all (up to 8) passes of one sort.
 size_t scratchBytesSort(uint32_t max_n) {
     uint32_t tiles = (max_n + kSortTile - 1) / kSortTile + 1;
-    return sizeof(uint32_t) * (256 * (size_t)tiles + 16);
+    return sizeof(uint32_t) * (8 * 256 * (size_t)tiles + 16);
 }
 
 } // namespace pe

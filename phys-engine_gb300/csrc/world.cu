@@ -256,7 +256,7 @@ void World::ensureScratch(uint32_t maxN) {
     scratchN_ = maxN;
     // The narrowphase uses 256-item tiles for its look-back.
     wsScan_.reserve((maxN + 255) / 256 + 16);
-    wsSortHist_.reserve(256 * 8 + 16);
+    wsSortHist_.reserve(256 * 8 + 64);
     wsSortState_.reserve(scratchBytesSort(maxN) / sizeof(uint32_t) + 16);
     ws_.scanState = wsScan_.ptr;
     ws_.sortHist = wsSortHist_.ptr;
@@ -305,7 +305,7 @@ void World::ensureCapacity() {
     bb_ = BroadBuffers{bbKeyTmp32_.ptr, bbValTmp_.ptr, bbMinX_.ptr, bbMaxX_.ptr, bbYZ_.ptr, bbIdx_.ptr, bbLen_.ptr,
                        bbOff_.ptr, bbWidth_.ptr, bbWidthTmp_.ptr, bbFirst_.ptr, bbCellCount_.ptr, bbInGrid_.ptr,
                        bbOverflow_.ptr, bbEntryOff_.ptr, bbEntryKeys_.ptr, bbEntryKeysTmp_.ptr, bbEntryVals_.ptr,
-                       bbEntryValsTmp_.ptr, entryCap_, bbCounters_.ptr};
+                       bbEntryValsTmp_.ptr, entryCap_, gridKeyBits_, bbCounters_.ptr};
 
     if (pairCap_ < 4u * nc) pairCap_ = std::max<uint32_t>(65536, 4u * nc);
     pairKeys_.reserve(pairCap_);
@@ -315,8 +315,8 @@ void World::ensureCapacity() {
     pairA_.reserve(pairCap_);
     pairB_.reserve(pairCap_);
     pairCounters_.reserve(4);
-    pb_ = PairBuffers{pairKeys_.ptr, pairKeysTmp_.ptr, pairCap_, pairFlags_.ptr, pairPos_.ptr, pairA_.ptr, pairB_.ptr,
-                      pairCounters_.ptr};
+    pb_ = PairBuffers{pairKeys_.ptr, pairKeysTmp_.ptr, pairCap_, 32u, false, pairFlags_.ptr, pairPos_.ptr,
+                      pairA_.ptr, pairB_.ptr, pairCounters_.ptr};
 
     if (mcap_ < pairCap_) mcap_ = pairCap_;
     const uint32_t m = mcap_;
@@ -498,7 +498,11 @@ bool World::finishStep() {
     }
     bool retry = false, grew = false;
     if (h.err & kErrSmallPath) {
-        lastMEstimate_ = h.manifolds;  // the single-block path was too small: full path
+        // A single-block path or the sorted key width was too small: re-run with
+        // the sizes this attempt measured.
+        lastMEstimate_ = std::max(lastMEstimate_, h.manifolds);
+        lastRawEstimate_ = std::max(lastRawEstimate_, h.rawPairs);
+        if (h.cellKeyBits > gridKeyBits_) gridKeyBits_ = std::min<uint32_t>(64, 8 * ((h.cellKeyBits + 9) / 8));
         retry = true;
     }
     if (h.rawPairs > pairCap_) {
@@ -545,6 +549,13 @@ bool World::finishStep() {
     lastPairs_ = h.pairs;
     lastManifolds_ = h.manifolds;
     lastMEstimate_ = h.manifolds;
+    lastRawEstimate_ = h.rawPairs;
+    // Cell-key width: whole bytes with at least two bits of slack, widened
+    // early so the captured graph rarely changes.
+    if (algorithm == 1) {
+        uint32_t want = std::min<uint32_t>(64, 8 * ((h.cellKeyBits + 9) / 8));
+        if (want > gridKeyBits_ || want + 8 < gridKeyBits_) gridKeyBits_ = want;
+    }
     cur_ = 1 - cur_;
     cache_ = 1 - cache_;
     deviceNewer_ = true;
@@ -556,7 +567,8 @@ bool World::GraphKey::operator==(const GraphKey &o) const {
     return nb == o.nb && nc == o.nc && pairCap == o.pairCap && entryCap == o.entryCap && mcap == o.mcap &&
            cacheCap == o.cacheCap && dt == o.dt && gx == o.gx && gy == o.gy && gz == o.gz &&
            algorithm == o.algorithm && iterations == o.iterations && orderMode == o.orderMode &&
-           coopBlocks == o.coopBlocks && blockSolver == o.blockSolver && cellSize == o.cellSize && dense == o.dense &&
+           coopBlocks == o.coopBlocks && blockSolver == o.blockSolver && pairBits == o.pairBits &&
+           blockPairs == o.blockPairs && gridKeyBits == o.gridKeyBits && cellSize == o.cellSize && dense == o.dense &&
            localIdentity == o.localIdentity && forces == o.forces;
 }
 
@@ -577,6 +589,9 @@ World::GraphKey World::currentKey(float dt) const {
     k.orderMode = orderMode;
     k.coopBlocks = coopBlocks_;
     k.blockSolver = blockSolver_;
+    k.pairBits = pb_.bits;
+    k.blockPairs = pb_.blockPath;
+    k.gridKeyBits = bb_.keyBits;
     k.cellSize = cellSize;
     k.dense = dense_;
     k.localIdentity = localIdentity_;
@@ -603,6 +618,13 @@ unsigned long long World::launchStep(float dt) {
     // Small manifold counts run the single-block solver (with headroom over
     // the last step's count; an overflow re-runs the step on the full path).
     blockSolver_ = lastMEstimate_ + lastMEstimate_ / 4 + 64 <= kBlockMaxManifolds && nb_ <= kBlockMaxBodies;
+    // Pair keys need bits for input indices < nc; the small finalize path is
+    // used while the last raw pair count leaves headroom.
+    uint32_t bits = 1;
+    while (bits < 32 && (1ull << bits) < (unsigned long long)std::max<uint32_t>(nc_, 2)) ++bits;
+    pb_.bits = bits;
+    pb_.blockPath = lastRawEstimate_ + lastRawEstimate_ / 4 + 256 <= kBlockMaxPairs;
+    bb_.keyBits = gridKeyBits_;
     if (graphsDisabled_) {
         const unsigned long long l0 = g_kernelLaunches;
         runPipeline(dt);
@@ -849,6 +871,11 @@ void World::broadphaseOnly(const float *mins, const float *maxs, uint32_t n, int
         }
         launchStepInit(st, n, s);
         BroadInput in{inMin_.ptr, inMax_.ptr, &st->inputCount, std::max<uint32_t>(n, 1)};
+        uint32_t bits = 1;
+        while (bits < 32 && (1ull << bits) < (unsigned long long)std::max<uint32_t>(n, 2)) ++bits;
+        pb_.bits = bits;
+        pb_.blockPath = false;
+        bb_.keyBits = 64;
         if (algo == 0) {
             launchSapKeys(in, sapKeys_.ptr, sapVals_.ptr, s);
             launchSap(in, sapKeys_.ptr, sapVals_.ptr, bb_, pb_, st, ws_, s);

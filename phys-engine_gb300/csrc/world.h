@@ -163,7 +163,8 @@ class World {
     int cache_ = 0;
     uint64_t steps_ = 0;
     uint32_t lastErr_ = 0;
-    uint32_t lastPairs_ = 0, lastManifolds_ = 0, lastMEstimate_ = 0;
+    uint32_t lastPairs_ = 0, lastManifolds_ = 0, lastMEstimate_ = 0, lastRawEstimate_ = 0;
+    uint32_t gridKeyBits_ = 64;
     uint64_t possiblePairs_ = 0, dynamicAlive_ = 0;
     StepCounters counters_;
 
@@ -225,7 +226,8 @@ class World {
         uint32_t nb, nc, pairCap, entryCap, mcap, cacheCap;
         float dt, gx, gy, gz;
         int algorithm, iterations, orderMode, coopBlocks;
-        bool blockSolver;
+        bool blockSolver, blockPairs;
+        uint32_t pairBits, gridKeyBits;
         double cellSize;
         bool dense, localIdentity, forces;
         bool operator==(const GraphKey &o) const;
