@@ -14,24 +14,6 @@ namespace pe {
 
 constexpr int kNarrowThreads = 256;
 
-__device__ __forceinline__ SupportShape supportShape(const WorldView &w, uint32_t c, const Tf &t) {
-    SupportShape s;
-    s.shape = colliderShape(w.cflags[c]);
-    float4 sh = w.cshape[c];
-    s.radius = sh.x;
-    s.he = V3{sh.x, sh.y, sh.z};
-    s.tf = t;
-    s.verts = nullptr;
-    s.nverts = 0;
-    if (s.shape == kShapeHull) {
-        uint32_t h = __float_as_uint(sh.w);
-        uint32_t b = w.hullOffset[h];
-        s.verts = w.hullVerts + b;
-        s.nverts = w.hullOffset[h + 1] - b;
-    }
-    return s;
-}
-
 __global__ void __launch_bounds__(kNarrowThreads)
 k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *__restrict__ pairB,
               const uint32_t *d_pairs, ManifoldView out, uint32_t mcap, DevStats *st, unsigned long long *state,
@@ -54,50 +36,9 @@ k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *_
         cb = pairB[p];
         ba = w.cbody[ca];
         bb = w.cbody[cb];
-        const uint32_t sa = colliderShape(w.cflags[ca]), sb = colliderShape(w.cflags[cb]);
-        V3 lpa = w.clpos ? f4xyz(w.clpos[ca]) : V3{0.0f, 0.0f, 0.0f};
-        Q lqa = w.clrot ? f4q(w.clrot[ca]) : qidentity();
-        V3 lpb = w.clpos ? f4xyz(w.clpos[cb]) : V3{0.0f, 0.0f, 0.0f};
-        Q lqb = w.clrot ? f4q(w.clrot[cb]) : qidentity();
-        V3 pa = f4xyz(w.cur.pos[ba]), pb = f4xyz(w.cur.pos[bb]);
-        Q qa = f4q(w.cur.rot[ba]), qb = f4q(w.cur.rot[bb]);
-        Tf tA{pa + rotate(qa, lpa), qmul(qa, lqa)};
-        Tf tB{pb + rotate(qb, lpb), qmul(qb, lqb)};
-        const float4 sha = w.cshape[ca], shb = w.cshape[cb];
-        if (sa == kShapeHull || sb == kShapeHull) {
-            category = 3;
-            bool failed;
-            hit = hullContact(supportShape(w, ca, tA), supportShape(w, cb, tB), lm, failed);
-            if (failed) atomicAdd(&st->epaFailures, 1ull);
-        } else {
-            category = sa + sb;
-            if (sa == kShapeSphere && sb == kShapeSphere) {
-                hit = sphereSphere(sha.x, tA, shb.x, tB, lm);
-            } else if (sa == kShapeSphere) {
-                hit = sphereBox(sha.x, tA, V3{shb.x, shb.y, shb.z}, tB, lm);
-            } else if (sb == kShapeSphere) {
-                hit = sphereBox(shb.x, tB, V3{sha.x, sha.y, sha.z}, tA, lm);
-                if (hit) {
-                    lm.normal = -lm.normal;
-                    for (uint32_t k = 0; k < lm.count; ++k) {
-                        V3 t = lm.anchorA[k];
-                        lm.anchorA[k] = lm.anchorB[k];
-                        lm.anchorB[k] = t;
-                    }
-                }
-            } else {
-                hit = boxBox(V3{sha.x, sha.y, sha.z}, tA, V3{shb.x, shb.y, shb.z}, tB, lm);
-            }
-        }
-        if (hit) {
-            for (uint32_t k = 0; k < lm.count; ++k) {
-                lm.anchorA[k] = lpa + rotate(lqa, lm.anchorA[k]);
-                lm.anchorB[k] = lpb + rotate(lqb, lm.anchorB[k]);
-            }
-            const float4 ma = w.mat[ba], mb = w.mat[bb];
-            restitution = smax(ma.y, mb.y);
-            friction = sqrtf(smax(ma.z, 0.0f) * smax(mb.z, 0.0f));
-        }
+        bool epaFailed;
+        hit = narrowphasePair(w, ca, cb, ba, bb, lm, restitution, friction, category, epaFailed);
+        if (epaFailed) atomicAdd(&st->epaFailures, 1ull);
         aggregatedCount(st->npCandidates, category);
         if (hit) aggregatedCount(st->npContacts, category);
     }

@@ -15,38 +15,10 @@
 // among the uncoloured manifolds at both its bodies.
 #include "pe_block.cuh"
 #include "pe_kernels.cuh"
+#include "pe_solve.cuh"
 #include "pe_stages.h"
 
 namespace pe {
-
-constexpr uint32_t kUncolored = 0xFFFFFFFFu;
-constexpr uint32_t kMaxRounds = 4096;
-constexpr int kSolveThreads = 256;
-constexpr int kBlockSolveThreads = 512;
-
-__device__ __forceinline__ uint32_t colorPriority(uint32_t m) {
-    uint32_t h = m;
-    h ^= h >> 16;
-    h *= 0x85ebca6bu;
-    h ^= h >> 13;
-    h *= 0xc2b2ae35u;
-    h ^= h >> 16;
-    return h;
-}
-
-__device__ __forceinline__ float4 ld4(const float4 *p) { return __ldcg(p); }
-__device__ __forceinline__ void st4(float4 *p, const float4 &v) { __stcg(p, v); }
-
-struct SolveArgs {
-    WorldView w;
-    ManifoldView mv;
-    SolverBuffers sb;
-    CacheView oldCache;
-    const uint32_t *oldCount;
-    DevStats *st;
-    uint32_t mcap;
-    int iterations;
-};
 
 // ------------------------------------------------------------- colouring ---
 __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
@@ -134,302 +106,10 @@ __global__ void k_order_init(SolveArgs a, int serial) {
     }
 }
 
-// --------------------------------------------------------------- prepare ---
-// prepareBody (:275-287) + prepareContactPoints (:101-214) + the cache lookup
-// of warmStartPrepared (:448-490).  Data are written in solve order k.
-__device__ void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t stride, uint32_t M) {
-    const uint32_t mcap = a.mcap;
-    const WorldView &w = a.w;
-    const float inverseDt = 1.0f / smax(w.dt, 1e-6f);
-    const uint32_t cacheN = *a.oldCount;
-    uint64_t prepared = 0, comparisons = 0, matches = 0;
-    for (uint32_t k = begin; k < M; k += stride) {
-        const uint32_t m = a.sb.order[k];
-        const uint32_t ia = a.mv.bodyA[m], ib = a.mv.bodyB[m];
-        const float4 nf = a.mv.normalFriction[m];
-        const V3 n{nf.x, nf.y, nf.z};
-        // A manifold whose body handles are stale is not solved and not cached
-        // (sequential_impulse_solver.cpp:317-320).
-        const bool valid = ia < w.nb && ib < w.nb && (w.bflags[ia] & kBodyAlive) && (w.bflags[ib] & kBodyAlive) &&
-                           w.bgen[ia] == a.mv.genA[m] && w.bgen[ib] == a.mv.genB[m];
-        a.sb.pbody[k] = make_uint2(valid ? ia : 0u, valid ? ib : 0u);
-        if (!valid) {
-            a.sb.pcount[k] = 0;
-            a.sb.pm[k] = make_float4(0.0f, 1.0f, 0.0f, 1.0f);
-            a.sb.pn[k] = nf;
-            for (uint32_t p = 0; p < 4; ++p) {
-                float4 imp = a.mv.impulse[4 * m + p];
-                imp.w = 0.0f;
-                a.sb.pimp[(size_t)p * mcap + k] = imp;
-            }
-            continue;
-        }
-        aggregatedAppend(&a.st->solved);
-        const uint32_t npts = a.mv.pointCount[m];
-        const float rest = a.mv.restitution[m];
-        const bool sA = (w.bflags[ia] & kBodyStatic) != 0, sB = (w.bflags[ib] & kBodyStatic) != 0;
-        const float imA = w.mat[ia].x, imB = w.mat[ib].x;
-        const float4 iA = w.iinv[ia], iB = w.iinv[ib];
-        const Q qA = f4q(w.cur.rot[ia]), qB = f4q(w.cur.rot[ib]);
-        const M3 IA = inverseInertiaWorld(qA, iA.x, iA.y, iA.z);
-        const M3 IB = inverseInertiaWorld(qB, iB.x, iB.y, iB.z);
-        const V3 linA = f4xyz(w.nxt.lin[ia]), angA = f4xyz(w.nxt.ang[ia]);
-        const V3 linB = f4xyz(w.nxt.lin[ib]), angB = f4xyz(w.nxt.ang[ib]);
-        a.sb.pm[k] = make_float4(imA, sA ? 1.0f : 0.0f, imB, sB ? 1.0f : 0.0f);
-        a.sb.pmInertia[0 * mcap + k] = make_float4(IA.m00, IA.m01, IA.m02, 0.0f);
-        a.sb.pmInertia[1 * mcap + k] = make_float4(IA.m10, IA.m11, IA.m12, 0.0f);
-        a.sb.pmInertia[2 * mcap + k] = make_float4(IA.m20, IA.m21, IA.m22, 0.0f);
-        a.sb.pmInertia[3 * mcap + k] = make_float4(IB.m00, IB.m01, IB.m02, 0.0f);
-        a.sb.pmInertia[4 * mcap + k] = make_float4(IB.m10, IB.m11, IB.m12, 0.0f);
-        a.sb.pmInertia[5 * mcap + k] = make_float4(IB.m20, IB.m21, IB.m22, 0.0f);
-
-        // Cache range for (bodyA, bodyB); generations must match.
-        const unsigned long long key = ((unsigned long long)ia << 32) | ib;
-        const unsigned long long gens = ((unsigned long long)a.mv.genA[m] << 32) | a.mv.genB[m];
-        uint32_t lo = 0, hi = cacheN;
-        while (lo < hi) {
-            uint32_t mid = (lo + hi) >> 1;
-            if (a.oldCache.key[mid] < key) lo = mid + 1;
-            else hi = mid;
-        }
-        uint32_t rb = lo, re = lo;
-        while (re < cacheN && a.oldCache.key[re] == key) ++re;
-        if (rb < re && a.oldCache.gens[rb] != gens) re = rb;
-
-        const float matchSq = 0.05f * 0.05f;
-        for (uint32_t p = 0; p < 4; ++p) {
-            float4 out[kPreparedVec4];
-            for (int v = 0; v < kPreparedVec4; ++v) out[v] = make_float4(0, 0, 0, 0);
-            float4 imp = a.mv.impulse[4 * m + p];
-            imp.w = 0.0f;
-            if (p < npts) {
-                const float4 aa = a.mv.anchorA[4 * m + p], ab = a.mv.anchorB[4 * m + p];
-                const V3 anchorA{aa.x, aa.y, aa.z}, anchorB{ab.x, ab.y, ab.z};
-                const float penetration = aa.w;
-                V3 offA = rotate(qA, anchorA), offB = rotate(qB, anchorB);
-                out[0] = make4(offA, 0.0f);
-                out[1] = make4(offB, 0.0f);
-                V3 tref = fabsf(n.x) < 0.9f ? V3{1.0f, 0.0f, 0.0f} : V3{0.0f, 1.0f, 0.0f};
-                V3 t1 = cross(n, tref);
-                float tl = sqrtf(dot(t1, t1));
-                if (tl > 1e-6f) {
-                    t1 = t1 / tl;
-                    V3 t2 = cross(n, t1);
-                    V3 vA = linA + cross(angA, offA), vB = linB + cross(angB, offB);
-                    float vin = dot(vB - vA, n);
-                    V3 jA = cross(offA, n), jB = cross(offB, n);
-                    V3 nrA = mul(IA, jA), nrB = mul(IB, jB);
-                    float ims = imA + imB;
-                    float iem = ims + dot(jA, nrA) + dot(jB, nrB);
-                    V3 tjA = cross(offA, t1), tjB = cross(offB, t1);
-                    V3 trA1 = mul(IA, tjA), trB1 = mul(IB, tjB);
-                    float tm00 = ims + dot(tjA, trA1) + dot(tjB, trB1);
-                    float ntr1 = ims * dot(n, t1) + dot(tjA, nrA) + dot(tjB, nrB);
-                    tjA = cross(offA, t2);
-                    tjB = cross(offB, t2);
-                    V3 trA2 = mul(IA, tjA), trB2 = mul(IB, tjB);
-                    float tm11 = ims + dot(tjA, trA2) + dot(tjB, trB2);
-                    float ntr2 = ims * dot(n, t2) + dot(tjA, nrA) + dot(tjB, nrB);
-                    float tm01 = dot(tjA, trA1) + dot(tjB, trB1);
-                    float det = tm00 * tm11 - tm01 * tm01;
-                    float itm00 = 0.0f, itm01 = 0.0f, itm11 = 0.0f;
-                    if (det > 0.0f) {
-                        float inv = 1.0f / det;
-                        itm00 = tm11 * inv;
-                        itm01 = -tm01 * inv;
-                        itm11 = tm00 * inv;
-                    }
-                    float bias = 0.0f, rv = 0.0f;
-                    if (!(iem <= 0.0f)) {
-                        ++prepared;
-                        bias = smax(penetration - 0.005f, 0.0f) * (0.2f * inverseDt);
-                        rv = vin < -1.0f ? rest * vin : 0.0f;
-                    }
-                    out[0].w = iem;
-                    out[1].w = bias;
-                    out[2] = make4(t1, rv);
-                    out[3] = make4(t2, itm00);
-                    out[4] = make4(nrA, itm01);
-                    out[5] = make4(nrB, itm11);
-                    out[6] = make4(trA1, ntr1);
-                    out[7] = make4(trB1, ntr2);
-                    out[8] = make4(trA2, 0.0f);
-                    out[9] = make4(trB2, 0.0f);
-                    if (!(iem <= 0.0f)) {
-                        for (uint32_t c = rb; c < re; ++c) {
-                            ++comparisons;
-                            const float4 ca = a.oldCache.anchorA[c], cb = a.oldCache.anchorB[c];
-                            V3 da = V3{ca.x, ca.y, ca.z} - anchorA, db = V3{cb.x, cb.y, cb.z} - anchorB;
-                            if (dot(da, da) > matchSq || dot(db, db) > matchSq) continue;
-                            const float t2c = a.oldCache.tangent2[c];
-                            float ni = smax(ca.w, 0.0f);
-                            float limit = smax(nf.w, 0.0f) * ni;
-                            float tlsq = cb.w * cb.w + t2c * t2c;
-                            float scale = tlsq > limit * limit ? limit / sqrtf(tlsq) : 1.0f;
-                            imp = make_float4(ni, cb.w * scale, t2c * scale, 1.0f);
-                            ++matches;
-                            break;
-                        }
-                    }
-                }
-            }
-            for (int v = 0; v < kPreparedVec4; ++v) a.sb.pp[(size_t)(v * 4 + p) * mcap + k] = out[v];
-            a.sb.pimp[(size_t)p * mcap + k] = imp;
-        }
-        a.sb.pn[k] = nf;
-        a.sb.pcount[k] = npts;
-    }
-    aggregatedAdd64(&a.st->preparedPoints, prepared);
-    aggregatedAdd64(&a.st->warmComparisons, comparisons);
-    aggregatedAdd64(&a.st->warmMatches, matches);
-}
-
 __global__ void k_prepare(SolveArgs a) {
     prepareRange(a, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, min(a.st->manifolds, a.mcap));
 }
 
-// ---------------------------------------------------------- solve sweeps ---
-struct BodyVel {
-    V3 lin, ang;
-};
-
-__device__ __forceinline__ void warmStartOne(const SolveArgs &a, uint32_t k) {
-    const uint32_t mcap = a.mcap;
-    const uint2 bi = a.sb.pbody[k];
-    const float4 pm = a.sb.pm[k];
-    const bool sA = pm.y != 0.0f, sB = pm.w != 0.0f;
-    const float4 nf = a.sb.pn[k];
-    const V3 n{nf.x, nf.y, nf.z};
-    const uint32_t npts = a.sb.pcount[k];
-    M3 IA, IB;
-    {
-        float4 r0 = a.sb.pmInertia[0 * mcap + k], r1 = a.sb.pmInertia[1 * mcap + k], r2 = a.sb.pmInertia[2 * mcap + k];
-        IA = M3{r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
-        r0 = a.sb.pmInertia[3 * mcap + k], r1 = a.sb.pmInertia[4 * mcap + k], r2 = a.sb.pmInertia[5 * mcap + k];
-        IB = M3{r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
-    }
-    V3 linA = f4xyz(ld4(&a.w.nxt.lin[bi.x])), angA = f4xyz(ld4(&a.w.nxt.ang[bi.x]));
-    V3 linB = f4xyz(ld4(&a.w.nxt.lin[bi.y])), angB = f4xyz(ld4(&a.w.nxt.ang[bi.y]));
-    bool any = false;
-    for (uint32_t p = 0; p < npts; ++p) {
-        const float4 imp = a.sb.pimp[(size_t)p * mcap + k];
-        if (imp.w == 0.0f) continue;
-        const float4 offA4 = a.sb.pp[(size_t)(0 * 4 + p) * mcap + k];
-        const float4 offB4 = a.sb.pp[(size_t)(1 * 4 + p) * mcap + k];
-        const float4 t14 = a.sb.pp[(size_t)(2 * 4 + p) * mcap + k];
-        const float4 t24 = a.sb.pp[(size_t)(3 * 4 + p) * mcap + k];
-        V3 wi = n * imp.x + f4xyz(t14) * imp.y + f4xyz(t24) * imp.z;
-        V3 nw = -wi;
-        if (!sA) {
-            linA += nw * pm.x;
-            angA += mul(IA, cross(f4xyz(offA4), nw));
-        }
-        if (!sB) {
-            linB += wi * pm.z;
-            angB += mul(IB, cross(f4xyz(offB4), wi));
-        }
-        any = true;
-    }
-    if (!any) return;
-    if (!sA) {
-        st4(&a.w.nxt.lin[bi.x], make4(linA, 0.0f));
-        st4(&a.w.nxt.ang[bi.x], make4(angA, 0.0f));
-    }
-    if (!sB) {
-        st4(&a.w.nxt.lin[bi.y], make4(linB, 0.0f));
-        st4(&a.w.nxt.ang[bi.y], make4(angB, 0.0f));
-    }
-}
-
-// solvePrepared (:520-603) for one manifold.
-__device__ __forceinline__ void solveOne(const SolveArgs &a, uint32_t k) {
-    const uint32_t mcap = a.mcap;
-    const uint2 bi = a.sb.pbody[k];
-    const float4 pm = a.sb.pm[k];
-    const bool sA = pm.y != 0.0f, sB = pm.w != 0.0f;
-    const float4 nf = a.sb.pn[k];
-    const V3 n{nf.x, nf.y, nf.z};
-    const float friction = nf.w;
-    const uint32_t npts = a.sb.pcount[k];
-    V3 linA = f4xyz(ld4(&a.w.nxt.lin[bi.x])), angA = f4xyz(ld4(&a.w.nxt.ang[bi.x]));
-    V3 linB = f4xyz(ld4(&a.w.nxt.lin[bi.y])), angB = f4xyz(ld4(&a.w.nxt.ang[bi.y]));
-    for (uint32_t p = 0; p < npts; ++p) {
-        const float4 o0 = a.sb.pp[(size_t)(0 * 4 + p) * mcap + k];
-        if (o0.w <= 0.0f) continue;  // inverseEffectiveMass <= 0
-        const float4 o1 = a.sb.pp[(size_t)(1 * 4 + p) * mcap + k];
-        const float4 o2 = a.sb.pp[(size_t)(2 * 4 + p) * mcap + k];
-        const float4 o3 = a.sb.pp[(size_t)(3 * 4 + p) * mcap + k];
-        const float4 o4 = a.sb.pp[(size_t)(4 * 4 + p) * mcap + k];
-        const float4 o5 = a.sb.pp[(size_t)(5 * 4 + p) * mcap + k];
-        float4 imp = a.sb.pimp[(size_t)p * mcap + k];
-        const V3 offA = f4xyz(o0), offB = f4xyz(o1), t1 = f4xyz(o2), t2 = f4xyz(o3);
-        const float iem = o0.w, bias = o1.w, rv = o2.w, itm00 = o3.w, itm01 = o4.w, itm11 = o5.w;
-        const V3 vA = linA + cross(angA, offA);
-        const V3 vB = linB + cross(angB, offB);
-        const V3 rel = vB - vA;
-        float vn = dot(rel, n);
-        float delta = -(vn + rv - bias) / iem;
-        float prev = imp.x;
-        imp.x = smax(prev + delta, 0.0f);
-        float applied = imp.x - prev;
-        V3 impulse = n * applied;
-        if (!sA) {
-            linA += (-impulse) * pm.x;
-            angA += f4xyz(o4) * (-applied);
-        }
-        if (!sB) {
-            linB += impulse * pm.z;
-            angB += f4xyz(o5) * applied;
-        }
-        if (itm00 <= 0.0f || itm11 <= 0.0f) {
-            a.sb.pimp[(size_t)p * mcap + k] = imp;
-            continue;
-        }
-        const float4 o6 = a.sb.pp[(size_t)(6 * 4 + p) * mcap + k];
-        const float4 o7 = a.sb.pp[(size_t)(7 * 4 + p) * mcap + k];
-        const float4 o8 = a.sb.pp[(size_t)(8 * 4 + p) * mcap + k];
-        const float4 o9 = a.sb.pp[(size_t)(9 * 4 + p) * mcap + k];
-        const float ntr1 = o6.w, ntr2 = o7.w;
-        float limit = smax(friction, 0.0f) * imp.x;
-        float tv1 = dot(rel, t1) + ntr1 * applied;
-        float tv2 = dot(rel, t2) + ntr2 * applied;
-        float d1 = -(itm00 * tv1 + itm01 * tv2);
-        float d2 = -(itm01 * tv1 + itm11 * tv2);
-        float p1 = imp.y, p2 = imp.z;
-        imp.y += d1;
-        imp.z += d2;
-        float lsq = imp.y * imp.y + imp.z * imp.z;
-        if (lsq > limit * limit) {
-            float s = limit / sqrtf(lsq);
-            imp.y *= s;
-            imp.z *= s;
-        }
-        float a1 = imp.y - p1, a2 = imp.z - p2;
-        V3 ti = t1 * a1 + t2 * a2;
-        V3 rA = f4xyz(o6) * a1 + f4xyz(o8) * a2;
-        V3 rB = f4xyz(o7) * a1 + f4xyz(o9) * a2;
-        if (!sA) {
-            linA += (-ti) * pm.x;
-            angA += -rA;
-        }
-        if (!sB) {
-            linB += ti * pm.z;
-            angB += rB;
-        }
-        a.sb.pimp[(size_t)p * mcap + k] = imp;
-    }
-    if (!sA) {
-        st4(&a.w.nxt.lin[bi.x], make4(linA, 0.0f));
-        st4(&a.w.nxt.ang[bi.x], make4(angA, 0.0f));
-    }
-    if (!sB) {
-        st4(&a.w.nxt.lin[bi.y], make4(linB, 0.0f));
-        st4(&a.w.nxt.ang[bi.y], make4(angB, 0.0f));
-    }
-}
-
-// Cooperative sweep: warm start, then `iterations` sweeps, each colour by colour
-// with a grid barrier between colours.
 __global__ void __launch_bounds__(kSolveThreads) k_solve_colored(SolveArgs a) {
     __shared__ uint32_t s_start[kMaxColors + 1];
     const uint32_t C = min(a.st->colors, (uint32_t)kMaxColors);
@@ -500,23 +180,6 @@ __global__ void k_cache_counts(SolveArgs a) {
     }
 }
 // Writes the cache entries of manifold m (npts points) starting at entry base.
-__device__ __forceinline__ void cacheWriteManifold(const SolveArgs &a, const CacheView &nc, uint32_t cacheCap,
-                                                   uint32_t m, uint32_t base, uint32_t npts) {
-    const unsigned long long key = ((unsigned long long)a.mv.bodyA[m] << 32) | a.mv.bodyB[m];
-    const unsigned long long gens = ((unsigned long long)a.mv.genA[m] << 32) | a.mv.genB[m];
-    for (uint32_t p = 0; p < npts; ++p) {
-        const uint32_t e = base + p;
-        if (e >= cacheCap) break;
-        const float4 aa = a.mv.anchorA[4 * m + p], ab = a.mv.anchorB[4 * m + p];
-        const float4 imp = a.mv.impulse[4 * m + p];
-        nc.key[e] = key;
-        nc.gens[e] = gens;
-        nc.anchorA[e] = make_float4(aa.x, aa.y, aa.z, imp.x);
-        nc.anchorB[e] = make_float4(ab.x, ab.y, ab.z, imp.y);
-        nc.tangent2[e] = imp.z;
-    }
-}
-
 __global__ void k_cache_write(SolveArgs a, CacheView nc, uint32_t cacheCap) {
     const uint32_t M = min(a.st->manifolds, a.mcap);
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < M; k += gridDim.x * blockDim.x)
@@ -524,184 +187,12 @@ __global__ void k_cache_write(SolveArgs a, CacheView nc, uint32_t cacheCap) {
 }
 
 
-// ------------------------------------------------------ single-block path ---
-// The whole solver for up to kBlockMaxManifolds manifolds in one thread block:
-// the same colouring, order, prepare, sweeps and cache rebuild as the
-// multi-kernel path, separated by __syncthreads instead of kernel boundaries
-// and grid barriers.  If the live manifold count exceeds the block capacity the
-// kernel only flags kErrSmallPath; the step is then re-run on the multi-kernel
-// path.
 __global__ void __launch_bounds__(kBlockSolveThreads)
 k_solve_block(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount, int serial) {
-    extern __shared__ unsigned long long s_sort[];  // kBlockMaxManifolds u64
-    uint32_t *s_dyn = reinterpret_cast<uint32_t *>(s_sort + kBlockMaxManifolds);
-    __shared__ uint32_t s_start[kMaxColors + 1], s_count[kMaxColors], s_colored, s_colors, s_scan[40];
-    const uint32_t M = min(a.st->manifolds, a.mcap);
-    if (M > kBlockMaxManifolds) {
-        if (threadIdx.x == 0) atomicOr(&a.st->err, kErrSmallPath);
-        return;
-    }
-    const WorldView &w = a.w;
-    SolverBuffers &sb = a.sb;
-    const uint32_t tid = threadIdx.x, nt = blockDim.x;
-    uint32_t C = 0;
-    if (serial) {
-        for (uint32_t k = tid; k < M; k += nt) sb.order[k] = k;
-        __syncthreads();
-    } else {
-        // --- colouring (Jones-Plassmann rounds, as k_color) ---
-        for (uint32_t c = tid; c < kMaxColors; c += nt) s_count[c] = 0;
-        if (tid == 0) {
-            s_colored = 0;
-            s_colors = 0;
-        }
-        uint32_t *s_color = reinterpret_cast<uint32_t *>(s_sort);  // reused before the order sort
-        for (uint32_t m = tid; m < M; m += nt) {
-            uint32_t ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
-            bool da = ba < w.nb && (w.bflags[ba] & kBodyAlive) && w.bgen[ba] == a.mv.genA[m] && !(w.bflags[ba] & kBodyStatic);
-            bool db = bb < w.nb && (w.bflags[bb] & kBodyAlive) && w.bgen[bb] == a.mv.genB[m] && !(w.bflags[bb] & kBodyStatic);
-            s_dyn[m] = (da ? 1u : 0u) | (db ? 2u : 0u);
-            s_color[m] = kUncolored;
-            if (da) {
-                __stcg(&sb.bodyUsed[2 * ba], 0ull);
-                __stcg(&sb.bodyUsed[2 * ba + 1], 0ull);
-            }
-            if (db) {
-                __stcg(&sb.bodyUsed[2 * bb], 0ull);
-                __stcg(&sb.bodyUsed[2 * bb + 1], 0ull);
-            }
-        }
-        __syncthreads();
-        const unsigned long long epoch0 = __ldcg(sb.epoch);
-        uint32_t round = 0;
-        for (; round < kMaxRounds; ++round) {
-            const unsigned long long stamp = (epoch0 + round + 1) << 32;
-            for (uint32_t m = tid; m < M; m += nt) {
-                if (s_color[m] != kUncolored) continue;
-                const unsigned long long p = stamp | colorPriority(m);
-                if (s_dyn[m] & 1u) atomicMax(&sb.bodyBest[a.mv.bodyA[m]], p);
-                if (s_dyn[m] & 2u) atomicMax(&sb.bodyBest[a.mv.bodyB[m]], p);
-            }
-            __syncthreads();
-            for (uint32_t m = tid; m < M; m += nt) {
-                if (s_color[m] != kUncolored) continue;
-                const unsigned long long p = stamp | colorPriority(m);
-                const uint32_t d = s_dyn[m], ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
-                // Atomics resolve in L2; read past L1 so no stale line is seen.
-                if ((d & 1u) && __ldcg(&sb.bodyBest[ba]) != p) continue;
-                if ((d & 2u) && __ldcg(&sb.bodyBest[bb]) != p) continue;
-                unsigned long long u0 = 0, u1 = 0;
-                if (d & 1u) {
-                    u0 |= __ldcg(&sb.bodyUsed[2 * ba]);
-                    u1 |= __ldcg(&sb.bodyUsed[2 * ba + 1]);
-                }
-                if (d & 2u) {
-                    u0 |= __ldcg(&sb.bodyUsed[2 * bb]);
-                    u1 |= __ldcg(&sb.bodyUsed[2 * bb + 1]);
-                }
-                uint32_t c;
-                if (~u0) c = __ffsll((long long)~u0) - 1;
-                else if (~u1) c = 64 + __ffsll((long long)~u1) - 1;
-                else {
-                    atomicOr(&a.st->err, kErrColors);
-                    c = kMaxColors - 1;
-                }
-                s_color[m] = c;
-                const unsigned long long bit = 1ull << (c & 63);
-                if (d & 1u) __stcg(&sb.bodyUsed[2 * ba + (c >> 6)], __ldcg(&sb.bodyUsed[2 * ba + (c >> 6)]) | bit);
-                if (d & 2u) __stcg(&sb.bodyUsed[2 * bb + (c >> 6)], __ldcg(&sb.bodyUsed[2 * bb + (c >> 6)]) | bit);
-                atomicAdd(&s_count[c], 1u);
-                atomicMax(&s_colors, c + 1);
-                atomicAdd(&s_colored, 1u);
-            }
-            __syncthreads();
-            if (s_colored >= M) break;
-            __syncthreads();
-        }
-        if (tid == 0) {
-            *sb.epoch = epoch0 + round + 2;
-            a.st->colorRounds = round + 1;
-            a.st->colors = s_colors;
-            if (round >= kMaxRounds) atomicOr(&a.st->err, kErrColors);
-            uint32_t acc = 0;
-            for (uint32_t c = 0; c < s_colors; ++c) {
-                s_start[c] = acc;
-                sb.colorCount[c] = s_count[c];
-                acc += s_count[c];
-            }
-            s_start[s_colors] = acc;
-        }
-        // colours to global (pair order) and the (colour, index) order
-        for (uint32_t m = tid; m < M; m += nt) sb.color[m] = s_color[m];
-        __syncthreads();
-        const uint32_t n2 = nextPow2(M > 0 ? M : 1);
-        uint32_t *keys = reinterpret_cast<uint32_t *>(s_sort);
-        for (uint32_t i = tid; i < n2; i += nt) keys[i] = i < M ? ((sb.color[i] << 12) | i) : 0xFFFFFFFFu;
-        __syncthreads();
-        blockBitonicSort<uint32_t>(keys, n2);
-        for (uint32_t k = tid; k < M; k += nt) sb.order[k] = keys[k] & 0xFFFu;
-        C = s_colors;
-        __syncthreads();
-    }
-    // --- prepare + warm-start matching ---
-    prepareRange(a, tid, nt, M);
-    __syncthreads();
-    // --- warm start and velocity iterations ---
-    if (serial) {
-        if (tid == 0) {
-            for (uint32_t k = 0; k < M; ++k) warmStartOne(a, k);
-            for (int it = 0; it < a.iterations; ++it)
-                for (uint32_t k = 0; k < M; ++k) solveOne(a, k);
-        }
-    } else {
-        for (uint32_t c = 0; c < C; ++c) {
-            for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) warmStartOne(a, k);
-            __syncthreads();
-        }
-        for (int it = 0; it < a.iterations; ++it)
-            for (uint32_t c = 0; c < C; ++c) {
-                for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) solveOne(a, k);
-                __syncthreads();
-            }
-    }
-    __syncthreads();
-    // --- impulses back to the manifolds ---
-    for (uint32_t k = tid; k < M; k += nt) {
-        const uint32_t m = sb.order[k];
-        for (uint32_t p = 0; p < 4; ++p) {
-            float4 imp = sb.pimp[(size_t)p * a.mcap + k];
-            imp.w = 0.0f;
-            a.mv.impulse[4 * m + p] = imp;
-        }
-    }
-    __syncthreads();
-    // --- cache rebuild: stable sort by (body A, body B) over solve order ---
-    const uint32_t n2 = nextPow2(M > 0 ? M : 1);
-    for (uint32_t i = tid; i < n2; i += nt) {
-        unsigned long long key = ~0ull;
-        if (i < M) {
-            const uint32_t m = sb.order[i];
-            key = ((unsigned long long)a.mv.bodyA[m] << 44) | ((unsigned long long)a.mv.bodyB[m] << 24) | i;
-        }
-        s_sort[i] = key;
-    }
-    __syncthreads();
-    blockBitonicSort<unsigned long long>(s_sort, n2);
-    for (uint32_t i = tid; i < M; i += nt) {
-        const uint32_t m = sb.order[(uint32_t)(s_sort[i] & 0xFFFu)];
-        const uint32_t ia = a.mv.bodyA[m], ib = a.mv.bodyB[m];
-        const bool valid = ia < w.nb && ib < w.nb && (w.bflags[ia] & kBodyAlive) && (w.bflags[ib] & kBodyAlive) &&
-                           w.bgen[ia] == a.mv.genA[m] && w.bgen[ib] == a.mv.genB[m];
-        s_dyn[i] = valid ? a.mv.pointCount[m] : 0u;
-    }
-    __syncthreads();
-    const uint32_t total = blockExclusiveScanArray(s_dyn, M, s_scan);
-    for (uint32_t i = tid; i < M; i += nt) {
-        const uint32_t m = sb.order[(uint32_t)(s_sort[i] & 0xFFFu)];
-        const uint32_t cnt = (i + 1 < M ? s_dyn[i + 1] : total) - s_dyn[i];
-        cacheWriteManifold(a, nc, cacheCap, m, s_dyn[i], cnt);
-    }
-    if (tid == 0) *newCount = total;
+    extern __shared__ unsigned long long s_sort[];  // kBlockMaxManifolds u64, then kBlockMaxManifolds u32
+    __shared__ BlockSolveShared sh;
+    solveBlock(a, nc, cacheCap, newCount, serial, kBlockMaxManifolds, s_sort,
+               reinterpret_cast<uint32_t *>(s_sort + kBlockMaxManifolds), sh);
 }
 
 static int gridFor(uint32_t n, int threads = 256, int maxBlocks = 152 * 8) {

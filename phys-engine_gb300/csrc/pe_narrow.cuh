@@ -484,4 +484,79 @@ __device__ inline bool hullContact(const SupportShape &A, const SupportShape &B,
     return true;
 }
 
+
+__device__ inline SupportShape supportShape(const WorldView &w, uint32_t c, const Tf &t) {
+    SupportShape s;
+    s.shape = colliderShape(w.cflags[c]);
+    float4 sh = w.cshape[c];
+    s.radius = sh.x;
+    s.he = V3{sh.x, sh.y, sh.z};
+    s.tf = t;
+    s.verts = nullptr;
+    s.nverts = 0;
+    if (s.shape == kShapeHull) {
+        uint32_t h = __float_as_uint(sh.w);
+        uint32_t b = w.hullOffset[h];
+        s.verts = w.hullVerts + b;
+        s.nverts = w.hullOffset[h + 1] - b;
+    }
+    return s;
+}
+
+// The world's generateContact lambda (src/world/physics_world.cpp:645-691) for
+// collider slots ca, cb of bodies ba, bb: world transforms, shape dispatch with
+// the box-sphere swap (narrowphase.cpp:353-365), anchors to body space,
+// restitution = max, friction = sqrt(max(fa,0) * max(fb,0)).  category: 0
+// sphere-sphere, 1 sphere-box, 2 box-box, 3 hull.
+__device__ inline bool narrowphasePair(const WorldView &w, uint32_t ca, uint32_t cb, uint32_t ba, uint32_t bb,
+                                       LocalManifold &lm, float &restitution, float &friction, uint32_t &category,
+                                       bool &epaFailed) {
+    epaFailed = false;
+    lm.count = 0;
+    const uint32_t sa = colliderShape(w.cflags[ca]), sb = colliderShape(w.cflags[cb]);
+    V3 lpa = w.clpos ? f4xyz(w.clpos[ca]) : V3{0.0f, 0.0f, 0.0f};
+    Q lqa = w.clrot ? f4q(w.clrot[ca]) : qidentity();
+    V3 lpb = w.clpos ? f4xyz(w.clpos[cb]) : V3{0.0f, 0.0f, 0.0f};
+    Q lqb = w.clrot ? f4q(w.clrot[cb]) : qidentity();
+    V3 pa = f4xyz(w.cur.pos[ba]), pb = f4xyz(w.cur.pos[bb]);
+    Q qa = f4q(w.cur.rot[ba]), qb = f4q(w.cur.rot[bb]);
+    Tf tA{pa + rotate(qa, lpa), qmul(qa, lqa)};
+    Tf tB{pb + rotate(qb, lpb), qmul(qb, lqb)};
+    const float4 sha = w.cshape[ca], shb = w.cshape[cb];
+    bool hit;
+    if (sa == kShapeHull || sb == kShapeHull) {
+        category = 3;
+        hit = hullContact(supportShape(w, ca, tA), supportShape(w, cb, tB), lm, epaFailed);
+    } else {
+        category = sa + sb;
+        if (sa == kShapeSphere && sb == kShapeSphere) {
+            hit = sphereSphere(sha.x, tA, shb.x, tB, lm);
+        } else if (sa == kShapeSphere) {
+            hit = sphereBox(sha.x, tA, V3{shb.x, shb.y, shb.z}, tB, lm);
+        } else if (sb == kShapeSphere) {
+            hit = sphereBox(shb.x, tB, V3{sha.x, sha.y, sha.z}, tA, lm);
+            if (hit) {
+                lm.normal = -lm.normal;
+                for (uint32_t k = 0; k < lm.count; ++k) {
+                    V3 t = lm.anchorA[k];
+                    lm.anchorA[k] = lm.anchorB[k];
+                    lm.anchorB[k] = t;
+                }
+            }
+        } else {
+            hit = boxBox(V3{sha.x, sha.y, sha.z}, tA, V3{shb.x, shb.y, shb.z}, tB, lm);
+        }
+    }
+    if (hit) {
+        for (uint32_t k = 0; k < lm.count; ++k) {
+            lm.anchorA[k] = lpa + rotate(lqa, lm.anchorA[k]);
+            lm.anchorB[k] = lpb + rotate(lqb, lm.anchorB[k]);
+        }
+        const float4 ma = w.mat[ba], mb = w.mat[bb];
+        restitution = smax(ma.y, mb.y);
+        friction = sqrtf(smax(ma.z, 0.0f) * smax(mb.z, 0.0f));
+    }
+    return hit;
+}
+
 } // namespace pe
