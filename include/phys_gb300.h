@@ -245,6 +245,35 @@ pe_status pe_generate_contact(int device, int shape_a, const float *dims_a, cons
                               int shape_b, const float *dims_b, const float *pos_b, const float *rot_b,
                               pe_contact_manifold *out, int *hit);
 
+/* Allocation-free sweep-and-prune query.  It has no counterpart in the
+   reference: it exists for callers that may not allocate device memory at all
+   (an engine that gives this library a fixed slice of its own memory arena, a
+   frame loop in which cudaMalloc's implicit synchronisation breaks the time
+   budget, a process that already holds nearly all of the GPU's memory).
+   Inputs and outputs are DEVICE pointers owned by the caller: d_mins/d_maxs
+   are n xyz triples, d_pairs receives up to `capacity` pairs (2 indices each,
+   first < second, in the same lexicographic order as pe_broadphase_find_pairs
+   with PE_BROADPHASE_SAP, which it equals), d_result receives two uint32
+   words: the number of pairs found, then 0 = all written, 1 = more pairs than
+   `capacity` (the first `capacity` written), 2 = more than
+   PE_NOALLOC_MAX_PAIRS (nothing written).  The call only enqueues one kernel on
+   `stream` (a cudaStream_t; NULL = default stream) and returns; results are
+   ready when the stream reaches that point.
+   Scratch is a fixed 557,056-byte device array inside the library, present on
+   every GPU that loads the library until the process exits; the call makes no
+   allocation.  n > PE_NOALLOC_MAX_BOXES is rejected with
+   PE_ERR_INVALID_ARGUMENT before anything is enqueued.  The first call on each
+   device looks up the array's device address (loading the library's device
+   code on that GPU if needed); make that first call before any stream capture.
+   All calls share the one array: calls whose kernels may overlap on the GPU
+   (different streams, or different host threads) race and corrupt each other's
+   results, so serialise them, e.g. on one stream. */
+#define PE_NOALLOC_MAX_BOXES 8192u
+#define PE_NOALLOC_MAX_PAIRS 32768u
+pe_status pe_broadphase_find_pairs_noalloc(int device, const float *d_mins, const float *d_maxs, uint32_t n,
+                                           uint32_t *d_pairs, uint32_t capacity, uint32_t *d_result,
+                                           void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -615,3 +615,27 @@ pe_status pe_generate_contact(int device, int sa, const float *da, const float *
 }
 
 } // extern "C"
+
+namespace pe {
+void findPairsNoAlloc(int device, const float *mins, const float *maxs, uint32_t n, uint32_t *pairs,
+                      uint32_t capacity, uint32_t *result, cudaStream_t s);
+}
+
+// Allocation-free SAP query for callers that may not allocate device memory;
+// the kernel, its fixed scratch array and the per-device set-up are in noalloc.cu.
+extern "C" pe_status pe_broadphase_find_pairs_noalloc(int device, const float *d_mins, const float *d_maxs,
+                                                      uint32_t n, uint32_t *d_pairs, uint32_t capacity,
+                                                      uint32_t *d_result, void *stream) {
+    if (!d_result || (n && (!d_mins || !d_maxs)) || (capacity && !d_pairs))
+        return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    if (n > PE_NOALLOC_MAX_BOXES)
+        return fail(PE_ERR_INVALID_ARGUMENT, "pe_broadphase_find_pairs_noalloc: " + std::to_string(n) +
+                                                 " boxes exceed its limit of " +
+                                                 std::to_string(PE_NOALLOC_MAX_BOXES) +
+                                                 " (PE_NOALLOC_MAX_BOXES); use pe_broadphase_find_pairs");
+    return guarded([&] {
+        pe::findPairsNoAlloc(device, d_mins, d_maxs, n, d_pairs, capacity, d_result,
+                             static_cast<cudaStream_t>(stream));
+        return PE_OK;
+    });
+}

@@ -105,6 +105,7 @@ SIGNATURES = {
                                                 ctypes.c_uint64, _P, _P]),
     "pe_generate_contact": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _P, _P, _P, ctypes.c_int, _P, _P, _P, _P,
                                            _P]),
+    "pe_broadphase_find_pairs_noalloc": (ctypes.c_int, [ctypes.c_int, _P, _P, _u32, _P, _u32, _P, _P]),
 }
 
 _lib = None
