@@ -245,6 +245,66 @@ pe_status pe_generate_contact(int device, int shape_a, const float *dims_a, cons
                               int shape_b, const float *dims_b, const float *pos_b, const float *rot_b,
                               pe_contact_manifold *out, int *hit);
 
+/* ------------------------------------------------------------------------
+   Batched worlds.  The reference steps one PhysicsWorld at a time; a batch
+   holds many independent worlds and steps all of them with one persistent
+   kernel launch per world-size bucket, captured in one CUDA graph per step.
+   Each world behaves as a PhysicsWorld (physics_world.hpp:21-153) of sphere and
+   box bodies, one collider each, with the SAP broadphase and the graph-colour
+   solve order, and gives the same results as a pe_world holding the same
+   bodies.  Limits: <= 8192 bodies and <= 4096 contact manifolds per world.
+   ------------------------------------------------------------------------ */
+typedef struct pe_batch pe_batch;
+
+typedef struct pe_batch_bucket {
+    uint32_t min_bodies, max_bodies; /* world sizes in this bucket */
+    uint32_t world_count;
+    uint32_t threads;                /* kernel variant: threads per block ... */
+    uint32_t min_blocks_per_sm;      /* ... and the residency its registers are sized for */
+    uint32_t blocks;                 /* persistent blocks launched */
+    double tuned_ms;                 /* autotuner's time per launch; 0 = not tuned */
+    double candidate_ms[8];          /* per kernel variant; -1 = does not fit, 0 = not timed */
+} pe_batch_bucket;
+
+/* world_body_counts[w] bodies per world; the per-body arrays hold all worlds'
+   bodies back to back, with the meaning of pe_world_create_bodies (shapes
+   sphere or box; linear_velocity and spin may be NULL).  On a validation
+   failure returns PE_ERR_CREATE_FAILED with the failing body in *failed_index. */
+pe_status pe_batch_create(int device, uint32_t world_count, const uint32_t *world_body_counts, const uint8_t *shape,
+                          const float *dims, const float *position, const float *density, const uint8_t *is_static,
+                          const float *restitution, const float *friction, const float *linear_velocity,
+                          const float *spin, pe_batch **out, uint64_t *failed_index);
+void pe_batch_destroy(pe_batch *batch);
+pe_status pe_batch_set_gravity(pe_batch *batch, float x, float y, float z);
+/* Solver velocity iterations of every world (the reference's fixed 8 by default). */
+pe_status pe_batch_set_iterations(pe_batch *batch, int iterations);
+/* `steps` steps of every world (PhysicsWorld::step(dt) per world). */
+pe_status pe_batch_step(pe_batch *batch, float dt, uint32_t steps);
+/* Times every kernel variant on every bucket (`repetitions` launches each,
+   from the current state, which stays unchanged) and keeps the fastest. */
+pe_status pe_batch_autotune(pe_batch *batch, float dt, int repetitions);
+pe_status pe_batch_bucket_count(pe_batch *batch, uint32_t *count);
+pe_status pe_batch_get_bucket(pe_batch *batch, uint32_t index, pe_batch_bucket *out);
+pe_status pe_batch_body_count(pe_batch *batch, uint64_t *count);
+/* All bodies, world by world (positions/linear/angular xyz, rotations xyzw);
+   any pointer may be NULL. */
+pe_status pe_batch_read_bodies(pe_batch *batch, float *positions, float *rotations, float *linear, float *angular);
+pe_status pe_batch_write_bodies(pe_batch *batch, const float *positions, const float *rotations,
+                                const float *linear, const float *angular);
+/* Per-body force for the next step, from host memory (RigidBody::applyForce;
+   like PhysicsWorld::step, the step clears it afterwards). */
+pe_status pe_batch_write_forces(pe_batch *batch, const float *forces);
+pe_status pe_batch_read_poses(pe_batch *batch, float *positions, float *rotations);
+/* Last step's StepStats, candidate pairs and contacts of one world (body
+   indices within the world). */
+pe_status pe_batch_get_world_stats(pe_batch *batch, uint32_t world, pe_step_stats *out);
+pe_status pe_batch_get_world_pairs(pe_batch *batch, uint32_t world, uint32_t *pairs, uint32_t capacity,
+                                   uint32_t *count);
+pe_status pe_batch_get_world_contacts(pe_batch *batch, uint32_t world, pe_contact_manifold *out, uint32_t capacity,
+                                      uint32_t *count);
+pe_status pe_batch_get_stream(pe_batch *batch, void **stream);
+pe_status pe_batch_set_graphs(pe_batch *batch, int enabled);
+
 /* Allocation-free sweep-and-prune query.  It has no counterpart in the
    reference: it exists for callers that may not allocate device memory at all
    (an engine that gives this library a fixed slice of its own memory arena, a

@@ -7,11 +7,16 @@
 #include <string>
 
 #include "phys_gb300.h"
+#include "batch.h"
 #include "world.h"
 
 struct pe_world {
     std::unique_ptr<pe::World> w;
     uint64_t npWorkers = 1, solverWorkers = 1, bpWorkers = 1;
+};
+
+struct pe_batch {
+    std::unique_ptr<pe::Batch> b;
 };
 
 namespace {
@@ -612,6 +617,203 @@ pe_status pe_generate_contact(int device, int sa, const float *da, const float *
         std::memcpy(out->feature, &res[9], 4 * sizeof(uint32_t));
         return PE_OK;
     });
+}
+
+
+// ----------------------------------------------------------------- batch ---
+pe_status pe_batch_create(int device, uint32_t worldCount, const uint32_t *worldBodies, const uint8_t *shape,
+                          const float *dims, const float *position, const float *density, const uint8_t *isStatic,
+                          const float *restitution, const float *friction, const float *linearVelocity,
+                          const float *spin, pe_batch **out, uint64_t *failedIndex) {
+    if (!out || !worldBodies || !shape || !dims || !position || !density || !isStatic || !restitution || !friction)
+        return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        std::vector<uint32_t> counts(worldBodies, worldBodies + worldCount);
+        uint64_t total = 0;
+        for (uint32_t n : counts) total += n;
+        std::vector<pe::HostBody> bodies(total);
+        std::vector<pe::HostCollider> colliders(total);
+        uint64_t i = 0;
+        for (uint32_t w = 0; w < worldCount; ++w) {
+            for (uint32_t k = 0; k < counts[w]; ++k, ++i) {
+                if (shape[i] != PE_SHAPE_SPHERE && shape[i] != PE_SHAPE_BOX)
+                    return fail(PE_ERR_INVALID_ARGUMENT, "sphere or box shapes expected");
+                const float *d = dims + 3 * i;
+                if (const char *err = makeBody(shape[i], d, position + 3 * i, density[i], isStatic[i],
+                                               restitution[i], friction[i], bodies[i])) {
+                    if (failedIndex) *failedIndex = i;
+                    return fail(PE_ERR_CREATE_FAILED, err);
+                }
+                pe::HostBody &hb = bodies[i];
+                if (linearVelocity) {
+                    hb.lin[0] = linearVelocity[3 * i];
+                    hb.lin[1] = linearVelocity[3 * i + 1];
+                    hb.lin[2] = linearVelocity[3 * i + 2];
+                }
+                if (spin && (spin[3 * i] != 0.0f || spin[3 * i + 1] != 0.0f || spin[3 * i + 2] != 0.0f)) {
+                    hb.ang[0] = spin[3 * i];
+                    hb.ang[1] = spin[3 * i + 1];
+                    hb.ang[2] = spin[3 * i + 2];
+                    integrateRotation(hb, 1.0f);
+                    hb.ang[0] = hb.ang[1] = hb.ang[2] = 0.0f;
+                }
+                pe::HostCollider &c = colliders[i];
+                c.body = k;
+                c.shape = shape[i];
+                if (shape[i] == PE_SHAPE_SPHERE) {
+                    c.dims[0] = d[0];
+                } else {
+                    c.dims[0] = d[0] * 0.5f;
+                    c.dims[1] = d[1] * 0.5f;
+                    c.dims[2] = d[2] * 0.5f;
+                }
+            }
+        }
+        std::unique_ptr<pe_batch> b(new pe_batch);
+        b->b.reset(new pe::Batch(device));
+        b->b->create(counts, bodies, colliders);
+        *out = b.release();
+        return PE_OK;
+    });
+}
+
+void pe_batch_destroy(pe_batch *batch) { delete batch; }
+
+pe_status pe_batch_set_gravity(pe_batch *batch, float x, float y, float z) {
+    if (!batch) return fail(PE_ERR_INVALID_ARGUMENT, "null batch");
+    batch->b->gravity[0] = x;
+    batch->b->gravity[1] = y;
+    batch->b->gravity[2] = z;
+    batch->b->invalidateGraphs();
+    return PE_OK;
+}
+
+pe_status pe_batch_set_iterations(pe_batch *batch, int iterations) {
+    if (!batch || iterations < 0 || iterations > 4096) return fail(PE_ERR_INVALID_ARGUMENT, "invalid iteration count");
+    batch->b->iterations = iterations;
+    batch->b->invalidateGraphs();
+    return PE_OK;
+}
+
+pe_status pe_batch_step(pe_batch *batch, float dt, uint32_t steps) {
+    if (!batch) return fail(PE_ERR_INVALID_ARGUMENT, "null batch");
+    return guarded([&] {
+        for (uint32_t k = 0; k < steps; ++k) batch->b->step(dt);
+        return PE_OK;
+    });
+}
+
+pe_status pe_batch_autotune(pe_batch *batch, float dt, int repetitions) {
+    if (!batch) return fail(PE_ERR_INVALID_ARGUMENT, "null batch");
+    return guarded([&] {
+        batch->b->autotune(dt, repetitions);
+        return PE_OK;
+    });
+}
+
+pe_status pe_batch_bucket_count(pe_batch *batch, uint32_t *count) {
+    if (!batch || !count) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    *count = (uint32_t)batch->b->buckets().size();
+    return PE_OK;
+}
+
+pe_status pe_batch_get_bucket(pe_batch *batch, uint32_t index, pe_batch_bucket *out) {
+    if (!batch || !out) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    const auto &bs = batch->b->buckets();
+    if (index >= bs.size()) return fail(PE_ERR_INVALID_ARGUMENT, "bucket index out of range");
+    const pe::BatchBucket &b = bs[index];
+    std::memset(out, 0, sizeof(*out));
+    out->min_bodies = b.lo;
+    out->max_bodies = b.hi;
+    out->world_count = (uint32_t)b.worlds.size();
+    out->threads = (uint32_t)pe::kBatchVariants[b.variant].threads;
+    out->min_blocks_per_sm = (uint32_t)pe::kBatchVariants[b.variant].minBlocks;
+    out->blocks = b.blocks;
+    out->tuned_ms = b.tunedMs;
+    for (size_t v = 0; v < b.candidateMs.size() && v < 8; ++v) out->candidate_ms[v] = b.candidateMs[v];
+    return PE_OK;
+}
+
+pe_status pe_batch_body_count(pe_batch *batch, uint64_t *count) {
+    if (!batch || !count) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    *count = batch->b->bodyCount();
+    return PE_OK;
+}
+
+pe_status pe_batch_read_bodies(pe_batch *batch, float *pos, float *rot, float *lin, float *ang) {
+    if (!batch) return fail(PE_ERR_INVALID_ARGUMENT, "null batch");
+    return guarded([&] {
+        batch->b->readBodies(pos, rot, lin, ang);
+        return PE_OK;
+    });
+}
+
+pe_status pe_batch_write_bodies(pe_batch *batch, const float *pos, const float *rot, const float *lin,
+                                const float *ang) {
+    if (!batch) return fail(PE_ERR_INVALID_ARGUMENT, "null batch");
+    return guarded([&] {
+        batch->b->writeBodies(pos, rot, lin, ang);
+        return PE_OK;
+    });
+}
+
+pe_status pe_batch_write_forces(pe_batch *batch, const float *forces) {
+    if (!batch || !forces) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        batch->b->writeForces(forces);
+        return PE_OK;
+    });
+}
+
+pe_status pe_batch_read_poses(pe_batch *batch, float *pos, float *rot) {
+    if (!batch || !pos || !rot) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        batch->b->readPoses(pos, rot);
+        return PE_OK;
+    });
+}
+
+pe_status pe_batch_get_world_stats(pe_batch *batch, uint32_t world, pe_step_stats *out) {
+    if (!batch || !out) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        pe::StepCounters c;
+        batch->b->worldCounters(world, c);
+        fillStats(c, out);
+        return PE_OK;
+    });
+}
+
+pe_status pe_batch_get_world_pairs(pe_batch *batch, uint32_t world, uint32_t *pairs, uint32_t capacity,
+                                   uint32_t *count) {
+    if (!batch || !count) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        *count = batch->b->worldPairs(world, pairs, capacity);
+        if (*count && (!pairs || capacity < *count)) return fail(PE_ERR_CAPACITY, "pair buffer too small");
+        return PE_OK;
+    });
+}
+
+pe_status pe_batch_get_world_contacts(pe_batch *batch, uint32_t world, pe_contact_manifold *out, uint32_t capacity,
+                                      uint32_t *count) {
+    if (!batch || !count) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        *count = batch->b->worldManifolds(world, out, capacity);
+        if (*count && (!out || capacity < *count)) return fail(PE_ERR_CAPACITY, "contact buffer too small");
+        return PE_OK;
+    });
+}
+
+pe_status pe_batch_get_stream(pe_batch *batch, void **stream) {
+    if (!batch || !stream) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    *stream = (void *)batch->b->stream();
+    return PE_OK;
+}
+
+pe_status pe_batch_set_graphs(pe_batch *batch, int enabled) {
+    if (!batch) return fail(PE_ERR_INVALID_ARGUMENT, "null batch");
+    batch->b->setGraphsEnabled(enabled != 0);
+    return PE_OK;
 }
 
 } // extern "C"

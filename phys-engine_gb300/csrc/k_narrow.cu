@@ -48,22 +48,7 @@ k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *_
     __syncthreads();
     const uint32_t m = s_prefix + local;
     if (hit) {
-        if (m < mcap) {
-            out.bodyA[m] = ba;
-            out.genA[m] = w.cbgen[ca];
-            out.bodyB[m] = bb;
-            out.genB[m] = w.cbgen[cb];
-            out.normalFriction[m] = make4(lm.normal, friction);
-            out.restitution[m] = restitution;
-            out.pointCount[m] = lm.count;
-            for (uint32_t k = 0; k < 4; ++k) {
-                const bool live = k < lm.count;
-                out.anchorA[4 * m + k] = live ? make4(lm.anchorA[k], lm.depth[k]) : make_float4(0, 0, 0, 0);
-                out.anchorB[4 * m + k] = live ? make4(lm.anchorB[k], 0.0f) : make_float4(0, 0, 0, 0);
-                out.impulse[4 * m + k] = make_float4(0, 0, 0, 0);
-                out.feature[4 * m + k] = live ? lm.feature[k] : 0u;
-            }
-        }
+        if (m < mcap) storeManifold(out, m, w, ca, cb, ba, bb, lm, restitution, friction);
         aggregatedAppend(&st->points);
         if (lm.count > 1) atomicAdd(&st->points, lm.count - 1);
     }

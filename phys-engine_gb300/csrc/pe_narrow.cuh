@@ -559,4 +559,25 @@ __device__ inline bool narrowphasePair(const WorldView &w, uint32_t ca, uint32_t
     return hit;
 }
 
+// Writes one manifold record in pair order: body handles from the colliders,
+// collider-space anchors already moved to body space, zero impulses.
+__device__ __forceinline__ void storeManifold(const ManifoldView &out, uint32_t m, const WorldView &w, uint32_t ca,
+                                              uint32_t cb, uint32_t ba, uint32_t bb, const LocalManifold &lm,
+                                              float restitution, float friction) {
+    out.bodyA[m] = ba;
+    out.genA[m] = w.cbgen[ca];
+    out.bodyB[m] = bb;
+    out.genB[m] = w.cbgen[cb];
+    out.normalFriction[m] = make4(lm.normal, friction);
+    out.restitution[m] = restitution;
+    out.pointCount[m] = lm.count;
+    for (uint32_t k = 0; k < 4; ++k) {
+        const bool live = k < lm.count;
+        out.anchorA[4 * m + k] = live ? make4(lm.anchorA[k], lm.depth[k]) : make_float4(0, 0, 0, 0);
+        out.anchorB[4 * m + k] = live ? make4(lm.anchorB[k], 0.0f) : make_float4(0, 0, 0, 0);
+        out.impulse[4 * m + k] = make_float4(0, 0, 0, 0);
+        out.feature[4 * m + k] = live ? lm.feature[k] : 0u;
+    }
+}
+
 } // namespace pe

@@ -790,23 +790,22 @@ struct ManifoldRecord {
 };
 static_assert(sizeof(ManifoldRecord) == 216, "manifold record layout");
 
-void World::downloadManifolds(void *records, uint32_t count) {
-    const uint32_t M = std::min(count, lastManifolds_);
+void downloadManifoldRecords(const ManifoldView &mv, uint32_t M, void *records) {
     std::vector<uint32_t> ba(M), ga(M), bbv(M), gb(M), cnt(M), feat(4 * (size_t)M);
     std::vector<float4> nf(M), aa(4 * (size_t)M), ab(4 * (size_t)M), im(4 * (size_t)M);
     std::vector<float> rest(M);
     if (M) {
-        PE_CHECK(cudaMemcpy(ba.data(), mBodyA_.ptr, M * 4, cudaMemcpyDeviceToHost));
-        PE_CHECK(cudaMemcpy(ga.data(), mGenA_.ptr, M * 4, cudaMemcpyDeviceToHost));
-        PE_CHECK(cudaMemcpy(bbv.data(), mBodyB_.ptr, M * 4, cudaMemcpyDeviceToHost));
-        PE_CHECK(cudaMemcpy(gb.data(), mGenB_.ptr, M * 4, cudaMemcpyDeviceToHost));
-        PE_CHECK(cudaMemcpy(cnt.data(), mCount_.ptr, M * 4, cudaMemcpyDeviceToHost));
-        PE_CHECK(cudaMemcpy(feat.data(), mFeature_.ptr, 4 * (size_t)M * 4, cudaMemcpyDeviceToHost));
-        PE_CHECK(cudaMemcpy(nf.data(), mNormal_.ptr, M * sizeof(float4), cudaMemcpyDeviceToHost));
-        PE_CHECK(cudaMemcpy(aa.data(), mAnchorA_.ptr, 4 * (size_t)M * sizeof(float4), cudaMemcpyDeviceToHost));
-        PE_CHECK(cudaMemcpy(ab.data(), mAnchorB_.ptr, 4 * (size_t)M * sizeof(float4), cudaMemcpyDeviceToHost));
-        PE_CHECK(cudaMemcpy(im.data(), mImpulse_.ptr, 4 * (size_t)M * sizeof(float4), cudaMemcpyDeviceToHost));
-        PE_CHECK(cudaMemcpy(rest.data(), mRest_.ptr, M * 4, cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(ba.data(), mv.bodyA, M * 4, cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(ga.data(), mv.genA, M * 4, cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(bbv.data(), mv.bodyB, M * 4, cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(gb.data(), mv.genB, M * 4, cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(cnt.data(), mv.pointCount, M * 4, cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(feat.data(), mv.feature, 4 * (size_t)M * 4, cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(nf.data(), mv.normalFriction, M * sizeof(float4), cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(aa.data(), mv.anchorA, 4 * (size_t)M * sizeof(float4), cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(ab.data(), mv.anchorB, 4 * (size_t)M * sizeof(float4), cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(im.data(), mv.impulse, 4 * (size_t)M * sizeof(float4), cudaMemcpyDeviceToHost));
+        PE_CHECK(cudaMemcpy(rest.data(), mv.restitution, M * 4, cudaMemcpyDeviceToHost));
     }
     ManifoldRecord *out = (ManifoldRecord *)records;
     for (uint32_t m = 0; m < M; ++m) {
@@ -833,6 +832,10 @@ void World::downloadManifolds(void *records, uint32_t count) {
             r.feature[k] = feat[4 * m + k];
         }
     }
+}
+
+void World::downloadManifolds(void *records, uint32_t count) {
+    downloadManifoldRecords(manifoldView(), std::min(count, lastManifolds_), records);
 }
 
 void World::downloadOrder(uint32_t *order, uint32_t *colors) {

@@ -2,6 +2,7 @@
 // (src/world/physics_world.cpp:162-339) kept as a host mirror, device
 // structure-of-arrays state, and the step pipeline.
 #pragma once
+#include <utility>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -22,6 +23,10 @@ template <class T> struct DeviceArray {
         if (ptr) cudaFree(ptr);
         ptr = nullptr;
         count = 0;
+    }
+    void swap(DeviceArray &o) {
+        std::swap(ptr, o.ptr);
+        std::swap(count, o.count);
     }
     // Grows to at least n elements (contents are not kept); zero-filled.
     void reserve(size_t n) {
@@ -73,6 +78,9 @@ struct StepCounters {
     uint64_t kernelLaunches = 0;
     bool graphed = false;  // the step ran from a captured CUDA graph
 };
+
+// Copies M manifolds of a device manifold view into pe_contact_manifold records.
+void downloadManifoldRecords(const ManifoldView &mv, uint32_t M, void *records);
 
 class World {
   public:

@@ -106,7 +106,32 @@ SIGNATURES = {
     "pe_generate_contact": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _P, _P, _P, ctypes.c_int, _P, _P, _P, _P,
                                            _P]),
     "pe_broadphase_find_pairs_noalloc": (ctypes.c_int, [ctypes.c_int, _P, _P, _u32, _P, _u32, _P, _P]),
+    "pe_batch_create": (ctypes.c_int, [ctypes.c_int, _u32, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                                       ctypes.POINTER(_P), ctypes.POINTER(ctypes.c_uint64)]),
+    "pe_batch_destroy": (None, [_P]),
+    "pe_batch_set_gravity": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float]),
+    "pe_batch_set_iterations": (ctypes.c_int, [_P, ctypes.c_int]),
+    "pe_batch_step": (ctypes.c_int, [_P, ctypes.c_float, _u32]),
+    "pe_batch_autotune": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int]),
+    "pe_batch_bucket_count": (ctypes.c_int, [_P, _P]),
+    "pe_batch_get_bucket": (ctypes.c_int, [_P, _u32, _P]),
+    "pe_batch_body_count": (ctypes.c_int, [_P, _P]),
+    "pe_batch_read_bodies": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "pe_batch_write_bodies": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "pe_batch_write_forces": (ctypes.c_int, [_P, _P]),
+    "pe_batch_read_poses": (ctypes.c_int, [_P, _P, _P]),
+    "pe_batch_get_world_stats": (ctypes.c_int, [_P, _u32, _P]),
+    "pe_batch_get_world_pairs": (ctypes.c_int, [_P, _u32, _P, _u32, _P]),
+    "pe_batch_get_world_contacts": (ctypes.c_int, [_P, _u32, _P, _u32, _P]),
+    "pe_batch_get_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+    "pe_batch_set_graphs": (ctypes.c_int, [_P, ctypes.c_int]),
 }
+
+BUCKET_DTYPE = np.dtype([
+    ("min_bodies", "<u4"), ("max_bodies", "<u4"), ("world_count", "<u4"), ("threads", "<u4"),
+    ("min_blocks_per_sm", "<u4"), ("blocks", "<u4"), ("tuned_ms", "<f8"), ("candidate_ms", "<f8", (8,)),
+])
+assert BUCKET_DTYPE.itemsize == 96
 
 _lib = None
 
@@ -361,3 +386,112 @@ def generate_contact(shape_a, dims_a, pos_a, quat_a, shape_b, dims_b, pos_b, qua
                                     _ptr(_f32(quat_a)), int(shape_b), _ptr(_f32(dims_b)), _ptr(_f32(pos_b)),
                                     _ptr(_f32(quat_b)), _ptr(out), ctypes.byref(hit)))
     return bool(hit.value), out[0]
+
+
+class GpuBatch:
+    """Many independent worlds stepped together (sphere/box bodies, one collider
+    each, SAP broadphase, graph-colour solve order).  ``scenes`` is a list of
+    :class:`phys_gb300.scenes.Scene` without hulls; world ``w`` holds the bodies
+    of ``scenes[w]`` in order."""
+
+    def __init__(self, scenes, device=0, iterations=8, gravity=(0.0, -9.81, 0.0)):
+        self.lib = lib()
+        counts = np.array([s.count for s in scenes], np.uint32)
+        cat = lambda f, dt: np.ascontiguousarray(np.concatenate([getattr(s, f) for s in scenes]), dt)
+        shape = cat("shape", np.uint8)
+        if np.any(shape > 1):
+            raise ValueError("batched worlds hold spheres and boxes only")
+        h = _P()
+        failed = ctypes.c_uint64()
+        self.counts = counts
+        self.starts = np.concatenate([[0], np.cumsum(counts, dtype=np.int64)])
+        check(self.lib.pe_batch_create(
+            int(device), len(counts), _ptr(counts), _ptr(shape), _ptr(cat("dims", np.float32)),
+            _ptr(cat("pos", np.float32)), _ptr(cat("density", np.float32)), _ptr(cat("is_static", np.uint8)),
+            _ptr(cat("restitution", np.float32)), _ptr(cat("friction", np.float32)),
+            _ptr(cat("linvel", np.float32)), _ptr(cat("spin", np.float32)), ctypes.byref(h), ctypes.byref(failed)))
+        self.h = h
+        self.n = int(self.starts[-1])
+        check(self.lib.pe_batch_set_iterations(self.h, int(iterations)))
+        check(self.lib.pe_batch_set_gravity(self.h, *[float(x) for x in gravity]))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pe_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def world_count(self):
+        return len(self.counts)
+
+    def step(self, dt, steps=1):
+        check(self.lib.pe_batch_step(self.h, float(dt), int(steps)))
+
+    def autotune(self, dt, repetitions=3):
+        check(self.lib.pe_batch_autotune(self.h, float(dt), int(repetitions)))
+
+    def buckets(self):
+        n = _u32()
+        check(self.lib.pe_batch_bucket_count(self.h, ctypes.byref(n)))
+        out = np.zeros(n.value, BUCKET_DTYPE)
+        for i in range(n.value):
+            check(self.lib.pe_batch_get_bucket(self.h, i, _ptr(out[i:i + 1])))
+        return out
+
+    def set_graphs(self, on):
+        check(self.lib.pe_batch_set_graphs(self.h, int(bool(on))))
+
+    def stream(self):
+        s = _P()
+        check(self.lib.pe_batch_get_stream(self.h, ctypes.byref(s)))
+        return s.value
+
+    def bodies(self):
+        """(pos[n,3], rot[n,4], lin[n,3], ang[n,3]) of all worlds, world by world."""
+        pos = np.zeros((self.n, 3), np.float32)
+        rot = np.zeros((self.n, 4), np.float32)
+        lin = np.zeros((self.n, 3), np.float32)
+        ang = np.zeros((self.n, 3), np.float32)
+        check(self.lib.pe_batch_read_bodies(self.h, _ptr(pos), _ptr(rot), _ptr(lin), _ptr(ang)))
+        return pos, rot, lin, ang
+
+    def world_bodies(self, w):
+        s, e = self.starts[w], self.starts[w + 1]
+        return tuple(a[s:e] for a in self.bodies())
+
+    def write_bodies(self, pos=None, rot=None, lin=None, ang=None):
+        f = lambda a: None if a is None else _ptr(_f32(a))
+        check(self.lib.pe_batch_write_bodies(self.h, f(pos), f(rot), f(lin), f(ang)))
+
+    def write_forces(self, forces):
+        check(self.lib.pe_batch_write_forces(self.h, _ptr(_f32(forces))))
+
+    def read_poses(self, pos, rot):
+        check(self.lib.pe_batch_read_poses(self.h, _ptr(pos), _ptr(rot)))
+
+    def stats(self, w):
+        st = np.zeros(1, STATS_DTYPE)
+        check(self.lib.pe_batch_get_world_stats(self.h, int(w), _ptr(st)))
+        return st[0]
+
+    def pairs(self, w):
+        cnt = _u32()
+        check_size(self.lib.pe_batch_get_world_pairs(self.h, int(w), None, 0, ctypes.byref(cnt)))
+        out = np.zeros((cnt.value, 2), np.uint32)
+        if cnt.value:
+            check(self.lib.pe_batch_get_world_pairs(self.h, int(w), _ptr(out), cnt.value, ctypes.byref(cnt)))
+        return out
+
+    def contacts(self, w):
+        cnt = _u32()
+        check_size(self.lib.pe_batch_get_world_contacts(self.h, int(w), None, 0, ctypes.byref(cnt)))
+        out = np.zeros(cnt.value, MANIFOLD_DTYPE)
+        if cnt.value:
+            check(self.lib.pe_batch_get_world_contacts(self.h, int(w), _ptr(out), cnt.value, ctypes.byref(cnt)))
+        return out
