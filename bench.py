@@ -291,6 +291,8 @@ def run_gpu(args, rank, world_size, local_rank):
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
+    if world_size == 1 and not args.no_batched:
+        line["batched"] = run_batched(args, local_rank, flush, peak)
     if world_size == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, steps, el, _ = cpu_port_rate(scene, 20.0, 60, threads)
@@ -301,6 +303,136 @@ def run_gpu(args, rank, world_size, local_rank):
     print(json.dumps(line), flush=True)
 
 
+BATCH_WORLDS = 4096
+BATCH_MIN, BATCH_MAX = 16, 2048
+
+
+def batch_world_sizes(count=BATCH_WORLDS, seed=SEED):
+    """Body counts log-uniform in [16, 2048] (Python's Mersenne Twister, stable
+    across platforms)."""
+    import random
+
+    r = random.Random(seed)
+    ratio = BATCH_MAX / BATCH_MIN
+    return [int(round(BATCH_MIN * ratio ** r.random())) for _ in range(count)]
+
+
+def batch_scenes(sizes):
+    from phys_gb300 import scenes
+
+    return [scenes.generate(scenes.MIXED_VOLUME, n, SEED + w) for w, n in enumerate(sizes)]
+
+
+def run_batched(args, local_rank, flush, peak):
+    """4,096 independent worlds (each the mixed workload scaled to its body
+    count, seed 42 + w) stepped by the batch engine, against looping the plain
+    single-world GPU step over a stratified sample of the same worlds."""
+    import torch
+
+    from phys_gb300 import engine
+
+    sizes = batch_world_sizes()
+    sc = batch_scenes(sizes)
+    batch = engine.GpuBatch(sc, device=local_rank, iterations=ITERATIONS)
+    stream = torch.cuda.ExternalStream(batch.stream(), device=torch.device("cuda", local_rank))
+    for _ in range(args.warmup):
+        batch.step(DT)
+    batch.autotune(DT, 3)
+    for _ in range(2):
+        batch.step(DT)
+    steps = max(1, min(args.steps, 60))
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    torch.cuda.synchronize()
+    algo_bytes = 0.0
+    totals = {"pairs": 0, "manifolds": 0, "points": 0}
+    sample_worlds = range(0, len(sizes), 64)
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.add_(1.0)
+        starts[k].record(stream)
+        batch.step(DT)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends))
+    # workload of the last step, every world (for the roofline bytes)
+    for w in range(len(sizes)):
+        st = batch.stats(w)
+        algo_bytes += sum(stage_bytes(st, sizes[w], ITERATIONS).values())
+        totals["pairs"] += int(st["candidate_pairs"])
+        totals["manifolds"] += int(st["contact_count"])
+        totals["points"] += int(st["contact_points"])
+    world_steps = len(sizes) * steps / (ms / 1000.0)
+    step_ms = ms / steps
+
+    # e2e through the C ABI with host buffers: forces in, step, poses out
+    n = batch.n
+    forces = torch.zeros((n, 3), dtype=torch.float32).pin_memory().numpy()
+    pp = torch.empty((n, 3), dtype=torch.float32).pin_memory().numpy()
+    pq = torch.empty((n, 4), dtype=torch.float32).pin_memory().numpy()
+    e2e_steps = max(1, min(steps, 30))
+    e2e_s = 0.0
+    for _ in range(e2e_steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        batch.write_forces(forces)
+        batch.step(DT)
+        batch.read_poses(pp, pq)
+        e2e_s += time.perf_counter() - t0
+    buckets = batch.buckets()
+    batch.close()
+
+    # plain loop: the single-world engine stepping each sampled world in turn
+    sample = list(range(0, len(sizes), 16))
+    worlds = []
+    for w in sample:
+        gw = engine.GpuWorld(device=local_rank, algo=engine.SAP, iterations=ITERATIONS, order=engine.ORDER_COLOR)
+        gw.load_scene(sc[w])
+        worlds.append(gw)
+    for _ in range(3):
+        for gw in worlds:
+            gw.step(DT)
+    plain_steps = 5
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(plain_steps):
+        for gw in worlds:
+            gw.step(DT)
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    plain_world_steps = len(worlds) * plain_steps / plain_s
+    for gw in worlds:
+        gw.close()
+    achieved = algo_bytes / (step_ms / 1000.0) / 1e9
+    return {
+        "metric": "world-steps/s, 4096 batched worlds (forward)",
+        "value": world_steps, "unit": "world-steps/s", "steps": steps, "ms_per_step": step_ms,
+        "body_steps_per_s": sum(sizes) * steps / (ms / 1000.0),
+        "config": {"workload": "batched_4096", "worlds": len(sizes), "bodies": int(sum(sizes)),
+                   "bodies_per_world": f"log-uniform in [{BATCH_MIN}, {BATCH_MAX}] (seed {SEED}), "
+                                       f"min {min(sizes)}, max {max(sizes)}",
+                   "world": "mixed workload scaled to the world's body count, seed 42 + world",
+                   "broadphase": "SAP", "solver_iterations": ITERATIONS, "solver_order": "graph colour",
+                   "dt": DT, "steps_of_reference_run": 600,
+                   "l2": "flushed before every timed step (512 MiB write)"},
+        "workload_per_step": totals,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "algorithmic_bytes_per_step": algo_bytes},
+        "e2e": {"value": len(sizes) * e2e_steps / e2e_s, "unit": "world-steps/s",
+                "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 32 * n, "steps": e2e_steps},
+        "gpu_launches": int(steps * len(buckets)),
+        "autotune": [{"bodies": [int(b["min_bodies"]), int(min(b["max_bodies"], BATCH_MAX))],
+                      "worlds": int(b["world_count"]), "threads": int(b["threads"]),
+                      "min_blocks_per_sm": int(b["min_blocks_per_sm"]), "blocks": int(b["blocks"]),
+                      "ms": float(b["tuned_ms"]), "candidates_ms": [float(x) for x in b["candidate_ms"][:5]]}
+                     for b in buckets],
+        "plain_loop": {"value": plain_world_steps, "unit": "world-steps/s",
+                       "sample": f"every 16th world ({len(worlds)} worlds), {plain_steps} steps each, wall clock "
+                                 f"of the single-world engine's step (CUDA graph per world, synchronous step)"},
+        "speedup_vs_plain_loop": world_steps / plain_world_steps,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -308,6 +440,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 4096-world batched measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
