@@ -89,6 +89,7 @@ def oracle_lib():
         lib.ow_get_bodies_f64.argtypes = [_P, _P, _P, _P, _P]
         lib.ow_set_velocity.argtypes = [_P, ctypes.c_uint32, _P, _P]
         lib.ow_set_velocity_f64.argtypes = [_P, ctypes.c_uint32, _P, _P]
+        lib.ow_set_position_f64.argtypes = [_P, ctypes.c_uint32, _P]
         lib.ow_apply_spin.argtypes = [_P, ctypes.c_uint32, _P]
         lib.ow_set_material.argtypes = [_P, ctypes.c_uint32, ctypes.c_double, ctypes.c_double, ctypes.c_double]
         lib.ow_get_material.argtypes = [_P, ctypes.c_uint32, _P, _P, _P]
@@ -282,6 +283,9 @@ class OracleWorld(_CpuWorld):
         lin = None if lin is None else np.ascontiguousarray(lin, np.float64)
         ang = None if ang is None else np.ascontiguousarray(ang, np.float64)
         self.lib.ow_set_velocity_f64(self.h, int(idx), _ptr(lin), _ptr(ang))
+
+    def set_position_f64(self, idx, pos):
+        self.lib.ow_set_position_f64(self.h, int(idx), _ptr(np.ascontiguousarray(pos, np.float64)))
 
     def set_material(self, idx, mass, friction, restitution):
         self.lib.ow_set_material(self.h, int(idx), float(mass), float(friction), float(restitution))

@@ -1679,6 +1679,12 @@ void ow_set_velocity_f64(ow_world *world, uint32_t i, const double *lin, const d
         if (ang) w.bodies[i].ang = {T(ang[0]), T(ang[1]), T(ang[2])};
     });
 }
+void ow_set_position_f64(ow_world *world, uint32_t i, const double *pos) {
+    dispatch(world, [&](auto &w) {
+        using T = decltype(w.gravity.x);
+        w.bodies[i].pos = {T(pos[0]), T(pos[1]), T(pos[2])};
+    });
+}
 // RigidBody::setAngularVelocity + integrateRotation(1) + setAngularVelocity(0)
 // (rigid_body.hpp:95-99, rigid_body.cpp:110-125); integrateRotation returns early
 // for static bodies (rigid_body.cpp:112-113), so their orientation stays identity.

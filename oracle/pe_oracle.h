@@ -108,6 +108,8 @@ void ow_get_bodies(const ow_world *world, float *pos, float *quat, float *lin, f
 void ow_get_bodies_f64(const ow_world *world, double *pos, double *quat, double *lin, double *ang);
 void ow_set_velocity(ow_world *world, uint32_t index, const float *lin, const float *ang);
 void ow_set_velocity_f64(ow_world *world, uint32_t index, const double *lin, const double *ang);
+/* Body position in the world's precision (finite differences). */
+void ow_set_position_f64(ow_world *world, uint32_t index, const double *pos);
 /* The reference's orientation idiom: setAngularVelocity(spin); integrateRotation(1);
    setAngularVelocity(0) (tests/solver/sequential_impulse_solver_tests.cpp:349-351). */
 void ow_apply_spin(ow_world *world, uint32_t index, const float *spin);

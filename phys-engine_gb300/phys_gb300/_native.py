@@ -21,6 +21,7 @@ BUILD = PKG_DIR / "_build"
 INCLUDE = REPO_DIR / "include"
 ENGINE_SO = BUILD / "libphys_gb300.so"
 SCENES_SO = BUILD / "libpe_scenes.so"
+FP64_SO = BUILD / "libphys_gb300_fp64.so"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [
@@ -66,6 +67,17 @@ def build_scenes(force: bool = False) -> pathlib.Path:
     return SCENES_SO
 
 
+def build_fp64(force: bool = False) -> pathlib.Path:
+    """The FP64 CPU evaluation of the differentiable rollout (a checking
+    library for the GPU adjoint; plain C++ built from the same headers)."""
+    src = CSRC / "rollout_fp64.cpp"
+    deps = [src, CSRC / "ad_math.cuh", CSRC / "ad_geom.cuh", CSRC / "ad_world.cuh", INCLUDE / "phys_gb300_fp64.h"]
+    BUILD.mkdir(parents=True, exist_ok=True)
+    if force or _stale(FP64_SO, deps):
+        _run(["g++", *CXX_FLAGS, f"-I{INCLUDE}", f"-I{CSRC}", "-shared", "-o", str(FP64_SO), str(src)])
+    return FP64_SO
+
+
 def build_engine(force: bool = False) -> pathlib.Path:
     """Compile every .cu / .cpp under csrc/ (except scenes.cpp) for sm_103a and
     link libphys_gb300.so.  Translation units compile in parallel."""
@@ -99,6 +111,10 @@ def _load(path: pathlib.Path, builder) -> ctypes.CDLL:
 
 def scenes_lib() -> ctypes.CDLL:
     return _load(SCENES_SO, build_scenes)
+
+
+def fp64_lib() -> ctypes.CDLL:
+    return _load(FP64_SO, build_fp64)
 
 
 def engine_lib() -> ctypes.CDLL:

@@ -30,6 +30,14 @@ def test_scene_library_exports():
         assert hasattr(lib, n), n
 
 
+def test_fp64_library_exports():
+    lib = ctypes.CDLL(str(_native.build_fp64()))
+    names = declared("phys_gb300_fp64.h")
+    assert names == ["pe_fp64_body_properties", "pe_fp64_rollout"]
+    for n in names:
+        assert hasattr(lib, n), n
+
+
 def test_scenes_are_deterministic_and_valid():
     a = scenes.generate(scenes.MIXED_VOLUME, 2000, 42)
     b = scenes.generate(scenes.MIXED_VOLUME, 2000, 42)
