@@ -305,6 +305,44 @@ pe_status pe_batch_get_world_contacts(pe_batch *batch, uint32_t world, pe_contac
 pe_status pe_batch_get_stream(pe_batch *batch, void **stream);
 pe_status pe_batch_set_graphs(pe_batch *batch, int enabled);
 
+/* ------------------------------------------------------------------------
+   Differentiable batched rollout (no reference counterpart; the reference has
+   no differentiation).  Many independent worlds of sphere/box bodies (1 to 256
+   per world, one collider each) are stepped `steps` times with
+   PhysicsWorld::step's algorithm (SAP pair set, graph-colour solve order) on
+   the GPU; the adjoint returns the gradients of sum(d_final . final state)
+   with respect to the initial state and to each body's mass (the RigidBody
+   field; the inverse inertia stays as created), friction and restitution.
+   The contact set of the forward pass is frozen in the adjoint (pairs, kept
+   contact features, colour order, warm-start matches, clamp branches); contact
+   points, normals and depths are differentiated as functions of the poses.
+   Memory: states are checkpointed every `checkpoint_every` steps and each
+   segment is recomputed once during the adjoint.
+   State arrays are DEVICE pointers holding all worlds' bodies back to back:
+   positions / linear / angular velocities 3 floats per body, rotations 4
+   (x, y, z, w).  Calls run on `stream` and return when the work is done.
+   ------------------------------------------------------------------------ */
+typedef struct pe_rollout pe_rollout;
+
+/* dims / density / is_static as pe_world_create_bodies; mass_out (host, may be
+   NULL) receives the created masses (volume x density). */
+pe_status pe_rollout_create(int device, uint32_t world_count, const uint32_t *world_body_counts,
+                            const uint8_t *shape, const float *dims, const float *density, const uint8_t *is_static,
+                            uint32_t steps, float dt, int iterations, uint32_t checkpoint_every, pe_rollout **out,
+                            float *mass_out);
+void pe_rollout_destroy(pe_rollout *rollout);
+pe_status pe_rollout_set_gravity(pe_rollout *rollout, float x, float y, float z);
+pe_status pe_rollout_forward(pe_rollout *rollout, const float *x0, const float *q0, const float *v0,
+                             const float *w0, const float *mass, const float *friction, const float *restitution,
+                             float *x_final, float *q_final, float *v_final, float *w_final, void *stream);
+/* Adjoint of the last forward call; any d_final_* input or output may be NULL. */
+pe_status pe_rollout_backward(pe_rollout *rollout, const float *d_final_x, const float *d_final_q,
+                              const float *d_final_v, const float *d_final_w, float *d_x0, float *d_q0,
+                              float *d_v0, float *d_w0, float *d_mass, float *d_friction, float *d_restitution,
+                              void *stream);
+/* Device time of the last forward and backward calls (ms). */
+pe_status pe_rollout_timings(pe_rollout *rollout, double *forward_ms, double *backward_ms);
+
 /* Allocation-free sweep-and-prune query.  It has no counterpart in the
    reference: it exists for callers that may not allocate device memory at all
    (an engine that gives this library a fixed slice of its own memory arena, a

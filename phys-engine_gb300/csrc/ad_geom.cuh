@@ -39,7 +39,7 @@ template <class S> AD_HD S boxProjectedRadius(const V3<S> &he, const M3<S> &r, c
 
 // intersectSphereSphere (narrowphase.cpp:132-160)
 template <class S>
-AD_HD bool sphereSphere(const S &rA, const Tf<S> &tA, const S &rB, const Tf<S> &tB, Contact<S> &m) {
+AD_HDN bool sphereSphere(const S &rA, const Tf<S> &tA, const S &rB, const Tf<S> &tB, Contact<S> &m) {
     V3<S> delta = tB.p - tA.p;
     S distance = length(delta);
     S radii = rA + rB;
@@ -58,7 +58,7 @@ AD_HD bool sphereSphere(const S &rA, const Tf<S> &tA, const S &rB, const Tf<S> &
 
 // intersectSphereBox (narrowphase.cpp:162-248)
 template <class S>
-AD_HD bool sphereBox(const S &r, const Tf<S> &tS, const V3<S> &he, const Tf<S> &tB, Contact<S> &m) {
+AD_HDN bool sphereBox(const S &r, const Tf<S> &tS, const V3<S> &he, const Tf<S> &tB, Contact<S> &m) {
     V3<S> c = rotate(conj(tB.q), tS.p - tB.p);
     V3<S> cl{clampv(c.x, -he.x, he.x), clampv(c.y, -he.y, he.y), clampv(c.z, -he.z, he.z)};
     V3<S> dl = cl - c;
@@ -114,7 +114,7 @@ AD_HD bool satAxis(const M3<S> &rA, const V3<S> &heA, const M3<S> &rB, const V3<
 
 // testOBBOBB (sat.cpp:66-102)
 template <class S>
-AD_HD bool satBoxBox(const V3<S> &heA, const Tf<S> &tA, const M3<S> &rA, const V3<S> &heB, const Tf<S> &tB,
+AD_HDN bool satBoxBox(const V3<S> &heA, const Tf<S> &tA, const M3<S> &rA, const V3<S> &heB, const Tf<S> &tB,
                      const M3<S> &rB, V3<S> &axis, S &depth) {
     depth = ADL(S, 3.402823466e+38f);
     V3<S> cd = tB.p - tA.p;
@@ -132,7 +132,7 @@ AD_HD bool satBoxBox(const V3<S> &heA, const Tf<S> &tA, const M3<S> &rA, const V
 
 // addFaceCandidates (narrowphase.cpp:281-304) for one source box face.
 template <class S>
-AD_HD void boxFaceCandidates(const V3<S> &srcHe, const Tf<S> &srcTf, const V3<S> &othHe, const Tf<S> &othTf,
+AD_HDN void boxFaceCandidates(const V3<S> &srcHe, const Tf<S> &srcTf, const V3<S> &othHe, const Tf<S> &othTf,
                              const V3<S> &dir, uint32_t source, V3<S> *contacts, S *depths, uint32_t *feats,
                              uint32_t &count) {
     S otherSurface = dot(boxSupport(othHe, othTf, -dir), dir);
@@ -176,7 +176,7 @@ AD_HD void boxFaceCandidates(const V3<S> &srcHe, const Tf<S> &srcTf, const V3<S>
 
 // intersectBoxBox (narrowphase.cpp:250-324)
 template <class S>
-AD_HD bool boxBox(const V3<S> &heA, const Tf<S> &tA, const V3<S> &heB, const Tf<S> &tB, Contact<S> &m) {
+AD_HDN bool boxBox(const V3<S> &heA, const Tf<S> &tA, const V3<S> &heB, const Tf<S> &tB, Contact<S> &m) {
     M3<S> rA = toMat3(tA.q), rB = toMat3(tB.q);
     V3<S> normal;
     S penetration;
@@ -222,7 +222,7 @@ AD_HD bool boxBox(const V3<S> &heA, const Tf<S> &tA, const V3<S> &heB, const Tf<
 // Shape dispatch with the box-sphere swap (narrowphase.cpp:326-374).
 // shape: 0 sphere (dims.x = radius), 1 box (dims = half extents).
 template <class S>
-AD_HD bool contactPair(uint32_t sa, const V3<S> &da, const Tf<S> &tA, uint32_t sb, const V3<S> &db,
+AD_HDN bool contactPair(uint32_t sa, const V3<S> &da, const Tf<S> &tA, uint32_t sb, const V3<S> &db,
                        const Tf<S> &tB, Contact<S> &m) {
     m.count = 0;
     bool hit;
@@ -259,7 +259,7 @@ template <class S> struct Prepared {
 constexpr int kPreparedScalars = 38;
 
 template <class S>
-AD_HD void preparePoint(const V3<S> &n, const V3<S> &anchorA, const V3<S> &anchorB, const S &penetration,
+AD_HDN void preparePoint(const V3<S> &n, const V3<S> &anchorA, const V3<S> &anchorB, const S &penetration,
                         const Q<S> &qA, const Q<S> &qB, const M3<S> &IA, const M3<S> &IB, const S &imA,
                         const S &imB, const V3<S> &linA, const V3<S> &angA, const V3<S> &linB, const V3<S> &angB,
                         const S &rest, const S &inverseDt, Prepared<S> &o) {

@@ -11,8 +11,12 @@
 
 #if defined(__CUDACC__)
 #define AD_HD __host__ __device__ __forceinline__
+// Large routines are compiled once and called, which keeps the kernels' code
+// size and compile time down.
+#define AD_HDN __host__ __device__ __noinline__
 #else
 #define AD_HD inline
+#define AD_HDN inline
 #endif
 
 namespace pe {

@@ -212,7 +212,7 @@ template <class S> struct PointIn {
     S ln, l1, l2;
 };
 template <class S>
-AD_HD void pointForward(const V3<S> &n, const S &friction, const S *c, const S &imA, const S &imB, bool sA, bool sB,
+AD_HDN void pointForward(const V3<S> &n, const S &friction, const S *c, const S &imA, const S &imB, bool sA, bool sB,
                         PointIn<S> &st) {
     const S iem = c[kPIem];
     if (val(iem) <= 0.0f) return;
@@ -267,7 +267,7 @@ AD_HD void pointForward(const V3<S> &n, const S &friction, const S *c, const S &
 // prepared constants go to ac[], of the normal to an, of the friction to amu,
 // of the inverse masses to aimA / aimB.
 template <class S>
-AD_HD void pointReverse(const V3<S> &n, const S &friction, const S *c, const S &imA, const S &imB, bool sA, bool sB,
+AD_HDN void pointReverse(const V3<S> &n, const S &friction, const S *c, const S &imA, const S &imB, bool sA, bool sB,
                         const PointIn<S> &in, PointIn<S> &a, S *ac, V3<S> &an, S &amu, S &aimA, S &aimB) {
     const S iem = c[kPIem];
     if (val(iem) <= 0.0f) return;
@@ -796,7 +796,7 @@ AD_HD void forwardStep(const WorldParams<S> &W, const StateView<S> &in, const Ca
 // evaluated in dual numbers for directions [base, base + kDualChunk); returns
 // the directional derivatives of sum(adjoint * output) in g[].
 template <class S>
-AD_HD bool manifoldDualChunk(const WorldParams<S> &W, const StateView<S> &in, const StateView<S> &v1,
+AD_HDN bool manifoldDualChunk(const WorldParams<S> &W, const StateView<S> &in, const StateView<S> &v1,
                              const StepScratch<S> &sc, const AdjointView<S> &adj, uint32_t k, int base, S *g) {
     using D = Dual<S, kDualChunk>;
     const uint32_t m = sc.order[k];

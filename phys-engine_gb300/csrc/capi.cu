@@ -8,6 +8,7 @@
 
 #include "phys_gb300.h"
 #include "batch.h"
+#include "rollout.h"
 #include "world.h"
 
 struct pe_world {
@@ -17,6 +18,10 @@ struct pe_world {
 
 struct pe_batch {
     std::unique_ptr<pe::Batch> b;
+};
+
+struct pe_rollout {
+    std::unique_ptr<pe::Rollout> r;
 };
 
 namespace {
@@ -813,6 +818,79 @@ pe_status pe_batch_get_stream(pe_batch *batch, void **stream) {
 pe_status pe_batch_set_graphs(pe_batch *batch, int enabled) {
     if (!batch) return fail(PE_ERR_INVALID_ARGUMENT, "null batch");
     batch->b->setGraphsEnabled(enabled != 0);
+    return PE_OK;
+}
+
+
+// --------------------------------------------------------------- rollout ---
+pe_status pe_rollout_create(int device, uint32_t worldCount, const uint32_t *worldBodies, const uint8_t *shape,
+                            const float *dims, const float *density, const uint8_t *isStatic, uint32_t steps,
+                            float dt, int iterations, uint32_t checkpointEvery, pe_rollout **out, float *massOut) {
+    if (!out || !worldBodies || !shape || !dims || !density || !isStatic)
+        return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    return guarded([&] {
+        std::vector<uint32_t> counts(worldBodies, worldBodies + worldCount);
+        uint64_t total = 0;
+        for (uint32_t n : counts) total += n;
+        std::vector<uint8_t> sh(shape, shape + total), st(isStatic, isStatic + total);
+        std::vector<float> he(3 * total), ii(3 * total);
+        for (uint64_t i = 0; i < total; ++i) {
+            if (shape[i] != PE_SHAPE_SPHERE && shape[i] != PE_SHAPE_BOX)
+                return fail(PE_ERR_INVALID_ARGUMENT, "sphere or box shapes expected");
+            pe::HostBody b;
+            if (const char *err = makeBody(shape[i], dims + 3 * i, dims + 3 * i, density[i], isStatic[i], 0.0f, 0.0f, b))
+                return fail(PE_ERR_CREATE_FAILED, std::string("body ") + std::to_string(i) + ": " + err);
+            for (int j = 0; j < 3; ++j) {
+                he[3 * i + j] = shape[i] == PE_SHAPE_SPHERE ? dims[3 * i] : dims[3 * i + j] * 0.5f;
+                ii[3 * i + j] = b.iinv[j];
+            }
+            if (massOut) massOut[i] = b.mass;
+        }
+        std::unique_ptr<pe_rollout> r(new pe_rollout);
+        r->r.reset(new pe::Rollout(device));
+        r->r->create(counts, sh, st, he, ii, steps, dt, iterations, checkpointEvery);
+        *out = r.release();
+        return PE_OK;
+    });
+}
+
+void pe_rollout_destroy(pe_rollout *rollout) { delete rollout; }
+
+pe_status pe_rollout_set_gravity(pe_rollout *rollout, float x, float y, float z) {
+    if (!rollout) return fail(PE_ERR_INVALID_ARGUMENT, "null rollout");
+    rollout->r->gravity[0] = x;
+    rollout->r->gravity[1] = y;
+    rollout->r->gravity[2] = z;
+    return PE_OK;
+}
+
+pe_status pe_rollout_forward(pe_rollout *rollout, const float *x0, const float *q0, const float *v0, const float *w0,
+                             const float *mass, const float *friction, const float *restitution, float *xT,
+                             float *qT, float *vT, float *wT, void *stream) {
+    if (!rollout) return fail(PE_ERR_INVALID_ARGUMENT, "null rollout");
+    return guarded([&] {
+        rollout->r->forward(x0, q0, v0, w0, mass, friction, restitution, xT, qT, vT, wT,
+                            static_cast<cudaStream_t>(stream));
+        return PE_OK;
+    });
+}
+
+pe_status pe_rollout_backward(pe_rollout *rollout, const float *dx, const float *dq, const float *dv, const float *dw,
+                              float *dx0, float *dq0, float *dv0, float *dw0, float *dmass, float *dfriction,
+                              float *drest, void *stream) {
+    if (!rollout) return fail(PE_ERR_INVALID_ARGUMENT, "null rollout");
+    return guarded([&] {
+        rollout->r->backward(dx, dq, dv, dw, dx0, dq0, dv0, dw0, dmass, dfriction, drest,
+                             static_cast<cudaStream_t>(stream));
+        return PE_OK;
+    });
+}
+
+pe_status pe_rollout_timings(pe_rollout *rollout, double *fwd, double *bwd) {
+    if (!rollout) return fail(PE_ERR_INVALID_ARGUMENT, "null rollout");
+    if (fwd) *fwd = rollout->r->lastForwardMs();
+    if (bwd) *bwd = rollout->r->lastBackwardMs();
     return PE_OK;
 }
 

@@ -125,6 +125,13 @@ SIGNATURES = {
     "pe_batch_get_world_contacts": (ctypes.c_int, [_P, _u32, _P, _u32, _P]),
     "pe_batch_get_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "pe_batch_set_graphs": (ctypes.c_int, [_P, ctypes.c_int]),
+    "pe_rollout_create": (ctypes.c_int, [ctypes.c_int, _u32, _P, _P, _P, _P, _P, _u32, ctypes.c_float, ctypes.c_int,
+                                         _u32, ctypes.POINTER(_P), _P]),
+    "pe_rollout_destroy": (None, [_P]),
+    "pe_rollout_set_gravity": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float]),
+    "pe_rollout_forward": (ctypes.c_int, [_P] + [_P] * 12),
+    "pe_rollout_backward": (ctypes.c_int, [_P] + [_P] * 12),
+    "pe_rollout_timings": (ctypes.c_int, [_P, _P, _P]),
 }
 
 BUCKET_DTYPE = np.dtype([

@@ -1,0 +1,151 @@
+"""GPU tests of the differentiable rollout: the forward pass equals the batched
+engine bit for bit; the FP32 adjoint matches the FP64 CPU adjoint within 1e-3
+(relative to the larger of the entry and 1 % of the largest gradient); the
+torch.autograd.Function harness gives the gradients of a centre-of-mass loss
+that match central finite differences through the oracle's FP64 step."""
+import numpy as np
+import pytest
+
+from helpers import assert_bit_equal
+from oracle import cpu
+from phys_gb300 import rollout, scenes
+
+pytestmark = pytest.mark.gpu
+
+DT = 1 / 120
+ITERS = 10
+
+
+def sliding_boxes(n, seed, embed=0.02, impact=False):
+    sc = scenes.generate(scenes.BOXES_ON_PLANE, n, seed)
+    rng = np.random.default_rng(seed)
+    ang = rng.uniform(0, 2 * np.pi, n)
+    speed = rng.uniform(1.5, 2.5, n)
+    sc.linvel[1:] = np.stack([speed * np.cos(ang), np.zeros(n), speed * np.sin(ang)], 1).astype(np.float32)
+    sc.pos[1:, 1] -= np.float32(embed)
+    if impact:
+        sc.linvel[1:, 1] = np.float32(-2.0)
+    return sc
+
+
+def mixed_world(seed):
+    sc = sliding_boxes(4, seed)
+    extra = scenes.generate(scenes.SPHERES_ON_FLOOR, 3, seed)
+    for f in ("shape", "is_static", "dims", "pos", "density", "restitution", "friction", "linvel", "spin", "hull_id",
+              "mass", "inv_inertia"):
+        setattr(sc, f, np.concatenate([getattr(sc, f), getattr(extra, f)[1:]]))
+    r = sc.dims[-3:, 0]
+    sc.pos[-3] = [5.0, r[0] - 0.02, 5.0]
+    sc.pos[-2] = [5.0 + r[0] + r[1] - 0.04, r[1] - 0.02, 5.0]
+    sc.linvel[-3:] = 0
+    sc.linvel[-1] = [0.5, 0.0, 0.0]
+    sc.pos[-1] = [-5.0, r[2] - 0.02, -5.0]
+    sc.restitution[-3:] = [0.1, 0.2, 0.25]
+    return sc
+
+
+def torch_state(roll):
+    import torch
+
+    x0, q0, v0, w0 = roll.initial_state()
+    t = lambda a: torch.tensor(a, device="cuda:0")
+    return t(x0), t(q0), t(v0), t(w0), t(roll.mass), t(roll.friction), t(roll.restitution)
+
+
+def test_rollout_forward_matches_batch_engine(gpu):
+    sc = [sliding_boxes(6, 1), mixed_world(2), scenes.generate(scenes.MIXED_VOLUME, 40, 3)]
+    steps = 30
+    roll = rollout.GpuRollout(sc, steps, DT, iterations=ITERS, checkpoint_every=7)
+    outs = roll.forward(*torch_state(roll))
+    batch = gpu.GpuBatch(sc, iterations=ITERS)
+    batch.step(DT, steps)
+    ref = batch.bodies()
+    for k, (o, r) in enumerate(zip(outs, ref)):
+        assert_bit_equal(o.cpu().numpy(), r, f"state {k}")
+
+
+def test_rollout_gradients_match_fp64_adjoint(gpu):
+    import torch
+
+    sc = [sliding_boxes(6, 1), mixed_world(2), sliding_boxes(5, 4, impact=True)]
+    steps = [20, 20, 8]
+    rng = np.random.default_rng(5)
+    for w, s in enumerate(sc):
+        roll = rollout.GpuRollout([s], steps[w], DT, iterations=ITERS, checkpoint_every=6)
+        state = torch_state(roll)
+        outs = roll.forward(*state)
+        d = [rng.normal(size=tuple(o.shape)).astype(np.float32) for o in outs]
+        grads = roll.backward(*[torch.tensor(a, device="cuda:0") for a in d])
+        mass32, iinv, he = rollout.body_properties(s)
+        x0, q0, v0, w0 = roll.initial_state()
+        _, ref = rollout.fp64_rollout(s.shape, s.is_static, he, iinv, [x0, q0, v0, w0], roll.mass, roll.friction,
+                                      roll.restitution, steps[w], DT, ITERS, d_final=d)
+        dyn = ~s.is_static.astype(bool)
+        for name, g, r in zip(("x0", "q0", "v0", "w0", "mass", "friction", "restitution"), grads, ref):
+            g = g.cpu().numpy()[dyn]
+            r = r[dyn]
+            scale = np.abs(r).max()
+            if scale == 0:
+                assert np.abs(g).max() < 1e-5, (w, name)
+                continue
+            err = np.abs(g - r) / np.maximum(np.abs(r), 1e-2 * scale)
+            assert err.max() <= 1e-3, (w, name, float(err.max()), g.ravel()[:6], r.ravel()[:6])
+
+
+def test_rollout_autograd_com_loss_matches_oracle_fd(gpu):
+    import torch
+
+    # boxes (half extents U[0.2,0.5], friction U[0.2,0.8], restitution U[0,0.3])
+    # on a plane, sliding, two worlds; loss = |COM_final - target|^2
+    sc = [sliding_boxes(8, 11), sliding_boxes(8, 12)]
+    steps = 24
+    roll = rollout.GpuRollout(sc, steps, DT, iterations=ITERS, checkpoint_every=10)
+    fn = rollout.rollout_function()
+    x0, q0, v0, w0, m, f, r = (t.requires_grad_(True) for t in torch_state(roll))
+    xT, qT, vT, wT = fn.apply(roll, x0, q0, v0, w0, m, f, r)
+    target = torch.tensor([[1.0, 0.5, -2.0], [-3.0, 0.2, 1.0]], device="cuda:0")
+    loss = 0
+    dyn = torch.tensor(~np.concatenate([s.is_static for s in sc]).astype(bool), device="cuda:0")
+    for w in range(2):
+        s0, s1 = int(roll.starts[w]), int(roll.starts[w + 1])
+        mw = m[s0:s1] * dyn[s0:s1]
+        com = (mw[:, None] * xT[s0:s1]).sum(0) / mw.sum()
+        loss = loss + ((com - target[w]) ** 2).sum()
+    loss.backward()
+
+    def oracle_loss(w, which, i, j, eps):
+        s = sc[w]
+        ow = cpu.OracleWorld(fp64=True, algo=0, iterations=ITERS, order_mode=1)
+        ow.load_scene(s)
+        mat = np.array([ow.material(k) for k in range(s.count)])
+        if which == "v":
+            b = ow.bodies_f64()
+            v = b["lin"][i].copy()
+            v[j] += eps
+            ow.set_velocity_f64(i, v, b["ang"][i])
+        elif which in ("m", "f", "r"):
+            mm, ff, rr = mat[i]
+            mm, ff, rr = mm + eps * (which == "m"), ff + eps * (which == "f"), rr + eps * (which == "r")
+            ow.set_material(i, mm, ff, rr)
+            mat[i] = (mm, ff, rr)
+        for _ in range(steps):
+            ow.step(DT)
+        x = ow.bodies_f64()["pos"]
+        mw = mat[:, 0] * (~s.is_static.astype(bool))
+        com = (mw[:, None] * x).sum(0) / mw.sum()
+        return float(((com - target[w].cpu().numpy().astype(np.float64)) ** 2).sum())
+
+    def fd(w, which, i, j=0, eps=1e-4):
+        return (oracle_loss(w, which, i, j, eps) - oracle_loss(w, which, i, j, -eps)) / (2 * eps)
+
+    gv, gm, gf, gr = v0.grad.cpu().numpy(), m.grad.cpu().numpy(), f.grad.cpu().numpy(), r.grad.cpu().numpy()
+    checks = []
+    for w in range(2):
+        base = int(roll.starts[w])
+        for i in (1, 3, 6):
+            checks += [(w, "v", i, 0, gv[base + i, 0]), (w, "v", i, 2, gv[base + i, 2]),
+                       (w, "m", i, 0, gm[base + i]), (w, "f", i, 0, gf[base + i])]
+    scale = max(abs(c[4]) for c in checks)
+    for w, which, i, j, a in checks:
+        ref = fd(w, which, i, j)
+        assert abs(a - ref) <= 1e-3 * max(abs(ref), 1e-2 * scale), (w, which, i, j, a, ref)
