@@ -293,6 +293,7 @@ def run_gpu(args, rank, world_size, local_rank):
     }
     if world_size == 1 and not args.no_batched:
         line["batched"] = run_batched(args, local_rank, flush, peak)
+        line["differentiable"] = run_differentiable(args, local_rank)
     if world_size == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, steps, el, _ = cpu_port_rate(scene, 20.0, 60, threads)
@@ -430,6 +431,119 @@ def run_batched(args, local_rank, flush, peak):
                        "sample": f"every 16th world ({len(worlds)} worlds), {plain_steps} steps each, wall clock "
                                  f"of the single-world engine's step (CUDA graph per world, synchronous step)"},
         "speedup_vs_plain_loop": world_steps / plain_world_steps,
+    }
+
+
+DIFF_WORLDS = 1024
+DIFF_BODIES = 64
+DIFF_STEPS = 120
+DIFF_DT = 1.0 / 120.0
+DIFF_CHECKPOINT = 10
+
+
+def run_differentiable(args, local_rank):
+    """1,024 worlds x 64 boxes (half extents U[0.2,0.5], friction U[0.2,0.8],
+    restitution U[0,0.3]) at rest on a plane, 120 steps at dt = 1/120; loss =
+    squared distance of each world's final centre of mass from a seeded target
+    within 5 m; gradients with respect to initial velocities, masses, frictions
+    and restitutions through the GPU adjoint (checkpoint every 10 steps)."""
+    import random
+
+    import torch
+
+    from phys_gb300 import engine, rollout, scenes
+
+    sc = [scenes.generate(scenes.BOXES_ON_PLANE, DIFF_BODIES, SEED + w) for w in range(DIFF_WORLDS)]
+    roll = rollout.GpuRollout(sc, DIFF_STEPS, DIFF_DT, iterations=ITERATIONS, checkpoint_every=DIFF_CHECKPOINT,
+                              device=local_rank)
+    fn = rollout.rollout_function()
+    dev = torch.device("cuda", local_rank)
+    r = random.Random(SEED)
+    targets = []
+    for _ in range(DIFF_WORLDS):
+        while True:
+            t = [r.uniform(-5, 5) for _ in range(3)]
+            if sum(c * c for c in t) <= 25.0:
+                break
+        targets.append(t)
+    target = torch.tensor(targets, device=dev)
+    x0n, q0n, v0n, w0n = roll.initial_state()
+    dyn = torch.tensor(~roll.is_static.astype(bool), device=dev)
+    world_of = torch.tensor(np.repeat(np.arange(DIFF_WORLDS), roll.counts), device=dev)
+
+    def one(host):
+        """Host tensors in (pinned), loss + gradients out to the host."""
+        ins = [t.to(dev, non_blocking=True) for t in host]
+        for t in ins[2:]:
+            t.requires_grad_(True)
+        x0, q0, v0, w0, m, f, rs = ins
+        xT, qT, vT, wT = fn.apply(roll, x0, q0, v0, w0, m, f, rs)
+        mw = m * dyn
+        msum = torch.zeros(DIFF_WORLDS, device=dev).index_add_(0, world_of, mw)
+        com = torch.zeros(DIFF_WORLDS, 3, device=dev).index_add_(0, world_of, mw[:, None] * xT) / msum[:, None]
+        loss = ((com - target) ** 2).sum()
+        loss.backward()
+        grads = [v0.grad, m.grad, f.grad, rs.grad]
+        return float(loss.item()), [g.to("cpu", non_blocking=True) for g in grads]
+
+    pin = lambda a: torch.tensor(a).pin_memory()
+    host = [pin(x0n), pin(q0n), pin(v0n), pin(w0n), pin(roll.mass), pin(roll.friction), pin(roll.restitution)]
+    for _ in range(2):
+        one(host)
+    reps = 3
+    fwd_ms = bwd_ms = 0.0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        loss, grads = one(host)
+        f_ms, b_ms = roll.timings()
+        fwd_ms += f_ms
+        bwd_ms += b_ms
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    device_s = (fwd_ms + bwd_ms) / 1000.0
+    ws = DIFF_WORLDS * DIFF_STEPS * reps
+    h2d = sum(int(t.numel() * t.element_size()) for t in host)
+    d2h = 4 * roll.n * 6 + 4
+    # plain loop: forward steps of the single-world engine over a sample of the same worlds
+    worlds = []
+    for w in range(0, DIFF_WORLDS, 32):
+        gw = engine.GpuWorld(device=local_rank, algo=engine.SAP, iterations=ITERATIONS, order=engine.ORDER_COLOR)
+        gw.load_scene(sc[w])
+        worlds.append(gw)
+    for _ in range(3):
+        for gw in worlds:
+            gw.step(DIFF_DT)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    plain_steps = 10
+    for _ in range(plain_steps):
+        for gw in worlds:
+            gw.step(DIFF_DT)
+    torch.cuda.synchronize()
+    plain = len(worlds) * plain_steps / (time.perf_counter() - t1)
+    for gw in worlds:
+        gw.close()
+    value = ws / device_s
+    return {
+        "metric": "world-steps/s, 1024 worlds forward + adjoint", "value": value, "unit": "world-steps/s",
+        "rollouts": reps, "forward_ms_per_rollout": fwd_ms / reps, "adjoint_ms_per_rollout": bwd_ms / reps,
+        "config": {"workload": "differentiable_1024x64", "worlds": DIFF_WORLDS, "bodies_per_world": DIFF_BODIES,
+                   "shapes": "boxes half-extents U[0.2,0.5] on a static 40x1x40 m plane, at rest",
+                   "friction": "U[0.2,0.8]", "restitution": "U[0,0.3]", "steps": DIFF_STEPS, "dt": DIFF_DT,
+                   "solver_iterations": ITERATIONS, "checkpoint_every": DIFF_CHECKPOINT,
+                   "loss": "sum over worlds of |final centre of mass - target|^2, targets seeded within 5 m",
+                   "gradients": "initial velocities, masses, frictions, restitutions (torch.autograd)"},
+        "loss": loss,
+        "e2e": {"value": ws / e2e_s, "unit": "world-steps/s", "h2d_bytes_per_step": h2d / DIFF_STEPS,
+                "d2h_bytes_per_step": d2h / DIFF_STEPS,
+                "note": "each rollout copies the initial state and parameters in from pinned host memory and "
+                        "the loss and the four gradient arrays out; bytes per step = per rollout / 120"},
+        "gpu_launches": 2 * reps,
+        "plain_loop": {"value": plain, "unit": "world-steps/s",
+                       "sample": f"every 32nd world ({len(worlds)} worlds), {plain_steps} forward steps each, "
+                                 f"wall clock of the single-world engine's step"},
+        "speedup_vs_plain_loop": value / plain,
     }
 
 

@@ -1067,50 +1067,63 @@ AD_HD void backwardStep(const WorldParams<S> &W, const StateView<S> &in, const C
         adj.amuM[k] = amu;
     }
     T::sync();
-    // 5. contact geometry + preparation (dual numbers), 6. materials
-    for (uint32_t k = tid; k < M; k += nt) {
+    // 5. contact geometry + preparation (dual numbers): one (manifold, chunk of
+    // four directions) per thread; 6. materials with the last chunk
+    constexpr int kChunks = (kDualInputs + kDualChunk - 1) / kDualChunk;
+    for (uint32_t item = tid; item < M * kChunks; item += nt) {
+        const uint32_t k = item / kChunks;
+        const int chunk = (int)(item % kChunks), base = chunk * kDualChunk;
         const uint32_t m = sc.order[k];
         const uint32_t a = sc.mA[m], b = sc.mB[m];
         const bool sA = W.isStatic[a] != 0, sB = W.isStatic[b] != 0;
-        S gr[kDualChunk * ((kDualInputs + kDualChunk - 1) / kDualChunk)];
-        bool ok = true;
-        for (int base = 0; base < kDualInputs && ok; base += kDualChunk)
-            ok = manifoldDualChunk(W, in, v1, sc, adj, k, base, gr + base);
-        if (!ok) {
+        S gr[kDualChunk];
+        if (!manifoldDualChunk(W, in, v1, sc, adj, k, base, gr)) {
             T::orErr(&sc.counts[3], kAdErrReplay);
             continue;
         }
-        if (!sA) {
-            for (int e = 0; e < 3; ++e) {
-                T::add(&adj.ax[3 * a + e], gr[e]);
-                T::add(&adj.av[3 * a + e], gr[14 + e]);
-                T::add(&adj.aw[3 * a + e], gr[17 + e]);
+        for (int j = 0; j < kDualChunk; ++j) {
+            const int d = base + j;
+            if (d >= kDualInputs) break;
+            const S gv = gr[j];
+            if (d < 3) {
+                if (!sA) T::add(&adj.ax[3 * a + d], gv);
+            } else if (d < 7) {
+                if (!sA) T::add(&adj.aq[4 * a + (d - 3)], gv);
+            } else if (d < 10) {
+                if (!sB) T::add(&adj.ax[3 * b + (d - 7)], gv);
+            } else if (d < 14) {
+                if (!sB) T::add(&adj.aq[4 * b + (d - 10)], gv);
+            } else if (d < 17) {
+                if (!sA) T::add(&adj.av[3 * a + (d - 14)], gv);
+            } else if (d < 20) {
+                if (!sA) T::add(&adj.aw[3 * a + (d - 17)], gv);
+            } else if (d < 23) {
+                if (!sB) T::add(&adj.av[3 * b + (d - 20)], gv);
+            } else if (d < 26) {
+                if (!sB) T::add(&adj.aw[3 * b + (d - 23)], gv);
+            } else if (d == 26) {
+                if (!sA) T::add(&adj.amass[a], gv);
+            } else if (d == 27) {
+                if (!sB) T::add(&adj.amass[b], gv);
+            } else {
+                // restitution = max(ra, rb)
+                const S arest = adj.arestM[k] + gv;
+                if (W.rest[a] < W.rest[b]) {
+                    if (!sB) T::add(&adj.arest[b], arest);
+                } else if (!sA) {
+                    T::add(&adj.arest[a], arest);
+                }
             }
-            for (int e = 0; e < 4; ++e) T::add(&adj.aq[4 * a + e], gr[3 + e]);
-            T::add(&adj.amass[a], gr[26]);
         }
-        if (!sB) {
-            for (int e = 0; e < 3; ++e) {
-                T::add(&adj.ax[3 * b + e], gr[7 + e]);
-                T::add(&adj.av[3 * b + e], gr[20 + e]);
-                T::add(&adj.aw[3 * b + e], gr[23 + e]);
+        if (chunk == 0) {
+            // friction = sqrt(max(fa, 0) * max(fb, 0))
+            const S fm = sc.mMu[m];
+            if (fm > z) {
+                const S fa = smax(W.mu[a], z), fb = smax(W.mu[b], z);
+                const S amu = adj.amuM[k] * (S(0.5f) / fm);
+                if (!sA && !(W.mu[a] < z)) T::add(&adj.amu[a], amu * fb);
+                if (!sB && !(W.mu[b] < z)) T::add(&adj.amu[b], amu * fa);
             }
-            for (int e = 0; e < 4; ++e) T::add(&adj.aq[4 * b + e], gr[10 + e]);
-            T::add(&adj.amass[b], gr[27]);
-        }
-        // restitution = max(ra, rb); friction = sqrt(max(fa, 0) * max(fb, 0))
-        const S arest = adj.arestM[k] + gr[28];
-        if (W.rest[a] < W.rest[b]) {
-            if (!sB) T::add(&adj.arest[b], arest);
-        } else if (!sA) {
-            T::add(&adj.arest[a], arest);
-        }
-        const S fm = sc.mMu[m];
-        if (fm > z) {
-            const S fa = smax(W.mu[a], z), fb = smax(W.mu[b], z);
-            const S amu = adj.amuM[k] * (S(0.5f) / fm);
-            if (!sA && !(W.mu[a] < z)) T::add(&adj.amu[a], amu * fb);
-            if (!sB && !(W.mu[b] < z)) T::add(&adj.amu[b], amu * fa);
         }
     }
     T::sync();
