@@ -150,6 +150,20 @@ def stage_bytes(stats, bodies, iterations):
 
 
 # ------------------------------------------------------------ CPU legs
+def profiled_traffic(kernel, algorithmic_bytes):
+    """DRAM bytes (read + write) of `kernel` from the committed ncu capture
+    (profiles/traffic.json), scaled from the captured launch to one of
+    `algorithmic_bytes` by the ratio of algorithmic bytes; or None."""
+    p = REPO / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    entry = json.loads(p.read_text()).get(kernel)
+    if not entry:
+        return None
+    scale = algorithmic_bytes / entry["algorithmic_bytes_per_launch"]
+    return {"bytes": entry["dram_bytes_per_launch"] * scale, "source": entry["source"]}
+
+
 def cpu_port_rate(scene, budget_s: float, max_steps: int, threads: int):
     """Oracle port (reference algorithm, reference order) on the host cores."""
     from oracle import cpu
@@ -267,19 +281,26 @@ def run_gpu(args, rank, world_size, local_rank):
         return
     peak, peak_kind = measured_peaks()
     stage_ms = {k[:-3]: v for k, v in acc.items()}
-    dominant = max(stage_ms, key=stage_ms.get)
+    # The top kernel of the step is the single-block contact solver (one launch
+    # per step whenever the manifold count fits a block); its stage events then
+    # time exactly that kernel.
+    block_solver = totals["manifolds"] / args.steps < 3000
+    dominant = "solver" if block_solver else max(stage_ms, key=stage_ms.get)
+    kernel = "k_solve_block" if block_solver else f"{dominant} stage"
     achieved = stage_b[dominant] / (stage_ms[dominant] / 1000.0) / 1e9 if stage_ms[dominant] > 0 else 0.0
     step_bytes = sum(stage_b.values())
+    traffic = profiled_traffic(kernel, stage_b[dominant] / args.steps)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": f"synthetic (scene generator, seed {SEED})",
         "config": workload_config(scene, "graph colour"),
         "roofline": {
-            "bound": "hbm", "stage": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "bound": "hbm", "kernel": kernel, "stage": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-            "traffic": None,
-            "algorithmic_bytes_per_step": stage_b[dominant] / args.steps,
+            "traffic": traffic["bytes"] if traffic else None,
+            "traffic_source": traffic["source"] if traffic else None,
+            "algorithmic_bytes_per_launch": stage_b[dominant] / args.steps,
             "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()},
             "whole_step": {"algorithmic_bytes_per_step": step_bytes / args.steps,
                            "achieved_gbs": step_bytes / (max_ms / 1000.0) / 1e9 / world_size,
@@ -332,7 +353,7 @@ def run_batched(args, local_rank, flush, peak):
 
     from phys_gb300 import engine
 
-    sizes = batch_world_sizes()
+    sizes = batch_world_sizes(args.batch_worlds)
     sc = batch_scenes(sizes)
     batch = engine.GpuBatch(sc, device=local_rank, iterations=ITERATIONS)
     stream = torch.cuda.ExternalStream(batch.stream(), device=torch.device("cuda", local_rank))
@@ -406,10 +427,10 @@ def run_batched(args, local_rank, flush, peak):
         gw.close()
     achieved = algo_bytes / (step_ms / 1000.0) / 1e9
     return {
-        "metric": "world-steps/s, 4096 batched worlds (forward)",
+        "metric": f"world-steps/s, {len(sizes)} batched worlds (forward)",
         "value": world_steps, "unit": "world-steps/s", "steps": steps, "ms_per_step": step_ms,
         "body_steps_per_s": sum(sizes) * steps / (ms / 1000.0),
-        "config": {"workload": "batched_4096", "worlds": len(sizes), "bodies": int(sum(sizes)),
+        "config": {"workload": f"batched_{len(sizes)}", "worlds": len(sizes), "bodies": int(sum(sizes)),
                    "bodies_per_world": f"log-uniform in [{BATCH_MIN}, {BATCH_MAX}] (seed {SEED}), "
                                        f"min {min(sizes)}, max {max(sizes)}",
                    "world": "mixed workload scaled to the world's body count, seed 42 + world",
@@ -417,8 +438,11 @@ def run_batched(args, local_rank, flush, peak):
                    "dt": DT, "steps_of_reference_run": 600,
                    "l2": "flushed before every timed step (512 MiB write)"},
         "workload_per_step": totals,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "algorithmic_bytes_per_step": algo_bytes},
+        "roofline": {"bound": "hbm", "kernel": "k_batch_step (one launch per size bucket)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": (profiled_traffic("k_batch_step", algo_bytes) or {}).get("bytes"),
+                     "traffic_source": (profiled_traffic("k_batch_step", algo_bytes) or {}).get("source"),
+                     "algorithmic_bytes_per_step": algo_bytes},
         "e2e": {"value": len(sizes) * e2e_steps / e2e_s, "unit": "world-steps/s",
                 "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 32 * n, "steps": e2e_steps},
         "gpu_launches": int(steps * len(buckets)),
@@ -453,14 +477,15 @@ def run_differentiable(args, local_rank):
 
     from phys_gb300 import engine, rollout, scenes
 
-    sc = [scenes.generate(scenes.BOXES_ON_PLANE, DIFF_BODIES, SEED + w) for w in range(DIFF_WORLDS)]
+    W = args.diff_worlds
+    sc = [scenes.generate(scenes.BOXES_ON_PLANE, DIFF_BODIES, SEED + w) for w in range(W)]
     roll = rollout.GpuRollout(sc, DIFF_STEPS, DIFF_DT, iterations=ITERATIONS, checkpoint_every=DIFF_CHECKPOINT,
                               device=local_rank)
     fn = rollout.rollout_function()
     dev = torch.device("cuda", local_rank)
     r = random.Random(SEED)
     targets = []
-    for _ in range(DIFF_WORLDS):
+    for _ in range(W):
         while True:
             t = [r.uniform(-5, 5) for _ in range(3)]
             if sum(c * c for c in t) <= 25.0:
@@ -469,7 +494,7 @@ def run_differentiable(args, local_rank):
     target = torch.tensor(targets, device=dev)
     x0n, q0n, v0n, w0n = roll.initial_state()
     dyn = torch.tensor(~roll.is_static.astype(bool), device=dev)
-    world_of = torch.tensor(np.repeat(np.arange(DIFF_WORLDS), roll.counts), device=dev)
+    world_of = torch.tensor(np.repeat(np.arange(W), roll.counts), device=dev)
 
     def one(host):
         """Host tensors in (pinned), loss + gradients out to the host."""
@@ -479,8 +504,8 @@ def run_differentiable(args, local_rank):
         x0, q0, v0, w0, m, f, rs = ins
         xT, qT, vT, wT = fn.apply(roll, x0, q0, v0, w0, m, f, rs)
         mw = m * dyn
-        msum = torch.zeros(DIFF_WORLDS, device=dev).index_add_(0, world_of, mw)
-        com = torch.zeros(DIFF_WORLDS, 3, device=dev).index_add_(0, world_of, mw[:, None] * xT) / msum[:, None]
+        msum = torch.zeros(W, device=dev).index_add_(0, world_of, mw)
+        com = torch.zeros(W, 3, device=dev).index_add_(0, world_of, mw[:, None] * xT) / msum[:, None]
         loss = ((com - target) ** 2).sum()
         loss.backward()
         grads = [v0.grad, m.grad, f.grad, rs.grad]
@@ -502,12 +527,12 @@ def run_differentiable(args, local_rank):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     device_s = (fwd_ms + bwd_ms) / 1000.0
-    ws = DIFF_WORLDS * DIFF_STEPS * reps
+    ws = W * DIFF_STEPS * reps
     h2d = sum(int(t.numel() * t.element_size()) for t in host)
     d2h = 4 * roll.n * 6 + 4
     # plain loop: forward steps of the single-world engine over a sample of the same worlds
     worlds = []
-    for w in range(0, DIFF_WORLDS, 32):
+    for w in range(0, W, 32):
         gw = engine.GpuWorld(device=local_rank, algo=engine.SAP, iterations=ITERATIONS, order=engine.ORDER_COLOR)
         gw.load_scene(sc[w])
         worlds.append(gw)
@@ -526,9 +551,9 @@ def run_differentiable(args, local_rank):
         gw.close()
     value = ws / device_s
     return {
-        "metric": "world-steps/s, 1024 worlds forward + adjoint", "value": value, "unit": "world-steps/s",
+        "metric": f"world-steps/s, {W} worlds forward + adjoint", "value": value, "unit": "world-steps/s",
         "rollouts": reps, "forward_ms_per_rollout": fwd_ms / reps, "adjoint_ms_per_rollout": bwd_ms / reps,
-        "config": {"workload": "differentiable_1024x64", "worlds": DIFF_WORLDS, "bodies_per_world": DIFF_BODIES,
+        "config": {"workload": f"differentiable_{W}x{DIFF_BODIES}", "worlds": W, "bodies_per_world": DIFF_BODIES,
                    "shapes": "boxes half-extents U[0.2,0.5] on a static 40x1x40 m plane, at rest",
                    "friction": "U[0.2,0.8]", "restitution": "U[0,0.3]", "steps": DIFF_STEPS, "dt": DIFF_DT,
                    "solver_iterations": ITERATIONS, "checkpoint_every": DIFF_CHECKPOINT,
@@ -554,7 +579,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-batched", action="store_true", help="skip the 4096-world batched measurement")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched-world and differentiable-rollout measurements")
+    ap.add_argument("--batch-worlds", type=int, default=BATCH_WORLDS, help="worlds of the batched measurement")
+    ap.add_argument("--diff-worlds", type=int, default=DIFF_WORLDS, help="worlds of the differentiable rollout")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
