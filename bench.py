@@ -183,6 +183,22 @@ def cpu_port_rate(scene, budget_s: float, max_steps: int, threads: int):
     return scene.count * steps / el, steps, el, load_s
 
 
+def max_over_ranks(value, world_size, device):
+    """The slowest rank's figure (every rank calls this; world_size 1 is local)."""
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    if world_size > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world_size, units_per_rank, max_seconds):
+    """Whole-job throughput of independent replicas: every rank processes
+    `units_per_rank`, the job ends with the slowest rank."""
+    return world_size * units_per_rank / max_seconds
+
+
 def run_reference(args, rank, world_size):
     if rank != 0:
         return
@@ -251,11 +267,8 @@ def run_gpu(args, rank, world_size, local_rank):
             totals["points"] += int(st["contact_points"])
         torch.cuda.synchronize()
     elapsed_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    t = torch.tensor([elapsed_ms], dtype=torch.float64, device=f"cuda:{local_rank}")
-    if world_size > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    max_ms = float(t.item())
-    value = world_size * scene.count * args.steps / (max_ms / 1000.0)
+    max_ms = max_over_ranks(elapsed_ms, world_size, f"cuda:{local_rank}")
+    value = replica_throughput(world_size, scene.count * args.steps, max_ms / 1000.0)
 
     # e2e: forces in from pinned host memory, step, poses out, every step
     forces = torch.zeros((scene.count, 3), dtype=torch.float32).pin_memory().numpy()
@@ -272,10 +285,8 @@ def run_gpu(args, rank, world_size, local_rank):
         w.step(DT)
         w.read_poses(poses_p, poses_q)
         e2e_s += time.perf_counter() - t0
-    te = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{local_rank}")
-    if world_size > 1:
-        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = world_size * scene.count * e2e_steps / float(te.item())
+    e2e_value = replica_throughput(world_size, scene.count * e2e_steps,
+                                   max_over_ranks(e2e_s, world_size, f"cuda:{local_rank}"))
 
     if rank != 0:
         return
