@@ -298,6 +298,137 @@ __global__ void k_grid_overflow_pairs(BroadInput in, const uint32_t *overflow, c
     }
 }
 
+// Per-body pair emission (grid): body a gathers its partners b > a from the
+// cells it covers (its own entry in each cell is found by a binary search on
+// (cell, index); the later entries of the cell are exactly the partners with a
+// higher index), keeps a pair in its lowest shared cell only, adds overflow
+// partners, sorts its few partners and writes them in body order (block scan +
+// decoupled look-back).  The result equals the reference's sorted, unique pair
+// list (broadphase.cpp:144-172) after the slot mapping and same-body filter
+// (physics_world.cpp:623-633), so no pair sort or finalize is needed.  The
+// comparison counter gets the per-cell comparisons (sum of n(n-1)/2 over cells)
+// and the overflow comparisons, as the reference counts them.
+constexpr uint32_t kBodyPartners = 32;
+constexpr int kBodyPairThreads = 256;
+
+__global__ void __launch_bounds__(kBodyPairThreads)
+k_grid_body_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const uint32_t *overflow,
+                  const uint32_t *d_entries, uint32_t ecap, const unsigned long long *ekeys, const uint32_t *evals,
+                  const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen, uint32_t *pairA,
+                  uint32_t *pairB, uint32_t cap, DevStats *st, unsigned long long *state, uint32_t *counter) {
+    __shared__ uint32_t s_tile, s_scan[9], s_prefix;
+    // Entries were not written this attempt (key width refused): nothing to scan.
+    if (st->err & (kErrSmallPath | kErrEntryCapacity)) return;
+    const uint32_t n = *in.d_n;
+    const uint32_t E = min(*d_entries, ecap);
+    const uint32_t F = st->overflowCount;
+    const uint32_t by = bitsFor((uint32_t)(st->cellHi[1] - st->cellLo[1]));
+    const uint32_t bz = bitsFor((uint32_t)(st->cellHi[2] - st->cellLo[2]));
+    if (blockIdx.x == 0 && threadIdx.x == 0 && F)
+        atomicAdd(&st->gridComparisons, (unsigned long long)F * (n - F) + (unsigned long long)F * (F - 1) / 2);
+    const uint32_t ntiles = max((n + kBodyPairThreads - 1) / kBodyPairThreads, 1u);
+    for (;;) {
+        const uint32_t tile = takeTile(counter, &s_tile);
+        if (tile >= ntiles) return;
+        const uint32_t a = tile * kBodyPairThreads + threadIdx.x;
+        uint32_t part[kBodyPartners];
+        uint32_t cnt = 0;
+        unsigned long long cmp = 0;
+        if (a < n) {
+            const float4 amn = in.mn[a], amx = in.mx[a];
+            auto add = [&](uint32_t b) {
+                if (cnt < kBodyPartners) part[cnt] = b;
+                ++cnt;
+            };
+            if (inGrid[a]) {
+                const int4 fa = firstCell[a];
+                const int cx = fa.w & 0xFF, cy = (fa.w >> 8) & 0xFF, cz = (fa.w >> 16) & 0xFF;
+                for (int x = 0; x < cx; ++x)
+                    for (int y = 0; y < cy; ++y)
+                        for (int z = 0; z < cz; ++z) {
+                            const unsigned long long key = packCell(fa.x + x, fa.y + y, fa.z + z, st, by, bz);
+                            uint32_t lo = 0, hi = E;
+                            while (lo < hi) {
+                                const uint32_t mid = (lo + hi) >> 1;
+                                const unsigned long long k2 = ekeys[mid];
+                                if (k2 < key || (k2 == key && evals[mid] < a)) lo = mid + 1;
+                                else hi = mid;
+                            }
+                            for (uint32_t f = lo + 1; f < E && ekeys[f] == key; ++f) {
+                                ++cmp;
+                                const uint32_t b = evals[f];
+                                if (!overlaps(amn, amx, in.mn[b], in.mx[b])) continue;
+                                const int4 fb = firstCell[b];
+                                if (packCell(max(fa.x, fb.x), max(fa.y, fb.y), max(fa.z, fb.z), st, by, bz) != key)
+                                    continue;
+                                add(b);
+                            }
+                        }
+                for (uint32_t k = 0; k < F; ++k) {
+                    const uint32_t o = overflow[k];
+                    if (o > a && overlaps(amn, amx, in.mn[o], in.mx[o])) add(o);
+                }
+            } else {
+                for (uint32_t b = a + 1; b < n; ++b)
+                    if (overlaps(amn, amx, in.mn[b], in.mx[b])) add(b);
+            }
+            if (cnt > kBodyPartners) atomicOr(&st->err, kErrBodyPairs);
+            const uint32_t m = min(cnt, kBodyPartners);
+            for (uint32_t i = 1; i < m; ++i) {
+                const uint32_t v = part[i];
+                uint32_t j = i;
+                while (j > 0 && part[j - 1] > v) {
+                    part[j] = part[j - 1];
+                    --j;
+                }
+                part[j] = v;
+            }
+        }
+        const uint32_t m = min(cnt, kBodyPartners);
+        const uint32_t sa = a < n ? (inSlot ? inSlot[a] : a) : 0u;
+        uint32_t kept = 0;
+        for (uint32_t j = 0; j < m; ++j) {
+            const uint32_t sb = inSlot ? inSlot[part[j]] : part[j];
+            if (cbody && cbody[sa] == cbody[sb] && cbgen[sa] == cbgen[sb]) continue;
+            ++kept;
+        }
+        if (cnt) {
+            atomicAdd(&st->rawPairs, cnt);  // no duplicates: raw = unique
+            atomicAdd(&st->uniquePairs, cnt);
+        }
+        if (cmp) atomicAdd(&st->gridComparisons, cmp);
+        uint32_t total;
+        const uint32_t local = blockExclusiveScan(kept, total, s_scan);
+        if (threadIdx.x == 0) s_prefix = lookbackExclusive(state, tile, total, &st->err);
+        __syncthreads();
+        uint32_t o = s_prefix + local;
+        for (uint32_t j = 0; j < m; ++j) {
+            const uint32_t sb = inSlot ? inSlot[part[j]] : part[j];
+            if (cbody && cbody[sa] == cbody[sb] && cbgen[sa] == cbgen[sb]) continue;
+            if (o < cap) {
+                pairA[o] = sa;
+                pairB[o] = sb;
+            }
+            ++o;
+        }
+        if (threadIdx.x == 0 && tile + 1 == ntiles) st->pairs = s_prefix + total;
+        __syncthreads();
+    }
+}
+
+void launchGridBodyPairs(const BroadInput &in, const BroadBuffers &bb, PairBuffers &pb, const uint32_t *inSlot,
+                         const uint32_t *cbody, const uint32_t *cbgen, DevStats *st, Scratch &ws, cudaStream_t s) {
+    uint32_t tiles = (in.maxN + kBodyPairThreads - 1) / kBodyPairThreads;
+    if (tiles == 0) tiles = 1;
+    PE_CHECK(cudaMemsetAsync(ws.scanState, 0, sizeof(unsigned long long) * (tiles + 1), s));
+    const uint32_t grid = tiles < 152u * 8u ? tiles : 152u * 8u;
+    k_grid_body_pairs<<<grid, kBodyPairThreads, 0, s>>>(in, bb.firstCell, bb.inGrid, bb.overflow,
+                                                         &st->gridEntryCount, bb.entryCap, bb.entryKeys,
+                                                         bb.entryVals, inSlot, cbody, cbgen, pb.a, pb.b, pb.cap, st,
+                                                         ws.scanState, (uint32_t *)(ws.scanState + tiles));
+    PE_LAUNCHED();
+}
+
 // ------------------------------------------------------------ finalize -----
 __global__ void k_pairs_flags(const uint32_t *d_raw, uint32_t cap, uint32_t bits, const unsigned long long *keys,
                               const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen, uint32_t *flags,
@@ -402,6 +533,7 @@ void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBu
     PE_LAUNCHED();
     launchRadixSort<unsigned long long>(bb.entryKeys, bb.entryKeysTmp, bb.entryVals, bb.entryValsTmp,
                                         &st->gridEntryCount, bb.entryCap, 0, (int)bb.keyBits, ws, err, s);
+    if (pb.bodyPath) return;  // pairs come from launchGridBodyPairs
     k_grid_cell_pairs<<<gridFor(bb.entryCap), 256, 0, s>>>(&st->gridEntryCount, bb.entryCap, bb.entryKeys,
                                                            bb.entryVals, bb.firstCell, in, pb.keys, pb.cap, pb.bits,
                                                            st);

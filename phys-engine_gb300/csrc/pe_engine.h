@@ -38,6 +38,7 @@ enum : uint32_t {
     kErrEntryCapacity = 16u,
     kErrEpa = 32u,
     kErrSmallPath = 64u,  // a single-block path saw more work than it holds: re-run on the full path
+    kErrBodyPairs = 128u, // a body had more grid partners than the per-body pair path holds
 };
 
 // Body flag bits (bflags) and collider flag layout (cflags).

@@ -35,6 +35,7 @@ struct PairBuffers {
     uint32_t cap;
     uint32_t bits;         // pair key = (first << bits) | second
     bool blockPath;        // single-block finalize (raw pairs <= kBlockMaxPairs)
+    bool bodyPath;         // grid: pairs emitted per body in final order (no sort / finalize)
     uint32_t *flags, *pos;
     uint32_t *a, *b;       // candidate pairs (collider slots), lexicographic
     uint32_t *counters;    // [4]
@@ -82,6 +83,10 @@ void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, Broad
                DevStats *st, Scratch &ws, cudaStream_t s);
 void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBuffers &pb, DevStats *st, Scratch &ws,
                 cudaStream_t s);
+// Grid pairs emitted body by body in lexicographic order, mapped to slots and
+// filtered (replaces the per-cell pairs and the finalize when pb.bodyPath).
+void launchGridBodyPairs(const BroadInput &in, const BroadBuffers &bb, PairBuffers &pb, const uint32_t *inSlot,
+                         const uint32_t *cbody, const uint32_t *cbgen, DevStats *st, Scratch &ws, cudaStream_t s);
 void launchPairsFinalize(const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen, PairBuffers &pb,
                          DevStats *st, Scratch &ws, cudaStream_t s);
 void launchNarrowphase(const WorldView &w, const PairBuffers &pb, const ManifoldView &mv, uint32_t mcap, DevStats *st,

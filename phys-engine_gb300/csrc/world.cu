@@ -315,7 +315,7 @@ void World::ensureCapacity() {
     pairA_.reserve(pairCap_);
     pairB_.reserve(pairCap_);
     pairCounters_.reserve(4);
-    pb_ = PairBuffers{pairKeys_.ptr, pairKeysTmp_.ptr, pairCap_, 32u, false, pairFlags_.ptr, pairPos_.ptr,
+    pb_ = PairBuffers{pairKeys_.ptr, pairKeysTmp_.ptr, pairCap_, 32u, false, false, pairFlags_.ptr, pairPos_.ptr,
                       pairA_.ptr, pairB_.ptr, pairCounters_.ptr};
 
     if (mcap_ < pairCap_) mcap_ = pairCap_;
@@ -473,7 +473,10 @@ void World::runPipeline(float dt) {
     BroadInput in{dense_ ? aabbMin_.ptr : inMin_.ptr, dense_ ? aabbMax_.ptr : inMax_.ptr, &st->inputCount, nc_};
     if (sap) launchSap(in, sapKeys_.ptr, sapVals_.ptr, bb_, pb_, st, ws_, s);
     else launchGrid(in, cellSize, bb_, pb_, st, ws_, s);
-    launchPairsFinalize(dense_ ? nullptr : inSlot_.ptr, cbody_.ptr, cbgen_.ptr, pb_, st, ws_, s);
+    if (!sap && pb_.bodyPath)
+        launchGridBodyPairs(in, bb_, pb_, dense_ ? nullptr : inSlot_.ptr, cbody_.ptr, cbgen_.ptr, st, ws_, s);
+    else
+        launchPairsFinalize(dense_ ? nullptr : inSlot_.ptr, cbody_.ptr, cbgen_.ptr, pb_, st, ws_, s);
     PE_CHECK(cudaEventRecordWithFlags(evStage_[2], s, cudaEventRecordExternal));
     ManifoldView mv = manifoldView();
     launchNarrowphase(w, pb_, mv, mcap_, st, ws_, s);
@@ -497,6 +500,12 @@ bool World::finishStep() {
                                                          "grid cell range exceeds 64 key bits"));
     }
     bool retry = false, grew = false;
+    if (h.err & kErrBodyPairs) {
+        // A body had more grid partners than the per-body path holds: this
+        // world uses the sort-based pair path from now on.
+        bodyPairs_ = false;
+        retry = true;
+    }
     if (h.err & kErrSmallPath) {
         // A single-block path or the sorted key width was too small: re-run with
         // the sizes this attempt measured.
@@ -568,7 +577,7 @@ bool World::GraphKey::operator==(const GraphKey &o) const {
            cacheCap == o.cacheCap && dt == o.dt && gx == o.gx && gy == o.gy && gz == o.gz &&
            algorithm == o.algorithm && iterations == o.iterations && orderMode == o.orderMode &&
            coopBlocks == o.coopBlocks && blockSolver == o.blockSolver && pairBits == o.pairBits &&
-           blockPairs == o.blockPairs && gridKeyBits == o.gridKeyBits && cellSize == o.cellSize && dense == o.dense &&
+           blockPairs == o.blockPairs && bodyPairs == o.bodyPairs && gridKeyBits == o.gridKeyBits && cellSize == o.cellSize && dense == o.dense &&
            localIdentity == o.localIdentity && forces == o.forces;
 }
 
@@ -591,6 +600,7 @@ World::GraphKey World::currentKey(float dt) const {
     k.blockSolver = blockSolver_;
     k.pairBits = pb_.bits;
     k.blockPairs = pb_.blockPath;
+    k.bodyPairs = pb_.bodyPath;
     k.gridKeyBits = bb_.keyBits;
     k.cellSize = cellSize;
     k.dense = dense_;
@@ -624,6 +634,7 @@ unsigned long long World::launchStep(float dt) {
     while (bits < 32 && (1ull << bits) < (unsigned long long)std::max<uint32_t>(nc_, 2)) ++bits;
     pb_.bits = bits;
     pb_.blockPath = lastRawEstimate_ + lastRawEstimate_ / 4 + 256 <= kBlockMaxPairs;
+    pb_.bodyPath = algorithm == 1 && bodyPairs_;
     bb_.keyBits = gridKeyBits_;
     if (graphsDisabled_) {
         const unsigned long long l0 = g_kernelLaunches;
@@ -878,6 +889,7 @@ void World::broadphaseOnly(const float *mins, const float *maxs, uint32_t n, int
         while (bits < 32 && (1ull << bits) < (unsigned long long)std::max<uint32_t>(n, 2)) ++bits;
         pb_.bits = bits;
         pb_.blockPath = false;
+        pb_.bodyPath = false;
         bb_.keyBits = 64;
         if (algo == 0) {
             launchSapKeys(in, sapKeys_.ptr, sapVals_.ptr, s);

@@ -234,7 +234,7 @@ class World {
         uint32_t nb, nc, pairCap, entryCap, mcap, cacheCap;
         float dt, gx, gy, gz;
         int algorithm, iterations, orderMode, coopBlocks;
-        bool blockSolver, blockPairs;
+        bool blockSolver, blockPairs, bodyPairs;
         uint32_t pairBits, gridKeyBits;
         double cellSize;
         bool dense, localIdentity, forces;
@@ -248,6 +248,7 @@ class World {
     std::string graphError_;
     int coopBlocks_ = 1;
     bool blockSolver_ = true;
+    bool bodyPairs_ = true;  // grid pairs per body (off after a body overflowed its partner list)
     GraphKey currentKey(float dt) const;
     void dropGraphs();
     unsigned long long launchStep(float dt);
