@@ -187,12 +187,24 @@ __global__ void k_cache_write(SolveArgs a, CacheView nc, uint32_t cacheCap) {
 }
 
 
+// Velocity staging slots of the single-block solver (bodies touched by contacts).
+constexpr uint32_t kStageSlots = 3072;
+constexpr size_t kBlockSolveSmem = kBlockMaxManifolds * (8 + 4 + 8) + kStageSlots * (32 + 4);
+
 __global__ void __launch_bounds__(kBlockSolveThreads)
 k_solve_block(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount, int serial) {
-    extern __shared__ unsigned long long s_sort[];  // kBlockMaxManifolds u64, then kBlockMaxManifolds u32
+    // kBlockMaxManifolds u64 sort keys, u32 flags, uint2 stage slots; then the
+    // staged velocities (2 float4 per slot) and the body of each slot.
+    extern __shared__ unsigned long long s_sort[];
     __shared__ BlockSolveShared sh;
+    unsigned char *base = reinterpret_cast<unsigned char *>(s_sort);
+    VelStage vs;
+    vs.slot = reinterpret_cast<uint2 *>(base + kBlockMaxManifolds * 12);
+    vs.v = reinterpret_cast<float4 *>(base + kBlockMaxManifolds * 20);
+    vs.slotBody = reinterpret_cast<uint32_t *>(base + kBlockMaxManifolds * 20 + kStageSlots * 32);
+    vs.cap = kStageSlots;
     solveBlock(a, nc, cacheCap, newCount, serial, kBlockMaxManifolds, s_sort,
-               reinterpret_cast<uint32_t *>(s_sort + kBlockMaxManifolds), sh);
+               reinterpret_cast<uint32_t *>(s_sort + kBlockMaxManifolds), sh, a.sb.bodySlot ? &vs : nullptr);
 }
 
 static int gridFor(uint32_t n, int threads = 256, int maxBlocks = 152 * 8) {
@@ -230,14 +242,14 @@ int maxCooperativeBlocks(int smCount) {
 
 void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &oldCache, const uint32_t *oldCacheCount,
                   const CacheView &newCache, uint32_t *newCacheCount, uint32_t cacheCap, SolverBuffers &sb,
-                  int iterations, int orderMode, int coopBlocks, bool blockPath, DevStats *st, Scratch &ws,
-                  cudaStream_t s) {
-    SolveArgs a{w, mv, sb, oldCache, oldCacheCount, st, sb.mcap, iterations};
+                  int iterations, int orderMode, int coopBlocks, bool blockPath, bool pairOrderCache, DevStats *st,
+                  Scratch &ws, cudaStream_t s) {
+    SolveArgs a{w, mv, sb, oldCache, oldCacheCount, st, sb.mcap, iterations, pairOrderCache};
     uint32_t *err = &st->err;
     const uint32_t mcap = sb.mcap;
     if (blockPath) {
         static bool configured = false;
-        const size_t smem = kBlockMaxManifolds * (sizeof(unsigned long long) + sizeof(uint32_t));
+        const size_t smem = kBlockSolveSmem;
         if (!configured) {
             PE_CHECK(cudaFuncSetAttribute(k_solve_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             configured = true;

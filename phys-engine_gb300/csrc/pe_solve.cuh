@@ -35,6 +35,34 @@ struct SolveArgs {
     DevStats *st;
     uint32_t mcap;
     int iterations;
+    // Collider i belongs to body i for every live collider: manifold (pair)
+    // order is then (body A, body B) order with one manifold per key, which is
+    // already the order of the rebuilt warm-start cache.
+    bool pairOrderCache;
+};
+
+// Where the velocity iterations read and write body velocities: the world's
+// arrays by body index, or shared-memory copies by staging slot.
+struct GlobalVel {
+    const SolveArgs &a;
+    __device__ __forceinline__ uint2 bodies(uint32_t k) const { return a.sb.pbody[k]; }
+    __device__ __forceinline__ V3 lin(uint32_t b) const { return f4xyz(ld4(&a.w.nxt.lin[b])); }
+    __device__ __forceinline__ V3 ang(uint32_t b) const { return f4xyz(ld4(&a.w.nxt.ang[b])); }
+    __device__ __forceinline__ void store(uint32_t b, const V3 &l, const V3 &w) const {
+        st4(&a.w.nxt.lin[b], make4(l, 0.0f));
+        st4(&a.w.nxt.ang[b], make4(w, 0.0f));
+    }
+};
+struct SharedVel {
+    float4 *v;          // slot s: lin at 2s, ang at 2s + 1
+    const uint2 *slot;  // per solve index k: slots of body A and body B
+    __device__ __forceinline__ uint2 bodies(uint32_t k) const { return slot[k]; }
+    __device__ __forceinline__ V3 lin(uint32_t s) const { return f4xyz(v[2 * s]); }
+    __device__ __forceinline__ V3 ang(uint32_t s) const { return f4xyz(v[2 * s + 1]); }
+    __device__ __forceinline__ void store(uint32_t s, const V3 &l, const V3 &w) const {
+        v[2 * s] = make4(l, 0.0f);
+        v[2 * s + 1] = make4(w, 0.0f);
+    }
 };
 
 struct BlockSolveShared {
@@ -43,7 +71,18 @@ struct BlockSolveShared {
     uint32_t scan[40];
     uint32_t colored;
     uint32_t colors;
+    uint32_t slots;
 };
+
+// Shared-memory copies of the velocities of the bodies the manifolds touch,
+// used by the single-block solver for the warm start and the iterations.
+struct VelStage {
+    float4 *v;            // [2 * cap]
+    uint2 *slot;          // [maxM] slots of body A / body B per solve index
+    uint32_t *slotBody;   // [cap] body of each slot
+    uint32_t cap;
+};
+constexpr uint32_t kSlotFree = 0xFFFFFFFFu, kSlotMarked = 0xFFFFFFFEu, kSlotClaimed = 0xFFFFFFFDu;
 
 // --------------------------------------------------------------- prepare ---
 // prepareBody (:275-287) + prepareContactPoints (:101-214) + the cache lookup
@@ -201,9 +240,9 @@ struct BodyVel {
     V3 lin, ang;
 };
 
-__device__ __forceinline__ void warmStartOne(const SolveArgs &a, uint32_t k) {
+template <class Vel> __device__ __forceinline__ void warmStartOne(const SolveArgs &a, uint32_t k, const Vel &vel) {
     const uint32_t mcap = a.mcap;
-    const uint2 bi = a.sb.pbody[k];
+    const uint2 bi = vel.bodies(k);
     const float4 pm = a.sb.pm[k];
     const bool sA = pm.y != 0.0f, sB = pm.w != 0.0f;
     const float4 nf = a.sb.pn[k];
@@ -216,8 +255,8 @@ __device__ __forceinline__ void warmStartOne(const SolveArgs &a, uint32_t k) {
         r0 = a.sb.pmInertia[3 * mcap + k], r1 = a.sb.pmInertia[4 * mcap + k], r2 = a.sb.pmInertia[5 * mcap + k];
         IB = M3{r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
     }
-    V3 linA = f4xyz(ld4(&a.w.nxt.lin[bi.x])), angA = f4xyz(ld4(&a.w.nxt.ang[bi.x]));
-    V3 linB = f4xyz(ld4(&a.w.nxt.lin[bi.y])), angB = f4xyz(ld4(&a.w.nxt.ang[bi.y]));
+    V3 linA = vel.lin(bi.x), angA = vel.ang(bi.x);
+    V3 linB = vel.lin(bi.y), angB = vel.ang(bi.y);
     bool any = false;
     for (uint32_t p = 0; p < npts; ++p) {
         const float4 imp = a.sb.pimp[(size_t)p * mcap + k];
@@ -239,28 +278,23 @@ __device__ __forceinline__ void warmStartOne(const SolveArgs &a, uint32_t k) {
         any = true;
     }
     if (!any) return;
-    if (!sA) {
-        st4(&a.w.nxt.lin[bi.x], make4(linA, 0.0f));
-        st4(&a.w.nxt.ang[bi.x], make4(angA, 0.0f));
-    }
-    if (!sB) {
-        st4(&a.w.nxt.lin[bi.y], make4(linB, 0.0f));
-        st4(&a.w.nxt.ang[bi.y], make4(angB, 0.0f));
-    }
+    if (!sA) vel.store(bi.x, linA, angA);
+    if (!sB) vel.store(bi.y, linB, angB);
 }
+__device__ __forceinline__ void warmStartOne(const SolveArgs &a, uint32_t k) { warmStartOne(a, k, GlobalVel{a}); }
 
 // solvePrepared (:520-603) for one manifold.
-__device__ __forceinline__ void solveOne(const SolveArgs &a, uint32_t k) {
+template <class Vel> __device__ __forceinline__ void solveOne(const SolveArgs &a, uint32_t k, const Vel &vel) {
     const uint32_t mcap = a.mcap;
-    const uint2 bi = a.sb.pbody[k];
+    const uint2 bi = vel.bodies(k);
     const float4 pm = a.sb.pm[k];
     const bool sA = pm.y != 0.0f, sB = pm.w != 0.0f;
     const float4 nf = a.sb.pn[k];
     const V3 n{nf.x, nf.y, nf.z};
     const float friction = nf.w;
     const uint32_t npts = a.sb.pcount[k];
-    V3 linA = f4xyz(ld4(&a.w.nxt.lin[bi.x])), angA = f4xyz(ld4(&a.w.nxt.ang[bi.x]));
-    V3 linB = f4xyz(ld4(&a.w.nxt.lin[bi.y])), angB = f4xyz(ld4(&a.w.nxt.ang[bi.y]));
+    V3 linA = vel.lin(bi.x), angA = vel.ang(bi.x);
+    V3 linB = vel.lin(bi.y), angB = vel.ang(bi.y);
     for (uint32_t p = 0; p < npts; ++p) {
         const float4 o0 = a.sb.pp[(size_t)(0 * 4 + p) * mcap + k];
         if (o0.w <= 0.0f) continue;  // inverseEffectiveMass <= 0
@@ -326,15 +360,10 @@ __device__ __forceinline__ void solveOne(const SolveArgs &a, uint32_t k) {
         }
         a.sb.pimp[(size_t)p * mcap + k] = imp;
     }
-    if (!sA) {
-        st4(&a.w.nxt.lin[bi.x], make4(linA, 0.0f));
-        st4(&a.w.nxt.ang[bi.x], make4(angA, 0.0f));
-    }
-    if (!sB) {
-        st4(&a.w.nxt.lin[bi.y], make4(linB, 0.0f));
-        st4(&a.w.nxt.ang[bi.y], make4(angB, 0.0f));
-    }
+    if (!sA) vel.store(bi.x, linA, angA);
+    if (!sB) vel.store(bi.y, linB, angB);
 }
+__device__ __forceinline__ void solveOne(const SolveArgs &a, uint32_t k) { solveOne(a, k, GlobalVel{a}); }
 
 // Cooperative sweep: warm start, then `iterations` sweeps, each colour by colour
 // with a grid barrier between colours.
@@ -367,7 +396,8 @@ __device__ __forceinline__ void cacheWriteManifold(const SolveArgs &a, const Cac
 // s_sort holds maxM u64 and s_dyn maxM u32 (shared memory); sh the small
 // shared arrays.  All threads of the block call it.
 __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint32_t cacheCap, uint32_t *newCount, int serial,
-                           uint32_t maxM, unsigned long long *s_sort, uint32_t *s_dyn, BlockSolveShared &sh) {
+                           uint32_t maxM, unsigned long long *s_sort, uint32_t *s_dyn, BlockSolveShared &sh,
+                           const VelStage *vs = nullptr) {
     uint32_t *s_start = sh.start, *s_count = sh.count, *s_scan = sh.scan;
     uint32_t &s_colored = sh.colored, &s_colors = sh.colors;
     const uint32_t M = min(a.st->manifolds, a.mcap);
@@ -468,18 +498,90 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
         // colours to global (pair order) and the (colour, index) order
         for (uint32_t m = tid; m < M; m += nt) sb.color[m] = s_color[m];
         __syncthreads();
-        const uint32_t n2 = nextPow2(M > 0 ? M : 1);
-        uint32_t *keys = reinterpret_cast<uint32_t *>(s_sort);
-        for (uint32_t i = tid; i < n2; i += nt) keys[i] = i < M ? ((sb.color[i] << 12) | i) : 0xFFFFFFFFu;
-        __syncthreads();
-        blockBitonicSort<uint32_t>(keys, n2);
-        for (uint32_t k = tid; k < M; k += nt) sb.order[k] = keys[k] & 0xFFFu;
+        const uint32_t nw = nt >> 5, Cc = s_colors;
+        if (nw * Cc <= 2 * maxM) {
+            // Stable placement: a manifold goes to the start of its colour plus
+            // the number of earlier manifolds of that colour (warp ranks from
+            // match_any, per-warp colour counts scanned across warps).
+            uint32_t *wc = reinterpret_cast<uint32_t *>(s_sort);  // [warps][colours]
+            const uint32_t lane = tid & 31, warp = tid >> 5;
+            for (uint32_t c = tid; c < Cc; c += nt) s_count[c] = 0;
+            for (uint32_t m0 = 0; m0 < M; m0 += nt) {
+                for (uint32_t i = tid; i < nw * Cc; i += nt) wc[i] = 0;
+                __syncthreads();
+                const uint32_t m = m0 + tid;
+                const uint32_t c = m < M ? __ldcg(&sb.color[m]) : 0xFFFFFFFFu;
+                const uint32_t peers = __match_any_sync(0xffffffffu, c);
+                const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+                if (m < M && rank == 0) wc[warp * Cc + c] = __popc(peers);
+                __syncthreads();
+                for (uint32_t cc = tid; cc < Cc; cc += nt) {
+                    uint32_t run = s_count[cc];
+                    for (uint32_t w2 = 0; w2 < nw; ++w2) {
+                        const uint32_t t = wc[w2 * Cc + cc];
+                        wc[w2 * Cc + cc] = run;
+                        run += t;
+                    }
+                    s_count[cc] = run;
+                }
+                __syncthreads();
+                if (m < M) sb.order[s_start[c] + wc[warp * Cc + c] + rank] = m;
+                __syncthreads();
+            }
+        } else {
+            const uint32_t n2 = nextPow2(M > 0 ? M : 1);
+            uint32_t *keys = reinterpret_cast<uint32_t *>(s_sort);
+            for (uint32_t i = tid; i < n2; i += nt) keys[i] = i < M ? ((sb.color[i] << 12) | i) : 0xFFFFFFFFu;
+            __syncthreads();
+            blockBitonicSort<uint32_t>(keys, n2);
+            for (uint32_t k = tid; k < M; k += nt) sb.order[k] = keys[k] & 0xFFFu;
+        }
         C = s_colors;
         __syncthreads();
     }
     // --- prepare + warm-start matching ---
     prepareRange(a, tid, nt, M);
     __syncthreads();
+    // --- stage the touched bodies' velocities in shared memory ---
+    const bool stage = vs != nullptr && !serial && M > 0;
+    bool staged = false;
+    if (stage) {
+        for (uint32_t k = tid; k < M; k += nt) {
+            if (!sb.pcount[k]) continue;  // invalid manifold: touches no body
+            const uint2 bi = sb.pbody[k];
+            sb.bodySlot[bi.x] = kSlotMarked;
+            sb.bodySlot[bi.y] = kSlotMarked;
+        }
+        if (tid == 0) sh.slots = 0;
+        __syncthreads();
+        for (uint32_t k = tid; k < M; k += nt) {
+            if (!sb.pcount[k]) continue;
+            const uint2 bi = sb.pbody[k];
+            const uint32_t b2[2] = {bi.x, bi.y};
+            for (int j = 0; j < 2; ++j)
+                if (atomicCAS(&sb.bodySlot[b2[j]], kSlotMarked, kSlotClaimed) == kSlotMarked) {
+                    const uint32_t sl = atomicAdd(&sh.slots, 1u);
+                    if (sl < vs->cap) vs->slotBody[sl] = b2[j];
+                    atomicExch(&sb.bodySlot[b2[j]], sl);
+                }
+        }
+        __syncthreads();
+        const uint32_t nslots = sh.slots;
+        staged = nslots <= vs->cap;
+        if (staged) {
+            for (uint32_t k = tid; k < M; k += nt) {
+                const uint2 bi = sb.pbody[k];
+                vs->slot[k] = sb.pcount[k] ? make_uint2(__ldcg(&sb.bodySlot[bi.x]), __ldcg(&sb.bodySlot[bi.y]))
+                                           : make_uint2(0u, 0u);
+            }
+            for (uint32_t sl = tid; sl < nslots; sl += nt) {
+                const uint32_t b = vs->slotBody[sl];
+                vs->v[2 * sl] = ld4(&w.nxt.lin[b]);
+                vs->v[2 * sl + 1] = ld4(&w.nxt.ang[b]);
+            }
+        }
+        __syncthreads();
+    }
     // --- warm start and velocity iterations ---
     if (serial) {
         if (tid == 0) {
@@ -487,6 +589,17 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
             for (int it = 0; it < a.iterations; ++it)
                 for (uint32_t k = 0; k < M; ++k) solveOne(a, k);
         }
+    } else if (staged) {
+        const SharedVel sv{vs->v, vs->slot};
+        for (uint32_t c = 0; c < C; ++c) {
+            for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) warmStartOne(a, k, sv);
+            __syncthreads();
+        }
+        for (int it = 0; it < a.iterations; ++it)
+            for (uint32_t c = 0; c < C; ++c) {
+                for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) solveOne(a, k, sv);
+                __syncthreads();
+            }
     } else {
         for (uint32_t c = 0; c < C; ++c) {
             for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) warmStartOne(a, k);
@@ -499,6 +612,23 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
             }
     }
     __syncthreads();
+    if (stage) {
+        if (staged) {
+            const uint32_t nslots = sh.slots;
+            for (uint32_t sl = tid; sl < nslots; sl += nt) {
+                const uint32_t b = vs->slotBody[sl];
+                st4(&w.nxt.lin[b], vs->v[2 * sl]);
+                st4(&w.nxt.ang[b], vs->v[2 * sl + 1]);
+            }
+        }
+        __syncthreads();
+        for (uint32_t k = tid; k < M; k += nt) {
+            if (!sb.pcount[k]) continue;
+            const uint2 bi = sb.pbody[k];
+            sb.bodySlot[bi.x] = kSlotFree;
+            sb.bodySlot[bi.y] = kSlotFree;
+        }
+    }
     // --- impulses back to the manifolds ---
     for (uint32_t k = tid; k < M; k += nt) {
         const uint32_t m = sb.order[k];
@@ -509,7 +639,26 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
         }
     }
     __syncthreads();
-    // --- cache rebuild: stable sort by (body A, body B) over solve order ---
+    // --- cache rebuild ---
+    if (a.pairOrderCache) {
+        // Manifold order is (body A, body B) order with one manifold per key:
+        // the cache is the manifolds' points in manifold order.
+        for (uint32_t i = tid; i < M; i += nt) {
+            const uint32_t ia = a.mv.bodyA[i], ib = a.mv.bodyB[i];
+            const bool valid = ia < w.nb && ib < w.nb && (w.bflags[ia] & kBodyAlive) && (w.bflags[ib] & kBodyAlive) &&
+                               w.bgen[ia] == a.mv.genA[i] && w.bgen[ib] == a.mv.genB[i];
+            s_dyn[i] = valid ? a.mv.pointCount[i] : 0u;
+        }
+        __syncthreads();
+        const uint32_t total = blockExclusiveScanArray(s_dyn, M, s_scan);
+        for (uint32_t i = tid; i < M; i += nt) {
+            const uint32_t cnt = (i + 1 < M ? s_dyn[i + 1] : total) - s_dyn[i];
+            cacheWriteManifold(a, nc, cacheCap, i, s_dyn[i], cnt);
+        }
+        if (tid == 0) *newCount = total;
+        return;
+    }
+    // stable sort by (body A, body B) over solve order
     const uint32_t n2 = nextPow2(M > 0 ? M : 1);
     for (uint32_t i = tid; i < n2; i += nt) {
         unsigned long long key = ~0ull;

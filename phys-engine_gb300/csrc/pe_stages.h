@@ -63,6 +63,7 @@ struct SolverBuffers {
     unsigned long long *cacheKeys, *cacheKeysTmp;
     uint32_t *cacheVals, *cacheValsTmp;
     uint32_t *cacheCounts, *cacheOff;
+    uint32_t *bodySlot;             // [nb] velocity staging slot; 0xFFFFFFFF between steps (single-block path)
     uint32_t *bar;                  // grid barrier [2]
     uint32_t *counters;             // [4]
 };
@@ -93,8 +94,8 @@ void launchNarrowphase(const WorldView &w, const PairBuffers &pb, const Manifold
                        Scratch &ws, cudaStream_t s);
 void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &oldCache, const uint32_t *oldCacheCount,
                   const CacheView &newCache, uint32_t *newCacheCount, uint32_t cacheCap, SolverBuffers &sb,
-                  int iterations, int orderMode, int coopBlocks, bool blockPath, DevStats *st, Scratch &ws,
-                  cudaStream_t s);
+                  int iterations, int orderMode, int coopBlocks, bool blockPath, bool pairOrderCache, DevStats *st,
+                  Scratch &ws, cudaStream_t s);
 // Largest manifold count the single-block solver handles, and the largest
 // body index it can key (bodies < 2^20).
 constexpr uint32_t kBlockMaxManifolds = 4096;

@@ -217,6 +217,7 @@ void World::push() {
     std::vector<float4> cs(nc_), lp(nc_), lr(nc_);
     dense_ = true;
     localIdentity_ = true;
+    bool identity = true;
     for (uint32_t i = 0; i < nc_; ++i) {
         const HostCollider &c = colliders[i];
         cb[i] = c.body;
@@ -233,7 +234,9 @@ void World::push() {
             localIdentity_ = false;
         bool valid = c.alive && c.body < nb_ && bodies[c.body].alive && bodies[c.body].generation == c.bodyGeneration;
         if (!valid) dense_ = false;
+        if (!valid || c.body != i) identity = false;
     }
+    identityColliders_ = identity && nc_ == nb_;
     upload(cbody_, cb, stream_);
     upload(cbgen_, cg, stream_);
     upload(cflags_, cf, stream_);
@@ -356,6 +359,11 @@ void World::ensureCapacity() {
     sCacheOff_.reserve(m);
     sBar_.reserve(2);
     sCounters_.reserve(4);
+    if (sBodySlot_.count < nb || !sBodySlot_.ptr) {
+        // staging slots are "free" (all ones) between steps
+        sBodySlot_.reserve(nb);
+        PE_CHECK(cudaMemset(sBodySlot_.ptr, 0xFF, sBodySlot_.count * sizeof(uint32_t)));
+    }
     sb_ = SolverBuffers{m,
                         sBest_.ptr,
                         sUsed_.ptr,
@@ -380,6 +388,7 @@ void World::ensureCapacity() {
                         sCacheValsTmp_.ptr,
                         sCacheCounts_.ptr,
                         sCacheOff_.ptr,
+                        sBodySlot_.ptr,
                         sBar_.ptr,
                         sCounters_.ptr};
 
@@ -482,7 +491,7 @@ void World::runPipeline(float dt) {
     launchNarrowphase(w, pb_, mv, mcap_, st, ws_, s);
     PE_CHECK(cudaEventRecordWithFlags(evStage_[3], s, cudaEventRecordExternal));
     launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], cacheView(1 - cache_), &cCount_.ptr[1 - cache_],
-                 cacheCap_, sb_, iterations, orderMode, coopBlocks_, blockSolver_, st, ws_, s);
+                 cacheCap_, sb_, iterations, orderMode, coopBlocks_, blockSolver_, identityColliders_, st, ws_, s);
     PE_CHECK(cudaEventRecordWithFlags(evStage_[4], s, cudaEventRecordExternal));
     launchIntegratePose(w, s);
     PE_CHECK(cudaEventRecordWithFlags(evStage_[5], s, cudaEventRecordExternal));
@@ -578,7 +587,7 @@ bool World::GraphKey::operator==(const GraphKey &o) const {
            algorithm == o.algorithm && iterations == o.iterations && orderMode == o.orderMode &&
            coopBlocks == o.coopBlocks && blockSolver == o.blockSolver && pairBits == o.pairBits &&
            blockPairs == o.blockPairs && bodyPairs == o.bodyPairs && gridKeyBits == o.gridKeyBits && cellSize == o.cellSize && dense == o.dense &&
-           localIdentity == o.localIdentity && forces == o.forces;
+           localIdentity == o.localIdentity && forces == o.forces && identityColliders == o.identityColliders;
 }
 
 World::GraphKey World::currentKey(float dt) const {
@@ -606,6 +615,7 @@ World::GraphKey World::currentKey(float dt) const {
     k.dense = dense_;
     k.localIdentity = localIdentity_;
     k.forces = forces_;
+    k.identityColliders = identityColliders_;
     return k;
 }
 
@@ -999,7 +1009,7 @@ void World::solveOnly(std::vector<float> &recs, uint32_t count, float dt, int it
     blocks = std::min<uint32_t>(blocks, (uint32_t)maxCooperativeBlocks(smCount_));
     const bool block = count <= kBlockMaxManifolds && nb_ <= kBlockMaxBodies;
     launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], cacheView(1 - cache_), &cCount_.ptr[1 - cache_],
-                 cacheCap_, sb_, iters, mode, (int)blocks, block, st, ws_, s);
+                 cacheCap_, sb_, iters, mode, (int)blocks, block, false, st, ws_, s);
     PE_CHECK(cudaMemcpyAsync(hostStats_, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
     PE_CHECK(cudaStreamSynchronize(s));
     if (hostStats_->err & (kErrTimeout | kErrColors)) throw std::runtime_error("solve failed on the device");

@@ -210,6 +210,7 @@ class World {
     // solver
     SolverBuffers sb_{};
     DeviceArray<unsigned long long> sBest_, sUsed_, sEpoch_, sCacheKeys_, sCacheKeysTmp_;
+    DeviceArray<uint32_t> sBodySlot_;
     DeviceArray<uint32_t> sColor_, sDyn_, sColorCount_, sOrderKeys_, sOrderKeysTmp_, sOrder_, sOrderTmp_, sPcount_,
         sCacheVals_, sCacheValsTmp_, sCacheCounts_, sCacheOff_, sBar_, sCounters_;
     DeviceArray<float4> sPm_, sPmI_, sPp_, sPimp_, sPn_;
@@ -237,7 +238,7 @@ class World {
         bool blockSolver, blockPairs, bodyPairs;
         uint32_t pairBits, gridKeyBits;
         double cellSize;
-        bool dense, localIdentity, forces;
+        bool dense, localIdentity, forces, identityColliders;
         bool operator==(const GraphKey &o) const;
     };
     cudaGraphExec_t graph_[2] = {nullptr, nullptr};
@@ -248,7 +249,8 @@ class World {
     std::string graphError_;
     int coopBlocks_ = 1;
     bool blockSolver_ = true;
-    bool bodyPairs_ = true;  // grid pairs per body (off after a body overflowed its partner list)
+    bool bodyPairs_ = true;
+    bool identityColliders_ = false;  // collider i is body i for every slot (unique body pair per manifold)  // grid pairs per body (off after a body overflowed its partner list)
     GraphKey currentKey(float dt) const;
     void dropGraphs();
     unsigned long long launchStep(float dt);
