@@ -8,11 +8,16 @@
 //                      (src/dynamics/rigid_body.cpp:103-125, physics_world.cpp:759-767).
 #include "pe_bodies.cuh"
 #include "pe_kernels.cuh"
+#include "pe_stages.h"
 
 namespace pe {
 
-__global__ void k_integrate_aabb(WorldView w, uint32_t *sapKeys, uint32_t *sapVals) {
+// st (nullable): the step's counters are initialised here as well, which saves
+// a launch at the head of the step.
+__global__ void k_integrate_aabb(WorldView w, uint32_t *sapKeys, uint32_t *sapVals, DevStats *st,
+                                 uint32_t inputCount) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (st && i == 0) initStepStats(st, inputCount);
     if (i < w.nb) {
         const uint32_t f = w.bflags[i];
         V3 lin = f4xyz(w.cur.lin[i]);
@@ -79,10 +84,14 @@ __global__ void k_integrate_pose(WorldView w) {
     w.nxt.rot[i] = q4;
 }
 
-void launchIntegrateAabb(const WorldView &w, uint32_t *sapKeys, uint32_t *sapVals, cudaStream_t s) {
+void launchIntegrateAabb(const WorldView &w, uint32_t *sapKeys, uint32_t *sapVals, DevStats *st,
+                         uint32_t inputCount, cudaStream_t s) {
     uint32_t n = w.nb > w.nc ? w.nb : w.nc;
-    if (!n) return;
-    k_integrate_aabb<<<(n + 255) / 256, 256, 0, s>>>(w, sapKeys, sapVals);
+    if (!n) {
+        if (st) launchStepInit(st, inputCount, s);
+        return;
+    }
+    k_integrate_aabb<<<(n + 255) / 256, 256, 0, s>>>(w, sapKeys, sapVals, st, inputCount);
     PE_LAUNCHED();
 }
 

@@ -29,14 +29,7 @@ __device__ __forceinline__ void emitPair(uint32_t a, uint32_t b, unsigned long l
 }
 
 __global__ void k_step_init(DevStats *st, uint32_t inputCount) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        memset(st, 0, sizeof(DevStats));
-        st->inputCount = inputCount;
-        for (int a = 0; a < 3; ++a) {
-            st->cellLo[a] = 0x7FFFFFFF;
-            st->cellHi[a] = (int32_t)0x80000000;
-        }
-    }
+    if (threadIdx.x == 0 && blockIdx.x == 0) initStepStats(st, inputCount);
 }
 
 // ---------------------------------------------------------------- SAP ------
@@ -156,10 +149,13 @@ __device__ __forceinline__ double cellFloor(float x, double cell, double inv) {
 }
 
 // gridRange (broadphase.cpp:62-88) per input box.
+// fixedCell > 0: the cell size is given (no k_grid_cellsize launch); this
+// kernel records it.
 __global__ void k_grid_range(BroadInput in, DevStats *st, int4 *firstCell, uint32_t *cellCount, uint8_t *inGrid,
-                             uint32_t *overflow) {
+                             uint32_t *overflow, double fixedCell) {
     const uint32_t n = *in.d_n;
-    const double cell = st->cellSize;
+    if (fixedCell > 0.0 && blockIdx.x == 0 && threadIdx.x == 0) st->cellSize = fixedCell;
+    const double cell = fixedCell > 0.0 ? fixedCell : st->cellSize;
     const double inv = 1.0 / cell;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 mn = in.mn[i], mx = in.mx[i];
@@ -523,9 +519,12 @@ void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBu
         launchRadixSort<unsigned long long>(bb.widthKeys, bb.widthTmp, nullptr, nullptr, in.d_n, in.maxN, 0, 64, ws,
                                             err, s);
     }
-    k_grid_cellsize<<<1, 1, 0, s>>>(bb.widthKeys, &bb.counters[0], fixedCell, st);
-    PE_LAUNCHED();
-    k_grid_range<<<gridFor(in.maxN), 256, 0, s>>>(in, st, bb.firstCell, bb.cellCount, bb.inGrid, bb.overflow);
+    if (fixedCell <= 0.0) {
+        k_grid_cellsize<<<1, 1, 0, s>>>(bb.widthKeys, &bb.counters[0], fixedCell, st);
+        PE_LAUNCHED();
+    }
+    k_grid_range<<<gridFor(in.maxN), 256, 0, s>>>(in, st, bb.firstCell, bb.cellCount, bb.inGrid, bb.overflow,
+                                                  fixedCell);
     PE_LAUNCHED();
     launchScanExclusive(bb.cellCount, bb.entryOff, in.d_n, in.maxN, &st->gridEntryCount, ws, err, s);
     k_grid_entries<<<gridFor(in.maxN), 256, 0, s>>>(in, bb.firstCell, bb.inGrid, bb.entryOff, bb.entryKeys,

@@ -33,4 +33,14 @@ __device__ __forceinline__ void aggregatedCount(unsigned long long *counters, ui
     if ((int)(threadIdx.x & 31) == leader) atomicAdd(&counters[key], (unsigned long long)__popc(peers));
 }
 
+// Counters of a new step: all zero, the bound count, empty grid bounds.
+__device__ __forceinline__ void initStepStats(DevStats *st, uint32_t inputCount) {
+    memset(st, 0, sizeof(DevStats));
+    st->inputCount = inputCount;
+    for (int a = 0; a < 3; ++a) {
+        st->cellLo[a] = 0x7FFFFFFF;
+        st->cellHi[a] = (int32_t)0x80000000;
+    }
+}
+
 } // namespace pe

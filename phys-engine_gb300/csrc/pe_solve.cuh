@@ -296,14 +296,20 @@ template <class Vel> __device__ __forceinline__ void solveOne(const SolveArgs &a
     V3 linA = vel.lin(bi.x), angA = vel.ang(bi.x);
     V3 linB = vel.lin(bi.y), angB = vel.ang(bi.y);
     for (uint32_t p = 0; p < npts; ++p) {
+        // All of the point's constants are requested at once (one memory round
+        // trip); points with no effective mass are skipped after the loads.
         const float4 o0 = a.sb.pp[(size_t)(0 * 4 + p) * mcap + k];
-        if (o0.w <= 0.0f) continue;  // inverseEffectiveMass <= 0
         const float4 o1 = a.sb.pp[(size_t)(1 * 4 + p) * mcap + k];
         const float4 o2 = a.sb.pp[(size_t)(2 * 4 + p) * mcap + k];
         const float4 o3 = a.sb.pp[(size_t)(3 * 4 + p) * mcap + k];
         const float4 o4 = a.sb.pp[(size_t)(4 * 4 + p) * mcap + k];
         const float4 o5 = a.sb.pp[(size_t)(5 * 4 + p) * mcap + k];
+        const float4 o6 = a.sb.pp[(size_t)(6 * 4 + p) * mcap + k];
+        const float4 o7 = a.sb.pp[(size_t)(7 * 4 + p) * mcap + k];
+        const float4 o8 = a.sb.pp[(size_t)(8 * 4 + p) * mcap + k];
+        const float4 o9 = a.sb.pp[(size_t)(9 * 4 + p) * mcap + k];
         float4 imp = a.sb.pimp[(size_t)p * mcap + k];
+        if (o0.w <= 0.0f) continue;  // inverseEffectiveMass <= 0
         const V3 offA = f4xyz(o0), offB = f4xyz(o1), t1 = f4xyz(o2), t2 = f4xyz(o3);
         const float iem = o0.w, bias = o1.w, rv = o2.w, itm00 = o3.w, itm01 = o4.w, itm11 = o5.w;
         const V3 vA = linA + cross(angA, offA);
@@ -327,10 +333,6 @@ template <class Vel> __device__ __forceinline__ void solveOne(const SolveArgs &a
             a.sb.pimp[(size_t)p * mcap + k] = imp;
             continue;
         }
-        const float4 o6 = a.sb.pp[(size_t)(6 * 4 + p) * mcap + k];
-        const float4 o7 = a.sb.pp[(size_t)(7 * 4 + p) * mcap + k];
-        const float4 o8 = a.sb.pp[(size_t)(8 * 4 + p) * mcap + k];
-        const float4 o9 = a.sb.pp[(size_t)(9 * 4 + p) * mcap + k];
         const float ntr1 = o6.w, ntr2 = o7.w;
         float limit = smax(friction, 0.0f) * imp.x;
         float tv1 = dot(rel, t1) + ntr1 * applied;

@@ -75,7 +75,9 @@ constexpr int kPreparedVec4 = 10;
 void launchStepInit(DevStats *st, uint32_t inputCount, cudaStream_t s);
 void launchSetManifoldCount(DevStats *st, uint32_t count, cudaStream_t s);
 void launchSapKeys(const BroadInput &in, uint32_t *keys, uint32_t *vals, cudaStream_t s);
-void launchIntegrateAabb(const WorldView &w, uint32_t *sapKeys, uint32_t *sapVals, cudaStream_t s);
+// st != nullptr: also initialises the step's counters (in place of launchStepInit).
+void launchIntegrateAabb(const WorldView &w, uint32_t *sapKeys, uint32_t *sapVals, DevStats *st, uint32_t inputCount,
+                         cudaStream_t s);
 void launchCollect(const WorldView &w, uint32_t *flags, uint32_t *pos, float4 *inMin, float4 *inMax, uint32_t *inSlot,
                    uint32_t *sapKeys, uint32_t *sapVals, uint32_t *d_count, Scratch &ws, uint32_t *d_err,
                    cudaStream_t s);

@@ -469,12 +469,11 @@ void World::runPipeline(float dt) {
     WorldView w = view(dt);
     DevStats *st = stats_.ptr;
     PE_CHECK(cudaEventRecordWithFlags(evStage_[0], s, cudaEventRecordExternal));
-    launchStepInit(st, dense_ ? nc_ : 0u, s);
     const bool sap = algorithm == 0;
     if (dense_) {
-        launchIntegrateAabb(w, sap ? sapKeys_.ptr : nullptr, sapVals_.ptr, s);
+        launchIntegrateAabb(w, sap ? sapKeys_.ptr : nullptr, sapVals_.ptr, st, nc_, s);
     } else {
-        launchIntegrateAabb(w, nullptr, nullptr, s);
+        launchIntegrateAabb(w, nullptr, nullptr, st, 0u, s);
         launchCollect(w, collectFlags_.ptr, collectPos_.ptr, inMin_.ptr, inMax_.ptr, inSlot_.ptr,
                       sap ? sapKeys_.ptr : nullptr, sapVals_.ptr, &st->inputCount, ws_, &st->err, s);
     }
