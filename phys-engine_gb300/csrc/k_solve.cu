@@ -204,7 +204,7 @@ k_solve_block(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount, 
     vs.slotBody = reinterpret_cast<uint32_t *>(base + kBlockMaxManifolds * 20 + kStageSlots * 32);
     vs.cap = kStageSlots;
     solveBlock(a, nc, cacheCap, newCount, serial, kBlockMaxManifolds, s_sort,
-               reinterpret_cast<uint32_t *>(s_sort + kBlockMaxManifolds), sh, a.sb.bodySlot ? &vs : nullptr);
+               reinterpret_cast<uint32_t *>(s_sort + kBlockMaxManifolds), sh, &vs);
 }
 
 static int gridFor(uint32_t n, int threads = 256, int maxBlocks = 152 * 8) {

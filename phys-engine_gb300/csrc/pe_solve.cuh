@@ -82,12 +82,16 @@ struct VelStage {
     uint32_t *slotBody;   // [cap] body of each slot
     uint32_t cap;
 };
-constexpr uint32_t kSlotFree = 0xFFFFFFFFu, kSlotMarked = 0xFFFFFFFEu, kSlotClaimed = 0xFFFFFFFDu;
+constexpr uint32_t kSlotFree = 0xFFFFFFFFu;
 
 // --------------------------------------------------------------- prepare ---
 // prepareBody (:275-287) + prepareContactPoints (:101-214) + the cache lookup
 // of warmStartPrepared (:448-490).  Data are written in solve order k.
-__device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t stride, uint32_t M) {
+// cacheKeys: the old cache's keys (a shared-memory copy in the single-block
+// path; the global array otherwise).
+__device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t stride, uint32_t M,
+                                    const unsigned long long *cacheKeys = nullptr) {
+    if (!cacheKeys) cacheKeys = a.oldCache.key;
     const uint32_t mcap = a.mcap;
     const WorldView &w = a.w;
     const float inverseDt = 1.0f / smax(w.dt, 1e-6f);
@@ -139,11 +143,11 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
         uint32_t lo = 0, hi = cacheN;
         while (lo < hi) {
             uint32_t mid = (lo + hi) >> 1;
-            if (a.oldCache.key[mid] < key) lo = mid + 1;
+            if (cacheKeys[mid] < key) lo = mid + 1;
             else hi = mid;
         }
         uint32_t rb = lo, re = lo;
-        while (re < cacheN && a.oldCache.key[re] == key) ++re;
+        while (re < cacheN && cacheKeys[re] == key) ++re;
         if (rb < re && a.oldCache.gens[rb] != gens) re = rb;
 
         const float matchSq = 0.05f * 0.05f;
@@ -388,6 +392,14 @@ __device__ __forceinline__ void cacheWriteManifold(const SolveArgs &a, const Cac
 }
 
 
+// The manifold's body handles are live (sequential_impulse_solver.cpp:317-320).
+__device__ __forceinline__ bool manifoldBodiesValid(const SolveArgs &a, uint32_t m) {
+    const uint32_t ia = a.mv.bodyA[m], ib = a.mv.bodyB[m];
+    const WorldView &w = a.w;
+    return ia < w.nb && ib < w.nb && (w.bflags[ia] & kBodyAlive) && (w.bflags[ib] & kBodyAlive) &&
+           w.bgen[ia] == a.mv.genA[m] && w.bgen[ib] == a.mv.genB[m];
+}
+
 // ------------------------------------------------------ single-block path ---
 // The whole solver for up to kBlockMaxManifolds manifolds in one thread block:
 // the same colouring, order, prepare, sweeps and cache rebuild as the
@@ -411,16 +423,86 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
     const SolverBuffers &sb = a.sb;
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
     uint32_t C = 0;
+    bool slotted = false;  // bodies got staging slots (colour path with a VelStage)
     if (serial) {
         for (uint32_t k = tid; k < M; k += nt) sb.order[k] = k;
         __syncthreads();
     } else {
-        // --- colouring (Jones-Plassmann rounds, as k_color) ---
+        // --- staging slots for the bodies of valid manifolds, assigned through a
+        // shared-memory hash table (in the sort area, free at this point); the
+        // colouring's per-body arrays and, after prepare, the staged velocities
+        // use them ---
+        if (vs) {
+            uint32_t *tkey = reinterpret_cast<uint32_t *>(s_sort);
+            uint32_t T = 1;
+            while (2 * T * 2 <= 3 * maxM) T <<= 1;  // key + value words fit the maxM * 12-byte sort area
+            uint32_t *tval = tkey + T;
+            for (uint32_t i = tid; i < T; i += nt) tkey[i] = kSlotFree;
+            if (tid == 0) {
+                sh.slots = 0;
+                sh.colored = 0;  // table overflow flag until the colouring starts
+            }
+            __syncthreads();
+            for (uint32_t m = tid; m < M; m += nt) {
+                if (!manifoldBodiesValid(a, m)) continue;
+                const uint32_t b2[2] = {a.mv.bodyA[m], a.mv.bodyB[m]};
+                for (int j = 0; j < 2; ++j) {
+                    uint32_t h = (b2[j] * 2654435761u) & (T - 1), probes = 0;
+                    for (;; h = (h + 1) & (T - 1)) {
+                        const uint32_t old = atomicCAS(&tkey[h], kSlotFree, b2[j]);
+                        if (old == kSlotFree || old == b2[j]) break;
+                        if (++probes == T) {
+                            sh.colored = 1;
+                            break;
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+            for (uint32_t i = tid; i < T; i += nt) {
+                const uint32_t key = tkey[i];
+                if (key == kSlotFree) continue;
+                const uint32_t sl = atomicAdd(&sh.slots, 1u);
+                tval[i] = sl;
+                if (sl < vs->cap) vs->slotBody[sl] = key;
+            }
+            __syncthreads();
+            slotted = sh.colored == 0 && sh.slots <= vs->cap;
+            if (slotted) {
+                auto find = [&](uint32_t body) {
+                    uint32_t h = (body * 2654435761u) & (T - 1);
+                    for (uint32_t probes = 0; probes < T && tkey[h] != body; ++probes) h = (h + 1) & (T - 1);
+                    return tval[h];
+                };
+                for (uint32_t m = tid; m < M; m += nt)
+                    vs->slot[m] = manifoldBodiesValid(a, m) ? make_uint2(find(a.mv.bodyA[m]), find(a.mv.bodyB[m]))
+                                                            : make_uint2(0u, 0u);
+                unsigned long long *best = reinterpret_cast<unsigned long long *>(vs->v);
+                for (uint32_t sl = tid; sl < 3 * sh.slots; sl += nt) best[sl < sh.slots ? sl : vs->cap + (sl - sh.slots)] = 0ull;
+            }
+            __syncthreads();
+        }
+        // --- colouring (Jones-Plassmann rounds, as k_color); per-body arrays in
+        // shared memory by slot when slotted, else in global memory by body ---
         for (uint32_t c = tid; c < kMaxColors; c += nt) s_count[c] = 0;
         if (tid == 0) {
             s_colored = 0;
             s_colors = 0;
         }
+        unsigned long long *cBest = sb.bodyBest, *cUsed = sb.bodyUsed;
+        if (slotted) {
+            cBest = reinterpret_cast<unsigned long long *>(vs->v);
+            cUsed = cBest + vs->cap;
+        }
+        auto cid = [&](uint32_t m, int side) -> uint32_t {
+            return slotted ? (side ? vs->slot[m].y : vs->slot[m].x) : (side ? a.mv.bodyB[m] : a.mv.bodyA[m]);
+        };
+        // Atomics resolve in L2; global reads go past L1 so no stale line is seen.
+        auto ldc = [&](const unsigned long long *p) { return slotted ? *p : __ldcg(p); };
+        auto stc = [&](unsigned long long *p, unsigned long long v) {
+            if (slotted) *p = v;
+            else __stcg(p, v);
+        };
         uint32_t *s_color = reinterpret_cast<uint32_t *>(s_sort);  // reused before the order sort
         for (uint32_t m = tid; m < M; m += nt) {
             uint32_t ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
@@ -428,13 +510,15 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
             bool db = bb < w.nb && (w.bflags[bb] & kBodyAlive) && w.bgen[bb] == a.mv.genB[m] && !(w.bflags[bb] & kBodyStatic);
             s_dyn[m] = (da ? 1u : 0u) | (db ? 2u : 0u);
             s_color[m] = kUncolored;
-            if (da) {
-                __stcg(&sb.bodyUsed[2 * ba], 0ull);
-                __stcg(&sb.bodyUsed[2 * ba + 1], 0ull);
-            }
-            if (db) {
-                __stcg(&sb.bodyUsed[2 * bb], 0ull);
-                __stcg(&sb.bodyUsed[2 * bb + 1], 0ull);
+            if (!slotted) {
+                if (da) {
+                    __stcg(&sb.bodyUsed[2 * ba], 0ull);
+                    __stcg(&sb.bodyUsed[2 * ba + 1], 0ull);
+                }
+                if (db) {
+                    __stcg(&sb.bodyUsed[2 * bb], 0ull);
+                    __stcg(&sb.bodyUsed[2 * bb + 1], 0ull);
+                }
             }
         }
         __syncthreads();
@@ -445,25 +529,24 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
             for (uint32_t m = tid; m < M; m += nt) {
                 if (s_color[m] != kUncolored) continue;
                 const unsigned long long p = stamp | colorPriority(m);
-                if (s_dyn[m] & 1u) atomicMax(&sb.bodyBest[a.mv.bodyA[m]], p);
-                if (s_dyn[m] & 2u) atomicMax(&sb.bodyBest[a.mv.bodyB[m]], p);
+                if (s_dyn[m] & 1u) atomicMax(&cBest[cid(m, 0)], p);
+                if (s_dyn[m] & 2u) atomicMax(&cBest[cid(m, 1)], p);
             }
             __syncthreads();
             for (uint32_t m = tid; m < M; m += nt) {
                 if (s_color[m] != kUncolored) continue;
                 const unsigned long long p = stamp | colorPriority(m);
-                const uint32_t d = s_dyn[m], ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
-                // Atomics resolve in L2; read past L1 so no stale line is seen.
-                if ((d & 1u) && __ldcg(&sb.bodyBest[ba]) != p) continue;
-                if ((d & 2u) && __ldcg(&sb.bodyBest[bb]) != p) continue;
+                const uint32_t d = s_dyn[m], ba = cid(m, 0), bb = cid(m, 1);
+                if ((d & 1u) && ldc(&cBest[ba]) != p) continue;
+                if ((d & 2u) && ldc(&cBest[bb]) != p) continue;
                 unsigned long long u0 = 0, u1 = 0;
                 if (d & 1u) {
-                    u0 |= __ldcg(&sb.bodyUsed[2 * ba]);
-                    u1 |= __ldcg(&sb.bodyUsed[2 * ba + 1]);
+                    u0 |= ldc(&cUsed[2 * ba]);
+                    u1 |= ldc(&cUsed[2 * ba + 1]);
                 }
                 if (d & 2u) {
-                    u0 |= __ldcg(&sb.bodyUsed[2 * bb]);
-                    u1 |= __ldcg(&sb.bodyUsed[2 * bb + 1]);
+                    u0 |= ldc(&cUsed[2 * bb]);
+                    u1 |= ldc(&cUsed[2 * bb + 1]);
                 }
                 uint32_t c;
                 if (~u0) c = __ffsll((long long)~u0) - 1;
@@ -474,8 +557,8 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
                 }
                 s_color[m] = c;
                 const unsigned long long bit = 1ull << (c & 63);
-                if (d & 1u) __stcg(&sb.bodyUsed[2 * ba + (c >> 6)], __ldcg(&sb.bodyUsed[2 * ba + (c >> 6)]) | bit);
-                if (d & 2u) __stcg(&sb.bodyUsed[2 * bb + (c >> 6)], __ldcg(&sb.bodyUsed[2 * bb + (c >> 6)]) | bit);
+                if (d & 1u) stc(&cUsed[2 * ba + (c >> 6)], ldc(&cUsed[2 * ba + (c >> 6)]) | bit);
+                if (d & 2u) stc(&cUsed[2 * bb + (c >> 6)], ldc(&cUsed[2 * bb + (c >> 6)]) | bit);
                 atomicAdd(&s_count[c], 1u);
                 atomicMax(&s_colors, c + 1);
                 atomicAdd(&s_colored, 1u);
@@ -540,47 +623,32 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
         }
         C = s_colors;
         __syncthreads();
+        if (slotted) {
+            // slots by manifold -> slots by solve index (through the sort area)
+            uint2 *tmp = reinterpret_cast<uint2 *>(s_sort);
+            for (uint32_t k = tid; k < M; k += nt) tmp[k] = vs->slot[sb.order[k]];
+            __syncthreads();
+            for (uint32_t k = tid; k < M; k += nt) vs->slot[k] = tmp[k];
+            __syncthreads();
+        }
     }
-    // --- prepare + warm-start matching ---
-    prepareRange(a, tid, nt, M);
+    // --- prepare + warm-start matching (old cache keys searched in shared memory when they fit) ---
+    {
+        const uint32_t cacheN = *a.oldCount;
+        const bool keysInShared = cacheN <= maxM;
+        if (keysInShared)
+            for (uint32_t i = tid; i < cacheN; i += nt) s_sort[i] = a.oldCache.key[i];
+        __syncthreads();
+        prepareRange(a, tid, nt, M, keysInShared ? s_sort : nullptr);
+    }
     __syncthreads();
-    // --- stage the touched bodies' velocities in shared memory ---
-    const bool stage = vs != nullptr && !serial && M > 0;
-    bool staged = false;
-    if (stage) {
-        for (uint32_t k = tid; k < M; k += nt) {
-            if (!sb.pcount[k]) continue;  // invalid manifold: touches no body
-            const uint2 bi = sb.pbody[k];
-            sb.bodySlot[bi.x] = kSlotMarked;
-            sb.bodySlot[bi.y] = kSlotMarked;
-        }
-        if (tid == 0) sh.slots = 0;
-        __syncthreads();
-        for (uint32_t k = tid; k < M; k += nt) {
-            if (!sb.pcount[k]) continue;
-            const uint2 bi = sb.pbody[k];
-            const uint32_t b2[2] = {bi.x, bi.y};
-            for (int j = 0; j < 2; ++j)
-                if (atomicCAS(&sb.bodySlot[b2[j]], kSlotMarked, kSlotClaimed) == kSlotMarked) {
-                    const uint32_t sl = atomicAdd(&sh.slots, 1u);
-                    if (sl < vs->cap) vs->slotBody[sl] = b2[j];
-                    atomicExch(&sb.bodySlot[b2[j]], sl);
-                }
-        }
-        __syncthreads();
-        const uint32_t nslots = sh.slots;
-        staged = nslots <= vs->cap;
-        if (staged) {
-            for (uint32_t k = tid; k < M; k += nt) {
-                const uint2 bi = sb.pbody[k];
-                vs->slot[k] = sb.pcount[k] ? make_uint2(__ldcg(&sb.bodySlot[bi.x]), __ldcg(&sb.bodySlot[bi.y]))
-                                           : make_uint2(0u, 0u);
-            }
-            for (uint32_t sl = tid; sl < nslots; sl += nt) {
-                const uint32_t b = vs->slotBody[sl];
-                vs->v[2 * sl] = ld4(&w.nxt.lin[b]);
-                vs->v[2 * sl + 1] = ld4(&w.nxt.ang[b]);
-            }
+    // --- stage the touched bodies' velocities in shared memory (slots from above) ---
+    const bool staged = slotted;
+    if (staged) {
+        for (uint32_t sl = tid; sl < sh.slots; sl += nt) {
+            const uint32_t b = vs->slotBody[sl];
+            vs->v[2 * sl] = ld4(&w.nxt.lin[b]);
+            vs->v[2 * sl + 1] = ld4(&w.nxt.ang[b]);
         }
         __syncthreads();
     }
@@ -614,22 +682,14 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
             }
     }
     __syncthreads();
-    if (stage) {
-        if (staged) {
-            const uint32_t nslots = sh.slots;
-            for (uint32_t sl = tid; sl < nslots; sl += nt) {
-                const uint32_t b = vs->slotBody[sl];
-                st4(&w.nxt.lin[b], vs->v[2 * sl]);
-                st4(&w.nxt.ang[b], vs->v[2 * sl + 1]);
-            }
+    if (staged) {
+        const uint32_t nslots = sh.slots;
+        for (uint32_t sl = tid; sl < nslots; sl += nt) {
+            const uint32_t b = vs->slotBody[sl];
+            st4(&w.nxt.lin[b], vs->v[2 * sl]);
+            st4(&w.nxt.ang[b], vs->v[2 * sl + 1]);
         }
         __syncthreads();
-        for (uint32_t k = tid; k < M; k += nt) {
-            if (!sb.pcount[k]) continue;
-            const uint2 bi = sb.pbody[k];
-            sb.bodySlot[bi.x] = kSlotFree;
-            sb.bodySlot[bi.y] = kSlotFree;
-        }
     }
     // --- impulses back to the manifolds ---
     for (uint32_t k = tid; k < M; k += nt) {

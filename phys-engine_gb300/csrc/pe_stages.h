@@ -63,7 +63,6 @@ struct SolverBuffers {
     unsigned long long *cacheKeys, *cacheKeysTmp;
     uint32_t *cacheVals, *cacheValsTmp;
     uint32_t *cacheCounts, *cacheOff;
-    uint32_t *bodySlot;             // [nb] velocity staging slot; 0xFFFFFFFF between steps (single-block path)
     uint32_t *bar;                  // grid barrier [2]
     uint32_t *counters;             // [4]
 };

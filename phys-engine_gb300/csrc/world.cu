@@ -359,11 +359,6 @@ void World::ensureCapacity() {
     sCacheOff_.reserve(m);
     sBar_.reserve(2);
     sCounters_.reserve(4);
-    if (sBodySlot_.count < nb || !sBodySlot_.ptr) {
-        // staging slots are "free" (all ones) between steps
-        sBodySlot_.reserve(nb);
-        PE_CHECK(cudaMemset(sBodySlot_.ptr, 0xFF, sBodySlot_.count * sizeof(uint32_t)));
-    }
     sb_ = SolverBuffers{m,
                         sBest_.ptr,
                         sUsed_.ptr,
@@ -388,7 +383,6 @@ void World::ensureCapacity() {
                         sCacheValsTmp_.ptr,
                         sCacheCounts_.ptr,
                         sCacheOff_.ptr,
-                        sBodySlot_.ptr,
                         sBar_.ptr,
                         sCounters_.ptr};
 

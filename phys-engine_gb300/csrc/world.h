@@ -210,7 +210,6 @@ class World {
     // solver
     SolverBuffers sb_{};
     DeviceArray<unsigned long long> sBest_, sUsed_, sEpoch_, sCacheKeys_, sCacheKeysTmp_;
-    DeviceArray<uint32_t> sBodySlot_;
     DeviceArray<uint32_t> sColor_, sDyn_, sColorCount_, sOrderKeys_, sOrderKeysTmp_, sOrder_, sOrderTmp_, sPcount_,
         sCacheVals_, sCacheValsTmp_, sCacheCounts_, sCacheOff_, sBar_, sCounters_;
     DeviceArray<float4> sPm_, sPmI_, sPp_, sPimp_, sPn_;
