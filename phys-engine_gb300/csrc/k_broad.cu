@@ -412,12 +412,216 @@ k_grid_body_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, c
     }
 }
 
+// ------------------------------------------------------------ hashed grid --
+// With a fixed cell size the grid needs no global cell range: a cell is keyed
+// by its exact coordinates (21 bits each) and entries are grouped by a hash of
+// the key (counting pass, scan, fill).  Each body then gathers its partners
+// from the buckets of its cells, keeping the entries with its exact cell key,
+// as the sorted grid does.  Cells, overflow boxes, pairs, their order and the
+// comparison / entry / overflow counters are those of the reference's grid
+// (broadphase.cpp:62-182).
+__device__ __forceinline__ bool cellKey21(int x, int y, int z, unsigned long long &key) {
+    const int lim = 1 << 20;
+    if (x < -lim || x >= lim || y < -lim || y >= lim || z < -lim || z >= lim) return false;
+    key = ((unsigned long long)(x + lim) << 42) | ((unsigned long long)(y + lim) << 21) | (unsigned long long)(z + lim);
+    return true;
+}
+__device__ __forceinline__ uint32_t bucketOf(unsigned long long key, uint32_t logB) {
+    return (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - logB));
+}
+
+// Cell range per box (as k_grid_range) and the entry count of each bucket.
+__global__ void k_hgrid_count(BroadInput in, DevStats *st, int4 *firstCell, uint8_t *inGrid, uint32_t *overflow,
+                              double cell, uint32_t *bucketCount, uint32_t logB) {
+    const uint32_t n = *in.d_n;
+    const double inv = 1.0 / cell;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->cellSize = cell;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 mn = in.mn[i], mx = in.mx[i];
+        const double lower[3] = {cellFloor(mn.x, cell, inv), cellFloor(mn.y, cell, inv), cellFloor(mn.z, cell, inv)};
+        const double upper[3] = {cellFloor(mx.x, cell, inv), cellFloor(mx.y, cell, inv), cellFloor(mx.z, cell, inv)};
+        uint64_t total = 1;
+        int32_t first[3];
+        int counts[3];
+        bool ok = true;
+        for (int a = 0; a < 3 && ok; ++a) {
+            if (!isfinite(lower[a]) || !isfinite(upper[a]) || lower[a] < -2147483648.0 || upper[a] > 2147483647.0 ||
+                lower[a] > upper[a]) {
+                ok = false;
+                break;
+            }
+            const int64_t c = (int64_t)upper[a] - (int64_t)lower[a] + 1;
+            if (c > (int64_t)(64 / total)) {
+                ok = false;
+                break;
+            }
+            first[a] = (int32_t)lower[a];
+            counts[a] = (int)c;
+            total *= (uint64_t)c;
+        }
+        if (!ok) {
+            inGrid[i] = 0;
+            overflow[aggregatedAppend(&st->overflowCount)] = i;
+            continue;
+        }
+        unsigned long long k0, k1;
+        if (!cellKey21(first[0], first[1], first[2], k0) ||
+            !cellKey21(first[0] + counts[0] - 1, first[1] + counts[1] - 1, first[2] + counts[2] - 1, k1)) {
+            atomicOr(&st->err, kErrHashRange);
+            inGrid[i] = 0;
+            continue;
+        }
+        firstCell[i] = make_int4(first[0], first[1], first[2], counts[0] | (counts[1] << 8) | (counts[2] << 16));
+        inGrid[i] = 1;
+        for (int x = 0; x < counts[0]; ++x)
+            for (int y = 0; y < counts[1]; ++y)
+                for (int z = 0; z < counts[2]; ++z) {
+                    unsigned long long key;
+                    cellKey21(first[0] + x, first[1] + y, first[2] + z, key);
+                    atomicAdd(&bucketCount[bucketOf(key, logB)], 1u);
+                }
+    }
+}
+
+// Entries into their buckets: bucketOff[h] advances from the bucket's start to
+// its end, so afterwards bucket h is [bucketOff[h - 1], bucketOff[h]).
+__global__ void k_hgrid_fill(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, uint32_t *bucketOff,
+                             unsigned long long *keys, uint32_t *vals, uint32_t cap, uint32_t logB) {
+    const uint32_t n = *in.d_n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (!inGrid[i]) continue;
+        const int4 f = firstCell[i];
+        const int cx = f.w & 0xFF, cy = (f.w >> 8) & 0xFF, cz = (f.w >> 16) & 0xFF;
+        for (int x = 0; x < cx; ++x)
+            for (int y = 0; y < cy; ++y)
+                for (int z = 0; z < cz; ++z) {
+                    unsigned long long key;
+                    cellKey21(f.x + x, f.y + y, f.z + z, key);
+                    const uint32_t pos = atomicAdd(&bucketOff[bucketOf(key, logB)], 1u);
+                    if (pos < cap) {
+                        keys[pos] = key;
+                        vals[pos] = i;
+                    }
+                }
+    }
+}
+
+// Per-body pairs from the buckets (the counterpart of k_grid_body_pairs).
+__global__ void __launch_bounds__(kBodyPairThreads)
+k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const uint32_t *overflow,
+              const uint32_t *bucketOff, uint32_t logB, uint32_t ecap, const unsigned long long *ekeys,
+              const uint32_t *evals, const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen,
+              uint32_t *pairA, uint32_t *pairB, uint32_t cap, DevStats *st, unsigned long long *state,
+              uint32_t *counter) {
+    __shared__ uint32_t s_tile, s_scan[9], s_prefix;
+    // Out-of-range cells or too few entry slots: the host re-runs the step.
+    if ((st->err & kErrHashRange) || st->gridEntryCount > ecap) return;
+    const uint32_t n = *in.d_n;
+    const uint32_t F = st->overflowCount;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && F)
+        atomicAdd(&st->gridComparisons, (unsigned long long)F * (n - F) + (unsigned long long)F * (F - 1) / 2);
+    const uint32_t ntiles = max((n + kBodyPairThreads - 1) / kBodyPairThreads, 1u);
+    for (;;) {
+        const uint32_t tile = takeTile(counter, &s_tile);
+        if (tile >= ntiles) return;
+        const uint32_t a = tile * kBodyPairThreads + threadIdx.x;
+        uint32_t part[kBodyPartners];
+        uint32_t cnt = 0;
+        unsigned long long cmp = 0;
+        if (a < n) {
+            const float4 amn = in.mn[a], amx = in.mx[a];
+            auto add = [&](uint32_t b) {
+                if (cnt < kBodyPartners) part[cnt] = b;
+                ++cnt;
+            };
+            if (inGrid[a]) {
+                const int4 fa = firstCell[a];
+                const int cx = fa.w & 0xFF, cy = (fa.w >> 8) & 0xFF, cz = (fa.w >> 16) & 0xFF;
+                for (int x = 0; x < cx; ++x)
+                    for (int y = 0; y < cy; ++y)
+                        for (int z = 0; z < cz; ++z) {
+                            unsigned long long key;
+                            cellKey21(fa.x + x, fa.y + y, fa.z + z, key);
+                            const uint32_t h = bucketOf(key, logB);
+                            const uint32_t lo = h ? bucketOff[h - 1] : 0u, hi = bucketOff[h];
+                            for (uint32_t e = lo; e < hi; ++e) {
+                                if (ekeys[e] != key) continue;
+                                const uint32_t b = evals[e];
+                                if (b <= a) continue;
+                                ++cmp;
+                                if (!overlaps(amn, amx, in.mn[b], in.mx[b])) continue;
+                                const int4 fb = firstCell[b];
+                                unsigned long long low;
+                                cellKey21(max(fa.x, fb.x), max(fa.y, fb.y), max(fa.z, fb.z), low);
+                                if (low == key) add(b);
+                            }
+                        }
+                for (uint32_t k = 0; k < F; ++k) {
+                    const uint32_t o = overflow[k];
+                    if (o > a && overlaps(amn, amx, in.mn[o], in.mx[o])) add(o);
+                }
+            } else {
+                for (uint32_t b = a + 1; b < n; ++b)
+                    if (overlaps(amn, amx, in.mn[b], in.mx[b])) add(b);
+            }
+            if (cnt > kBodyPartners) atomicOr(&st->err, kErrBodyPairs);
+            const uint32_t m = min(cnt, kBodyPartners);
+            for (uint32_t i = 1; i < m; ++i) {
+                const uint32_t v = part[i];
+                uint32_t j = i;
+                while (j > 0 && part[j - 1] > v) {
+                    part[j] = part[j - 1];
+                    --j;
+                }
+                part[j] = v;
+            }
+        }
+        const uint32_t m = min(cnt, kBodyPartners);
+        const uint32_t sa = a < n ? (inSlot ? inSlot[a] : a) : 0u;
+        uint32_t kept = 0;
+        for (uint32_t j = 0; j < m; ++j) {
+            const uint32_t sb = inSlot ? inSlot[part[j]] : part[j];
+            if (cbody && cbody[sa] == cbody[sb] && cbgen[sa] == cbgen[sb]) continue;
+            ++kept;
+        }
+        if (cnt) {
+            atomicAdd(&st->rawPairs, cnt);
+            atomicAdd(&st->uniquePairs, cnt);
+        }
+        if (cmp) atomicAdd(&st->gridComparisons, cmp);
+        uint32_t total;
+        const uint32_t local = blockExclusiveScan(kept, total, s_scan);
+        if (threadIdx.x == 0) s_prefix = lookbackExclusive(state, tile, total, &st->err);
+        __syncthreads();
+        uint32_t o = s_prefix + local;
+        for (uint32_t j = 0; j < m; ++j) {
+            const uint32_t sb = inSlot ? inSlot[part[j]] : part[j];
+            if (cbody && cbody[sa] == cbody[sb] && cbgen[sa] == cbgen[sb]) continue;
+            if (o < cap) {
+                pairA[o] = sa;
+                pairB[o] = sb;
+            }
+            ++o;
+        }
+        if (threadIdx.x == 0 && tile + 1 == ntiles) st->pairs = s_prefix + total;
+        __syncthreads();
+    }
+}
+
 void launchGridBodyPairs(const BroadInput &in, const BroadBuffers &bb, PairBuffers &pb, const uint32_t *inSlot,
                          const uint32_t *cbody, const uint32_t *cbgen, DevStats *st, Scratch &ws, cudaStream_t s) {
     uint32_t tiles = (in.maxN + kBodyPairThreads - 1) / kBodyPairThreads;
     if (tiles == 0) tiles = 1;
     PE_CHECK(cudaMemsetAsync(ws.scanState, 0, sizeof(unsigned long long) * (tiles + 1), s));
     const uint32_t grid = tiles < 152u * 8u ? tiles : 152u * 8u;
+    if (bb.hashed) {
+        k_hgrid_pairs<<<grid, kBodyPairThreads, 0, s>>>(in, bb.firstCell, bb.inGrid, bb.overflow, bb.bucketOff,
+                                                         bb.logBuckets, bb.entryCap, bb.entryKeys, bb.entryVals, inSlot,
+                                                         cbody, cbgen, pb.a, pb.b, pb.cap, st, ws.scanState,
+                                                         (uint32_t *)(ws.scanState + tiles));
+        PE_LAUNCHED();
+        return;
+    }
     k_grid_body_pairs<<<grid, kBodyPairThreads, 0, s>>>(in, bb.firstCell, bb.inGrid, bb.overflow,
                                                          &st->gridEntryCount, bb.entryCap, bb.entryKeys,
                                                          bb.entryVals, inSlot, cbody, cbgen, pb.a, pb.b, pb.cap, st,
@@ -511,6 +715,19 @@ void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, Broad
 void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBuffers &pb, DevStats *st, Scratch &ws,
                 cudaStream_t s) {
     uint32_t *err = &st->err;
+    if (bb.hashed) {
+        // fixed cell size: count per bucket, scan, fill (pairs: launchGridBodyPairs)
+        const uint32_t B = 1u << bb.logBuckets;
+        PE_CHECK(cudaMemsetAsync(bb.bucketCount, 0, B * sizeof(uint32_t), s));
+        k_hgrid_count<<<gridFor(in.maxN), 256, 0, s>>>(in, st, bb.firstCell, bb.inGrid, bb.overflow, fixedCell,
+                                                       bb.bucketCount, bb.logBuckets);
+        PE_LAUNCHED();
+        launchScanExclusive(bb.bucketCount, bb.bucketOff, nullptr, B, &st->gridEntryCount, ws, err, s);
+        k_hgrid_fill<<<gridFor(in.maxN), 256, 0, s>>>(in, bb.firstCell, bb.inGrid, bb.bucketOff, bb.entryKeys,
+                                                      bb.entryVals, bb.entryCap, bb.logBuckets);
+        PE_LAUNCHED();
+        return;
+    }
     // counters[0] counts the non-zero widths of this call.
     PE_CHECK(cudaMemsetAsync(bb.counters, 0, 4 * sizeof(uint32_t), s));
     if (fixedCell <= 0.0) {

@@ -189,22 +189,28 @@ __global__ void k_cache_write(SolveArgs a, CacheView nc, uint32_t cacheCap) {
 
 // Velocity staging slots of the single-block solver (bodies touched by contacts).
 constexpr uint32_t kStageSlots = 3072;
-constexpr size_t kBlockSolveSmem = kBlockMaxManifolds * (8 + 4 + 8) + kStageSlots * (32 + 4);
+constexpr size_t blockSolveSmem(uint32_t blockM, uint32_t stageSlots) {
+    return (size_t)blockM * (8 + 4 + 8) + (size_t)stageSlots * (32 + 4);
+}
 
+// blockM: manifold capacity of this launch (power of two); shared memory is
+// sized for it and for `stageSlots` staged bodies, so that the rest of the
+// SM's unified L1 / shared storage caches the prepared contact constants.
 __global__ void __launch_bounds__(kBlockSolveThreads)
-k_solve_block(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount, int serial) {
-    // kBlockMaxManifolds u64 sort keys, u32 flags, uint2 stage slots; then the
-    // staged velocities (2 float4 per slot) and the body of each slot.
+k_solve_block(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount, int serial, uint32_t blockM,
+              uint32_t stageSlots) {
+    // blockM u64 sort keys, u32 flags, uint2 stage slots; then the staged
+    // velocities (2 float4 per slot) and the body of each slot.
     extern __shared__ unsigned long long s_sort[];
     __shared__ BlockSolveShared sh;
     unsigned char *base = reinterpret_cast<unsigned char *>(s_sort);
     VelStage vs;
-    vs.slot = reinterpret_cast<uint2 *>(base + kBlockMaxManifolds * 12);
-    vs.v = reinterpret_cast<float4 *>(base + kBlockMaxManifolds * 20);
-    vs.slotBody = reinterpret_cast<uint32_t *>(base + kBlockMaxManifolds * 20 + kStageSlots * 32);
-    vs.cap = kStageSlots;
-    solveBlock(a, nc, cacheCap, newCount, serial, kBlockMaxManifolds, s_sort,
-               reinterpret_cast<uint32_t *>(s_sort + kBlockMaxManifolds), sh, &vs);
+    vs.slot = reinterpret_cast<uint2 *>(base + (size_t)blockM * 12);
+    vs.v = reinterpret_cast<float4 *>(base + (size_t)blockM * 20);
+    vs.slotBody = reinterpret_cast<uint32_t *>(base + (size_t)blockM * 20 + (size_t)stageSlots * 32);
+    vs.cap = stageSlots;
+    solveBlock(a, nc, cacheCap, newCount, serial, blockM, s_sort, reinterpret_cast<uint32_t *>(s_sort + blockM), sh,
+               stageSlots ? &vs : nullptr);
 }
 
 static int gridFor(uint32_t n, int threads = 256, int maxBlocks = 152 * 8) {
@@ -242,19 +248,27 @@ int maxCooperativeBlocks(int smCount) {
 
 void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &oldCache, const uint32_t *oldCacheCount,
                   const CacheView &newCache, uint32_t *newCacheCount, uint32_t cacheCap, SolverBuffers &sb,
-                  int iterations, int orderMode, int coopBlocks, bool blockPath, bool pairOrderCache, DevStats *st,
-                  Scratch &ws, cudaStream_t s) {
+                  int iterations, int orderMode, int coopBlocks, bool blockPath, uint32_t blockM, bool pairOrderCache,
+                  DevStats *st, Scratch &ws, cudaStream_t s) {
     SolveArgs a{w, mv, sb, oldCache, oldCacheCount, st, sb.mcap, iterations, pairOrderCache};
     uint32_t *err = &st->err;
     const uint32_t mcap = sb.mcap;
     if (blockPath) {
         static bool configured = false;
-        const size_t smem = kBlockSolveSmem;
         if (!configured) {
-            PE_CHECK(cudaFuncSetAttribute(k_solve_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            PE_CHECK(cudaFuncSetAttribute(k_solve_block, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)blockSolveSmem(kBlockMaxManifolds, kStageSlots)));
             configured = true;
         }
-        k_solve_block<<<1, kBlockSolveThreads, smem, s>>>(a, newCache, cacheCap, newCacheCount, orderMode == 0 ? 1 : 0);
+        uint32_t bm = kBlockMaxManifolds;
+        if (blockM && blockM < kBlockMaxManifolds) {
+            bm = 64;
+            while (bm < blockM) bm <<= 1;
+        }
+        uint32_t slots = 2 * bm < kStageSlots ? 2 * bm : kStageSlots;
+        const size_t smem = blockSolveSmem(bm, slots);
+        k_solve_block<<<1, kBlockSolveThreads, smem, s>>>(a, newCache, cacheCap, newCacheCount, orderMode == 0 ? 1 : 0,
+                                                          bm, slots);
         PE_LAUNCHED();
         return;
     }

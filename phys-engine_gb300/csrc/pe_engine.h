@@ -39,6 +39,7 @@ enum : uint32_t {
     kErrEpa = 32u,
     kErrSmallPath = 64u,  // a single-block path saw more work than it holds: re-run on the full path
     kErrBodyPairs = 128u, // a body had more grid partners than the per-body pair path holds
+    kErrHashRange = 256u, // a grid cell lies outside the hashed grid's coordinate range
 };
 
 // Body flag bits (bflags) and collider flag layout (cflags).

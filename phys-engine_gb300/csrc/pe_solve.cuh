@@ -429,13 +429,13 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
         __syncthreads();
     } else {
         // --- staging slots for the bodies of valid manifolds, assigned through a
-        // shared-memory hash table (in the sort area, free at this point); the
-        // colouring's per-body arrays and, after prepare, the staged velocities
-        // use them ---
+        // shared-memory hash table (in the velocity area, free until the
+        // colouring); the colouring's per-body arrays and, after prepare, the
+        // staged velocities use them ---
         if (vs) {
-            uint32_t *tkey = reinterpret_cast<uint32_t *>(s_sort);
+            uint32_t *tkey = reinterpret_cast<uint32_t *>(vs->v);
             uint32_t T = 1;
-            while (2 * T * 2 <= 3 * maxM) T <<= 1;  // key + value words fit the maxM * 12-byte sort area
+            while (2 * T <= 4 * vs->cap) T <<= 1;  // key + value words fit the 8 words per slot
             uint32_t *tval = tkey + T;
             for (uint32_t i = tid; i < T; i += nt) tkey[i] = kSlotFree;
             if (tid == 0) {
@@ -477,6 +477,7 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
                 for (uint32_t m = tid; m < M; m += nt)
                     vs->slot[m] = manifoldBodiesValid(a, m) ? make_uint2(find(a.mv.bodyA[m]), find(a.mv.bodyB[m]))
                                                             : make_uint2(0u, 0u);
+                __syncthreads();  // the colouring arrays below overwrite the table
                 unsigned long long *best = reinterpret_cast<unsigned long long *>(vs->v);
                 for (uint32_t sl = tid; sl < 3 * sh.slots; sl += nt) best[sl < sh.slots ? sl : vs->cap + (sl - sh.slots)] = 0ull;
             }

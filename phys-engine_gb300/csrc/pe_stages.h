@@ -28,6 +28,10 @@ struct BroadBuffers {
     uint32_t entryCap;
     uint32_t keyBits;    // cell-key bits sorted this step (from the previous step's cell range)
     uint32_t *counters;  // [4] device scratch counters
+    // hashed grid (fixed cell size): entries grouped by a hash of the cell
+    uint32_t *bucketCount, *bucketOff;  // [1 << logBuckets]
+    uint32_t logBuckets;
+    bool hashed;
 };
 
 struct PairBuffers {
@@ -95,8 +99,8 @@ void launchNarrowphase(const WorldView &w, const PairBuffers &pb, const Manifold
                        Scratch &ws, cudaStream_t s);
 void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &oldCache, const uint32_t *oldCacheCount,
                   const CacheView &newCache, uint32_t *newCacheCount, uint32_t cacheCap, SolverBuffers &sb,
-                  int iterations, int orderMode, int coopBlocks, bool blockPath, bool pairOrderCache, DevStats *st,
-                  Scratch &ws, cudaStream_t s);
+                  int iterations, int orderMode, int coopBlocks, bool blockPath, uint32_t blockM, bool pairOrderCache,
+                  DevStats *st, Scratch &ws, cudaStream_t s);
 // Largest manifold count the single-block solver handles, and the largest
 // body index it can key (bodies < 2^20).
 constexpr uint32_t kBlockMaxManifolds = 4096;

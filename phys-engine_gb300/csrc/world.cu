@@ -305,10 +305,16 @@ void World::ensureCapacity() {
     bbEntryKeysTmp_.reserve(entryCap_);
     bbEntryVals_.reserve(entryCap_);
     bbEntryValsTmp_.reserve(entryCap_);
+    // hashed grid buckets: a power of two, about two per collider
+    uint32_t logB = 10;
+    while ((1u << logB) < 2u * nc && logB < 30) ++logB;
+    bbBucketCount_.reserve(1u << logB);
+    bbBucketOff_.reserve(1u << logB);
     bb_ = BroadBuffers{bbKeyTmp32_.ptr, bbValTmp_.ptr, bbMinX_.ptr, bbMaxX_.ptr, bbYZ_.ptr, bbIdx_.ptr, bbLen_.ptr,
                        bbOff_.ptr, bbWidth_.ptr, bbWidthTmp_.ptr, bbFirst_.ptr, bbCellCount_.ptr, bbInGrid_.ptr,
                        bbOverflow_.ptr, bbEntryOff_.ptr, bbEntryKeys_.ptr, bbEntryKeysTmp_.ptr, bbEntryVals_.ptr,
-                       bbEntryValsTmp_.ptr, entryCap_, gridKeyBits_, bbCounters_.ptr};
+                       bbEntryValsTmp_.ptr, entryCap_, gridKeyBits_, bbCounters_.ptr, bbBucketCount_.ptr,
+                       bbBucketOff_.ptr, logB, false};
 
     if (pairCap_ < 4u * nc) pairCap_ = std::max<uint32_t>(65536, 4u * nc);
     pairKeys_.reserve(pairCap_);
@@ -484,7 +490,8 @@ void World::runPipeline(float dt) {
     launchNarrowphase(w, pb_, mv, mcap_, st, ws_, s);
     PE_CHECK(cudaEventRecordWithFlags(evStage_[3], s, cudaEventRecordExternal));
     launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], cacheView(1 - cache_), &cCount_.ptr[1 - cache_],
-                 cacheCap_, sb_, iterations, orderMode, coopBlocks_, blockSolver_, identityColliders_, st, ws_, s);
+                 cacheCap_, sb_, iterations, orderMode, coopBlocks_, blockSolver_, blockM_, identityColliders_, st,
+                 ws_, s);
     PE_CHECK(cudaEventRecordWithFlags(evStage_[4], s, cudaEventRecordExternal));
     launchIntegratePose(w, s);
     PE_CHECK(cudaEventRecordWithFlags(evStage_[5], s, cudaEventRecordExternal));
@@ -502,6 +509,12 @@ bool World::finishStep() {
                                                          "grid cell range exceeds 64 key bits"));
     }
     bool retry = false, grew = false;
+    if (h.err & kErrHashRange) {
+        // A cell coordinate beyond the hashed grid's 21-bit range: use the
+        // sorted grid from now on.
+        hashGrid_ = false;
+        retry = true;
+    }
     if (h.err & kErrBodyPairs) {
         // A body had more grid partners than the per-body path holds: this
         // world uses the sort-based pair path from now on.
@@ -578,8 +591,8 @@ bool World::GraphKey::operator==(const GraphKey &o) const {
     return nb == o.nb && nc == o.nc && pairCap == o.pairCap && entryCap == o.entryCap && mcap == o.mcap &&
            cacheCap == o.cacheCap && dt == o.dt && gx == o.gx && gy == o.gy && gz == o.gz &&
            algorithm == o.algorithm && iterations == o.iterations && orderMode == o.orderMode &&
-           coopBlocks == o.coopBlocks && blockSolver == o.blockSolver && pairBits == o.pairBits &&
-           blockPairs == o.blockPairs && bodyPairs == o.bodyPairs && gridKeyBits == o.gridKeyBits && cellSize == o.cellSize && dense == o.dense &&
+           coopBlocks == o.coopBlocks && blockSolver == o.blockSolver && blockM == o.blockM && pairBits == o.pairBits &&
+           blockPairs == o.blockPairs && bodyPairs == o.bodyPairs && hashed == o.hashed && gridKeyBits == o.gridKeyBits && cellSize == o.cellSize && dense == o.dense &&
            localIdentity == o.localIdentity && forces == o.forces && identityColliders == o.identityColliders;
 }
 
@@ -600,9 +613,11 @@ World::GraphKey World::currentKey(float dt) const {
     k.orderMode = orderMode;
     k.coopBlocks = coopBlocks_;
     k.blockSolver = blockSolver_;
+    k.blockM = blockM_;
     k.pairBits = pb_.bits;
     k.blockPairs = pb_.blockPath;
     k.bodyPairs = pb_.bodyPath;
+    k.hashed = bb_.hashed;
     k.gridKeyBits = bb_.keyBits;
     k.cellSize = cellSize;
     k.dense = dense_;
@@ -631,6 +646,8 @@ unsigned long long World::launchStep(float dt) {
     // Small manifold counts run the single-block solver (with headroom over
     // the last step's count; an overflow re-runs the step on the full path).
     blockSolver_ = lastMEstimate_ + lastMEstimate_ / 4 + 64 <= kBlockMaxManifolds && nb_ <= kBlockMaxBodies;
+    blockM_ = 64;
+    while (blockM_ < lastMEstimate_ + lastMEstimate_ / 4 + 64 && blockM_ < kBlockMaxManifolds) blockM_ <<= 1;
     // Pair keys need bits for input indices < nc; the small finalize path is
     // used while the last raw pair count leaves headroom.
     uint32_t bits = 1;
@@ -638,6 +655,7 @@ unsigned long long World::launchStep(float dt) {
     pb_.bits = bits;
     pb_.blockPath = lastRawEstimate_ + lastRawEstimate_ / 4 + 256 <= kBlockMaxPairs;
     pb_.bodyPath = algorithm == 1 && bodyPairs_;
+    bb_.hashed = pb_.bodyPath && cellSize > 0.0 && hashGrid_;
     bb_.keyBits = gridKeyBits_;
     if (graphsDisabled_) {
         const unsigned long long l0 = g_kernelLaunches;
@@ -893,6 +911,7 @@ void World::broadphaseOnly(const float *mins, const float *maxs, uint32_t n, int
         pb_.bits = bits;
         pb_.blockPath = false;
         pb_.bodyPath = false;
+        bb_.hashed = false;
         bb_.keyBits = 64;
         if (algo == 0) {
             launchSapKeys(in, sapKeys_.ptr, sapVals_.ptr, s);
@@ -1002,7 +1021,7 @@ void World::solveOnly(std::vector<float> &recs, uint32_t count, float dt, int it
     blocks = std::min<uint32_t>(blocks, (uint32_t)maxCooperativeBlocks(smCount_));
     const bool block = count <= kBlockMaxManifolds && nb_ <= kBlockMaxBodies;
     launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], cacheView(1 - cache_), &cCount_.ptr[1 - cache_],
-                 cacheCap_, sb_, iters, mode, (int)blocks, block, false, st, ws_, s);
+                 cacheCap_, sb_, iters, mode, (int)blocks, block, 0u, false, st, ws_, s);
     PE_CHECK(cudaMemcpyAsync(hostStats_, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
     PE_CHECK(cudaStreamSynchronize(s));
     if (hostStats_->err & (kErrTimeout | kErrColors)) throw std::runtime_error("solve failed on the device");

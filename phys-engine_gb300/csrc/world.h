@@ -190,6 +190,7 @@ class World {
     DeviceArray<uint32_t> sapKeys_, sapVals_;
     // broadphase / pairs
     BroadBuffers bb_{};
+    DeviceArray<uint32_t> bbBucketCount_, bbBucketOff_;
     DeviceArray<uint32_t> bbKeyTmp32_, bbValTmp_, bbIdx_, bbLen_, bbOff_, bbCellCount_, bbOverflow_, bbEntryOff_,
         bbEntryVals_, bbEntryValsTmp_, bbCounters_;
     DeviceArray<float> bbMinX_, bbMaxX_;
@@ -234,7 +235,8 @@ class World {
         uint32_t nb, nc, pairCap, entryCap, mcap, cacheCap;
         float dt, gx, gy, gz;
         int algorithm, iterations, orderMode, coopBlocks;
-        bool blockSolver, blockPairs, bodyPairs;
+        bool blockSolver, blockPairs, bodyPairs, hashed;
+        uint32_t blockM;
         uint32_t pairBits, gridKeyBits;
         double cellSize;
         bool dense, localIdentity, forces, identityColliders;
@@ -248,7 +250,9 @@ class World {
     std::string graphError_;
     int coopBlocks_ = 1;
     bool blockSolver_ = true;
+    uint32_t blockM_ = kBlockMaxManifolds;  // manifold capacity of the single-block solver launch
     bool bodyPairs_ = true;
+    bool hashGrid_ = true;  // fixed-cell grid through hashed buckets (off after a cell left its range)
     bool identityColliders_ = false;  // collider i is body i for every slot (unique body pair per manifold)  // grid pairs per body (off after a body overflowed its partner list)
     GraphKey currentKey(float dt) const;
     void dropGraphs();
