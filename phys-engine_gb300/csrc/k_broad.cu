@@ -137,14 +137,18 @@ __global__ void k_grid_cellsize(const unsigned long long *sortedWidths, const ui
 }
 
 // floor((double)x / cell) exactly as the reference computes it
-// (broadphase.cpp:66-71).  x * (1/cell) is within a few ulps of the rounded
-// quotient; away from integer boundaries both floor to the same value, so the
-// division only runs when the product lies within 1e-9 (relative) of one.
-__device__ __forceinline__ double cellFloor(float x, double cell, double inv) {
-    const double q = (double)x * inv;
-    const double f = floor(q);
-    const double tol = 1e-9 * fmax(1.0, fabs(q));
-    if (q - f > tol && (f + 1.0) - q > tol && isfinite(q)) return f;
+// (broadphase.cpp:66-71).  The float product q = x * invf (invf = 1/cell
+// rounded to float) is within 2^-23 (relative) of the exact quotient; when q
+// lies farther than 1e-6 (relative) from both neighbouring integers, the exact
+// quotient and its double rounding floor to the same integer as q, so the
+// double division only runs near cell boundaries and for |q| >= 2^20.
+__device__ __forceinline__ double cellFloor(float x, double cell, float invf) {
+    const float q = x * invf;
+    if (fabsf(q) < 1048576.0f) {
+        const float f = floorf(q);
+        const float tol = 1e-6f * fmaxf(1.0f, fabsf(q));
+        if (q - f > tol && (f + 1.0f) - q > tol) return (double)f;
+    }
     return floor((double)x / cell);
 }
 
@@ -156,7 +160,7 @@ __global__ void k_grid_range(BroadInput in, DevStats *st, int4 *firstCell, uint3
     const uint32_t n = *in.d_n;
     if (fixedCell > 0.0 && blockIdx.x == 0 && threadIdx.x == 0) st->cellSize = fixedCell;
     const double cell = fixedCell > 0.0 ? fixedCell : st->cellSize;
-    const double inv = 1.0 / cell;
+    const float inv = (float)(1.0 / cell);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 mn = in.mn[i], mx = in.mx[i];
         double lower[3] = {cellFloor(mn.x, cell, inv), cellFloor(mn.y, cell, inv), cellFloor(mn.z, cell, inv)};
@@ -395,7 +399,10 @@ k_grid_body_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, c
         if (cmp) atomicAdd(&st->gridComparisons, cmp);
         uint32_t total;
         const uint32_t local = blockExclusiveScan(kept, total, s_scan);
-        if (threadIdx.x == 0) s_prefix = lookbackExclusive(state, tile, total, &st->err);
+        if (threadIdx.x < 32) {
+            const uint32_t pre = lookbackExclusiveWarp(state, tile, total, &st->err);
+            if (threadIdx.x == 0) s_prefix = pre;
+        }
         __syncthreads();
         uint32_t o = s_prefix + local;
         for (uint32_t j = 0; j < m; ++j) {
@@ -430,78 +437,77 @@ __device__ __forceinline__ uint32_t bucketOf(unsigned long long key, uint32_t lo
     return (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> (64 - logB));
 }
 
-// Cell range per box (as k_grid_range) and the entry count of each bucket.
-__global__ void k_hgrid_count(BroadInput in, DevStats *st, int4 *firstCell, uint8_t *inGrid, uint32_t *overflow,
-                              double cell, uint32_t *bucketCount, uint32_t logB) {
+constexpr uint32_t kNoEntry = 0xFFFFFFFFu;
+
+// Cell range per box (as k_grid_range) and one entry per covered cell, pushed
+// onto its bucket's list: entry e holds (cell key, body) and the bucket's
+// previous head.  Entry slots come from one counter (a warp scan of the boxes'
+// cell counts, one atomic per warp), so entry order varies from run to run;
+// nothing downstream depends on it (each body sorts its partners).
+__global__ void k_hgrid_insert(BroadInput in, DevStats *st, int4 *firstCell, uint8_t *inGrid, uint32_t *overflow,
+                               double cell, float inv, uint32_t *bucketHead, uint32_t logB,
+                               unsigned long long *keys, uint32_t *vals, uint32_t *next, uint32_t ecap) {
     const uint32_t n = *in.d_n;
-    const double inv = 1.0 / cell;
+    const uint32_t lane = threadIdx.x & 31;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->cellSize = cell;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 mn = in.mn[i], mx = in.mx[i];
-        const double lower[3] = {cellFloor(mn.x, cell, inv), cellFloor(mn.y, cell, inv), cellFloor(mn.z, cell, inv)};
-        const double upper[3] = {cellFloor(mx.x, cell, inv), cellFloor(mx.y, cell, inv), cellFloor(mx.z, cell, inv)};
-        uint64_t total = 1;
-        int32_t first[3];
-        int counts[3];
-        bool ok = true;
-        for (int a = 0; a < 3 && ok; ++a) {
-            if (!isfinite(lower[a]) || !isfinite(upper[a]) || lower[a] < -2147483648.0 || upper[a] > 2147483647.0 ||
-                lower[a] > upper[a]) {
-                ok = false;
-                break;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + lane;
+        uint32_t total = 0;
+        int32_t first[3] = {0, 0, 0};
+        int counts[3] = {0, 0, 0};
+        if (i < n) {
+            const float4 mn = in.mn[i], mx = in.mx[i];
+            const double lower[3] = {cellFloor(mn.x, cell, inv), cellFloor(mn.y, cell, inv), cellFloor(mn.z, cell, inv)};
+            const double upper[3] = {cellFloor(mx.x, cell, inv), cellFloor(mx.y, cell, inv), cellFloor(mx.z, cell, inv)};
+            uint64_t cells = 1;
+            bool ok = true;
+            for (int a = 0; a < 3 && ok; ++a) {
+                if (!isfinite(lower[a]) || !isfinite(upper[a]) || lower[a] < -2147483648.0 ||
+                    upper[a] > 2147483647.0 || lower[a] > upper[a]) {
+                    ok = false;
+                    break;
+                }
+                const int64_t c = (int64_t)upper[a] - (int64_t)lower[a] + 1;
+                if (c > (int64_t)(64 / cells)) {
+                    ok = false;
+                    break;
+                }
+                first[a] = (int32_t)lower[a];
+                counts[a] = (int)c;
+                cells *= (uint64_t)c;
             }
-            const int64_t c = (int64_t)upper[a] - (int64_t)lower[a] + 1;
-            if (c > (int64_t)(64 / total)) {
-                ok = false;
-                break;
+            unsigned long long k0, k1;
+            if (!ok) {
+                inGrid[i] = 0;
+                overflow[aggregatedAppend(&st->overflowCount)] = i;
+            } else if (!cellKey21(first[0], first[1], first[2], k0) ||
+                       !cellKey21(first[0] + counts[0] - 1, first[1] + counts[1] - 1, first[2] + counts[2] - 1, k1)) {
+                atomicOr(&st->err, kErrHashRange);
+                inGrid[i] = 0;
+            } else {
+                firstCell[i] = make_int4(first[0], first[1], first[2], counts[0] | (counts[1] << 8) | (counts[2] << 16));
+                inGrid[i] = 1;
+                total = (uint32_t)cells;
             }
-            first[a] = (int32_t)lower[a];
-            counts[a] = (int)c;
-            total *= (uint64_t)c;
         }
-        if (!ok) {
-            inGrid[i] = 0;
-            overflow[aggregatedAppend(&st->overflowCount)] = i;
-            continue;
+        uint32_t incl = total;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += t;
         }
-        unsigned long long k0, k1;
-        if (!cellKey21(first[0], first[1], first[2], k0) ||
-            !cellKey21(first[0] + counts[0] - 1, first[1] + counts[1] - 1, first[2] + counts[2] - 1, k1)) {
-            atomicOr(&st->err, kErrHashRange);
-            inGrid[i] = 0;
-            continue;
-        }
-        firstCell[i] = make_int4(first[0], first[1], first[2], counts[0] | (counts[1] << 8) | (counts[2] << 16));
-        inGrid[i] = 1;
-        for (int x = 0; x < counts[0]; ++x)
+        uint32_t wbase = 0;
+        if (lane == 31 && incl) wbase = atomicAdd(&st->gridEntryCount, incl);
+        uint32_t e = __shfl_sync(0xffffffffu, wbase, 31) + incl - total;
+        for (int x = 0; x < counts[0] && total; ++x)
             for (int y = 0; y < counts[1]; ++y)
-                for (int z = 0; z < counts[2]; ++z) {
+                for (int z = 0; z < counts[2]; ++z, ++e) {
+                    if (e >= ecap) continue;  // the host re-runs the step with more entry slots
                     unsigned long long key;
                     cellKey21(first[0] + x, first[1] + y, first[2] + z, key);
-                    atomicAdd(&bucketCount[bucketOf(key, logB)], 1u);
-                }
-    }
-}
-
-// Entries into their buckets: bucketOff[h] advances from the bucket's start to
-// its end, so afterwards bucket h is [bucketOff[h - 1], bucketOff[h]).
-__global__ void k_hgrid_fill(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, uint32_t *bucketOff,
-                             unsigned long long *keys, uint32_t *vals, uint32_t cap, uint32_t logB) {
-    const uint32_t n = *in.d_n;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (!inGrid[i]) continue;
-        const int4 f = firstCell[i];
-        const int cx = f.w & 0xFF, cy = (f.w >> 8) & 0xFF, cz = (f.w >> 16) & 0xFF;
-        for (int x = 0; x < cx; ++x)
-            for (int y = 0; y < cy; ++y)
-                for (int z = 0; z < cz; ++z) {
-                    unsigned long long key;
-                    cellKey21(f.x + x, f.y + y, f.z + z, key);
-                    const uint32_t pos = atomicAdd(&bucketOff[bucketOf(key, logB)], 1u);
-                    if (pos < cap) {
-                        keys[pos] = key;
-                        vals[pos] = i;
-                    }
+                    keys[e] = key;
+                    vals[e] = i;
+                    next[e] = atomicExch(&bucketHead[bucketOf(key, logB)], e);
                 }
     }
 }
@@ -509,8 +515,8 @@ __global__ void k_hgrid_fill(BroadInput in, const int4 *firstCell, const uint8_t
 // Per-body pairs from the buckets (the counterpart of k_grid_body_pairs).
 __global__ void __launch_bounds__(kBodyPairThreads)
 k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const uint32_t *overflow,
-              const uint32_t *bucketOff, uint32_t logB, uint32_t ecap, const unsigned long long *ekeys,
-              const uint32_t *evals, const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen,
+              const uint32_t *bucketHead, uint32_t logB, uint32_t ecap, const unsigned long long *ekeys,
+              const uint32_t *evals, const uint32_t *enext, const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen,
               uint32_t *pairA, uint32_t *pairB, uint32_t cap, DevStats *st, unsigned long long *state,
               uint32_t *counter) {
     __shared__ uint32_t s_tile, s_scan[9], s_prefix;
@@ -534,28 +540,48 @@ k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const
                 if (cnt < kBodyPartners) part[cnt] = b;
                 ++cnt;
             };
+            // The body's cell range is read with its box (unused off the grid).
+            const int4 fa = firstCell[a];
             if (inGrid[a]) {
-                const int4 fa = firstCell[a];
                 const int cx = fa.w & 0xFF, cy = (fa.w >> 8) & 0xFF, cz = (fa.w >> 16) & 0xFF;
-                for (int x = 0; x < cx; ++x)
-                    for (int y = 0; y < cy; ++y)
-                        for (int z = 0; z < cz; ++z) {
-                            unsigned long long key;
-                            cellKey21(fa.x + x, fa.y + y, fa.z + z, key);
-                            const uint32_t h = bucketOf(key, logB);
-                            const uint32_t lo = h ? bucketOff[h - 1] : 0u, hi = bucketOff[h];
-                            for (uint32_t e = lo; e < hi; ++e) {
-                                if (ekeys[e] != key) continue;
-                                const uint32_t b = evals[e];
-                                if (b <= a) continue;
-                                ++cmp;
-                                if (!overlaps(amn, amx, in.mn[b], in.mx[b])) continue;
-                                const int4 fb = firstCell[b];
-                                unsigned long long low;
-                                cellKey21(max(fa.x, fb.x), max(fa.y, fb.y), max(fa.z, fb.z), low);
-                                if (low == key) add(b);
-                            }
+                const int cells = cx * cy * cz;
+                // The list heads of four cells are requested together; then each
+                // list node's key, body and link in one round trip, and a
+                // candidate's box and cell range in one more.  Partners are
+                // sorted afterwards, so the visit order does not matter.  A
+                // list holds at most ecap nodes.
+                for (int c0 = 0; c0 < cells; c0 += 4) {
+                    unsigned long long key[4];
+                    uint32_t head[4];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int c = c0 + j;
+                        key[j] = 0;
+                        head[j] = kNoEntry;
+                        if (c < cells) {
+                            const int z = c % cz, y = (c / cz) % cy, x = c / (cz * cy);
+                            cellKey21(fa.x + x, fa.y + y, fa.z + z, key[j]);
+                            head[j] = bucketHead[bucketOf(key[j], logB)];
                         }
+                    }
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        uint32_t e = head[j];
+                        for (uint32_t hops = 0; e < ecap && hops < ecap; ++hops) {
+                            const unsigned long long k2 = ekeys[e];
+                            const uint32_t b = evals[e];
+                            e = enext[e];
+                            if (k2 != key[j] || b <= a) continue;
+                            ++cmp;
+                            const float4 bmn = in.mn[b], bmx = in.mx[b];
+                            const int4 fb = firstCell[b];
+                            if (!overlaps(amn, amx, bmn, bmx)) continue;
+                            unsigned long long low;
+                            cellKey21(max(fa.x, fb.x), max(fa.y, fb.y), max(fa.z, fb.z), low);
+                            if (low == key[j]) add(b);
+                        }
+                    }
+                }
                 for (uint32_t k = 0; k < F; ++k) {
                     const uint32_t o = overflow[k];
                     if (o > a && overlaps(amn, amx, in.mn[o], in.mx[o])) add(o);
@@ -591,7 +617,10 @@ k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const
         if (cmp) atomicAdd(&st->gridComparisons, cmp);
         uint32_t total;
         const uint32_t local = blockExclusiveScan(kept, total, s_scan);
-        if (threadIdx.x == 0) s_prefix = lookbackExclusive(state, tile, total, &st->err);
+        if (threadIdx.x < 32) {
+            const uint32_t pre = lookbackExclusiveWarp(state, tile, total, &st->err);
+            if (threadIdx.x == 0) s_prefix = pre;
+        }
         __syncthreads();
         uint32_t o = s_prefix + local;
         for (uint32_t j = 0; j < m; ++j) {
@@ -615,8 +644,9 @@ void launchGridBodyPairs(const BroadInput &in, const BroadBuffers &bb, PairBuffe
     PE_CHECK(cudaMemsetAsync(ws.scanState, 0, sizeof(unsigned long long) * (tiles + 1), s));
     const uint32_t grid = tiles < 152u * 8u ? tiles : 152u * 8u;
     if (bb.hashed) {
-        k_hgrid_pairs<<<grid, kBodyPairThreads, 0, s>>>(in, bb.firstCell, bb.inGrid, bb.overflow, bb.bucketOff,
-                                                         bb.logBuckets, bb.entryCap, bb.entryKeys, bb.entryVals, inSlot,
+        k_hgrid_pairs<<<grid, kBodyPairThreads, 0, s>>>(in, bb.firstCell, bb.inGrid, bb.overflow, bb.bucketHead,
+                                                         bb.logBuckets, bb.entryCap, bb.entryKeys, bb.entryVals,
+                                                         bb.entryNext, inSlot,
                                                          cbody, cbgen, pb.a, pb.b, pb.cap, st, ws.scanState,
                                                          (uint32_t *)(ws.scanState + tiles));
         PE_LAUNCHED();
@@ -716,15 +746,12 @@ void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBu
                 cudaStream_t s) {
     uint32_t *err = &st->err;
     if (bb.hashed) {
-        // fixed cell size: count per bucket, scan, fill (pairs: launchGridBodyPairs)
+        // fixed cell size: bucket lists of the covered cells (pairs: launchGridBodyPairs)
         const uint32_t B = 1u << bb.logBuckets;
-        PE_CHECK(cudaMemsetAsync(bb.bucketCount, 0, B * sizeof(uint32_t), s));
-        k_hgrid_count<<<gridFor(in.maxN), 256, 0, s>>>(in, st, bb.firstCell, bb.inGrid, bb.overflow, fixedCell,
-                                                       bb.bucketCount, bb.logBuckets);
-        PE_LAUNCHED();
-        launchScanExclusive(bb.bucketCount, bb.bucketOff, nullptr, B, &st->gridEntryCount, ws, err, s);
-        k_hgrid_fill<<<gridFor(in.maxN), 256, 0, s>>>(in, bb.firstCell, bb.inGrid, bb.bucketOff, bb.entryKeys,
-                                                      bb.entryVals, bb.entryCap, bb.logBuckets);
+        PE_CHECK(cudaMemsetAsync(bb.bucketHead, 0xFF, B * sizeof(uint32_t), s));
+        k_hgrid_insert<<<gridFor(in.maxN), 256, 0, s>>>(in, st, bb.firstCell, bb.inGrid, bb.overflow, fixedCell,
+                                                        (float)(1.0 / fixedCell), bb.bucketHead, bb.logBuckets,
+                                                        bb.entryKeys, bb.entryVals, bb.entryNext, bb.entryCap);
         PE_LAUNCHED();
         return;
     }

@@ -12,7 +12,11 @@
 
 namespace pe {
 
-constexpr int kNarrowThreads = 256;
+// Small tiles spread the few candidate pairs of a step over many SMs: each
+// pair is a long dependent chain of arithmetic, so latency, not issue rate,
+// bounds a tile.
+constexpr int kNarrowThreads = 64;
+static_assert(kNarrowThreads >= (int)kMinLookbackTile, "look-back scratch is sized for kMinLookbackTile");
 
 __global__ void __launch_bounds__(kNarrowThreads)
 k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *__restrict__ pairB,
@@ -44,7 +48,10 @@ k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *_
     }
     uint32_t total;
     const uint32_t local = blockExclusiveScan(hit ? 1u : 0u, total, s_scan);
-    if (threadIdx.x == 0) s_prefix = lookbackExclusive(state, tile, total, &st->err);
+    if (threadIdx.x < 32) {
+        const uint32_t pre = lookbackExclusiveWarp(state, tile, total, &st->err);
+        if (threadIdx.x == 0) s_prefix = pre;
+    }
     __syncthreads();
     const uint32_t m = s_prefix + local;
     if (hit) {

@@ -29,38 +29,52 @@ __device__ __forceinline__ unsigned long long ldvol64(const unsigned long long *
     return *(volatile const unsigned long long *)p;
 }
 
-// Look-back for one 32-bit counter per tile.  state[t] = (flag << 32) | value,
-// flag 1 = tile aggregate, 2 = inclusive prefix.  Returns the exclusive prefix
-// of `tile` and publishes its inclusive prefix.  Called by one thread.
-__device__ __forceinline__ uint32_t lookbackExclusive(unsigned long long *state, uint32_t tile, uint32_t aggregate,
-                                                      uint32_t *err) {
+// Look-back for one 32-bit counter per tile, done by one full warp.
+// state[t] = (flag << 32) | value, flag 1 = tile aggregate, 2 = inclusive
+// prefix.  Publishes the tile's aggregate, then each round reads the states of
+// 32 predecessors at once (lane i: tile - 1 - base - i) and sums them up to the
+// nearest inclusive prefix, so a walk over many finished tiles costs one
+// memory round trip per 32 tiles.  Publishes the tile's inclusive prefix; every
+// lane returns the exclusive prefix.
+__device__ __forceinline__ uint32_t lookbackExclusiveWarp(unsigned long long *state, uint32_t tile,
+                                                          uint32_t aggregate, uint32_t *err) {
+    const uint32_t lane = threadIdx.x & 31;
     if (tile == 0) {
-        atomicExch(&state[0], (2ull << 32) | aggregate);
+        if (lane == 0) atomicExch(&state[0], (2ull << 32) | aggregate);
         return 0;
     }
-    atomicExch(&state[tile], (1ull << 32) | aggregate);
-    uint32_t prefix = 0;
-    int64_t t = (int64_t)tile - 1;
-    uint32_t spins = 0;
-    while (t >= 0) {
-        unsigned long long v = ldvol64(&state[t]);
-        uint32_t flag = (uint32_t)(v >> 32);
-        if (flag == 0) {
+    if (lane == 0) atomicExch(&state[tile], (1ull << 32) | aggregate);
+    uint32_t prefix = 0, spins = 0;
+    int64_t base = (int64_t)tile - 1;
+    while (base >= 0) {
+        const int64_t t = base - (int64_t)lane;
+        // Lanes before tile 0 read as an inclusive prefix of 0.
+        const unsigned long long v = t >= 0 ? ldvol64(&state[t]) : (2ull << 32);
+        const uint32_t flag = (uint32_t)(v >> 32);
+        const uint32_t done = __ballot_sync(0xffffffffu, flag == 2);
+        const uint32_t zero = __ballot_sync(0xffffffffu, flag == 0);
+        const uint32_t first = done & (0u - done);           // nearest inclusive prefix
+        const uint32_t upto = done ? (first << 1) - 1u : 0xffffffffu;
+        if (zero & upto) {
             if (++spins > kSpinLimit) {
-                atomicOr(err, kErrTimeout);
+                if (lane == 0) atomicOr(err, kErrTimeout);
                 break;
             }
             continue;
         }
-        prefix += (uint32_t)v;
-        if (flag == 2) break;
-        --t;
+        uint32_t s = ((upto >> lane) & 1u) ? (uint32_t)v : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        prefix += s;
+        if (done) break;
+        base -= 32;
     }
-    atomicExch(&state[tile], (2ull << 32) | (prefix + aggregate));
+    if (lane == 0) atomicExch(&state[tile], (2ull << 32) | (prefix + aggregate));
     return prefix;
 }
 
-// Block-wide exclusive scan of one value per thread (blockDim.x == 256).
+// Block-wide exclusive scan of one value per thread (blockDim.x a multiple of
+// 32, at most 256).
 __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t &total, uint32_t *smem /*[9]*/) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t incl = v;

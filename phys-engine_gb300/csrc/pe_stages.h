@@ -11,6 +11,10 @@ struct BroadInput {
     uint32_t maxN;        // launch bound
 };
 
+// Fewest items per tile of any single-pass kernel with a tile look-back
+// (scratch holds one state word per tile).
+constexpr uint32_t kMinLookbackTile = 64;
+
 struct BroadBuffers {
     // SAP
     uint32_t *keyTmp32, *valTmp;
@@ -28,8 +32,10 @@ struct BroadBuffers {
     uint32_t entryCap;
     uint32_t keyBits;    // cell-key bits sorted this step (from the previous step's cell range)
     uint32_t *counters;  // [4] device scratch counters
-    // hashed grid (fixed cell size): entries grouped by a hash of the cell
-    uint32_t *bucketCount, *bucketOff;  // [1 << logBuckets]
+    // hashed grid (fixed cell size): per bucket (a hash of the cell key) a list
+    // of entries; entryNext[e] links entry e to the bucket's next entry
+    uint32_t *bucketHead;  // [1 << logBuckets]
+    uint32_t *entryNext;   // [entryCap]
     uint32_t logBuckets;
     bool hashed;
 };

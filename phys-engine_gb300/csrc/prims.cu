@@ -46,7 +46,10 @@ k_scan_exclusive(const uint32_t *in, uint32_t *out, const uint32_t *d_n, uint32_
         }
         uint32_t agg;
         const uint32_t excl = blockExclusiveScan(sum, agg, s_scan);
-        if (threadIdx.x == 0) s_prefix = lookbackExclusive(state, tile, agg, err);
+        if (threadIdx.x < 32) {
+            const uint32_t pre = lookbackExclusiveWarp(state, tile, agg, err);
+            if (threadIdx.x == 0) s_prefix = pre;
+        }
         __syncthreads();
         uint32_t run = s_prefix + excl;
 #pragma unroll

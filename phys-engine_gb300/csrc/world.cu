@@ -257,8 +257,9 @@ void World::push() {
 void World::ensureScratch(uint32_t maxN) {
     if (maxN <= scratchN_ && wsScan_.ptr) return;
     scratchN_ = maxN;
-    // The narrowphase uses 256-item tiles for its look-back.
-    wsScan_.reserve((maxN + 255) / 256 + 16);
+    // Look-back state per tile; the smallest tiles (the narrowphase's) hold
+    // kMinLookbackTile items.
+    wsScan_.reserve((maxN + kMinLookbackTile - 1) / kMinLookbackTile + 16);
     wsSortHist_.reserve(256 * 8 + 64);
     wsSortState_.reserve(scratchBytesSort(maxN) / sizeof(uint32_t) + 16);
     ws_.scanState = wsScan_.ptr;
@@ -308,13 +309,13 @@ void World::ensureCapacity() {
     // hashed grid buckets: a power of two, about two per collider
     uint32_t logB = 10;
     while ((1u << logB) < 2u * nc && logB < 30) ++logB;
-    bbBucketCount_.reserve(1u << logB);
-    bbBucketOff_.reserve(1u << logB);
+    bbBucketHead_.reserve(1u << logB);
+    bbEntryNext_.reserve(entryCap_);
     bb_ = BroadBuffers{bbKeyTmp32_.ptr, bbValTmp_.ptr, bbMinX_.ptr, bbMaxX_.ptr, bbYZ_.ptr, bbIdx_.ptr, bbLen_.ptr,
                        bbOff_.ptr, bbWidth_.ptr, bbWidthTmp_.ptr, bbFirst_.ptr, bbCellCount_.ptr, bbInGrid_.ptr,
                        bbOverflow_.ptr, bbEntryOff_.ptr, bbEntryKeys_.ptr, bbEntryKeysTmp_.ptr, bbEntryVals_.ptr,
-                       bbEntryValsTmp_.ptr, entryCap_, gridKeyBits_, bbCounters_.ptr, bbBucketCount_.ptr,
-                       bbBucketOff_.ptr, logB, false};
+                       bbEntryValsTmp_.ptr, entryCap_, gridKeyBits_, bbCounters_.ptr, bbBucketHead_.ptr,
+                       bbEntryNext_.ptr, logB, false};
 
     if (pairCap_ < 4u * nc) pairCap_ = std::max<uint32_t>(65536, 4u * nc);
     pairKeys_.reserve(pairCap_);

@@ -190,7 +190,7 @@ class World {
     DeviceArray<uint32_t> sapKeys_, sapVals_;
     // broadphase / pairs
     BroadBuffers bb_{};
-    DeviceArray<uint32_t> bbBucketCount_, bbBucketOff_;
+    DeviceArray<uint32_t> bbBucketHead_, bbEntryNext_;
     DeviceArray<uint32_t> bbKeyTmp32_, bbValTmp_, bbIdx_, bbLen_, bbOff_, bbCellCount_, bbOverflow_, bbEntryOff_,
         bbEntryVals_, bbEntryValsTmp_, bbCounters_;
     DeviceArray<float> bbMinX_, bbMaxX_;
