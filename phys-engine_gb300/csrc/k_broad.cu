@@ -333,7 +333,7 @@ k_grid_body_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, c
         const uint32_t a = tile * kBodyPairThreads + threadIdx.x;
         uint32_t part[kBodyPartners];
         uint32_t cnt = 0;
-        unsigned long long cmp = 0;
+        uint32_t cmp = 0;
         if (a < n) {
             const float4 amn = in.mn[a], amx = in.mx[a];
             auto add = [&](uint32_t b) {
@@ -392,11 +392,18 @@ k_grid_body_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, c
             if (cbody && cbody[sa] == cbody[sb] && cbgen[sa] == cbgen[sb]) continue;
             ++kept;
         }
-        if (cnt) {
-            atomicAdd(&st->rawPairs, cnt);  // no duplicates: raw = unique
-            atomicAdd(&st->uniquePairs, cnt);
+        {
+            // one atomic per warp and counter
+            const uint32_t wc = __reduce_add_sync(0xffffffffu, cnt);
+            const uint32_t wm = __reduce_add_sync(0xffffffffu, cmp);
+            if ((threadIdx.x & 31) == 0) {
+                if (wc) {
+                    atomicAdd(&st->rawPairs, wc);  // no duplicates: raw = unique
+                    atomicAdd(&st->uniquePairs, wc);
+                }
+                if (wm) atomicAdd(&st->gridComparisons, (unsigned long long)wm);
+            }
         }
-        if (cmp) atomicAdd(&st->gridComparisons, cmp);
         uint32_t total;
         const uint32_t local = blockExclusiveScan(kept, total, s_scan);
         if (threadIdx.x < 32) {
@@ -444,37 +451,69 @@ constexpr uint32_t kNoEntry = 0xFFFFFFFFu;
 // previous head.  Entry slots come from one counter (a warp scan of the boxes'
 // cell counts, one atomic per warp), so entry order varies from run to run;
 // nothing downstream depends on it (each body sorts its partners).
-__global__ void k_hgrid_insert(BroadInput in, DevStats *st, int4 *firstCell, uint8_t *inGrid, uint32_t *overflow,
-                               double cell, float inv, uint32_t *bucketHead, uint32_t logB,
-                               unsigned long long *keys, uint32_t *vals, uint32_t *next, uint32_t ecap) {
+__device__ __forceinline__ bool cellFloorFast(float x, float invf, int &cellOut) {
+    const float q = x * invf;
+    if (!(fabsf(q) < 1048576.0f)) return false;
+    const float f = floorf(q);
+    const float tol = 1e-6f * fmaxf(1.0f, fabsf(q));
+    if (!(q - f > tol && (f + 1.0f) - q > tol)) return false;
+    cellOut = (int)f;
+    return true;
+}
+
+__global__ void __launch_bounds__(256)
+k_hgrid_insert(BroadInput in, DevStats *st, int4 *firstCell, uint8_t *inGrid, uint32_t *overflow, double cell,
+               float inv, uint32_t *bucketHead, uint32_t logB, unsigned long long *keys, uint32_t *vals,
+               uint32_t *next, uint32_t ecap) {
+    __shared__ uint32_t s_scan[9], s_base;
     const uint32_t n = *in.d_n;
-    const uint32_t lane = threadIdx.x & 31;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->cellSize = cell;
-    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += gridDim.x * blockDim.x) {
-        const uint32_t i = base + lane;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
         uint32_t total = 0;
         int32_t first[3] = {0, 0, 0};
         int counts[3] = {0, 0, 0};
         if (i < n) {
             const float4 mn = in.mn[i], mx = in.mx[i];
-            const double lower[3] = {cellFloor(mn.x, cell, inv), cellFloor(mn.y, cell, inv), cellFloor(mn.z, cell, inv)};
-            const double upper[3] = {cellFloor(mx.x, cell, inv), cellFloor(mx.y, cell, inv), cellFloor(mx.z, cell, inv)};
-            uint64_t cells = 1;
-            bool ok = true;
-            for (int a = 0; a < 3 && ok; ++a) {
-                if (!isfinite(lower[a]) || !isfinite(upper[a]) || lower[a] < -2147483648.0 ||
-                    upper[a] > 2147483647.0 || lower[a] > upper[a]) {
-                    ok = false;
-                    break;
+            int lo[3], hi[3];
+            bool ok = cellFloorFast(mn.x, inv, lo[0]) && cellFloorFast(mn.y, inv, lo[1]) &&
+                      cellFloorFast(mn.z, inv, lo[2]) && cellFloorFast(mx.x, inv, hi[0]) &&
+                      cellFloorFast(mx.y, inv, hi[1]) && cellFloorFast(mx.z, inv, hi[2]);
+            uint32_t cells = 1;
+            if (ok) {
+                // all six floors exact from the float products (|cell| < 2^20)
+                for (int a2 = 0; a2 < 3 && ok; ++a2) {
+                    const int c = hi[a2] - lo[a2] + 1;
+                    if (lo[a2] > hi[a2] || c > (int)(64 / cells)) {
+                        ok = false;
+                        break;
+                    }
+                    first[a2] = lo[a2];
+                    counts[a2] = c;
+                    cells *= (uint32_t)c;
                 }
-                const int64_t c = (int64_t)upper[a] - (int64_t)lower[a] + 1;
-                if (c > (int64_t)(64 / cells)) {
-                    ok = false;
-                    break;
+            } else {
+                // gridRange in double (broadphase.cpp:62-88)
+                const double lower[3] = {cellFloor(mn.x, cell, inv), cellFloor(mn.y, cell, inv),
+                                         cellFloor(mn.z, cell, inv)};
+                const double upper[3] = {cellFloor(mx.x, cell, inv), cellFloor(mx.y, cell, inv),
+                                         cellFloor(mx.z, cell, inv)};
+                ok = true;
+                for (int a2 = 0; a2 < 3 && ok; ++a2) {
+                    if (!isfinite(lower[a2]) || !isfinite(upper[a2]) || lower[a2] < -2147483648.0 ||
+                        upper[a2] > 2147483647.0 || lower[a2] > upper[a2]) {
+                        ok = false;
+                        break;
+                    }
+                    const int64_t c = (int64_t)upper[a2] - (int64_t)lower[a2] + 1;
+                    if (c > (int64_t)(64 / cells)) {
+                        ok = false;
+                        break;
+                    }
+                    first[a2] = (int32_t)lower[a2];
+                    counts[a2] = (int)c;
+                    cells *= (uint32_t)c;
                 }
-                first[a] = (int32_t)lower[a];
-                counts[a] = (int)c;
-                cells *= (uint64_t)c;
             }
             unsigned long long k0, k1;
             if (!ok) {
@@ -487,18 +526,16 @@ __global__ void k_hgrid_insert(BroadInput in, DevStats *st, int4 *firstCell, uin
             } else {
                 firstCell[i] = make_int4(first[0], first[1], first[2], counts[0] | (counts[1] << 8) | (counts[2] << 16));
                 inGrid[i] = 1;
-                total = (uint32_t)cells;
+                total = cells;
             }
         }
-        uint32_t incl = total;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= (uint32_t)o) incl += t;
-        }
-        uint32_t wbase = 0;
-        if (lane == 31 && incl) wbase = atomicAdd(&st->gridEntryCount, incl);
-        uint32_t e = __shfl_sync(0xffffffffu, wbase, 31) + incl - total;
+        // entry slots: block scan of the cell counts, one atomic per block
+        uint32_t blockTotal;
+        const uint32_t local = blockExclusiveScan(total, blockTotal, s_scan);
+        if (threadIdx.x == 0) s_base = blockTotal ? atomicAdd(&st->gridEntryCount, blockTotal) : 0u;
+        __syncthreads();
+        uint32_t e = s_base + local;
+        __syncthreads();
         for (int x = 0; x < counts[0] && total; ++x)
             for (int y = 0; y < counts[1]; ++y)
                 for (int z = 0; z < counts[2]; ++z, ++e) {
@@ -533,7 +570,7 @@ k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const
         const uint32_t a = tile * kBodyPairThreads + threadIdx.x;
         uint32_t part[kBodyPartners];
         uint32_t cnt = 0;
-        unsigned long long cmp = 0;
+        uint32_t cmp = 0;
         if (a < n) {
             const float4 amn = in.mn[a], amx = in.mx[a];
             auto add = [&](uint32_t b) {
@@ -550,18 +587,24 @@ k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const
                 // candidate's box and cell range in one more.  Partners are
                 // sorted afterwards, so the visit order does not matter.  A
                 // list holds at most ecap nodes.
+                int x = 0, y = 0, z = 0;  // next cell, z fastest
                 for (int c0 = 0; c0 < cells; c0 += 4) {
                     unsigned long long key[4];
                     uint32_t head[4];
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
-                        const int c = c0 + j;
                         key[j] = 0;
                         head[j] = kNoEntry;
-                        if (c < cells) {
-                            const int z = c % cz, y = (c / cz) % cy, x = c / (cz * cy);
+                        if (c0 + j < cells) {
                             cellKey21(fa.x + x, fa.y + y, fa.z + z, key[j]);
                             head[j] = bucketHead[bucketOf(key[j], logB)];
+                            if (++z == cz) {
+                                z = 0;
+                                if (++y == cy) {
+                                    y = 0;
+                                    ++x;
+                                }
+                            }
                         }
                     }
 #pragma unroll
@@ -610,11 +653,18 @@ k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const
             if (cbody && cbody[sa] == cbody[sb] && cbgen[sa] == cbgen[sb]) continue;
             ++kept;
         }
-        if (cnt) {
-            atomicAdd(&st->rawPairs, cnt);
-            atomicAdd(&st->uniquePairs, cnt);
+        {
+            // one atomic per warp and counter
+            const uint32_t wc = __reduce_add_sync(0xffffffffu, cnt);
+            const uint32_t wm = __reduce_add_sync(0xffffffffu, cmp);
+            if ((threadIdx.x & 31) == 0) {
+                if (wc) {
+                    atomicAdd(&st->rawPairs, wc);  // no duplicates: raw = unique
+                    atomicAdd(&st->uniquePairs, wc);
+                }
+                if (wm) atomicAdd(&st->gridComparisons, (unsigned long long)wm);
+            }
         }
-        if (cmp) atomicAdd(&st->gridComparisons, cmp);
         uint32_t total;
         const uint32_t local = blockExclusiveScan(kept, total, s_scan);
         if (threadIdx.x < 32) {
