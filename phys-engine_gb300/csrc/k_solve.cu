@@ -106,8 +106,23 @@ __global__ void k_order_init(SolveArgs a, int serial) {
     }
 }
 
-__global__ void k_prepare(SolveArgs a) {
-    prepareRange(a, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, min(a.st->manifolds, a.mcap));
+// Prepare of every manifold, by manifold index, before the colouring, and the
+// manifold flags (sb.dyn) the single-block front reads.  The old cache's keys
+// are copied to shared memory when at most keyCap of them.
+constexpr int kPrepareThreads = 64;
+constexpr uint32_t kPrepareKeyCap = 4096;
+__global__ void __launch_bounds__(kPrepareThreads) k_prepare(SolveArgs a, uint32_t keyCap) {
+    extern __shared__ unsigned long long s_keys[];
+    const uint32_t M = min(a.st->manifolds, a.mcap);
+    for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x)
+        a.sb.dyn[m] = manifoldFlags(a, m);
+    const uint32_t cacheN = *a.oldCount;
+    const bool inShared = cacheN <= keyCap;
+    if (inShared)
+        for (uint32_t i = threadIdx.x; i < cacheN; i += blockDim.x) s_keys[i] = a.oldCache.key[i];
+    __syncthreads();
+    prepareRange(a, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, min(a.st->manifolds, a.mcap),
+                 inShared ? s_keys : nullptr);
 }
 
 __global__ void __launch_bounds__(kSolveThreads) k_solve_colored(SolveArgs a) {
@@ -124,12 +139,12 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve_colored(SolveArgs a) {
     __syncthreads();
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
     for (uint32_t c = 0; c < C; ++c) {
-        for (uint32_t k = s_start[c] + gtid; k < s_start[c + 1]; k += gstride) warmStartOne(a, k);
+        for (uint32_t k = s_start[c] + gtid; k < s_start[c + 1]; k += gstride) warmStartOne(a, k, a.sb.order[k]);
         gridBarrier(a.sb.bar, &a.st->err);
     }
     for (int it = 0; it < a.iterations; ++it)
         for (uint32_t c = 0; c < C; ++c) {
-            for (uint32_t k = s_start[c] + gtid; k < s_start[c + 1]; k += gstride) solveOne(a, k);
+            for (uint32_t k = s_start[c] + gtid; k < s_start[c + 1]; k += gstride) solveOne(a, k, a.sb.order[k]);
             gridBarrier(a.sb.bar, &a.st->err);
         }
 }
@@ -138,18 +153,17 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve_colored(SolveArgs a) {
 __global__ void k_solve_serial(SolveArgs a) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     const uint32_t M = min(a.st->manifolds, a.mcap);
-    for (uint32_t k = 0; k < M; ++k) warmStartOne(a, k);
+    for (uint32_t k = 0; k < M; ++k) warmStartOne(a, k, k);
     for (int it = 0; it < a.iterations; ++it)
-        for (uint32_t k = 0; k < M; ++k) solveOne(a, k);
+        for (uint32_t k = 0; k < M; ++k) solveOne(a, k, k);
 }
 
 // Solved impulses back to the manifolds (pair order).
 __global__ void k_impulses_out(SolveArgs a) {
     const uint32_t M = min(a.st->manifolds, a.mcap);
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < M; k += gridDim.x * blockDim.x) {
-        const uint32_t m = a.sb.order[k];
+    for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
         for (uint32_t p = 0; p < 4; ++p) {
-            float4 imp = a.sb.pimp[(size_t)p * a.mcap + k];
+            float4 imp = a.sb.pimp[(size_t)p * a.mcap + m];
             imp.w = 0.0f;
             a.mv.impulse[4 * m + p] = imp;
         }
@@ -199,6 +213,7 @@ constexpr size_t blockSolveSmem(uint32_t blockM, uint32_t stageSlots) {
 __global__ void __launch_bounds__(kBlockSolveThreads)
 k_solve_block(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount, int serial, uint32_t blockM,
               uint32_t stageSlots) {
+    // The manifolds were prepared by k_prepare, launched before this kernel.
     // blockM u64 sort keys, u32 flags, uint2 stage slots; then the staged
     // velocities (2 float4 per slot) and the body of each slot.
     extern __shared__ unsigned long long s_sort[];
@@ -210,7 +225,7 @@ k_solve_block(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount, 
     vs.slotBody = reinterpret_cast<uint32_t *>(base + (size_t)blockM * 20 + (size_t)stageSlots * 32);
     vs.cap = stageSlots;
     solveBlock(a, nc, cacheCap, newCount, serial, blockM, s_sort, reinterpret_cast<uint32_t *>(s_sort + blockM), sh,
-               stageSlots ? &vs : nullptr);
+               stageSlots ? &vs : nullptr, true);
 }
 
 static int gridFor(uint32_t n, int threads = 256, int maxBlocks = 152 * 8) {
@@ -266,7 +281,11 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
             while (bm < blockM) bm <<= 1;
         }
         uint32_t slots = 2 * bm < kStageSlots ? 2 * bm : kStageSlots;
+        if (orderMode != 0 && launchSolverCluster(a, newCache, newCacheCount, cacheCap, bm, slots, s)) return;
         const size_t smem = blockSolveSmem(bm, slots);
+        k_prepare<<<(bm + kPrepareThreads - 1) / kPrepareThreads, kPrepareThreads,
+                    kPrepareKeyCap * sizeof(unsigned long long), s>>>(a, kPrepareKeyCap);
+        PE_LAUNCHED();
         k_solve_block<<<1, kBlockSolveThreads, smem, s>>>(a, newCache, cacheCap, newCacheCount, orderMode == 0 ? 1 : 0,
                                                           bm, slots);
         PE_LAUNCHED();
@@ -281,7 +300,8 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
     if (!serial)
         launchRadixSort<uint32_t>(sb.orderKeys, sb.orderKeysTmp, sb.order, sb.orderTmp, &st->manifolds, mcap, 0, 8,
                                   ws, err, s);
-    k_prepare<<<gridFor(mcap), 256, 0, s>>>(a);
+    k_prepare<<<gridFor(mcap, kPrepareThreads), kPrepareThreads, kPrepareKeyCap * sizeof(unsigned long long), s>>>(
+        a, kPrepareKeyCap);
     PE_LAUNCHED();
     if (serial) {
         k_solve_serial<<<1, 32, 0, s>>>(a);

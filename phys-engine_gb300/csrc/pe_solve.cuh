@@ -45,7 +45,7 @@ struct SolveArgs {
 // arrays by body index, or shared-memory copies by staging slot.
 struct GlobalVel {
     const SolveArgs &a;
-    __device__ __forceinline__ uint2 bodies(uint32_t k) const { return a.sb.pbody[k]; }
+    __device__ __forceinline__ uint2 bodies(uint32_t, uint32_t m) const { return a.sb.pbody[m]; }
     __device__ __forceinline__ V3 lin(uint32_t b) const { return f4xyz(ld4(&a.w.nxt.lin[b])); }
     __device__ __forceinline__ V3 ang(uint32_t b) const { return f4xyz(ld4(&a.w.nxt.ang[b])); }
     __device__ __forceinline__ void store(uint32_t b, const V3 &l, const V3 &w) const {
@@ -56,7 +56,7 @@ struct GlobalVel {
 struct SharedVel {
     float4 *v;          // slot s: lin at 2s, ang at 2s + 1
     const uint2 *slot;  // per solve index k: slots of body A and body B
-    __device__ __forceinline__ uint2 bodies(uint32_t k) const { return slot[k]; }
+    __device__ __forceinline__ uint2 bodies(uint32_t k, uint32_t) const { return slot[k]; }
     __device__ __forceinline__ V3 lin(uint32_t s) const { return f4xyz(v[2 * s]); }
     __device__ __forceinline__ V3 ang(uint32_t s) const { return f4xyz(v[2 * s + 1]); }
     __device__ __forceinline__ void store(uint32_t s, const V3 &l, const V3 &w) const {
@@ -86,9 +86,10 @@ constexpr uint32_t kSlotFree = 0xFFFFFFFFu;
 
 // --------------------------------------------------------------- prepare ---
 // prepareBody (:275-287) + prepareContactPoints (:101-214) + the cache lookup
-// of warmStartPrepared (:448-490).  Data are written in solve order k.
-// cacheKeys: the old cache's keys (a shared-memory copy in the single-block
-// path; the global array otherwise).
+// of warmStartPrepared (:448-490).  Data are written by manifold index m (no
+// dependence on the solve order, so prepare may run before the colouring).
+// cacheKeys: the old cache's keys (a shared-memory copy when they fit; the
+// global array otherwise).
 __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t stride, uint32_t M,
                                     const unsigned long long *cacheKeys = nullptr) {
     if (!cacheKeys) cacheKeys = a.oldCache.key;
@@ -97,8 +98,8 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
     const float inverseDt = 1.0f / smax(w.dt, 1e-6f);
     const uint32_t cacheN = *a.oldCount;
     uint64_t prepared = 0, comparisons = 0, matches = 0;
-    for (uint32_t k = begin; k < M; k += stride) {
-        const uint32_t m = a.sb.order[k];
+    for (uint32_t m = begin; m < M; m += stride) {
+        const uint32_t k = m;  // data index
         const uint32_t ia = a.mv.bodyA[m], ib = a.mv.bodyB[m];
         const float4 nf = a.mv.normalFriction[m];
         const V3 n{nf.x, nf.y, nf.z};
@@ -240,35 +241,54 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
 
 
 // ---------------------------------------------------------- solve sweeps ---
-struct BodyVel {
-    V3 lin, ang;
+// Where the sweeps read a manifold's prepared data: the solver arrays by
+// manifold index (GlobalPrep), or shared-memory copies by a local index.
+struct GlobalPrep {
+    const SolveArgs &a;
+    __device__ __forceinline__ float4 pm(uint32_t i) const { return a.sb.pm[i]; }
+    __device__ __forceinline__ float4 pn(uint32_t i) const { return a.sb.pn[i]; }
+    __device__ __forceinline__ uint32_t count(uint32_t i) const { return a.sb.pcount[i]; }
+    __device__ __forceinline__ float4 inertia(int r, uint32_t i) const { return a.sb.pmInertia[(size_t)r * a.mcap + i]; }
+    __device__ __forceinline__ float4 pt(int v, uint32_t p, uint32_t i) const {
+        return a.sb.pp[(size_t)(v * 4 + p) * a.mcap + i];
+    }
+    __device__ __forceinline__ float4 imp(uint32_t p, uint32_t i) const { return a.sb.pimp[(size_t)p * a.mcap + i]; }
+    __device__ __forceinline__ void setImp(uint32_t p, uint32_t i, const float4 &v) const {
+        a.sb.pimp[(size_t)p * a.mcap + i] = v;
+    }
 };
 
-template <class Vel> __device__ __forceinline__ void warmStartOne(const SolveArgs &a, uint32_t k, const Vel &vel) {
-    const uint32_t mcap = a.mcap;
-    const uint2 bi = vel.bodies(k);
-    const float4 pm = a.sb.pm[k];
+// Warm start of one manifold (warmStartPrepared's application, :491-517).  k:
+// solve index (velocity slots), i: data index (prepared data).  Point 0's data
+// are requested together with the manifold's, so a one-point manifold costs
+// one memory round trip.
+template <class Prep, class Vel>
+__device__ __forceinline__ void warmStartOne(const Prep &pr, uint32_t k, uint32_t i, const Vel &vel) {
+    const uint2 bi = vel.bodies(k, i);
+    const float4 pm = pr.pm(i);
+    const float4 nf = pr.pn(i);
+    const uint32_t npts = pr.count(i);
+    float4 r[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) r[j] = pr.inertia(j, i);
+    float4 imp = pr.imp(0, i);
+    float4 offA4 = pr.pt(0, 0, i), offB4 = pr.pt(1, 0, i), t14 = pr.pt(2, 0, i), t24 = pr.pt(3, 0, i);
     const bool sA = pm.y != 0.0f, sB = pm.w != 0.0f;
-    const float4 nf = a.sb.pn[k];
     const V3 n{nf.x, nf.y, nf.z};
-    const uint32_t npts = a.sb.pcount[k];
-    M3 IA, IB;
-    {
-        float4 r0 = a.sb.pmInertia[0 * mcap + k], r1 = a.sb.pmInertia[1 * mcap + k], r2 = a.sb.pmInertia[2 * mcap + k];
-        IA = M3{r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
-        r0 = a.sb.pmInertia[3 * mcap + k], r1 = a.sb.pmInertia[4 * mcap + k], r2 = a.sb.pmInertia[5 * mcap + k];
-        IB = M3{r0.x, r0.y, r0.z, r1.x, r1.y, r1.z, r2.x, r2.y, r2.z};
-    }
+    const M3 IA{r[0].x, r[0].y, r[0].z, r[1].x, r[1].y, r[1].z, r[2].x, r[2].y, r[2].z};
+    const M3 IB{r[3].x, r[3].y, r[3].z, r[4].x, r[4].y, r[4].z, r[5].x, r[5].y, r[5].z};
     V3 linA = vel.lin(bi.x), angA = vel.ang(bi.x);
     V3 linB = vel.lin(bi.y), angB = vel.ang(bi.y);
     bool any = false;
     for (uint32_t p = 0; p < npts; ++p) {
-        const float4 imp = a.sb.pimp[(size_t)p * mcap + k];
+        if (p > 0) {
+            imp = pr.imp(p, i);
+            offA4 = pr.pt(0, p, i);
+            offB4 = pr.pt(1, p, i);
+            t14 = pr.pt(2, p, i);
+            t24 = pr.pt(3, p, i);
+        }
         if (imp.w == 0.0f) continue;
-        const float4 offA4 = a.sb.pp[(size_t)(0 * 4 + p) * mcap + k];
-        const float4 offB4 = a.sb.pp[(size_t)(1 * 4 + p) * mcap + k];
-        const float4 t14 = a.sb.pp[(size_t)(2 * 4 + p) * mcap + k];
-        const float4 t24 = a.sb.pp[(size_t)(3 * 4 + p) * mcap + k];
         V3 wi = n * imp.x + f4xyz(t14) * imp.y + f4xyz(t24) * imp.z;
         V3 nw = -wi;
         if (!sA) {
@@ -285,37 +305,40 @@ template <class Vel> __device__ __forceinline__ void warmStartOne(const SolveArg
     if (!sA) vel.store(bi.x, linA, angA);
     if (!sB) vel.store(bi.y, linB, angB);
 }
-__device__ __forceinline__ void warmStartOne(const SolveArgs &a, uint32_t k) { warmStartOne(a, k, GlobalVel{a}); }
+template <class Vel> __device__ __forceinline__ void warmStartOne(const SolveArgs &a, uint32_t k, uint32_t m, const Vel &vel) {
+    warmStartOne(GlobalPrep{a}, k, m, vel);
+}
+__device__ __forceinline__ void warmStartOne(const SolveArgs &a, uint32_t k, uint32_t m) {
+    warmStartOne(GlobalPrep{a}, k, m, GlobalVel{a});
+}
 
-// solvePrepared (:520-603) for one manifold.
-template <class Vel> __device__ __forceinline__ void solveOne(const SolveArgs &a, uint32_t k, const Vel &vel) {
-    const uint32_t mcap = a.mcap;
-    const uint2 bi = vel.bodies(k);
-    const float4 pm = a.sb.pm[k];
+// solvePrepared (:520-603) for one manifold; k, i as for warmStartOne.
+template <class Prep, class Vel>
+__device__ __forceinline__ void solveOne(const Prep &pr, uint32_t k, uint32_t i, const Vel &vel) {
+    const uint2 bi = vel.bodies(k, i);
+    const float4 pm = pr.pm(i);
+    const float4 nf = pr.pn(i);
+    const uint32_t npts = pr.count(i);
+    // Point 0's constants come with the manifold's (one memory round trip);
+    // further points load theirs in turn.
+    float4 o[10];
+#pragma unroll
+    for (int v = 0; v < 10; ++v) o[v] = pr.pt(v, 0, i);
+    float4 imp = pr.imp(0, i);
     const bool sA = pm.y != 0.0f, sB = pm.w != 0.0f;
-    const float4 nf = a.sb.pn[k];
     const V3 n{nf.x, nf.y, nf.z};
     const float friction = nf.w;
-    const uint32_t npts = a.sb.pcount[k];
     V3 linA = vel.lin(bi.x), angA = vel.ang(bi.x);
     V3 linB = vel.lin(bi.y), angB = vel.ang(bi.y);
     for (uint32_t p = 0; p < npts; ++p) {
-        // All of the point's constants are requested at once (one memory round
-        // trip); points with no effective mass are skipped after the loads.
-        const float4 o0 = a.sb.pp[(size_t)(0 * 4 + p) * mcap + k];
-        const float4 o1 = a.sb.pp[(size_t)(1 * 4 + p) * mcap + k];
-        const float4 o2 = a.sb.pp[(size_t)(2 * 4 + p) * mcap + k];
-        const float4 o3 = a.sb.pp[(size_t)(3 * 4 + p) * mcap + k];
-        const float4 o4 = a.sb.pp[(size_t)(4 * 4 + p) * mcap + k];
-        const float4 o5 = a.sb.pp[(size_t)(5 * 4 + p) * mcap + k];
-        const float4 o6 = a.sb.pp[(size_t)(6 * 4 + p) * mcap + k];
-        const float4 o7 = a.sb.pp[(size_t)(7 * 4 + p) * mcap + k];
-        const float4 o8 = a.sb.pp[(size_t)(8 * 4 + p) * mcap + k];
-        const float4 o9 = a.sb.pp[(size_t)(9 * 4 + p) * mcap + k];
-        float4 imp = a.sb.pimp[(size_t)p * mcap + k];
-        if (o0.w <= 0.0f) continue;  // inverseEffectiveMass <= 0
-        const V3 offA = f4xyz(o0), offB = f4xyz(o1), t1 = f4xyz(o2), t2 = f4xyz(o3);
-        const float iem = o0.w, bias = o1.w, rv = o2.w, itm00 = o3.w, itm01 = o4.w, itm11 = o5.w;
+        if (p > 0) {
+#pragma unroll
+            for (int v = 0; v < 10; ++v) o[v] = pr.pt(v, p, i);
+            imp = pr.imp(p, i);
+        }
+        if (o[0].w <= 0.0f) continue;  // inverseEffectiveMass <= 0
+        const V3 offA = f4xyz(o[0]), offB = f4xyz(o[1]), t1 = f4xyz(o[2]), t2 = f4xyz(o[3]);
+        const float iem = o[0].w, bias = o[1].w, rv = o[2].w, itm00 = o[3].w, itm01 = o[4].w, itm11 = o[5].w;
         const V3 vA = linA + cross(angA, offA);
         const V3 vB = linB + cross(angB, offB);
         const V3 rel = vB - vA;
@@ -327,17 +350,17 @@ template <class Vel> __device__ __forceinline__ void solveOne(const SolveArgs &a
         V3 impulse = n * applied;
         if (!sA) {
             linA += (-impulse) * pm.x;
-            angA += f4xyz(o4) * (-applied);
+            angA += f4xyz(o[4]) * (-applied);
         }
         if (!sB) {
             linB += impulse * pm.z;
-            angB += f4xyz(o5) * applied;
+            angB += f4xyz(o[5]) * applied;
         }
         if (itm00 <= 0.0f || itm11 <= 0.0f) {
-            a.sb.pimp[(size_t)p * mcap + k] = imp;
+            pr.setImp(p, i, imp);
             continue;
         }
-        const float ntr1 = o6.w, ntr2 = o7.w;
+        const float ntr1 = o[6].w, ntr2 = o[7].w;
         float limit = smax(friction, 0.0f) * imp.x;
         float tv1 = dot(rel, t1) + ntr1 * applied;
         float tv2 = dot(rel, t2) + ntr2 * applied;
@@ -348,14 +371,14 @@ template <class Vel> __device__ __forceinline__ void solveOne(const SolveArgs &a
         imp.z += d2;
         float lsq = imp.y * imp.y + imp.z * imp.z;
         if (lsq > limit * limit) {
-            float s = limit / sqrtf(lsq);
-            imp.y *= s;
-            imp.z *= s;
+            float sc = limit / sqrtf(lsq);
+            imp.y *= sc;
+            imp.z *= sc;
         }
         float a1 = imp.y - p1, a2 = imp.z - p2;
         V3 ti = t1 * a1 + t2 * a2;
-        V3 rA = f4xyz(o6) * a1 + f4xyz(o8) * a2;
-        V3 rB = f4xyz(o7) * a1 + f4xyz(o9) * a2;
+        V3 rA = f4xyz(o[6]) * a1 + f4xyz(o[8]) * a2;
+        V3 rB = f4xyz(o[7]) * a1 + f4xyz(o[9]) * a2;
         if (!sA) {
             linA += (-ti) * pm.x;
             angA += -rA;
@@ -364,12 +387,17 @@ template <class Vel> __device__ __forceinline__ void solveOne(const SolveArgs &a
             linB += ti * pm.z;
             angB += rB;
         }
-        a.sb.pimp[(size_t)p * mcap + k] = imp;
+        pr.setImp(p, i, imp);
     }
     if (!sA) vel.store(bi.x, linA, angA);
     if (!sB) vel.store(bi.y, linB, angB);
 }
-__device__ __forceinline__ void solveOne(const SolveArgs &a, uint32_t k) { solveOne(a, k, GlobalVel{a}); }
+template <class Vel> __device__ __forceinline__ void solveOne(const SolveArgs &a, uint32_t k, uint32_t m, const Vel &vel) {
+    solveOne(GlobalPrep{a}, k, m, vel);
+}
+__device__ __forceinline__ void solveOne(const SolveArgs &a, uint32_t k, uint32_t m) {
+    solveOne(GlobalPrep{a}, k, m, GlobalVel{a});
+}
 
 // Cooperative sweep: warm start, then `iterations` sweeps, each colour by colour
 // with a grid barrier between colours.
@@ -382,7 +410,7 @@ __device__ __forceinline__ void cacheWriteManifold(const SolveArgs &a, const Cac
         const uint32_t e = base + p;
         if (e >= cacheCap) break;
         const float4 aa = a.mv.anchorA[4 * m + p], ab = a.mv.anchorB[4 * m + p];
-        const float4 imp = a.mv.impulse[4 * m + p];
+        const float4 imp = __ldcg(&a.mv.impulse[4 * m + p]);  // may come from other SMs of a cluster
         nc.key[e] = key;
         nc.gens[e] = gens;
         nc.anchorA[e] = make_float4(aa.x, aa.y, aa.z, imp.x);
@@ -400,42 +428,52 @@ __device__ __forceinline__ bool manifoldBodiesValid(const SolveArgs &a, uint32_t
            w.bgen[ia] == a.mv.genA[m] && w.bgen[ib] == a.mv.genB[m];
 }
 
-// ------------------------------------------------------ single-block path ---
-// The whole solver for up to kBlockMaxManifolds manifolds in one thread block:
-// the same colouring, order, prepare, sweeps and cache rebuild as the
-// multi-kernel path, separated by __syncthreads instead of kernel boundaries
-// and grid barriers.  If the live manifold count exceeds the block capacity the
-// kernel only flags kErrSmallPath; the step is then re-run on the multi-kernel
-// path.
-// s_sort holds maxM u64 and s_dyn maxM u32 (shared memory); sh the small
-// shared arrays.  All threads of the block call it.
-__device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint32_t cacheCap, uint32_t *newCount, int serial,
-                           uint32_t maxM, unsigned long long *s_sort, uint32_t *s_dyn, BlockSolveShared &sh,
-                           const VelStage *vs = nullptr) {
+// Per-manifold body flags: bit 0 / bit 1 body A / B live, of the manifold's
+// generation and dynamic (the colouring's "dynamic side"); bit 2 both handles
+// live (the manifold is solved).
+constexpr uint32_t kFlagDynA = 1u, kFlagDynB = 2u, kFlagValid = 4u;
+__device__ __forceinline__ uint32_t manifoldFlags(const SolveArgs &a, uint32_t m) {
+    const uint32_t ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
+    const WorldView &w = a.w;
+    const bool okA = ba < w.nb && (w.bflags[ba] & kBodyAlive) && w.bgen[ba] == a.mv.genA[m];
+    const bool okB = bb < w.nb && (w.bflags[bb] & kBodyAlive) && w.bgen[bb] == a.mv.genB[m];
+    return (okA && !(w.bflags[ba] & kBodyStatic) ? kFlagDynA : 0u) |
+           (okB && !(w.bflags[bb] & kBodyStatic) ? kFlagDynB : 0u) | (okA && okB ? kFlagValid : 0u);
+}
+
+// Front of the single-block solver: staging slots, colouring and the solve
+// order.  Afterwards sb.order and s_dyn map solve index k to manifold m (colour
+// path; the reference order is the identity), sh.start / sh.colors hold the
+// colour ranges and, when it returns true, vs->slot[k] the staging slots of
+// solve index k's bodies and vs->slotBody / sh.slots the staged bodies.
+// mflags: manifoldFlags of every manifold, written by an earlier launch or
+// cluster rank (nullptr: computed here).
+__device__ inline bool solveBlockFront(const SolveArgs &a, uint32_t M, int serial, uint32_t maxM,
+                                       unsigned long long *s_sort, uint32_t *s_dyn, BlockSolveShared &sh,
+                                       const VelStage *vs, const uint32_t *mflags = nullptr) {
     uint32_t *s_start = sh.start, *s_count = sh.count, *s_scan = sh.scan;
     uint32_t &s_colored = sh.colored, &s_colors = sh.colors;
-    const uint32_t M = min(a.st->manifolds, a.mcap);
-    if (M > maxM) {
-        if (threadIdx.x == 0) atomicOr(&a.st->err, kErrSmallPath);
-        return;
-    }
     const WorldView &w = a.w;
     const SolverBuffers &sb = a.sb;
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
-    uint32_t C = 0;
     bool slotted = false;  // bodies got staging slots (colour path with a VelStage)
     if (serial) {
         for (uint32_t k = tid; k < M; k += nt) sb.order[k] = k;
         __syncthreads();
     } else {
+        // --- body flags of every manifold (s_dyn until the placement) ---
+        for (uint32_t m = tid; m < M; m += nt) s_dyn[m] = mflags ? __ldcg(&mflags[m]) : manifoldFlags(a, m);
+        __syncthreads();
         // --- staging slots for the bodies of valid manifolds, assigned through a
         // shared-memory hash table (in the velocity area, free until the
         // colouring); the colouring's per-body arrays and, after prepare, the
         // staged velocities use them ---
         if (vs) {
             uint32_t *tkey = reinterpret_cast<uint32_t *>(vs->v);
-            uint32_t T = 1;
-            while (2 * T <= 4 * vs->cap) T <<= 1;  // key + value words fit the 8 words per slot
+            // at most 2M keys: a table of >= 4M entries (load <= 1/2) where the
+            // key and value words fit the velocity area's 8 words per slot
+            uint32_t T = 32;
+            while (T < 4 * M && 2 * T <= 4 * vs->cap) T <<= 1;
             uint32_t *tval = tkey + T;
             for (uint32_t i = tid; i < T; i += nt) tkey[i] = kSlotFree;
             if (tid == 0) {
@@ -444,7 +482,7 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
             }
             __syncthreads();
             for (uint32_t m = tid; m < M; m += nt) {
-                if (!manifoldBodiesValid(a, m)) continue;
+                if (!(s_dyn[m] & kFlagValid)) continue;
                 const uint32_t b2[2] = {a.mv.bodyA[m], a.mv.bodyB[m]};
                 for (int j = 0; j < 2; ++j) {
                     uint32_t h = (b2[j] * 2654435761u) & (T - 1), probes = 0;
@@ -459,10 +497,15 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
                 }
             }
             __syncthreads();
-            for (uint32_t i = tid; i < T; i += nt) {
+            for (uint32_t i = tid; i < T; i += nt) {  // T is a multiple of 32: whole warps
                 const uint32_t key = tkey[i];
+                const uint32_t lane = tid & 31;
+                const uint32_t used = __ballot_sync(0xffffffffu, key != kSlotFree);
+                uint32_t base = 0;
+                if (lane == 0 && used) base = atomicAdd(&sh.slots, (uint32_t)__popc(used));
+                base = __shfl_sync(0xffffffffu, base, 0);
                 if (key == kSlotFree) continue;
-                const uint32_t sl = atomicAdd(&sh.slots, 1u);
+                const uint32_t sl = base + __popc(used & ((1u << lane) - 1u));
                 tval[i] = sl;
                 if (sl < vs->cap) vs->slotBody[sl] = key;
             }
@@ -475,8 +518,8 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
                     return tval[h];
                 };
                 for (uint32_t m = tid; m < M; m += nt)
-                    vs->slot[m] = manifoldBodiesValid(a, m) ? make_uint2(find(a.mv.bodyA[m]), find(a.mv.bodyB[m]))
-                                                            : make_uint2(0u, 0u);
+                    vs->slot[m] = (s_dyn[m] & kFlagValid) ? make_uint2(find(a.mv.bodyA[m]), find(a.mv.bodyB[m]))
+                                                          : make_uint2(0u, 0u);
                 __syncthreads();  // the colouring arrays below overwrite the table
                 unsigned long long *best = reinterpret_cast<unsigned long long *>(vs->v);
                 for (uint32_t sl = tid; sl < 3 * sh.slots; sl += nt) best[sl < sh.slots ? sl : vs->cap + (sl - sh.slots)] = 0ull;
@@ -506,12 +549,11 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
         };
         uint32_t *s_color = reinterpret_cast<uint32_t *>(s_sort);  // reused before the order sort
         for (uint32_t m = tid; m < M; m += nt) {
-            uint32_t ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
-            bool da = ba < w.nb && (w.bflags[ba] & kBodyAlive) && w.bgen[ba] == a.mv.genA[m] && !(w.bflags[ba] & kBodyStatic);
-            bool db = bb < w.nb && (w.bflags[bb] & kBodyAlive) && w.bgen[bb] == a.mv.genB[m] && !(w.bflags[bb] & kBodyStatic);
-            s_dyn[m] = (da ? 1u : 0u) | (db ? 2u : 0u);
+            const uint32_t fl = s_dyn[m];
+            const bool da = fl & kFlagDynA, db = fl & kFlagDynB;
             s_color[m] = kUncolored;
             if (!slotted) {
+                const uint32_t ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
                 if (da) {
                     __stcg(&sb.bodyUsed[2 * ba], 0ull);
                     __stcg(&sb.bodyUsed[2 * ba + 1], 0ull);
@@ -534,35 +576,47 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
                 if (s_dyn[m] & 2u) atomicMax(&cBest[cid(m, 1)], p);
             }
             __syncthreads();
-            for (uint32_t m = tid; m < M; m += nt) {
-                if (s_color[m] != kUncolored) continue;
-                const unsigned long long p = stamp | colorPriority(m);
-                const uint32_t d = s_dyn[m], ba = cid(m, 0), bb = cid(m, 1);
-                if ((d & 1u) && ldc(&cBest[ba]) != p) continue;
-                if ((d & 2u) && ldc(&cBest[bb]) != p) continue;
-                unsigned long long u0 = 0, u1 = 0;
-                if (d & 1u) {
-                    u0 |= ldc(&cUsed[2 * ba]);
-                    u1 |= ldc(&cUsed[2 * ba + 1]);
+            // (m0 advances uniformly so that whole warps aggregate the counters)
+            for (uint32_t m0 = 0; m0 < M; m0 += nt) {
+                const uint32_t m = m0 + tid;
+                uint32_t c = kUncolored;
+                if (m < M && s_color[m] == kUncolored) {
+                    const unsigned long long p = stamp | colorPriority(m);
+                    const uint32_t d = s_dyn[m], ba = cid(m, 0), bb = cid(m, 1);
+                    const bool wins = (!(d & 1u) || ldc(&cBest[ba]) == p) && (!(d & 2u) || ldc(&cBest[bb]) == p);
+                    if (wins) {
+                        unsigned long long u0 = 0, u1 = 0;
+                        if (d & 1u) {
+                            u0 |= ldc(&cUsed[2 * ba]);
+                            u1 |= ldc(&cUsed[2 * ba + 1]);
+                        }
+                        if (d & 2u) {
+                            u0 |= ldc(&cUsed[2 * bb]);
+                            u1 |= ldc(&cUsed[2 * bb + 1]);
+                        }
+                        if (~u0) c = __ffsll((long long)~u0) - 1;
+                        else if (~u1) c = 64 + __ffsll((long long)~u1) - 1;
+                        else {
+                            atomicOr(&a.st->err, kErrColors);
+                            c = kMaxColors - 1;
+                        }
+                        s_color[m] = c;
+                        const unsigned long long bit = 1ull << (c & 63);
+                        if (d & 1u) stc(&cUsed[2 * ba + (c >> 6)], ldc(&cUsed[2 * ba + (c >> 6)]) | bit);
+                        if (d & 2u) stc(&cUsed[2 * bb + (c >> 6)], ldc(&cUsed[2 * bb + (c >> 6)]) | bit);
+                    }
                 }
-                if (d & 2u) {
-                    u0 |= ldc(&cUsed[2 * bb]);
-                    u1 |= ldc(&cUsed[2 * bb + 1]);
+                // one shared-memory atomic per warp and counter
+                const uint32_t lane = tid & 31;
+                const bool got = c != kUncolored;
+                const uint32_t gotMask = __ballot_sync(0xffffffffu, got);
+                const uint32_t top = __reduce_max_sync(0xffffffffu, got ? c + 1 : 0u);
+                if (lane == 0 && gotMask) {
+                    atomicAdd(&s_colored, (uint32_t)__popc(gotMask));
+                    atomicMax(&s_colors, top);
                 }
-                uint32_t c;
-                if (~u0) c = __ffsll((long long)~u0) - 1;
-                else if (~u1) c = 64 + __ffsll((long long)~u1) - 1;
-                else {
-                    atomicOr(&a.st->err, kErrColors);
-                    c = kMaxColors - 1;
-                }
-                s_color[m] = c;
-                const unsigned long long bit = 1ull << (c & 63);
-                if (d & 1u) stc(&cUsed[2 * ba + (c >> 6)], ldc(&cUsed[2 * ba + (c >> 6)]) | bit);
-                if (d & 2u) stc(&cUsed[2 * bb + (c >> 6)], ldc(&cUsed[2 * bb + (c >> 6)]) | bit);
-                atomicAdd(&s_count[c], 1u);
-                atomicMax(&s_colors, c + 1);
-                atomicAdd(&s_colored, 1u);
+                const uint32_t peers = __match_any_sync(0xffffffffu, c);
+                if (got && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&s_count[c], (uint32_t)__popc(peers));
             }
             __syncthreads();
             if (s_colored >= M) break;
@@ -611,7 +665,11 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
                     s_count[cc] = run;
                 }
                 __syncthreads();
-                if (m < M) sb.order[s_start[c] + wc[warp * Cc + c] + rank] = m;
+                if (m < M) {
+                    const uint32_t k = s_start[c] + wc[warp * Cc + c] + rank;
+                    sb.order[k] = m;
+                    s_dyn[k] = m;  // solve index -> manifold for the sweeps
+                }
                 __syncthreads();
             }
         } else {
@@ -620,88 +678,33 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
             for (uint32_t i = tid; i < n2; i += nt) keys[i] = i < M ? ((sb.color[i] << 12) | i) : 0xFFFFFFFFu;
             __syncthreads();
             blockBitonicSort<uint32_t>(keys, n2);
-            for (uint32_t k = tid; k < M; k += nt) sb.order[k] = keys[k] & 0xFFFu;
+            __syncthreads();  // s_dyn (colouring flags) is read no more
+            for (uint32_t k = tid; k < M; k += nt) {
+                sb.order[k] = keys[k] & 0xFFFu;
+                s_dyn[k] = keys[k] & 0xFFFu;
+            }
         }
-        C = s_colors;
         __syncthreads();
         if (slotted) {
             // slots by manifold -> slots by solve index (through the sort area)
             uint2 *tmp = reinterpret_cast<uint2 *>(s_sort);
-            for (uint32_t k = tid; k < M; k += nt) tmp[k] = vs->slot[sb.order[k]];
+            for (uint32_t k = tid; k < M; k += nt) tmp[k] = vs->slot[s_dyn[k]];
             __syncthreads();
             for (uint32_t k = tid; k < M; k += nt) vs->slot[k] = tmp[k];
             __syncthreads();
         }
     }
-    // --- prepare + warm-start matching (old cache keys searched in shared memory when they fit) ---
-    {
-        const uint32_t cacheN = *a.oldCount;
-        const bool keysInShared = cacheN <= maxM;
-        if (keysInShared)
-            for (uint32_t i = tid; i < cacheN; i += nt) s_sort[i] = a.oldCache.key[i];
-        __syncthreads();
-        prepareRange(a, tid, nt, M, keysInShared ? s_sort : nullptr);
-    }
-    __syncthreads();
-    // --- stage the touched bodies' velocities in shared memory (slots from above) ---
-    const bool staged = slotted;
-    if (staged) {
-        for (uint32_t sl = tid; sl < sh.slots; sl += nt) {
-            const uint32_t b = vs->slotBody[sl];
-            vs->v[2 * sl] = ld4(&w.nxt.lin[b]);
-            vs->v[2 * sl + 1] = ld4(&w.nxt.ang[b]);
-        }
-        __syncthreads();
-    }
-    // --- warm start and velocity iterations ---
-    if (serial) {
-        if (tid == 0) {
-            for (uint32_t k = 0; k < M; ++k) warmStartOne(a, k);
-            for (int it = 0; it < a.iterations; ++it)
-                for (uint32_t k = 0; k < M; ++k) solveOne(a, k);
-        }
-    } else if (staged) {
-        const SharedVel sv{vs->v, vs->slot};
-        for (uint32_t c = 0; c < C; ++c) {
-            for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) warmStartOne(a, k, sv);
-            __syncthreads();
-        }
-        for (int it = 0; it < a.iterations; ++it)
-            for (uint32_t c = 0; c < C; ++c) {
-                for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) solveOne(a, k, sv);
-                __syncthreads();
-            }
-    } else {
-        for (uint32_t c = 0; c < C; ++c) {
-            for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) warmStartOne(a, k);
-            __syncthreads();
-        }
-        for (int it = 0; it < a.iterations; ++it)
-            for (uint32_t c = 0; c < C; ++c) {
-                for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) solveOne(a, k);
-                __syncthreads();
-            }
-    }
-    __syncthreads();
-    if (staged) {
-        const uint32_t nslots = sh.slots;
-        for (uint32_t sl = tid; sl < nslots; sl += nt) {
-            const uint32_t b = vs->slotBody[sl];
-            st4(&w.nxt.lin[b], vs->v[2 * sl]);
-            st4(&w.nxt.ang[b], vs->v[2 * sl + 1]);
-        }
-        __syncthreads();
-    }
-    // --- impulses back to the manifolds ---
-    for (uint32_t k = tid; k < M; k += nt) {
-        const uint32_t m = sb.order[k];
-        for (uint32_t p = 0; p < 4; ++p) {
-            float4 imp = sb.pimp[(size_t)p * a.mcap + k];
-            imp.w = 0.0f;
-            a.mv.impulse[4 * m + p] = imp;
-        }
-    }
-    __syncthreads();
+    return slotted;
+}
+
+// Warm-start cache rebuild (:623-681) of the single-block solver, after the
+// impulses are back in the manifolds.
+__device__ inline void solveBlockCache(const SolveArgs &a, const CacheView &nc, uint32_t cacheCap, uint32_t *newCount,
+                                       uint32_t M, unsigned long long *s_sort, uint32_t *s_dyn, BlockSolveShared &sh) {
+    uint32_t *s_scan = sh.scan;
+    const WorldView &w = a.w;
+    const SolverBuffers &sb = a.sb;
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
     // --- cache rebuild ---
     if (a.pairOrderCache) {
         // Manifold order is (body A, body B) order with one manifold per key:
@@ -747,8 +750,121 @@ __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint3
         const uint32_t cnt = (i + 1 < M ? s_dyn[i + 1] : total) - s_dyn[i];
         cacheWriteManifold(a, nc, cacheCap, m, s_dyn[i], cnt);
     }
-    if (tid == 0) *newCount = total;
+    if (tid == 0) *newCount = total;}
+
+// Sweeps of the single-block solver after prepare: velocity staging (when
+// slotted), warm start and iterations colour by colour, write-back, impulses
+// back to the manifolds.
+__device__ inline void solveBlockSweeps(const SolveArgs &a, uint32_t M, int serial, uint32_t C, bool slotted,
+                                        const uint32_t *s_dyn, BlockSolveShared &sh, const VelStage *vs) {
+    const uint32_t *s_start = sh.start;
+    const WorldView &w = a.w;
+    const SolverBuffers &sb = a.sb;
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    // --- stage the touched bodies' velocities in shared memory (slots from above) ---
+    const bool staged = slotted;
+    if (staged) {
+        for (uint32_t sl = tid; sl < sh.slots; sl += nt) {
+            const uint32_t b = vs->slotBody[sl];
+            vs->v[2 * sl] = ld4(&w.nxt.lin[b]);
+            vs->v[2 * sl + 1] = ld4(&w.nxt.ang[b]);
+        }
+        __syncthreads();
+    }
+    // --- warm start and velocity iterations ---
+    // (manifold of solve index k: k itself in reference order, s_dyn[k] otherwise)
+    if (serial) {
+        if (tid == 0) {
+            for (uint32_t k = 0; k < M; ++k) warmStartOne(a, k, k);
+            for (int it = 0; it < a.iterations; ++it)
+                for (uint32_t k = 0; k < M; ++k) solveOne(a, k, k);
+        }
+    } else if (staged) {
+        const SharedVel sv{vs->v, vs->slot};
+        for (uint32_t c = 0; c < C; ++c) {
+            for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) warmStartOne(a, k, s_dyn[k], sv);
+            __syncthreads();
+        }
+        for (int it = 0; it < a.iterations; ++it)
+            for (uint32_t c = 0; c < C; ++c) {
+                for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) solveOne(a, k, s_dyn[k], sv);
+                __syncthreads();
+            }
+    } else {
+        for (uint32_t c = 0; c < C; ++c) {
+            for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) warmStartOne(a, k, s_dyn[k]);
+            __syncthreads();
+        }
+        for (int it = 0; it < a.iterations; ++it)
+            for (uint32_t c = 0; c < C; ++c) {
+                for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) solveOne(a, k, s_dyn[k]);
+                __syncthreads();
+            }
+    }
+    __syncthreads();
+    if (staged) {
+        const uint32_t nslots = sh.slots;
+        for (uint32_t sl = tid; sl < nslots; sl += nt) {
+            const uint32_t b = vs->slotBody[sl];
+            st4(&w.nxt.lin[b], vs->v[2 * sl]);
+            st4(&w.nxt.ang[b], vs->v[2 * sl + 1]);
+        }
+        __syncthreads();
+    }
+    // --- impulses back to the manifolds ---
+    for (uint32_t m = tid; m < M; m += nt) {
+        for (uint32_t p = 0; p < 4; ++p) {
+            float4 imp = sb.pimp[(size_t)p * a.mcap + m];
+            imp.w = 0.0f;
+            a.mv.impulse[4 * m + p] = imp;
+        }
+    }
+    __syncthreads();
 }
+
+// ------------------------------------------------------ single-block path ---
+// The whole solver for up to kBlockMaxManifolds manifolds in one thread block:
+// the same colouring, order, prepare, sweeps and cache rebuild as the
+// multi-kernel path, separated by __syncthreads instead of kernel boundaries
+// and grid barriers.  If the live manifold count exceeds the block capacity the
+// kernel only flags kErrSmallPath; the step is then re-run on the multi-kernel
+// path.
+// s_sort holds maxM u64 and s_dyn maxM u32 (shared memory); sh the small
+// shared arrays.  prepared: the prepared data and the manifold flags (sb.dyn)
+// were written by a launch before this one (else the block computes them
+// itself).  All threads of the block call it.
+__device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint32_t cacheCap, uint32_t *newCount, int serial,
+                           uint32_t maxM, unsigned long long *s_sort, uint32_t *s_dyn, BlockSolveShared &sh,
+                           const VelStage *vs = nullptr, bool prepared = false) {
+    const uint32_t M = min(a.st->manifolds, a.mcap);
+    if (M > maxM) {
+        if (threadIdx.x == 0) atomicOr(&a.st->err, kErrSmallPath);
+        return;
+    }
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    const bool slotted = solveBlockFront(a, M, serial, maxM, s_sort, s_dyn, sh, vs, prepared ? a.sb.dyn : nullptr);
+    const uint32_t C = serial ? 0u : sh.colors;
+    // --- prepare + warm-start matching (old cache keys searched in shared memory when they fit) ---
+    if (!prepared) {
+        const uint32_t cacheN = *a.oldCount;
+        const bool keysInShared = cacheN <= maxM;
+        if (keysInShared)
+            for (uint32_t i = tid; i < cacheN; i += nt) s_sort[i] = a.oldCache.key[i];
+        __syncthreads();
+        prepareRange(a, tid, nt, M, keysInShared ? s_sort : nullptr);
+    }
+    __syncthreads();
+    solveBlockSweeps(a, M, serial, C, slotted, s_dyn, sh, vs);
+    solveBlockCache(a, nc, cacheCap, newCount, M, s_sort, s_dyn, sh);
+}
+
+
+// The solver on one thread-block cluster (k_solve_cluster.cu): colour order
+// only.  Returns false, launching nothing, when the device cannot run the
+// cluster or the capacities do not fit its shared memory.
+ClusterSolveLayout clusterSolveLayout(uint32_t blockM, uint32_t stageSlots);
+bool launchSolverCluster(const SolveArgs &a, const CacheView &newCache, uint32_t *newCacheCount, uint32_t cacheCap,
+                         uint32_t blockM, uint32_t stageSlots, cudaStream_t s);
 
 
 } // namespace pe

@@ -75,6 +75,9 @@ struct SolverBuffers {
     uint32_t *cacheCounts, *cacheOff;
     uint32_t *bar;                  // grid barrier [2]
     uint32_t *counters;             // [4]
+    // cluster solver hand-off: staging slots by solve index, body of each slot
+    uint2 *stageSlot;               // [mcap]
+    uint32_t *stageBody;            // [2 * mcap + 64]
 };
 
 constexpr int kMaxColors = 128;
@@ -110,6 +113,17 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
 // Largest manifold count the single-block solver handles, and the largest
 // body index it can key (bodies < 2^20).
 constexpr uint32_t kBlockMaxManifolds = 4096;
+
+// Cluster solver: ranks per cluster, dynamic shared memory per rank, and the
+// per-rank layout (byte offsets into the dynamic shared memory).
+constexpr uint32_t kClusterRanks = 8;
+constexpr uint32_t kClusterSmemMax = 224 * 1024;
+struct ClusterSolveLayout {
+    uint32_t blockM, stageSlots;   // capacities of the single-block front (rank 0)
+    uint32_t localCap, pointCap;   // manifolds / prepared points held per rank
+    uint32_t offVel, offPm, offPn, offSlot, offM, offCnt, offOff, offPt;
+    uint32_t smemBytes;
+};
 constexpr uint32_t kBlockMaxBodies = 1u << 20;
 int maxCooperativeBlocks(int smCount);
 void launchGeneratePairs(const float4 *in, float4 *out, uint32_t n, cudaStream_t s);

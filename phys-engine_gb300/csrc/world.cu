@@ -366,6 +366,8 @@ void World::ensureCapacity() {
     sCacheOff_.reserve(m);
     sBar_.reserve(2);
     sCounters_.reserve(4);
+    sStageSlot_.reserve(m);
+    sStageBody_.reserve(2 * (size_t)m + 64);
     sb_ = SolverBuffers{m,
                         sBest_.ptr,
                         sUsed_.ptr,
@@ -391,7 +393,9 @@ void World::ensureCapacity() {
                         sCacheCounts_.ptr,
                         sCacheOff_.ptr,
                         sBar_.ptr,
-                        sCounters_.ptr};
+                        sCounters_.ptr,
+                        sStageSlot_.ptr,
+                        sStageBody_.ptr};
 
     // Warm-start caches keep their contents when they grow.
     const uint32_t needCache = 4 * m;
