@@ -75,9 +75,13 @@ struct SolverBuffers {
     uint32_t *cacheCounts, *cacheOff;
     uint32_t *bar;                  // grid barrier [2]
     uint32_t *counters;             // [4]
-    // cluster solver hand-off: staging slots by solve index, body of each slot
+    // cluster solver hand-off: staging slots by solve index, body of each slot;
+    // islands: per root slot the range of its manifolds in compList (solve
+    // indices)
     uint2 *stageSlot;               // [mcap]
     uint32_t *stageBody;            // [2 * mcap + 64]
+    uint2 *compRange;               // [2 * mcap + 64]
+    uint32_t *compList;             // [mcap]
 };
 
 constexpr int kMaxColors = 128;
@@ -121,7 +125,8 @@ constexpr uint32_t kClusterSmemMax = 224 * 1024;
 struct ClusterSolveLayout {
     uint32_t blockM, stageSlots;   // capacities of the single-block front (rank 0)
     uint32_t localCap, pointCap;   // manifolds / prepared points held per rank
-    uint32_t offVel, offPm, offPn, offSlot, offM, offCnt, offOff, offPt;
+    uint32_t islandSlots;          // staging slots the island path holds per rank
+    uint32_t offVel, offScan, offPm, offPn, offSlot, offM, offCnt, offOff, offPt;
     uint32_t smemBytes;
 };
 constexpr uint32_t kBlockMaxBodies = 1u << 20;

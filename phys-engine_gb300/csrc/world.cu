@@ -368,6 +368,8 @@ void World::ensureCapacity() {
     sCounters_.reserve(4);
     sStageSlot_.reserve(m);
     sStageBody_.reserve(2 * (size_t)m + 64);
+    sCompRange_.reserve(2 * (size_t)m + 64);
+    sCompList_.reserve(m);
     sb_ = SolverBuffers{m,
                         sBest_.ptr,
                         sUsed_.ptr,
@@ -395,7 +397,9 @@ void World::ensureCapacity() {
                         sBar_.ptr,
                         sCounters_.ptr,
                         sStageSlot_.ptr,
-                        sStageBody_.ptr};
+                        sStageBody_.ptr,
+                        sCompRange_.ptr,
+                        sCompList_.ptr};
 
     // Warm-start caches keep their contents when they grow.
     const uint32_t needCache = 4 * m;
