@@ -292,12 +292,12 @@ def run_gpu(args, rank, world_size, local_rank):
         return
     peak, peak_kind = measured_peaks()
     stage_ms = {k[:-3]: v for k, v in acc.items()}
-    # The top kernel of the step is the single-block contact solver (one launch
-    # per step whenever the manifold count fits a block); its stage events then
-    # time exactly that kernel.
+    # The top kernel of the step is the contact solver on one thread-block
+    # cluster (one launch per step whenever the manifold count fits the block
+    # capacity); the solver stage's events then time exactly that kernel.
     block_solver = totals["manifolds"] / args.steps < 3000
     dominant = "solver" if block_solver else max(stage_ms, key=stage_ms.get)
-    kernel = "k_solve_block" if block_solver else f"{dominant} stage"
+    kernel = "k_solve_cluster" if block_solver else f"{dominant} stage"
     achieved = stage_b[dominant] / (stage_ms[dominant] / 1000.0) / 1e9 if stage_ms[dominant] > 0 else 0.0
     step_bytes = sum(stage_b.values())
     traffic = profiled_traffic(kernel, stage_b[dominant] / args.steps)

@@ -106,29 +106,32 @@ __device__ __forceinline__ bool satAxis(const M3 &rA, const V3 &heA, const M3 &r
     return true;
 }
 
-// testOBBOBB (sat.cpp:66-102): face axes of A, of B, then A_i x B_j.
+// Column j of a rotation matrix (a box's local axis j in world space).
+__device__ __forceinline__ V3 matColumn(const M3 &r, int j) {
+    return j == 0 ? V3{r.m00, r.m10, r.m20} : j == 1 ? V3{r.m01, r.m11, r.m21} : V3{r.m02, r.m12, r.m22};
+}
+
+// testOBBOBB (sat.cpp:66-102): face axes of A, of B, then A_i x B_j, in that
+// order.  One rolled loop over the 15 axes: the kernel runs this once per pair,
+// so a single copy of the axis test (fetched once) beats 15 unrolled copies.
 __device__ __forceinline__ bool satBoxBox(const V3 &heA, const Tf &tA, const M3 &rA, const V3 &heB, const Tf &tB,
                                           const M3 &rB, V3 &axis, float &depth) {
     depth = 3.402823466e+38f;
     V3 cd = tB.p - tA.p;
-    V3 ax[3] = {{rA.m00, rA.m10, rA.m20}, {rA.m01, rA.m11, rA.m21}, {rA.m02, rA.m12, rA.m22}};
-    V3 bx[3] = {{rB.m00, rB.m10, rB.m20}, {rB.m01, rB.m11, rB.m21}, {rB.m02, rB.m12, rB.m22}};
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-        if (!satAxis(rA, heA, rB, heB, cd, ax[i], axis, depth)) return false;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-        if (!satAxis(rA, heA, rB, heB, cd, bx[i], axis, depth)) return false;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-            if (!satAxis(rA, heA, rB, heB, cd, cross(ax[i], bx[j]), axis, depth)) return false;
+#pragma unroll 1
+    for (int t = 0; t < 15; ++t) {
+        V3 ax;
+        if (t < 3) ax = matColumn(rA, t);
+        else if (t < 6) ax = matColumn(rB, t - 3);
+        else ax = cross(matColumn(rA, (t - 6) / 3), matColumn(rB, (t - 6) % 3));
+        if (!satAxis(rA, heA, rB, heB, cd, ax, axis, depth)) return false;
+    }
     return true;
 }
 
 // addFaceCandidates (narrowphase.cpp:281-304) for one source box face.
-__device__ __forceinline__ void boxFaceCandidates(const V3 &srcHe, const Tf &srcTf, const V3 &othHe, const Tf &othTf,
+// (not inlined: its two calls per box pair share one copy of the code)
+static __device__ __noinline__ void boxFaceCandidates(const V3 &srcHe, const Tf &srcTf, const V3 &othHe, const Tf &othTf,
                                                   const V3 &dir, uint32_t source, V3 *contacts, float *depths,
                                                   uint32_t *feats, uint32_t &count) {
     float otherSurface = dot(boxSupport(othHe, othTf, -dir), dir);
