@@ -607,14 +607,31 @@ k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const
                             }
                         }
                     }
+                    // the four lists are walked side by side: one round trip
+                    // per hop for all of them
+                    uint32_t e[4] = {head[0], head[1], head[2], head[3]};
+                    for (uint32_t hops = 0; hops < ecap; ++hops) {
+                        unsigned long long k2[4];
+                        uint32_t bv[4];
+                        bool live = false;
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        uint32_t e = head[j];
-                        for (uint32_t hops = 0; e < ecap && hops < ecap; ++hops) {
-                            const unsigned long long k2 = ekeys[e];
-                            const uint32_t b = evals[e];
-                            e = enext[e];
-                            if (k2 != key[j] || b <= a) continue;
+                        for (int j = 0; j < 4; ++j) {
+                            k2[j] = 0;
+                            bv[j] = 0;
+                            if (e[j] < ecap) {
+                                k2[j] = ekeys[e[j]];
+                                bv[j] = evals[e[j]];
+                                e[j] = enext[e[j]];
+                                live = true;
+                            } else {
+                                k2[j] = ~key[j];  // no match
+                            }
+                        }
+                        if (!live) break;
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const uint32_t b = bv[j];
+                            if (k2[j] != key[j] || b <= a) continue;
                             ++cmp;
                             const float4 bmn = in.mn[b], bmx = in.mx[b];
                             const int4 fb = firstCell[b];
@@ -647,11 +664,16 @@ k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const
         }
         const uint32_t m = min(cnt, kBodyPartners);
         const uint32_t sa = a < n ? (inSlot ? inSlot[a] : a) : 0u;
+        // partners to collider slots, same-body pairs dropped (once; part[]
+        // then holds the kept slots)
         uint32_t kept = 0;
-        for (uint32_t j = 0; j < m; ++j) {
-            const uint32_t sb = inSlot ? inSlot[part[j]] : part[j];
-            if (cbody && cbody[sa] == cbody[sb] && cbgen[sa] == cbgen[sb]) continue;
-            ++kept;
+        if (m) {
+            const uint32_t ba = cbody ? cbody[sa] : 0u, ga = cbody ? cbgen[sa] : 0u;
+            for (uint32_t j = 0; j < m; ++j) {
+                const uint32_t sb = inSlot ? inSlot[part[j]] : part[j];
+                if (cbody && ba == cbody[sb] && ga == cbgen[sb]) continue;
+                part[kept++] = sb;
+            }
         }
         {
             // one atomic per warp and counter
@@ -673,14 +695,11 @@ k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const
         }
         __syncthreads();
         uint32_t o = s_prefix + local;
-        for (uint32_t j = 0; j < m; ++j) {
-            const uint32_t sb = inSlot ? inSlot[part[j]] : part[j];
-            if (cbody && cbody[sa] == cbody[sb] && cbgen[sa] == cbgen[sb]) continue;
+        for (uint32_t j = 0; j < kept; ++j, ++o) {
             if (o < cap) {
                 pairA[o] = sa;
-                pairB[o] = sb;
+                pairB[o] = part[j];
             }
-            ++o;
         }
         if (threadIdx.x == 0 && tile + 1 == ntiles) st->pairs = s_prefix + total;
         __syncthreads();
