@@ -84,11 +84,14 @@ struct LocalPrep {
 
 // ------------------------------------------------------------- islands ---
 // Manifolds joined by a shared dynamic body form an island (static bodies are
-// never written, so they join nothing).  Islands share no written state: one
-// thread can run every sweep of a small island on its own, in the island's
-// (colour, index) order, with no barrier at all; that is the order the
-// colour-phase sweeps give every body of the island.
-constexpr uint32_t kIslandMax = 8;           // larger islands take the colour-phase path
+// never written, so they join nothing; the reference's own island rule,
+// sequential_impulse_solver.cpp:366-442).  Islands share no written state, and
+// the graph colouring of a manifold depends only on the manifolds of its
+// island (its neighbours all are), so one thread can colour a small island
+// (greedy in decreasing priority: the Jones-Plassmann result), order it by
+// (colour, index) and run every sweep of it on its own, with no barrier: each
+// body then sees exactly the updates, in the order, that the colour-phase
+// sweeps give it.
 constexpr uint32_t kNoIsland = 0xFFFFFFFFu;
 constexpr uint32_t kIslandUniteLimit = 1u << 16;
 
@@ -140,72 +143,18 @@ struct LocalOnlyPrep {
     }
 };
 
+struct IslandShared {
+    uint32_t classCount[kIslandMax + 1], classBase[kIslandMax + 2], localUsed, pointUsed, bodyUsed, units;
+};
+
 struct ClusterShared {
     BlockSolveShared solve;
     uint32_t start[kMaxColors + 1];   // colour ranges of the solve order
     uint32_t lstart[kMaxColors + 1];  // colour ranges of this rank's local manifolds
-    uint32_t colors, slots, slotted, islands;
-    uint32_t rankManifolds[kClusterRanks];
-    uint32_t islandFail;
+    uint32_t colors, slots, slotted;
+    IslandShared island;
 };
 
-// Islands of the ordered manifolds (rank 0, after the front): per root slot
-// the range of its manifolds (solve indices, in no particular order) in
-// sb.compList.  work: 3 * cap words (the front's velocity area); rootK: M
-// words.  Returns whether every island is small, all slots fit the per-rank
-// velocity arrays and every rank's islands fit its local manifold capacity.
-__device__ bool islandFront(const SolveArgs &a, uint32_t M, uint32_t S, const uint32_t *order, const uint2 *slotK,
-                            uint32_t *work, uint32_t cap, uint32_t *rootK, const ClusterSolveLayout &lay,
-                            ClusterShared &cs) {
-    const SolverBuffers &sb = a.sb;
-    const uint32_t tid = threadIdx.x, nt = blockDim.x;
-    uint32_t *parent = work, *cnt = work + cap, *cur = work + 2 * cap;
-    for (uint32_t sl = tid; sl < S; sl += nt) {
-        parent[sl] = sl;
-        cnt[sl] = 0;
-    }
-    if (tid < kClusterRanks) cs.rankManifolds[tid] = 0;
-    if (tid == 0) cs.islandFail = S > lay.islandSlots ? 1u : 0u;
-    __syncthreads();
-    for (uint32_t k = tid; k < M; k += nt) {
-        const uint32_t fl = __ldcg(&sb.dyn[order[k]]);
-        rootK[k] = fl;
-        if ((fl & (kFlagValid | kFlagDynA | kFlagDynB)) == (kFlagValid | kFlagDynA | kFlagDynB))
-            if (!islandUnite(parent, slotK[k].x, slotK[k].y)) cs.islandFail = 1;
-    }
-    __syncthreads();
-    for (uint32_t sl = tid; sl < S; sl += nt) parent[sl] = islandFind(parent, sl);
-    __syncthreads();
-    for (uint32_t k = tid; k < M; k += nt) {
-        const uint32_t fl = rootK[k];
-        uint32_t r = kNoIsland;
-        if (fl & kFlagValid) {
-            if (fl & kFlagDynA) r = parent[slotK[k].x];
-            else if (fl & kFlagDynB) r = parent[slotK[k].y];
-            else cs.islandFail = 1;  // solved manifold without a dynamic body: colour-phase path
-        }
-        rootK[k] = r;
-        if (r != kNoIsland) atomicAdd(&cnt[r], 1u);
-    }
-    __syncthreads();
-    for (uint32_t sl = tid; sl < S; sl += nt) {
-        const uint32_t c = cnt[sl];
-        if (c > kIslandMax) cs.islandFail = 1;
-        if (c) atomicAdd(&cs.rankManifolds[sl % kClusterRanks], c);
-        cur[sl] = c;
-    }
-    __syncthreads();
-    blockExclusiveScanArray(cur, S, cs.solve.scan);
-    for (uint32_t sl = tid; sl < S; sl += nt) sb.compRange[sl] = make_uint2(cur[sl], cnt[sl]);
-    if (tid < kClusterRanks && cs.rankManifolds[tid] > lay.localCap) cs.islandFail = 1;
-    __syncthreads();
-    for (uint32_t k = tid; k < M; k += nt) {
-        const uint32_t r = rootK[k];
-        if (r != kNoIsland) sb.compList[atomicAdd(&cur[r], 1u)] = k;
-    }
-    __syncthreads();
-    return cs.islandFail == 0;
-}
 
 // Warm-start cache rebuild after the sweeps (all ranks, after a cluster
 // barrier): in manifold order every rank writes its interleaved share (as
@@ -234,112 +183,251 @@ __device__ void solveClusterCache(const SolveArgs &a, const CacheView &nc, uint3
     if (rank == 0 && tid == 0) *newCount = total;
 }
 
-// Island sweeps (all ranks): rank r takes the islands whose root slot is r
-// modulo R, one thread per island; every rank holds the velocities of all
-// staged bodies (slot-indexed) and its islands' prepared data.
-__device__ void solveIslands(const SolveArgs &a, const ClusterSolveLayout &lay, uint32_t rank, uint32_t S, float4 *sv,
-                             float4 *spm, float4 *spn, float4 *spt, uint2 *sslot, uint32_t *sm, uint32_t *scnt,
-                             uint32_t *soff, uint32_t *scan, ClusterShared &cs) {
+
+
+// One island, as its owning thread sees it: manifolds in solve order (colour,
+// index), their colours, flags, points and local body indices, the island's
+// bodies.
+struct IslandPlan {
+    uint32_t n, nbody, points, colors;
+    uint32_t ks[kIslandMax], color[kIslandMax], fl[kIslandMax], cnt[kIslandMax];
+    uint2 slot[kIslandMax];
+    uint32_t body[2 * kIslandMax];
+};
+
+// Reads the island of root body r (n manifolds), colours it (greedy in
+// decreasing priority: the colour is the first one free among the higher-
+// priority neighbours at the dynamic bodies, the Jones-Plassmann round one
+// more than theirs) and orders it by (colour, index).  Writes the colours and
+// the colour statistics.
+__device__ void planIsland(const SolveArgs &a, uint32_t r, uint32_t n, IslandPlan &P) {
     const SolverBuffers &sb = a.sb;
+    uint32_t ks[kIslandMax], fl[kIslandMax];
+    uint2 slot[kIslandMax];
+    for (uint32_t j = 0; j < n; ++j) {
+        const uint32_t m = __ldcg(&sb.islandList[(size_t)r * kIslandMax + j]);
+        uint32_t i = j;
+        for (; i > 0 && ks[i - 1] > m; --i) ks[i] = ks[i - 1];
+        ks[i] = m;
+    }
+    P.nbody = 0;
+    auto local = [&](uint32_t b) {
+        for (uint32_t i = 0; i < P.nbody; ++i)
+            if (P.body[i] == b) return i;
+        P.body[P.nbody] = b;
+        return P.nbody++;
+    };
+    for (uint32_t j = 0; j < n; ++j) {
+        const uint32_t m = ks[j];
+        fl[j] = __ldcg(&sb.dyn[m]);
+        slot[j].x = local(a.mv.bodyA[m]);
+        slot[j].y = local(a.mv.bodyB[m]);
+    }
+    uint32_t byPri[kIslandMax], color[kIslandMax];
+    for (uint32_t j = 0; j < n; ++j) {
+        const uint32_t p = colorPriority(ks[j]);
+        uint32_t i = j;
+        for (; i > 0 && colorPriority(ks[byPri[i - 1]]) < p; --i) byPri[i] = byPri[i - 1];
+        byPri[i] = j;
+    }
+    uint32_t used[2 * kIslandMax], round[2 * kIslandMax];
+    for (uint32_t i = 0; i < P.nbody; ++i) used[i] = round[i] = 0;
+    uint32_t colors = 0, rounds = 0;
+    for (uint32_t t = 0; t < n; ++t) {
+        const uint32_t j = byPri[t];
+        const bool dA = fl[j] & kFlagDynA, dB = fl[j] & kFlagDynB;
+        const uint32_t mask = (dA ? used[slot[j].x] : 0u) | (dB ? used[slot[j].y] : 0u);
+        const uint32_t c = __ffs(~mask) - 1;
+        const uint32_t rd = max(dA ? round[slot[j].x] : 0u, dB ? round[slot[j].y] : 0u) + 1;
+        color[j] = c;
+        colors = max(colors, c + 1);
+        rounds = max(rounds, rd);
+        if (dA) {
+            used[slot[j].x] |= 1u << c;
+            round[slot[j].x] = max(round[slot[j].x], rd);
+        }
+        if (dB) {
+            used[slot[j].y] |= 1u << c;
+            round[slot[j].y] = max(round[slot[j].y], rd);
+        }
+        sb.color[ks[j]] = c;
+    }
+    atomicMax(&a.st->colors, colors);
+    atomicMax(&a.st->colorRounds, rounds);
+    // (colour, index) order
+    uint32_t ord[kIslandMax];
+    for (uint32_t j = 0; j < n; ++j) {
+        uint32_t i = j;
+        for (; i > 0 && color[ord[i - 1]] > color[j]; --i) ord[i] = ord[i - 1];
+        ord[i] = j;
+    }
+    P.n = n;
+    P.colors = colors;
+    P.points = 0;
+    for (uint32_t t = 0; t < n; ++t) {
+        const uint32_t j = ord[t];
+        P.ks[t] = ks[j];
+        P.color[t] = color[j];
+        P.fl[t] = fl[j];
+        P.slot[t] = slot[j];
+        P.cnt[t] = __ldcg(&sb.pcount[ks[j]]);
+        P.points += P.cnt[t];
+    }
+}
+
+// The island on its own thread (when it does not fit this rank's shared
+// memory): prepared data from the solver arrays, velocities thread-local.
+__device__ void solveIslandAlone(const SolveArgs &a, const IslandPlan &P) {
     const WorldView &w = a.w;
-    const uint32_t tid = threadIdx.x, nt = blockDim.x;
-    for (uint32_t sl = tid; sl < S; sl += nt) {
-        const uint32_t b = __ldcg(&sb.stageBody[sl]);
-        sv[2 * sl] = ld4(&w.nxt.lin[b]);
-        sv[2 * sl + 1] = ld4(&w.nxt.ang[b]);
+    float4 vel[4 * kIslandMax];
+    for (uint32_t i = 0; i < P.nbody; ++i) {
+        vel[2 * i] = ld4(&w.nxt.lin[P.body[i]]);
+        vel[2 * i + 1] = ld4(&w.nxt.ang[P.body[i]]);
     }
-    // local manifold ranges: a block scan of each thread's island sizes
-    uint32_t mine = 0;
-    for (uint32_t r = rank + kClusterRanks * tid; r < S; r += kClusterRanks * nt) mine += __ldcg(&sb.compRange[r]).y;
-    scan[tid] = mine;
-    __syncthreads();
-    blockExclusiveScanArray(scan, nt, cs.solve.scan);
-    const uint32_t base = scan[tid];
-    __syncthreads();
-    // each island's manifolds in solve order, then their data
-    uint32_t L = base, points = 0;
-    for (uint32_t r = rank + kClusterRanks * tid; r < S; r += kClusterRanks * nt) {
-        const uint2 rng = __ldcg(&sb.compRange[r]);
-        if (!rng.y) continue;
-        uint32_t ks[kIslandMax];
-        const uint32_t n = min(rng.y, kIslandMax);
-        for (uint32_t j = 0; j < n; ++j) {
-            const uint32_t k = __ldcg(&sb.compList[rng.x + j]);
-            uint32_t i = j;
-            for (; i > 0 && ks[i - 1] > k; --i) ks[i] = ks[i - 1];
-            ks[i] = k;
-        }
-        for (uint32_t j = 0; j < n; ++j, ++L) {
-            const uint32_t k = ks[j], m = __ldcg(&sb.order[k]);
-            sm[L] = m;
-            sslot[L] = __ldcg(&sb.stageSlot[k]);
-            spm[L] = __ldcg(&sb.pm[m]);
-            spn[L] = __ldcg(&sb.pn[m]);
-            scnt[L] = __ldcg(&sb.pcount[m]);
-            points += scnt[L];
-        }
-    }
-    const uint32_t end = L;
-    scan[tid] = points;
-    __syncthreads();
-    blockExclusiveScanArray(scan, nt, cs.solve.scan);
-    uint32_t o = scan[tid];
-    for (uint32_t L2 = base; L2 < end; ++L2) {
-        const uint32_t n = scnt[L2], m = sm[L2];
-        if (o + n > lay.pointCap) {  // past the local capacity: the solver arrays
-            soff[L2] = kNoLocal;
-            continue;
-        }
-        soff[L2] = o;
-        for (uint32_t p = 0; p < n; ++p) {
-#pragma unroll
-            for (int v = 0; v < kPreparedVec4; ++v)
-                spt[(size_t)v * lay.pointCap + o + p] = __ldcg(&sb.pp[(size_t)(v * 4 + p) * a.mcap + m]);
-            spt[(size_t)10 * lay.pointCap + o + p] = __ldcg(&sb.pimp[(size_t)p * a.mcap + m]);
-        }
-        o += n;
-    }
-    __syncthreads();  // velocities of every slot loaded
-    // sweeps: every island on its own thread, pass by pass (pass 0: warm start)
-    const LocalPrep pr{a, spm, spn, sm, scnt, soff, spt, lay.pointCap};
-    const SharedVel vel{sv, sslot};
-    uint32_t b0 = base;
-    for (uint32_t r = rank + kClusterRanks * tid; r < S; r += kClusterRanks * nt) {
-        const uint32_t n = min(__ldcg(&sb.compRange[r]).y, kIslandMax);
-        if (!n) continue;
-        bool local = true;
-        for (uint32_t j = 0; j < n; ++j) local = local && soff[b0 + j] != kNoLocal;
-        if (local) {
-            const LocalOnlyPrep lp{a, spm, spn, sm, scnt, soff, spt, lay.pointCap};
-            for (uint32_t j = 0; j < n; ++j) warmStartOne(lp, b0 + j, b0 + j, vel);
-            for (int it = 0; it < a.iterations; ++it)
-                for (uint32_t j = 0; j < n; ++j) solveOne(lp, b0 + j, b0 + j, vel);
-        } else {
-            for (uint32_t j = 0; j < n; ++j) warmStartOne(pr, b0 + j, b0 + j, vel);
-            for (int it = 0; it < a.iterations; ++it)
-                for (uint32_t j = 0; j < n; ++j) solveOne(pr, b0 + j, b0 + j, vel);
-        }
-        b0 += n;
-    }
-    // velocities of the islands' dynamic bodies and the impulses back
-    for (uint32_t L2 = base; L2 < end; ++L2) {
-        const float4 pm = spm[L2];
-        const uint2 sl = sslot[L2];
-        if (pm.y == 0.0f) {
-            const uint32_t b = __ldcg(&sb.stageBody[sl.x]);
-            st4(&w.nxt.lin[b], sv[2 * sl.x]);
-            st4(&w.nxt.ang[b], sv[2 * sl.x + 1]);
-        }
-        if (pm.w == 0.0f) {
-            const uint32_t b = __ldcg(&sb.stageBody[sl.y]);
-            st4(&w.nxt.lin[b], sv[2 * sl.y]);
-            st4(&w.nxt.ang[b], sv[2 * sl.y + 1]);
-        }
-        const uint32_t m = sm[L2], n = scnt[L2];
-        for (uint32_t p = 0; p < n; ++p) {
-            float4 imp = pr.imp(p, L2);
+    const GlobalPrep pr{a};
+    const SharedVel v{vel, P.slot};
+    for (uint32_t t = 0; t < P.n; ++t) warmStartOne(pr, t, P.ks[t], v);
+    for (int it = 0; it < a.iterations; ++it)
+        for (uint32_t t = 0; t < P.n; ++t) solveOne(pr, t, P.ks[t], v);
+    for (uint32_t t = 0; t < P.n; ++t) {
+        const uint32_t m = P.ks[t];
+        for (uint32_t p = 0; p < P.cnt[t]; ++p) {
+            float4 imp = pr.imp(p, m);
             imp.w = 0.0f;
             a.mv.impulse[4 * m + p] = imp;
+        }
+        if (P.fl[t] & kFlagDynA) {
+            st4(&w.nxt.lin[P.body[P.slot[t].x]], vel[2 * P.slot[t].x]);
+            st4(&w.nxt.ang[P.body[P.slot[t].x]], vel[2 * P.slot[t].x + 1]);
+        }
+        if (P.fl[t] & kFlagDynB) {
+            st4(&w.nxt.lin[P.body[P.slot[t].y]], vel[2 * P.slot[t].y]);
+            st4(&w.nxt.ang[P.body[P.slot[t].y]], vel[2 * P.slot[t].y + 1]);
+        }
+    }
+}
+
+// Island sweeps of one rank.  Islands are packed into warp-sized units by
+// size (32 / n islands of n manifolds per unit, one manifold per lane); a
+// warp runs a unit colour phase by colour phase (__syncwarp between phases),
+// so an island's manifolds of one colour run side by side and islands of a
+// unit run together.  Each manifold's prepared data and each island's body
+// velocities sit in this rank's shared memory.  ownRoot: the island this
+// thread owns (kNoIsland if none).
+constexpr uint32_t kIslandUnits = 32;  // warp units per rank
+
+__device__ void solveIslandsRank(const SolveArgs &a, const ClusterSolveLayout &lay, unsigned char *smem, uint32_t ownRoot,
+                                 IslandShared &is) {
+    const SolverBuffers &sb = a.sb;
+    const WorldView &w = a.w;
+    const uint32_t tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    float4 *spm = reinterpret_cast<float4 *>(smem + lay.offPm);
+    float4 *spn = reinterpret_cast<float4 *>(smem + lay.offPn);
+    float4 *spt = reinterpret_cast<float4 *>(smem + lay.offPt);
+    uint2 *sslot = reinterpret_cast<uint2 *>(smem + lay.offSlot);
+    uint32_t *sm = reinterpret_cast<uint32_t *>(smem + lay.offM);
+    uint32_t *scnt = reinterpret_cast<uint32_t *>(smem + lay.offCnt);
+    uint32_t *soff = reinterpret_cast<uint32_t *>(smem + lay.offOff);
+    float4 *sv = reinterpret_cast<float4 *>(smem + lay.offVel);                      // [2 * islandBodies]
+    uint32_t *laneL = reinterpret_cast<uint32_t *>(smem + lay.offVel + (size_t)lay.islandBodies * 32);
+    uint32_t *unitC = laneL + kIslandUnits * 32;
+    uint32_t *scol = unitC + kIslandUnits;                                             // [localCap]
+    if (tid <= kIslandMax) is.classCount[tid] = 0;
+    if (tid == 0) is.localUsed = is.pointUsed = is.bodyUsed = 0;
+    for (uint32_t i = tid; i < kIslandUnits * 32; i += nt) laneL[i] = kNoLocal;
+    for (uint32_t i = tid; i < kIslandUnits; i += nt) unitC[i] = 0;
+    __syncthreads();
+    IslandPlan P;
+    uint32_t idx = 0;
+    if (ownRoot != kNoIsland) {
+        planIsland(a, ownRoot, __ldcg(&reinterpret_cast<uint32_t *>(sb.bodyUsed)[w.nb + ownRoot]), P);
+        idx = atomicAdd(&is.classCount[P.n], 1u);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t base = 0;
+        for (uint32_t c = 1; c <= kIslandMax; ++c) {
+            is.classBase[c] = base;
+            const uint32_t per = 32 / c;
+            base += (is.classCount[c] + per - 1) / per;
+        }
+        is.units = base;
+    }
+    __syncthreads();
+    bool packed = false;
+    uint32_t L0 = 0, B0 = 0;
+    if (ownRoot != kNoIsland) {
+        const uint32_t per = 32 / P.n;
+        const uint32_t u = is.classBase[P.n] + idx / per, lane0 = (idx % per) * P.n;
+        if (u < kIslandUnits) {
+            L0 = atomicAdd(&is.localUsed, P.n);
+            const uint32_t P0 = atomicAdd(&is.pointUsed, P.points);
+            B0 = atomicAdd(&is.bodyUsed, P.nbody);
+            packed = L0 + P.n <= lay.localCap && P0 + P.points <= lay.pointCap && B0 + P.nbody <= lay.islandBodies;
+            if (packed) {
+                uint32_t o = P0;
+                for (uint32_t t = 0; t < P.n; ++t) {
+                    const uint32_t m = P.ks[t], L = L0 + t;
+                    sm[L] = m;
+                    sslot[L] = make_uint2(B0 + P.slot[t].x, B0 + P.slot[t].y);
+                    spm[L] = __ldcg(&sb.pm[m]);
+                    spn[L] = __ldcg(&sb.pn[m]);
+                    scnt[L] = P.cnt[t];
+                    soff[L] = o;
+                    scol[L] = P.color[t];
+                    for (uint32_t p = 0; p < P.cnt[t]; ++p) {
+#pragma unroll
+                        for (int v = 0; v < kPreparedVec4; ++v)
+                            spt[(size_t)v * lay.pointCap + o + p] = __ldcg(&sb.pp[(size_t)(v * 4 + p) * a.mcap + m]);
+                        spt[(size_t)10 * lay.pointCap + o + p] = __ldcg(&sb.pimp[(size_t)p * a.mcap + m]);
+                    }
+                    o += P.cnt[t];
+                    laneL[u * 32 + lane0 + t] = L;
+                }
+                for (uint32_t i = 0; i < P.nbody; ++i) {
+                    sv[2 * (B0 + i)] = ld4(&w.nxt.lin[P.body[i]]);
+                    sv[2 * (B0 + i) + 1] = ld4(&w.nxt.ang[P.body[i]]);
+                }
+                atomicMax(&unitC[u], P.colors);
+            }
+        }
+        if (!packed) solveIslandAlone(a, P);
+    }
+    __syncthreads();
+    // warp units: pass by pass (pass 0: warm start), colour by colour
+    const LocalOnlyPrep pr{a, spm, spn, sm, scnt, soff, spt, lay.pointCap};
+    const SharedVel v{sv, sslot};
+    for (uint32_t u = warp; u < min(is.units, kIslandUnits); u += nt >> 5) {
+        const uint32_t L = laneL[u * 32 + lane], C = unitC[u];
+        const uint32_t c = L != kNoLocal ? scol[L] : kNoLocal;
+        for (int pass = 0; pass <= a.iterations; ++pass)
+            for (uint32_t cc = 0; cc < C; ++cc) {
+                if (c == cc) {
+                    if (pass == 0) warmStartOne(pr, L, L, v);
+                    else solveOne(pr, L, L, v);
+                }
+                __syncwarp();
+            }
+    }
+    __syncthreads();
+    if (packed) {
+        for (uint32_t t = 0; t < P.n; ++t) {
+            const uint32_t m = P.ks[t], L = L0 + t;
+            for (uint32_t p = 0; p < P.cnt[t]; ++p) {
+                float4 imp = pr.imp(p, L);
+                imp.w = 0.0f;
+                a.mv.impulse[4 * m + p] = imp;
+            }
+            if (P.fl[t] & kFlagDynA) {
+                const uint32_t i = B0 + P.slot[t].x;
+                st4(&w.nxt.lin[P.body[P.slot[t].x]], sv[2 * i]);
+                st4(&w.nxt.ang[P.body[P.slot[t].x]], sv[2 * i + 1]);
+            }
+            if (P.fl[t] & kFlagDynB) {
+                const uint32_t i = B0 + P.slot[t].y;
+                st4(&w.nxt.lin[P.body[P.slot[t].y]], sv[2 * i]);
+                st4(&w.nxt.ang[P.body[P.slot[t].y]], sv[2 * i + 1]);
+            }
         }
     }
 }
@@ -359,18 +447,85 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
         return;
     }
 
-    // ---- 0. ranks 1..: the manifold flags the front reads ----
-    // (manifolds interleaved over the ranks: a few hundred manifolds spread
-    // over all seven SMs, whose scattered loads are what costs time)
-    const uint32_t pfirst = rank - 1 + (kClusterRanks - 1) * tid, pstride = (kClusterRanks - 1) * nt;
-    if (rank != 0)
-        for (uint32_t m = pfirst; m < M; m += pstride) sb.dyn[m] = manifoldFlags(a, m);
-    __threadfence();
-    cluster.sync();
-
-    // ---- 1. rank 0: slots, colours, order; ranks 1..: prepare ----
+    // ---- 0. all ranks: manifold flags, island sets, prepare ----
+    // (manifolds spread over all SMs: their scattered loads are what costs time)
+    const uint32_t g = tid * kClusterRanks + rank, G = kClusterRanks * nt;  // consecutive manifolds: other SMs
+    uint32_t *par = reinterpret_cast<uint32_t *>(sb.bodyUsed);  // island parent of a body
+    uint32_t *icnt = par + w.nb;                                 // manifolds of an island, at its root
+    if (g == 0) sb.counters[2] = 0;                              // island path refused
+    for (uint32_t m = g; m < M; m += G) {
+        const uint32_t fl = manifoldFlags(a, m);
+        sb.dyn[m] = fl;
+        if (fl & kFlagValid) {
+            const uint32_t ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
+            if (fl & kFlagDynA) {
+                par[ba] = ba;
+                icnt[ba] = 0;
+            }
+            if (fl & kFlagDynB) {
+                par[bb] = bb;
+                icnt[bb] = 0;
+            }
+        }
+    }
     unsigned long long *s_sort = reinterpret_cast<unsigned long long *>(smem);
     uint32_t *s_dyn = reinterpret_cast<uint32_t *>(smem + (size_t)lay.blockM * 8);
+    {
+        // old cache keys in this rank's shared memory when they fit
+        const uint32_t cacheN = *a.oldCount;
+        const bool keysInShared = (size_t)cacheN * 8 <= lay.smemBytes;
+        if (keysInShared)
+            for (uint32_t i = tid; i < cacheN; i += nt) s_sort[i] = a.oldCache.key[i];
+        __syncthreads();
+        prepareRange(a, g, G, M, keysInShared ? s_sort : nullptr);
+    }
+    __threadfence();
+    cluster.sync();
+    // ---- 1. islands: union of the two dynamic bodies of every solved manifold ----
+    for (uint32_t m = g; m < M; m += G) {
+        const uint32_t fl = __ldcg(&sb.dyn[m]);
+        if ((fl & (kFlagValid | kFlagDynA | kFlagDynB)) == (kFlagValid | kFlagDynA | kFlagDynB))
+            if (!islandUnite(par, a.mv.bodyA[m], a.mv.bodyB[m])) atomicOr(&sb.counters[2], 1u);
+    }
+    __threadfence();
+    cluster.sync();
+    // ---- 2. each solved manifold joins its island's list; the first to join
+    // owns the island (M <= blockM <= threads of the cluster: one manifold per
+    // thread) ----
+    uint32_t ownRoot = kNoIsland;
+    for (uint32_t m = g; m < M; m += G) {
+        const uint32_t fl = __ldcg(&sb.dyn[m]);
+        if (!(fl & kFlagValid)) {
+            // an unsolved manifold that still shapes the colouring: colour-phase path
+            if (fl & (kFlagDynA | kFlagDynB)) atomicOr(&sb.counters[2], 1u);
+            continue;
+        }
+        if (!(fl & (kFlagDynA | kFlagDynB))) {
+            atomicOr(&sb.counters[2], 1u);  // solved manifold without a dynamic body
+            continue;
+        }
+        const uint32_t r = islandFind(par, (fl & kFlagDynA) ? a.mv.bodyA[m] : a.mv.bodyB[m]);
+        const uint32_t pos = atomicAdd(&icnt[r], 1u);
+        if (pos < kIslandMax) sb.islandList[(size_t)r * kIslandMax + pos] = m;
+        else atomicOr(&sb.counters[2], 1u);
+        if (pos == 0) ownRoot = r;
+    }
+    __threadfence();
+    cluster.sync();
+    // The island path needs the cache in manifold order (one manifold per body
+    // pair): a cache sorted over the solve order needs the order, which only
+    // the colour-phase path materialises.
+    if (__ldcg(&sb.counters[2]) == 0 && G >= M && a.pairOrderCache) {
+        // ---- island path ----
+        if (g == 0) atomicMax(&a.st->colorRounds, 1u);  // one round when nothing is coloured
+        solveIslandsRank(a, lay, smem, ownRoot, cs.island);
+        __threadfence();
+        cluster.sync();
+        solveClusterCache(a, nc, cacheCap, newCount, M, rank, smem, s_sort, s_dyn, cs);
+        return;
+    }
+
+    // ---- colour-phase path: rank 0 assigns slots, colours and orders ----
     if (rank == 0) {
         VelStage vs;
         vs.slot = reinterpret_cast<uint2 *>(smem + (size_t)lay.blockM * 12);
@@ -382,23 +537,10 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
             for (uint32_t k = tid; k < M; k += nt) sb.stageSlot[k] = vs.slot[k];
             for (uint32_t sl = tid; sl < cs.solve.slots; sl += nt) sb.stageBody[sl] = vs.slotBody[sl];
         }
-        bool islands = false;
-        if (slotted)
-            islands = islandFront(a, M, cs.solve.slots, s_dyn, vs.slot, reinterpret_cast<uint32_t *>(vs.v), vs.cap,
-                                  reinterpret_cast<uint32_t *>(s_sort), lay, cs);
         if (tid == 0) {
             sb.counters[0] = slotted ? cs.solve.slots : 0u;
             sb.counters[1] = slotted ? 1u : 0u;
-            sb.counters[2] = islands ? 1u : 0u;
         }
-    } else {
-        // old cache keys in this rank's shared memory when they fit
-        const uint32_t cacheN = *a.oldCount;
-        const bool keysInShared = (size_t)cacheN * 8 <= lay.smemBytes;
-        if (keysInShared)
-            for (uint32_t i = tid; i < cacheN; i += nt) s_sort[i] = a.oldCache.key[i];
-        __syncthreads();
-        prepareRange(a, pfirst, pstride, M, keysInShared ? s_sort : nullptr);
     }
     __threadfence();
     cluster.sync();
@@ -407,7 +549,6 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
     if (tid == 0) {
         cs.slotted = __ldcg(&sb.counters[1]);
         cs.slots = __ldcg(&sb.counters[0]);
-        cs.islands = __ldcg(&sb.counters[2]);
         const uint32_t C = min(__ldcg(&a.st->colors), (uint32_t)kMaxColors);
         cs.colors = C;
         uint32_t acc = 0, lacc = 0;
@@ -438,14 +579,6 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
     uint32_t *sm = reinterpret_cast<uint32_t *>(smem + lay.offM);
     uint32_t *scnt = reinterpret_cast<uint32_t *>(smem + lay.offCnt);
     uint32_t *soff = reinterpret_cast<uint32_t *>(smem + lay.offOff);
-    if (cs.islands) {
-        solveIslands(a, lay, rank, cs.slots, sv, spm, spn, spt, sslot, sm, scnt, soff,
-                     reinterpret_cast<uint32_t *>(smem + lay.offScan), cs);
-        __threadfence();
-        cluster.sync();
-        solveClusterCache(a, nc, cacheCap, newCount, M, rank, smem, s_sort, s_dyn, cs);
-        return;
-    }
     const uint32_t C = cs.colors, Lr = cs.lstart[C], S = cs.slots;
     if (Lr > lay.localCap) {  // cannot happen: localCap covers blockM / R + one per colour
         if (tid == 0) atomicOr(&a.st->err, kErrSmallPath);
@@ -535,11 +668,12 @@ ClusterSolveLayout clusterSolveLayout(uint32_t blockM, uint32_t stageSlots) {
         off += (bytes + 15) & ~(size_t)15;
         return (uint32_t)o;
     };
-    // the velocity area holds this rank's slice (colour-phase path) or every
-    // staged slot (island path)
-    l.islandSlots = stageSlots < 2048u ? stageSlots : 2048u;
-    l.offVel = take((size_t)(velSlots > l.islandSlots ? velSlots : l.islandSlots) * 32);
-    l.offScan = take((size_t)kBlockSolveThreads * 4);
+    // the velocity area: this rank's slice of the staged velocities (colour-
+    // phase path) or the islands' body velocities, unit lane maps and colours
+    // (island path)
+    l.islandBodies = 2 * l.localCap;
+    const size_t islandArea = (size_t)l.islandBodies * 32 + (kIslandUnits * 32 + kIslandUnits) * 4 + (size_t)l.localCap * 4;
+    l.offVel = take(std::max<size_t>((size_t)velSlots * 32, islandArea));
     l.offPm = take((size_t)l.localCap * 16);
     l.offPn = take((size_t)l.localCap * 16);
     l.offSlot = take((size_t)l.localCap * 8);

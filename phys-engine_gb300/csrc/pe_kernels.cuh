@@ -25,6 +25,13 @@ __device__ __forceinline__ void aggregatedAdd64(unsigned long long *counter, uns
     if (g.thread_rank() == 0 && s) atomicAdd(counter, s);
 }
 
+__device__ __forceinline__ void aggregatedAdd32(uint32_t *counter, uint32_t v) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    const uint32_t s = cg::reduce(g, v, cg::plus<uint32_t>());
+    if (g.thread_rank() == 0 && s) atomicAdd(counter, s);
+}
+
 // Adds 1 to counters[key] once per group of converged lanes sharing the key.
 __device__ __forceinline__ void aggregatedCount(unsigned long long *counters, uint32_t key) {
     const uint32_t active = __activemask();

@@ -98,38 +98,49 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
     const float inverseDt = 1.0f / smax(w.dt, 1e-6f);
     const uint32_t cacheN = *a.oldCount;
     uint64_t prepared = 0, comparisons = 0, matches = 0;
+    uint32_t solved = 0;
     for (uint32_t m = begin; m < M; m += stride) {
         const uint32_t k = m;  // data index
+        // Everything indexed by m is requested at once, and the bodies' data
+        // with the validity check (indices clamped to a live array entry), so
+        // a one-point manifold costs three dependent memory round trips:
+        // manifold, bodies, warm-start cache.
         const uint32_t ia = a.mv.bodyA[m], ib = a.mv.bodyB[m];
+        const uint32_t gA = a.mv.genA[m], gB = a.mv.genB[m];
         const float4 nf = a.mv.normalFriction[m];
+        const uint32_t npts = a.mv.pointCount[m];
+        const float rest = a.mv.restitution[m];
+        const float4 aa0 = a.mv.anchorA[4 * m], ab0 = a.mv.anchorB[4 * m], imp0 = a.mv.impulse[4 * m];
+        const uint32_t ca = ia < w.nb ? ia : 0u, cb = ib < w.nb ? ib : 0u;
+        const uint32_t flA = w.bflags[ca], flB = w.bflags[cb], bgA = w.bgen[ca], bgB = w.bgen[cb];
+        const float imA = w.mat[ca].x, imB = w.mat[cb].x;
+        const float4 iA = w.iinv[ca], iB = w.iinv[cb];
+        const float4 qA4 = w.cur.rot[ca], qB4 = w.cur.rot[cb];
+        const float4 lA4 = w.nxt.lin[ca], aA4 = w.nxt.ang[ca], lB4 = w.nxt.lin[cb], aB4 = w.nxt.ang[cb];
         const V3 n{nf.x, nf.y, nf.z};
         // A manifold whose body handles are stale is not solved and not cached
         // (sequential_impulse_solver.cpp:317-320).
-        const bool valid = ia < w.nb && ib < w.nb && (w.bflags[ia] & kBodyAlive) && (w.bflags[ib] & kBodyAlive) &&
-                           w.bgen[ia] == a.mv.genA[m] && w.bgen[ib] == a.mv.genB[m];
+        const bool valid = ia < w.nb && ib < w.nb && (flA & kBodyAlive) && (flB & kBodyAlive) && bgA == gA &&
+                           bgB == gB;
         a.sb.pbody[k] = make_uint2(valid ? ia : 0u, valid ? ib : 0u);
         if (!valid) {
             a.sb.pcount[k] = 0;
             a.sb.pm[k] = make_float4(0.0f, 1.0f, 0.0f, 1.0f);
             a.sb.pn[k] = nf;
             for (uint32_t p = 0; p < 4; ++p) {
-                float4 imp = a.mv.impulse[4 * m + p];
+                float4 imp = p == 0 ? imp0 : a.mv.impulse[4 * m + p];
                 imp.w = 0.0f;
                 a.sb.pimp[(size_t)p * mcap + k] = imp;
             }
             continue;
         }
-        aggregatedAppend(&a.st->solved);
-        const uint32_t npts = a.mv.pointCount[m];
-        const float rest = a.mv.restitution[m];
-        const bool sA = (w.bflags[ia] & kBodyStatic) != 0, sB = (w.bflags[ib] & kBodyStatic) != 0;
-        const float imA = w.mat[ia].x, imB = w.mat[ib].x;
-        const float4 iA = w.iinv[ia], iB = w.iinv[ib];
-        const Q qA = f4q(w.cur.rot[ia]), qB = f4q(w.cur.rot[ib]);
+        ++solved;
+        const bool sA = (flA & kBodyStatic) != 0, sB = (flB & kBodyStatic) != 0;
+        const Q qA = f4q(qA4), qB = f4q(qB4);
         const M3 IA = inverseInertiaWorld(qA, iA.x, iA.y, iA.z);
         const M3 IB = inverseInertiaWorld(qB, iB.x, iB.y, iB.z);
-        const V3 linA = f4xyz(w.nxt.lin[ia]), angA = f4xyz(w.nxt.ang[ia]);
-        const V3 linB = f4xyz(w.nxt.lin[ib]), angB = f4xyz(w.nxt.ang[ib]);
+        const V3 linA = f4xyz(lA4), angA = f4xyz(aA4);
+        const V3 linB = f4xyz(lB4), angB = f4xyz(aB4);
         a.sb.pm[k] = make_float4(imA, sA ? 1.0f : 0.0f, imB, sB ? 1.0f : 0.0f);
         a.sb.pmInertia[0 * mcap + k] = make_float4(IA.m00, IA.m01, IA.m02, 0.0f);
         a.sb.pmInertia[1 * mcap + k] = make_float4(IA.m10, IA.m11, IA.m12, 0.0f);
@@ -138,9 +149,10 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
         a.sb.pmInertia[4 * mcap + k] = make_float4(IB.m10, IB.m11, IB.m12, 0.0f);
         a.sb.pmInertia[5 * mcap + k] = make_float4(IB.m20, IB.m21, IB.m22, 0.0f);
 
-        // Cache range for (bodyA, bodyB); generations must match.
+        // Cache range for (bodyA, bodyB); generations must match.  The range's
+        // first entry is requested with its generations.
         const unsigned long long key = ((unsigned long long)ia << 32) | ib;
-        const unsigned long long gens = ((unsigned long long)a.mv.genA[m] << 32) | a.mv.genB[m];
+        const unsigned long long gens = ((unsigned long long)gA << 32) | gB;
         uint32_t lo = 0, hi = cacheN;
         while (lo < hi) {
             uint32_t mid = (lo + hi) >> 1;
@@ -149,16 +161,25 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
         }
         uint32_t rb = lo, re = lo;
         while (re < cacheN && cacheKeys[re] == key) ++re;
-        if (rb < re && a.oldCache.gens[rb] != gens) re = rb;
+        float4 c0a = make_float4(0, 0, 0, 0), c0b = make_float4(0, 0, 0, 0);
+        float c0t = 0.0f;
+        if (rb < re) {
+            const unsigned long long g0 = a.oldCache.gens[rb];
+            c0a = a.oldCache.anchorA[rb];
+            c0b = a.oldCache.anchorB[rb];
+            c0t = a.oldCache.tangent2[rb];
+            if (g0 != gens) re = rb;
+        }
 
         const float matchSq = 0.05f * 0.05f;
         for (uint32_t p = 0; p < 4; ++p) {
             float4 out[kPreparedVec4];
             for (int v = 0; v < kPreparedVec4; ++v) out[v] = make_float4(0, 0, 0, 0);
-            float4 imp = a.mv.impulse[4 * m + p];
+            float4 imp = p == 0 ? imp0 : a.mv.impulse[4 * m + p];
             imp.w = 0.0f;
             if (p < npts) {
-                const float4 aa = a.mv.anchorA[4 * m + p], ab = a.mv.anchorB[4 * m + p];
+                const float4 aa = p == 0 ? aa0 : a.mv.anchorA[4 * m + p];
+                const float4 ab = p == 0 ? ab0 : a.mv.anchorB[4 * m + p];
                 const V3 anchorA{aa.x, aa.y, aa.z}, anchorB{ab.x, ab.y, ab.z};
                 const float penetration = aa.w;
                 V3 offA = rotate(qA, anchorA), offB = rotate(qB, anchorB);
@@ -213,10 +234,11 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
                     if (!(iem <= 0.0f)) {
                         for (uint32_t c = rb; c < re; ++c) {
                             ++comparisons;
-                            const float4 ca = a.oldCache.anchorA[c], cb = a.oldCache.anchorB[c];
+                            const float4 ca = c == rb ? c0a : a.oldCache.anchorA[c];
+                            const float4 cb = c == rb ? c0b : a.oldCache.anchorB[c];
                             V3 da = V3{ca.x, ca.y, ca.z} - anchorA, db = V3{cb.x, cb.y, cb.z} - anchorB;
                             if (dot(da, da) > matchSq || dot(db, db) > matchSq) continue;
-                            const float t2c = a.oldCache.tangent2[c];
+                            const float t2c = c == rb ? c0t : a.oldCache.tangent2[c];
                             float ni = smax(ca.w, 0.0f);
                             float limit = smax(nf.w, 0.0f) * ni;
                             float tlsq = cb.w * cb.w + t2c * t2c;
@@ -234,6 +256,7 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
         a.sb.pn[k] = nf;
         a.sb.pcount[k] = npts;
     }
+    aggregatedAdd32(&a.st->solved, solved);
     aggregatedAdd64(&a.st->preparedPoints, prepared);
     aggregatedAdd64(&a.st->warmComparisons, comparisons);
     aggregatedAdd64(&a.st->warmMatches, matches);

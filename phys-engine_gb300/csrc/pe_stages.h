@@ -75,13 +75,12 @@ struct SolverBuffers {
     uint32_t *cacheCounts, *cacheOff;
     uint32_t *bar;                  // grid barrier [2]
     uint32_t *counters;             // [4]
-    // cluster solver hand-off: staging slots by solve index, body of each slot;
-    // islands: per root slot the range of its manifolds in compList (solve
-    // indices)
+    // cluster solver: staging slots by solve index and the body of each slot
+    // (colour-phase path); the manifolds of each island, kIslandMax entries
+    // per root body (island path)
     uint2 *stageSlot;               // [mcap]
     uint32_t *stageBody;            // [2 * mcap + 64]
-    uint2 *compRange;               // [2 * mcap + 64]
-    uint32_t *compList;             // [mcap]
+    uint32_t *islandList;           // [kIslandMax * nb]
 };
 
 constexpr int kMaxColors = 128;
@@ -120,13 +119,17 @@ constexpr uint32_t kBlockMaxManifolds = 4096;
 
 // Cluster solver: ranks per cluster, dynamic shared memory per rank, and the
 // per-rank layout (byte offsets into the dynamic shared memory).
+// Islands (manifolds joined by shared dynamic bodies) of at most this many
+// manifolds are solved by one thread each; a larger one sends the step to the
+// colour-phase path.
+constexpr uint32_t kIslandMax = 16;
 constexpr uint32_t kClusterRanks = 8;
 constexpr uint32_t kClusterSmemMax = 224 * 1024;
 struct ClusterSolveLayout {
     uint32_t blockM, stageSlots;   // capacities of the single-block front (rank 0)
     uint32_t localCap, pointCap;   // manifolds / prepared points held per rank
-    uint32_t islandSlots;          // staging slots the island path holds per rank
-    uint32_t offVel, offScan, offPm, offPn, offSlot, offM, offCnt, offOff, offPt;
+    uint32_t islandBodies;         // island path: body slots per rank
+    uint32_t offVel, offPm, offPn, offSlot, offM, offCnt, offOff, offPt;
     uint32_t smemBytes;
 };
 constexpr uint32_t kBlockMaxBodies = 1u << 20;

@@ -368,8 +368,7 @@ void World::ensureCapacity() {
     sCounters_.reserve(4);
     sStageSlot_.reserve(m);
     sStageBody_.reserve(2 * (size_t)m + 64);
-    sCompRange_.reserve(2 * (size_t)m + 64);
-    sCompList_.reserve(m);
+    sIslandList_.reserve((size_t)kIslandMax * nb);
     sb_ = SolverBuffers{m,
                         sBest_.ptr,
                         sUsed_.ptr,
@@ -398,8 +397,7 @@ void World::ensureCapacity() {
                         sCounters_.ptr,
                         sStageSlot_.ptr,
                         sStageBody_.ptr,
-                        sCompRange_.ptr,
-                        sCompList_.ptr};
+                        sIslandList_.ptr};
 
     // Warm-start caches keep their contents when they grow.
     const uint32_t needCache = 4 * m;
@@ -882,12 +880,25 @@ void World::downloadManifolds(void *records, uint32_t count) {
 void World::downloadOrder(uint32_t *order, uint32_t *colors) {
     const uint32_t M = lastManifolds_;
     if (!M) return;
-    if (order) PE_CHECK(cudaMemcpy(order, sOrder_.ptr, M * 4, cudaMemcpyDeviceToHost));
-    if (colors) {
-        if (orderMode == 0)
-            for (uint32_t m = 0; m < M; ++m) colors[m] = m;
-        else
-            PE_CHECK(cudaMemcpy(colors, sColor_.ptr, M * 4, cudaMemcpyDeviceToHost));
+    if (orderMode == 0) {
+        for (uint32_t m = 0; m < M; ++m) {
+            if (order) order[m] = m;
+            if (colors) colors[m] = m;
+        }
+        return;
+    }
+    // The solve order is (colour, manifold index); the island solver does not
+    // materialise it, so it is derived from the colours here.
+    std::vector<uint32_t> c(M);
+    PE_CHECK(cudaMemcpy(c.data(), sColor_.ptr, M * 4, cudaMemcpyDeviceToHost));
+    if (colors) std::memcpy(colors, c.data(), M * 4);
+    if (order) {
+        uint32_t C = 0;
+        for (uint32_t v : c) C = std::max(C, v + 1);
+        std::vector<uint32_t> start(C + 1, 0);
+        for (uint32_t v : c) ++start[v + 1];
+        for (uint32_t k = 0; k < C; ++k) start[k + 1] += start[k];
+        for (uint32_t m = 0; m < M; ++m) order[start[c[m]]++] = m;
     }
 }
 

@@ -212,9 +212,9 @@ class World {
     SolverBuffers sb_{};
     DeviceArray<unsigned long long> sBest_, sUsed_, sEpoch_, sCacheKeys_, sCacheKeysTmp_;
     DeviceArray<uint32_t> sColor_, sDyn_, sColorCount_, sOrderKeys_, sOrderKeysTmp_, sOrder_, sOrderTmp_, sPcount_,
-        sCacheVals_, sCacheValsTmp_, sCacheCounts_, sCacheOff_, sBar_, sCounters_, sStageBody_, sCompList_;
+        sCacheVals_, sCacheValsTmp_, sCacheCounts_, sCacheOff_, sBar_, sCounters_, sStageBody_, sIslandList_;
     DeviceArray<float4> sPm_, sPmI_, sPp_, sPimp_, sPn_;
-    DeviceArray<uint2> sPbody_, sStageSlot_, sCompRange_;
+    DeviceArray<uint2> sPbody_, sStageSlot_;
     // warm-start caches (two copies)
     DeviceArray<unsigned long long> cKey_[2], cGens_[2];
     DeviceArray<float4> cA_[2], cB_[2];
