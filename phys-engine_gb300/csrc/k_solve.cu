@@ -158,11 +158,12 @@ __global__ void k_solve_serial(SolveArgs a) {
         for (uint32_t k = 0; k < M; ++k) solveOne(a, k, k);
 }
 
-// Solved impulses back to the manifolds (pair order).
+// Solved impulses of the live points back to the manifolds (pair order).
 __global__ void k_impulses_out(SolveArgs a) {
     const uint32_t M = min(a.st->manifolds, a.mcap);
     for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
-        for (uint32_t p = 0; p < 4; ++p) {
+        const uint32_t live = a.sb.pcount[m];
+        for (uint32_t p = 0; p < live; ++p) {
             float4 imp = a.sb.pimp[(size_t)p * a.mcap + m];
             imp.w = 0.0f;
             a.mv.impulse[4 * m + p] = imp;

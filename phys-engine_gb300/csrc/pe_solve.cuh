@@ -127,12 +127,7 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
             a.sb.pcount[k] = 0;
             a.sb.pm[k] = make_float4(0.0f, 1.0f, 0.0f, 1.0f);
             a.sb.pn[k] = nf;
-            for (uint32_t p = 0; p < 4; ++p) {
-                float4 imp = p == 0 ? imp0 : a.mv.impulse[4 * m + p];
-                imp.w = 0.0f;
-                a.sb.pimp[(size_t)p * mcap + k] = imp;
-            }
-            continue;
+            continue;  // no live points: nothing is solved or written back
         }
         ++solved;
         const bool sA = (flA & kBodyStatic) != 0, sB = (flB & kBodyStatic) != 0;
@@ -172,7 +167,10 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
         }
 
         const float matchSq = 0.05f * 0.05f;
-        for (uint32_t p = 0; p < 4; ++p) {
+        // live points only: the sweeps, the impulses written back and the
+        // cache read no other
+        const uint32_t live = npts < 4u ? npts : 4u;
+        for (uint32_t p = 0; p < live; ++p) {
             float4 out[kPreparedVec4];
             for (int v = 0; v < kPreparedVec4; ++v) out[v] = make_float4(0, 0, 0, 0);
             float4 imp = p == 0 ? imp0 : a.mv.impulse[4 * m + p];
@@ -254,7 +252,7 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
             a.sb.pimp[(size_t)p * mcap + k] = imp;
         }
         a.sb.pn[k] = nf;
-        a.sb.pcount[k] = npts;
+        a.sb.pcount[k] = live;
     }
     aggregatedAdd32(&a.st->solved, solved);
     aggregatedAdd64(&a.st->preparedPoints, prepared);
@@ -834,9 +832,10 @@ __device__ inline void solveBlockSweeps(const SolveArgs &a, uint32_t M, int seri
         }
         __syncthreads();
     }
-    // --- impulses back to the manifolds ---
+    // --- impulses of the live points back to the manifolds ---
     for (uint32_t m = tid; m < M; m += nt) {
-        for (uint32_t p = 0; p < 4; ++p) {
+        const uint32_t live = sb.pcount[m];
+        for (uint32_t p = 0; p < live; ++p) {
             float4 imp = sb.pimp[(size_t)p * a.mcap + m];
             imp.w = 0.0f;
             a.mv.impulse[4 * m + p] = imp;

@@ -1001,6 +1001,8 @@ void World::solveOnly(std::vector<float> &recs, uint32_t count, float dt, int it
         ga[m] = r[m].aGen;
         bbv[m] = r[m].bIdx;
         gb[m] = r[m].bGen;
+        // a ContactManifold holds at most four points (manifold.hpp:21-34)
+        if (r[m].pointCount > 4) throw std::invalid_argument("a contact manifold holds at most 4 points");
         cnt[m] = r[m].pointCount;
         nf[m] = make_float4(r[m].normal[0], r[m].normal[1], r[m].normal[2], r[m].friction);
         rest[m] = r[m].restitution;
