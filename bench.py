@@ -318,8 +318,9 @@ def run_gpu(args, rank, world_size, local_rank):
                            "frac": step_bytes / (max_ms / 1000.0) / 1e9 / world_size / peak},
         },
         "workload_per_step": {k: v / args.steps for k, v in totals.items()},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 16 * scene.count,
-                "d2h_bytes_per_step": 32 * scene.count, "steps": e2e_steps},
+        # forces in: 3 floats per body; poses out: 3 + 4 floats per body
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * scene.count,
+                "d2h_bytes_per_step": 28 * scene.count, "steps": e2e_steps},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }

@@ -84,6 +84,38 @@ __global__ void k_integrate_pose(WorldView w) {
     w.nxt.rot[i] = q4;
 }
 
+// Caller forces (3 floats per body) into the force array; RigidBody::applyForce
+// ignores static bodies (rigid_body.cpp), dead slots get none.
+__global__ void k_expand_forces(const float *f3, const uint32_t *bflags, float4 *force, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t fl = bflags[i];
+    const bool dyn = (fl & kBodyAlive) && !(fl & kBodyStatic);
+    force[i] = dyn ? make_float4(f3[3 * i], f3[3 * i + 1], f3[3 * i + 2], 0.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+// Positions as 3 floats per body (the caller's layout).
+__global__ void k_pack_positions(const float4 *pos, float *p3, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = pos[i];
+    p3[3 * i] = p.x;
+    p3[3 * i + 1] = p.y;
+    p3[3 * i + 2] = p.z;
+}
+
+void launchExpandForces(const float *f3, const uint32_t *bflags, float4 *force, uint32_t n, cudaStream_t s) {
+    if (!n) return;
+    k_expand_forces<<<(n + 255) / 256, 256, 0, s>>>(f3, bflags, force, n);
+    PE_LAUNCHED();
+}
+
+void launchPackPositions(const float4 *pos, float *p3, uint32_t n, cudaStream_t s) {
+    if (!n) return;
+    k_pack_positions<<<(n + 255) / 256, 256, 0, s>>>(pos, p3, n);
+    PE_LAUNCHED();
+}
+
 void launchIntegrateAabb(const WorldView &w, uint32_t *sapKeys, uint32_t *sapVals, DevStats *st,
                          uint32_t inputCount, cudaStream_t s) {
     uint32_t n = w.nb > w.nc ? w.nb : w.nc;

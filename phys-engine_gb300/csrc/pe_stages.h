@@ -97,6 +97,10 @@ void launchCollect(const WorldView &w, uint32_t *flags, uint32_t *pos, float4 *i
                    uint32_t *sapKeys, uint32_t *sapVals, uint32_t *d_count, Scratch &ws, uint32_t *d_err,
                    cudaStream_t s);
 void launchIntegratePose(const WorldView &w, cudaStream_t s);
+// Host-facing transfers: caller forces (3 floats per body) into the force
+// array with static / dead bodies masked; positions packed to 3 floats.
+void launchExpandForces(const float *f3, const uint32_t *bflags, float4 *force, uint32_t n, cudaStream_t s);
+void launchPackPositions(const float4 *pos, float *p3, uint32_t n, cudaStream_t s);
 void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, BroadBuffers &bb, PairBuffers &pb,
                DevStats *st, Scratch &ws, cudaStream_t s);
 void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBuffers &pb, DevStats *st, Scratch &ws,

@@ -762,14 +762,13 @@ void World::writeForces(const float *forces, uint32_t n) {
         push();
     }
     n = std::min<uint32_t>(n, nb_);
-    float4 *stage = pinnedBuffer(std::max<uint32_t>(n, 1));
-    for (uint32_t i = 0; i < n; ++i) {
-        const bool dyn = bodies[i].alive && !bodies[i].isStatic;  // applyForce ignores static bodies
-        stage[i] = dyn ? make_float4(forces[3 * i], forces[3 * i + 1], forces[3 * i + 2], 0.0f)
-                       : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (n) {
+        // the caller's array as it is; static and dead bodies masked on the device
+        xfer3_.reserve(3 * (size_t)nb_);
+        PE_CHECK(cudaMemcpyAsync(xfer3_.ptr, forces, 3 * (size_t)n * sizeof(float), cudaMemcpyHostToDevice, stream_));
+        launchExpandForces(xfer3_.ptr, bflags_.ptr, force_.ptr, n, stream_);
     }
-    if (n) PE_CHECK(cudaMemcpyAsync(force_.ptr, stage, n * sizeof(float4), cudaMemcpyHostToDevice, stream_));
-    PE_CHECK(cudaStreamSynchronize(stream_));
+    PE_CHECK(cudaStreamSynchronize(stream_));  // the caller may reuse its array on return
     forces_ = true;
 }
 
@@ -779,25 +778,19 @@ void World::readPoses(float *positions, float *rotations) {
         pull();
         push();
     }
-    float4 *stage = pinnedBuffer(2 * (size_t)std::max<uint32_t>(nb_, 1));
     if (nb_) {
-        PE_CHECK(cudaMemcpyAsync(stage, pos_[cur_].ptr, nb_ * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
-        PE_CHECK(cudaMemcpyAsync(stage + nb_, rot_[cur_].ptr, nb_ * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
-        PE_CHECK(cudaStreamSynchronize(stream_));
-    }
-    for (uint32_t i = 0; i < nb_; ++i) {
+        // positions packed to the caller's 3 floats on the device; rotations
+        // are already 4 floats per body
         if (positions) {
-            positions[3 * i] = stage[i].x;
-            positions[3 * i + 1] = stage[i].y;
-            positions[3 * i + 2] = stage[i].z;
+            xfer3_.reserve(3 * (size_t)nb_);
+            launchPackPositions(pos_[cur_].ptr, xfer3_.ptr, nb_, stream_);
+            PE_CHECK(cudaMemcpyAsync(positions, xfer3_.ptr, 3 * (size_t)nb_ * sizeof(float), cudaMemcpyDeviceToHost,
+                                     stream_));
         }
-        if (rotations) {
-            const float4 &q = stage[nb_ + i];
-            rotations[4 * i] = q.x;
-            rotations[4 * i + 1] = q.y;
-            rotations[4 * i + 2] = q.z;
-            rotations[4 * i + 3] = q.w;
-        }
+        if (rotations)
+            PE_CHECK(cudaMemcpyAsync(rotations, rot_[cur_].ptr, (size_t)nb_ * sizeof(float4), cudaMemcpyDeviceToHost,
+                                     stream_));
+        PE_CHECK(cudaStreamSynchronize(stream_));
     }
 }
 

@@ -263,3 +263,24 @@ def test_pair_buffer_growth(gpu):
         ow.step(1 / 60)
         compare_worlds(gw, ow, f"step {s}")
     assert gw.stats()["candidate_pairs"] > 65536
+
+
+def test_world_read_poses_matches_bodies(gpu):
+    """read_poses (positions packed on the device, rotations copied as they
+    are) returns the state pe_world_read_bodies reports, and forces written
+    through write_forces reach dynamic bodies only."""
+    sc = scenes.generate(scenes.SPHERES_ON_FLOOR, 60, 3)
+    gw = gpu.GpuWorld(order=gpu.ORDER_COLOR)
+    gw.load_scene(sc)
+    rng = np.random.default_rng(4)
+    for _ in range(5):
+        gw.write_forces(rng.normal(size=(sc.count, 3)).astype(np.float32) * 20)
+        gw.step(1 / 60)
+    pos = np.zeros((sc.count, 3), np.float32)
+    rot = np.zeros((sc.count, 4), np.float32)
+    gw.read_poses(pos, rot)
+    b = gw.bodies()
+    assert_bit_equal(pos, b["pos"], "read_poses positions")
+    assert_bit_equal(rot, b["quat"], "read_poses rotations")
+    static = sc.is_static.astype(bool)
+    assert np.all(b["lin"][static] == 0)
