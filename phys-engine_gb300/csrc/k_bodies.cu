@@ -13,11 +13,13 @@
 namespace pe {
 
 // st (nullable): the step's counters are initialised here as well, which saves
-// a launch at the head of the step.
+// a launch at the head of the step; so is clearing `fill` (nFill words set to
+// all ones: the hashed grid's empty bucket lists), which saves a memset node.
 __global__ void k_integrate_aabb(WorldView w, uint32_t *sapKeys, uint32_t *sapVals, DevStats *st,
-                                 uint32_t inputCount) {
+                                 uint32_t inputCount, uint32_t *fill, uint32_t nFill) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (st && i == 0) initStepStats(st, inputCount);
+    for (uint32_t j = i; j < nFill; j += gridDim.x * blockDim.x) fill[j] = 0xFFFFFFFFu;
     if (i < w.nb) {
         const uint32_t f = w.bflags[i];
         V3 lin = f4xyz(w.cur.lin[i]);
@@ -117,13 +119,14 @@ void launchPackPositions(const float4 *pos, float *p3, uint32_t n, cudaStream_t 
 }
 
 void launchIntegrateAabb(const WorldView &w, uint32_t *sapKeys, uint32_t *sapVals, DevStats *st,
-                         uint32_t inputCount, cudaStream_t s) {
+                         uint32_t inputCount, cudaStream_t s, uint32_t *fill, uint32_t nFill) {
     uint32_t n = w.nb > w.nc ? w.nb : w.nc;
     if (!n) {
         if (st) launchStepInit(st, inputCount, s);
+        if (nFill) PE_CHECK(cudaMemsetAsync(fill, 0xFF, nFill * sizeof(uint32_t), s));
         return;
     }
-    k_integrate_aabb<<<(n + 255) / 256, 256, 0, s>>>(w, sapKeys, sapVals, st, inputCount);
+    k_integrate_aabb<<<(n + 255) / 256, 256, 0, s>>>(w, sapKeys, sapVals, st, inputCount, fill, nFill);
     PE_LAUNCHED();
 }
 

@@ -464,9 +464,12 @@ __device__ __forceinline__ bool cellFloorFast(float x, float invf, int &cellOut)
 __global__ void __launch_bounds__(256)
 k_hgrid_insert(BroadInput in, DevStats *st, int4 *firstCell, uint8_t *inGrid, uint32_t *overflow, double cell,
                float inv, uint32_t *bucketHead, uint32_t logB, unsigned long long *keys, uint32_t *vals,
-               uint32_t *next, uint32_t ecap) {
+               uint32_t *next, uint32_t ecap, unsigned long long *zeroState, uint32_t nZeroState) {
     __shared__ uint32_t s_scan[9], s_base;
     const uint32_t n = *in.d_n;
+    // look-back states of the kernels that follow (cleared here, not by memsets)
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nZeroState; j += gridDim.x * blockDim.x)
+        zeroState[j] = 0ull;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->cellSize = cell;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
@@ -707,10 +710,11 @@ k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const
 }
 
 void launchGridBodyPairs(const BroadInput &in, const BroadBuffers &bb, PairBuffers &pb, const uint32_t *inSlot,
-                         const uint32_t *cbody, const uint32_t *cbgen, DevStats *st, Scratch &ws, cudaStream_t s) {
+                         const uint32_t *cbody, const uint32_t *cbgen, DevStats *st, Scratch &ws, cudaStream_t s,
+                         bool stateCleared) {
     uint32_t tiles = (in.maxN + kBodyPairThreads - 1) / kBodyPairThreads;
     if (tiles == 0) tiles = 1;
-    PE_CHECK(cudaMemsetAsync(ws.scanState, 0, sizeof(unsigned long long) * (tiles + 1), s));
+    if (!stateCleared) PE_CHECK(cudaMemsetAsync(ws.scanState, 0, sizeof(unsigned long long) * (tiles + 1), s));
     const uint32_t grid = tiles < 152u * 8u ? tiles : 152u * 8u;
     if (bb.hashed) {
         k_hgrid_pairs<<<grid, kBodyPairThreads, 0, s>>>(in, bb.firstCell, bb.inGrid, bb.overflow, bb.bucketHead,
@@ -817,10 +821,11 @@ void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBu
     if (bb.hashed) {
         // fixed cell size: bucket lists of the covered cells (pairs: launchGridBodyPairs)
         const uint32_t B = 1u << bb.logBuckets;
-        PE_CHECK(cudaMemsetAsync(bb.bucketHead, 0xFF, B * sizeof(uint32_t), s));
+        if (!bb.headsCleared) PE_CHECK(cudaMemsetAsync(bb.bucketHead, 0xFF, B * sizeof(uint32_t), s));
         k_hgrid_insert<<<gridFor(in.maxN), 256, 0, s>>>(in, st, bb.firstCell, bb.inGrid, bb.overflow, fixedCell,
                                                         (float)(1.0 / fixedCell), bb.bucketHead, bb.logBuckets,
-                                                        bb.entryKeys, bb.entryVals, bb.entryNext, bb.entryCap);
+                                                        bb.entryKeys, bb.entryVals, bb.entryNext, bb.entryCap,
+                                                        bb.zeroState, bb.nZeroState);
         PE_LAUNCHED();
         return;
     }

@@ -65,13 +65,14 @@ k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *_
 }
 
 void launchNarrowphase(const WorldView &w, const PairBuffers &pb, const ManifoldView &mv, uint32_t mcap, DevStats *st,
-                       Scratch &ws, cudaStream_t s) {
+                       Scratch &ws, cudaStream_t s, unsigned long long *state, bool stateCleared) {
     uint32_t tiles = (pb.cap + kNarrowThreads - 1) / kNarrowThreads;
     if (tiles == 0) tiles = 1;
-    PE_CHECK(cudaMemsetAsync(ws.scanState, 0, sizeof(unsigned long long) * (tiles + 1), s));
+    if (!state) state = ws.scanState;
+    if (!stateCleared) PE_CHECK(cudaMemsetAsync(state, 0, sizeof(unsigned long long) * (tiles + 1), s));
     const uint32_t grid = tiles < 152u * 8u ? tiles : 152u * 8u;
-    k_narrowphase<<<grid, kNarrowThreads, 0, s>>>(w, pb.a, pb.b, &st->pairs, mv, mcap, st, ws.scanState,
-                                                   (uint32_t *)(ws.scanState + tiles));
+    k_narrowphase<<<grid, kNarrowThreads, 0, s>>>(w, pb.a, pb.b, &st->pairs, mv, mcap, st, state,
+                                                   (uint32_t *)(state + tiles));
     PE_LAUNCHED();
 }
 

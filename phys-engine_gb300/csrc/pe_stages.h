@@ -36,6 +36,12 @@ struct BroadBuffers {
     // of entries; entryNext[e] links entry e to the bucket's next entry
     uint32_t *bucketHead;  // [1 << logBuckets]
     uint32_t *entryNext;   // [entryCap]
+    // set per launch by the step pipeline: the bucket heads were cleared by
+    // the integrate kernel; the insert kernel zeroes nZeroState look-back
+    // words at zeroState (the pair and narrowphase tiles' states)
+    bool headsCleared;
+    unsigned long long *zeroState;
+    uint32_t nZeroState;
     uint32_t logBuckets;
     bool hashed;
 };
@@ -92,7 +98,8 @@ void launchSetManifoldCount(DevStats *st, uint32_t count, cudaStream_t s);
 void launchSapKeys(const BroadInput &in, uint32_t *keys, uint32_t *vals, cudaStream_t s);
 // st != nullptr: also initialises the step's counters (in place of launchStepInit).
 void launchIntegrateAabb(const WorldView &w, uint32_t *sapKeys, uint32_t *sapVals, DevStats *st, uint32_t inputCount,
-                         cudaStream_t s);
+                         cudaStream_t s, uint32_t *fill = nullptr,
+                         uint32_t nFill = 0);
 void launchCollect(const WorldView &w, uint32_t *flags, uint32_t *pos, float4 *inMin, float4 *inMax, uint32_t *inSlot,
                    uint32_t *sapKeys, uint32_t *sapVals, uint32_t *d_count, Scratch &ws, uint32_t *d_err,
                    cudaStream_t s);
@@ -108,11 +115,12 @@ void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBu
 // Grid pairs emitted body by body in lexicographic order, mapped to slots and
 // filtered (replaces the per-cell pairs and the finalize when pb.bodyPath).
 void launchGridBodyPairs(const BroadInput &in, const BroadBuffers &bb, PairBuffers &pb, const uint32_t *inSlot,
-                         const uint32_t *cbody, const uint32_t *cbgen, DevStats *st, Scratch &ws, cudaStream_t s);
+                         const uint32_t *cbody, const uint32_t *cbgen, DevStats *st, Scratch &ws, cudaStream_t s,
+                         bool stateCleared = false);
 void launchPairsFinalize(const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen, PairBuffers &pb,
                          DevStats *st, Scratch &ws, cudaStream_t s);
 void launchNarrowphase(const WorldView &w, const PairBuffers &pb, const ManifoldView &mv, uint32_t mcap, DevStats *st,
-                       Scratch &ws, cudaStream_t s);
+                       Scratch &ws, cudaStream_t s, unsigned long long *state = nullptr, bool stateCleared = false);
 void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &oldCache, const uint32_t *oldCacheCount,
                   const CacheView &newCache, uint32_t *newCacheCount, uint32_t cacheCap, SolverBuffers &sb,
                   int iterations, int orderMode, int coopBlocks, bool blockPath, uint32_t blockM, bool pairOrderCache,
