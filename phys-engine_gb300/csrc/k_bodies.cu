@@ -12,14 +12,8 @@
 
 namespace pe {
 
-// st (nullable): the step's counters are initialised here as well, which saves
-// a launch at the head of the step; so is clearing `fill` (nFill words set to
-// all ones: the hashed grid's empty bucket lists), which saves a memset node.
-__global__ void k_integrate_aabb(WorldView w, uint32_t *sapKeys, uint32_t *sapVals, DevStats *st,
-                                 uint32_t inputCount, uint32_t *fill, uint32_t nFill) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (st && i == 0) initStepStats(st, inputCount);
-    for (uint32_t j = i; j < nFill; j += gridDim.x * blockDim.x) fill[j] = 0xFFFFFFFFu;
+// One body (velocity) and one collider (AABB, SAP key) of k_integrate_aabb.
+__device__ __forceinline__ void integrateAabbOne(const WorldView &w, uint32_t *sapKeys, uint32_t *sapVals, uint32_t i) {
     if (i < w.nb) {
         const uint32_t f = w.bflags[i];
         V3 lin = f4xyz(w.cur.lin[i]);
@@ -43,6 +37,24 @@ __global__ void k_integrate_aabb(WorldView w, uint32_t *sapKeys, uint32_t *sapVa
             sapKeys[i] = orderedFloatKey(mn.x);
             sapVals[i] = i;
         }
+    }
+}
+
+// st (nullable): the step's counters are initialised here as well, which saves
+// a launch at the head of the step; so is clearing `fill` (nFill words set to
+// all ones: the hashed grid's empty bucket lists), which saves a memset node.
+__global__ void k_integrate_aabb(WorldView w, uint32_t *sapKeys, uint32_t *sapVals, DevStats *st,
+                                 uint32_t inputCount, uint32_t *fill, uint32_t nFill) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (st && i == 0) {
+        initStepStats(st, inputCount);
+        st->stamp[0] = globalNs();
+    }
+    for (uint32_t j = i; j < nFill; j += gridDim.x * blockDim.x) fill[j] = 0xFFFFFFFFu;
+    integrateAabbOne(w, sapKeys, sapVals, i);
+    if (st) {
+        __syncthreads();
+        if (threadIdx.x == 0) atomicMax(&st->stamp[1], globalNs());
     }
 }
 
@@ -70,20 +82,26 @@ __global__ void k_collect_scatter(WorldView w, const uint32_t *flags, const uint
     }
 }
 
-__global__ void k_integrate_pose(WorldView w) {
+__global__ void k_integrate_pose(WorldView w, DevStats *st) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= w.nb) return;
-    const uint32_t f = w.bflags[i];
-    float4 p4 = w.cur.pos[i], q4 = w.cur.rot[i];
-    if ((f & kBodyAlive) && !(f & kBodyStatic)) {
-        V3 pos = f4xyz(p4);
-        Q rot = f4q(q4);
-        integratePose(pos, rot, f4xyz(w.nxt.lin[i]), f4xyz(w.nxt.ang[i]), w.dt);
-        p4 = make4(pos, 0.0f);
-        q4 = make4(rot);
+    if (st && i == 0) st->stamp[4] = globalNs();
+    if (i < w.nb) {
+        const uint32_t f = w.bflags[i];
+        float4 p4 = w.cur.pos[i], q4 = w.cur.rot[i];
+        if ((f & kBodyAlive) && !(f & kBodyStatic)) {
+            V3 pos = f4xyz(p4);
+            Q rot = f4q(q4);
+            integratePose(pos, rot, f4xyz(w.nxt.lin[i]), f4xyz(w.nxt.ang[i]), w.dt);
+            p4 = make4(pos, 0.0f);
+            q4 = make4(rot);
+        }
+        w.nxt.pos[i] = p4;
+        w.nxt.rot[i] = q4;
     }
-    w.nxt.pos[i] = p4;
-    w.nxt.rot[i] = q4;
+    if (st) {
+        __syncthreads();
+        if (threadIdx.x == 0) atomicMax(&st->stamp[5], globalNs());
+    }
 }
 
 // Caller forces (3 floats per body) into the force array; RigidBody::applyForce
@@ -141,9 +159,9 @@ void launchCollect(const WorldView &w, uint32_t *flags, uint32_t *pos, float4 *i
     PE_LAUNCHED();
 }
 
-void launchIntegratePose(const WorldView &w, cudaStream_t s) {
+void launchIntegratePose(const WorldView &w, cudaStream_t s, DevStats *st) {
     if (!w.nb) return;
-    k_integrate_pose<<<(w.nb + 255) / 256, 256, 0, s>>>(w);
+    k_integrate_pose<<<(w.nb + 255) / 256, 256, 0, s>>>(w, st);
     PE_LAUNCHED();
 }
 

@@ -23,6 +23,7 @@ k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *_
               const uint32_t *d_pairs, ManifoldView out, uint32_t mcap, DevStats *st, unsigned long long *state,
               uint32_t *counter) {
     __shared__ uint32_t s_tile, s_scan[9], s_prefix;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->stamp[2] = globalNs();
     const uint32_t P = min(*d_pairs, mcap);
     const uint32_t ntiles = max((P + kNarrowThreads - 1) / kNarrowThreads, 1u);
     for (;;) {
@@ -59,7 +60,10 @@ k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *_
         aggregatedAppend(&st->points);
         if (lm.count > 1) atomicAdd(&st->points, lm.count - 1);
     }
-    if (threadIdx.x == 0 && tile + 1 == ntiles) st->manifolds = s_prefix + total;
+    if (threadIdx.x == 0 && tile + 1 == ntiles) {
+        st->manifolds = s_prefix + total;
+        st->stamp[3] = globalNs();
+    }
     __syncthreads();
     }
 }

@@ -91,6 +91,12 @@ struct DevStats {
     uint32_t cellKeyBits;    // bits of the packed grid cell key this step needed
     int32_t cellLo[3];
     int32_t cellHi[3];
+    // Stage boundaries (global timer, ns), written by the stage kernels
+    // themselves instead of event nodes in the step graph: integrate start,
+    // integrate end (latest block), narrowphase start, narrowphase end (last
+    // tile), pose start, pose end (latest block).  Not cleared per step: the
+    // "latest block" entries are maxima of an increasing clock.
+    unsigned long long stamp[6];
 };
 
 struct WorldView {

@@ -41,8 +41,14 @@ __device__ __forceinline__ void aggregatedCount(unsigned long long *counters, ui
 }
 
 // Counters of a new step: all zero, the bound count, empty grid bounds.
+__device__ __forceinline__ unsigned long long globalNs() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 __device__ __forceinline__ void initStepStats(DevStats *st, uint32_t inputCount) {
-    memset(st, 0, sizeof(DevStats));
+    memset(st, 0, offsetof(DevStats, stamp));  // the stage stamps are kept
     st->inputCount = inputCount;
     for (int a = 0; a < 3; ++a) {
         st->cellLo[a] = 0x7FFFFFFF;

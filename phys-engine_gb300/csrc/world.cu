@@ -25,7 +25,6 @@ World::World(int device) : device_(device) {
     PE_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     PE_CHECK(cudaEventCreate(&evStart_));
     PE_CHECK(cudaEventCreate(&evEnd_));
-    for (auto &e : evStage_) PE_CHECK(cudaEventCreate(&e));
     PE_CHECK(cudaMallocHost(&hostStats_, sizeof(DevStats)));
     std::memset(hostStats_, 0, sizeof(DevStats));
     stats_.reserve(1);
@@ -37,8 +36,6 @@ World::~World() {
     if (stream_) cudaStreamSynchronize(stream_);
     dropGraphs();
     if (hostStats_) cudaFreeHost(hostStats_);
-    for (auto &e : evStage_)
-        if (e) cudaEventDestroy(e);
     if (pinned_) cudaFreeHost(pinned_);
     if (evStart_) cudaEventDestroy(evStart_);
     if (evEnd_) cudaEventDestroy(evEnd_);
@@ -476,7 +473,6 @@ void World::runPipeline(float dt) {
     cudaStream_t s = stream_;
     WorldView w = view(dt);
     DevStats *st = stats_.ptr;
-    PE_CHECK(cudaEventRecordWithFlags(evStage_[0], s, cudaEventRecordExternal));
     const bool sap = algorithm == 0;
     // Dense hashed grid with per-body pairs: the integrate kernel clears the
     // bucket heads and the insert kernel the look-back states of the pair and
@@ -495,7 +491,6 @@ void World::runPipeline(float dt) {
         launchCollect(w, collectFlags_.ptr, collectPos_.ptr, inMin_.ptr, inMax_.ptr, inSlot_.ptr,
                       sap ? sapKeys_.ptr : nullptr, sapVals_.ptr, &st->inputCount, ws_, &st->err, s);
     }
-    PE_CHECK(cudaEventRecordWithFlags(evStage_[1], s, cudaEventRecordExternal));
     BroadInput in{dense_ ? aabbMin_.ptr : inMin_.ptr, dense_ ? aabbMax_.ptr : inMax_.ptr, &st->inputCount, nc_};
     if (sap) launchSap(in, sapKeys_.ptr, sapVals_.ptr, bb_, pb_, st, ws_, s);
     else launchGrid(in, cellSize, bb_, pb_, st, ws_, s);
@@ -503,16 +498,12 @@ void World::runPipeline(float dt) {
         launchGridBodyPairs(in, bb_, pb_, dense_ ? nullptr : inSlot_.ptr, cbody_.ptr, cbgen_.ptr, st, ws_, s, fused);
     else
         launchPairsFinalize(dense_ ? nullptr : inSlot_.ptr, cbody_.ptr, cbgen_.ptr, pb_, st, ws_, s);
-    PE_CHECK(cudaEventRecordWithFlags(evStage_[2], s, cudaEventRecordExternal));
     ManifoldView mv = manifoldView();
     launchNarrowphase(w, pb_, mv, mcap_, st, ws_, s, fused ? ws_.scanState + narrowOff : nullptr, fused);
-    PE_CHECK(cudaEventRecordWithFlags(evStage_[3], s, cudaEventRecordExternal));
     launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], cacheView(1 - cache_), &cCount_.ptr[1 - cache_],
                  cacheCap_, sb_, iterations, orderMode, coopBlocks_, blockSolver_, blockM_, identityColliders_, st,
                  ws_, s);
-    PE_CHECK(cudaEventRecordWithFlags(evStage_[4], s, cudaEventRecordExternal));
-    launchIntegratePose(w, s);
-    PE_CHECK(cudaEventRecordWithFlags(evStage_[5], s, cudaEventRecordExternal));
+    launchIntegratePose(w, s, st);
     PE_CHECK(cudaMemcpyAsync(hostStats_, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
 }
 
@@ -740,7 +731,10 @@ void World::step(float dt) {
         if (finishStep()) {
             float ms = 0, st[5] = {0, 0, 0, 0, 0};
             PE_CHECK(cudaEventElapsedTime(&ms, evStart_, evEnd_));
-            for (int k = 0; k < 5; ++k) PE_CHECK(cudaEventElapsedTime(&st[k], evStage_[k], evStage_[k + 1]));
+            // stage times from the stamps the stage kernels wrote (0 when a
+            // stage ran no stamping kernel this step)
+            const unsigned long long *t = hostStats_->stamp;
+            for (int k = 0; k < 5; ++k) st[k] = t[k + 1] > t[k] ? (float)((t[k + 1] - t[k]) * 1e-6) : 0.0f;
             counters_.gpuMs = ms;
             counters_.integrateMs = st[0];
             counters_.broadphaseMs = st[1];

@@ -230,7 +230,6 @@ class World {
     DeviceArray<DevStats> stats_;
     DevStats *hostStats_ = nullptr;
     cudaEvent_t evStart_ = nullptr, evEnd_ = nullptr;
-    cudaEvent_t evStage_[6] = {};
     // Captured step pipelines, one per ping-pong parity, valid for graphKey_.
     struct GraphKey {
         uint32_t nb, nc, pairCap, entryCap, mcap, cacheCap;
