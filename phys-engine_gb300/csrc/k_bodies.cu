@@ -82,7 +82,10 @@ __global__ void k_collect_scatter(WorldView w, const uint32_t *flags, const uint
     }
 }
 
-__global__ void k_integrate_pose(WorldView w, DevStats *st) {
+// hostOut (nullable, host memory the device can write): the last block to
+// finish copies the step's counters there, which saves a copy node after the
+// kernel; done is its arrival counter (left at zero for the next step).
+__global__ void k_integrate_pose(WorldView w, DevStats *st, DevStats *hostOut, uint32_t *done) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (st && i == 0) st->stamp[4] = globalNs();
     if (i < w.nb) {
@@ -100,7 +103,24 @@ __global__ void k_integrate_pose(WorldView w, DevStats *st) {
     }
     if (st) {
         __syncthreads();
-        if (threadIdx.x == 0) atomicMax(&st->stamp[5], globalNs());
+        __shared__ bool s_last;
+        if (threadIdx.x == 0) {
+            atomicMax(&st->stamp[5], globalNs());
+            s_last = false;
+            if (hostOut) {
+                __threadfence();
+                s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+            }
+        }
+        __syncthreads();
+        if (s_last) {
+            // every block's counters are in: copy them out (8 bytes per lane)
+            __threadfence();
+            const unsigned long long *src = reinterpret_cast<const unsigned long long *>(st);
+            unsigned long long *dst = reinterpret_cast<unsigned long long *>(hostOut);
+            for (uint32_t k = threadIdx.x; k < sizeof(DevStats) / 8; k += blockDim.x) dst[k] = __ldcg(&src[k]);
+            if (threadIdx.x == 0) *done = 0;
+        }
     }
 }
 
@@ -159,9 +179,9 @@ void launchCollect(const WorldView &w, uint32_t *flags, uint32_t *pos, float4 *i
     PE_LAUNCHED();
 }
 
-void launchIntegratePose(const WorldView &w, cudaStream_t s, DevStats *st) {
+void launchIntegratePose(const WorldView &w, cudaStream_t s, DevStats *st, DevStats *hostOut, uint32_t *done) {
     if (!w.nb) return;
-    k_integrate_pose<<<(w.nb + 255) / 256, 256, 0, s>>>(w, st);
+    k_integrate_pose<<<(w.nb + 255) / 256, 256, 0, s>>>(w, st, hostOut, done);
     PE_LAUNCHED();
 }
 

@@ -98,6 +98,7 @@ struct DevStats {
     // "latest block" entries are maxima of an increasing clock.
     unsigned long long stamp[6];
 };
+static_assert(sizeof(DevStats) % 8 == 0, "DevStats is copied in 8-byte words");
 
 struct WorldView {
     uint32_t nb, nc;

@@ -103,7 +103,10 @@ void launchIntegrateAabb(const WorldView &w, uint32_t *sapKeys, uint32_t *sapVal
 void launchCollect(const WorldView &w, uint32_t *flags, uint32_t *pos, float4 *inMin, float4 *inMax, uint32_t *inSlot,
                    uint32_t *sapKeys, uint32_t *sapVals, uint32_t *d_count, Scratch &ws, uint32_t *d_err,
                    cudaStream_t s);
-void launchIntegratePose(const WorldView &w, cudaStream_t s, DevStats *st = nullptr);
+// hostOut (nullable): pinned host memory the counters are copied to by the
+// kernel's last block (done: a zeroed arrival counter).
+void launchIntegratePose(const WorldView &w, cudaStream_t s, DevStats *st = nullptr, DevStats *hostOut = nullptr,
+                         uint32_t *done = nullptr);
 // Host-facing transfers: caller forces (3 floats per body) into the force
 // array with static / dead bodies masked; positions packed to 3 floats.
 void launchExpandForces(const float *f3, const uint32_t *bflags, float4 *force, uint32_t n, cudaStream_t s);

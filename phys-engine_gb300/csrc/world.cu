@@ -28,6 +28,7 @@ World::World(int device) : device_(device) {
     PE_CHECK(cudaMallocHost(&hostStats_, sizeof(DevStats)));
     std::memset(hostStats_, 0, sizeof(DevStats));
     stats_.reserve(1);
+    poseDone_.reserve(1);
     cCount_.reserve(2);
     sEpoch_.reserve(1);
 }
@@ -503,8 +504,10 @@ void World::runPipeline(float dt) {
     launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], cacheView(1 - cache_), &cCount_.ptr[1 - cache_],
                  cacheCap_, sb_, iterations, orderMode, coopBlocks_, blockSolver_, blockM_, identityColliders_, st,
                  ws_, s);
-    launchIntegratePose(w, s, st);
-    PE_CHECK(cudaMemcpyAsync(hostStats_, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
+    // the pose kernel's last block copies the counters to the pinned host
+    // mirror (the device writes it directly); with no bodies a copy node does
+    if (nb_) launchIntegratePose(w, s, st, hostStats_, poseDone_.ptr);
+    else PE_CHECK(cudaMemcpyAsync(hostStats_, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
 }
 
 bool World::finishStep() {

@@ -180,6 +180,7 @@ class World {
     DeviceArray<float4> pos_[2], rot_[2], lin_[2], ang_[2];
     DeviceArray<float4> force_, mat_, iinv_;
     DeviceArray<float> xfer3_;  // 3 floats per body: caller forces in, positions out
+    DeviceArray<uint32_t> poseDone_;  // arrival counter of the pose kernel's blocks
     DeviceArray<uint32_t> bflags_, bgen_;
     DeviceArray<uint32_t> cbody_, cbgen_, cflags_;
     DeviceArray<float4> cshape_, clpos_, clrot_, aabbMin_, aabbMax_;
