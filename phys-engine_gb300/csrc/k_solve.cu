@@ -284,7 +284,7 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
         uint32_t slots = 2 * bm < kStageSlots ? 2 * bm : kStageSlots;
         if (orderMode != 0 && launchSolverCluster(a, newCache, newCacheCount, cacheCap, bm, slots, s)) return;
         const size_t smem = blockSolveSmem(bm, slots);
-        k_prepare<<<(bm + kPrepareThreads - 1) / kPrepareThreads, kPrepareThreads,
+        k_prepare<<<(4 * bm + kPrepareThreads - 1) / kPrepareThreads, kPrepareThreads,
                     kPrepareKeyCap * sizeof(unsigned long long), s>>>(a, kPrepareKeyCap);
         PE_LAUNCHED();
         k_solve_block<<<1, kBlockSolveThreads, smem, s>>>(a, newCache, cacheCap, newCacheCount, orderMode == 0 ? 1 : 0,

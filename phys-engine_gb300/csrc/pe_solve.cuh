@@ -97,20 +97,29 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
     const WorldView &w = a.w;
     const float inverseDt = 1.0f / smax(w.dt, 1e-6f);
     const uint32_t cacheN = *a.oldCount;
+    const float matchSq = 0.05f * 0.05f;
     uint64_t prepared = 0, comparisons = 0, matches = 0;
     uint32_t solved = 0;
-    for (uint32_t m = begin; m < M; m += stride) {
+    // Work items are (manifold, point) pairs q = p M + m (all point-0 items
+    // first, so consecutive threads take consecutive manifolds): a manifold's
+    // points are independent here, so the slowest point, not the sum of a
+    // manifold's points, bounds the pass.  Each item reads its manifold's data;
+    // point 0's item also writes the per-manifold outputs.  Everything indexed
+    // by m and the bodies' data (indices clamped to a live entry) are requested
+    // at once: an item costs three dependent memory round trips (manifold,
+    // bodies, warm-start cache).
+    for (uint32_t q = begin; q < 4 * M; q += stride) {
+        const uint32_t p = q / M, m = q - p * M;
         const uint32_t k = m;  // data index
-        // Everything indexed by m is requested at once, and the bodies' data
-        // with the validity check (indices clamped to a live array entry), so
-        // a one-point manifold costs three dependent memory round trips:
-        // manifold, bodies, warm-start cache.
+        const uint32_t npts = a.mv.pointCount[m];
+        const uint32_t live = npts < 4u ? npts : 4u;  // live points (at most four)
+        if (p > 0 && p >= live) continue;
         const uint32_t ia = a.mv.bodyA[m], ib = a.mv.bodyB[m];
         const uint32_t gA = a.mv.genA[m], gB = a.mv.genB[m];
         const float4 nf = a.mv.normalFriction[m];
-        const uint32_t npts = a.mv.pointCount[m];
         const float rest = a.mv.restitution[m];
-        const float4 aa0 = a.mv.anchorA[4 * m], ab0 = a.mv.anchorB[4 * m], imp0 = a.mv.impulse[4 * m];
+        const float4 aa = a.mv.anchorA[4 * m + p], ab = a.mv.anchorB[4 * m + p];
+        float4 imp = a.mv.impulse[4 * m + p];
         const uint32_t ca = ia < w.nb ? ia : 0u, cb = ib < w.nb ? ib : 0u;
         const uint32_t flA = w.bflags[ca], flB = w.bflags[cb], bgA = w.bgen[ca], bgB = w.bgen[cb];
         const float imA = w.mat[ca].x, imB = w.mat[cb].x;
@@ -122,30 +131,35 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
         // (sequential_impulse_solver.cpp:317-320).
         const bool valid = ia < w.nb && ib < w.nb && (flA & kBodyAlive) && (flB & kBodyAlive) && bgA == gA &&
                            bgB == gB;
-        a.sb.pbody[k] = make_uint2(valid ? ia : 0u, valid ? ib : 0u);
-        if (!valid) {
-            a.sb.pcount[k] = 0;
-            a.sb.pm[k] = make_float4(0.0f, 1.0f, 0.0f, 1.0f);
-            a.sb.pn[k] = nf;
-            continue;  // no live points: nothing is solved or written back
-        }
-        ++solved;
         const bool sA = (flA & kBodyStatic) != 0, sB = (flB & kBodyStatic) != 0;
         const Q qA = f4q(qA4), qB = f4q(qB4);
         const M3 IA = inverseInertiaWorld(qA, iA.x, iA.y, iA.z);
         const M3 IB = inverseInertiaWorld(qB, iB.x, iB.y, iB.z);
+        if (p == 0) {
+            a.sb.pbody[k] = make_uint2(valid ? ia : 0u, valid ? ib : 0u);
+            a.sb.pn[k] = nf;
+            if (!valid) {
+                a.sb.pcount[k] = 0;
+                a.sb.pm[k] = make_float4(0.0f, 1.0f, 0.0f, 1.0f);
+                continue;  // no live points: nothing is solved or written back
+            }
+            ++solved;
+            a.sb.pcount[k] = live;
+            a.sb.pm[k] = make_float4(imA, sA ? 1.0f : 0.0f, imB, sB ? 1.0f : 0.0f);
+            a.sb.pmInertia[0 * mcap + k] = make_float4(IA.m00, IA.m01, IA.m02, 0.0f);
+            a.sb.pmInertia[1 * mcap + k] = make_float4(IA.m10, IA.m11, IA.m12, 0.0f);
+            a.sb.pmInertia[2 * mcap + k] = make_float4(IA.m20, IA.m21, IA.m22, 0.0f);
+            a.sb.pmInertia[3 * mcap + k] = make_float4(IB.m00, IB.m01, IB.m02, 0.0f);
+            a.sb.pmInertia[4 * mcap + k] = make_float4(IB.m10, IB.m11, IB.m12, 0.0f);
+            a.sb.pmInertia[5 * mcap + k] = make_float4(IB.m20, IB.m21, IB.m22, 0.0f);
+            if (live == 0) continue;
+        } else if (!valid) {
+            continue;
+        }
         const V3 linA = f4xyz(lA4), angA = f4xyz(aA4);
         const V3 linB = f4xyz(lB4), angB = f4xyz(aB4);
-        a.sb.pm[k] = make_float4(imA, sA ? 1.0f : 0.0f, imB, sB ? 1.0f : 0.0f);
-        a.sb.pmInertia[0 * mcap + k] = make_float4(IA.m00, IA.m01, IA.m02, 0.0f);
-        a.sb.pmInertia[1 * mcap + k] = make_float4(IA.m10, IA.m11, IA.m12, 0.0f);
-        a.sb.pmInertia[2 * mcap + k] = make_float4(IA.m20, IA.m21, IA.m22, 0.0f);
-        a.sb.pmInertia[3 * mcap + k] = make_float4(IB.m00, IB.m01, IB.m02, 0.0f);
-        a.sb.pmInertia[4 * mcap + k] = make_float4(IB.m10, IB.m11, IB.m12, 0.0f);
-        a.sb.pmInertia[5 * mcap + k] = make_float4(IB.m20, IB.m21, IB.m22, 0.0f);
 
-        // Cache range for (bodyA, bodyB); generations must match.  The range's
-        // first entry is requested with its generations.
+        // Cache range for (bodyA, bodyB); generations must match.
         const unsigned long long key = ((unsigned long long)ia << 32) | ib;
         const unsigned long long gens = ((unsigned long long)gA << 32) | gB;
         uint32_t lo = 0, hi = cacheN;
@@ -156,103 +170,81 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
         }
         uint32_t rb = lo, re = lo;
         while (re < cacheN && cacheKeys[re] == key) ++re;
-        float4 c0a = make_float4(0, 0, 0, 0), c0b = make_float4(0, 0, 0, 0);
-        float c0t = 0.0f;
-        if (rb < re) {
-            const unsigned long long g0 = a.oldCache.gens[rb];
-            c0a = a.oldCache.anchorA[rb];
-            c0b = a.oldCache.anchorB[rb];
-            c0t = a.oldCache.tangent2[rb];
-            if (g0 != gens) re = rb;
-        }
+        if (rb < re && a.oldCache.gens[rb] != gens) re = rb;
 
-        const float matchSq = 0.05f * 0.05f;
-        // live points only: the sweeps, the impulses written back and the
-        // cache read no other
-        const uint32_t live = npts < 4u ? npts : 4u;
-        for (uint32_t p = 0; p < live; ++p) {
-            float4 out[kPreparedVec4];
-            for (int v = 0; v < kPreparedVec4; ++v) out[v] = make_float4(0, 0, 0, 0);
-            float4 imp = p == 0 ? imp0 : a.mv.impulse[4 * m + p];
-            imp.w = 0.0f;
-            if (p < npts) {
-                const float4 aa = p == 0 ? aa0 : a.mv.anchorA[4 * m + p];
-                const float4 ab = p == 0 ? ab0 : a.mv.anchorB[4 * m + p];
-                const V3 anchorA{aa.x, aa.y, aa.z}, anchorB{ab.x, ab.y, ab.z};
-                const float penetration = aa.w;
-                V3 offA = rotate(qA, anchorA), offB = rotate(qB, anchorB);
-                out[0] = make4(offA, 0.0f);
-                out[1] = make4(offB, 0.0f);
-                V3 tref = fabsf(n.x) < 0.9f ? V3{1.0f, 0.0f, 0.0f} : V3{0.0f, 1.0f, 0.0f};
-                V3 t1 = cross(n, tref);
-                float tl = sqrtf(dot(t1, t1));
-                if (tl > 1e-6f) {
-                    t1 = t1 / tl;
-                    V3 t2 = cross(n, t1);
-                    V3 vA = linA + cross(angA, offA), vB = linB + cross(angB, offB);
-                    float vin = dot(vB - vA, n);
-                    V3 jA = cross(offA, n), jB = cross(offB, n);
-                    V3 nrA = mul(IA, jA), nrB = mul(IB, jB);
-                    float ims = imA + imB;
-                    float iem = ims + dot(jA, nrA) + dot(jB, nrB);
-                    V3 tjA = cross(offA, t1), tjB = cross(offB, t1);
-                    V3 trA1 = mul(IA, tjA), trB1 = mul(IB, tjB);
-                    float tm00 = ims + dot(tjA, trA1) + dot(tjB, trB1);
-                    float ntr1 = ims * dot(n, t1) + dot(tjA, nrA) + dot(tjB, nrB);
-                    tjA = cross(offA, t2);
-                    tjB = cross(offB, t2);
-                    V3 trA2 = mul(IA, tjA), trB2 = mul(IB, tjB);
-                    float tm11 = ims + dot(tjA, trA2) + dot(tjB, trB2);
-                    float ntr2 = ims * dot(n, t2) + dot(tjA, nrA) + dot(tjB, nrB);
-                    float tm01 = dot(tjA, trA1) + dot(tjB, trB1);
-                    float det = tm00 * tm11 - tm01 * tm01;
-                    float itm00 = 0.0f, itm01 = 0.0f, itm11 = 0.0f;
-                    if (det > 0.0f) {
-                        float inv = 1.0f / det;
-                        itm00 = tm11 * inv;
-                        itm01 = -tm01 * inv;
-                        itm11 = tm00 * inv;
-                    }
-                    float bias = 0.0f, rv = 0.0f;
-                    if (!(iem <= 0.0f)) {
-                        ++prepared;
-                        bias = smax(penetration - 0.005f, 0.0f) * (0.2f * inverseDt);
-                        rv = vin < -1.0f ? rest * vin : 0.0f;
-                    }
-                    out[0].w = iem;
-                    out[1].w = bias;
-                    out[2] = make4(t1, rv);
-                    out[3] = make4(t2, itm00);
-                    out[4] = make4(nrA, itm01);
-                    out[5] = make4(nrB, itm11);
-                    out[6] = make4(trA1, ntr1);
-                    out[7] = make4(trB1, ntr2);
-                    out[8] = make4(trA2, 0.0f);
-                    out[9] = make4(trB2, 0.0f);
-                    if (!(iem <= 0.0f)) {
-                        for (uint32_t c = rb; c < re; ++c) {
-                            ++comparisons;
-                            const float4 ca = c == rb ? c0a : a.oldCache.anchorA[c];
-                            const float4 cb = c == rb ? c0b : a.oldCache.anchorB[c];
-                            V3 da = V3{ca.x, ca.y, ca.z} - anchorA, db = V3{cb.x, cb.y, cb.z} - anchorB;
-                            if (dot(da, da) > matchSq || dot(db, db) > matchSq) continue;
-                            const float t2c = c == rb ? c0t : a.oldCache.tangent2[c];
-                            float ni = smax(ca.w, 0.0f);
-                            float limit = smax(nf.w, 0.0f) * ni;
-                            float tlsq = cb.w * cb.w + t2c * t2c;
-                            float scale = tlsq > limit * limit ? limit / sqrtf(tlsq) : 1.0f;
-                            imp = make_float4(ni, cb.w * scale, t2c * scale, 1.0f);
-                            ++matches;
-                            break;
-                        }
-                    }
+        float4 out[kPreparedVec4];
+        for (int v = 0; v < kPreparedVec4; ++v) out[v] = make_float4(0, 0, 0, 0);
+        imp.w = 0.0f;
+        const V3 anchorA{aa.x, aa.y, aa.z}, anchorB{ab.x, ab.y, ab.z};
+        const float penetration = aa.w;
+        V3 offA = rotate(qA, anchorA), offB = rotate(qB, anchorB);
+        out[0] = make4(offA, 0.0f);
+        out[1] = make4(offB, 0.0f);
+        V3 tref = fabsf(n.x) < 0.9f ? V3{1.0f, 0.0f, 0.0f} : V3{0.0f, 1.0f, 0.0f};
+        V3 t1 = cross(n, tref);
+        float tl = sqrtf(dot(t1, t1));
+        if (tl > 1e-6f) {
+            t1 = t1 / tl;
+            V3 t2 = cross(n, t1);
+            V3 vA = linA + cross(angA, offA), vB = linB + cross(angB, offB);
+            float vin = dot(vB - vA, n);
+            V3 jA = cross(offA, n), jB = cross(offB, n);
+            V3 nrA = mul(IA, jA), nrB = mul(IB, jB);
+            float ims = imA + imB;
+            float iem = ims + dot(jA, nrA) + dot(jB, nrB);
+            V3 tjA = cross(offA, t1), tjB = cross(offB, t1);
+            V3 trA1 = mul(IA, tjA), trB1 = mul(IB, tjB);
+            float tm00 = ims + dot(tjA, trA1) + dot(tjB, trB1);
+            float ntr1 = ims * dot(n, t1) + dot(tjA, nrA) + dot(tjB, nrB);
+            tjA = cross(offA, t2);
+            tjB = cross(offB, t2);
+            V3 trA2 = mul(IA, tjA), trB2 = mul(IB, tjB);
+            float tm11 = ims + dot(tjA, trA2) + dot(tjB, trB2);
+            float ntr2 = ims * dot(n, t2) + dot(tjA, nrA) + dot(tjB, nrB);
+            float tm01 = dot(tjA, trA1) + dot(tjB, trB1);
+            float det = tm00 * tm11 - tm01 * tm01;
+            float itm00 = 0.0f, itm01 = 0.0f, itm11 = 0.0f;
+            if (det > 0.0f) {
+                float inv = 1.0f / det;
+                itm00 = tm11 * inv;
+                itm01 = -tm01 * inv;
+                itm11 = tm00 * inv;
+            }
+            float bias = 0.0f, rv = 0.0f;
+            if (!(iem <= 0.0f)) {
+                ++prepared;
+                bias = smax(penetration - 0.005f, 0.0f) * (0.2f * inverseDt);
+                rv = vin < -1.0f ? rest * vin : 0.0f;
+            }
+            out[0].w = iem;
+            out[1].w = bias;
+            out[2] = make4(t1, rv);
+            out[3] = make4(t2, itm00);
+            out[4] = make4(nrA, itm01);
+            out[5] = make4(nrB, itm11);
+            out[6] = make4(trA1, ntr1);
+            out[7] = make4(trB1, ntr2);
+            out[8] = make4(trA2, 0.0f);
+            out[9] = make4(trB2, 0.0f);
+            if (!(iem <= 0.0f)) {
+                for (uint32_t c = rb; c < re; ++c) {
+                    ++comparisons;
+                    const float4 ca = a.oldCache.anchorA[c], cb = a.oldCache.anchorB[c];
+                    V3 da = V3{ca.x, ca.y, ca.z} - anchorA, db = V3{cb.x, cb.y, cb.z} - anchorB;
+                    if (dot(da, da) > matchSq || dot(db, db) > matchSq) continue;
+                    const float t2c = a.oldCache.tangent2[c];
+                    float ni = smax(ca.w, 0.0f);
+                    float limit = smax(nf.w, 0.0f) * ni;
+                    float tlsq = cb.w * cb.w + t2c * t2c;
+                    float scale = tlsq > limit * limit ? limit / sqrtf(tlsq) : 1.0f;
+                    imp = make_float4(ni, cb.w * scale, t2c * scale, 1.0f);
+                    ++matches;
+                    break;
                 }
             }
-            for (int v = 0; v < kPreparedVec4; ++v) a.sb.pp[(size_t)(v * 4 + p) * mcap + k] = out[v];
-            a.sb.pimp[(size_t)p * mcap + k] = imp;
         }
-        a.sb.pn[k] = nf;
-        a.sb.pcount[k] = live;
+        for (int v = 0; v < kPreparedVec4; ++v) a.sb.pp[(size_t)(v * 4 + p) * mcap + k] = out[v];
+        a.sb.pimp[(size_t)p * mcap + k] = imp;
     }
     aggregatedAdd32(&a.st->solved, solved);
     aggregatedAdd64(&a.st->preparedPoints, prepared);
