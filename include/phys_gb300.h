@@ -147,8 +147,12 @@ pe_status pe_world_set_solver(pe_world *world, int iterations, int order);
    (physics_world.hpp:66-73): validated like the reference (0 is invalid); the
    GPU path has no host worker threads. */
 pe_status pe_world_set_worker_counts(pe_world *world, uint64_t narrowphase, uint64_t solver, uint64_t broadphase);
-/* setSleepingEnabled (physics_world.hpp:63): only `false` is supported. */
+/* setSleepingEnabled / isSleepingEnabled (physics_world.hpp:63-64): islands
+   whose bodies stay below 0.05 m/s and 0.05 rad/s for half a second of
+   simulated time sleep (no gravity, no solve, fixed pose) until a contact, an
+   edit or a wake request wakes them (src/world/physics_world.cpp:341-516). */
 pe_status pe_world_set_sleeping_enabled(pe_world *world, int enabled);
+pe_status pe_world_get_sleeping_enabled(const pe_world *world, int *enabled);
 
 /* createSphere / createBox (physics_world.hpp:43-50): same validation and mass
    properties as RigidBody::createSphere / createBox (src/dynamics/rigid_body.cpp:25-91). */
@@ -181,9 +185,20 @@ pe_status pe_world_add_collider(pe_world *world, pe_handle body, int shape, cons
 pe_status pe_world_remove_body(pe_world *world, pe_handle body);
 pe_status pe_world_remove_collider(pe_world *world, pe_handle collider);
 
-/* getBody (physics_world.hpp:54-55) read / write of the public state. */
+/* getBody (physics_world.hpp:54-55) read / write of the public state.  With
+   sleeping on, a changed velocity or force wakes the body at once (the
+   reference's setters); a changed pose, mass, material or static flag wakes it
+   at the next step (prepareSleeping's comparison). */
 pe_status pe_world_get_body(pe_world *world, pe_handle body, pe_body_state *out);
 pe_status pe_world_set_body(pe_world *world, pe_handle body, const pe_body_state *state);
+/* RigidBody::isSleeping / wakeUp / applyForce / setLinearVelocity +
+   setAngularVelocity (rigid_body.hpp:53-95); NULL leaves a velocity as it is. */
+pe_status pe_world_body_is_sleeping(pe_world *world, pe_handle body, int *sleeping);
+pe_status pe_world_body_wake_up(pe_world *world, pe_handle body);
+pe_status pe_world_body_apply_force(pe_world *world, pe_handle body, const float *force);
+pe_status pe_world_body_set_velocity(pe_world *world, pe_handle body, const float *linear, const float *angular);
+/* isSleeping() of every body slot (0 for empty slots).  No reference counterpart. */
+pe_status pe_world_read_sleeping(pe_world *world, uint8_t *sleeping);
 /* RigidBody::integrateRotation (rigid_body.cpp:110-125) on one body; with
    dt = 1 and an angular velocity this is the reference's orientation idiom. */
 pe_status pe_world_body_integrate_rotation(pe_world *world, pe_handle body, float dt);
@@ -197,7 +212,8 @@ pe_status pe_world_read_bodies(pe_world *world, float *positions, float *rotatio
 /* Per-step host I/O without the host mirror (no reference counterpart; the
    reference's equivalents are RigidBody::applyForce and getPosition/getRotation
    per body): set the accumulated force of body slots [0, n) from xyz triples
-   (static bodies ignore it, like applyForce), and copy all current positions
+   (static bodies ignore it, like applyForce, and a nonzero force wakes its
+   body), and copy all current positions
    (xyz) / rotations (xyzw) out.  Either output pointer may be NULL. */
 pe_status pe_world_write_forces(pe_world *world, const float *forces, uint32_t n);
 pe_status pe_world_read_poses(pe_world *world, float *positions, float *rotations);

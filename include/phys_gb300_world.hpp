@@ -80,24 +80,36 @@ class BodyRef {
     float friction() const { return s_.friction; }
     bool isStatic() const { return s_.is_static != 0; }
     float getInverseMass() const { return isStatic() || s_.mass <= 0.0f ? 0.0f : 1.0f / s_.mass; }
+    // The velocity setters, applyForce and applyLinearImpulse wake the body
+    // like the reference's (rigid_body.hpp:54-95).
+    bool isSleeping() const {
+        int v = 0;
+        if (ok_) throwIf(pe_world_body_is_sleeping(w_, h_, &v));
+        return v != 0;
+    }
+    void wakeUp() {
+        if (ok_) throwIf(pe_world_body_wake_up(w_, h_));
+    }
     void setLinearVelocity(const Vec3 &v) {
-        s_.linear_velocity[0] = v.x;
-        s_.linear_velocity[1] = v.y;
-        s_.linear_velocity[2] = v.z;
-        commit();
+        const float l[3] = {v.x, v.y, v.z};
+        if (ok_) throwIf(pe_world_body_set_velocity(w_, h_, l, nullptr));
+        refresh();
     }
     void setAngularVelocity(const Vec3 &v) {
-        s_.angular_velocity[0] = v.x;
-        s_.angular_velocity[1] = v.y;
-        s_.angular_velocity[2] = v.z;
-        commit();
+        const float a[3] = {v.x, v.y, v.z};
+        if (ok_) throwIf(pe_world_body_set_velocity(w_, h_, nullptr, a));
+        refresh();
     }
     void applyForce(const Vec3 &f) {
-        if (isStatic()) return;
-        s_.force[0] += f.x;
-        s_.force[1] += f.y;
-        s_.force[2] += f.z;
-        commit();
+        const float v[3] = {f.x, f.y, f.z};
+        if (ok_) throwIf(pe_world_body_apply_force(w_, h_, v));
+        refresh();
+    }
+    void applyLinearImpulse(const Vec3 &j) {
+        if (isStatic() || (j.x == 0.0f && j.y == 0.0f && j.z == 0.0f)) return;
+        const float m = getInverseMass();
+        setLinearVelocity({s_.linear_velocity[0] + j.x * m, s_.linear_velocity[1] + j.y * m,
+                           s_.linear_velocity[2] + j.z * m});
     }
     void clearForces() {
         s_.force[0] = s_.force[1] = s_.force[2] = 0.0f;
@@ -175,7 +187,11 @@ class PhysicsWorld {
     std::size_t getSolverWorkerCount() const { return solverWorkers_; }
     std::size_t getBroadPhaseWorkerCount() const { return broadWorkers_; }
     void setSleepingEnabled(bool enabled) { throwIf(pe_world_set_sleeping_enabled(w_, enabled)); }
-    bool isSleepingEnabled() const { return false; }
+    bool isSleepingEnabled() const {
+        int v = 0;
+        throwIf(pe_world_get_sleeping_enabled(w_, &v));
+        return v != 0;
+    }
 
     void step(float dt) {
         throwIf(pe_world_set_gravity(w_, gravity.x, gravity.y, gravity.z));

@@ -83,6 +83,11 @@ def oracle_lib():
         lib.ow_create_hull_body.argtypes = [_P, ctypes.c_int, _P, ctypes.c_float, _P, ctypes.c_int,
                                             ctypes.c_float, ctypes.c_float, _P]
         lib.ow_remove_body.argtypes = [_P, ctypes.c_uint32, ctypes.c_uint32]
+        lib.ow_remove_collider.argtypes = [_P, ctypes.c_uint32, ctypes.c_uint32]
+        lib.ow_set_sleeping_enabled.argtypes = [_P, ctypes.c_int]
+        lib.ow_get_sleeping.argtypes = [_P, _P]
+        lib.ow_wake_body.argtypes = [_P, ctypes.c_uint32]
+        lib.ow_apply_force.argtypes = [_P, ctypes.c_uint32, _P]
         lib.ow_body_slot_count.argtypes = [_P]
         lib.ow_body_slot_count.restype = ctypes.c_uint32
         lib.ow_get_bodies.argtypes = [_P, _P, _P, _P, _P]
@@ -129,6 +134,12 @@ def ref_lib():
         lib.rw_create_body.argtypes = [_P, ctypes.c_int, _P, _P, ctypes.c_float, ctypes.c_int,
                                        ctypes.c_float, ctypes.c_float, _P, ctypes.c_char_p, ctypes.c_int]
         lib.rw_remove_body.argtypes = [_P, ctypes.c_uint32, ctypes.c_uint32]
+        lib.rw_remove_collider.argtypes = [_P, ctypes.c_uint32, ctypes.c_uint32]
+        lib.rw_set_sleeping_enabled.argtypes = [_P, ctypes.c_int]
+        lib.rw_get_sleeping.argtypes = [_P, _P]
+        lib.rw_wake_body.argtypes = [_P, ctypes.c_uint32]
+        lib.rw_apply_force.argtypes = [_P, ctypes.c_uint32, _P]
+        lib.rw_set_material.argtypes = [_P, ctypes.c_uint32, ctypes.c_float, ctypes.c_float, ctypes.c_float]
         lib.rw_body_slot_count.argtypes = [_P]
         lib.rw_body_slot_count.restype = ctypes.c_uint32
         lib.rw_apply_spin.argtypes = [_P, ctypes.c_uint32, _P]
@@ -203,6 +214,23 @@ class _CpuWorld:
 
     def remove_body(self, idx, gen):
         getattr(self.lib, self._prefix + "remove_body")(self.h, int(idx), int(gen))
+
+    def remove_collider(self, idx, gen):
+        getattr(self.lib, self._prefix + "remove_collider")(self.h, int(idx), int(gen))
+
+    def set_sleeping_enabled(self, enabled):
+        getattr(self.lib, self._prefix + "set_sleeping_enabled")(self.h, int(bool(enabled)))
+
+    def sleeping(self):
+        out = np.zeros(self.body_count(), np.uint8)
+        getattr(self.lib, self._prefix + "get_sleeping")(self.h, _ptr(out))
+        return out.astype(bool)
+
+    def wake_body(self, idx):
+        getattr(self.lib, self._prefix + "wake_body")(self.h, int(idx))
+
+    def apply_force(self, idx, force):
+        getattr(self.lib, self._prefix + "apply_force")(self.h, int(idx), _ptr(_f32(force)))
 
     def step(self, dt):
         getattr(self.lib, self._prefix + "step")(self.h, float(dt))
@@ -344,6 +372,9 @@ class RefWorld(_CpuWorld):
 
     def set_gravity(self, g):
         self.lib.rw_set_gravity(self.h, float(g[0]), float(g[1]), float(g[2]))
+
+    def set_material(self, idx, mass, friction, restitution):
+        self.lib.rw_set_material(self.h, int(idx), float(mass), float(friction), float(restitution))
 
     def bounds(self):
         n = self.body_count()

@@ -143,8 +143,16 @@ template <class T> struct Body {
     M3<T> invInertiaLocal{};
     uint32_t generation = 0;
     bool alive = false;
+    // Sleep flags (rigid_body.hpp:53-58, :132-133)
+    bool sleeping = false;
+    bool wakeRequested = true;
     // RigidBody::getInverseMass (rigid_body.hpp:72-75)
     T inverseMass() const { return isStatic || mass <= T(0) ? T(0) : T(1) / mass; }
+    bool isSleeping() const { return !isStatic && sleeping; }
+    void wakeUp() {
+        sleeping = false;
+        wakeRequested = true;
+    }
 };
 
 template <class T> struct Aabb {
@@ -970,17 +978,20 @@ template <class T> struct World : WorldBase {
             bodies[idx] = b;
             bodies[idx].generation = g;
             bodies[idx].alive = true;
+            bodies[idx].wakeUp();
             gen = g;
             return idx;
         }
         bodies.push_back(b);
         bodies.back().generation = 0;
         bodies.back().alive = true;
+        bodies.back().wakeUp();
         gen = 0;
         return (uint32_t)bodies.size() - 1;
     }
     // PhysicsWorld::addCollider (physics_world.cpp:276-298)
     uint32_t addCollider(const Collider<T> &c, uint32_t &gen) {
+        if (Body<T> *b = getBody(c.bodyIndex, c.bodyGeneration)) b->wakeUp();
         if (!freeColliders.empty()) {
             uint32_t idx = freeColliders.back();
             freeColliders.pop_back();
@@ -988,6 +999,7 @@ template <class T> struct World : WorldBase {
             colliders[idx] = c;
             colliders[idx].generation = g;
             colliders[idx].alive = true;
+            if (idx < sleepColliders.size()) sleepColliders[idx] = colliders[idx];
             gen = g;
             return idx;
         }
@@ -1002,6 +1014,7 @@ template <class T> struct World : WorldBase {
         if (idx >= bodies.size()) return;
         Body<T> &b = bodies[idx];
         if (!b.alive || b.generation != gen) return;
+        wakeContacts(idx, gen);
         b.alive = false;
         b.generation++;
         freeBodies.push_back(idx);
@@ -1015,15 +1028,188 @@ template <class T> struct World : WorldBase {
         }
     }
 
+    // PhysicsWorld::removeCollider (physics_world.cpp:300-315)
+    void removeCollider(uint32_t idx, uint32_t gen) {
+        if (idx >= colliders.size()) return;
+        Collider<T> &c = colliders[idx];
+        if (!c.alive || c.generation != gen) return;
+        if (Body<T> *b = getBody(c.bodyIndex, c.bodyGeneration)) b->wakeUp();
+        wakeContacts(c.bodyIndex, c.bodyGeneration);
+        c.alive = false;
+        c.generation++;
+        freeColliders.push_back(idx);
+    }
+
+    // ---------------- sleeping (physics_world.cpp:341-516) -------------------
+    struct SleepState {
+        Tf<T> pose{{}, {T(0), T(0), T(0), T(1)}};
+        T mass{}, restitution{}, friction{};
+        bool isStatic = false;
+        bool integratedVelocity = false;
+        uint32_t parent = 0;
+        bool hasAwake = false, hasSleeping = false, needsWake = false;
+        T quietTime{}, islandQuietTime{};
+    };
+    bool sleepingEnabled = false;
+    V3<T> sleepGravity{};
+    std::vector<SleepState> sleepStates;
+    std::vector<Collider<T>> sleepColliders;
+
+    // PhysicsWorld::setSleepingEnabled (physics_world.cpp:341-351)
+    void setSleepingEnabled(bool enabled) {
+        if (sleepingEnabled == enabled) return;
+        sleepingEnabled = enabled;
+        sleepStates.clear();
+        sleepColliders.clear();
+        for (auto &b : bodies)
+            if (b.alive) b.wakeUp();
+    }
+    // PhysicsWorld::wakeContacts (physics_world.cpp:353-371): the dynamic bodies
+    // touching a body in the last step's contacts.
+    void wakeContacts(uint32_t idx, uint32_t gen) {
+        if (!sleepingEnabled) return;
+        for (const Manifold<T> &m : contacts) {
+            if (m.aIdx == idx && m.aGen == gen)
+                if (Body<T> *o = getBody(m.bIdx, m.bGen); o && !o->isStatic) o->wakeUp();
+            if (m.bIdx == idx && m.bGen == gen)
+                if (Body<T> *o = getBody(m.aIdx, m.aGen); o && !o->isStatic) o->wakeUp();
+        }
+    }
+    // PhysicsWorld::sleepRoot (physics_world.cpp:373-381), path halving.
+    uint32_t sleepRoot(uint32_t i) {
+        while (sleepStates[i].parent != i) {
+            sleepStates[i].parent = sleepStates[sleepStates[i].parent].parent;
+            i = sleepStates[i].parent;
+        }
+        return i;
+    }
+    // PhysicsWorld::wakeSleepIslands (physics_world.cpp:383-432): islands are
+    // the dynamic bodies joined by contacts (a static body joins nothing); an
+    // island with a wake request, or with awake and sleeping bodies, wakes.
+    void wakeSleepIslands() {
+        for (uint32_t i = 0; i < bodies.size(); ++i) {
+            SleepState &st = sleepStates[i];
+            st.parent = i;
+            st.hasAwake = st.hasSleeping = st.needsWake = false;
+        }
+        for (const Manifold<T> &m : contacts) {
+            Body<T> *A = getBody(m.aIdx, m.aGen), *B = getBody(m.bIdx, m.bGen);
+            if (!A || !B || m.pointCount == 0) continue;
+            if (!A->isStatic && !B->isStatic) {
+                uint32_t ra = sleepRoot(m.aIdx), rb = sleepRoot(m.bIdx);
+                sleepStates[std::max(ra, rb)].parent = std::min(ra, rb);
+            } else if (A->isStatic && A->wakeRequested && !B->isStatic) {
+                B->wakeUp();
+            } else if (B->isStatic && B->wakeRequested && !A->isStatic) {
+                A->wakeUp();
+            }
+        }
+        for (uint32_t i = 0; i < bodies.size(); ++i) {
+            const Body<T> &b = bodies[i];
+            if (!b.alive || b.isStatic) continue;
+            SleepState &island = sleepStates[sleepRoot(i)];
+            island.hasAwake |= !b.isSleeping();
+            island.hasSleeping |= b.isSleeping();
+            island.needsWake |= b.wakeRequested;
+        }
+        for (uint32_t i = 0; i < bodies.size(); ++i) {
+            Body<T> &b = bodies[i];
+            if (!b.alive || b.isStatic) continue;
+            const SleepState &island = sleepStates[sleepRoot(i)];
+            if (island.needsWake || (island.hasAwake && island.hasSleeping)) {
+                b.wakeUp();
+                sleepStates[i].quietTime = T(0);
+            }
+        }
+    }
+    static bool sameV(const V3<T> &a, const V3<T> &b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+    static bool sameTf(const Tf<T> &a, const Tf<T> &b) {
+        return sameV(a.p, b.p) && a.q.x == b.q.x && a.q.y == b.q.y && a.q.z == b.q.z && a.q.w == b.q.w;
+    }
+    // sameColliderGeometry (physics_world.cpp:38-46)
+    static bool sameGeometry(const Collider<T> &a, const Collider<T> &b) {
+        if (a.bodyIndex != b.bodyIndex || a.bodyGeneration != b.bodyGeneration || !sameTf(a.local, b.local) ||
+            a.shape != b.shape)
+            return false;
+        if (a.shape == kSphere) return a.radius == b.radius;
+        if (a.shape == kBox) return sameV(a.halfExtents, b.halfExtents);
+        return a.hull == b.hull;
+    }
+    // PhysicsWorld::prepareSleeping (physics_world.cpp:434-466): edits since the
+    // last step (gravity, mass, material, static flag, pose, collider geometry)
+    // wake the bodies they touch.
+    void prepareSleeping() {
+        sleepStates.resize(bodies.size());
+        const size_t previousColliders = sleepColliders.size();
+        sleepColliders.resize(colliders.size());
+        const bool gravityChanged = !sameV(gravity, sleepGravity);
+        for (uint32_t i = 0; i < bodies.size(); ++i) {
+            Body<T> &b = bodies[i];
+            if (!b.alive) continue;
+            const SleepState &prev = sleepStates[i];
+            if (gravityChanged || prev.mass != b.mass || prev.isStatic != b.isStatic || prev.friction != b.friction ||
+                prev.restitution != b.restitution || !sameTf(prev.pose, Tf<T>{b.pos, b.rot}))
+                b.wakeUp();
+        }
+        for (uint32_t i = 0; i < colliders.size(); ++i) {
+            const Collider<T> &c = colliders[i];
+            if (!c.alive || sameGeometry(c, sleepColliders[i])) continue;
+            if (i < previousColliders)
+                if (Body<T> *old = getBody(sleepColliders[i].bodyIndex, sleepColliders[i].bodyGeneration)) old->wakeUp();
+            if (Body<T> *b = getBody(c.bodyIndex, c.bodyGeneration)) b->wakeUp();
+        }
+        wakeSleepIslands();
+    }
+    // PhysicsWorld::finishSleeping (physics_world.cpp:468-516): half a second of
+    // island-wide quiet (|v|^2 and |w|^2 <= 0.05^2, no wake request) puts an
+    // island to sleep with zero velocities.
+    void finishSleeping(T dt) {
+        const T quietSpeedSquared = T(0.05f) * T(0.05f);
+        const T timeToSleep = T(0.5f);
+        for (SleepState &st : sleepStates) st.islandQuietTime = std::numeric_limits<T>::max();
+        for (uint32_t i = 0; i < bodies.size(); ++i) {
+            Body<T> &b = bodies[i];
+            if (!b.alive || b.isStatic) continue;
+            SleepState &st = sleepStates[i];
+            if (!b.isSleeping()) {
+                if (!b.wakeRequested && dt > T(0) && std::isfinite(dt) && dot(b.lin, b.lin) <= quietSpeedSquared &&
+                    dot(b.ang, b.ang) <= quietSpeedSquared)
+                    st.quietTime = std::min(st.quietTime + dt, timeToSleep);
+                else
+                    st.quietTime = T(0);
+            }
+            SleepState &island = sleepStates[sleepRoot(i)];
+            island.islandQuietTime = std::min(island.islandQuietTime, st.quietTime);
+        }
+        for (uint32_t i = 0; i < bodies.size(); ++i) {
+            Body<T> &b = bodies[i];
+            if (!b.alive) continue;
+            if (!b.isStatic && sleepStates[sleepRoot(i)].islandQuietTime >= timeToSleep) {
+                b.sleeping = true;
+                b.lin = b.ang = V3<T>{};
+            }
+            SleepState &st = sleepStates[i];
+            st.pose = Tf<T>{b.pos, b.rot};
+            st.mass = b.mass;
+            st.isStatic = b.isStatic;
+            st.friction = b.friction;
+            st.restitution = b.restitution;
+            b.wakeRequested = false;
+        }
+        for (uint32_t i = 0; i < colliders.size(); ++i)
+            if (colliders[i].alive) sleepColliders[i] = colliders[i];
+        sleepGravity = gravity;
+    }
+
     // RigidBody::integrateVelocity (rigid_body.cpp:94-101)
     void integrateVelocity(Body<T> &b, T dt) {
-        if (b.isStatic) return;
+        if (b.isStatic || b.sleeping) return;
         V3<T> acc = gravity + b.force * b.inverseMass();
         b.lin += acc * dt;
     }
     // RigidBody::integratePosition / integrateRotation (rigid_body.cpp:103-125)
     static void integratePose(Body<T> &b, T dt) {
-        if (b.isStatic) return;
+        if (b.isStatic || b.sleeping) return;
         b.pos += b.lin * dt;
         Q<T> spin{b.ang.x, b.ang.y, b.ang.z, T(0)};
         Q<T> d = qmul(spin, b.rot);
@@ -1139,6 +1325,8 @@ template <class T> struct World : WorldBase {
             Manifold<T> &m = cs[ord ? ord[k] : k];
             Body<T> *A = getBody(m.aIdx, m.aGen), *B = getBody(m.bIdx, m.bGen);
             if (!A || !B) continue;
+            // contacts among static and sleeping bodies only are not solved (:321-324)
+            if (sleepingEnabled && (A->isStatic || A->isSleeping()) && (B->isStatic || B->isSleeping())) continue;
             PManifold p{};
             p.m = &m;
             p.a = prepareBody(A, m.aIdx);
@@ -1251,8 +1439,16 @@ template <class T> struct World : WorldBase {
             for (PManifold &p : pc) solveOne(p);
         ss.velocity_point_visits = prepared * (uint64_t)iters;
 
-        // Cache update (sequential_impulse_solver.cpp:623-681), sleeping off.
+        // Cache update (sequential_impulse_solver.cpp:623-681): with sleeping
+        // on, the entries of sleeping contacts are carried over first.
         std::vector<Cached<T>> next;
+        if (sleepingEnabled)
+            for (const Cached<T> &c : cache) {
+                const Body<T> *A = getBody(c.aIdx, c.aGen), *B = getBody(c.bIdx, c.bGen);
+                if (A && B && (A->isSleeping() || B->isSleeping()) && (A->isStatic || A->isSleeping()) &&
+                    (B->isStatic || B->isSleeping()))
+                    next.push_back(c);
+            }
         for (const PManifold &p : pc) {
             const Manifold<T> &m = *p.m;
             for (uint32_t i = 0; i < m.pointCount; ++i) {
@@ -1277,10 +1473,11 @@ template <class T> struct World : WorldBase {
                   [](uint32_t a, uint32_t b) { return colorPriority(a) > colorPriority(b); });
         // Per dynamic body, the colours already taken by coloured manifolds.
         std::vector<std::vector<uint32_t>> used(bodies.size());
+        // (a sleeping body is not dynamic here: its contacts are not solved)
         auto dynamicBody = [&](uint32_t idx, uint32_t gen) {
             if (idx >= bodies.size()) return false;
             const Body<T> &b = bodies[idx];
-            return b.alive && b.generation == gen && !b.isStatic;
+            return b.alive && b.generation == gen && !b.isStatic && !(sleepingEnabled && b.sleeping);
         };
         uint32_t ncol = 0;
         for (uint32_t m : byPrio) {
@@ -1304,10 +1501,15 @@ template <class T> struct World : WorldBase {
         return ncol;
     }
 
-    // PhysicsWorld::step (physics_world.cpp:518-782), sleeping off.
+    // PhysicsWorld::step (physics_world.cpp:518-782)
     void step(T dt) {
-        for (auto &b : bodies)
-            if (b.alive) integrateVelocity(b, dt);
+        if (sleepingEnabled) prepareSleeping();
+        for (uint32_t i = 0; i < bodies.size(); ++i) {
+            Body<T> &b = bodies[i];
+            if (!b.alive) continue;
+            if (sleepingEnabled) sleepStates[i].integratedVelocity = !b.isSleeping();
+            integrateVelocity(b, dt);
+        }
         for (auto &c : colliders) {
             if (!c.alive) continue;
             Body<T> *b = getBody(c.bodyIndex, c.bodyGeneration);
@@ -1400,6 +1602,13 @@ template <class T> struct World : WorldBase {
             contacts.push_back(results[k]);
         }
         stats.contact_count = contacts.size();
+        if (sleepingEnabled) {
+            // contacts can wake an island after gravity integration (:741-748)
+            wakeSleepIslands();
+            for (uint32_t i = 0; i < bodies.size(); ++i)
+                if (bodies[i].alive && !sleepStates[i].integratedVelocity && !bodies[i].isSleeping())
+                    integrateVelocity(bodies[i], dt);
+        }
 
         if (orderMode == 1) {
             stats.color_count = colorManifolds(contacts, order, colors);
@@ -1417,9 +1626,10 @@ template <class T> struct World : WorldBase {
             integratePose(b, dt);
             b.force = {};
         }
-        stats.awake_body_count = 0;
+        if (sleepingEnabled) finishSleeping(dt);
+        stats.awake_body_count = stats.sleeping_body_count = 0;
         for (auto &b : bodies)
-            if (b.alive && !b.isStatic) ++stats.awake_body_count;
+            if (b.alive && !b.isStatic) ++(b.isSleeping() ? stats.sleeping_body_count : stats.awake_body_count);
     }
 };
 
@@ -1655,6 +1865,30 @@ int ow_create_hull_body(ow_world *world, int hull_id, const float *pos, float ma
 void ow_remove_body(ow_world *world, uint32_t index, uint32_t generation) {
     dispatch(world, [&](auto &w) { w.removeBody(index, generation); });
 }
+void ow_remove_collider(ow_world *world, uint32_t index, uint32_t generation) {
+    dispatch(world, [&](auto &w) { w.removeCollider(index, generation); });
+}
+void ow_set_sleeping_enabled(ow_world *world, int enabled) {
+    dispatch(world, [&](auto &w) { w.setSleepingEnabled(enabled != 0); });
+}
+void ow_get_sleeping(const ow_world *world, uint8_t *sleeping) {
+    dispatch(world, [&](auto &w) {
+        for (size_t i = 0; i < w.bodies.size(); ++i) sleeping[i] = w.bodies[i].isSleeping() ? 1 : 0;
+    });
+}
+void ow_wake_body(ow_world *world, uint32_t i) {
+    dispatch(world, [&](auto &w) { w.bodies[i].wakeUp(); });
+}
+// RigidBody::applyForce (rigid_body.hpp:77-85)
+void ow_apply_force(ow_world *world, uint32_t i, const float *f) {
+    dispatch(world, [&](auto &w) {
+        using T = decltype(w.gravity.x);
+        auto &b = w.bodies[i];
+        if (b.isStatic) return;
+        if (f[0] != 0.0f || f[1] != 0.0f || f[2] != 0.0f) b.wakeUp();
+        b.force += V3<T>{T(f[0]), T(f[1]), T(f[2])};
+    });
+}
 uint32_t ow_body_slot_count(const ow_world *world) {
     return dispatch(world, [&](auto &w) { return (uint32_t)w.bodies.size(); });
 }
@@ -1665,9 +1899,11 @@ void ow_get_bodies(const ow_world *world, float *pos, float *quat, float *lin, f
 void ow_get_bodies_f64(const ow_world *world, double *pos, double *quat, double *lin, double *ang) {
     dispatch(world, [&](auto &w) { getBodiesT(w, pos, quat, lin, ang); });
 }
+// setLinearVelocity / setAngularVelocity wake the body (rigid_body.hpp:59-63, :91-95)
 void ow_set_velocity(ow_world *world, uint32_t i, const float *lin, const float *ang) {
     dispatch(world, [&](auto &w) {
         using T = decltype(w.gravity.x);
+        if (lin || ang) w.bodies[i].wakeUp();
         if (lin) w.bodies[i].lin = {T(lin[0]), T(lin[1]), T(lin[2])};
         if (ang) w.bodies[i].ang = {T(ang[0]), T(ang[1]), T(ang[2])};
     });
@@ -1675,6 +1911,7 @@ void ow_set_velocity(ow_world *world, uint32_t i, const float *lin, const float 
 void ow_set_velocity_f64(ow_world *world, uint32_t i, const double *lin, const double *ang) {
     dispatch(world, [&](auto &w) {
         using T = decltype(w.gravity.x);
+        if (lin || ang) w.bodies[i].wakeUp();
         if (lin) w.bodies[i].lin = {T(lin[0]), T(lin[1]), T(lin[2])};
         if (ang) w.bodies[i].ang = {T(ang[0]), T(ang[1]), T(ang[2])};
     });
@@ -1692,6 +1929,7 @@ void ow_apply_spin(ow_world *world, uint32_t i, const float *spin) {
     dispatch(world, [&](auto &w) {
         using T = decltype(w.gravity.x);
         auto &b = w.bodies[i];
+        b.wakeUp();
         if (b.isStatic) return;
         b.ang = {T(spin[0]), T(spin[1]), T(spin[2])};
         Q<T> s{b.ang.x, b.ang.y, b.ang.z, T(0)};

@@ -101,6 +101,14 @@ int ow_create_hull_body(ow_world *world, int hull_id, const float *pos, float ma
                         const float *inv_inertia_diag, int is_static, float restitution,
                         float friction, uint32_t *handles);
 void ow_remove_body(ow_world *world, uint32_t index, uint32_t generation);
+void ow_remove_collider(ow_world *world, uint32_t index, uint32_t generation);
+/* setSleepingEnabled (physics_world.hpp:63); per-slot isSleeping(); wakeUp();
+   applyForce (rigid_body.hpp:53-85).  set_velocity and apply_spin wake the body
+   like the reference's velocity setters. */
+void ow_set_sleeping_enabled(ow_world *world, int enabled);
+void ow_get_sleeping(const ow_world *world, uint8_t *sleeping);
+void ow_wake_body(ow_world *world, uint32_t index);
+void ow_apply_force(ow_world *world, uint32_t index, const float *force);
 uint32_t ow_body_slot_count(const ow_world *world);
 
 /* Per-body state by slot (positions, quaternions xyzw, linear/angular velocity). */

@@ -152,7 +152,36 @@ void rw_remove_body(rw_world *w, uint32_t index, uint32_t generation) {
     w->world.removeBody({index, generation});
 }
 
+void rw_remove_collider(rw_world *w, uint32_t index, uint32_t generation) {
+    w->world.removeCollider({index, generation});
+}
+
 uint32_t rw_body_slot_count(const rw_world *w) { return (uint32_t)w->bodies.size(); }
+
+void rw_set_sleeping_enabled(rw_world *w, int enabled) { w->world.setSleepingEnabled(enabled != 0); }
+
+void rw_get_sleeping(const rw_world *w, uint8_t *sleeping) {
+    for (size_t i = 0; i < w->bodies.size(); ++i) {
+        const RigidBody *b = w->world.getBody(w->bodies[i]);
+        sleeping[i] = b && b->isSleeping() ? 1 : 0;
+    }
+}
+
+void rw_wake_body(rw_world *w, uint32_t index) {
+    if (RigidBody *b = w->world.getBody(w->bodies[index])) b->wakeUp();
+}
+
+void rw_apply_force(rw_world *w, uint32_t index, const float *f) {
+    if (RigidBody *b = w->world.getBody(w->bodies[index])) b->applyForce({f[0], f[1], f[2]});
+}
+
+void rw_set_material(rw_world *w, uint32_t index, float mass, float friction, float restitution) {
+    if (RigidBody *b = w->world.getBody(w->bodies[index])) {
+        b->mass = mass;
+        b->friction = friction;
+        b->restitution = restitution;
+    }
+}
 
 // Orientation idiom of the reference's own tests
 // (tests/solver/sequential_impulse_solver_tests.cpp:349-351).

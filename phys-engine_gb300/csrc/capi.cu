@@ -63,7 +63,7 @@ void fillStats(const pe::StepCounters &c, pe_step_stats *o) {
     o->contact_count = c.contactCount;
     o->solved_contact_count = c.solvedContactCount;
     o->awake_body_count = c.awakeBodyCount;
-    o->sleeping_body_count = 0;
+    o->sleeping_body_count = c.sleepingBodyCount;
     o->x_window_comparisons = c.xWindow;
     o->aabb_pairs = c.aabbPairs;
     o->grid_comparisons = c.gridComparisons;
@@ -170,7 +170,7 @@ pe_status createBody(pe_world *world, int shape, const float *dims, const float 
 
 // RigidBody::integrateRotation (src/dynamics/rigid_body.cpp:110-125).
 void integrateRotation(pe::HostBody &b, float dt) {
-    if (b.isStatic) return;
+    if (b.isStatic || b.sleeping) return;
     const float wx = b.ang[0], wy = b.ang[1], wz = b.ang[2];
     const float x = b.rot[0], y = b.rot[1], z = b.rot[2], w = b.rot[3];
     const float sw = 0.0f;
@@ -266,7 +266,14 @@ pe_status pe_world_set_worker_counts(pe_world *world, uint64_t np, uint64_t solv
 }
 pe_status pe_world_set_sleeping_enabled(pe_world *world, int enabled) {
     if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
-    if (enabled) return fail(PE_ERR_UNSUPPORTED, "sleeping islands are not part of the GPU path");
+    return guarded([&] {
+        world->w->setSleepingEnabled(enabled != 0);
+        return PE_OK;
+    });
+}
+pe_status pe_world_get_sleeping_enabled(const pe_world *world, int *enabled) {
+    if (!world || !enabled) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    *enabled = world->w->sleepingEnabled ? 1 : 0;
     return PE_OK;
 }
 
@@ -379,6 +386,14 @@ pe_status pe_world_set_body(pe_world *world, pe_handle h, const pe_body_state *i
         world->w->pull();
         pe::HostBody *b = world->w->body(h.index, h.generation);
         if (!b) return fail(PE_ERR_STALE_HANDLE, "stale body handle");
+        // A changed velocity or force wakes the body like the reference's
+        // setters (setLinearVelocity / setAngularVelocity / applyForce,
+        // rigid_body.hpp:54-95); pose, mass, material and static-flag edits
+        // wake it at the next step like prepareSleeping's comparison.
+        if (std::memcmp(b->lin, in->linear_velocity, sizeof(b->lin)) != 0 ||
+            std::memcmp(b->ang, in->angular_velocity, sizeof(b->ang)) != 0 ||
+            (!in->is_static && std::memcmp(b->force, in->force, sizeof(b->force)) != 0))
+            b->wakeUp();
         std::memcpy(b->pos, in->position, sizeof(b->pos));
         std::memcpy(b->rot, in->rotation, sizeof(b->rot));
         std::memcpy(b->lin, in->linear_velocity, sizeof(b->lin));
@@ -390,6 +405,75 @@ pe_status pe_world_set_body(pe_world *world, pe_handle h, const pe_body_state *i
         b->friction = in->friction;
         b->isStatic = in->is_static != 0;
         world->w->touch();
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_body_is_sleeping(pe_world *world, pe_handle h, int *sleeping) {
+    if (!world || !sleeping) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        world->w->pull();
+        pe::HostBody *b = world->w->body(h.index, h.generation);
+        if (!b) return fail(PE_ERR_STALE_HANDLE, "stale body handle");
+        *sleeping = b->isSleeping() ? 1 : 0;
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_body_wake_up(pe_world *world, pe_handle h) {
+    if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
+    return guarded([&] {
+        world->w->pull();
+        pe::HostBody *b = world->w->body(h.index, h.generation);
+        if (!b) return fail(PE_ERR_STALE_HANDLE, "stale body handle");
+        b->wakeUp();
+        world->w->touch();
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_body_apply_force(pe_world *world, pe_handle h, const float *force) {
+    if (!world || !force) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        world->w->pull();
+        pe::HostBody *b = world->w->body(h.index, h.generation);
+        if (!b) return fail(PE_ERR_STALE_HANDLE, "stale body handle");
+        // RigidBody::applyForce (rigid_body.hpp:77-85)
+        if (!b->isStatic) {
+            if (force[0] != 0.0f || force[1] != 0.0f || force[2] != 0.0f) b->wakeUp();
+            for (int k = 0; k < 3; ++k) b->force[k] += force[k];
+        }
+        world->w->touch();
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_body_set_velocity(pe_world *world, pe_handle h, const float *linear, const float *angular) {
+    if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
+    return guarded([&] {
+        world->w->pull();
+        pe::HostBody *b = world->w->body(h.index, h.generation);
+        if (!b) return fail(PE_ERR_STALE_HANDLE, "stale body handle");
+        // setLinearVelocity / setAngularVelocity wake the body (rigid_body.hpp:59-63, :91-95)
+        if (linear) {
+            b->wakeUp();
+            std::memcpy(b->lin, linear, sizeof(b->lin));
+        }
+        if (angular) {
+            b->wakeUp();
+            std::memcpy(b->ang, angular, sizeof(b->ang));
+        }
+        world->w->touch();
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_read_sleeping(pe_world *world, uint8_t *sleeping) {
+    if (!world || !sleeping) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        world->w->pull();
+        const auto &bs = world->w->bodies;
+        for (size_t i = 0; i < bs.size(); ++i) sleeping[i] = bs[i].alive && bs[i].isSleeping() ? 1 : 0;
         return PE_OK;
     });
 }

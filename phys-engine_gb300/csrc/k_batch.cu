@@ -55,7 +55,7 @@ __device__ __forceinline__ uint32_t scanBlock(uint32_t v, uint32_t &total, uint3
 __device__ __forceinline__ WorldView worldView(const BatchView &b, const WorldDesc &d) {
     const uint32_t s = d.bodyStart;
     const BodyState &c = b.state[b.parity], &n = b.state[b.parity ^ 1u];
-    WorldView w;
+    WorldView w{};
     w.nb = w.nc = d.bodyCount;
     w.cur = BodyState{c.pos + s, c.rot + s, c.lin + s, c.ang + s};
     w.nxt = BodyState{n.pos + s, n.rot + s, n.lin + s, n.ang + s};

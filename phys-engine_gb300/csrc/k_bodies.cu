@@ -17,7 +17,21 @@ __device__ __forceinline__ void integrateAabbOne(const WorldView &w, uint32_t *s
     if (i < w.nb) {
         const uint32_t f = w.bflags[i];
         V3 lin = f4xyz(w.cur.lin[i]);
-        if ((f & kBodyAlive) && !(f & kBodyStatic)) {
+        bool integrate = (f & kBodyAlive) && !(f & kBodyStatic);
+        if (w.sleepMode) {
+            // integrateVelocity skips sleeping bodies; SleepState::integratedVelocity
+            // = !isSleeping() (physics_world.cpp:528-537); the island scratch
+            // of this step starts empty.
+            const uint32_t sf = w.sleepIn[i];
+            const bool asleep = (sf & kSleepAsleep) != 0;
+            if (asleep) integrate = false;
+            w.sleepOut[i] = (sf & ~kSleepIntegrated) | (asleep && !(f & kBodyStatic) ? 0u : kSleepIntegrated);
+            w.quietOut[i] = w.quietIn[i];
+            w.sleepParent[i] = i;
+            w.sleepIsland[i] = 0u;
+            w.sleepQuietMin[i] = 0x7F800000u;  // +inf: no quiet time folded in yet
+        }
+        if (integrate) {
             const V3 force = w.force ? f4xyz(w.force[i]) : V3{0.0f, 0.0f, 0.0f};
             lin = integrateVelocity(lin, V3{w.gx, w.gy, w.gz}, force, w.mat[i].x, w.dt);
         }
@@ -91,7 +105,9 @@ __global__ void k_integrate_pose(WorldView w, DevStats *st, DevStats *hostOut, u
     if (i < w.nb) {
         const uint32_t f = w.bflags[i];
         float4 p4 = w.cur.pos[i], q4 = w.cur.rot[i];
-        if ((f & kBodyAlive) && !(f & kBodyStatic)) {
+        const bool dyn = (f & kBodyAlive) && !(f & kBodyStatic);
+        const uint32_t sf = w.sleepMode ? w.sleepOut[i] : 0u;
+        if (dyn && !(sf & kSleepAsleep)) {
             V3 pos = f4xyz(p4);
             Q rot = f4q(q4);
             integratePose(pos, rot, f4xyz(w.nxt.lin[i]), f4xyz(w.nxt.ang[i]), w.dt);
@@ -100,6 +116,24 @@ __global__ void k_integrate_pose(WorldView w, DevStats *st, DevStats *hostOut, u
         }
         w.nxt.pos[i] = p4;
         w.nxt.rot[i] = q4;
+        if (w.sleepMode && dyn) {
+            // finishSleeping's first loop (physics_world.cpp:474-490): the quiet
+            // time of an awake body, folded into its island's minimum.
+            const float quietSpeedSquared = 0.05f * 0.05f, timeToSleep = 0.5f;
+            float q = w.quietOut[i];
+            if (!(sf & kSleepAsleep)) {
+                const V3 v = f4xyz(w.nxt.lin[i]), a = f4xyz(w.nxt.ang[i]);
+                if (!(sf & kSleepWake) && w.dt > 0.0f && isfinite(w.dt) && dot(v, v) <= quietSpeedSquared &&
+                    dot(a, a) <= quietSpeedSquared) {
+                    const float t = q + w.dt;
+                    q = timeToSleep < t ? timeToSleep : t;
+                } else {
+                    q = 0.0f;
+                }
+                w.quietOut[i] = q;
+            }
+            atomicMin(&w.sleepQuietMin[w.sleepParent[i]], __float_as_uint(q));
+        }
     }
     if (st) {
         __syncthreads();
@@ -126,12 +160,14 @@ __global__ void k_integrate_pose(WorldView w, DevStats *st, DevStats *hostOut, u
 
 // Caller forces (3 floats per body) into the force array; RigidBody::applyForce
 // ignores static bodies (rigid_body.cpp), dead slots get none.
-__global__ void k_expand_forces(const float *f3, const uint32_t *bflags, float4 *force, uint32_t n) {
+__global__ void k_expand_forces(const float *f3, const uint32_t *bflags, float4 *force, uint32_t n, uint32_t *sleep) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t fl = bflags[i];
     const bool dyn = (fl & kBodyAlive) && !(fl & kBodyStatic);
-    force[i] = dyn ? make_float4(f3[3 * i], f3[3 * i + 1], f3[3 * i + 2], 0.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float fx = f3[3 * i], fy = f3[3 * i + 1], fz = f3[3 * i + 2];
+    force[i] = dyn ? make_float4(fx, fy, fz, 0.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (sleep && dyn && (fx != 0.0f || fy != 0.0f || fz != 0.0f)) sleep[i] = (sleep[i] & ~kSleepAsleep) | kSleepWake;
 }
 
 // Positions as 3 floats per body (the caller's layout).
@@ -144,9 +180,10 @@ __global__ void k_pack_positions(const float4 *pos, float *p3, uint32_t n) {
     p3[3 * i + 2] = p.z;
 }
 
-void launchExpandForces(const float *f3, const uint32_t *bflags, float4 *force, uint32_t n, cudaStream_t s) {
+void launchExpandForces(const float *f3, const uint32_t *bflags, float4 *force, uint32_t n, cudaStream_t s,
+                        uint32_t *sleep) {
     if (!n) return;
-    k_expand_forces<<<(n + 255) / 256, 256, 0, s>>>(f3, bflags, force, n);
+    k_expand_forces<<<(n + 255) / 256, 256, 0, s>>>(f3, bflags, force, n, sleep);
     PE_LAUNCHED();
 }
 

@@ -28,8 +28,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
     SolverBuffers &sb = a.sb;
     for (uint32_t m = gtid; m < M; m += gstride) {
         uint32_t ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
-        bool da = ba < w.nb && (w.bflags[ba] & kBodyAlive) && w.bgen[ba] == a.mv.genA[m] && !(w.bflags[ba] & kBodyStatic);
-        bool db = bb < w.nb && (w.bflags[bb] & kBodyAlive) && w.bgen[bb] == a.mv.genB[m] && !(w.bflags[bb] & kBodyStatic);
+        bool da = ba < w.nb && w.bgen[ba] == a.mv.genA[m] && bodyMoves(w.bflags[ba]);
+        bool db = bb < w.nb && w.bgen[bb] == a.mv.genB[m] && bodyMoves(w.bflags[bb]);
         sb.dyn[m] = (da ? 1u : 0u) | (db ? 2u : 0u);
         sb.color[m] = kUncolored;
         if (da) {
@@ -190,7 +190,8 @@ __global__ void k_cache_counts(SolveArgs a) {
         const uint32_t m = a.sb.cacheVals[k];
         const uint32_t ia = a.mv.bodyA[m], ib = a.mv.bodyB[m];
         const bool valid = ia < w.nb && ib < w.nb && (w.bflags[ia] & kBodyAlive) && (w.bflags[ib] & kBodyAlive) &&
-                           w.bgen[ia] == a.mv.genA[m] && w.bgen[ib] == a.mv.genB[m];
+                           w.bgen[ia] == a.mv.genA[m] && w.bgen[ib] == a.mv.genB[m] &&
+                           solvedPair(w, w.bflags[ia], w.bflags[ib]);
         a.sb.cacheCounts[k] = valid ? a.mv.pointCount[m] : 0u;
     }
 }

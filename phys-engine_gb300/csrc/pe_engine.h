@@ -40,10 +40,21 @@ enum : uint32_t {
     kErrSmallPath = 64u,  // a single-block path saw more work than it holds: re-run on the full path
     kErrBodyPairs = 128u, // a body had more grid partners than the per-body pair path holds
     kErrHashRange = 256u, // a grid cell lies outside the hashed grid's coordinate range
+    kErrCacheCapacity = 512u, // the warm-start cache with carried sleeping entries exceeds its capacity
 };
 
-// Body flag bits (bflags) and collider flag layout (cflags).
-enum : uint32_t { kBodyAlive = 1u, kBodyStatic = 2u };
+// Body flag bits (bflags) and collider flag layout (cflags).  kBodySleeping
+// is derived data the step writes for the solver: the body sleeps this step
+// (after the contact wake pass).
+enum : uint32_t { kBodyAlive = 1u, kBodyStatic = 2u, kBodySleeping = 4u };
+// Per-body sleep flags (PhysicsWorld sleeping, physics_world.cpp:341-516):
+// RigidBody::sleeping, RigidBody::wakeRequested, and the per-step record of
+// whether gravity was integrated (SleepState::integratedVelocity).
+enum : uint32_t { kSleepAsleep = 1u, kSleepWake = 2u, kSleepIntegrated = 4u };
+// A body that moves under impulses: alive, not static, not sleeping.
+__host__ __device__ inline bool bodyMoves(uint32_t bflags) {
+    return (bflags & (kBodyAlive | kBodyStatic | kBodySleeping)) == kBodyAlive;
+}
 enum : uint32_t { kColliderAlive = 1u };
 __host__ __device__ inline uint32_t colliderShape(uint32_t cflags) { return (cflags >> 8) & 0xFFu; }
 enum : uint32_t { kShapeSphere = 0, kShapeBox = 1, kShapeHull = 2 };
@@ -89,6 +100,10 @@ struct DevStats {
     uint32_t windowWork;     // SAP flattened window work
     uint32_t solved;         // manifolds whose bodies are valid (prepared)
     uint32_t cellKeyBits;    // bits of the packed grid cell key this step needed
+    uint32_t awakeBodies;    // sleeping on: live dynamic bodies awake / asleep after the step
+    uint32_t sleepingBodies;
+    uint32_t carried;        // sleeping on: warm-start entries carried for sleeping contacts
+    uint32_t pad0;
     int32_t cellLo[3];
     int32_t cellHi[3];
     // Stage boundaries (global timer, ns), written by the stage kernels
@@ -119,6 +134,17 @@ struct WorldView {
     float4 *aabbMin;
     float4 *aabbMax;
     float gx, gy, gz, dt;
+    // Sleeping (zero / null when off).  Sleep flags and quiet times are read
+    // from the step's input copy and written to its output copy; parent,
+    // island and quietMin are per-body scratch of the island pass.
+    uint32_t sleepMode;
+    const uint32_t *sleepIn;
+    uint32_t *sleepOut;
+    const float *quietIn;
+    float *quietOut;
+    uint32_t *sleepParent;
+    uint32_t *sleepIsland;
+    uint32_t *sleepQuietMin;
 };
 
 // Contact manifolds (structure of arrays; manifold m owns points 4m..4m+3).

@@ -84,6 +84,12 @@ struct VelStage {
 };
 constexpr uint32_t kSlotFree = 0xFFFFFFFFu;
 
+// With sleeping on, a manifold among static and sleeping bodies only is not
+// solved, cached or counted (sequential_impulse_solver.cpp:321-324).
+__device__ __forceinline__ bool solvedPair(const WorldView &w, uint32_t flA, uint32_t flB) {
+    return !w.sleepMode || bodyMoves(flA) || bodyMoves(flB);
+}
+
 // --------------------------------------------------------------- prepare ---
 // prepareBody (:275-287) + prepareContactPoints (:101-214) + the cache lookup
 // of warmStartPrepared (:448-490).  Data are written by manifold index m (no
@@ -130,7 +136,7 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
         // A manifold whose body handles are stale is not solved and not cached
         // (sequential_impulse_solver.cpp:317-320).
         const bool valid = ia < w.nb && ib < w.nb && (flA & kBodyAlive) && (flB & kBodyAlive) && bgA == gA &&
-                           bgB == gB;
+                           bgB == gB && solvedPair(w, flA, flB);
         const bool sA = (flA & kBodyStatic) != 0, sB = (flB & kBodyStatic) != 0;
         const Q qA = f4q(qA4), qB = f4q(qB4);
         const M3 IA = inverseInertiaWorld(qA, iA.x, iA.y, iA.z);
@@ -438,7 +444,7 @@ __device__ __forceinline__ bool manifoldBodiesValid(const SolveArgs &a, uint32_t
     const uint32_t ia = a.mv.bodyA[m], ib = a.mv.bodyB[m];
     const WorldView &w = a.w;
     return ia < w.nb && ib < w.nb && (w.bflags[ia] & kBodyAlive) && (w.bflags[ib] & kBodyAlive) &&
-           w.bgen[ia] == a.mv.genA[m] && w.bgen[ib] == a.mv.genB[m];
+           w.bgen[ia] == a.mv.genA[m] && w.bgen[ib] == a.mv.genB[m] && solvedPair(w, w.bflags[ia], w.bflags[ib]);
 }
 
 // Per-manifold body flags: bit 0 / bit 1 body A / B live, of the manifold's
@@ -450,8 +456,10 @@ __device__ __forceinline__ uint32_t manifoldFlags(const SolveArgs &a, uint32_t m
     const WorldView &w = a.w;
     const bool okA = ba < w.nb && (w.bflags[ba] & kBodyAlive) && w.bgen[ba] == a.mv.genA[m];
     const bool okB = bb < w.nb && (w.bflags[bb] & kBodyAlive) && w.bgen[bb] == a.mv.genB[m];
-    return (okA && !(w.bflags[ba] & kBodyStatic) ? kFlagDynA : 0u) |
-           (okB && !(w.bflags[bb] & kBodyStatic) ? kFlagDynB : 0u) | (okA && okB ? kFlagValid : 0u);
+    const bool dA = okA && !(w.bflags[ba] & (kBodyStatic | kBodySleeping));
+    const bool dB = okB && !(w.bflags[bb] & (kBodyStatic | kBodySleeping));
+    return (dA ? kFlagDynA : 0u) | (dB ? kFlagDynB : 0u) |
+           (okA && okB && (!w.sleepMode || dA || dB) ? kFlagValid : 0u);
 }
 
 // Front of the single-block solver: staging slots, colouring and the solve
@@ -725,7 +733,8 @@ __device__ inline void solveBlockCache(const SolveArgs &a, const CacheView &nc, 
         for (uint32_t i = tid; i < M; i += nt) {
             const uint32_t ia = a.mv.bodyA[i], ib = a.mv.bodyB[i];
             const bool valid = ia < w.nb && ib < w.nb && (w.bflags[ia] & kBodyAlive) && (w.bflags[ib] & kBodyAlive) &&
-                               w.bgen[ia] == a.mv.genA[i] && w.bgen[ib] == a.mv.genB[i];
+                               w.bgen[ia] == a.mv.genA[i] && w.bgen[ib] == a.mv.genB[i] &&
+                               solvedPair(w, w.bflags[ia], w.bflags[ib]);
             s_dyn[i] = valid ? a.mv.pointCount[i] : 0u;
         }
         __syncthreads();
@@ -753,7 +762,8 @@ __device__ inline void solveBlockCache(const SolveArgs &a, const CacheView &nc, 
         const uint32_t m = sb.order[(uint32_t)(s_sort[i] & 0xFFFu)];
         const uint32_t ia = a.mv.bodyA[m], ib = a.mv.bodyB[m];
         const bool valid = ia < w.nb && ib < w.nb && (w.bflags[ia] & kBodyAlive) && (w.bflags[ib] & kBodyAlive) &&
-                           w.bgen[ia] == a.mv.genA[m] && w.bgen[ib] == a.mv.genB[m];
+                           w.bgen[ia] == a.mv.genA[m] && w.bgen[ib] == a.mv.genB[m] &&
+                           solvedPair(w, w.bflags[ia], w.bflags[ib]);
         s_dyn[i] = valid ? a.mv.pointCount[m] : 0u;
     }
     __syncthreads();

@@ -109,7 +109,28 @@ void launchIntegratePose(const WorldView &w, cudaStream_t s, DevStats *st = null
                          uint32_t *done = nullptr);
 // Host-facing transfers: caller forces (3 floats per body) into the force
 // array with static / dead bodies masked; positions packed to 3 floats.
-void launchExpandForces(const float *f3, const uint32_t *bflags, float4 *force, uint32_t n, cudaStream_t s);
+// sleep (nullable): the committed sleep flags; a nonzero force wakes its body
+// (RigidBody::applyForce, rigid_body.hpp:77-85).
+void launchExpandForces(const float *f3, const uint32_t *bflags, float4 *force, uint32_t n, cudaStream_t s,
+                        uint32_t *sleep = nullptr);
+// Sleeping (k_sleep.cu).  launchSleepWake: the wake pass of prepareSleeping
+// over the last step's M contacts, on the committed sleep flags and quiet
+// times (run before a step that follows host edits).  launchSleepContacts: the
+// wake pass after the narrowphase inside the step (also writes the solver's
+// sleeping bit into bflags).  launchSleepFinish: finishSleeping's sleep
+// decision and counts after the pose kernel.  launchCacheCarry: the next
+// warm-start cache from the carried sleeping entries of the old cache and
+// the solver's entries (written to tmp).
+void launchSleepWake(const WorldView &w, const ManifoldView &mv, uint32_t Mhost, uint32_t mcap, uint32_t *flags,
+                     float *quiet, uint32_t *err, cudaStream_t s);
+void launchSleepContacts(const WorldView &w, const ManifoldView &mv, DevStats *st, uint32_t mcap, uint32_t *bflags,
+                         cudaStream_t s);
+void launchSleepFinish(const WorldView &w, DevStats *st, DevStats *hostOut, uint32_t *done, cudaStream_t s);
+void launchSleepBits(const WorldView &w, const uint32_t *flags, uint32_t *bflags, cudaStream_t s);
+void launchCacheCarry(const WorldView &w, const CacheView &oldCache, const uint32_t *oldCount, const CacheView &tmp,
+                      const uint32_t *tmpCount, const CacheView &newCache, uint32_t *newCount, uint32_t cap,
+                      uint32_t *carry, uint32_t *carryPos, uint32_t *carryTotal, DevStats *st, Scratch &ws,
+                      cudaStream_t s);
 void launchPackPositions(const float4 *pos, float *p3, uint32_t n, cudaStream_t s);
 void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, BroadBuffers &bb, PairBuffers &pb,
                DevStats *st, Scratch &ws, cudaStream_t s);

@@ -1,5 +1,6 @@
 // GPU world: host mirror, device state and the step pipeline
-// (PhysicsWorld::step, src/world/physics_world.cpp:518-782, sleeping off).
+// (PhysicsWorld::step, src/world/physics_world.cpp:518-782, with sleeping
+// islands, :341-516).
 #include "world.h"
 
 #include <algorithm>
@@ -11,6 +12,15 @@ namespace {
 template <class T> void upload(DeviceArray<T> &d, const std::vector<T> &h, cudaStream_t s) {
     d.reserve(h.size());
     if (!h.empty()) PE_CHECK(cudaMemcpyAsync(d.ptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+// Grows d to at least n elements keeping its first `keep` elements.
+template <class T> void reserveKeep(DeviceArray<T> &d, size_t n, size_t keep) {
+    if (n <= d.count && d.ptr) return;
+    DeviceArray<T> g;
+    g.reserve(n);
+    keep = std::min(keep, d.count);
+    if (d.ptr && keep) PE_CHECK(cudaMemcpy(g.ptr, d.ptr, keep * sizeof(T), cudaMemcpyDeviceToDevice));
+    d.swap(g);
 }
 inline uint32_t grow(uint32_t need, uint32_t have) {
     uint64_t n = std::max<uint64_t>(need, have);
@@ -56,12 +66,14 @@ uint32_t World::addBody(const HostBody &b, uint32_t &generation) {
         bodies[idx] = b;
         bodies[idx].generation = g;
         bodies[idx].alive = true;
+        bodies[idx].wakeUp();  // PhysicsWorld::addBody wakes the body (physics_world.cpp:171, :177)
         generation = g;
         return idx;
     }
     bodies.push_back(b);
     bodies.back().generation = 0;
     bodies.back().alive = true;
+    bodies.back().wakeUp();
     generation = 0;
     return (uint32_t)bodies.size() - 1;
 }
@@ -69,6 +81,8 @@ uint32_t World::addBody(const HostBody &b, uint32_t &generation) {
 uint32_t World::addCollider(const HostCollider &c, uint32_t &generation) {
     pull();
     hostDirty_ = true;
+    // PhysicsWorld::addCollider wakes the collider's body (physics_world.cpp:276-281)
+    if (HostBody *b = body(c.body, c.bodyGeneration)) b->wakeUp();
     if (!freeColliders.empty()) {
         uint32_t idx = freeColliders.back();
         freeColliders.pop_back();
@@ -92,6 +106,7 @@ void World::removeBody(uint32_t index, uint32_t generation) {
     HostBody &b = bodies[index];
     if (!b.alive || b.generation != generation) return;
     hostDirty_ = true;
+    wakeContacts(index, generation);
     b.alive = false;
     b.generation++;
     freeBodies.push_back(index);
@@ -111,6 +126,9 @@ void World::removeCollider(uint32_t index, uint32_t generation) {
     HostCollider &c = colliders[index];
     if (!c.alive || c.generation != generation) return;
     hostDirty_ = true;
+    // PhysicsWorld::removeCollider wakes the body and its contacts (physics_world.cpp:309-311)
+    if (HostBody *b = body(c.body, c.bodyGeneration)) b->wakeUp();
+    wakeContacts(c.body, c.bodyGeneration);
     c.alive = false;
     c.generation++;
     freeColliders.push_back(index);
@@ -130,6 +148,37 @@ HostCollider *World::collider(uint32_t index, uint32_t generation) {
     return &c;
 }
 
+void World::wakeContacts(uint32_t index, uint32_t generation) {
+    if (!sleepingEnabled || !lastManifolds_) return;
+    const uint32_t M = lastManifolds_;
+    std::vector<uint32_t> ba(M), ga(M), bbv(M), gb(M);
+    PE_CHECK(cudaMemcpy(ba.data(), mBodyA_.ptr, M * 4, cudaMemcpyDeviceToHost));
+    PE_CHECK(cudaMemcpy(ga.data(), mGenA_.ptr, M * 4, cudaMemcpyDeviceToHost));
+    PE_CHECK(cudaMemcpy(bbv.data(), mBodyB_.ptr, M * 4, cudaMemcpyDeviceToHost));
+    PE_CHECK(cudaMemcpy(gb.data(), mGenB_.ptr, M * 4, cudaMemcpyDeviceToHost));
+    for (uint32_t m = 0; m < M; ++m) {
+        if (ba[m] == index && ga[m] == generation)
+            if (HostBody *o = body(bbv[m], gb[m]); o && !o->isStatic) o->wakeUp();
+        if (bbv[m] == index && gb[m] == generation)
+            if (HostBody *o = body(ba[m], ga[m]); o && !o->isStatic) o->wakeUp();
+    }
+}
+
+void World::setSleepingEnabled(bool enabled) {
+    if (sleepingEnabled == enabled) return;
+    pull();
+    sleepingEnabled = enabled;
+    // the sleep states start over (quiet times zero, no snapshot) and every
+    // live body wakes
+    for (HostBody &b : bodies) {
+        b.quiet = 0.0f;
+        b.snapValid = false;
+        if (b.alive) b.wakeUp();
+    }
+    hostDirty_ = true;
+    dropGraphs();
+}
+
 int World::addHull(const float *verts, uint32_t count) {
     hostDirty_ = true;
     hullVerts.insert(hullVerts.end(), verts, verts + 3 * (size_t)count);
@@ -142,11 +191,19 @@ void World::pull() {
     if (!deviceNewer_) return;
     PE_CHECK(cudaSetDevice(device_));
     std::vector<float4> p(nb_), q(nb_), l(nb_), a(nb_);
+    std::vector<uint32_t> sf;
+    std::vector<float> qt;
     if (nb_) {
         PE_CHECK(cudaMemcpyAsync(p.data(), pos_[cur_].ptr, nb_ * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
         PE_CHECK(cudaMemcpyAsync(q.data(), rot_[cur_].ptr, nb_ * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
         PE_CHECK(cudaMemcpyAsync(l.data(), lin_[cur_].ptr, nb_ * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
         PE_CHECK(cudaMemcpyAsync(a.data(), ang_[cur_].ptr, nb_ * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
+        if (sleepingEnabled && sleep_[cur_].ptr) {
+            sf.resize(nb_);
+            qt.resize(nb_);
+            PE_CHECK(cudaMemcpyAsync(sf.data(), sleep_[cur_].ptr, nb_ * 4, cudaMemcpyDeviceToHost, stream_));
+            PE_CHECK(cudaMemcpyAsync(qt.data(), quiet_[cur_].ptr, nb_ * 4, cudaMemcpyDeviceToHost, stream_));
+        }
         PE_CHECK(cudaStreamSynchronize(stream_));
     }
     for (uint32_t i = 0; i < nb_ && i < bodies.size(); ++i) {
@@ -157,6 +214,19 @@ void World::pull() {
         b.ang[0] = a[i].x; b.ang[1] = a[i].y; b.ang[2] = a[i].z;
         // PhysicsWorld::step clears forces of live bodies (physics_world.cpp:766)
         if (b.alive) b.force[0] = b.force[1] = b.force[2] = 0.0f;
+        if (!sf.empty()) {
+            b.sleeping = (sf[i] & kSleepAsleep) != 0;
+            b.wakeRequested = (sf[i] & kSleepWake) != 0;
+            b.quiet = qt[i];
+        }
+        // the end-of-step state edits are compared against (finishSleeping, :506-511)
+        b.snapValid = true;
+        std::memcpy(b.snapPos, b.pos, sizeof(b.pos));
+        std::memcpy(b.snapRot, b.rot, sizeof(b.rot));
+        b.snapMass = b.mass;
+        b.snapRestitution = b.restitution;
+        b.snapFriction = b.friction;
+        b.snapStatic = b.isStatic;
     }
     deviceNewer_ = false;
 }
@@ -184,10 +254,26 @@ void World::push() {
     nc_ = (uint32_t)colliders.size();
     ensureCapacity();
     std::vector<float4> p(nb_), q(nb_), l(nb_), a(nb_), f(nb_), mat(nb_), ii(nb_);
-    std::vector<uint32_t> flags(nb_), gen(nb_);
+    std::vector<uint32_t> flags(nb_), gen(nb_), sf(sleepingEnabled ? nb_ : 0);
+    std::vector<float> qt(sleepingEnabled ? nb_ : 0);
     forces_ = false;
+    // prepareSleeping (physics_world.cpp:434-452): a gravity change, or an
+    // edit of a body's pose, mass, material or static flag since the last
+    // step, wakes the body.
+    const bool gravityChanged = gravity[0] != sleepGravity_[0] || gravity[1] != sleepGravity_[1] ||
+                                gravity[2] != sleepGravity_[2];
     for (uint32_t i = 0; i < nb_; ++i) {
-        const HostBody &b = bodies[i];
+        HostBody &b = bodies[i];
+        if (sleepingEnabled) {
+            if (b.alive &&
+                (gravityChanged || !b.snapValid || b.snapMass != b.mass || b.snapStatic != b.isStatic ||
+                 b.snapFriction != b.friction || b.snapRestitution != b.restitution || b.snapPos[0] != b.pos[0] ||
+                 b.snapPos[1] != b.pos[1] || b.snapPos[2] != b.pos[2] || b.snapRot[0] != b.rot[0] ||
+                 b.snapRot[1] != b.rot[1] || b.snapRot[2] != b.rot[2] || b.snapRot[3] != b.rot[3]))
+                b.wakeUp();
+            sf[i] = (b.sleeping ? kSleepAsleep : 0u) | (b.wakeRequested ? kSleepWake : 0u);
+            qt[i] = b.quiet;
+        }
         p[i] = make_float4(b.pos[0], b.pos[1], b.pos[2], 0.0f);
         q[i] = make_float4(b.rot[0], b.rot[1], b.rot[2], b.rot[3]);
         l[i] = make_float4(b.lin[0], b.lin[1], b.lin[2], 0.0f);
@@ -210,6 +296,11 @@ void World::push() {
     upload(iinv_, ii, stream_);
     upload(bflags_, flags, stream_);
     upload(bgen_, gen, stream_);
+    if (sleepingEnabled) {
+        upload(sleep_[cur_], sf, stream_);
+        upload(quiet_[cur_], qt, stream_);
+        wakeCheck_ = true;
+    }
 
     std::vector<uint32_t> cb(nc_), cg(nc_), cf(nc_);
     std::vector<float4> cs(nc_), lp(nc_), lr(nc_);
@@ -275,6 +366,16 @@ void World::ensureCapacity() {
         lin_[k].reserve(nb);
         ang_[k].reserve(nb);
     }
+    if (sleepingEnabled) {
+        for (int k = 0; k < 2; ++k) {
+            sleep_[k].reserve(nb);
+            quiet_[k].reserve(nb);
+        }
+        sParent_.reserve(nb);
+        sIsland_.reserve(nb);
+        sQuietMin_.reserve(nb);
+        sleepErr_.reserve(1);
+    }
     aabbMin_.reserve(nc);
     aabbMax_.reserve(nc);
     collectFlags_.reserve(nc);
@@ -329,17 +430,20 @@ void World::ensureCapacity() {
 
     if (mcap_ < pairCap_) mcap_ = pairCap_;
     const uint32_t m = mcap_;
-    mBodyA_.reserve(m);
-    mGenA_.reserve(m);
-    mBodyB_.reserve(m);
-    mGenB_.reserve(m);
-    mCount_.reserve(m);
-    mRest_.reserve(m);
-    mNormal_.reserve(m);
-    mAnchorA_.reserve(4 * (size_t)m);
-    mAnchorB_.reserve(4 * (size_t)m);
-    mImpulse_.reserve(4 * (size_t)m);
-    mFeature_.reserve(4 * (size_t)m);
+    // The last step's manifolds survive growth (contacts(), and the wake pass
+    // before the next step reads them).
+    const size_t keep = lastManifolds_;
+    reserveKeep(mBodyA_, m, keep);
+    reserveKeep(mGenA_, m, keep);
+    reserveKeep(mBodyB_, m, keep);
+    reserveKeep(mGenB_, m, keep);
+    reserveKeep(mCount_, m, keep);
+    reserveKeep(mRest_, m, keep);
+    reserveKeep(mNormal_, m, keep);
+    reserveKeep(mAnchorA_, 4 * (size_t)m, 4 * keep);
+    reserveKeep(mAnchorB_, 4 * (size_t)m, 4 * keep);
+    reserveKeep(mImpulse_, 4 * (size_t)m, 4 * keep);
+    reserveKeep(mFeature_, 4 * (size_t)m, 4 * keep);
 
     sBest_.reserve(nb);
     sUsed_.reserve(2 * (size_t)nb);
@@ -399,7 +503,7 @@ void World::ensureCapacity() {
                         sIslandList_.ptr};
 
     // Warm-start caches keep their contents when they grow.
-    const uint32_t needCache = 4 * m;
+    const uint32_t needCache = std::max(4 * m, cacheNeed_);
     if (cacheCap_ < needCache) {
         for (int k = 0; k < 2; ++k) {
             DeviceArray<unsigned long long> nk, ng;
@@ -430,11 +534,23 @@ void World::ensureCapacity() {
         }
         cacheCap_ = needCache;
     }
-    ensureScratch(std::max({nc, pairCap_, entryCap_, m}));
+    if (sleepingEnabled) {
+        // the solver's entries before the merge with the carried ones
+        tKey_.reserve(cacheCap_);
+        tGens_.reserve(cacheCap_);
+        tA_.reserve(cacheCap_);
+        tB_.reserve(cacheCap_);
+        tT2_.reserve(cacheCap_);
+        tCount_.reserve(1);
+        carry_.reserve(cacheCap_);
+        carryPos_.reserve(cacheCap_);
+        carryTotal_.reserve(1);
+    }
+    ensureScratch(std::max({nc, pairCap_, entryCap_, m, cacheCap_}));
 }
 
 WorldView World::view(float dt) {
-    WorldView w;
+    WorldView w{};
     w.nb = nb_;
     w.nc = nc_;
     w.cur = BodyState{pos_[cur_].ptr, rot_[cur_].ptr, lin_[cur_].ptr, ang_[cur_].ptr};
@@ -458,6 +574,16 @@ WorldView World::view(float dt) {
     w.gy = gravity[1];
     w.gz = gravity[2];
     w.dt = dt;
+    if (sleepingEnabled) {
+        w.sleepMode = 1;
+        w.sleepIn = sleep_[cur_].ptr;
+        w.sleepOut = sleep_[1 - cur_].ptr;
+        w.quietIn = quiet_[cur_].ptr;
+        w.quietOut = quiet_[1 - cur_].ptr;
+        w.sleepParent = sParent_.ptr;
+        w.sleepIsland = sIsland_.ptr;
+        w.sleepQuietMin = sQuietMin_.ptr;
+    }
     return w;
 }
 
@@ -501,13 +627,26 @@ void World::runPipeline(float dt) {
         launchPairsFinalize(dense_ ? nullptr : inSlot_.ptr, cbody_.ptr, cbgen_.ptr, pb_, st, ws_, s);
     ManifoldView mv = manifoldView();
     launchNarrowphase(w, pb_, mv, mcap_, st, ws_, s, fused ? ws_.scanState + narrowOff : nullptr, fused);
-    launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], cacheView(1 - cache_), &cCount_.ptr[1 - cache_],
-                 cacheCap_, sb_, iterations, orderMode, coopBlocks_, blockSolver_, blockM_, identityColliders_, st,
-                 ws_, s);
-    // the pose kernel's last block copies the counters to the pinned host
+    const bool sleeping = sleepingEnabled;
+    // contacts can wake islands after the gravity pass (physics_world.cpp:741-748)
+    if (sleeping) launchSleepContacts(w, mv, st, mcap_, bflags_.ptr, s);
+    // with sleeping on the solver's cache entries are merged with the carried
+    // entries of sleeping contacts into the next cache
+    const CacheView tmp{tKey_.ptr, tGens_.ptr, tA_.ptr, tB_.ptr, tT2_.ptr};
+    launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], sleeping ? tmp : cacheView(1 - cache_),
+                 sleeping ? tCount_.ptr : &cCount_.ptr[1 - cache_], cacheCap_, sb_, iterations, orderMode, coopBlocks_,
+                 blockSolver_, blockM_, identityColliders_, st, ws_, s);
+    if (sleeping)
+        launchCacheCarry(w, cacheView(cache_), &cCount_.ptr[cache_], tmp, tCount_.ptr, cacheView(1 - cache_),
+                         &cCount_.ptr[1 - cache_], cacheCap_, carry_.ptr, carryPos_.ptr, carryTotal_.ptr, st, ws_, s);
+    // the last kernel's last block copies the counters to the pinned host
     // mirror (the device writes it directly); with no bodies a copy node does
-    if (nb_) launchIntegratePose(w, s, st, hostStats_, poseDone_.ptr);
-    else PE_CHECK(cudaMemcpyAsync(hostStats_, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
+    if (nb_) {
+        launchIntegratePose(w, s, st, sleeping ? nullptr : hostStats_, poseDone_.ptr);
+        if (sleeping) launchSleepFinish(w, st, hostStats_, poseDone_.ptr, s);
+    } else {
+        PE_CHECK(cudaMemcpyAsync(hostStats_, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
+    }
 }
 
 bool World::finishStep() {
@@ -532,6 +671,11 @@ bool World::finishStep() {
         // world uses the sort-based pair path from now on.
         bodyPairs_ = false;
         retry = true;
+    }
+    if (h.err & kErrCacheCapacity) {
+        // carried sleeping entries and the solver's entries overflowed the cache
+        cacheNeed_ = grow(h.carried + 4 * std::max(h.manifolds, 1u), cacheCap_);
+        retry = grew = true;
     }
     if (h.err & kErrSmallPath) {
         // A single-block path or the sorted key width was too small: re-run with
@@ -563,7 +707,9 @@ bool World::finishStep() {
     c.candidatePairs = h.pairs;
     c.contactCount = h.manifolds;
     c.solvedContactCount = h.solved;
-    c.awakeBodyCount = dynamicAlive_;
+    c.awakeBodyCount = sleepingEnabled ? h.awakeBodies : dynamicAlive_;
+    c.sleepingBodyCount = sleepingEnabled ? h.sleepingBodies : 0;
+    if (sleepingEnabled) std::memcpy(sleepGravity_, gravity, sizeof(sleepGravity_));
     c.xWindow = h.xWindow;
     c.aabbPairs = h.uniquePairs;
     c.gridComparisons = h.gridComparisons;
@@ -605,7 +751,8 @@ bool World::GraphKey::operator==(const GraphKey &o) const {
            algorithm == o.algorithm && iterations == o.iterations && orderMode == o.orderMode &&
            coopBlocks == o.coopBlocks && blockSolver == o.blockSolver && blockM == o.blockM && pairBits == o.pairBits &&
            blockPairs == o.blockPairs && bodyPairs == o.bodyPairs && hashed == o.hashed && gridKeyBits == o.gridKeyBits && cellSize == o.cellSize && dense == o.dense &&
-           localIdentity == o.localIdentity && forces == o.forces && identityColliders == o.identityColliders;
+           localIdentity == o.localIdentity && forces == o.forces && identityColliders == o.identityColliders &&
+           sleeping == o.sleeping;
 }
 
 World::GraphKey World::currentKey(float dt) const {
@@ -636,6 +783,7 @@ World::GraphKey World::currentKey(float dt) const {
     k.localIdentity = localIdentity_;
     k.forces = forces_;
     k.identityColliders = identityColliders_;
+    k.sleeping = sleepingEnabled;
     return k;
 }
 
@@ -723,9 +871,25 @@ unsigned long long World::launchStep(float dt) {
 void World::step(float dt) {
     PE_CHECK(cudaSetDevice(device_));
     if (algorithm == 2) throw std::invalid_argument("DynamicTree requires a persistent DynamicAabbTree instance");
+    if (sleepingEnabled && (gravity[0] != sleepGravity_[0] || gravity[1] != sleepGravity_[1] ||
+                            gravity[2] != sleepGravity_[2]))
+        hostDirty_ = true;  // a gravity change wakes every body (physics_world.cpp:439-451)
     if (hostDirty_) {
         pull();
         push();
+    }
+    if (sleepingEnabled && wakeCheck_) {
+        // prepareSleeping's wake pass over the last step's contacts, on the
+        // committed state (outside the step's graph: a re-run of the step
+        // must not repeat it)
+        WorldView w = view(dt);
+        launchSleepWake(w, manifoldView(), lastManifolds_, mcap_, sleep_[cur_].ptr, quiet_[cur_].ptr, sleepErr_.ptr,
+                        stream_);
+        uint32_t err = 0;
+        PE_CHECK(cudaMemcpyAsync(&err, sleepErr_.ptr, 4, cudaMemcpyDeviceToHost, stream_));
+        PE_CHECK(cudaStreamSynchronize(stream_));
+        if (err) throw std::runtime_error("step failed on the device: a bounded wait timed out");
+        wakeCheck_ = false;
     }
     for (int attempt = 0; attempt < 8; ++attempt) {
         PE_CHECK(cudaEventRecord(evStart_, stream_));
@@ -774,7 +938,21 @@ void World::writeForces(const float *forces, uint32_t n) {
         // the caller's array as it is; static and dead bodies masked on the device
         xfer3_.reserve(3 * (size_t)nb_);
         PE_CHECK(cudaMemcpyAsync(xfer3_.ptr, forces, 3 * (size_t)n * sizeof(float), cudaMemcpyHostToDevice, stream_));
-        launchExpandForces(xfer3_.ptr, bflags_.ptr, force_.ptr, n, stream_);
+        // a nonzero force wakes its body (RigidBody::applyForce)
+        launchExpandForces(xfer3_.ptr, bflags_.ptr, force_.ptr, n, stream_,
+                           sleepingEnabled ? sleep_[cur_].ptr : nullptr);
+        if (sleepingEnabled) {
+            wakeCheck_ = true;
+            // keep a current host mirror current (a stale one is refreshed
+            // from the device flags at its next pull)
+            if (!deviceNewer_)
+                for (uint32_t i = 0; i < n; ++i) {
+                    HostBody &b = bodies[i];
+                    if (b.alive && !b.isStatic &&
+                        (forces[3 * i] != 0.0f || forces[3 * i + 1] != 0.0f || forces[3 * i + 2] != 0.0f))
+                        b.wakeUp();
+                }
+        }
     }
     PE_CHECK(cudaStreamSynchronize(stream_));  // the caller may reuse its array on return
     forces_ = true;
@@ -1043,11 +1221,26 @@ void World::solveOnly(std::vector<float> &recs, uint32_t count, float dt, int it
     while (blocks < want) blocks <<= 1;
     blocks = std::min<uint32_t>(blocks, (uint32_t)maxCooperativeBlocks(smCount_));
     const bool block = count <= kBlockMaxManifolds && nb_ <= kBlockMaxBodies;
-    launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], cacheView(1 - cache_), &cCount_.ptr[1 - cache_],
-                 cacheCap_, sb_, iters, mode, (int)blocks, block, 0u, false, st, ws_, s);
+    const bool sleeping = sleepingEnabled;
+    const CacheView tmp{tKey_.ptr, tGens_.ptr, tA_.ptr, tB_.ptr, tT2_.ptr};
+    if (sleeping) {
+        // the sleep state is carried over unchanged; the solver's sleeping bit
+        // comes from the committed flags
+        const size_t n = std::max<uint32_t>(nb_, 1);
+        PE_CHECK(cudaMemcpyAsync(sleep_[1 - cur_].ptr, sleep_[cur_].ptr, n * 4, cudaMemcpyDeviceToDevice, s));
+        PE_CHECK(cudaMemcpyAsync(quiet_[1 - cur_].ptr, quiet_[cur_].ptr, n * 4, cudaMemcpyDeviceToDevice, s));
+        launchSleepBits(w, sleep_[cur_].ptr, bflags_.ptr, s);
+    }
+    launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], sleeping ? tmp : cacheView(1 - cache_),
+                 sleeping ? tCount_.ptr : &cCount_.ptr[1 - cache_], cacheCap_, sb_, iters, mode, (int)blocks, block, 0u,
+                 false, st, ws_, s);
+    if (sleeping)
+        launchCacheCarry(w, cacheView(cache_), &cCount_.ptr[cache_], tmp, tCount_.ptr, cacheView(1 - cache_),
+                         &cCount_.ptr[1 - cache_], cacheCap_, carry_.ptr, carryPos_.ptr, carryTotal_.ptr, st, ws_, s);
     PE_CHECK(cudaMemcpyAsync(hostStats_, st, sizeof(DevStats), cudaMemcpyDeviceToHost, s));
     PE_CHECK(cudaStreamSynchronize(s));
-    if (hostStats_->err & (kErrTimeout | kErrColors)) throw std::runtime_error("solve failed on the device");
+    if (hostStats_->err & (kErrTimeout | kErrColors | kErrCacheCapacity))
+        throw std::runtime_error("solve failed on the device");
     counters_ = StepCounters{};
     counters_.solvedContactCount = hostStats_->solved;
     counters_.preparedPoints = hostStats_->preparedPoints;

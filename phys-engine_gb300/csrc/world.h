@@ -51,6 +51,23 @@ struct HostBody {
     float iinv[3] = {0, 0, 0};  // diagonal local inverse inertia
     uint32_t generation = 0;
     bool alive = false;
+    // RigidBody::sleeping / wakeRequested (rigid_body.hpp:132-133) and the
+    // body's quiet time (SleepState::quietTime)
+    bool sleeping = false;
+    bool wakeRequested = true;
+    float quiet = 0.0f;
+    // State at the end of the last step (SleepState pose, mass, material,
+    // static flag): host edits since then wake the body at the next step
+    // (PhysicsWorld::prepareSleeping, physics_world.cpp:434-452).
+    bool snapValid = false;
+    bool snapStatic = false;
+    float snapPos[3] = {0, 0, 0}, snapRot[4] = {0, 0, 0, 1};
+    float snapMass = 0, snapRestitution = 0, snapFriction = 0;
+    void wakeUp() {
+        sleeping = false;
+        wakeRequested = true;
+    }
+    bool isSleeping() const { return !isStatic && sleeping; }
 };
 
 struct HostCollider {
@@ -66,7 +83,7 @@ struct HostCollider {
 
 struct StepCounters {
     uint64_t possiblePairs = 0, candidatePairs = 0, contactCount = 0, solvedContactCount = 0;
-    uint64_t awakeBodyCount = 0, xWindow = 0, aabbPairs = 0, gridComparisons = 0, gridEntries = 0,
+    uint64_t awakeBodyCount = 0, sleepingBodyCount = 0, xWindow = 0, aabbPairs = 0, gridComparisons = 0, gridEntries = 0,
              gridOverflow = 0;
     double cellSize = 0;
     uint64_t npCandidates[4] = {0, 0, 0, 0}, npContacts[4] = {0, 0, 0, 0};
@@ -96,6 +113,7 @@ class World {
     double cellSize = 0.0;    // grid: <= 0 median (reference), > 0 fixed
     int iterations = 8;
     int orderMode = 1;        // 0 manifold order (serial), 1 graph-colour order
+    bool sleepingEnabled = false;  // PhysicsWorld::setSleepingEnabled
 
     // host mirror (bodies / colliders by slot)
     std::vector<HostBody> bodies;
@@ -117,6 +135,8 @@ class World {
     // modified so the next step uploads it.
     void pull();
     void touch() { hostDirty_ = true; }
+    // PhysicsWorld::setSleepingEnabled (physics_world.cpp:341-351).
+    void setSleepingEnabled(bool enabled);
 
     void step(float dt);
     // Bulk per-step I/O: set the accumulated force of bodies [0, n) (xyz each),
@@ -157,6 +177,9 @@ class World {
     void runPipeline(float dt);
     bool finishStep();
     void computePossiblePairs();
+    // PhysicsWorld::wakeContacts (physics_world.cpp:353-371) on the host mirror
+    // from the last step's contacts.
+    void wakeContacts(uint32_t index, uint32_t generation);
 
     int device_;
     int smCount_ = 152;
@@ -182,6 +205,18 @@ class World {
     DeviceArray<float> xfer3_;  // 3 floats per body: caller forces in, positions out
     DeviceArray<uint32_t> poseDone_;  // arrival counter of the pose kernel's blocks
     DeviceArray<uint32_t> bflags_, bgen_;
+    // sleeping: flags and quiet times (two copies, like the body state), the
+    // island scratch, and the warm-start merge buffers
+    DeviceArray<uint32_t> sleep_[2];
+    DeviceArray<float> quiet_[2];
+    DeviceArray<uint32_t> sParent_, sIsland_, sQuietMin_, sleepErr_;
+    DeviceArray<unsigned long long> tKey_, tGens_;
+    DeviceArray<float4> tA_, tB_;
+    DeviceArray<float> tT2_;
+    DeviceArray<uint32_t> tCount_, carry_, carryPos_, carryTotal_;
+    uint32_t cacheNeed_ = 0;   // warm-start capacity asked for by a carry overflow
+    bool wakeCheck_ = false;   // host edits since the last step: run the wake pass first
+    float sleepGravity_[3] = {0, 0, 0};  // PhysicsWorld::sleepGravity
     DeviceArray<uint32_t> cbody_, cbgen_, cflags_;
     DeviceArray<float4> cshape_, clpos_, clrot_, aabbMin_, aabbMax_;
     DeviceArray<uint32_t> hullOffset_;
@@ -240,7 +275,7 @@ class World {
         uint32_t blockM;
         uint32_t pairBits, gridKeyBits;
         double cellSize;
-        bool dense, localIdentity, forces, identityColliders;
+        bool dense, localIdentity, forces, identityColliders, sleeping;
         bool operator==(const GraphKey &o) const;
     };
     cudaGraphExec_t graph_[2] = {nullptr, nullptr};

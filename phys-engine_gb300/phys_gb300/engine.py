@@ -75,6 +75,7 @@ SIGNATURES = {
     "pe_world_set_solver": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
     "pe_world_set_worker_counts": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]),
     "pe_world_set_sleeping_enabled": (ctypes.c_int, [_P, ctypes.c_int]),
+    "pe_world_get_sleeping_enabled": (ctypes.c_int, [_P, _P]),
     "pe_world_create_sphere": (ctypes.c_int, [_P, ctypes.c_float, _P, ctypes.c_float, ctypes.c_int,
                                               ctypes.c_float, ctypes.c_float, _P, _P]),
     "pe_world_create_box": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, _P,
@@ -88,6 +89,11 @@ SIGNATURES = {
     "pe_world_get_body": (ctypes.c_int, [_P, Handle, _P]),
     "pe_world_set_body": (ctypes.c_int, [_P, Handle, _P]),
     "pe_world_body_integrate_rotation": (ctypes.c_int, [_P, Handle, ctypes.c_float]),
+    "pe_world_body_is_sleeping": (ctypes.c_int, [_P, Handle, _P]),
+    "pe_world_body_wake_up": (ctypes.c_int, [_P, Handle]),
+    "pe_world_body_apply_force": (ctypes.c_int, [_P, Handle, _P]),
+    "pe_world_body_set_velocity": (ctypes.c_int, [_P, Handle, _P, _P]),
+    "pe_world_read_sleeping": (ctypes.c_int, [_P, _P]),
     "pe_world_body_slot_count": (_u32, [_P]),
     "pe_world_read_bodies": (ctypes.c_int, [_P, _P, _P, _P, _P]),
     "pe_world_write_forces": (ctypes.c_int, [_P, _P, _u32]),
@@ -297,6 +303,44 @@ class GpuWorld:
 
     def remove_body(self, idx, gen):
         check(self.lib.pe_world_remove_body(self.h, Handle(int(idx), int(gen))))
+
+    def remove_collider(self, idx, gen):
+        check(self.lib.pe_world_remove_collider(self.h, Handle(int(idx), int(gen))))
+
+    # sleeping ------------------------------------------------------------
+    def set_sleeping_enabled(self, enabled):
+        check(self.lib.pe_world_set_sleeping_enabled(self.h, int(bool(enabled))))
+
+    def sleeping_enabled(self):
+        v = ctypes.c_int()
+        check(self.lib.pe_world_get_sleeping_enabled(self.h, ctypes.byref(v)))
+        return bool(v.value)
+
+    def sleeping(self):
+        """isSleeping() of every body slot."""
+        out = np.zeros(self.body_count(), np.uint8)
+        check(self.lib.pe_world_read_sleeping(self.h, _ptr(out)))
+        return out.astype(bool)
+
+    def is_sleeping(self, h):
+        v = ctypes.c_int()
+        check(self.lib.pe_world_body_is_sleeping(self.h, h, ctypes.byref(v)))
+        return bool(v.value)
+
+    def wake_up(self, h):
+        check(self.lib.pe_world_body_wake_up(self.h, h))
+
+    def apply_force(self, h, force):
+        check(self.lib.pe_world_body_apply_force(self.h, h, _ptr(_f32(force))))
+
+    def set_velocity(self, h, lin=None, ang=None):
+        check(self.lib.pe_world_body_set_velocity(self.h, h, _ptr(None if lin is None else _f32(lin)),
+                                                  _ptr(None if ang is None else _f32(ang))))
+
+    def set_material(self, h, mass, friction, restitution):
+        st = self.get_body(h)
+        st.mass, st.friction, st.restitution = float(mass), float(friction), float(restitution)
+        self.set_body(h, st)
 
     def body_count(self):
         return int(self.lib.pe_world_body_slot_count(self.h))

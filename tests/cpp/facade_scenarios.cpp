@@ -1,5 +1,6 @@
-// Scenarios of the reference's solver tests
-// (tests/solver/sequential_impulse_solver_tests.cpp:293-378 of bkuangs/phys-engine)
+// Scenarios of the reference's solver and sleeping tests
+// (tests/solver/sequential_impulse_solver_tests.cpp:293-378,
+// tests/world/sleeping_tests.cpp of bkuangs/phys-engine)
 // written against the phys_gb300 facade the way a caller of phys::PhysicsWorld
 // writes them; links libphys_gb300.so and runs on the GPU.  Exit code 0 = pass.
 #include <cmath>
@@ -86,9 +87,56 @@ static bool invalidInputs() {
     return true;
 }
 
+// Opt-in sleeping of a settled stack, after tests/world/sleeping_tests.cpp:72-110
+// and :172-200 of the reference.
+static bool settledStackSleepsAndWakes() {
+    const float dt = 1.0f / 120.0f;
+    PhysicsWorld world;
+    RigidBodyHandle floorBody, lower, upper, other;
+    ColliderHandle c;
+    std::string error;
+    if (!world.createBox(10, 1, 10, {0, -0.5f, 0}, 1, true, 0, 0.6f, floorBody, c, error) ||
+        !world.createBox(1, 1, 1, {0, 0.5f, 0}, 1, false, 0, 0.6f, lower, c, error) ||
+        !world.createBox(1, 1, 1, {0, 1.52f, 0}, 1, false, 0, 0.6f, upper, c, error) ||
+        !world.createBox(1, 1, 1, {3, 0.5f, 0}, 1, false, 0, 0.6f, other, c, error))
+        return false;
+    for (int i = 0; i < 360; ++i) world.step(dt);
+    if (world.isSleepingEnabled() || world.lastStepStats().awake_body_count != 3 ||
+        world.lastStepStats().solved_contact_count != 3)
+        return false;
+    world.setSleepingEnabled(true);
+    for (int i = 0; i < 120; ++i) world.step(dt);
+    StepStats st = world.lastStepStats();
+    if (!world.isSleepingEnabled() || st.sleeping_body_count != 3 || st.awake_body_count != 0 ||
+        st.solved_contact_count != 0 || world.contacts().size() != 3) {
+        std::fprintf(stderr, "stack did not sleep: %llu asleep\n", (unsigned long long)st.sleeping_body_count);
+        return false;
+    }
+    Vec3 p0 = world.getBody(upper).getPosition();
+    world.getBody(upper).applyForce({});
+    world.getBody(upper).applyLinearImpulse({});
+    for (int i = 0; i < 60; ++i) world.step(dt);
+    BodyRef u = world.getBody(upper);
+    Vec3 p1 = u.getPosition();
+    if (!u.isSleeping() || p0.x != p1.x || p0.y != p1.y || p0.z != p1.z) return false;
+    for (const ContactManifold &m : world.contacts())
+        if (m.pointCount != 4) return false;
+    world.getBody(upper).applyForce({0.1f, 0, 0});
+    if (world.getBody(upper).isSleeping()) return false;
+    world.step(dt);
+    if (world.getBody(lower).isSleeping() || world.getBody(upper).isSleeping() || !world.getBody(other).isSleeping() ||
+        world.lastStepStats().solved_contact_count != 2)
+        return false;
+    world.setSleepingEnabled(false);
+    if (world.getBody(other).isSleeping()) return false;
+    world.step(dt);
+    return world.lastStepStats().sleeping_body_count == 0 && world.lastStepStats().solved_contact_count == 3;
+}
+
 int main() {
     bool ok = boxLandsOnStaticFloor() && tiltedBoxSettlesFlat(1.0f / 60.0f, 0.6f, {0.0f, 0.0f, 1.0f}) &&
-              tiltedBoxSettlesFlat(1.0f / 120.0f, 0.9f, {0.6f, 0.0f, 0.8f}) && invalidInputs();
+              tiltedBoxSettlesFlat(1.0f / 120.0f, 0.9f, {0.6f, 0.0f, 0.8f}) && invalidInputs() &&
+              settledStackSleepsAndWakes();
     std::printf("%s\n", ok ? "facade scenarios ok" : "facade scenarios FAILED");
     return ok ? 0 : 1;
 }

@@ -12,7 +12,9 @@ Known-answer inputs restate the cases of the reference's own tests:
   broadphase  tests/collision/broadphase_tests.cpp:89-182
   narrowphase tests/collision/narrowphase_tests.cpp:35-182
   solver      tests/solver/sequential_impulse_solver_tests.cpp:24-291, 380-459
-plus seeded random AABB sets / contact pairs and short seeded world runs.
+plus seeded random AABB sets / contact pairs, short seeded world runs and the
+sleeping scenarios of tests/sleep_scenarios.py (tests/world/sleeping_tests.cpp).
+`python tests/golden/make_golden.py sleeping` regenerates one fixture only.
 """
 from __future__ import annotations
 
@@ -214,12 +216,36 @@ def make_solver():
     np.savez_compressed(HERE / "solver.npz", **out)
 
 
+def make_sleeping():
+    """Sleeping scenarios (tests/sleep_scenarios.py, after
+    tests/world/sleeping_tests.cpp and benchmarks/cpu_profile.cpp): every
+    observation of the reference world, scenario by scenario."""
+    sys.path.insert(0, str(REPO / "tests"))
+    import sleep_scenarios as ss
+
+    out = {}
+    for name, (ops, dt) in ss.scenarios().items():
+        obs = ss.run(cpu.RefWorld(), ops, dt)
+        out[f"{name}__checks"] = np.array(len(obs), np.uint32)
+        for k, o in enumerate(obs):
+            for f, v in o.items():
+                out[f"{name}__{k}__{f}"] = v
+    np.savez_compressed(HERE / "sleeping.npz", **out)
+
+
 def main():
     cpu.build_reference()
-    print("broadphase cases:", make_broadphase())
-    print("narrowphase cases:", make_narrowphase())
-    make_solver()
-    make_worlds()
+    only = set(sys.argv[1:])
+    if not only or "broadphase" in only:
+        print("broadphase cases:", make_broadphase())
+    if not only or "narrowphase" in only:
+        print("narrowphase cases:", make_narrowphase())
+    if not only or "solver" in only:
+        make_solver()
+    if not only or "worlds" in only:
+        make_worlds()
+    if not only or "sleeping" in only:
+        make_sleeping()
     for p in sorted(HERE.glob("*.npz")):
         print(p.name, p.stat().st_size)
 

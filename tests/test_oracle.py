@@ -203,3 +203,81 @@ def test_gjk_epa_matches_reference():
             assert np.float32(o[2]) == np.float32(r[2])
         agree += 1
     assert agree == 300
+
+
+# ---------------------------------------------------------------- sleeping islands
+def _sleeping_golden(golden, name):
+    g = golden("sleeping")
+    n = int(g[f"{name}__checks"])
+    return [{f: g[f"{name}__{k}__{f}"] for f in ("pos", "quat", "lin", "ang", "sleeping", "stats", "contacts")}
+            for k in range(n)]
+
+
+def assert_observations_equal(got, want, what, features=False):
+    import sleep_scenarios as ss
+
+    assert len(got) == len(want), f"{what}: {len(got)} checks != {len(want)}"
+    for k, (a, b) in enumerate(zip(got, want)):
+        for f in ("pos", "quat", "lin", "ang", "sleeping"):
+            assert_bit_equal(a[f], b[f], f"{what} check {k} {f}")
+        for i, f in enumerate(ss.STAT_FIELDS):
+            assert a["stats"][i] == b["stats"][i], f"{what} check {k} {f}: {a['stats'][i]} != {b['stats'][i]}"
+        assert_manifolds_equal(a["contacts"], b["contacts"], features=features, what=f"{what} check {k}")
+
+
+def _scenario_names():
+    import sleep_scenarios as ss
+
+    return list(ss.scenarios())
+
+
+@pytest.mark.parametrize("name", _scenario_names())
+def test_sleeping_oracle_golden(golden, name):
+    """The oracle's sleeping restatement against the reference's observations
+    (tests/golden/sleeping.npz), in the reference's manifold order."""
+    import sleep_scenarios as ss
+
+    ops, dt = ss.scenarios()[name]
+    got = ss.run(cpu.OracleWorld(), ops, dt)
+    assert_observations_equal(got, _sleeping_golden(golden, name), name)
+
+
+def test_sleeping_invariants_of_reference_tests(golden):
+    """Facts the reference's own sleeping tests assert (sleeping_tests.cpp),
+    read from the fixture: settled islands sleep with their contacts kept,
+    a mutation wakes the island but not through the static floor, a gravity
+    change wakes everything, the quiet-time thresholds are inclusive, and the
+    512-box profile scene sleeps whole (benchmarks/results/sleeping-release.txt:30-31)."""
+    import sleep_scenarios as ss
+
+    awake, asleep, solved, contacts = (ss.STAT_FIELDS.index(f) for f in
+                                       ("awake_body_count", "sleeping_body_count", "solved_contact_count",
+                                        "contact_count"))
+    o = _sleeping_golden(golden, "opt_in")
+    assert o[0]["stats"][awake] == 3 and o[0]["stats"][solved] == 3
+    assert o[1]["stats"][asleep] == 3 and o[1]["stats"][solved] == 0 and o[1]["stats"][contacts] == 3
+    assert np.all(o[1]["contacts"]["point_count"] == 4)
+    assert o[4]["stats"][asleep] == 0 and o[4]["stats"][solved] == 3
+    for k in range(5):
+        m = _sleeping_golden(golden, f"mutator_{k}")
+        assert m[1]["sleeping"][ss.UPPER] == 0
+        assert list(m[2]["sleeping"][[ss.LOWER, ss.UPPER, ss.OTHER]]) == [0, 0, 1] and m[2]["stats"][solved] == 2
+        assert m[3]["sleeping"][ss.UPPER] == 0
+    assert _sleeping_golden(golden, "property_3")[1]["stats"][asleep] == 0
+    for name in ("quiet_60", "quiet_120"):
+        q = [int(c["sleeping"][0]) for c in _sleeping_golden(golden, name)]
+        assert q == [0, 1, 0, 0, 0, 0, 1], (name, q)
+    s = _sleeping_golden(golden, "stacks_512")
+    assert s[1]["stats"][asleep] == 512 and s[1]["stats"][solved] == 0 and s[1]["stats"][contacts] == 512
+    assert int(s[1]["contacts"]["point_count"].sum()) == 2048
+
+
+@needs_ref
+def test_sleeping_oracle_matches_live_reference_in_grid():
+    """The settled stack under the uniform grid, against the live reference."""
+    import sleep_scenarios as ss
+
+    ops, dt = ss.scenarios()["mutator_0"]
+    r = cpu.RefWorld(algo=1)
+    o = cpu.OracleWorld(algo=1)
+    assert_observations_equal(ss.run(o, ops, dt), ss.run(r, ops, dt), "grid mutator_0")
