@@ -327,6 +327,8 @@ def run_gpu(args, rank, world_size, local_rank):
     if world_size == 1 and not args.no_batched:
         line["batched"] = run_batched(args, local_rank, flush, peak)
         line["differentiable"] = run_differentiable(args, local_rank)
+    if world_size == 1 and not args.no_sleeping:
+        line["sleeping"] = run_sleeping(args, local_rank, flush)
     if world_size == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, steps, el, _ = cpu_port_rate(scene, 20.0, 60, threads)
@@ -584,6 +586,93 @@ def run_differentiable(args, local_rank):
     }
 
 
+SLEEP_DT = 1.0 / 120.0
+SLEEP_WARMUP = 240
+SLEEP_ITERATIONS = 8
+# The reference's settled-box figures, sleeping enabled / disabled, Apple M2
+# (benchmarks/results/sleeping-release.txt:36-38 of bkuangs/phys-engine).
+SLEEP_REF_MS = {"enabled": 0.2372, "disabled": 1.8131}
+
+
+def timed_steps(w, steps, dt, stream, flush):
+    """Device time (ms) of `steps` steps, CUDA events on the world's stream, L2
+    flushed before each."""
+    import torch
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    launches = 0
+    torch.cuda.synchronize()
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.add_(1.0)
+        starts[k].record(stream)
+        w.step(dt)
+        ends[k].record(stream)
+        launches += int(w.stats()["kernel_launches"])
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in zip(starts, ends)), launches
+
+
+def run_sleeping(args, local_rank, flush):
+    """Sleeping islands: the reference's settled-box profile scene (512 unit
+    boxes in two-high stacks on a static floor, dt = 1/120, 8 iterations, 240
+    warm-up steps) and 128 copies of it side by side (65,536 boxes), stepped
+    with sleeping enabled and disabled; body-steps/s counts the dynamic bodies."""
+    import torch
+
+    from oracle import cpu
+    from phys_gb300 import engine, scenes
+
+    out = {}
+    for name, tiles in (("stacks_512", (1, 1)), ("stacks_65536", (16, 8))):
+        sc = scenes.box_stacks(*tiles)
+        bodies = int(sc.count - sc.is_static.sum())
+        res = {}
+        for enabled in (True, False):
+            w = engine.GpuWorld(device=local_rank, algo=engine.SAP, iterations=SLEEP_ITERATIONS,
+                                order=engine.ORDER_COLOR)
+            w.set_sleeping_enabled(enabled)
+            w.load_scene(sc)
+            for _ in range(SLEEP_WARMUP):
+                w.step(SLEEP_DT)
+            stream = torch.cuda.ExternalStream(w.stream(), device=torch.device("cuda", local_rank))
+            ms, launches = timed_steps(w, args.sleep_steps, SLEEP_DT, stream, flush)
+            st = w.stats()
+            res["enabled" if enabled else "disabled"] = {
+                "ms_per_step": ms / args.sleep_steps, "value": bodies * args.sleep_steps / (ms / 1000.0),
+                "sleeping_bodies": int(st["sleeping_body_count"]), "awake_bodies": int(st["awake_body_count"]),
+                "contacts": int(st["contact_count"]), "solved_contacts": int(st["solved_contact_count"]),
+                "gpu_launches": launches}
+            w.close()
+        e, d = res["enabled"], res["disabled"]
+        out[name] = {"metric": "body-steps/s, settled box stacks, sleeping enabled", "value": e["value"],
+                     "unit": UNIT, "bodies": bodies, "steps": args.sleep_steps, "warmup": SLEEP_WARMUP,
+                     "enabled": e, "disabled": d, "speedup_vs_disabled": d["ms_per_step"] / e["ms_per_step"]}
+    # CPU: the oracle port on the 512-box scene, both ways
+    sc = scenes.box_stacks()
+    port = {}
+    for enabled in (True, False):
+        ow = cpu.OracleWorld(algo=0, iterations=SLEEP_ITERATIONS, order_mode=0)
+        ow.set_sleeping_enabled(enabled)
+        ow.load_scene(sc)
+        for _ in range(SLEEP_WARMUP):
+            ow.step(SLEEP_DT)
+        t0 = time.perf_counter()
+        for _ in range(args.sleep_steps):
+            ow.step(SLEEP_DT)
+        port["enabled" if enabled else "disabled"] = (time.perf_counter() - t0) * 1000.0 / args.sleep_steps
+    out["cpu_baseline"] = {"kind": "port", "cores": 1, "workload": "stacks_512",
+                           "sample": f"{args.sleep_steps} steps after {SLEEP_WARMUP} warm-up steps, oracle "
+                                     "restatement (reference order, SAP, 8 iterations), one host thread",
+                           "ms_per_step_enabled": port["enabled"], "ms_per_step_disabled": port["disabled"]}
+    out["reference_published"] = {"ms_per_step_enabled": SLEEP_REF_MS["enabled"],
+                                  "ms_per_step_disabled": SLEEP_REF_MS["disabled"], "hardware": "Apple M2",
+                                  "broadphase": "dynamic AABB tree",
+                                  "source": "benchmarks/results/sleeping-release.txt"}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -595,6 +684,8 @@ def main():
                     help="skip the batched-world and differentiable-rollout measurements")
     ap.add_argument("--batch-worlds", type=int, default=BATCH_WORLDS, help="worlds of the batched measurement")
     ap.add_argument("--diff-worlds", type=int, default=DIFF_WORLDS, help="worlds of the differentiable rollout")
+    ap.add_argument("--sleep-steps", type=int, default=200, help="timed steps of the sleeping measurement")
+    ap.add_argument("--no-sleeping", action="store_true", help="skip the sleeping-island measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -110,3 +110,30 @@ def generate(kind: int, n: int, seed: int = 42) -> Scene:
         )
     finally:
         lib.pe_scene_free(ctypes.byref(cs))
+
+
+def box_stacks(tiles_x: int = 1, tiles_z: int = 1) -> Scene:
+    """The reference's settled-box profile scene (benchmarks/cpu_profile.cpp:20-41):
+    a static 30 x 1 x 20 floor box and 512 unit boxes (density 1, restitution 0,
+    friction 0.6) in 16 x 16 two-high stacks, 1.6 m apart along x and 1.2 m
+    along z.  tiles_x x tiles_z copies of it lie side by side with 0.5 m gaps
+    between the floors (floor, then its boxes, tile after tile)."""
+    f = np.float32
+    rows, cols, levels = np.meshgrid(np.arange(16), np.arange(16), np.arange(2), indexing="ij")
+    rows, cols, levels = rows.reshape(-1), cols.reshape(-1), levels.reshape(-1)  # row, column, level order
+    local = np.stack([f(-12.0) + f(1.6) * cols.astype(f), f(0.5) + f(1.02) * levels.astype(f),
+                      f(-9.0) + f(1.2) * rows.astype(f)], axis=1).astype(f)
+    pos, static, dims = [], [], []
+    for tz in range(tiles_z):
+        for tx in range(tiles_x):
+            off = np.array([f(30.5) * f(tx), f(0.0), f(20.5) * f(tz)], f)
+            pos.append(np.array([[0.0, -0.5, 0.0]], f) + off)
+            pos.append(local + off)
+            static.append(np.concatenate([[1], np.zeros(len(local), np.uint8)]).astype(np.uint8))
+            dims.append(np.concatenate([np.array([[30, 1, 20]], f), np.ones((len(local), 3), f)]))
+    pos, static, dims = np.concatenate(pos).astype(f), np.concatenate(static), np.concatenate(dims)
+    n = len(pos)
+    return Scene(shape=np.ones(n, np.uint8), is_static=static, dims=dims, pos=pos, density=np.ones(n, f),
+                 restitution=np.zeros(n, f), friction=np.full(n, f(0.6)), linvel=np.zeros((n, 3), f),
+                 spin=np.zeros((n, 3), f), hull_id=np.full(n, -1, np.int32), mass=np.zeros(n, f),
+                 inv_inertia=np.zeros((n, 3), f))
