@@ -178,7 +178,10 @@ pe_status pe_world_create_bodies(pe_world *world, uint32_t n, const uint8_t *sha
 pe_status pe_world_create_hull(pe_world *world, const float *vertices, uint32_t vertex_count,
                                const float *position, float mass, const float *inverse_inertia, int is_static,
                                float restitution, float friction, pe_handle *body, pe_handle *collider);
-/* addCollider (physics_world.hpp:57) for an existing body, with a local transform. */
+/* addCollider (physics_world.hpp:57) for an existing body, with a local
+   transform: dims = sphere radius or box half extents; local_position (xyz) and
+   local_rotation (xyzw) may be NULL (identity).  A body may hold several
+   colliders; pairs of colliders on one body are never candidates. */
 pe_status pe_world_add_collider(pe_world *world, pe_handle body, int shape, const float *dims,
                                 const float *local_position, const float *local_rotation, pe_handle *collider);
 /* removeBody / removeCollider (physics_world.hpp:41, 58) */

@@ -8,6 +8,8 @@
 //     member functions) instead of RigidBody*; it converts to false when the
 //     handle is stale, where the reference returns nullptr.
 //   * contacts() returns the manifolds by value (downloaded from the device).
+//   * colliders are added with addSphereCollider / addBoxCollider (the
+//     reference's addCollider takes a Collider struct with a shape variant).
 //   * solver iterations and order are configurable (the reference fixes 8 and
 //     manifold order); the default here is the reference's 8 with the GPU's
 //     graph-colour order.
@@ -178,6 +180,18 @@ class PhysicsWorld {
     }
     void removeBody(RigidBodyHandle h) { throwIf(pe_world_remove_body(w_, pe_handle{h.index, h.generation})); }
     void removeCollider(ColliderHandle h) { throwIf(pe_world_remove_collider(w_, pe_handle{h.index, h.generation})); }
+    // addCollider (physics_world.hpp:57) with a sphere or box shape at a local
+    // transform; an empty handle for a stale body, like the reference.
+    ColliderHandle addSphereCollider(RigidBodyHandle body, float radius, Vec3 localPosition = {},
+                                     Quaternion localRotation = {}) {
+        const float d[3] = {radius, 0.0f, 0.0f};
+        return addCollider(body, PE_SHAPE_SPHERE, d, localPosition, localRotation);
+    }
+    ColliderHandle addBoxCollider(RigidBodyHandle body, Vec3 halfExtents, Vec3 localPosition = {},
+                                  Quaternion localRotation = {}) {
+        const float d[3] = {halfExtents.x, halfExtents.y, halfExtents.z};
+        return addCollider(body, PE_SHAPE_BOX, d, localPosition, localRotation);
+    }
     BodyRef getBody(RigidBodyHandle h) { return BodyRef(w_, h); }
 
     void setNarrowPhaseWorkerCount(std::size_t n) { setWorkers(n, solverWorkers_, broadWorkers_, &npWorkers_); }
@@ -241,6 +255,14 @@ class PhysicsWorld {
     pe_world *native() const { return w_; }
 
   private:
+    ColliderHandle addCollider(RigidBodyHandle body, int shape, const float *dims, Vec3 lp, Quaternion lq) {
+        const float p[3] = {lp.x, lp.y, lp.z}, q[4] = {lq.x, lq.y, lq.z, lq.w};
+        pe_handle c{};
+        pe_status s = pe_world_add_collider(w_, pe_handle{body.index, body.generation}, shape, dims, p, q, &c);
+        if (s == PE_ERR_STALE_HANDLE) return {};
+        throwIf(s);
+        return {c.index, c.generation};
+    }
     bool finishCreate(pe_status s, pe_handle b, pe_handle c, RigidBodyHandle &body, ColliderHandle &collider,
                       std::string &errorMessage) {
         if (s == PE_ERR_CREATE_FAILED) {

@@ -84,6 +84,7 @@ def oracle_lib():
                                             ctypes.c_float, ctypes.c_float, _P]
         lib.ow_remove_body.argtypes = [_P, ctypes.c_uint32, ctypes.c_uint32]
         lib.ow_remove_collider.argtypes = [_P, ctypes.c_uint32, ctypes.c_uint32]
+        lib.ow_add_collider.argtypes = [_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, _P, _P, _P, _P]
         lib.ow_set_sleeping_enabled.argtypes = [_P, ctypes.c_int]
         lib.ow_get_sleeping.argtypes = [_P, _P]
         lib.ow_wake_body.argtypes = [_P, ctypes.c_uint32]
@@ -135,6 +136,7 @@ def ref_lib():
                                        ctypes.c_float, ctypes.c_float, _P, ctypes.c_char_p, ctypes.c_int]
         lib.rw_remove_body.argtypes = [_P, ctypes.c_uint32, ctypes.c_uint32]
         lib.rw_remove_collider.argtypes = [_P, ctypes.c_uint32, ctypes.c_uint32]
+        lib.rw_add_collider.argtypes = [_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, _P, _P, _P, _P]
         lib.rw_set_sleeping_enabled.argtypes = [_P, ctypes.c_int]
         lib.rw_get_sleeping.argtypes = [_P, _P]
         lib.rw_wake_body.argtypes = [_P, ctypes.c_uint32]
@@ -214,6 +216,17 @@ class _CpuWorld:
 
     def remove_body(self, idx, gen):
         getattr(self.lib, self._prefix + "remove_body")(self.h, int(idx), int(gen))
+
+    def add_collider(self, body_idx, body_gen, shape, dims, local_pos=(0, 0, 0), local_rot=(0, 0, 0, 1)):
+        """Collider on an existing body (dims: sphere radius / box half extents);
+        returns (collider idx, gen)."""
+        h = np.zeros(2, np.uint32)
+        rc = getattr(self.lib, self._prefix + "add_collider")(
+            self.h, int(body_idx), int(body_gen), int(shape), _ptr(_f32(dims)), _ptr(_f32(local_pos)),
+            _ptr(_f32(local_rot)), _ptr(h))
+        if rc != 0:
+            raise LookupError("stale body handle")
+        return h
 
     def remove_collider(self, idx, gen):
         getattr(self.lib, self._prefix + "remove_collider")(self.h, int(idx), int(gen))

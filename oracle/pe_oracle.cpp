@@ -1825,6 +1825,32 @@ int ow_create_body(ow_world *world, int shape, const float *dims, const float *p
     return 0;
 }
 
+// PhysicsWorld::addCollider (physics_world.cpp:276-298) with a local transform.
+int ow_add_collider(ow_world *world, uint32_t body_index, uint32_t body_generation, int shape, const float *dims,
+                    const float *local_pos, const float *local_rot, uint32_t *handle) {
+    return dispatch(world, [&](auto &w) {
+        using T = decltype(w.gravity.x);
+        if (!w.getBody(body_index, body_generation)) {
+            handle[0] = handle[1] = 0;
+            return 1;
+        }
+        Collider<T> c;
+        c.bodyIndex = body_index;
+        c.bodyGeneration = body_generation;
+        c.shape = shape;
+        if (shape == kSphere)
+            c.radius = T(dims[0]);
+        else
+            c.halfExtents = {T(dims[0]), T(dims[1]), T(dims[2])};
+        c.local.p = {T(local_pos[0]), T(local_pos[1]), T(local_pos[2])};
+        c.local.q = {T(local_rot[0]), T(local_rot[1]), T(local_rot[2]), T(local_rot[3])};
+        uint32_t g;
+        handle[0] = w.addCollider(c, g);
+        handle[1] = g;
+        return 0;
+    });
+}
+
 int ow_add_hull_shape(ow_world *world, uint32_t n, const float *v) {
     return dispatch(world, [&](auto &w) {
         using T = decltype(w.gravity.x);

@@ -102,6 +102,11 @@ int ow_create_hull_body(ow_world *world, int hull_id, const float *pos, float ma
                         float friction, uint32_t *handles);
 void ow_remove_body(ow_world *world, uint32_t index, uint32_t generation);
 void ow_remove_collider(ow_world *world, uint32_t index, uint32_t generation);
+/* addCollider on an existing body: shape 0 sphere (dims[0] radius) or 1 box
+   (dims = half extents), local position xyz and rotation xyzw.  Returns 1 for a
+   stale body (handle {0, 0}), else 0 with handle = {collider idx, gen}. */
+int ow_add_collider(ow_world *world, uint32_t body_index, uint32_t body_generation, int shape, const float *dims,
+                    const float *local_pos, const float *local_rot, uint32_t *handle);
 /* setSleepingEnabled (physics_world.hpp:63); per-slot isSleeping(); wakeUp();
    applyForce (rigid_body.hpp:53-85).  set_velocity and apply_spin wake the body
    like the reference's velocity setters. */

@@ -152,6 +152,20 @@ void rw_remove_body(rw_world *w, uint32_t index, uint32_t generation) {
     w->world.removeBody({index, generation});
 }
 
+int rw_add_collider(rw_world *w, uint32_t body_index, uint32_t body_generation, int shape, const float *dims,
+                    const float *local_pos, const float *local_rot, uint32_t *handle) {
+    Collider c{};
+    c.body = {body_index, body_generation};
+    if (shape == 0) c.shape = Sphere{dims[0]};
+    else c.shape = Box{{dims[0], dims[1], dims[2]}};
+    c.localTransform = Transform{{local_pos[0], local_pos[1], local_pos[2]},
+                                 Quaternion{local_rot[0], local_rot[1], local_rot[2], local_rot[3]}};
+    ColliderHandle h = w->world.addCollider(c);
+    handle[0] = h.index;
+    handle[1] = h.generation;
+    return w->world.getCollider(h) ? 0 : 1;
+}
+
 void rw_remove_collider(rw_world *w, uint32_t index, uint32_t generation) {
     w->world.removeCollider({index, generation});
 }

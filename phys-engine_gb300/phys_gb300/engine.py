@@ -304,6 +304,15 @@ class GpuWorld:
     def remove_body(self, idx, gen):
         check(self.lib.pe_world_remove_body(self.h, Handle(int(idx), int(gen))))
 
+    def add_collider(self, body_idx, body_gen, shape, dims, local_pos=(0, 0, 0), local_rot=(0, 0, 0, 1)):
+        """PhysicsWorld::addCollider on an existing body (dims: sphere radius /
+        box half extents); returns (collider idx, gen)."""
+        c = Handle()
+        check(self.lib.pe_world_add_collider(self.h, Handle(int(body_idx), int(body_gen)), int(shape),
+                                             _ptr(_f32(dims)), _ptr(_f32(local_pos)), _ptr(_f32(local_rot)),
+                                             ctypes.byref(c)))
+        return np.array([c.index, c.generation], np.uint32)
+
     def remove_collider(self, idx, gen):
         check(self.lib.pe_world_remove_collider(self.h, Handle(int(idx), int(gen))))
 

@@ -224,7 +224,7 @@ def make_sleeping():
     import sleep_scenarios as ss
 
     out = {}
-    for name, (ops, dt) in ss.scenarios().items():
+    for name, (ops, dt) in ss.all_scenarios().items():
         obs = ss.run(cpu.RefWorld(), ops, dt)
         out[f"{name}__checks"] = np.array(len(obs), np.uint32)
         for k, o in enumerate(obs):

@@ -1,8 +1,12 @@
-"""Sleeping scenarios driven through any world with the test interface (the
-oracle, the reference harness, the GPU engine), after the reference's
-tests/world/sleeping_tests.cpp: a settled stack on a static floor, wake-ups by
-every mutator, collisions and support changes, property and gravity edits,
-quiet-time thresholds, and larger settled scenes.
+"""World scenarios driven through any world with the test interface (the
+oracle, the reference harness, the GPU engine).
+
+``scenarios()``: sleeping, after the reference's tests/world/sleeping_tests.cpp —
+a settled stack on a static floor, wake-ups by every mutator, collisions and
+support changes, property and gravity edits, quiet-time thresholds, and larger
+settled scenes.  ``compound_scenarios()``: bodies with several colliders at
+local transforms (PhysicsWorld::addCollider, physics_world.cpp:276-298, :658-667,
+:679-686), the same-body pair filter (:629-633) and collider removal.
 
 A scenario is a list of operations; ``run`` returns the observations taken at
 each ("check",) operation: body state, sleep flags, step counters and contacts.
@@ -91,6 +95,58 @@ def scenarios():
     return out
 
 
+def _quat(axis, angle):
+    axis = np.asarray(axis, np.float64)
+    axis = axis / np.linalg.norm(axis)
+    s = np.sin(angle / 2)
+    return [float(axis[0] * s), float(axis[1] * s), float(axis[2] * s), float(np.cos(angle / 2))]
+
+
+def _compound_bodies():
+    """Dumbbells (a box with two spheres), L shapes (two boxes, one tilted) and
+    crosses (a sphere with a long box at a tilted local rotation), dropped in a
+    grid over a static floor; creation body index k is op index k."""
+    ops = [_box((0, -0.5, 0), True, (40, 1, 40))]
+    body = 1
+    rng = np.random.default_rng(7)
+    for i in range(4):
+        for j in range(3):
+            x, z = -6.0 + 4.0 * i, -4.0 + 4.0 * j
+            y = 1.5 + 1.3 * ((i + j) % 3)
+            kind = (i + j) % 3
+            spin = [float(v) for v in rng.uniform(-0.4, 0.4, 3)]
+            if kind == 0:
+                ops += [("body", 1, [1.2, 0.3, 0.3], [x, y, z], 1.0, 0, 0.1, 0.5),
+                        ("collider", body, 0, [0.35, 0, 0], [0.75, 0, 0], [0, 0, 0, 1]),
+                        ("collider", body, 0, [0.3, 0, 0], [-0.75, 0.05, 0], _quat([0, 1, 0], 0.3))]
+            elif kind == 1:
+                ops += [("body", 1, [1.0, 0.4, 0.4], [x, y, z], 2.0, 0, 0.0, 0.6),
+                        ("collider", body, 1, [0.2, 0.5, 0.2], [0.4, 0.5, 0], _quat([0, 0, 1], 0.5))]
+            else:
+                ops += [("body", 0, [0.3, 0, 0], [x, y, z], 1.5, 0, 0.2, 0.4),
+                        ("collider", body, 1, [0.9, 0.08, 0.12], [0, 0.1, 0], _quat([1, 1, 0], 0.7))]
+            ops.append(("spin", body, spin))
+            body += 1
+    return ops
+
+
+def compound_scenarios():
+    out = {}
+    base = _compound_bodies()
+    out["compound_drop"] = (base + [("steps", 40), ("check",)] * 5, np.float32(1.0 / 60.0))
+    out["compound_remove_collider"] = (base + [("steps", 60), ("check",), ("remove_extra", 2), ("remove_extra", 4),
+                                               ("steps", 1), ("check",), ("steps", 60), ("check",)],
+                                       np.float32(1.0 / 60.0))
+    out["compound_sleep"] = ([("sleep", True)] + base + [("steps", 100), ("check",)] * 4 +
+                             [("force", 3, (5, 0, 0)), ("steps", 1), ("check",), ("steps", 60), ("check",)],
+                             np.float32(1.0 / 60.0))
+    return out
+
+
+def all_scenarios():
+    return {**scenarios(), **compound_scenarios()}
+
+
 def _is_gpu(world):
     return type(world).__name__ == "GpuWorld"
 
@@ -116,6 +172,7 @@ def observe(world, removed=()):
 
 def run(world, ops, dt):
     handles = []
+    extra = []  # (collider idx, gen) of added colliders, in order
     obs = []
     removed = set()
     gpu = _is_gpu(world)
@@ -149,6 +206,15 @@ def run(world, ops, dt):
             h = handles[op[1]]
             world.remove_body(int(h[0]), int(h[1]))
             removed.add(int(h[0]))
+        elif kind == "collider":
+            h = handles[op[1]]
+            extra.append(world.add_collider(int(h[0]), int(h[1]), op[2], np.asarray(op[3], np.float32),
+                                            np.asarray(op[4], np.float32), np.asarray(op[5], np.float32)))
+        elif kind == "remove_extra":
+            c = extra[op[1]]
+            world.remove_collider(int(c[0]), int(c[1]))
+        elif kind == "spin":
+            world.apply_spin(_handle(world, handles[op[1]]), np.asarray(op[2], np.float32))
         elif kind == "remove_collider":
             h = handles[op[1]]
             world.remove_collider(int(h[2]), int(h[3]))

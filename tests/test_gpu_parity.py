@@ -290,31 +290,33 @@ def test_world_read_poses_matches_bodies(gpu):
 def _sleep_names():
     import sleep_scenarios as ss
 
-    return list(ss.scenarios())
+    return list(ss.all_scenarios())
 
 
 @pytest.mark.parametrize("name", _sleep_names())
 def test_sleeping_scenarios_match_oracle(gpu, name):
     """Sleeping scenarios (settle, wake by every mutator, collisions, support
-    and property changes, quiet-time thresholds, the 512-box profile scene):
-    GPU graph-colour order against the oracle in the same order, bit for bit."""
+    and property changes, quiet-time thresholds, the 512-box profile scene) and
+    multi-collider bodies: GPU graph-colour order against the oracle in the same
+    order, bit for bit."""
     import sleep_scenarios as ss
     from test_oracle import assert_observations_equal
 
-    ops, dt = ss.scenarios()[name]
+    ops, dt = ss.all_scenarios()[name]
     got = ss.run(gpu.GpuWorld(), ops, dt)
     want = ss.run(cpu.OracleWorld(order_mode=1), ops, dt)
     assert_observations_equal(got, want, name, features=True)
 
 
-@pytest.mark.parametrize("name", ["opt_in", "mutator_0", "collision_wake", "remove_floor_collider", "stacks_512"])
+@pytest.mark.parametrize("name", ["opt_in", "mutator_0", "collision_wake", "remove_floor_collider", "stacks_512",
+                                  "compound_drop", "compound_remove_collider"])
 def test_sleeping_manifold_order_matches_reference(gpu, golden, name):
     """The GPU in the reference's manifold order against the reference's own
     observations (tests/golden/sleeping.npz)."""
     import sleep_scenarios as ss
     from test_oracle import _sleeping_golden, assert_observations_equal
 
-    ops, dt = ss.scenarios()[name]
+    ops, dt = ss.all_scenarios()[name]
     got = ss.run(gpu.GpuWorld(order=gpu.ORDER_MANIFOLD), ops, dt)
     assert_observations_equal(got, _sleeping_golden(golden, name), name)
 
@@ -324,8 +326,8 @@ def test_sleeping_grid_and_direct_launches(gpu, algo, graphs):
     import sleep_scenarios as ss
     from test_oracle import assert_observations_equal
 
-    for name in ("mutator_0", "replace_lower", "boxes_on_plane"):
-        ops, dt = ss.scenarios()[name]
+    for name in ("mutator_0", "replace_lower", "boxes_on_plane", "compound_drop"):
+        ops, dt = ss.all_scenarios()[name]
         g = gpu.GpuWorld(algo=algo)
         g.set_graphs(graphs)
         assert_observations_equal(ss.run(g, ops, dt), ss.run(cpu.OracleWorld(algo=algo, order_mode=1), ops, dt),
@@ -336,7 +338,7 @@ def test_sleeping_write_forces_wakes(gpu):
     """Bulk forces wake their bodies like applyForce; zero forces do not."""
     import sleep_scenarios as ss
 
-    ops, dt = ss.scenarios()["mutator_0"]
+    ops, dt = ss.all_scenarios()["mutator_0"]
     g = gpu.GpuWorld()
     o = cpu.OracleWorld(order_mode=1)
     ss.run(g, ops[:-6], dt)

@@ -228,16 +228,17 @@ def assert_observations_equal(got, want, what, features=False):
 def _scenario_names():
     import sleep_scenarios as ss
 
-    return list(ss.scenarios())
+    return list(ss.all_scenarios())
 
 
 @pytest.mark.parametrize("name", _scenario_names())
 def test_sleeping_oracle_golden(golden, name):
-    """The oracle's sleeping restatement against the reference's observations
-    (tests/golden/sleeping.npz), in the reference's manifold order."""
+    """The oracle's sleeping and multi-collider restatement against the
+    reference's observations (tests/golden/sleeping.npz), in the reference's
+    manifold order."""
     import sleep_scenarios as ss
 
-    ops, dt = ss.scenarios()[name]
+    ops, dt = ss.all_scenarios()[name]
     got = ss.run(cpu.OracleWorld(), ops, dt)
     assert_observations_equal(got, _sleeping_golden(golden, name), name)
 
@@ -277,7 +278,7 @@ def test_sleeping_oracle_matches_live_reference_in_grid():
     """The settled stack under the uniform grid, against the live reference."""
     import sleep_scenarios as ss
 
-    ops, dt = ss.scenarios()["mutator_0"]
+    ops, dt = ss.all_scenarios()["mutator_0"]
     r = cpu.RefWorld(algo=1)
     o = cpu.OracleWorld(algo=1)
     assert_observations_equal(ss.run(o, ops, dt), ss.run(r, ops, dt), "grid mutator_0")
