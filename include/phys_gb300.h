@@ -129,6 +129,11 @@ int pe_device_count(void);
 /* PhysicsWorld::PhysicsWorld() / ~PhysicsWorld() (physics_world.hpp:24-25) */
 pe_status pe_world_create(int device, pe_world **out);
 void pe_world_destroy(pe_world *world);
+/* The PhysicsWorld copy constructor (physics_world.hpp:28, physics_world.cpp:74-93):
+   an independent world on the same device with the same bodies, colliders,
+   settings, last contacts, candidate pairs, warm-start cache, step counters and
+   sleep state; stepping either leaves the other unchanged. */
+pe_status pe_world_clone(pe_world *world, pe_world **out);
 
 /* PhysicsWorld::gravity (physics_world.hpp:37) */
 pe_status pe_world_set_gravity(pe_world *world, float x, float y, float z);

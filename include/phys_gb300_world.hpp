@@ -8,6 +8,8 @@
 //     member functions) instead of RigidBody*; it converts to false when the
 //     handle is stale, where the reference returns nullptr.
 //   * contacts() returns the manifolds by value (downloaded from the device).
+//   * copies and moves are supported like the reference's; a moved-from world
+//     holds no device world.
 //   * colliders are added with addSphereCollider / addBoxCollider (the
 //     reference's addCollider takes a Collider struct with a shape variant).
 //   * solver iterations and order are configurable (the reference fixes 8 and
@@ -157,9 +159,45 @@ class PhysicsWorld {
         throwIf(pe_world_create(device, &w_));
         throwIf(pe_world_set_solver(w_, solverIterations, order));
     }
-    ~PhysicsWorld() { pe_world_destroy(w_); }
-    PhysicsWorld(const PhysicsWorld &) = delete;
-    PhysicsWorld &operator=(const PhysicsWorld &) = delete;
+    ~PhysicsWorld() {
+        if (w_) pe_world_destroy(w_);
+    }
+    // Copies are independent worlds with the same state (physics_world.cpp:74-120).
+    PhysicsWorld(const PhysicsWorld &o)
+        : gravity(o.gravity), broadPhaseAlgorithm(o.broadPhaseAlgorithm), npWorkers_(o.npWorkers_),
+          solverWorkers_(o.solverWorkers_), broadWorkers_(o.broadWorkers_) {
+        throwIf(pe_world_clone(o.w_, &w_));
+    }
+    PhysicsWorld &operator=(const PhysicsWorld &o) {
+        if (this == &o) return *this;
+        pe_world *c = nullptr;
+        throwIf(pe_world_clone(o.w_, &c));
+        if (w_) pe_world_destroy(w_);
+        w_ = c;
+        gravity = o.gravity;
+        broadPhaseAlgorithm = o.broadPhaseAlgorithm;
+        npWorkers_ = o.npWorkers_;
+        solverWorkers_ = o.solverWorkers_;
+        broadWorkers_ = o.broadWorkers_;
+        return *this;
+    }
+    PhysicsWorld(PhysicsWorld &&o) noexcept
+        : gravity(o.gravity), broadPhaseAlgorithm(o.broadPhaseAlgorithm), w_(o.w_), npWorkers_(o.npWorkers_),
+          solverWorkers_(o.solverWorkers_), broadWorkers_(o.broadWorkers_) {
+        o.w_ = nullptr;
+    }
+    PhysicsWorld &operator=(PhysicsWorld &&o) noexcept {
+        if (this == &o) return *this;
+        if (w_) pe_world_destroy(w_);
+        w_ = o.w_;
+        o.w_ = nullptr;
+        gravity = o.gravity;
+        broadPhaseAlgorithm = o.broadPhaseAlgorithm;
+        npWorkers_ = o.npWorkers_;
+        solverWorkers_ = o.solverWorkers_;
+        broadWorkers_ = o.broadWorkers_;
+        return *this;
+    }
 
     bool createSphere(float radius, Vec3 position, float density, bool isStatic, float restitution, float friction,
                       RigidBodyHandle &body, ColliderHandle &collider, std::string &errorMessage) {

@@ -219,6 +219,24 @@ pe_status pe_world_create(int device, pe_world **out) {
 
 void pe_world_destroy(pe_world *world) { delete world; }
 
+pe_status pe_world_clone(pe_world *world, pe_world **out) {
+    if (!world || !out) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        auto *c = new pe_world;
+        try {
+            c->w = world->w->clone();
+        } catch (...) {
+            delete c;
+            throw;
+        }
+        c->npWorkers = world->npWorkers;
+        c->solverWorkers = world->solverWorkers;
+        c->bpWorkers = world->bpWorkers;
+        *out = c;
+        return PE_OK;
+    });
+}
+
 pe_status pe_world_set_gravity(pe_world *world, float x, float y, float z) {
     if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
     world->w->gravity[0] = x;

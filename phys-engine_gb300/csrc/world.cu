@@ -179,6 +179,86 @@ void World::setSleepingEnabled(bool enabled) {
     dropGraphs();
 }
 
+std::unique_ptr<World> World::clone() {
+    PE_CHECK(cudaSetDevice(device_));
+    if (hostDirty_) {
+        pull();
+        push();
+    }
+    pull();
+    PE_CHECK(cudaStreamSynchronize(stream_));
+    auto c = std::make_unique<World>(device_);
+    c->gravity[0] = gravity[0];
+    c->gravity[1] = gravity[1];
+    c->gravity[2] = gravity[2];
+    c->algorithm = algorithm;
+    c->cellSize = cellSize;
+    c->iterations = iterations;
+    c->orderMode = orderMode;
+    c->sleepingEnabled = sleepingEnabled;
+    c->bodies = bodies;
+    c->freeBodies = freeBodies;
+    c->colliders = colliders;
+    c->freeColliders = freeColliders;
+    c->hullVerts = hullVerts;
+    c->hullOffsets = hullOffsets;
+    std::memcpy(c->sleepGravity_, sleepGravity_, sizeof(sleepGravity_));
+    c->pairCap_ = pairCap_;
+    c->entryCap_ = entryCap_;
+    c->mcap_ = mcap_;
+    c->cacheNeed_ = std::max(cacheNeed_, cacheCap_);
+    c->gridKeyBits_ = gridKeyBits_;
+    c->hashGrid_ = hashGrid_;
+    c->bodyPairs_ = bodyPairs_;
+    c->lastMEstimate_ = lastMEstimate_;
+    c->lastRawEstimate_ = lastRawEstimate_;
+    c->lastPairs_ = lastPairs_;
+    c->lastManifolds_ = lastManifolds_;
+    c->counters_ = counters_;
+    c->steps_ = steps_;
+    c->lastErr_ = lastErr_;
+    c->graphsDisabled_ = graphsDisabled_;
+    c->push();  // allocates with the same capacities and uploads the bodies
+    c->forces_ = forces_;
+    c->wakeCheck_ = wakeCheck_;
+    cudaStream_t s = stream_;
+    auto d2d = [&](void *dst, const void *src, size_t bytes) {
+        if (bytes) PE_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, s));
+    };
+    const size_t nb = nb_;
+    d2d(c->force_.ptr, force_.ptr, nb * sizeof(float4));
+    // contacts of the last step, its candidate pairs and solve colours
+    const size_t M = lastManifolds_, P = lastPairs_;
+    d2d(c->mBodyA_.ptr, mBodyA_.ptr, M * 4);
+    d2d(c->mGenA_.ptr, mGenA_.ptr, M * 4);
+    d2d(c->mBodyB_.ptr, mBodyB_.ptr, M * 4);
+    d2d(c->mGenB_.ptr, mGenB_.ptr, M * 4);
+    d2d(c->mCount_.ptr, mCount_.ptr, M * 4);
+    d2d(c->mRest_.ptr, mRest_.ptr, M * 4);
+    d2d(c->mNormal_.ptr, mNormal_.ptr, M * sizeof(float4));
+    d2d(c->mAnchorA_.ptr, mAnchorA_.ptr, 4 * M * sizeof(float4));
+    d2d(c->mAnchorB_.ptr, mAnchorB_.ptr, 4 * M * sizeof(float4));
+    d2d(c->mImpulse_.ptr, mImpulse_.ptr, 4 * M * sizeof(float4));
+    d2d(c->mFeature_.ptr, mFeature_.ptr, 4 * M * 4);
+    d2d(c->sColor_.ptr, sColor_.ptr, M * 4);
+    d2d(c->pairA_.ptr, pairA_.ptr, P * 4);
+    d2d(c->pairB_.ptr, pairB_.ptr, P * 4);
+    // warm-start cache (the copy's current cache is its slot cache_)
+    uint32_t K = 0;
+    PE_CHECK(cudaMemcpyAsync(&K, &cCount_.ptr[cache_], 4, cudaMemcpyDeviceToHost, s));
+    PE_CHECK(cudaStreamSynchronize(s));
+    K = std::min(K, cacheCap_);
+    const int to = c->cache_;
+    d2d(c->cKey_[to].ptr, cKey_[cache_].ptr, (size_t)K * 8);
+    d2d(c->cGens_[to].ptr, cGens_[cache_].ptr, (size_t)K * 8);
+    d2d(c->cA_[to].ptr, cA_[cache_].ptr, (size_t)K * sizeof(float4));
+    d2d(c->cB_[to].ptr, cB_[cache_].ptr, (size_t)K * sizeof(float4));
+    d2d(c->cT2_[to].ptr, cT2_[cache_].ptr, (size_t)K * 4);
+    PE_CHECK(cudaStreamSynchronize(s));
+    PE_CHECK(cudaMemcpy(&c->cCount_.ptr[to], &K, 4, cudaMemcpyHostToDevice));
+    return c;
+}
+
 int World::addHull(const float *verts, uint32_t count) {
     hostDirty_ = true;
     hullVerts.insert(hullVerts.end(), verts, verts + 3 * (size_t)count);

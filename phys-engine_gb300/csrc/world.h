@@ -4,6 +4,7 @@
 #pragma once
 #include <utility>
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -137,6 +138,9 @@ class World {
     void touch() { hostDirty_ = true; }
     // PhysicsWorld::setSleepingEnabled (physics_world.cpp:341-351).
     void setSleepingEnabled(bool enabled);
+    // The PhysicsWorld copy constructor (physics_world.cpp:74-93): bodies,
+    // colliders, contacts, warm-start cache, step counters and sleep state.
+    std::unique_ptr<World> clone();
 
     void step(float dt);
     // Bulk per-step I/O: set the accumulated force of bodies [0, n) (xyz each),

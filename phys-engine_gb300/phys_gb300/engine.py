@@ -67,6 +67,7 @@ SIGNATURES = {
     "pe_device_count": (ctypes.c_int, []),
     "pe_world_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_P)]),
     "pe_world_destroy": (None, [_P]),
+    "pe_world_clone": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "pe_world_set_gravity": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float]),
     "pe_world_get_gravity": (ctypes.c_int, [_P, _P]),
     "pe_world_set_broadphase": (ctypes.c_int, [_P, ctypes.c_int]),
@@ -200,6 +201,14 @@ class GpuWorld:
         if getattr(self, "h", None):
             self.lib.pe_world_destroy(self.h)
             self.h = None
+
+    def clone(self):
+        """An independent copy (the PhysicsWorld copy constructor)."""
+        h = _P()
+        check(self.lib.pe_world_clone(self.h, ctypes.byref(h)))
+        c = GpuWorld.__new__(GpuWorld)
+        c.lib, c.h, c.device = self.lib, h, self.device
+        return c
 
     def __del__(self):
         try:

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <stdexcept>
 #include <string>
+#include <utility>
 
 #include "phys_gb300_world.hpp"
 
@@ -127,6 +128,16 @@ static bool settledStackSleepsAndWakes() {
     if (world.getBody(lower).isSleeping() || world.getBody(upper).isSleeping() || !world.getBody(other).isSleeping() ||
         world.lastStepStats().solved_contact_count != 2)
         return false;
+    // copies and moves own independent state (sleeping_tests.cpp:330-343)
+    for (int i = 0; i < 120; ++i) world.step(dt);
+    PhysicsWorld copied = world;
+    PhysicsWorld moved = std::move(copied);
+    moved.step(dt);
+    if (moved.lastStepStats().sleeping_body_count != 3 || moved.lastStepStats().solved_contact_count != 0)
+        return false;
+    moved.getBody(upper).wakeUp();
+    moved.step(dt);
+    if (moved.getBody(lower).isSleeping() || !world.getBody(lower).isSleeping()) return false;
     world.setSleepingEnabled(false);
     if (world.getBody(other).isSleeping()) return false;
     world.step(dt);

@@ -358,3 +358,67 @@ def test_sleeping_write_forces_wakes(gpu):
     for k in ("pos", "quat", "lin", "ang"):
         assert_bit_equal(g.bodies()[k], o.bodies()[k], k)
     assert g.sleeping().tolist() == o.sleeping().tolist()
+
+
+# ------------------------------------------------------------- world copy ---
+def test_world_clone_is_independent_and_continues(gpu):
+    """PhysicsWorld's copy constructor (physics_world.cpp:74-93): the copy
+    carries bodies, contacts and the warm-start cache, so stepping it continues
+    the original's trajectory bit for bit; editing or stepping one leaves the
+    other unchanged."""
+    sc = scenes.generate(scenes.MIXED_VOLUME, 3000, 9)
+    g = gpu.GpuWorld(algo=1, iterations=10)
+    o = cpu.OracleWorld(algo=1, iterations=10, order_mode=1)
+    hg = g.load_scene(sc)
+    o.load_scene(sc)
+    for _ in range(30):
+        g.step(1 / 60)
+        o.step(1 / 60)
+    c = g.clone()
+    oc = o.clone()
+    compare_worlds(c, o, "fresh copy")
+    assert c.stats()["contact_count"] == g.stats()["contact_count"]
+    for _ in range(20):
+        g.step(1 / 60)
+        o.step(1 / 60)
+    compare_worlds(g, o, "original after 20 steps")
+    compare_worlds(c, oc, "copy not stepped")
+    for _ in range(20):
+        c.step(1 / 60)
+        oc.step(1 / 60)
+    compare_worlds(c, o, "copy after 20 steps (warm-start cache carried)")
+    c.remove_body(int(hg[5, 0]), int(hg[5, 1]))
+    oc.remove_body(int(hg[5, 0]), int(hg[5, 1]))
+    c.step(1 / 60)
+    oc.step(1 / 60)
+    g.step(1 / 60)
+    o.step(1 / 60)
+    compare_worlds(g, o, "original after the copy's edit")
+    gb, ob = c.bodies(), oc.bodies()
+    for k in gb:
+        gb[k][5] = ob[k][5] = 0
+        assert_bit_equal(gb[k], ob[k], f"edited copy {k}")
+    assert_manifolds_equal(c.contacts(), oc.contacts(), what="edited copy")
+
+
+def test_world_clone_sleeping_state(gpu):
+    """Copies own independent sleeping state (sleeping_tests.cpp:330-343)."""
+    import sleep_scenarios as ss
+
+    ops, dt = ss.all_scenarios()["mutator_0"]
+    g = gpu.GpuWorld()
+    o = cpu.OracleWorld(order_mode=1)
+    hg = ss.run(g, ops[:-6], dt)
+    ss.run(o, ops[:-6], dt)
+    c = g.clone()
+    oc = o.clone()
+    assert c.sleeping().tolist() == [False, True, True, True]
+    c.wake_up(gpu.Handle(ss.UPPER, 0))
+    oc.wake_body(ss.UPPER)
+    for w in (c, oc, g, o):
+        w.step(dt)
+    assert c.sleeping().tolist() == oc.sleeping().tolist() == [False, False, False, True]
+    assert g.sleeping().tolist() == [False, True, True, True]
+    for k in ("pos", "quat", "lin", "ang"):
+        assert_bit_equal(c.bodies()[k], oc.bodies()[k], k)
+    assert c.stats()["solved_contact_count"] == oc.stats()["solved_contact_count"] == 2
