@@ -30,7 +30,7 @@ typedef enum pe_status {
     PE_ERR_CREATE_FAILED = 2,    /* createSphere/createBox returned false */
     PE_ERR_STALE_HANDLE = 3,     /* getBody/getCollider returned nullptr */
     PE_ERR_CAPACITY = 4,         /* caller buffer too small; *count holds the size needed */
-    PE_ERR_UNSUPPORTED = 5,      /* e.g. BroadPhaseAlgorithm::DynamicTree on the GPU path */
+    PE_ERR_UNSUPPORTED = 5,      /* an option outside the GPU path */
     PE_ERR_CUDA = 6,             /* CUDA runtime failure (no device, out of memory, ...) */
     PE_ERR_DEVICE = 7            /* device-side failure: a bounded wait timed out, colour overflow */
 } pe_status;
@@ -138,8 +138,10 @@ pe_status pe_world_clone(pe_world *world, pe_world **out);
 /* PhysicsWorld::gravity (physics_world.hpp:37) */
 pe_status pe_world_set_gravity(pe_world *world, float x, float y, float z);
 pe_status pe_world_get_gravity(const pe_world *world, float *xyz);
-/* PhysicsWorld::broadPhaseAlgorithm (physics_world.hpp:38); DynamicTree is
-   accepted here and rejected by pe_world_step with PE_ERR_UNSUPPORTED. */
+/* PhysicsWorld::broadPhaseAlgorithm (physics_world.hpp:38).  DynamicTree
+   builds a linear BVH over the colliders every step; it reports the pair set
+   the reference's incremental tree reports (every tight-AABB overlap, sorted),
+   without its tree-maintenance counters. */
 pe_status pe_world_set_broadphase(pe_world *world, int algorithm);
 pe_status pe_world_get_broadphase(const pe_world *world, int *algorithm);
 /* Grid cell size: <= 0 keeps the reference's median policy

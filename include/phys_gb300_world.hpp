@@ -247,11 +247,9 @@ class PhysicsWorld {
 
     void step(float dt) {
         throwIf(pe_world_set_gravity(w_, gravity.x, gravity.y, gravity.z));
-        if (broadPhaseAlgorithm == BroadPhaseAlgorithm::DynamicTree)
-            throw std::invalid_argument("DynamicTree requires a persistent DynamicAabbTree instance");
-        throwIf(pe_world_set_broadphase(w_, broadPhaseAlgorithm == BroadPhaseAlgorithm::UniformGrid
-                                                ? PE_BROADPHASE_GRID
-                                                : PE_BROADPHASE_SAP));
+        throwIf(pe_world_set_broadphase(w_, broadPhaseAlgorithm == BroadPhaseAlgorithm::UniformGrid ? PE_BROADPHASE_GRID
+                                            : broadPhaseAlgorithm == BroadPhaseAlgorithm::DynamicTree ? PE_BROADPHASE_TREE
+                                                                                                       : PE_BROADPHASE_SAP));
         throwIf(pe_world_step(w_, dt));
     }
 

@@ -1529,10 +1529,14 @@ template <class T> struct World : WorldBase {
             slots.push_back(i);
         }
         ow_step_stats bp{};
-        if (algo == 1)
+        if (algo == 1) {
             gridPairs(bounds, cellSize, pairs, bp);
-        else
+        } else {
             sapPairs(bounds, pairs, bp, threads);
+            // DynamicTree: the same sorted pair set (dynamic_aabb_tree.cpp:306-327)
+            // and no sweep counters
+            if (algo == 2) bp.x_window_comparisons = 0;
+        }
         stats = ow_step_stats{};
         stats.x_window_comparisons = bp.x_window_comparisons;
         stats.aabb_pairs = bp.aabb_pairs;

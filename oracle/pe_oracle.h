@@ -80,7 +80,8 @@ ow_world *ow_create(int fp64);
 ow_world *ow_clone(const ow_world *world);
 void ow_destroy(ow_world *world);
 void ow_set_gravity(ow_world *world, double gx, double gy, double gz);
-/* algo: 0 sweep-and-prune, 1 uniform grid.  cell_size <= 0 selects the
+/* algo: 0 sweep-and-prune, 1 uniform grid, 2 dynamic tree (the same sorted
+   pairs as sweep-and-prune; no sweep counters).  cell_size <= 0 selects the
    reference's median cell size; > 0 fixes the grid cell. */
 void ow_set_broadphase(ow_world *world, int algo, double cell_size);
 /* order_mode: 0 manifold order (the reference), 1 graph-colour order. */

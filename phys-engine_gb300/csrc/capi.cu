@@ -596,8 +596,6 @@ const char *pe_world_graph_error(pe_world *world) { return world ? world->w->gra
 
 pe_status pe_world_step(pe_world *world, float dt) {
     if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
-    if (world->w->algorithm == PE_BROADPHASE_TREE)
-        return fail(PE_ERR_UNSUPPORTED, "DynamicTree broadphase is not part of the GPU path");
     return guarded([&] {
         world->w->step(dt);
         return PE_OK;

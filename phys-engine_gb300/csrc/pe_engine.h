@@ -41,6 +41,7 @@ enum : uint32_t {
     kErrBodyPairs = 128u, // a body had more grid partners than the per-body pair path holds
     kErrHashRange = 256u, // a grid cell lies outside the hashed grid's coordinate range
     kErrCacheCapacity = 512u, // the warm-start cache with carried sleeping entries exceeds its capacity
+    kErrTreeDepth = 1024u,    // a BVH traversal outgrew its stack
 };
 
 // Body flag bits (bflags) and collider flag layout (cflags).  kBodySleeping

@@ -46,6 +46,16 @@ struct BroadBuffers {
     bool hashed;
 };
 
+// Linear BVH of the DynamicTree selector (k_lbvh.cu), sized for maxN leaves.
+struct LbvhBuffers {
+    unsigned long long *keys, *keysTmp;   // Morton code << index bits | index
+    uint32_t *childL, *childR, *parent;   // internal nodes (leaf children flagged)
+    uint32_t *leafParent, *rangeMax, *visit;
+    float4 *leafMn, *leafMx;              // leaf bounds in sorted order
+    float4 *nodeMn, *nodeMx;              // internal node bounds
+    uint32_t *box;                        // [6] ordered-float bounds of the centres
+};
+
 struct PairBuffers {
     unsigned long long *keys, *keysTmp;
     uint32_t cap;
@@ -135,6 +145,10 @@ void launchPackPositions(const float4 *pos, float *p3, uint32_t n, cudaStream_t 
 void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, BroadBuffers &bb, PairBuffers &pb,
                DevStats *st, Scratch &ws, cudaStream_t s);
 void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBuffers &pb, DevStats *st, Scratch &ws,
+                cudaStream_t s);
+// DynamicTree: every overlapping pair through a linear BVH (pair keys for
+// launchPairsFinalize).
+void launchLbvh(const BroadInput &in, const LbvhBuffers &lb, PairBuffers &pb, DevStats *st, Scratch &ws,
                 cudaStream_t s);
 // Grid pairs emitted body by body in lexicographic order, mapped to slots and
 // filtered (replaces the per-cell pairs and the finalize when pb.bodyPath).

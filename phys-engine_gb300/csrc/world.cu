@@ -629,6 +629,26 @@ void World::ensureCapacity() {
     ensureScratch(std::max({nc, pairCap_, entryCap_, m, cacheCap_}));
 }
 
+void World::ensureLbvh() {
+    const uint32_t n = std::max<uint32_t>(nc_, 2);
+    lbKeys_.reserve(n);
+    lbKeysTmp_.reserve(n);
+    lbChildL_.reserve(n);
+    lbChildR_.reserve(n);
+    lbParent_.reserve(n);
+    lbLeafParent_.reserve(n);
+    lbRangeMax_.reserve(n);
+    lbVisit_.reserve(n);
+    lbBox_.reserve(8);
+    lbLeafMn_.reserve(n);
+    lbLeafMx_.reserve(n);
+    lbNodeMn_.reserve(n);
+    lbNodeMx_.reserve(n);
+    lb_ = LbvhBuffers{lbKeys_.ptr,     lbKeysTmp_.ptr, lbChildL_.ptr,  lbChildR_.ptr,   lbParent_.ptr,
+                      lbLeafParent_.ptr, lbRangeMax_.ptr, lbVisit_.ptr,  lbLeafMn_.ptr,   lbLeafMx_.ptr,
+                      lbNodeMn_.ptr,   lbNodeMx_.ptr,  lbBox_.ptr};
+}
+
 WorldView World::view(float dt) {
     WorldView w{};
     w.nb = nb_;
@@ -700,6 +720,7 @@ void World::runPipeline(float dt) {
     }
     BroadInput in{dense_ ? aabbMin_.ptr : inMin_.ptr, dense_ ? aabbMax_.ptr : inMax_.ptr, &st->inputCount, nc_};
     if (sap) launchSap(in, sapKeys_.ptr, sapVals_.ptr, bb_, pb_, st, ws_, s);
+    else if (algorithm == 2) launchLbvh(in, lb_, pb_, st, ws_, s);
     else launchGrid(in, cellSize, bb_, pb_, st, ws_, s);
     if (!sap && pb_.bodyPath)
         launchGridBodyPairs(in, bb_, pb_, dense_ ? nullptr : inSlot_.ptr, cbody_.ptr, cbgen_.ptr, st, ws_, s, fused);
@@ -733,11 +754,12 @@ bool World::finishStep() {
     PE_CHECK(cudaStreamSynchronize(stream_));
     const DevStats &h = *hostStats_;
     lastErr_ = h.err;
-    if (h.err & (kErrTimeout | kErrColors | kErrEntryCapacity)) {
+    if (h.err & (kErrTimeout | kErrColors | kErrEntryCapacity | kErrTreeDepth)) {
         throw std::runtime_error(std::string("step failed on the device: ") +
                                  ((h.err & kErrTimeout) ? "a bounded wait timed out" :
                                   (h.err & kErrColors) ? "more than 128 solver colours" :
-                                                         "grid cell range exceeds 64 key bits"));
+                                  (h.err & kErrTreeDepth) ? "a bounding-volume tree traversal outgrew its stack" :
+                                                            "grid cell range exceeds 64 key bits"));
     }
     bool retry = false, grew = false;
     if (h.err & kErrHashRange) {
@@ -950,7 +972,6 @@ unsigned long long World::launchStep(float dt) {
 
 void World::step(float dt) {
     PE_CHECK(cudaSetDevice(device_));
-    if (algorithm == 2) throw std::invalid_argument("DynamicTree requires a persistent DynamicAabbTree instance");
     if (sleepingEnabled && (gravity[0] != sleepGravity_[0] || gravity[1] != sleepGravity_[1] ||
                             gravity[2] != sleepGravity_[2]))
         hostDirty_ = true;  // a gravity change wakes every body (physics_world.cpp:439-451)
@@ -958,6 +979,7 @@ void World::step(float dt) {
         pull();
         push();
     }
+    if (algorithm == 2) ensureLbvh();  // before any capture: allocation is not captured
     if (sleepingEnabled && wakeCheck_) {
         // prepareSleeping's wake pass over the last step's contacts, on the
         // committed state (outside the step's graph: a re-run of the step

@@ -240,6 +240,12 @@ class World {
     DeviceArray<int4> bbFirst_;
     DeviceArray<uint8_t> bbInGrid_;
     uint32_t entryCap_ = 0;
+    // DynamicTree: linear BVH (allocated when the selector is first used)
+    LbvhBuffers lb_{};
+    DeviceArray<unsigned long long> lbKeys_, lbKeysTmp_;
+    DeviceArray<uint32_t> lbChildL_, lbChildR_, lbParent_, lbLeafParent_, lbRangeMax_, lbVisit_, lbBox_;
+    DeviceArray<float4> lbLeafMn_, lbLeafMx_, lbNodeMn_, lbNodeMx_;
+    void ensureLbvh();
     PairBuffers pb_{};
     DeviceArray<unsigned long long> pairKeys_, pairKeysTmp_;
     DeviceArray<uint32_t> pairFlags_, pairPos_, pairA_, pairB_, pairCounters_;

@@ -78,14 +78,14 @@ static bool invalidInputs() {
         return false;
     } catch (const std::invalid_argument &) {
     }
-    world.broadPhaseAlgorithm = BroadPhaseAlgorithm::DynamicTree;
-    try {
-        world.step(1.0f / 60.0f);
-        return false;
-    } catch (const std::invalid_argument &) {
-    }
     if (world.getBody(RigidBodyHandle{7, 3})) return false;  // stale handle -> "nullptr"
-    return true;
+    // the tree selector steps like the others (same candidate pairs)
+    world.broadPhaseAlgorithm = BroadPhaseAlgorithm::DynamicTree;
+    if (!world.createSphere(0.5f, {0, 0, 0}, 1.0f, false, 0, 0, b, c, error) ||
+        !world.createSphere(0.5f, {0.9f, 0, 0}, 1.0f, false, 0, 0, b, c, error))
+        return false;
+    world.step(1.0f / 60.0f);
+    return world.contacts().size() == 1 && world.lastStepStats().candidate_pairs == 1;
 }
 
 // Opt-in sleeping of a settled stack, after tests/world/sleeping_tests.cpp:72-110

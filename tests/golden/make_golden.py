@@ -165,6 +165,7 @@ def make_worlds():
         ("mixed_volume_grid", scenes.MIXED_VOLUME, 1500, 1, 40),
         ("pyramid_sap", scenes.PYRAMIDS_BOXES_ONLY, 1, 0, 60),
         ("boxes_plane_sap", scenes.BOXES_ON_PLANE, 64, 0, 60),
+        ("mixed_volume_tree", scenes.MIXED_VOLUME, 1500, 2, 40),
     ]
     for name, kind, n, algo, steps in runs:
         sc = scenes.generate(kind, n, 42)
@@ -178,7 +179,9 @@ def make_worlds():
         b = ref.bodies()
         st = ref.stats()
         mins, maxs = ref.bounds()
-        pairs, _ = cpu.broadphase("ref", mins, maxs, algo)
+        # the standalone call rejects the tree; the tree reports the same
+        # sorted pair set (dynamic_aabb_tree.cpp:306-327)
+        pairs, _ = cpu.broadphase("ref", mins, maxs, 0 if algo == 2 else algo)
         np.savez_compressed(
             HERE / f"world_{name}.npz", algo=np.array(algo), steps=np.array(steps), dt=np.array(dt),
             shape=sc.shape, is_static=sc.is_static, dims=sc.dims, pos=sc.pos, density=sc.density,

@@ -11,7 +11,7 @@ from phys_gb300 import scenes
 pytestmark = pytest.mark.gpu
 
 WORLD_RUNS = ["spheres_floor_sap", "spheres_floor_grid", "mixed_volume_sap", "mixed_volume_grid", "pyramid_sap",
-              "boxes_plane_sap"]
+              "boxes_plane_sap", "mixed_volume_tree"]
 
 
 def scene_from(g):
@@ -117,6 +117,8 @@ def test_world_manifold_order_matches_reference(gpu, golden, run):
     (scenes.MIXED_VOLUME, 6000, 0, 0.0, 10, 20),
     (scenes.PYRAMIDS_BOXES_ONLY, 2, 0, 0.0, 20, 40),
     (scenes.BOXES_ON_PLANE, 64, 1, 0.0, 8, 60),
+    (scenes.MIXED_VOLUME, 6000, 2, 0.0, 10, 30),
+    (scenes.PYRAMIDS_BOXES_ONLY, 2, 2, 0.0, 20, 30),
 ])
 def test_world_color_order_matches_oracle_every_step(gpu, kind, n, algo, cell, iters, steps):
     sc = scenes.generate(kind, n, 42)
@@ -240,10 +242,6 @@ def test_invalid_arguments_and_unsupported(gpu):
         w.create_body(1, [1, 1, 1], [0, 0, 0], 50.0, 0, 0, 0)  # Density is out of range
     with pytest.raises(ValueError):
         w.create_body(1, [100, 100, 1], [0, 0, 0], 1.0, 1, 0, 0)  # Box is too large
-    w.set_broadphase(gpu.TREE)
-    w.create_body(0, [0.5, 0, 0], [0, 0, 0], 1.0, 0, 0, 0)
-    with pytest.raises(NotImplementedError):
-        w.step(1 / 60)
     with pytest.raises(ValueError):
         gpu.check(w.lib.pe_world_set_worker_counts(w.h, 0, 1, 1))
 
@@ -321,7 +319,7 @@ def test_sleeping_manifold_order_matches_reference(gpu, golden, name):
     assert_observations_equal(got, _sleeping_golden(golden, name), name)
 
 
-@pytest.mark.parametrize("algo,graphs", [(1, True), (0, False)])
+@pytest.mark.parametrize("algo,graphs", [(1, True), (0, False), (2, True)])
 def test_sleeping_grid_and_direct_launches(gpu, algo, graphs):
     import sleep_scenarios as ss
     from test_oracle import assert_observations_equal
@@ -422,3 +420,36 @@ def test_world_clone_sleeping_state(gpu):
     for k in ("pos", "quat", "lin", "ang"):
         assert_bit_equal(c.bodies()[k], oc.bodies()[k], k)
     assert c.stats()["solved_contact_count"] == oc.stats()["solved_contact_count"] == 2
+
+
+
+# ------------------------------------------------------------ tree selector ---
+def test_tree_pairs_equal_sweep_on_large_and_degenerate_sets(gpu):
+    """The linear-BVH tree reports exactly the sweep-and-prune pair set: the
+    100k-body workload, a pile of coincident spheres (equal Morton codes, ties
+    broken by index), and worlds of zero, one and two bodies."""
+    sc = scenes.generate(scenes.MIXED_VOLUME, 100_000, 42)
+    worlds = {}
+    for algo in (0, 2):
+        w = gpu.GpuWorld(algo=algo, iterations=10)
+        w.load_scene(sc)
+        for _ in range(3):
+            w.step(1 / 60)
+        worlds[algo] = w
+    assert len(worlds[0].pairs()) > 1000
+    assert_bit_equal(worlds[2].pairs(), worlds[0].pairs(), "100k pairs")
+    for k in ("pos", "quat", "lin", "ang"):
+        assert_bit_equal(worlds[2].bodies()[k], worlds[0].bodies()[k], f"100k {k}")
+    assert worlds[2].stats()["aabb_pairs"] == worlds[0].stats()["aabb_pairs"]
+    assert worlds[2].stats()["x_window_comparisons"] == 0
+    for n in (0, 1, 2, 64):
+        g = gpu.GpuWorld(algo=2)
+        o = cpu.OracleWorld(algo=2, order_mode=1)
+        for i in range(n):
+            for w in (g, o):
+                w.create_body(0, [0.5, 0, 0], [0.0, 2.0 + 0.001 * (i % 3), 0.0], 1.0, 0, 0.0, 0.5)
+        for _ in range(3):
+            g.step(1 / 60)
+            o.step(1 / 60)
+        assert len(g.pairs()) == (n * (n - 1)) // 2 or n > 2
+        compare_worlds(g, o, f"{n} coincident spheres")

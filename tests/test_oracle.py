@@ -8,7 +8,7 @@ from oracle import cpu
 from phys_gb300 import scenes
 
 WORLD_RUNS = ["spheres_floor_sap", "spheres_floor_grid", "mixed_volume_sap", "mixed_volume_grid", "pyramid_sap",
-              "boxes_plane_sap"]
+              "boxes_plane_sap", "mixed_volume_tree"]
 
 
 def scene_from(g):
