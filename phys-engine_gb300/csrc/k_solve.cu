@@ -187,7 +187,7 @@ __global__ void k_cache_counts(SolveArgs a) {
     const uint32_t M = min(a.st->manifolds, a.mcap);
     const WorldView &w = a.w;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < M; k += gridDim.x * blockDim.x) {
-        const uint32_t m = a.sb.cacheVals[k];
+        const uint32_t m = a.pairOrderCache ? k : a.sb.cacheVals[k];
         const uint32_t ia = a.mv.bodyA[m], ib = a.mv.bodyB[m];
         const bool valid = ia < w.nb && ib < w.nb && (w.bflags[ia] & kBodyAlive) && (w.bflags[ib] & kBodyAlive) &&
                            w.bgen[ia] == a.mv.genA[m] && w.bgen[ib] == a.mv.genB[m] &&
@@ -199,7 +199,8 @@ __global__ void k_cache_counts(SolveArgs a) {
 __global__ void k_cache_write(SolveArgs a, CacheView nc, uint32_t cacheCap) {
     const uint32_t M = min(a.st->manifolds, a.mcap);
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < M; k += gridDim.x * blockDim.x)
-        cacheWriteManifold(a, nc, cacheCap, a.sb.cacheVals[k], a.sb.cacheOff[k], a.sb.cacheCounts[k]);
+        cacheWriteManifold(a, nc, cacheCap, a.pairOrderCache ? k : a.sb.cacheVals[k], a.sb.cacheOff[k],
+                           a.sb.cacheCounts[k]);
 }
 
 
@@ -312,14 +313,18 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
     else launchCooperative((const void *)k_solve_colored, coopBlocks, a, s);
     k_impulses_out<<<gridFor(mcap), 256, 0, s>>>(a);
     PE_LAUNCHED();
-    uint32_t keyBits = 1;
-    while (keyBits < 32 && (1ull << keyBits) < (unsigned long long)(w.nb > 2 ? w.nb : 2)) ++keyBits;
-    k_cache_keys<<<gridFor(mcap), 256, 0, s>>>(a, keyBits);
-    PE_LAUNCHED();
-    uint32_t bodyBits = 1;
-    while (bodyBits < 32 && (1ull << bodyBits) < (unsigned long long)(w.nb > 2 ? w.nb : 2)) ++bodyBits;
-    launchRadixSort<unsigned long long>(sb.cacheKeys, sb.cacheKeysTmp, sb.cacheVals, sb.cacheValsTmp,
-                                        &st->manifolds, mcap, 0, 2 * (int)bodyBits, ws, err, s);
+    if (!pairOrderCache) {
+        // several manifolds may share a body pair: cache order = (body pair,
+        // solve order), a stable sort of the solve order by pair key
+        uint32_t keyBits = 1;
+        while (keyBits < 32 && (1ull << keyBits) < (unsigned long long)(w.nb > 2 ? w.nb : 2)) ++keyBits;
+        k_cache_keys<<<gridFor(mcap), 256, 0, s>>>(a, keyBits);
+        PE_LAUNCHED();
+        launchRadixSort<unsigned long long>(sb.cacheKeys, sb.cacheKeysTmp, sb.cacheVals, sb.cacheValsTmp,
+                                            &st->manifolds, mcap, 0, 2 * (int)keyBits, ws, err, s);
+    }
+    // else one manifold per body pair, in (body A, body B) order: the cache is
+    // the manifolds' points in manifold order
     k_cache_counts<<<gridFor(mcap), 256, 0, s>>>(a);
     PE_LAUNCHED();
     launchScanExclusive(sb.cacheCounts, sb.cacheOff, &st->manifolds, mcap, newCacheCount, ws, err, s);

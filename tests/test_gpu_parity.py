@@ -453,3 +453,24 @@ def test_tree_pairs_equal_sweep_on_large_and_degenerate_sets(gpu):
             o.step(1 / 60)
         assert len(g.pairs()) == (n * (n - 1)) // 2 or n > 2
         compare_worlds(g, o, f"{n} coincident spheres")
+
+
+@pytest.mark.parametrize("sleeping", [False, True])
+def test_large_contact_counts_multikernel_solver(gpu, sleeping):
+    """More than 4096 manifolds take the multi-kernel solver (cooperative
+    colouring and sweeps, cache rebuilt in manifold order for one collider per
+    body): 16 copies of the 512-box stack scene against the oracle, every step."""
+    sc = scenes.box_stacks(4, 4)
+    g = gpu.GpuWorld(algo=0, iterations=8)
+    o = cpu.OracleWorld(algo=0, iterations=8, order_mode=1)
+    for w in (g, o):
+        w.set_sleeping_enabled(sleeping)
+        w.load_scene(sc)
+    for s in range(25):
+        g.step(1 / 120)
+        o.step(1 / 120)
+        if s % 6 == 0 or s == 24:
+            compare_worlds(g, o, f"step {s}")
+    assert g.stats()["contact_count"] > 4096
+    for f in ("solved_contact_count", "prepared_points", "warm_start_matches", "awake_body_count"):
+        assert g.stats()[f] == o.stats()[f], f
