@@ -262,6 +262,7 @@ __device__ __noinline__ void stepWorld(const BatchView &b, uint32_t wi, unsigned
     a.mcap = d.mCap;
     a.iterations = b.iterations;
     a.pairOrderCache = true;  // collider i is body i in every batched world
+    a.count = &st->manifolds;
     const CacheView nc = cacheSlice(b.cache[b.parity ^ 1u], d.cacheBase);
     uint32_t *newCount = b.cacheCount + (size_t)(b.parity ^ 1u) * b.worldCount + wi;
     solveBlock(a, nc, d.cacheCap, newCount, 0, b.maxM, smem, reinterpret_cast<uint32_t *>(smem + b.maxM), sh.solve);

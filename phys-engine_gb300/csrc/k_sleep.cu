@@ -119,7 +119,7 @@ __global__ void k_sleep_islands(WorldView w, const uint32_t *flags) {
 // Per live dynamic body: wake the islands that must wake.  inStep: the body
 // state is the step's output copy; bodies woken after the gravity pass get
 // their gravity now, and bflags receives the solver's sleeping bit.
-__global__ void k_sleep_apply(WorldView w, uint32_t *flags, float *quiet, uint32_t *bflags, int inStep) {
+__global__ void k_sleep_apply(WorldView w, uint32_t *flags, float *quiet, uint32_t *bflags, int inStep, DevStats *st) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < w.nb; i += gridDim.x * blockDim.x) {
         const uint32_t bf = w.bflags[i];
         if (!(bf & kBodyAlive) || (bf & kBodyStatic)) {
@@ -142,6 +142,7 @@ __global__ void k_sleep_apply(WorldView w, uint32_t *flags, float *quiet, uint32
             }
             w.sleepParent[i] = r;  // flattened for the pose and finish kernels
             bflags[i] = (f & kSleepAsleep) ? (bf | kBodySleeping) : (bf & ~kBodySleeping);
+            if (!(f & kSleepAsleep)) aggregatedAdd32(&st->awakeInStep, 1u);
         }
         flags[i] = f;
     }
@@ -260,18 +261,20 @@ __global__ void k_cache_merge(CacheView oc, const uint32_t *oldCount, const uint
 }
 
 // The solver's sleeping bit of every body from committed sleep flags.
-__global__ void k_sleep_bits(WorldView w, const uint32_t *flags, uint32_t *bflags) {
+__global__ void k_sleep_bits(WorldView w, const uint32_t *flags, uint32_t *bflags, DevStats *st) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < w.nb; i += gridDim.x * blockDim.x) {
         const uint32_t bf = w.bflags[i];
-        const bool asleep = (bf & kBodyAlive) && !(bf & kBodyStatic) && (flags[i] & kSleepAsleep);
+        const bool dyn = (bf & kBodyAlive) && !(bf & kBodyStatic);
+        const bool asleep = dyn && (flags[i] & kSleepAsleep);
         bflags[i] = asleep ? (bf | kBodySleeping) : (bf & ~kBodySleeping);
+        if (dyn && !asleep) aggregatedAdd32(&st->awakeInStep, 1u);
     }
 }
 
 // ------------------------------------------------------------- launchers ---
-void launchSleepBits(const WorldView &w, const uint32_t *flags, uint32_t *bflags, cudaStream_t s) {
+void launchSleepBits(const WorldView &w, const uint32_t *flags, uint32_t *bflags, DevStats *st, cudaStream_t s) {
     if (!w.nb) return;
-    k_sleep_bits<<<gridFor(w.nb), kSleepThreads, 0, s>>>(w, flags, bflags);
+    k_sleep_bits<<<gridFor(w.nb), kSleepThreads, 0, s>>>(w, flags, bflags, st);
     PE_LAUNCHED();
 }
 
@@ -286,7 +289,7 @@ void launchSleepWake(const WorldView &w, const ManifoldView &mv, uint32_t Mhost,
     }
     k_sleep_islands<<<gridFor(w.nb), kSleepThreads, 0, s>>>(w, flags);
     PE_LAUNCHED();
-    k_sleep_apply<<<gridFor(w.nb), kSleepThreads, 0, s>>>(w, flags, quiet, nullptr, 0);
+    k_sleep_apply<<<gridFor(w.nb), kSleepThreads, 0, s>>>(w, flags, quiet, nullptr, 0, nullptr);
     PE_LAUNCHED();
 }
 
@@ -298,7 +301,7 @@ void launchSleepContacts(const WorldView &w, const ManifoldView &mv, DevStats *s
     PE_LAUNCHED();
     k_sleep_islands<<<gridFor(w.nb), kSleepThreads, 0, s>>>(w, w.sleepOut);
     PE_LAUNCHED();
-    k_sleep_apply<<<gridFor(w.nb), kSleepThreads, 0, s>>>(w, w.sleepOut, w.quietOut, bflags, 1);
+    k_sleep_apply<<<gridFor(w.nb), kSleepThreads, 0, s>>>(w, w.sleepOut, w.quietOut, bflags, 1, st);
     PE_LAUNCHED();
 }
 

@@ -22,7 +22,7 @@ namespace pe {
 
 // ------------------------------------------------------------- colouring ---
 __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
-    const uint32_t M = min(a.st->manifolds, a.mcap);
+    const uint32_t M = min(*a.count, a.mcap);
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
     const WorldView &w = a.w;
     SolverBuffers &sb = a.sb;
@@ -98,8 +98,14 @@ __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
     }
 }
 
+// With sleeping on: the solver takes every manifold while some body is awake,
+// none otherwise (a contact among static and sleeping bodies is not solved).
+__global__ void k_solve_count(DevStats *st) {
+    if (threadIdx.x == 0) st->solveCount = st->awakeInStep ? st->manifolds : 0u;
+}
+
 __global__ void k_order_init(SolveArgs a, int serial) {
-    const uint32_t M = min(a.st->manifolds, a.mcap);
+    const uint32_t M = min(*a.count, a.mcap);
     for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
         a.sb.orderKeys[m] = serial ? 0u : a.sb.color[m];
         a.sb.order[m] = m;
@@ -113,7 +119,7 @@ constexpr int kPrepareThreads = 64;
 constexpr uint32_t kPrepareKeyCap = 4096;
 __global__ void __launch_bounds__(kPrepareThreads) k_prepare(SolveArgs a, uint32_t keyCap) {
     extern __shared__ unsigned long long s_keys[];
-    const uint32_t M = min(a.st->manifolds, a.mcap);
+    const uint32_t M = min(*a.count, a.mcap);
     for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x)
         a.sb.dyn[m] = manifoldFlags(a, m);
     const uint32_t cacheN = *a.oldCount;
@@ -121,7 +127,7 @@ __global__ void __launch_bounds__(kPrepareThreads) k_prepare(SolveArgs a, uint32
     if (inShared)
         for (uint32_t i = threadIdx.x; i < cacheN; i += blockDim.x) s_keys[i] = a.oldCache.key[i];
     __syncthreads();
-    prepareRange(a, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, min(a.st->manifolds, a.mcap),
+    prepareRange(a, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, min(*a.count, a.mcap),
                  inShared ? s_keys : nullptr);
 }
 
@@ -152,7 +158,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve_colored(SolveArgs a) {
 // Manifold order (the reference's own sequence), one thread.
 __global__ void k_solve_serial(SolveArgs a) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    const uint32_t M = min(a.st->manifolds, a.mcap);
+    const uint32_t M = min(*a.count, a.mcap);
     for (uint32_t k = 0; k < M; ++k) warmStartOne(a, k, k);
     for (int it = 0; it < a.iterations; ++it)
         for (uint32_t k = 0; k < M; ++k) solveOne(a, k, k);
@@ -160,7 +166,7 @@ __global__ void k_solve_serial(SolveArgs a) {
 
 // Solved impulses of the live points back to the manifolds (pair order).
 __global__ void k_impulses_out(SolveArgs a) {
-    const uint32_t M = min(a.st->manifolds, a.mcap);
+    const uint32_t M = min(*a.count, a.mcap);
     for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
         const uint32_t live = a.sb.pcount[m];
         for (uint32_t p = 0; p < live; ++p) {
@@ -176,7 +182,7 @@ __global__ void k_impulses_out(SolveArgs a) {
 // pair, stable with respect to solve order.
 // Sort key (bodyA << bits) | bodyB: the (bodyA, bodyB) order of the cache.
 __global__ void k_cache_keys(SolveArgs a, uint32_t bits) {
-    const uint32_t M = min(a.st->manifolds, a.mcap);
+    const uint32_t M = min(*a.count, a.mcap);
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < M; k += gridDim.x * blockDim.x) {
         const uint32_t m = a.sb.order[k];
         a.sb.cacheKeys[k] = ((unsigned long long)a.mv.bodyA[m] << bits) | a.mv.bodyB[m];
@@ -184,7 +190,7 @@ __global__ void k_cache_keys(SolveArgs a, uint32_t bits) {
     }
 }
 __global__ void k_cache_counts(SolveArgs a) {
-    const uint32_t M = min(a.st->manifolds, a.mcap);
+    const uint32_t M = min(*a.count, a.mcap);
     const WorldView &w = a.w;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < M; k += gridDim.x * blockDim.x) {
         const uint32_t m = a.pairOrderCache ? k : a.sb.cacheVals[k];
@@ -197,7 +203,7 @@ __global__ void k_cache_counts(SolveArgs a) {
 }
 // Writes the cache entries of manifold m (npts points) starting at entry base.
 __global__ void k_cache_write(SolveArgs a, CacheView nc, uint32_t cacheCap) {
-    const uint32_t M = min(a.st->manifolds, a.mcap);
+    const uint32_t M = min(*a.count, a.mcap);
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < M; k += gridDim.x * blockDim.x)
         cacheWriteManifold(a, nc, cacheCap, a.pairOrderCache ? k : a.sb.cacheVals[k], a.sb.cacheOff[k],
                            a.sb.cacheCounts[k]);
@@ -268,7 +274,12 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
                   const CacheView &newCache, uint32_t *newCacheCount, uint32_t cacheCap, SolverBuffers &sb,
                   int iterations, int orderMode, int coopBlocks, bool blockPath, uint32_t blockM, bool pairOrderCache,
                   DevStats *st, Scratch &ws, cudaStream_t s) {
-    SolveArgs a{w, mv, sb, oldCache, oldCacheCount, st, sb.mcap, iterations, pairOrderCache};
+    SolveArgs a{w, mv, sb, oldCache, oldCacheCount, st, sb.mcap, iterations, pairOrderCache,
+                w.sleepMode ? &st->solveCount : &st->manifolds};
+    if (w.sleepMode) {
+        k_solve_count<<<1, 32, 0, s>>>(st);
+        PE_LAUNCHED();
+    }
     uint32_t *err = &st->err;
     const uint32_t mcap = sb.mcap;
     if (blockPath) {
@@ -301,7 +312,7 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
     k_order_init<<<gridFor(mcap), 256, 0, s>>>(a, serial ? 1 : 0);
     PE_LAUNCHED();
     if (!serial)
-        launchRadixSort<uint32_t>(sb.orderKeys, sb.orderKeysTmp, sb.order, sb.orderTmp, &st->manifolds, mcap, 0, 8,
+        launchRadixSort<uint32_t>(sb.orderKeys, sb.orderKeysTmp, sb.order, sb.orderTmp, a.count, mcap, 0, 8,
                                   ws, err, s);
     k_prepare<<<gridFor(mcap, kPrepareThreads), kPrepareThreads, kPrepareKeyCap * sizeof(unsigned long long), s>>>(
         a, kPrepareKeyCap);
@@ -321,13 +332,13 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
         k_cache_keys<<<gridFor(mcap), 256, 0, s>>>(a, keyBits);
         PE_LAUNCHED();
         launchRadixSort<unsigned long long>(sb.cacheKeys, sb.cacheKeysTmp, sb.cacheVals, sb.cacheValsTmp,
-                                            &st->manifolds, mcap, 0, 2 * (int)keyBits, ws, err, s);
+                                            a.count, mcap, 0, 2 * (int)keyBits, ws, err, s);
     }
     // else one manifold per body pair, in (body A, body B) order: the cache is
     // the manifolds' points in manifold order
     k_cache_counts<<<gridFor(mcap), 256, 0, s>>>(a);
     PE_LAUNCHED();
-    launchScanExclusive(sb.cacheCounts, sb.cacheOff, &st->manifolds, mcap, newCacheCount, ws, err, s);
+    launchScanExclusive(sb.cacheCounts, sb.cacheOff, a.count, mcap, newCacheCount, ws, err, s);
     k_cache_write<<<gridFor(mcap), 256, 0, s>>>(a, newCache, cacheCap);
     PE_LAUNCHED();
 }

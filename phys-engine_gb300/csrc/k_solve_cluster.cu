@@ -441,7 +441,7 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
     const SolverBuffers &sb = a.sb;
     const WorldView &w = a.w;
-    const uint32_t M = min(a.st->manifolds, a.mcap);
+    const uint32_t M = min(*a.count, a.mcap);
     if (M > lay.blockM) {  // every rank sees the same count
         if (rank == 0 && tid == 0) atomicOr(&a.st->err, kErrSmallPath);
         return;

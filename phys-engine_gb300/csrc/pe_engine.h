@@ -104,6 +104,8 @@ struct DevStats {
     uint32_t awakeBodies;    // sleeping on: live dynamic bodies awake / asleep after the step
     uint32_t sleepingBodies;
     uint32_t carried;        // sleeping on: warm-start entries carried for sleeping contacts
+    uint32_t awakeInStep;    // sleeping on: live dynamic bodies awake after the contact wake pass
+    uint32_t solveCount;     // sleeping on: manifolds handed to the solver (0 when no body is awake)
     uint32_t pad0;
     int32_t cellLo[3];
     int32_t cellHi[3];

@@ -39,6 +39,9 @@ struct SolveArgs {
     // order is then (body A, body B) order with one manifold per key, which is
     // already the order of the rebuilt warm-start cache.
     bool pairOrderCache;
+    // Manifolds the solver takes, [0, *count): the step's manifold count, or
+    // with sleeping on zero when no body is awake (every contact is skipped).
+    const uint32_t *count;
 };
 
 // Where the velocity iterations read and write body velocities: the world's
@@ -860,7 +863,7 @@ __device__ inline void solveBlockSweeps(const SolveArgs &a, uint32_t M, int seri
 __device__ inline void solveBlock(const SolveArgs &a, const CacheView &nc, uint32_t cacheCap, uint32_t *newCount, int serial,
                            uint32_t maxM, unsigned long long *s_sort, uint32_t *s_dyn, BlockSolveShared &sh,
                            const VelStage *vs = nullptr, bool prepared = false) {
-    const uint32_t M = min(a.st->manifolds, a.mcap);
+    const uint32_t M = min(*a.count, a.mcap);
     if (M > maxM) {
         if (threadIdx.x == 0) atomicOr(&a.st->err, kErrSmallPath);
         return;

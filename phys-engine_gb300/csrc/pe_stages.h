@@ -136,7 +136,7 @@ void launchSleepWake(const WorldView &w, const ManifoldView &mv, uint32_t Mhost,
 void launchSleepContacts(const WorldView &w, const ManifoldView &mv, DevStats *st, uint32_t mcap, uint32_t *bflags,
                          cudaStream_t s);
 void launchSleepFinish(const WorldView &w, DevStats *st, DevStats *hostOut, uint32_t *done, cudaStream_t s);
-void launchSleepBits(const WorldView &w, const uint32_t *flags, uint32_t *bflags, cudaStream_t s);
+void launchSleepBits(const WorldView &w, const uint32_t *flags, uint32_t *bflags, DevStats *st, cudaStream_t s);
 void launchCacheCarry(const WorldView &w, const CacheView &oldCache, const uint32_t *oldCount, const CacheView &tmp,
                       const uint32_t *tmpCount, const CacheView &newCache, uint32_t *newCount, uint32_t cap,
                       uint32_t *carry, uint32_t *carryPos, uint32_t *carryTotal, DevStats *st, Scratch &ws,

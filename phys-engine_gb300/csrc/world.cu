@@ -215,6 +215,7 @@ std::unique_ptr<World> World::clone() {
     c->lastPairs_ = lastPairs_;
     c->lastManifolds_ = lastManifolds_;
     c->counters_ = counters_;
+    c->solveSkipped_ = solveSkipped_;
     c->steps_ = steps_;
     c->lastErr_ = lastErr_;
     c->graphsDisabled_ = graphsDisabled_;
@@ -826,7 +827,10 @@ bool World::finishStep() {
     c.warmComparisons = h.warmComparisons;
     c.warmMatches = h.warmMatches;
     c.velocityPointVisits = h.preparedPoints * (uint64_t)iterations;
-    c.colors = orderMode == 0 ? h.manifolds : h.colors;
+    // with every body asleep the solver ran on no manifold: every manifold has
+    // colour 0 (it has no moving body)
+    solveSkipped_ = sleepingEnabled && h.solveCount == 0;
+    c.colors = orderMode == 0 ? h.manifolds : solveSkipped_ ? (h.manifolds ? 1u : 0u) : h.colors;
     c.colorRounds = h.colorRounds;
     c.epaFailures = h.epaFailures;
     c.points = h.points;
@@ -1170,8 +1174,8 @@ void World::downloadOrder(uint32_t *order, uint32_t *colors) {
     }
     // The solve order is (colour, manifold index); the island solver does not
     // materialise it, so it is derived from the colours here.
-    std::vector<uint32_t> c(M);
-    PE_CHECK(cudaMemcpy(c.data(), sColor_.ptr, M * 4, cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> c(M, 0u);
+    if (!solveSkipped_) PE_CHECK(cudaMemcpy(c.data(), sColor_.ptr, M * 4, cudaMemcpyDeviceToHost));
     if (colors) std::memcpy(colors, c.data(), M * 4);
     if (order) {
         uint32_t C = 0;
@@ -1331,7 +1335,7 @@ void World::solveOnly(std::vector<float> &recs, uint32_t count, float dt, int it
         const size_t n = std::max<uint32_t>(nb_, 1);
         PE_CHECK(cudaMemcpyAsync(sleep_[1 - cur_].ptr, sleep_[cur_].ptr, n * 4, cudaMemcpyDeviceToDevice, s));
         PE_CHECK(cudaMemcpyAsync(quiet_[1 - cur_].ptr, quiet_[cur_].ptr, n * 4, cudaMemcpyDeviceToDevice, s));
-        launchSleepBits(w, sleep_[cur_].ptr, bflags_.ptr, s);
+        launchSleepBits(w, sleep_[cur_].ptr, bflags_.ptr, st, s);
     }
     launchSolver(w, mv, cacheView(cache_), &cCount_.ptr[cache_], sleeping ? tmp : cacheView(1 - cache_),
                  sleeping ? tCount_.ptr : &cCount_.ptr[1 - cache_], cacheCap_, sb_, iters, mode, (int)blocks, block, 0u,
@@ -1349,7 +1353,8 @@ void World::solveOnly(std::vector<float> &recs, uint32_t count, float dt, int it
     counters_.warmComparisons = hostStats_->warmComparisons;
     counters_.warmMatches = hostStats_->warmMatches;
     counters_.velocityPointVisits = hostStats_->preparedPoints * (uint64_t)iters;
-    counters_.colors = mode == 0 ? count : hostStats_->colors;
+    solveSkipped_ = sleepingEnabled && hostStats_->solveCount == 0;
+    counters_.colors = mode == 0 ? count : solveSkipped_ ? (count ? 1u : 0u) : hostStats_->colors;
     cur_ = 1 - cur_;
     cache_ = 1 - cache_;
     deviceNewer_ = true;

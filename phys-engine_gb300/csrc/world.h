@@ -220,6 +220,7 @@ class World {
     DeviceArray<uint32_t> tCount_, carry_, carryPos_, carryTotal_;
     uint32_t cacheNeed_ = 0;   // warm-start capacity asked for by a carry overflow
     bool wakeCheck_ = false;   // host edits since the last step: run the wake pass first
+    bool solveSkipped_ = false;  // the last step solved nothing: every body asleep
     float sleepGravity_[3] = {0, 0, 0};  // PhysicsWorld::sleepGravity
     DeviceArray<uint32_t> cbody_, cbgen_, cflags_;
     DeviceArray<float4> cshape_, clpos_, clrot_, aabbMin_, aabbMax_;
