@@ -49,7 +49,7 @@ __device__ __forceinline__ void integrateAabbOne(const WorldView &w, uint32_t *s
         w.aabbMax[i] = make4(mx, 0.0f);
         if (sapKeys) {
             sapKeys[i] = orderedFloatKey(mn.x);
-            sapVals[i] = i;
+            if (sapVals) sapVals[i] = i;
         }
     }
 }

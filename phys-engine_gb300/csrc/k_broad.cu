@@ -33,8 +33,44 @@ __global__ void k_step_init(DevStats *st, uint32_t inputCount) {
 }
 
 // ---------------------------------------------------------------- SAP ------
+// Temporal coherence of the SAP order: the last step's sorted order (sapVals)
+// is kept; its keys are refreshed and checked to still be strictly increasing
+// in (min.x key, index) — the order the sort defines — in which case the sort
+// is skipped (sortCount = 0), else the keys are laid out in index order and
+// sorted as usual.  Either way the sorted arrays are the same.
+__global__ void k_sap_presort(const uint32_t *d_n, const uint32_t *keyOf, uint32_t *keys, const uint32_t *vals,
+                              uint32_t *unsorted) {
+    const uint32_t n = *d_n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t p = vals[i];
+        bool bad = p >= n;
+        if (!bad) {
+            const uint32_t k = keyOf[p];
+            keys[i] = k;
+            if (i + 1 < n) {
+                const uint32_t q = vals[i + 1];
+                bad = q >= n || !(k < keyOf[q] || (k == keyOf[q] && p < q));
+            }
+        }
+        if (bad) atomicOr(unsorted, 1u);
+    }
+}
+
+__global__ void k_sap_order(const uint32_t *d_n, const uint32_t *keyOf, uint32_t *keys, uint32_t *vals,
+                            const uint32_t *unsorted, uint32_t *sortCount) {
+    const uint32_t n = *d_n;
+    const bool redo = *unsorted != 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *sortCount = redo ? n : 0u;
+    if (!redo) return;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        keys[i] = keyOf[i];
+        vals[i] = i;
+    }
+}
+
 __global__ void k_sap_gather(BroadInput in, const uint32_t *sortedVals, float *sMinX, float *sMaxX, float4 *sYZ,
-                             uint32_t *sIdx) {
+                             uint32_t *sIdx, uint32_t *unsorted) {
+    if (unsorted && blockIdx.x == 0 && threadIdx.x == 0) *unsorted = 0u;  // for the next step's check
     const uint32_t n = *in.d_n;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t idx = sortedVals[i];
@@ -803,10 +839,20 @@ void launchSapKeys(const BroadInput &in, uint32_t *keys, uint32_t *vals, cudaStr
 }
 
 void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, BroadBuffers &bb, PairBuffers &pb,
-               DevStats *st, Scratch &ws, cudaStream_t s) {
+               DevStats *st, Scratch &ws, cudaStream_t s, const SapCoherence *coh) {
     uint32_t *err = &st->err;
-    launchRadixSort<uint32_t>(sapKeys, bb.keyTmp32, sapVals, bb.valTmp, in.d_n, in.maxN, 0, 32, ws, err, s);
-    k_sap_gather<<<gridFor(in.maxN), 256, 0, s>>>(in, sapVals, bb.sMinX, bb.sMaxX, bb.sYZ, bb.sIdx);
+    const uint32_t *sortN = in.d_n;
+    if (coh) {
+        k_sap_presort<<<gridFor(in.maxN), 256, 0, s>>>(in.d_n, coh->keyOf, sapKeys, sapVals, coh->unsorted);
+        PE_LAUNCHED();
+        k_sap_order<<<gridFor(in.maxN), 256, 0, s>>>(in.d_n, coh->keyOf, sapKeys, sapVals, coh->unsorted,
+                                                     coh->sortCount);
+        PE_LAUNCHED();
+        sortN = coh->sortCount;
+    }
+    launchRadixSort<uint32_t>(sapKeys, bb.keyTmp32, sapVals, bb.valTmp, sortN, in.maxN, 0, 32, ws, err, s);
+    k_sap_gather<<<gridFor(in.maxN), 256, 0, s>>>(in, sapVals, bb.sMinX, bb.sMaxX, bb.sYZ, bb.sIdx,
+                                                  coh ? coh->unsorted : nullptr);
     PE_LAUNCHED();
     k_sap_window<<<gridFor(in.maxN), 256, 0, s>>>(in.d_n, bb.sMinX, bb.sMaxX, bb.len, st);
     PE_LAUNCHED();

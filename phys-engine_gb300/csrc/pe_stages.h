@@ -142,8 +142,15 @@ void launchCacheCarry(const WorldView &w, const CacheView &oldCache, const uint3
                       uint32_t *carry, uint32_t *carryPos, uint32_t *carryTotal, DevStats *st, Scratch &ws,
                       cudaStream_t s);
 void launchPackPositions(const float4 *pos, float *p3, uint32_t n, cudaStream_t s);
+// SAP order kept from step to step: keyOf[i] = min.x key of input i (written
+// by the integrate kernel), unsorted / sortCount = device words.
+struct SapCoherence {
+    const uint32_t *keyOf;
+    uint32_t *unsorted;
+    uint32_t *sortCount;
+};
 void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, BroadBuffers &bb, PairBuffers &pb,
-               DevStats *st, Scratch &ws, cudaStream_t s);
+               DevStats *st, Scratch &ws, cudaStream_t s, const SapCoherence *coh = nullptr);
 void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBuffers &pb, DevStats *st, Scratch &ws,
                 cudaStream_t s);
 // DynamicTree: every overlapping pair through a linear BVH (pair keys for

@@ -466,6 +466,8 @@ void World::ensureCapacity() {
     inMax_.reserve(nc);
     sapKeys_.reserve(nc);
     sapVals_.reserve(nc);
+    sapKeyOf_.reserve(nc);
+    sapWords_.reserve(2);
     bbKeyTmp32_.reserve(nc);
     bbValTmp_.reserve(nc);
     bbMinX_.reserve(nc);
@@ -711,8 +713,10 @@ void World::runPipeline(float dt) {
     bb_.headsCleared = fused;
     bb_.zeroState = fused ? ws_.scanState : nullptr;
     bb_.nZeroState = fused ? narrowOff + narrowTiles + 1 : 0;
+    // dense SAP keeps last step's order and skips the sort while it still holds
+    const SapCoherence coh{sapKeyOf_.ptr, sapWords_.ptr, sapWords_.ptr + 1};
     if (dense_) {
-        launchIntegrateAabb(w, sap ? sapKeys_.ptr : nullptr, sapVals_.ptr, st, nc_, s, fused ? bb_.bucketHead : nullptr,
+        launchIntegrateAabb(w, sap ? sapKeyOf_.ptr : nullptr, nullptr, st, nc_, s, fused ? bb_.bucketHead : nullptr,
                             fused ? (1u << bb_.logBuckets) : 0u);
     } else {
         launchIntegrateAabb(w, nullptr, nullptr, st, 0u, s);
@@ -720,7 +724,7 @@ void World::runPipeline(float dt) {
                       sap ? sapKeys_.ptr : nullptr, sapVals_.ptr, &st->inputCount, ws_, &st->err, s);
     }
     BroadInput in{dense_ ? aabbMin_.ptr : inMin_.ptr, dense_ ? aabbMax_.ptr : inMax_.ptr, &st->inputCount, nc_};
-    if (sap) launchSap(in, sapKeys_.ptr, sapVals_.ptr, bb_, pb_, st, ws_, s);
+    if (sap) launchSap(in, sapKeys_.ptr, sapVals_.ptr, bb_, pb_, st, ws_, s, dense_ ? &coh : nullptr);
     else if (algorithm == 2) launchLbvh(in, lb_, pb_, st, ws_, s);
     else launchGrid(in, cellSize, bb_, pb_, st, ws_, s);
     if (!sap && pb_.bodyPath)

@@ -229,7 +229,7 @@ class World {
     // broadphase input compaction
     DeviceArray<uint32_t> collectFlags_, collectPos_, inSlot_;
     DeviceArray<float4> inMin_, inMax_;
-    DeviceArray<uint32_t> sapKeys_, sapVals_;
+    DeviceArray<uint32_t> sapKeys_, sapVals_, sapKeyOf_, sapWords_;  // words: unsorted flag, sort count
     // broadphase / pairs
     BroadBuffers bb_{};
     DeviceArray<uint32_t> bbBucketHead_, bbEntryNext_;
