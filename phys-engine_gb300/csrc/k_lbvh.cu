@@ -252,8 +252,10 @@ void launchLbvh(const BroadInput &in, const LbvhBuffers &lb, PairBuffers &pb, De
     PE_LAUNCHED();
     k_lbvh_codes<<<g, kLbvhThreads, 0, s>>>(in, lb.box, lb.keys, indexBits);
     PE_LAUNCHED();
-    launchRadixSort<unsigned long long>(lb.keys, lb.keysTmp, nullptr, nullptr, in.d_n, in.maxN, 0, 30 + (int)indexBits,
-                                        ws, &st->err, s);
+    // The index bits are already ascending (keys are laid out by index) and the
+    // sort is stable, so sorting the 30 code bits orders the whole keys.
+    launchRadixSort<unsigned long long>(lb.keys, lb.keysTmp, nullptr, nullptr, in.d_n, in.maxN, (int)indexBits,
+                                        (int)indexBits + 30, ws, &st->err, s);
     k_lbvh_build<<<g, kLbvhThreads, 0, s>>>(in, lb.keys, indexBits, lb.childL, lb.childR, lb.parent, lb.leafParent,
                                             lb.rangeMax, lb.visit, lb.leafMn, lb.leafMx);
     PE_LAUNCHED();
