@@ -329,6 +329,8 @@ def run_gpu(args, rank, world_size, local_rank):
         line["differentiable"] = run_differentiable(args, local_rank)
     if world_size == 1 and not args.no_sleeping:
         line["sleeping"] = run_sleeping(args, local_rank, flush)
+    if world_size == 1 and not args.no_field:
+        line["reference_scene"] = run_reference_field(args, local_rank, flush)
     if world_size == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, steps, el, _ = cpu_port_rate(scene, 20.0, 60, threads)
@@ -673,6 +675,58 @@ def run_sleeping(args, local_rank, flush):
     return out
 
 
+# The reference's published mean step times on its own benchmark scene
+# (phys_collision_bench, mixed field, SAP, 120 Hz, 240 warm-up + 1,200 measured
+# steps, Apple M2): one worker per stage, and 4 + 4 + 4 workers at 10k
+# (benchmarks/results/mixed-sustained-sap-release.txt:161,285,347,
+# benchmarks/results/parallel-sap-sweep-release.txt:47-53).
+REF_FIELD_MS = {1000: 2.33, 5000: 13.10, 10000: 27.32}
+REF_FIELD_MS_4WORKERS = {5000: 4.17, 10000: 8.90}
+
+
+def run_reference_field(args, local_rank, flush):
+    """The reference's own benchmark scene (scenes.mixed_field: half spheres,
+    half unit boxes in two layers over a floor) at 1k, 5k and 10k bodies, SAP,
+    8 iterations, dt 1/120, 240 warm-up steps, then the timed steps; next to the
+    reference's published M2 times and the oracle port on the host cores."""
+    import torch
+
+    from oracle import cpu
+    from phys_gb300 import engine, scenes
+
+    out = {}
+    threads = os.cpu_count() or 1
+    for n in (1000, 5000, 10000):
+        sc = scenes.mixed_field(n, SEED)
+        w = engine.GpuWorld(device=local_rank, algo=engine.SAP, iterations=SLEEP_ITERATIONS, order=engine.ORDER_COLOR)
+        w.load_scene(sc)
+        for _ in range(240):
+            w.step(SLEEP_DT)
+        stream = torch.cuda.ExternalStream(w.stream(), device=torch.device("cuda", local_rank))
+        ms, launches = timed_steps(w, args.field_steps, SLEEP_DT, stream, flush)
+        st = w.stats()
+        w.close()
+        entry = {"bodies": n, "steps": args.field_steps, "ms_per_step": ms / args.field_steps,
+                 "value": n * args.field_steps / (ms / 1000.0), "unit": UNIT, "gpu_launches": launches,
+                 "contacts": int(st["contact_count"]), "candidate_pairs": int(st["candidate_pairs"]),
+                 "reference_m2_ms_per_step": REF_FIELD_MS[n]}
+        if n in REF_FIELD_MS_4WORKERS:
+            entry["reference_m2_4x3_workers_ms_per_step"] = REF_FIELD_MS_4WORKERS[n]
+        if n == 10000 and not args.no_cpu_baseline:
+            ow = cpu.OracleWorld(algo=0, iterations=SLEEP_ITERATIONS, order_mode=0, threads=threads)
+            ow.load_scene(sc)
+            for _ in range(240):
+                ow.step(SLEEP_DT)
+            t0, k = time.perf_counter(), 0
+            while k < 120 and time.perf_counter() - t0 < 10.0:
+                ow.step(SLEEP_DT)
+                k += 1
+            entry["cpu_port_ms_per_step"] = (time.perf_counter() - t0) * 1000.0 / k
+            entry["cpu_port_cores"] = threads
+        out[f"mixed_field_{n}"] = entry
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -686,6 +740,8 @@ def main():
     ap.add_argument("--diff-worlds", type=int, default=DIFF_WORLDS, help="worlds of the differentiable rollout")
     ap.add_argument("--sleep-steps", type=int, default=200, help="timed steps of the sleeping measurement")
     ap.add_argument("--no-sleeping", action="store_true", help="skip the sleeping-island measurement")
+    ap.add_argument("--field-steps", type=int, default=1200, help="timed steps of the reference-scene measurement")
+    ap.add_argument("--no-field", action="store_true", help="skip the reference's own benchmark scene")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -3,13 +3,16 @@
     python -m phys_gb300.run_workload mixed100k [--broadphase grid|sap|tree] [--steps N]
     python -m phys_gb300.run_workload stacks [--tiles X Z] [--sleeping] [--steps N]
     python -m phys_gb300.run_workload spheres1000 [--broadphase sap|grid|tree] [--steps N]
+    python -m phys_gb300.run_workload field [--bodies N] [--broadphase ...] [--steps N]
 
 `mixed100k` is the benchmark world (100,000 spheres and boxes in a 200 x 100 x
 200 m volume, dt 1/60, 10 solver iterations); `stacks` is the reference's
 settled-box profile scene (benchmarks/cpu_profile.cpp:20-41, 512 boxes in
 two-high stacks on a floor, dt 1/120, 8 iterations) repeated X x Z times;
 `spheres1000` is 1,000 spheres dropped onto a static floor (dt 1/60, 10
-iterations, SAP).
+iterations, SAP); `field` is the reference's own benchmark scene
+(benchmarks/bench_scenes.cpp:11-63: spheres and unit boxes in two layers over a
+floor, dt 1/120, 8 iterations, SAP).
 The printed `launches` (engine kernels over all steps) and `last_step_launches`
 let a profiler skip to the last steps of the run.
 """
@@ -32,7 +35,8 @@ def mixed100k_cell(scene) -> float:
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("workload", choices=("mixed100k", "stacks", "spheres1000"))
+    ap.add_argument("workload", choices=("mixed100k", "stacks", "spheres1000", "field"))
+    ap.add_argument("--bodies", type=int, default=10000)
     ap.add_argument("--broadphase", choices=("grid", "sap", "tree"), default=None)
     ap.add_argument("--tiles", type=int, nargs=2, default=(1, 1))
     ap.add_argument("--sleeping", action="store_true")
@@ -46,6 +50,11 @@ def main(argv=None):
         w = engine.GpuWorld(device=args.device, algo=algo[bp], iterations=10,
                             cell_size=mixed100k_cell(sc) if bp == "grid" else 0.0)
         dt = 1.0 / 60.0
+    elif args.workload == "field":
+        sc = scenes.mixed_field(args.bodies, 42)
+        bp = args.broadphase or "sap"
+        w = engine.GpuWorld(device=args.device, algo=algo[bp], iterations=8)
+        dt = 1.0 / 120.0
     elif args.workload == "spheres1000":
         sc = scenes.generate(scenes.SPHERES_ON_FLOOR, 1000, 42)
         bp = args.broadphase or "sap"

@@ -137,3 +137,43 @@ def box_stacks(tiles_x: int = 1, tiles_z: int = 1) -> Scene:
                  restitution=np.zeros(n, f), friction=np.full(n, f(0.6)), linvel=np.zeros((n, 3), f),
                  spin=np.zeros((n, 3), f), hull_id=np.full(n, -1, np.int32), mass=np.zeros(n, f),
                  inv_inertia=np.zeros((n, 3), f))
+
+
+def mixed_field(n: int, seed: int = 42) -> Scene:
+    """The reference's own benchmark scene (benchmarks/bench_scenes.cpp:11-63,
+    `phys_collision_bench ... mixed`): n dynamic bodies, half spheres (r 0.5) and
+    half unit boxes in random order, two layers on a 1.5 m grid with +-5 cm
+    jitter, restitution 0.1, friction 0.6, over one static floor slab 32 m wider
+    than the grid on every side (its height capped so its volume stays within
+    the body-size limit).  The reference draws the order and jitter from
+    std::mt19937 through library distributions; this restatement draws them
+    from numpy's generator with the same distributions."""
+    f = np.float32
+    cols_needed = (n + 1) // 2
+    columns = int(np.ceil(np.sqrt(float(cols_needed))))
+    rows = (cols_needed + columns - 1) // columns
+    spacing, margin = f(1.5), f(32.0)
+    fx = f(columns) * spacing + f(2.0) * margin
+    fz = f(rows) * spacing + f(2.0) * margin
+    fy = f(min(1.0, (4096.0 * 0.5) / (float(fx) * float(fz))))
+    rng = np.random.default_rng(seed)
+    sphere = np.zeros(n, bool)
+    sphere[: (n + 1) // 2] = True
+    rng.shuffle(sphere)
+    jitter = rng.uniform(-0.05, 0.05, size=(n, 3)).astype(f)
+    idx = np.arange(n)
+    column = (idx // 2) % columns
+    row = (idx // 2) // columns
+    pos = np.stack([(column.astype(f) - f(columns - 1) * f(0.5)) * spacing + jitter[:, 0],
+                    f(1.0) + (idx % 2).astype(f) * f(1.75) + jitter[:, 1],
+                    (row.astype(f) - f(rows - 1) * f(0.5)) * spacing + jitter[:, 2]], axis=1).astype(f)
+    m = n + 1
+    shape = np.concatenate([[1], np.where(sphere, 0, 1)]).astype(np.uint8)
+    dims = np.concatenate([np.array([[fx, fy, fz]], f),
+                           np.where(sphere[:, None], np.array([[0.5, 0, 0]], f), np.ones((n, 3), f))]).astype(f)
+    return Scene(shape=shape, is_static=np.concatenate([[1], np.zeros(n, np.uint8)]).astype(np.uint8), dims=dims,
+                 pos=np.concatenate([np.array([[0.0, -fy * f(0.5), 0.0]], f), pos]).astype(f),
+                 density=np.ones(m, f), restitution=np.concatenate([[0.0], np.full(n, 0.1)]).astype(f),
+                 friction=np.full(m, f(0.6)), linvel=np.zeros((m, 3), f), spin=np.zeros((m, 3), f),
+                 hull_id=np.full(m, -1, np.int32), mass=np.zeros(m, f), inv_inertia=np.zeros((m, 3), f))
+

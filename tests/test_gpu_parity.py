@@ -474,3 +474,19 @@ def test_large_contact_counts_multikernel_solver(gpu, sleeping):
     assert g.stats()["contact_count"] > 4096
     for f in ("solved_contact_count", "prepared_points", "warm_start_matches", "awake_body_count"):
         assert g.stats()[f] == o.stats()[f], f
+
+
+def test_reference_benchmark_scene_matches_oracle(gpu):
+    """The reference's own benchmark scene (mixed field over a floor, SAP,
+    8 iterations, 120 Hz) against the oracle in colour order, every 10 steps."""
+    sc = scenes.mixed_field(2000, 42)
+    g = gpu.GpuWorld(algo=0, iterations=8)
+    o = cpu.OracleWorld(algo=0, iterations=8, order_mode=1)
+    g.load_scene(sc)
+    o.load_scene(sc)
+    for s in range(60):
+        g.step(1 / 120)
+        o.step(1 / 120)
+        if s % 10 == 9:
+            compare_worlds(g, o, f"step {s}")
+    assert g.stats()["contact_count"] > 1000
