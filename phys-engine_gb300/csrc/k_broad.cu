@@ -910,8 +910,8 @@ void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBu
 __global__ void __launch_bounds__(1024)
 k_pairs_block(const unsigned long long *keys, uint32_t bits, const uint32_t *inSlot, const uint32_t *cbody,
               const uint32_t *cbgen, uint32_t *pairA, uint32_t *pairB, DevStats *st) {
-    extern __shared__ unsigned long long s_keys[];  // kBlockMaxPairs
-    uint32_t *s_flag = reinterpret_cast<uint32_t *>(s_keys + kBlockMaxPairs);
+    extern __shared__ unsigned long long s_buf[];  // 2 x kBlockMaxPairs keys, then kBlockMaxPairs flags
+    uint32_t *s_flag = reinterpret_cast<uint32_t *>(s_buf + 2 * kBlockMaxPairs);
     __shared__ uint32_t s_scan[40];
     const uint32_t n = st->rawPairs;
     if (n > kBlockMaxPairs) {
@@ -919,9 +919,9 @@ k_pairs_block(const unsigned long long *keys, uint32_t bits, const uint32_t *inS
         return;
     }
     const uint32_t n2 = nextPow2(n > 0 ? n : 1);
-    for (uint32_t i = threadIdx.x; i < n2; i += blockDim.x) s_keys[i] = i < n ? keys[i] : ~0ull;
+    for (uint32_t i = threadIdx.x; i < n2; i += blockDim.x) s_buf[i] = i < n ? keys[i] : ~0ull;
     __syncthreads();
-    blockBitonicSort<unsigned long long>(s_keys, n2);
+    const unsigned long long *s_keys = blockMergeSort<unsigned long long>(s_buf, s_buf + kBlockMaxPairs, n2);
     const unsigned long long mask = (1ull << bits) - 1ull;
     uint32_t unique = 0;
     for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
@@ -961,7 +961,7 @@ void launchPairsFinalize(const uint32_t *inSlot, const uint32_t *cbody, const ui
     uint32_t *err = &st->err;
     if (pb.blockPath) {
         static bool configured = false;
-        const size_t smem = kBlockMaxPairs * (sizeof(unsigned long long) + sizeof(uint32_t));
+        const size_t smem = kBlockMaxPairs * (2 * sizeof(unsigned long long) + sizeof(uint32_t));
         if (!configured) {
             PE_CHECK(cudaFuncSetAttribute(k_pairs_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             configured = true;

@@ -26,6 +26,62 @@ template <class K> __device__ __forceinline__ void blockBitonicSort(K *s, uint32
     }
 }
 
+// Sorts a[0, n) ascending (n a power of two, tail padded with the maximum key)
+// by merging: each thread sorts its own C = max(1, n / blockDim.x) consecutive
+// keys in registers, then runs of C, 2C, ... are merged pairwise between a and
+// b, every thread producing C outputs after a merge-path binary search (ties
+// taken from the left run).  Returns the buffer (a or b) that holds the result.
+// C is at most kMergeSortPer; all threads of the block call it.
+constexpr uint32_t kMergeSortPer = 16;
+template <class K> __device__ __forceinline__ K *blockMergeSort(K *a, K *b, uint32_t n) {
+    const uint32_t T = blockDim.x, t = threadIdx.x;
+    const uint32_t C = n > T ? n / T : 1u;
+    if (t * C < n) {
+        K r[kMergeSortPer];
+#pragma unroll
+        for (uint32_t c = 0; c < kMergeSortPer; ++c)
+            if (c < C) r[c] = a[t * C + c];
+        // insertion sort of the thread's run
+        for (uint32_t c = 1; c < C; ++c) {
+            const K v = r[c];
+            uint32_t d = c;
+            while (d > 0 && r[d - 1] > v) {
+                r[d] = r[d - 1];
+                --d;
+            }
+            r[d] = v;
+        }
+#pragma unroll
+        for (uint32_t c = 0; c < kMergeSortPer; ++c)
+            if (c < C) a[t * C + c] = r[c];
+    }
+    __syncthreads();
+    K *src = a, *dst = b;
+    for (uint32_t R = C; R < n; R <<= 1) {
+        const uint32_t o = t * C;
+        if (o < n) {
+            const uint32_t base = (o / (2 * R)) * (2 * R), k = o - base;
+            const K *A = src + base, *B = src + base + R;
+            uint32_t lo = k > R ? k - R : 0u, hi = k < R ? k : R;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (A[mid] <= B[k - mid - 1]) lo = mid + 1;
+                else hi = mid;
+            }
+            uint32_t i = lo, j = k - lo;
+            for (uint32_t c = 0; c < C; ++c) {
+                if (j >= R || (i < R && A[i] <= B[j])) dst[o + c] = A[i++];
+                else dst[o + c] = B[j++];
+            }
+        }
+        __syncthreads();
+        K *tmp = src;
+        src = dst;
+        dst = tmp;
+    }
+    return src;
+}
+
 __device__ __forceinline__ uint32_t nextPow2(uint32_t v) {
     uint32_t p = 1;
     while (p < v) p <<= 1;

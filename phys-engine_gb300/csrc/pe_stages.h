@@ -100,7 +100,10 @@ struct SolverBuffers {
 };
 
 constexpr int kMaxColors = 128;
-constexpr uint32_t kBlockMaxPairs = 16384;
+constexpr uint32_t kBlockMaxPairs = 8192;
+// The single-block finalize (a shared-memory merge sort) is chosen while the
+// expected raw pair count is at most this.
+constexpr uint32_t kBlockPreferredPairs = 6144;
 constexpr int kPreparedVec4 = 10;
 
 void launchStepInit(DevStats *st, uint32_t inputCount, cudaStream_t s);

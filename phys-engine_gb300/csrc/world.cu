@@ -923,7 +923,7 @@ unsigned long long World::launchStep(float dt) {
     uint32_t bits = 1;
     while (bits < 32 && (1ull << bits) < (unsigned long long)std::max<uint32_t>(nc_, 2)) ++bits;
     pb_.bits = bits;
-    pb_.blockPath = lastRawEstimate_ + lastRawEstimate_ / 4 + 256 <= kBlockMaxPairs;
+    pb_.blockPath = lastRawEstimate_ + lastRawEstimate_ / 4 + 256 <= kBlockPreferredPairs;
     pb_.bodyPath = algorithm == 1 && bodyPairs_;
     bb_.hashed = pb_.bodyPath && cellSize > 0.0 && hashGrid_;
     bb_.keyBits = gridKeyBits_;
