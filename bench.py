@@ -164,7 +164,7 @@ def profiled_traffic(kernel, algorithmic_bytes):
     return {"bytes": entry["dram_bytes_per_launch"] * scale, "source": entry["source"]}
 
 
-def cpu_port_rate(scene, budget_s: float, max_steps: int, threads: int):
+def cpu_port_rate(scene, budget_s: float, max_steps: int, threads: int, warmup: int = 1):
     """Oracle port (reference algorithm, reference order) on the host cores."""
     from oracle import cpu
 
@@ -172,7 +172,8 @@ def cpu_port_rate(scene, budget_s: float, max_steps: int, threads: int):
     t0 = time.perf_counter()
     w.load_scene(scene)
     load_s = time.perf_counter() - t0
-    w.step(DT)  # warm-up
+    for _ in range(max(warmup, 1)):
+        w.step(DT)
     steps, t0 = 0, time.perf_counter()
     while steps < max_steps:
         w.step(DT)
@@ -208,14 +209,15 @@ def run_reference(args, rank, world_size):
     scene = workload_scene()
     threads = os.cpu_count() or 1
     budget = 150.0
-    rate, steps, el, _ = cpu_port_rate(scene, budget, max(args.steps, 1), threads)
+    warmup = max(args.warmup, 1)
+    rate, steps, el, _ = cpu_port_rate(scene, budget, max(args.steps, 1), threads, warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world_size,
-        "steps": steps, "warmup": 1, "ms_per_step": 1000.0 * el / max(steps, 1), "higher_is_better": True,
+        "steps": steps, "warmup": warmup, "ms_per_step": 1000.0 * el / max(steps, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": f"synthetic (scene generator, seed {SEED})",
         "config": workload_config(scene, "manifold order (the reference's)"),
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{steps} consecutive steps (after 1 warm-up step) of the full 100k-body world; "
+                         "sample": f"{steps} consecutive steps (after {warmup} warm-up steps) of the full 100k-body world; "
                                    f"the reference's own build is not available on this host, so the oracle "
                                    f"restatement of its algorithm (bit-identical to it) is timed"},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
