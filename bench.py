@@ -283,9 +283,7 @@ def run_gpu(args, rank, world_size, local_rank):
             flush.add_(1.0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        w.write_forces(forces)
-        w.step(DT)
-        w.read_poses(poses_p, poses_q)
+        w.step_io(DT, forces, poses_p, poses_q)
         e2e_s += time.perf_counter() - t0
     e2e_value = replica_throughput(world_size, scene.count * e2e_steps,
                                    max_over_ranks(e2e_s, world_size, f"cuda:{local_rank}"))

@@ -227,6 +227,12 @@ pe_status pe_world_read_bodies(pe_world *world, float *positions, float *rotatio
    (xyz) / rotations (xyzw) out.  Either output pointer may be NULL. */
 pe_status pe_world_write_forces(pe_world *world, const float *forces, uint32_t n);
 pe_status pe_world_read_poses(pe_world *world, float *positions, float *rotations);
+/* pe_world_write_forces + pe_world_step + pe_world_read_poses in one call with a
+   single host-device synchronisation: the forces (n xyz triples, may be 0 / NULL)
+   are copied in, the step runs, and the new positions / rotations (either may
+   be NULL) are copied out.  Results are those of the three calls. */
+pe_status pe_world_step_io(pe_world *world, const float *forces, uint32_t n, float dt, float *positions,
+                           float *rotations);
 /* The CUDA stream (cudaStream_t) the world's kernels run on, for event timing
    by the caller. */
 pe_status pe_world_get_stream(pe_world *world, void **stream);

@@ -572,6 +572,15 @@ pe_status pe_world_write_forces(pe_world *world, const float *forces, uint32_t n
     });
 }
 
+pe_status pe_world_step_io(pe_world *world, const float *forces, uint32_t n, float dt, float *positions,
+                           float *rotations) {
+    if (!world || (n && !forces)) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        world->w->stepIO(forces, n, dt, positions, rotations);
+        return PE_OK;
+    });
+}
+
 pe_status pe_world_read_poses(pe_world *world, float *positions, float *rotations) {
     if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
     return guarded([&] {

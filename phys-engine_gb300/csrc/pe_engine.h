@@ -122,6 +122,12 @@ struct WorldView {
     uint32_t nb, nc;
     BodyState cur, nxt;
     const float4 *force;     // nullable: all forces zero
+    // nullable: the caller's forces as they were handed over (xyz for bodies
+    // [0, force3n), zero beyond), read in place of `force`
+    const float *force3;
+    uint32_t force3n;
+    // nullable: positions also written here as xyz per body by the pose kernel
+    float *pos3;
     const float4 *mat;       // invMass, restitution, friction, mass
     const float4 *iinv;      // diagonal local inverse inertia (xyz)
     const uint32_t *bflags;

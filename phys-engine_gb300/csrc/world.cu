@@ -659,6 +659,9 @@ WorldView World::view(float dt) {
     w.cur = BodyState{pos_[cur_].ptr, rot_[cur_].ptr, lin_[cur_].ptr, ang_[cur_].ptr};
     w.nxt = BodyState{pos_[1 - cur_].ptr, rot_[1 - cur_].ptr, lin_[1 - cur_].ptr, ang_[1 - cur_].ptr};
     w.force = forces_ ? force_.ptr : nullptr;
+    w.force3 = rawForces_ ? xfer3_.ptr : nullptr;
+    w.force3n = rawForces_ ? force3n_ : 0u;
+    w.pos3 = packPoses_ ? posOut_.ptr : nullptr;
     w.mat = mat_.ptr;
     w.iinv = iinv_.ptr;
     w.bflags = bflags_.ptr;
@@ -862,7 +865,7 @@ bool World::GraphKey::operator==(const GraphKey &o) const {
            coopBlocks == o.coopBlocks && blockSolver == o.blockSolver && blockM == o.blockM && pairBits == o.pairBits &&
            blockPairs == o.blockPairs && bodyPairs == o.bodyPairs && hashed == o.hashed && gridKeyBits == o.gridKeyBits && cellSize == o.cellSize && dense == o.dense &&
            localIdentity == o.localIdentity && forces == o.forces && identityColliders == o.identityColliders &&
-           sleeping == o.sleeping;
+           sleeping == o.sleeping && rawForces == o.rawForces && packPoses == o.packPoses && force3n == o.force3n;
 }
 
 World::GraphKey World::currentKey(float dt) const {
@@ -894,6 +897,9 @@ World::GraphKey World::currentKey(float dt) const {
     k.forces = forces_;
     k.identityColliders = identityColliders_;
     k.sleeping = sleepingEnabled;
+    k.rawForces = rawForces_;
+    k.packPoses = packPoses_;
+    k.force3n = rawForces_ ? force3n_ : 0u;
     return k;
 }
 
@@ -978,7 +984,13 @@ unsigned long long World::launchStep(float dt) {
     return graphLaunches_[p];
 }
 
-void World::step(float dt) {
+void World::step(float dt) { runStep(dt, nullptr, 0, nullptr, nullptr); }
+
+void World::stepIO(const float *forces, uint32_t n, float dt, float *positions, float *rotations) {
+    runStep(dt, forces, n, positions, rotations);
+}
+
+void World::runStep(float dt, const float *forces, uint32_t nForces, float *positions, float *rotations) {
     PE_CHECK(cudaSetDevice(device_));
     if (sleepingEnabled && (gravity[0] != sleepGravity_[0] || gravity[1] != sleepGravity_[1] ||
                             gravity[2] != sleepGravity_[2]))
@@ -988,6 +1000,27 @@ void World::step(float dt) {
         push();
     }
     if (algorithm == 2) ensureLbvh();  // before any capture: allocation is not captured
+    // Step I/O without extra kernels: the step reads the caller's forces where
+    // they land and writes packed positions from its pose kernel.  With
+    // sleeping on, forces go through the expanding kernel (it wakes bodies).
+    rawForces_ = packPoses_ = false;
+    force3n_ = 0;
+    if (forces && nForces) {
+        if (sleepingEnabled || forces_) {  // forces_: forces written earlier for this step
+            stageForces(forces, nForces);
+        } else {
+            force3n_ = std::min<uint32_t>(nForces, nb_);
+            xfer3_.reserve(3 * (size_t)std::max<uint32_t>(nb_, 1));
+            if (force3n_)
+                PE_CHECK(cudaMemcpyAsync(xfer3_.ptr, forces, 3 * (size_t)force3n_ * sizeof(float),
+                                         cudaMemcpyHostToDevice, stream_));
+            rawForces_ = force3n_ > 0;
+        }
+    }
+    if (positions && nb_) {
+        posOut_.reserve(3 * (size_t)nb_);
+        packPoses_ = true;
+    }
     if (sleepingEnabled && wakeCheck_) {
         // prepareSleeping's wake pass over the last step's contacts, on the
         // committed state (outside the step's graph: a re-run of the step
@@ -1005,7 +1038,14 @@ void World::step(float dt) {
         PE_CHECK(cudaEventRecord(evStart_, stream_));
         const unsigned long long launches = launchStep(dt);
         PE_CHECK(cudaEventRecord(evEnd_, stream_));
+        // poses of this attempt's output copy, read back under the same
+        // synchronisation as the step (a re-run attempt copies them again)
+        if (nb_ && positions)
+            PE_CHECK(cudaMemcpyAsync(positions, posOut_.ptr, 3 * (size_t)nb_ * sizeof(float), cudaMemcpyDeviceToHost,
+                                     stream_));
+        if (nb_ && rotations) enqueuePoses(1 - cur_, nullptr, rotations);
         if (finishStep()) {
+            rawForces_ = packPoses_ = false;
             float ms = 0, st[5] = {0, 0, 0, 0, 0};
             PE_CHECK(cudaEventElapsedTime(&ms, evStart_, evEnd_));
             // stage times from the stamps the stage kernels wrote (0 when a
@@ -1043,6 +1083,14 @@ void World::writeForces(const float *forces, uint32_t n) {
         pull();
         push();
     }
+    stageForces(forces, n);
+    PE_CHECK(cudaStreamSynchronize(stream_));  // the caller may reuse its array on return
+}
+
+// Caller forces copied as they are and expanded on the device (static and dead
+// bodies masked); enqueued only: the caller's array must stay valid until the
+// stream is next synchronised.
+void World::stageForces(const float *forces, uint32_t n) {
     n = std::min<uint32_t>(n, nb_);
     if (n) {
         // the caller's array as it is; static and dead bodies masked on the device
@@ -1064,7 +1112,6 @@ void World::writeForces(const float *forces, uint32_t n) {
                 }
         }
     }
-    PE_CHECK(cudaStreamSynchronize(stream_));  // the caller may reuse its array on return
     forces_ = true;
 }
 
@@ -1075,19 +1122,23 @@ void World::readPoses(float *positions, float *rotations) {
         push();
     }
     if (nb_) {
-        // positions packed to the caller's 3 floats on the device; rotations
-        // are already 4 floats per body
-        if (positions) {
-            xfer3_.reserve(3 * (size_t)nb_);
-            launchPackPositions(pos_[cur_].ptr, xfer3_.ptr, nb_, stream_);
-            PE_CHECK(cudaMemcpyAsync(positions, xfer3_.ptr, 3 * (size_t)nb_ * sizeof(float), cudaMemcpyDeviceToHost,
-                                     stream_));
-        }
-        if (rotations)
-            PE_CHECK(cudaMemcpyAsync(rotations, rot_[cur_].ptr, (size_t)nb_ * sizeof(float4), cudaMemcpyDeviceToHost,
-                                     stream_));
+        enqueuePoses(cur_, positions, rotations);
         PE_CHECK(cudaStreamSynchronize(stream_));
     }
+}
+
+// Positions packed to the caller's 3 floats on the device (rotations are
+// already 4 floats per body) from state copy `which`; enqueued only.
+void World::enqueuePoses(int which, float *positions, float *rotations) {
+    if (positions) {
+        xfer3_.reserve(3 * (size_t)nb_);
+        launchPackPositions(pos_[which].ptr, xfer3_.ptr, nb_, stream_);
+        PE_CHECK(cudaMemcpyAsync(positions, xfer3_.ptr, 3 * (size_t)nb_ * sizeof(float), cudaMemcpyDeviceToHost,
+                                 stream_));
+    }
+    if (rotations)
+        PE_CHECK(cudaMemcpyAsync(rotations, rot_[which].ptr, (size_t)nb_ * sizeof(float4), cudaMemcpyDeviceToHost,
+                                 stream_));
 }
 
 // ------------------------------------------------------------- downloads ---

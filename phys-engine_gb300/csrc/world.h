@@ -147,6 +147,9 @@ class World {
     // and read the current poses (positions xyz, rotations xyzw).
     void writeForces(const float *forces, uint32_t n);
     void readPoses(float *positions, float *rotations);
+    // writeForces + step + readPoses with one synchronisation (any pointer may
+    // be null).
+    void stepIO(const float *forces, uint32_t n, float dt, float *positions, float *rotations);
     // Standalone stages (BroadPhase::findCandidatePairs, solve on explicit manifolds).
     void broadphaseOnly(const float *mins, const float *maxs, uint32_t n, int algo, double cell,
                         std::vector<uint32_t> &pairs, StepCounters &c);
@@ -179,6 +182,9 @@ class World {
     ManifoldView manifoldView();
     CacheView cacheView(int which);
     void runPipeline(float dt);
+    void runStep(float dt, const float *forces, uint32_t nForces, float *positions, float *rotations);
+    void stageForces(const float *forces, uint32_t n);
+    void enqueuePoses(int which, float *positions, float *rotations);
     bool finishStep();
     void computePossiblePairs();
     // PhysicsWorld::wakeContacts (physics_world.cpp:353-371) on the host mirror
@@ -207,6 +213,11 @@ class World {
     DeviceArray<float4> pos_[2], rot_[2], lin_[2], ang_[2];
     DeviceArray<float4> force_, mat_, iinv_;
     DeviceArray<float> xfer3_;  // 3 floats per body: caller forces in, positions out
+    DeviceArray<float> posOut_;  // 3 floats per body: positions written by the step for the caller
+    // this step reads the caller's forces from xfer3_ (force3n bodies) and
+    // writes packed positions to posOut_ (set per step by runStep)
+    bool rawForces_ = false, packPoses_ = false;
+    uint32_t force3n_ = 0;
     DeviceArray<uint32_t> poseDone_;  // arrival counter of the pose kernel's blocks
     DeviceArray<uint32_t> bflags_, bgen_;
     // sleeping: flags and quiet times (two copies, like the body state), the
@@ -286,7 +297,8 @@ class World {
         uint32_t blockM;
         uint32_t pairBits, gridKeyBits;
         double cellSize;
-        bool dense, localIdentity, forces, identityColliders, sleeping;
+        bool dense, localIdentity, forces, identityColliders, sleeping, rawForces, packPoses;
+        uint32_t force3n;
         bool operator==(const GraphKey &o) const;
     };
     cudaGraphExec_t graph_[2] = {nullptr, nullptr};

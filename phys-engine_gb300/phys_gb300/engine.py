@@ -99,6 +99,7 @@ SIGNATURES = {
     "pe_world_read_bodies": (ctypes.c_int, [_P, _P, _P, _P, _P]),
     "pe_world_write_forces": (ctypes.c_int, [_P, _P, _u32]),
     "pe_world_read_poses": (ctypes.c_int, [_P, _P, _P]),
+    "pe_world_step_io": (ctypes.c_int, [_P, _P, _u32, ctypes.c_float, _P, _P]),
     "pe_world_get_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "pe_world_set_graphs": (ctypes.c_int, [_P, ctypes.c_int]),
     "pe_world_graph_error": (ctypes.c_char_p, [_P]),
@@ -388,6 +389,12 @@ class GpuWorld:
 
     def read_poses(self, positions=None, rotations=None):
         check(self.lib.pe_world_read_poses(self.h, _ptr(positions), _ptr(rotations)))
+
+    def step_io(self, dt, forces=None, positions=None, rotations=None):
+        """write_forces + step + read_poses with one synchronisation."""
+        f = None if forces is None else _f32(forces)
+        check(self.lib.pe_world_step_io(self.h, _ptr(f), 0 if f is None else len(f), float(dt), _ptr(positions),
+                                        _ptr(rotations)))
 
     def stream(self) -> int:
         s = _P()

@@ -490,3 +490,25 @@ def test_reference_benchmark_scene_matches_oracle(gpu):
         if s % 10 == 9:
             compare_worlds(g, o, f"step {s}")
     assert g.stats()["contact_count"] > 1000
+
+
+def test_step_io_equals_separate_calls(gpu):
+    """pe_world_step_io = write_forces + step + read_poses, bit for bit."""
+    sc = scenes.generate(scenes.MIXED_VOLUME, 5000, 3)
+    a = gpu.GpuWorld(algo=1, cell_size=2.2, iterations=10)
+    b = gpu.GpuWorld(algo=1, cell_size=2.2, iterations=10)
+    a.load_scene(sc)
+    b.load_scene(sc)
+    rng = np.random.default_rng(1)
+    n = sc.count
+    for s in range(12):
+        f = rng.normal(size=(n, 3)).astype(np.float32) * (s % 3)
+        pa, qa = np.zeros((n, 3), np.float32), np.zeros((n, 4), np.float32)
+        pb, qb = np.zeros((n, 3), np.float32), np.zeros((n, 4), np.float32)
+        a.step_io(1 / 60, f, pa, qa)
+        b.write_forces(f)
+        b.step(1 / 60)
+        b.read_poses(pb, qb)
+        assert_bit_equal(pa, pb, f"step {s} positions")
+        assert_bit_equal(qa, qb, f"step {s} rotations")
+    compare_worlds(a, b, "after step_io")
