@@ -131,30 +131,6 @@ __global__ void __launch_bounds__(kPrepareThreads) k_prepare(SolveArgs a, uint32
                  inShared ? s_keys : nullptr);
 }
 
-__global__ void __launch_bounds__(kSolveThreads) k_solve_colored(SolveArgs a) {
-    __shared__ uint32_t s_start[kMaxColors + 1];
-    const uint32_t C = min(a.st->colors, (uint32_t)kMaxColors);
-    if (threadIdx.x == 0) {
-        uint32_t acc = 0;
-        for (uint32_t c = 0; c < C; ++c) {
-            s_start[c] = acc;
-            acc += a.sb.colorCount[c];
-        }
-        s_start[C] = acc;
-    }
-    __syncthreads();
-    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
-    for (uint32_t c = 0; c < C; ++c) {
-        for (uint32_t k = s_start[c] + gtid; k < s_start[c + 1]; k += gstride) warmStartOne(a, k, a.sb.order[k]);
-        gridBarrier(a.sb.bar, &a.st->err);
-    }
-    for (int it = 0; it < a.iterations; ++it)
-        for (uint32_t c = 0; c < C; ++c) {
-            for (uint32_t k = s_start[c] + gtid; k < s_start[c + 1]; k += gstride) solveOne(a, k, a.sb.order[k]);
-            gridBarrier(a.sb.bar, &a.st->err);
-        }
-}
-
 // Manifold order (the reference's own sequence), one thread.
 __global__ void k_solve_serial(SolveArgs a) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
@@ -261,10 +237,9 @@ static void launchCooperative(const void *fn, int blocks, SolveArgs &args, cudaS
 int maxCooperativeBlocks(int smCount) {
     static int perSm = -1;
     if (perSm < 0) {
-        int a = 0, b = 0;
+        int a = 0;
         PE_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_color, kSolveThreads, 0));
-        PE_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_solve_colored, kSolveThreads, 0));
-        perSm = a < b ? a : b;
+        perSm = a;
         if (perSm < 1) perSm = 1;
     }
     return perSm * smCount;
@@ -309,19 +284,24 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
     PE_CHECK(cudaMemsetAsync(sb.bar, 0, 2 * sizeof(uint32_t), s));
     const bool serial = orderMode == 0;
     if (!serial) launchCooperative((const void *)k_color, coopBlocks, a, s);
-    k_order_init<<<gridFor(mcap), 256, 0, s>>>(a, serial ? 1 : 0);
-    PE_LAUNCHED();
-    if (!serial)
-        launchRadixSort<uint32_t>(sb.orderKeys, sb.orderKeysTmp, sb.order, sb.orderTmp, a.count, mcap, 0, 8,
-                                  ws, err, s);
+    // the solve order itself is needed by the serial sweep and by a cache
+    // rebuilt in solve order; the island sweeps order each island themselves
+    if (serial || !pairOrderCache) {
+        k_order_init<<<gridFor(mcap), 256, 0, s>>>(a, serial ? 1 : 0);
+        PE_LAUNCHED();
+        if (!serial)
+            launchRadixSort<uint32_t>(sb.orderKeys, sb.orderKeysTmp, sb.order, sb.orderTmp, a.count, mcap, 0, 8,
+                                      ws, err, s);
+    }
     k_prepare<<<gridFor(mcap, kPrepareThreads), kPrepareThreads, kPrepareKeyCap * sizeof(unsigned long long), s>>>(
         a, kPrepareKeyCap);
     PE_LAUNCHED();
     if (serial) {
         k_solve_serial<<<1, 32, 0, s>>>(a);
         PE_LAUNCHED();
+    } else {
+        launchSolveIslands(a, ws, s);
     }
-    else launchCooperative((const void *)k_solve_colored, coopBlocks, a, s);
     k_impulses_out<<<gridFor(mcap), 256, 0, s>>>(a);
     PE_LAUNCHED();
     if (!pairOrderCache) {

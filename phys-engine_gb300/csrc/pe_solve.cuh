@@ -414,15 +414,101 @@ __device__ __forceinline__ void solveOne(const Prep &pr, uint32_t k, uint32_t i,
     if (!sA) vel.store(bi.x, linA, angA);
     if (!sB) vel.store(bi.y, linB, angB);
 }
+// solveOne for prepared data read from L2 (the island sweeps of the
+// multi-kernel path): each further point's constants are requested while the
+// point before it is solved (they do not depend on it), so only the first load
+// is on the update chain.  The arithmetic is solveOne's, operation for operation.
+template <class Prep, class Vel>
+__device__ __forceinline__ void solveOneChained(const Prep &pr, uint32_t k, uint32_t i, const Vel &vel) {
+    const uint2 bi = vel.bodies(k, i);
+    const float4 pm = pr.pm(i);
+    const float4 nf = pr.pn(i);
+    const uint32_t npts = pr.count(i);
+    float4 o[10], on[10];
+#pragma unroll
+    for (int v = 0; v < 10; ++v) o[v] = pr.pt(v, 0, i);
+    float4 imp = pr.imp(0, i), impn = imp;
+    const bool sA = pm.y != 0.0f, sB = pm.w != 0.0f;
+    const V3 n{nf.x, nf.y, nf.z};
+    const float friction = nf.w;
+    V3 linA = vel.lin(bi.x), angA = vel.ang(bi.x);
+    V3 linB = vel.lin(bi.y), angB = vel.ang(bi.y);
+    for (uint32_t p = 0; p < npts; ++p) {
+        if (p > 0) {
+#pragma unroll
+            for (int v = 0; v < 10; ++v) o[v] = on[v];
+            imp = impn;
+        }
+        if (p + 1 < npts) {
+#pragma unroll
+            for (int v = 0; v < 10; ++v) on[v] = pr.pt(v, p + 1, i);
+            impn = pr.imp(p + 1, i);
+        }
+        if (o[0].w <= 0.0f) continue;  // inverseEffectiveMass <= 0
+        const V3 offA = f4xyz(o[0]), offB = f4xyz(o[1]), t1 = f4xyz(o[2]), t2 = f4xyz(o[3]);
+        const float iem = o[0].w, bias = o[1].w, rv = o[2].w, itm00 = o[3].w, itm01 = o[4].w, itm11 = o[5].w;
+        const V3 vA = linA + cross(angA, offA);
+        const V3 vB = linB + cross(angB, offB);
+        const V3 rel = vB - vA;
+        float vn = dot(rel, n);
+        float delta = -(vn + rv - bias) / iem;
+        float prev = imp.x;
+        imp.x = smax(prev + delta, 0.0f);
+        float applied = imp.x - prev;
+        V3 impulse = n * applied;
+        if (!sA) {
+            linA += (-impulse) * pm.x;
+            angA += f4xyz(o[4]) * (-applied);
+        }
+        if (!sB) {
+            linB += impulse * pm.z;
+            angB += f4xyz(o[5]) * applied;
+        }
+        if (itm00 <= 0.0f || itm11 <= 0.0f) {
+            pr.setImp(p, i, imp);
+            continue;
+        }
+        const float ntr1 = o[6].w, ntr2 = o[7].w;
+        float limit = smax(friction, 0.0f) * imp.x;
+        float tv1 = dot(rel, t1) + ntr1 * applied;
+        float tv2 = dot(rel, t2) + ntr2 * applied;
+        float d1 = -(itm00 * tv1 + itm01 * tv2);
+        float d2 = -(itm01 * tv1 + itm11 * tv2);
+        float p1 = imp.y, p2 = imp.z;
+        imp.y += d1;
+        imp.z += d2;
+        float lsq = imp.y * imp.y + imp.z * imp.z;
+        if (lsq > limit * limit) {
+            float sc = limit / sqrtf(lsq);
+            imp.y *= sc;
+            imp.z *= sc;
+        }
+        float a1 = imp.y - p1, a2 = imp.z - p2;
+        V3 ti = t1 * a1 + t2 * a2;
+        V3 rA = f4xyz(o[6]) * a1 + f4xyz(o[8]) * a2;
+        V3 rB = f4xyz(o[7]) * a1 + f4xyz(o[9]) * a2;
+        if (!sA) {
+            linA += (-ti) * pm.x;
+            angA += -rA;
+        }
+        if (!sB) {
+            linB += ti * pm.z;
+            angB += rB;
+        }
+        pr.setImp(p, i, imp);
+    }
+    if (!sA) vel.store(bi.x, linA, angA);
+    if (!sB) vel.store(bi.y, linB, angB);
+}
 template <class Vel> __device__ __forceinline__ void solveOne(const SolveArgs &a, uint32_t k, uint32_t m, const Vel &vel) {
     solveOne(GlobalPrep{a}, k, m, vel);
 }
 __device__ __forceinline__ void solveOne(const SolveArgs &a, uint32_t k, uint32_t m) {
     solveOne(GlobalPrep{a}, k, m, GlobalVel{a});
 }
-
-// Cooperative sweep: warm start, then `iterations` sweeps, each colour by colour
-// with a grid barrier between colours.
+__device__ __forceinline__ void solveOneChained(const SolveArgs &a, uint32_t k, uint32_t m) {
+    solveOneChained(GlobalPrep{a}, k, m, GlobalVel{a});
+}
 
 __device__ __forceinline__ void cacheWriteManifold(const SolveArgs &a, const CacheView &nc, uint32_t cacheCap,
                                                    uint32_t m, uint32_t base, uint32_t npts) {

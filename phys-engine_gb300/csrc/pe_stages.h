@@ -97,6 +97,15 @@ struct SolverBuffers {
     uint2 *stageSlot;               // [mcap]
     uint32_t *stageBody;            // [2 * mcap + 64]
     uint32_t *islandList;           // [kIslandMax * nb]
+    // island sweeps of the multi-kernel path (k_solve_islands.cu)
+    uint32_t *islPar;               // [2 * nb] union-find parents, then per-root manifold counts
+    uint32_t *islOff;               // [nb] list offset of each root's island
+    uint32_t *islRoot, *islSlot;    // [mcap] island root and slot of each solved manifold
+    uint32_t *islList;              // [mcap] manifolds island by island
+    uint32_t *islRoots, *islLone;   // [mcap] island roots; solved manifolds without a dynamic body
+    unsigned long long *islKeys, *islKeysTmp;  // [mcap] island queue (as u32), spare
+    unsigned long long *islSort;    // [2 * mcap] sort scratch of large islands
+    uint32_t *islCounters;          // [8] islands, lone manifolds, work queue, listed manifolds, queue fills
 };
 
 constexpr int kMaxColors = 128;
@@ -134,6 +143,9 @@ void launchExpandForces(const float *f3, const uint32_t *bflags, float4 *force, 
 // decision and counts after the pose kernel.  launchCacheCarry: the next
 // warm-start cache from the carried sleeping entries of the old cache and
 // the solver's entries (written to tmp).
+struct SolveArgs;
+// The multi-kernel path's sweeps island by island (after k_color and prepare).
+void launchSolveIslands(const SolveArgs &a, Scratch &ws, cudaStream_t s);
 void launchSleepWake(const WorldView &w, const ManifoldView &mv, uint32_t Mhost, uint32_t mcap, uint32_t *flags,
                      float *quiet, uint32_t *err, cudaStream_t s);
 void launchSleepContacts(const WorldView &w, const ManifoldView &mv, DevStats *st, uint32_t mcap, uint32_t *bflags,

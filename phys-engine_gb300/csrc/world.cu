@@ -555,6 +555,17 @@ void World::ensureCapacity() {
     sStageSlot_.reserve(m);
     sStageBody_.reserve(2 * (size_t)m + 64);
     sIslandList_.reserve((size_t)kIslandMax * nb);
+    sIslPar_.reserve(2 * (size_t)nb);
+    sIslOff_.reserve(nb);
+    sIslRoot_.reserve(m);
+    sIslSlot_.reserve(m);
+    sIslList_.reserve(m);
+    sIslRoots_.reserve(m);
+    sIslLone_.reserve(m);
+    sIslCounters_.reserve(8);
+    sIslKeys_.reserve(m);
+    sIslKeysTmp_.reserve(m);
+    sIslSort_.reserve(2 * (size_t)m);
     sb_ = SolverBuffers{m,
                         sBest_.ptr,
                         sUsed_.ptr,
@@ -583,7 +594,18 @@ void World::ensureCapacity() {
                         sCounters_.ptr,
                         sStageSlot_.ptr,
                         sStageBody_.ptr,
-                        sIslandList_.ptr};
+                        sIslandList_.ptr,
+                        sIslPar_.ptr,
+                        sIslOff_.ptr,
+                        sIslRoot_.ptr,
+                        sIslSlot_.ptr,
+                        sIslList_.ptr,
+                        sIslRoots_.ptr,
+                        sIslLone_.ptr,
+                        sIslKeys_.ptr,
+                        sIslKeysTmp_.ptr,
+                        sIslSort_.ptr,
+                        sIslCounters_.ptr};
 
     // Warm-start caches keep their contents when they grow.
     const uint32_t needCache = std::max(4 * m, cacheNeed_);
@@ -629,7 +651,7 @@ void World::ensureCapacity() {
         carryPos_.reserve(cacheCap_);
         carryTotal_.reserve(1);
     }
-    ensureScratch(std::max({nc, pairCap_, entryCap_, m, cacheCap_}));
+    ensureScratch(std::max({nc, nb, pairCap_, entryCap_, m, cacheCap_}));
 }
 
 void World::ensureLbvh() {

@@ -272,6 +272,8 @@ class World {
     DeviceArray<unsigned long long> sBest_, sUsed_, sEpoch_, sCacheKeys_, sCacheKeysTmp_;
     DeviceArray<uint32_t> sColor_, sDyn_, sColorCount_, sOrderKeys_, sOrderKeysTmp_, sOrder_, sOrderTmp_, sPcount_,
         sCacheVals_, sCacheValsTmp_, sCacheCounts_, sCacheOff_, sBar_, sCounters_, sStageBody_, sIslandList_;
+    DeviceArray<uint32_t> sIslPar_, sIslOff_, sIslRoot_, sIslSlot_, sIslList_, sIslRoots_, sIslLone_, sIslCounters_;
+    DeviceArray<unsigned long long> sIslKeys_, sIslKeysTmp_, sIslSort_;
     DeviceArray<float4> sPm_, sPmI_, sPp_, sPimp_, sPn_;
     DeviceArray<uint2> sPbody_, sStageSlot_;
     // warm-start caches (two copies)
