@@ -239,7 +239,8 @@ int maxCooperativeBlocks(int smCount) {
     if (perSm < 0) {
         int a = 0;
         PE_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_color, kSolveThreads, 0));
-        perSm = a;
+        const int b = solveIslandsBlocksPerSm();
+        perSm = a < b ? a : b;
         if (perSm < 1) perSm = 1;
     }
     return perSm * smCount;
@@ -300,7 +301,7 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
         k_solve_serial<<<1, 32, 0, s>>>(a);
         PE_LAUNCHED();
     } else {
-        launchSolveIslands(a, ws, s);
+        launchSolveIslands(a, coopBlocks, ws, s);
     }
     k_impulses_out<<<gridFor(mcap), 256, 0, s>>>(a);
     PE_LAUNCHED();

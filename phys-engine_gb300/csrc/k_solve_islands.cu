@@ -13,10 +13,18 @@
 //   k_isl_count : each solved manifold's island and slot in it; islands listed
 //   k_isl_fill  : manifolds into their islands' lists (offsets from a scan);
 //                 islands of 32 manifolds or more queued before the others
-//   k_isl_solve : one warp per island (large ones first, from a queue): the
-//                 island's manifolds sorted by (colour, index), then warm start
-//                 and iterations colour by colour with __syncwarp; manifolds
-//                 without a dynamic body (nothing to share) are solved alone
+//   k_isl_solve : one warp per island (those of 32 manifolds or more first,
+//                 from a queue): the island's manifolds sorted by (colour,
+//                 index), then warm start and iterations colour by colour with
+//                 __syncwarp; islands of fewer than kIslThread manifolds one
+//                 per thread, manifold after manifold in that order (a stack
+//                 of two boxes would leave 30 lanes idle); manifolds without a
+//                 dynamic body (nothing to share) are solved alone
+//   k_isl_solve_large : when some island has kIslLarge manifolds or more, all
+//                 islands together in grid-wide colour sweeps instead: the
+//                 manifolds bucketed by colour, a grid barrier per colour.
+//                 Manifolds of one colour share no dynamic body, so their
+//                 order inside a colour does not change the result.
 #include "pe_kernels.cuh"
 #include "pe_prims.cuh"
 #include "pe_solve.cuh"
@@ -29,6 +37,20 @@ namespace {
 constexpr int kIslThreads = 128;           // four warps per block
 constexpr uint32_t kIslWarpSort = 1024;    // island keys sorted in shared memory up to this size
 constexpr uint32_t kIslNone = 0xFFFFFFFFu;
+// An island of this many manifolds (a settled pile; one warp would take it
+// colour by colour 32 manifolds at a time) sends every island of the step to
+// the grid-wide sweeps: measured on piles of 5,000 and 10,000 bodies, keeping
+// the smaller islands on warps only adds their sweep time to the grid's.
+constexpr uint32_t kIslLarge = 512;
+constexpr uint32_t kIslThread = 8;         // islands of fewer manifolds: one thread each
+// islCounters: [0] islands, [1] lone manifolds (solved, no dynamic body), [2]
+// work queue of k_isl_solve, [3] listed manifolds, [4] / [5] islands of 32
+// manifolds or more / kIslThread to 31 queued, [6] smaller islands, [7] set
+// when an island reached kIslLarge manifolds; [kIslColorCount + c] manifolds
+// of colour c in the grid-wide sweeps, [kIslColorFill + c] their fill cursors
+constexpr uint32_t kIslColorCount = 8;
+constexpr uint32_t kIslColorFill = 8 + kMaxColors;
+static_assert(kIslColorFill + kMaxColors == kIslCounterWords, "island counter layout");
 
 inline uint32_t islGrid(uint32_t n) {
     const uint32_t b = (n + kIslThreads - 1) / kIslThreads;
@@ -69,7 +91,7 @@ __global__ void k_isl_init(SolveArgs a) {
     const uint32_t M = min(*a.count, a.mcap);
     uint32_t *par = islPar(a), *cnt = islCnt(a);
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
-    if (t < 8) a.sb.islCounters[t] = 0u;
+    for (uint32_t i = t; i < kIslCounterWords; i += stride) a.sb.islCounters[i] = 0u;
     for (uint32_t i = t; i < a.w.nb; i += stride) cnt[i] = 0u;
     for (uint32_t m = t; m < M; m += stride) {
         const uint32_t fl = a.sb.dyn[m];
@@ -88,9 +110,6 @@ __global__ void k_isl_unite(SolveArgs a) {
     }
 }
 
-// islCounters: [0] islands, [1] lone manifolds (solved, no dynamic body),
-// [2] work queue of k_isl_solve, [3] listed manifolds, [4] / [5] large / small
-// islands queued.
 __global__ void k_isl_count(SolveArgs a) {
     const uint32_t M = min(*a.count, a.mcap);
     uint32_t *par = islPar(a), *cnt = islCnt(a);
@@ -101,6 +120,7 @@ __global__ void k_isl_count(SolveArgs a) {
             root = islFind(par, (fl & kFlagDynA) ? a.mv.bodyA[m] : a.mv.bodyB[m], a.w.nb);
             const uint32_t pos = atomicAdd(&cnt[root], 1u);
             a.sb.islSlot[m] = pos;
+            if (pos + 1 == kIslLarge) a.sb.islCounters[7] = 1u;
             if (pos == 0) a.sb.islRoots[atomicAdd(&a.sb.islCounters[0], 1u)] = root;
         } else if (fl & kFlagValid) {
             a.sb.islLone[atomicAdd(&a.sb.islCounters[1], 1u)] = m;
@@ -109,22 +129,34 @@ __global__ void k_isl_count(SolveArgs a) {
     }
 }
 
+// Islands of at least this many manifolds go to the grid-wide sweeps: all
+// once some island is large, none otherwise.
+__device__ __forceinline__ uint32_t islSweepFrom(const SolveArgs &a) {
+    return a.sb.islCounters[7] ? 1u : kIslNone;
+}
+
 __global__ void k_isl_fill(SolveArgs a) {
     const uint32_t M = min(*a.count, a.mcap);
     const uint32_t *cnt = islCnt(a);
+    const uint32_t sweepFrom = islSweepFrom(a);
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
     for (uint32_t m = t; m < M; m += stride) {
         const uint32_t r = a.sb.islRoot[m];
-        if (r != kIslNone) a.sb.islList[a.sb.islOff[r] + a.sb.islSlot[m]] = m;
+        if (r == kIslNone) continue;
+        a.sb.islList[a.sb.islOff[r] + a.sb.islSlot[m]] = m;
+        if (cnt[r] >= sweepFrom) aggregatedAppendKeyed(a.sb.islCounters + kIslColorCount, a.sb.color[m]);
     }
-    // the queue: islands of 32 manifolds or more at the front (a warp's
-    // lanes all busy; they bound the sweep), the others behind them
-    uint32_t *queue = reinterpret_cast<uint32_t *>(a.sb.islKeys);
+    // the warp queue: islands of 32 manifolds or more at the front (a warp's
+    // lanes all busy; they bound the sweep), those of kIslThread to 31 from
+    // the back; smaller ones to the per-thread list
+    uint32_t *queue = reinterpret_cast<uint32_t *>(a.sb.islKeys), *tiny = queue + a.mcap;
     const uint32_t nIsl = a.sb.islCounters[0];
     for (uint32_t i = t; i < nIsl; i += stride) {
         const uint32_t r = a.sb.islRoots[i];
+        if (cnt[r] >= sweepFrom) continue;
         if (cnt[r] >= 32) queue[atomicAdd(&a.sb.islCounters[4], 1u)] = r;
-        else queue[nIsl - 1 - atomicAdd(&a.sb.islCounters[5], 1u)] = r;
+        else if (cnt[r] >= kIslThread) queue[nIsl - 1 - atomicAdd(&a.sb.islCounters[5], 1u)] = r;
+        else tiny[aggregatedAppend(&a.sb.islCounters[6])] = r;
     }
 }
 
@@ -153,12 +185,40 @@ __global__ void __launch_bounds__(kIslThreads) k_isl_solve(SolveArgs a) {
     __shared__ uint32_t s_start[kIslThreads / 32][kMaxColors + 1];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t nIsl = a.sb.islCounters[0];
+    const uint32_t nFront = a.sb.islCounters[4], nWarp = nFront + a.sb.islCounters[5], nTiny = a.sb.islCounters[6];
+    const uint32_t nItems = nWarp + (nTiny + 31) / 32;
+    const uint32_t *queue = reinterpret_cast<const uint32_t *>(a.sb.islKeys), *tiny = queue + a.mcap;
     for (;;) {
         uint32_t i = 0;
         if (lane == 0) i = atomicAdd(&a.sb.islCounters[2], 1u);
         i = __shfl_sync(0xffffffffu, i, 0);
-        if (i >= nIsl) break;
-        const uint32_t r = reinterpret_cast<const uint32_t *>(a.sb.islKeys)[i];
+        if (i >= nItems) break;
+        if (i >= nWarp) {
+            // 32 small islands, one per lane, each swept manifold after
+            // manifold in (colour, index) order
+            const uint32_t t = (i - nWarp) * 32 + lane;
+            if (t < nTiny) {
+                const uint32_t r = tiny[t];
+                const uint32_t n = islCnt(a)[r], base = a.sb.islOff[r];
+                unsigned long long *keys = &s_keys[warp][lane * kIslThread];
+                for (uint32_t j = 0; j < n; ++j) {
+                    const uint32_t m = a.sb.islList[base + j];
+                    const unsigned long long key = ((unsigned long long)a.sb.color[m] << 32) | m;
+                    uint32_t p = j;
+                    for (; p > 0 && keys[p - 1] > key; --p) keys[p] = keys[p - 1];
+                    keys[p] = key;
+                }
+                for (int pass = 0; pass <= a.iterations; ++pass)
+                    for (uint32_t j = 0; j < n; ++j) {
+                        const uint32_t m = (uint32_t)(keys[j] & 0xFFFFFFFFull);
+                        if (pass == 0) warmStartOne(a, j, m);
+                        else solveOneChained(a, j, m);
+                    }
+            }
+            __syncwarp();
+            continue;
+        }
+        const uint32_t r = i < nFront ? queue[i] : queue[nIsl - 1 - (i - nFront)];
         const uint32_t n = islCnt(a)[r], base = a.sb.islOff[r];
         // the island's manifolds in (colour, index) order
         const uint32_t n2 = nextPow2(n);
@@ -208,7 +268,54 @@ __global__ void __launch_bounds__(kIslThreads) k_isl_solve(SolveArgs a) {
     }
 }
 
-void launchSolveIslands(const SolveArgs &a, Scratch &ws, cudaStream_t s) {
+// Large islands, all together: bucket their manifolds by colour (the
+// bucket lists live in islKeysTmp), then warm start and iterations colour by
+// colour with a grid barrier after each colour.  Every block reads the same
+// counts, so with no large island all return before the first barrier.
+__global__ void __launch_bounds__(kSolveThreads) k_isl_solve_large(SolveArgs a) {
+    __shared__ uint32_t s_start[kMaxColors + 1];
+    const uint32_t *count = a.sb.islCounters + kIslColorCount;
+    uint32_t *fill = a.sb.islCounters + kIslColorFill;
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (int c = 0; c < kMaxColors; ++c) {
+            s_start[c] = acc;
+            acc += count[c];
+        }
+        s_start[kMaxColors] = acc;
+    }
+    __syncthreads();
+    if (s_start[kMaxColors] == 0) return;
+    const uint32_t M = min(*a.count, a.mcap);
+    const uint32_t *cnt = islCnt(a);
+    const uint32_t sweepFrom = islSweepFrom(a);
+    uint32_t *list = reinterpret_cast<uint32_t *>(a.sb.islKeysTmp);
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
+    for (uint32_t m = gtid; m < M; m += gstride) {
+        const uint32_t r = a.sb.islRoot[m];
+        if (r == kIslNone || cnt[r] < sweepFrom) continue;
+        const uint32_t c = a.sb.color[m];
+        list[s_start[c] + aggregatedAppendKeyed(fill, c)] = m;
+    }
+    gridBarrier(a.sb.bar, &a.st->err);
+    for (int pass = 0; pass <= a.iterations; ++pass)
+        for (int c = 0; c < kMaxColors; ++c) {
+            if (s_start[c] == s_start[c + 1]) continue;
+            for (uint32_t k = s_start[c] + gtid; k < s_start[c + 1]; k += gstride) {
+                if (pass == 0) warmStartOne(a, k, list[k]);
+                else solveOne(a, k, list[k]);
+            }
+            gridBarrier(a.sb.bar, &a.st->err);
+        }
+}
+
+int solveIslandsBlocksPerSm() {
+    int b = 0;
+    PE_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_isl_solve_large, kSolveThreads, 0));
+    return b;
+}
+
+void launchSolveIslands(const SolveArgs &a, int coopBlocks, Scratch &ws, cudaStream_t s) {
     const uint32_t mcap = a.mcap;
     k_isl_init<<<islGrid(mcap), kIslThreads, 0, s>>>(a);
     PE_LAUNCHED();
@@ -222,6 +329,19 @@ void launchSolveIslands(const SolveArgs &a, Scratch &ws, cudaStream_t s) {
     k_isl_fill<<<islGrid(mcap), kIslThreads, 0, s>>>(a);
     PE_LAUNCHED();
     k_isl_solve<<<152 * 4, kIslThreads, 0, s>>>(a);
+    PE_LAUNCHED();
+    SolveArgs args = a;
+    void *params[] = {&args};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(coopBlocks);
+    cfg.blockDim = dim3(kSolveThreads);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PE_CHECK(cudaLaunchKernelExC(&cfg, (const void *)k_isl_solve_large, params));
     PE_LAUNCHED();
 }
 

@@ -40,6 +40,19 @@ __device__ __forceinline__ void aggregatedCount(unsigned long long *counters, ui
     if ((int)(threadIdx.x & 31) == leader) atomicAdd(&counters[key], (unsigned long long)__popc(peers));
 }
 
+// Appends to counters[key]: one atomic per group of converged lanes sharing
+// the key; returns the lane's slot.
+__device__ __forceinline__ uint32_t aggregatedAppendKeyed(uint32_t *counters, uint32_t key) {
+    const uint32_t active = __activemask();
+    const uint32_t peers = __match_any_sync(active, key);
+    const uint32_t lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(&counters[key], (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
 // Counters of a new step: all zero, the bound count, empty grid bounds.
 __device__ __forceinline__ unsigned long long globalNs() {
     unsigned long long t;

@@ -105,7 +105,8 @@ struct SolverBuffers {
     uint32_t *islRoots, *islLone;   // [mcap] island roots; solved manifolds without a dynamic body
     unsigned long long *islKeys, *islKeysTmp;  // [mcap] island queue (as u32), spare
     unsigned long long *islSort;    // [2 * mcap] sort scratch of large islands
-    uint32_t *islCounters;          // [8] islands, lone manifolds, work queue, listed manifolds, queue fills
+    uint32_t *islCounters;          // [kIslCounterWords] islands, lone manifolds, work queue, listed manifolds,
+                                    // queue fills; large islands' manifolds per colour and fill cursors
 };
 
 constexpr int kMaxColors = 128;
@@ -144,8 +145,11 @@ void launchExpandForces(const float *f3, const uint32_t *bflags, float4 *force, 
 // warm-start cache from the carried sleeping entries of the old cache and
 // the solver's entries (written to tmp).
 struct SolveArgs;
-// The multi-kernel path's sweeps island by island (after k_color and prepare).
-void launchSolveIslands(const SolveArgs &a, Scratch &ws, cudaStream_t s);
+// The multi-kernel path's sweeps island by island (after k_color and prepare);
+// islands of kIslLarge manifolds or more in grid-wide colour sweeps (a
+// cooperative launch of at most coopBlocks blocks).
+constexpr uint32_t kIslCounterWords = 8 + 2 * kMaxColors;
+void launchSolveIslands(const SolveArgs &a, int coopBlocks, Scratch &ws, cudaStream_t s);
 void launchSleepWake(const WorldView &w, const ManifoldView &mv, uint32_t Mhost, uint32_t mcap, uint32_t *flags,
                      float *quiet, uint32_t *err, cudaStream_t s);
 void launchSleepContacts(const WorldView &w, const ManifoldView &mv, DevStats *st, uint32_t mcap, uint32_t *bflags,
@@ -206,6 +210,8 @@ struct ClusterSolveLayout {
 };
 constexpr uint32_t kBlockMaxBodies = 1u << 20;
 int maxCooperativeBlocks(int smCount);
+// Co-resident blocks per SM of the large islands' cooperative sweep kernel.
+int solveIslandsBlocksPerSm();
 void launchGeneratePairs(const float4 *in, float4 *out, uint32_t n, cudaStream_t s);
 
 } // namespace pe

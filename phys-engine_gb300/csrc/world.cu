@@ -562,7 +562,7 @@ void World::ensureCapacity() {
     sIslList_.reserve(m);
     sIslRoots_.reserve(m);
     sIslLone_.reserve(m);
-    sIslCounters_.reserve(8);
+    sIslCounters_.reserve(kIslCounterWords);
     sIslKeys_.reserve(m);
     sIslKeysTmp_.reserve(m);
     sIslSort_.reserve(2 * (size_t)m);

@@ -492,6 +492,59 @@ def test_reference_benchmark_scene_matches_oracle(gpu):
     assert g.stats()["contact_count"] > 1000
 
 
+def island_mix_scene(patch: int, patches: int):
+    """A static floor with islands of the sizes the island sweeps tell apart:
+    `patches` patches of patch x patch touching unit boxes (a 30 x 30 patch is
+    one island of thousands of manifolds, a 10 x 10 one of 442), rows of 20
+    and of 12 touching spheres (islands of 39 and 23 manifolds) and two-high
+    box stacks (islands of two)."""
+    f = np.float32
+    pos, shape, dims = [[0.0, -0.5, 0.0]], [1], [[64.0, 1.0, 64.0]]
+    for p in range(patches):
+        x0, z0 = f(-31.0) + f(11.0) * f(p % 4), f(-31.0) + f(11.0) * f(p // 4)
+        for i in range(patch):
+            for k in range(patch):
+                pos.append([x0 + f(0.999) * f(i), 0.5, z0 + f(0.999) * f(k)])
+                shape.append(1)
+                dims.append([1.0, 1.0, 1.0])
+    for row, count in enumerate([20] * 6 + [12] * 6):
+        z0 = f(-31.0) if count == 20 else f(-8.0)
+        for i in range(count):
+            pos.append([f(16.0) + f(2.5) * f(row % 6), 0.499, z0 + f(0.998) * f(i)])
+            shape.append(0)
+            dims.append([0.5, 0.0, 0.0])
+    for i in range(10):
+        for level in range(2):
+            pos.append([f(-31.0) + f(2.0) * f(i), f(0.5) + f(1.0) * f(level), 20.0])
+            shape.append(1)
+            dims.append([1.0, 1.0, 1.0])
+    n = len(pos)
+    static = np.zeros(n, np.uint8)
+    static[0] = 1
+    return scenes.Scene(shape=np.array(shape, np.uint8), is_static=static, dims=np.array(dims, f),
+                        pos=np.array(pos, f), density=np.ones(n, f), restitution=np.zeros(n, f),
+                        friction=np.full(n, f(0.5)), linvel=np.zeros((n, 3), f), spin=np.zeros((n, 3), f),
+                        hull_id=np.full(n, -1, np.int32), mass=np.zeros(n, f), inv_inertia=np.zeros((n, 3), f))
+
+
+@pytest.mark.parametrize("patch,patches", [(30, 1), (10, 12)])
+def test_island_sizes_match_oracle(gpu, patch, patches):
+    """Islands of two manifolds to thousands against the oracle in colour
+    order: one island of thousands (every island in grid-wide sweeps), or
+    twelve of 442 with smaller ones (per-warp and per-thread sweeps)."""
+    sc = island_mix_scene(patch, patches)
+    g = gpu.GpuWorld(algo=0, iterations=8)
+    o = cpu.OracleWorld(algo=0, iterations=8, order_mode=1)
+    g.load_scene(sc)
+    o.load_scene(sc)
+    for s in range(12):
+        g.step(1 / 120)
+        o.step(1 / 120)
+        if s % 4 == 3:
+            compare_worlds(g, o, f"step {s}")
+    assert g.stats()["solved_contact_count"] > 4096
+
+
 def test_step_io_equals_separate_calls(gpu):
     """pe_world_step_io = write_forces + step + read_poses, bit for bit."""
     sc = scenes.generate(scenes.MIXED_VOLUME, 5000, 3)
