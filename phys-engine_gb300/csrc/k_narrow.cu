@@ -57,8 +57,7 @@ k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *_
     const uint32_t m = s_prefix + local;
     if (hit) {
         if (m < mcap) storeManifold(out, m, w, ca, cb, ba, bb, lm, restitution, friction);
-        aggregatedAppend(&st->points);
-        if (lm.count > 1) atomicAdd(&st->points, lm.count - 1);
+        aggregatedAdd32(&st->points, (uint32_t)lm.count);
     }
     if (threadIdx.x == 0 && tile + 1 == ntiles) {
         st->manifolds = s_prefix + total;

@@ -84,8 +84,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
             const uint32_t word = c >> 6;
             if (d & 1u) __stcg(&sb.bodyUsed[2 * ba + word], __ldcg(&sb.bodyUsed[2 * ba + word]) | bit);
             if (d & 2u) __stcg(&sb.bodyUsed[2 * bb + word], __ldcg(&sb.bodyUsed[2 * bb + word]) | bit);
-            atomicAdd(&sb.colorCount[c], 1u);
-            atomicMax(&a.st->colors, c + 1);
+            aggregatedAppendKeyed(sb.colorCount, c);
+            aggregatedMax32(&a.st->colors, c + 1);
             aggregatedAppend(&sb.counters[0]);
         }
         gridBarrier(sb.bar, &a.st->err);

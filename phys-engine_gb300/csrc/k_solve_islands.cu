@@ -118,12 +118,12 @@ __global__ void k_isl_count(SolveArgs a) {
         uint32_t root = kIslNone;
         if ((fl & kFlagValid) && (fl & (kFlagDynA | kFlagDynB))) {
             root = islFind(par, (fl & kFlagDynA) ? a.mv.bodyA[m] : a.mv.bodyB[m], a.w.nb);
-            const uint32_t pos = atomicAdd(&cnt[root], 1u);
+            const uint32_t pos = aggregatedAppendKeyed(cnt, root);
             a.sb.islSlot[m] = pos;
             if (pos + 1 == kIslLarge) a.sb.islCounters[7] = 1u;
-            if (pos == 0) a.sb.islRoots[atomicAdd(&a.sb.islCounters[0], 1u)] = root;
+            if (pos == 0) a.sb.islRoots[aggregatedAppend(&a.sb.islCounters[0])] = root;
         } else if (fl & kFlagValid) {
-            a.sb.islLone[atomicAdd(&a.sb.islCounters[1], 1u)] = m;
+            a.sb.islLone[aggregatedAppend(&a.sb.islCounters[1])] = m;
         }
         a.sb.islRoot[m] = root;
     }
@@ -154,8 +154,8 @@ __global__ void k_isl_fill(SolveArgs a) {
     for (uint32_t i = t; i < nIsl; i += stride) {
         const uint32_t r = a.sb.islRoots[i];
         if (cnt[r] >= sweepFrom) continue;
-        if (cnt[r] >= 32) queue[atomicAdd(&a.sb.islCounters[4], 1u)] = r;
-        else if (cnt[r] >= kIslThread) queue[nIsl - 1 - atomicAdd(&a.sb.islCounters[5], 1u)] = r;
+        if (cnt[r] >= 32) queue[aggregatedAppend(&a.sb.islCounters[4])] = r;
+        else if (cnt[r] >= kIslThread) queue[nIsl - 1 - aggregatedAppend(&a.sb.islCounters[5])] = r;
         else tiny[aggregatedAppend(&a.sb.islCounters[6])] = r;
     }
 }

@@ -32,6 +32,14 @@ __device__ __forceinline__ void aggregatedAdd32(uint32_t *counter, uint32_t v) {
     if (g.thread_rank() == 0 && s) atomicAdd(counter, s);
 }
 
+// Maximum into *counter: one atomic per converged group of lanes.
+__device__ __forceinline__ void aggregatedMax32(uint32_t *counter, uint32_t v) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    const uint32_t mx = cg::reduce(g, v, cg::greater<uint32_t>());
+    if (g.thread_rank() == 0) atomicMax(counter, mx);
+}
+
 // Adds 1 to counters[key] once per group of converged lanes sharing the key.
 __device__ __forceinline__ void aggregatedCount(unsigned long long *counters, uint32_t key) {
     const uint32_t active = __activemask();
