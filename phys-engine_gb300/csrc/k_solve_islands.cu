@@ -57,11 +57,17 @@ inline uint32_t islGrid(uint32_t n) {
     return b ? (b < 152u * 16u ? b : 152u * 16u) : 1u;
 }
 
-__device__ __forceinline__ uint32_t islFind(const uint32_t *par, uint32_t i, uint32_t nb) {
+// Root of i's island, halving the path on the way (par[i] = grandparent).
+// Safe beside concurrent unions: only non-roots are written, a non-root
+// never becomes a root again, and a grandparent stays an ancestor.
+__device__ __forceinline__ uint32_t islFind(uint32_t *par, uint32_t i, uint32_t nb) {
     for (uint32_t n = 0; n <= nb; ++n) {
         const uint32_t p = ldvol(&par[i]);
         if (p == i) return i;
-        i = p;
+        const uint32_t gp = ldvol(&par[p]);
+        if (gp == p) return p;
+        par[i] = gp;
+        i = gp;
     }
     return i;
 }
