@@ -10,9 +10,13 @@
 //
 // Colouring: priority(m) = a bijective 32-bit mix of m; every manifold takes the
 // smallest colour not used by a higher-priority manifold sharing one of its
-// dynamic bodies (greedy in decreasing priority), computed in parallel rounds
-// (Jones-Plassmann): a manifold is coloured once it holds the highest priority
-// among the uncoloured manifolds at both its bodies.
+// dynamic bodies (greedy in decreasing priority).  Computed without rounds: each
+// body lists its manifolds (up to kIslandMax), and a manifold is coloured as soon
+// as every higher-priority manifold at its dynamic bodies has its colour — the
+// colour then depends on those colours only, whenever it is computed.  A body
+// with more manifolds sends the step to parallel rounds (Jones-Plassmann): a
+// manifold is coloured once it holds the highest priority among the uncoloured
+// manifolds at both its bodies; the same colouring.
 #include "pe_block.cuh"
 #include "pe_kernels.cuh"
 #include "pe_solve.cuh"
@@ -26,6 +30,9 @@ __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
     const WorldView &w = a.w;
     SolverBuffers &sb = a.sb;
+    // per-body manifold lists: counts in islOff, lists in islandList (both
+    // free until the island sweeps)
+    uint32_t *incCount = sb.islOff, *inc = sb.islandList;
     for (uint32_t m = gtid; m < M; m += gstride) {
         uint32_t ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
         bool da = ba < w.nb && w.bgen[ba] == a.mv.genA[m] && bodyMoves(w.bflags[ba]);
@@ -35,15 +42,81 @@ __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
         if (da) {
             __stcg(&sb.bodyUsed[2 * ba], 0ull);
             __stcg(&sb.bodyUsed[2 * ba + 1], 0ull);
+            __stcg(&incCount[ba], 0u);
         }
         if (db) {
             __stcg(&sb.bodyUsed[2 * bb], 0ull);
             __stcg(&sb.bodyUsed[2 * bb + 1], 0ull);
+            __stcg(&incCount[bb], 0u);
         }
     }
     if (blockIdx.x == 0)
         for (int c = threadIdx.x; c < kMaxColors; c += blockDim.x) sb.colorCount[c] = 0;
     gridBarrier(sb.bar, &a.st->err);
+    // each dynamic body's manifolds
+    for (uint32_t m = gtid; m < M; m += gstride) {
+        const uint32_t d = sb.dyn[m];
+        for (int e = 0; e < 2; ++e) {
+            if (!(d & (1u << e))) continue;
+            const uint32_t b = e ? a.mv.bodyB[m] : a.mv.bodyA[m];
+            const uint32_t slot = atomicAdd(&incCount[b], 1u);
+            if (slot < kIslandMax) inc[(size_t)b * kIslandMax + slot] = m;
+            else sb.counters[1] = 1u;
+        }
+    }
+    gridBarrier(sb.bar, &a.st->err);
+    if (__ldcg(&sb.counters[1]) == 0u) {
+        uint32_t pass = 0;
+        bool pending = true;
+        for (; pending && pass < kSpinLimit; ++pass) {
+            pending = false;
+            for (uint32_t m = gtid; m < M; m += gstride) {
+                if (sb.color[m] != kUncolored) continue;
+                const uint32_t p = colorPriority(m), d = sb.dyn[m];
+                unsigned long long u0 = 0, u1 = 0;
+                bool ready = true;
+                for (int e = 0; e < 2 && ready; ++e) {
+                    if (!(d & (1u << e))) continue;
+                    const uint32_t b = e ? a.mv.bodyB[m] : a.mv.bodyA[m];
+                    const uint32_t n = min(__ldcg(&incCount[b]), kIslandMax);
+                    const uint32_t *list = inc + (size_t)b * kIslandMax;
+                    uint32_t cs[kIslandMax];
+#pragma unroll
+                    for (uint32_t i = 0; i < kIslandMax; ++i) {
+                        cs[i] = 0xFFFFFFFEu;  // not a higher-priority neighbour
+                        if (i < n) {
+                            const uint32_t o = __ldcg(&list[i]);
+                            if (o != m && colorPriority(o) > p) cs[i] = ldvol(&sb.color[o]);
+                        }
+                    }
+#pragma unroll
+                    for (uint32_t i = 0; i < kIslandMax; ++i) {
+                        if (cs[i] == 0xFFFFFFFEu) continue;
+                        if (cs[i] == kUncolored) ready = false;
+                        else if (cs[i] < 64) u0 |= 1ull << cs[i];
+                        else u1 |= 1ull << (cs[i] - 64);
+                    }
+                }
+                if (!ready) {
+                    pending = true;
+                    continue;
+                }
+                uint32_t c;
+                if (~u0) c = __ffsll((long long)~u0) - 1;
+                else if (~u1) c = 64 + __ffsll((long long)~u1) - 1;
+                else {
+                    atomicOr(&a.st->err, kErrColors);
+                    c = kMaxColors - 1;
+                }
+                *(volatile uint32_t *)&sb.color[m] = c;
+                aggregatedAppendKeyed(sb.colorCount, c);
+                aggregatedMax32(&a.st->colors, c + 1);
+            }
+        }
+        if (pending) atomicOr(&a.st->err, kErrTimeout);
+        aggregatedMax32(&a.st->colorRounds, pass);
+        return;
+    }
     const unsigned long long epoch0 = __ldcg(sb.epoch);
     uint32_t round = 0;
     for (; round < kMaxRounds; ++round) {

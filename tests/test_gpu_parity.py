@@ -492,12 +492,13 @@ def test_reference_benchmark_scene_matches_oracle(gpu):
     assert g.stats()["contact_count"] > 1000
 
 
-def island_mix_scene(patch: int, patches: int):
+def island_mix_scene(patch: int, patches: int, plate: bool = False):
     """A static floor with islands of the sizes the island sweeps tell apart:
     `patches` patches of patch x patch touching unit boxes (a 30 x 30 patch is
     one island of thousands of manifolds, a 10 x 10 one of 442), rows of 20
     and of 12 touching spheres (islands of 39 and 23 manifolds) and two-high
-    box stacks (islands of two)."""
+    box stacks (islands of two); with `plate`, a dynamic 8 x 0.5 x 8 plate
+    carrying 64 spheres (a body with 65 manifolds)."""
     f = np.float32
     pos, shape, dims = [[0.0, -0.5, 0.0]], [1], [[64.0, 1.0, 64.0]]
     for p in range(patches):
@@ -518,6 +519,15 @@ def island_mix_scene(patch: int, patches: int):
             pos.append([f(-31.0) + f(2.0) * f(i), f(0.5) + f(1.0) * f(level), 20.0])
             shape.append(1)
             dims.append([1.0, 1.0, 1.0])
+    if plate:
+        pos.append([20.0, 0.249, 14.0])
+        shape.append(1)
+        dims.append([8.0, 0.5, 8.0])
+        for i in range(8):
+            for k in range(8):
+                pos.append([f(16.5) + f(i), 0.998, f(10.5) + f(k)])
+                shape.append(0)
+                dims.append([0.5, 0.0, 0.0])
     n = len(pos)
     static = np.zeros(n, np.uint8)
     static[0] = 1
@@ -527,12 +537,14 @@ def island_mix_scene(patch: int, patches: int):
                         hull_id=np.full(n, -1, np.int32), mass=np.zeros(n, f), inv_inertia=np.zeros((n, 3), f))
 
 
-@pytest.mark.parametrize("patch,patches", [(30, 1), (10, 12)])
-def test_island_sizes_match_oracle(gpu, patch, patches):
+@pytest.mark.parametrize("patch,patches,plate", [(30, 1, False), (10, 12, False), (10, 12, True)])
+def test_island_sizes_match_oracle(gpu, patch, patches, plate):
     """Islands of two manifolds to thousands against the oracle in colour
     order: one island of thousands (every island in grid-wide sweeps), or
-    twelve of 442 with smaller ones (per-warp and per-thread sweeps)."""
-    sc = island_mix_scene(patch, patches)
+    twelve of 442 with smaller ones (per-warp and per-thread sweeps); a body
+    with more manifolds than the colouring's per-body lists hold (colouring
+    in rounds)."""
+    sc = island_mix_scene(patch, patches, plate)
     g = gpu.GpuWorld(algo=0, iterations=8)
     o = cpu.OracleWorld(algo=0, iterations=8, order_mode=1)
     g.load_scene(sc)
