@@ -33,6 +33,11 @@ __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
     // per-body manifold lists: counts in islOff, lists in islandList (both
     // free until the island sweeps)
     uint32_t *incCount = sb.islOff, *inc = sb.islandList;
+    if (M == 0) {  // nothing to colour (every block sees the same count)
+        if (blockIdx.x == 0)
+            for (int c = threadIdx.x; c < kMaxColors; c += blockDim.x) sb.colorCount[c] = 0;
+        return;
+    }
     for (uint32_t m = gtid; m < M; m += gstride) {
         uint32_t ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
         bool da = ba < w.nb && w.bgen[ba] == a.mv.genA[m] && bodyMoves(w.bflags[ba]);
