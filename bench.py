@@ -341,6 +341,15 @@ def run_gpu(args, rank, world_size, local_rank):
     print(json.dumps(line), flush=True)
 
 
+# Config 1: 1,000 spheres dropped on a floor, SAP, 10 iterations, 300 steps.
+SPHERES_BODIES = 1000
+SPHERES_STEPS = 300
+# Config 3: 256 box pyramids (16 x 16, 210 boxes each) + 20,000 hulls, 20
+# iterations with warm start, 1,000 steps.
+STACK_PYRAMIDS = 16
+STACK_ITERATIONS = 20
+STACK_STEPS = 1000
+
 BATCH_WORLDS = 4096
 BATCH_MIN, BATCH_MAX = 16, 2048
 
@@ -727,6 +736,67 @@ def run_reference_field(args, local_rank, flush):
     return out
 
 
+PROFILE_WORKLOADS = ("mixed100k", "stacks", "spheres1000", "field", "stacking_convex")
+
+
+def run_workload(args):
+    """Steps one named workload on the GPU (no timing) and prints its step
+    counters as JSON; the profiles under profiles/ are taken on these runs.
+    `mixed100k` is the benchmark world; `stacks` the reference's settled-box
+    profile scene (benchmarks/cpu_profile.cpp:20-41) repeated --tiles X Z times;
+    `spheres1000` 1,000 spheres dropped on a floor (SAP, 10 iterations, dt 1/60);
+    `field` the reference's own benchmark scene (benchmarks/bench_scenes.cpp:11-63,
+    SAP, 8 iterations, dt 1/120) with --bodies bodies; `stacking_convex` the 256
+    box pyramids plus 20,000 hulls (20 iterations, dt 1/60), or --pyramids per side.
+    `launches` (engine kernels over all steps) and `last_step_launches` let a
+    profiler skip to the last steps of the run."""
+    from phys_gb300 import engine, scenes
+
+    algo = {"sap": engine.SAP, "grid": engine.GRID, "tree": engine.TREE}
+    name = args.workload
+    if name == "mixed100k":
+        sc = workload_scene()
+        bp = args.broadphase or "grid"
+        w = engine.GpuWorld(device=0, algo=algo[bp], iterations=ITERATIONS,
+                            cell_size=cell_size(sc) if bp == "grid" else 0.0)
+        dt = DT
+    elif name == "field":
+        sc = scenes.mixed_field(args.bodies, SEED)
+        bp = args.broadphase or "sap"
+        w = engine.GpuWorld(device=0, algo=algo[bp], iterations=SLEEP_ITERATIONS)
+        dt = SLEEP_DT
+    elif name == "spheres1000":
+        sc = scenes.generate(scenes.SPHERES_ON_FLOOR, SPHERES_BODIES, SEED)
+        bp = args.broadphase or "sap"
+        w = engine.GpuWorld(device=0, algo=algo[bp], iterations=ITERATIONS)
+        dt = DT
+    elif name == "stacking_convex":
+        sc = scenes.generate(scenes.PYRAMIDS, args.pyramids, SEED)
+        bp = args.broadphase or "sap"
+        w = engine.GpuWorld(device=0, algo=algo[bp], iterations=STACK_ITERATIONS)
+        dt = DT
+    else:
+        sc = scenes.box_stacks(*args.tiles)
+        bp = args.broadphase or "sap"
+        w = engine.GpuWorld(device=0, algo=algo[bp], iterations=SLEEP_ITERATIONS)
+        dt = SLEEP_DT
+    w.set_sleeping_enabled(args.sleeping)
+    w.load_scene(sc)
+    launches = 0
+    for _ in range(args.profile_steps):
+        w.step(dt)
+        launches += int(w.stats()["kernel_launches"])
+    st = w.stats()
+    out = {"workload": name, "broadphase": bp, "bodies": sc.count, "steps": args.profile_steps,
+           "launches": launches, "last_step_launches": int(st["kernel_launches"])}
+    for f in ("candidate_pairs", "contact_count", "contact_points", "solved_contact_count", "awake_body_count",
+              "sleeping_body_count", "total_ms", "integrate_ms", "broadphase_ms", "narrowphase_ms", "solver_ms",
+              "pose_ms"):
+        out[f] = st[f].item()
+    w.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -742,7 +812,18 @@ def main():
     ap.add_argument("--no-sleeping", action="store_true", help="skip the sleeping-island measurement")
     ap.add_argument("--field-steps", type=int, default=1200, help="timed steps of the reference-scene measurement")
     ap.add_argument("--no-field", action="store_true", help="skip the reference's own benchmark scene")
+    ap.add_argument("--workload", choices=PROFILE_WORKLOADS, default=None,
+                    help="step one named workload untimed and print its counters (profiling runs)")
+    ap.add_argument("--profile-steps", type=int, default=8, help="steps of the --workload run")
+    ap.add_argument("--bodies", type=int, default=10000, help="bodies of the --workload field scene")
+    ap.add_argument("--pyramids", type=int, default=16, help="pyramids per side of --workload stacking_convex")
+    ap.add_argument("--broadphase", choices=("grid", "sap", "tree"), default=None, help="--workload broadphase")
+    ap.add_argument("--tiles", type=int, nargs=2, default=(1, 1), help="--workload stacks: copies along x and z")
+    ap.add_argument("--sleeping", action="store_true", help="--workload: sleeping islands enabled")
     args = ap.parse_args()
+    if args.workload:
+        run_workload(args)
+        return
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
 

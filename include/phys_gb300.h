@@ -397,7 +397,14 @@ pe_status pe_rollout_timings(pe_rollout *rollout, double *forward_ms, double *ba
    code on that GPU if needed); make that first call before any stream capture.
    All calls share the one array: calls whose kernels may overlap on the GPU
    (different streams, or different host threads) race and corrupt each other's
-   results, so serialise them, e.g. on one stream. */
+   results, so serialise them, e.g. on one stream.
+   Bounds must be finite with min <= max on every axis, the contract of the
+   reference's BroadPhase::findCandidatePairs (include/phys/collision/
+   broadphase.hpp:47-51); a NaN bound leaves the pair set unspecified.
+   The call switches to `device` to enqueue its kernel and puts the caller's
+   current device back before it returns (on errors too).  The array's device
+   address is looked up once per device and kept: do not call this on a device
+   after cudaDeviceReset in the same process. */
 #define PE_NOALLOC_MAX_BOXES 8192u
 #define PE_NOALLOC_MAX_PAIRS 32768u
 pe_status pe_broadphase_find_pairs_noalloc(int device, const float *d_mins, const float *d_maxs, uint32_t n,

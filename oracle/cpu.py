@@ -10,6 +10,7 @@ can drive every engine from the same records.
 from __future__ import annotations
 
 import ctypes
+import os
 import pathlib
 import subprocess
 
@@ -18,7 +19,23 @@ import numpy as np
 HERE = pathlib.Path(__file__).resolve().parent
 ORACLE_SO = HERE / "_build" / "libpe_oracle.so"
 REF_SO = HERE / "_ref" / "libref_harness.so"
-REFERENCE_SRC = pathlib.Path("/root/reference")
+
+
+def _reference_src() -> pathlib.Path:
+    """The reference checkout the `ref` target compiles: PE_REFERENCE_SRC, else
+    the location oracle/Makefile names (the build recipe owns that default)."""
+    env = os.environ.get("PE_REFERENCE_SRC")
+    if env:
+        return pathlib.Path(env)
+    try:
+        out = subprocess.run(["make", "-s", "-C", str(HERE), "print-ref"], check=True, capture_output=True,
+                             text=True).stdout.strip()
+    except (OSError, subprocess.CalledProcessError):
+        out = ""
+    return pathlib.Path(out) if out else HERE / "_no_reference"
+
+
+REFERENCE_SRC = _reference_src()
 
 MANIFOLD_DTYPE = np.dtype([
     ("body_a_index", "<u4"), ("body_a_generation", "<u4"),

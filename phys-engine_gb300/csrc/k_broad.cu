@@ -751,7 +751,8 @@ void launchGridBodyPairs(const BroadInput &in, const BroadBuffers &bb, PairBuffe
     uint32_t tiles = (in.maxN + kBodyPairThreads - 1) / kBodyPairThreads;
     if (tiles == 0) tiles = 1;
     if (!stateCleared) PE_CHECK(cudaMemsetAsync(ws.scanState, 0, sizeof(unsigned long long) * (tiles + 1), s));
-    const uint32_t grid = tiles < 152u * 8u ? tiles : 152u * 8u;
+    const uint32_t maxGrid = 8u * (uint32_t)smCount();
+    const uint32_t grid = tiles < maxGrid ? tiles : maxGrid;
     if (bb.hashed) {
         k_hgrid_pairs<<<grid, kBodyPairThreads, 0, s>>>(in, bb.firstCell, bb.inGrid, bb.overflow, bb.bucketHead,
                                                          bb.logBuckets, bb.entryCap, bb.entryKeys, bb.entryVals,
@@ -808,7 +809,8 @@ __global__ void k_pairs_scatter(const uint32_t *d_raw, uint32_t cap, uint32_t bi
     }
 }
 
-static inline int gridFor(uint32_t n, int threads = 256, int maxBlocks = 152 * 8) {
+static inline int gridFor(uint32_t n, int threads = 256, int maxBlocks = 0) {
+    if (maxBlocks <= 0) maxBlocks = 8 * smCount();
     uint32_t b = (n + threads - 1) / threads;
     if (b < 1) b = 1;
     return (int)(b < (uint32_t)maxBlocks ? b : (uint32_t)maxBlocks);
@@ -857,7 +859,7 @@ void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, Broad
     k_sap_window<<<gridFor(in.maxN), 256, 0, s>>>(in.d_n, bb.sMinX, bb.sMaxX, bb.len, st);
     PE_LAUNCHED();
     launchScanExclusive(bb.len, bb.off, in.d_n, in.maxN, &st->windowWork, ws, err, s);
-    k_sap_emit<<<152 * 8, 256, 0, s>>>(in.d_n, bb.off, bb.len, bb.sYZ, bb.sIdx, pb.keys, pb.cap, pb.bits, st);
+    k_sap_emit<<<8 * smCount(), 256, 0, s>>>(in.d_n, bb.off, bb.len, bb.sYZ, bb.sIdx, pb.keys, pb.cap, pb.bits, st);
     PE_LAUNCHED();
 }
 
@@ -901,7 +903,7 @@ void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBu
                                                            bb.entryVals, bb.firstCell, in, pb.keys, pb.cap, pb.bits,
                                                            st);
     PE_LAUNCHED();
-    k_grid_overflow_pairs<<<152 * 4, 256, 0, s>>>(in, bb.overflow, bb.inGrid, pb.keys, pb.cap, pb.bits, st);
+    k_grid_overflow_pairs<<<4 * smCount(), 256, 0, s>>>(in, bb.overflow, bb.inGrid, pb.keys, pb.cap, pb.bits, st);
     PE_LAUNCHED();
 }
 

@@ -34,7 +34,8 @@ constexpr int kLbvhStack = 64;
 
 inline int lbvhGrid(uint32_t n) {
     uint32_t b = (n + kLbvhThreads - 1) / kLbvhThreads;
-    return (int)(b ? (b < 152u * 8u ? b : 152u * 8u) : 1u);
+    const uint32_t maxGrid = 8u * (uint32_t)smCount();
+    return (int)(b ? (b < maxGrid ? b : maxGrid) : 1u);
 }
 
 __device__ __forceinline__ float orderedFloatDecode(uint32_t k) {

@@ -73,7 +73,8 @@ void launchNarrowphase(const WorldView &w, const PairBuffers &pb, const Manifold
     if (tiles == 0) tiles = 1;
     if (!state) state = ws.scanState;
     if (!stateCleared) PE_CHECK(cudaMemsetAsync(state, 0, sizeof(unsigned long long) * (tiles + 1), s));
-    const uint32_t grid = tiles < 152u * 8u ? tiles : 152u * 8u;
+    const uint32_t maxGrid = 8u * (uint32_t)smCount();
+    const uint32_t grid = tiles < maxGrid ? tiles : maxGrid;
     k_narrowphase<<<grid, kNarrowThreads, 0, s>>>(w, pb.a, pb.b, &st->pairs, mv, mcap, st, state,
                                                    (uint32_t *)(state + tiles));
     PE_LAUNCHED();

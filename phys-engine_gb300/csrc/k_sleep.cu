@@ -296,8 +296,8 @@ void launchSleepWake(const WorldView &w, const ManifoldView &mv, uint32_t Mhost,
 void launchSleepContacts(const WorldView &w, const ManifoldView &mv, DevStats *st, uint32_t mcap, uint32_t *bflags,
                          cudaStream_t s) {
     if (!w.nb) return;
-    k_sleep_contacts<<<gridFor(mcap < 4u * 152u * kSleepThreads ? mcap : 4u * 152u * kSleepThreads), kSleepThreads, 0,
-                       s>>>(w, mv, &st->manifolds, 0u, mcap, w.sleepOut, &st->err);
+    const uint32_t span = 4u * (uint32_t)smCount() * kSleepThreads;
+    k_sleep_contacts<<<gridFor(mcap < span ? mcap : span), kSleepThreads, 0, s>>>(w, mv, &st->manifolds, 0u, mcap, w.sleepOut, &st->err);
     PE_LAUNCHED();
     k_sleep_islands<<<gridFor(w.nb), kSleepThreads, 0, s>>>(w, w.sleepOut);
     PE_LAUNCHED();
@@ -315,7 +315,8 @@ void launchCacheCarry(const WorldView &w, const CacheView &oldCache, const uint3
                       const uint32_t *tmpCount, const CacheView &newCache, uint32_t *newCount, uint32_t cap,
                       uint32_t *carry, uint32_t *carryPos, uint32_t *carryTotal, DevStats *st, Scratch &ws,
                       cudaStream_t s) {
-    const uint32_t g = gridFor(cap < 4u * 152u * kSleepThreads ? cap : 4u * 152u * kSleepThreads);
+    const uint32_t span = 4u * (uint32_t)smCount() * kSleepThreads;
+    const uint32_t g = gridFor(cap < span ? cap : span);
     k_cache_carry_flags<<<g, kSleepThreads, 0, s>>>(w, oldCache, oldCount, cap, carry);
     PE_LAUNCHED();
     launchScanExclusive(carry, carryPos, oldCount, cap, carryTotal, ws, &st->err, s);

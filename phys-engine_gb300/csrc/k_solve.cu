@@ -291,7 +291,8 @@ k_solve_block(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount, 
                stageSlots ? &vs : nullptr, true);
 }
 
-static int gridFor(uint32_t n, int threads = 256, int maxBlocks = 152 * 8) {
+static int gridFor(uint32_t n, int threads = 256, int maxBlocks = 0) {
+    if (maxBlocks <= 0) maxBlocks = 8 * smCount();
     uint32_t b = (n + threads - 1) / threads;
     if (b < 1) b = 1;
     return (int)(b < (uint32_t)maxBlocks ? b : (uint32_t)maxBlocks);

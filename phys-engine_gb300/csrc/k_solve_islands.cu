@@ -54,7 +54,8 @@ static_assert(kIslColorFill + kMaxColors == kIslCounterWords, "island counter la
 
 inline uint32_t islGrid(uint32_t n) {
     const uint32_t b = (n + kIslThreads - 1) / kIslThreads;
-    return b ? (b < 152u * 16u ? b : 152u * 16u) : 1u;
+    const uint32_t maxGrid = 16u * (uint32_t)smCount();
+    return b ? (b < maxGrid ? b : maxGrid) : 1u;
 }
 
 // Root of i's island, halving the path on the way (par[i] = grandparent).
@@ -334,7 +335,7 @@ void launchSolveIslands(const SolveArgs &a, int coopBlocks, Scratch &ws, cudaStr
     launchScanExclusive(a.sb.islPar + a.w.nb, a.sb.islOff, nullptr, a.w.nb, &a.sb.islCounters[3], ws, &a.st->err, s);
     k_isl_fill<<<islGrid(mcap), kIslThreads, 0, s>>>(a);
     PE_LAUNCHED();
-    k_isl_solve<<<152 * 4, kIslThreads, 0, s>>>(a);
+    k_isl_solve<<<4 * smCount(), kIslThreads, 0, s>>>(a);
     PE_LAUNCHED();
     SolveArgs args = a;
     void *params[] = {&args};

@@ -137,7 +137,10 @@ unsigned char *g_scratchPtr[kMaxDevices] = {};
 
 // Device address of g_sapScratch on `device`, looked up on the first call for
 // that device with the device current.  The lookup makes the runtime load this
-// library's device code on that GPU if it has not yet done so.
+// library's device code on that GPU if it has not yet done so.  The address is
+// kept for the life of the process: it stays valid as long as the device's
+// primary context does, so the entry point must not be used on a device after
+// cudaDeviceReset (the module would be reloaded and the array could move).
 unsigned char *scratchOn(int device) {
     std::lock_guard<std::mutex> lock(g_setupMutex);
     if (!g_scratchPtr[device]) {
@@ -159,6 +162,15 @@ void findPairsNoAlloc(int device, const float *mins, const float *maxs, uint32_t
         throw std::invalid_argument("pe_broadphase_find_pairs_noalloc: " + std::to_string(n) +
                                     " boxes exceed its limit of " + std::to_string(kMaxBoxes) +
                                     " (PE_NOALLOC_MAX_BOXES); use pe_broadphase_find_pairs");
+    // The caller's current device is put back on every return, the error
+    // paths included: a host engine that drives several GPUs from one thread
+    // keeps its own notion of the current device.
+    int previous = 0;
+    PE_CHECK(cudaGetDevice(&previous));
+    struct RestoreDevice {
+        int device;
+        ~RestoreDevice() { cudaSetDevice(device); }
+    } restore{previous};
     PE_CHECK(cudaSetDevice(device));
     unsigned char *scratch = scratchOn(device);
     k_sap_noalloc<<<1, kThreads, 0, s>>>(mins, maxs, n, scratch, pairs, capacity, result);

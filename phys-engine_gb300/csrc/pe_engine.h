@@ -23,6 +23,10 @@ struct CudaError : std::runtime_error {
 // Every kernel launch of the engine is followed by PE_LAUNCHED(): it checks the
 // launch and counts it (the count is reported per step).
 extern unsigned long long g_kernelLaunches;
+
+// Streaming multiprocessors of the current device (queried once per device and
+// cached); launch sizes of the persistent and grid-stride kernels scale with it.
+int smCount();
 #define PE_LAUNCHED()                                                                               \
     do {                                                                                            \
         PE_CHECK(cudaGetLastError());                                                               \

@@ -6,6 +6,7 @@
 // ids are taken in launch order by running blocks, so the decoupled look-back
 // of a tile only ever waits on tiles that are being processed.
 #include <algorithm>
+#include <atomic>
 
 #include "pe_engine.h"
 #include "pe_prims.cuh"
@@ -14,9 +15,25 @@ namespace pe {
 
 unsigned long long g_kernelLaunches = 0;
 
+int smCount() {
+    constexpr int kMaxDevices = 64;
+    static std::atomic<int> cached[kMaxDevices] = {};
+    int dev = 0;
+    PE_CHECK(cudaGetDevice(&dev));
+    const bool cacheable = dev >= 0 && dev < kMaxDevices;
+    int n = cacheable ? cached[dev].load(std::memory_order_relaxed) : 0;
+    if (n == 0) {
+        PE_CHECK(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+        if (n < 1) n = 1;
+        if (cacheable) cached[dev].store(n, std::memory_order_relaxed);
+    }
+    return n;
+}
+
 namespace {
-constexpr uint32_t kPersistentBlocks = 152 * 4;
-inline uint32_t persistentGrid(uint32_t tiles) { return std::max<uint32_t>(1, std::min(tiles, kPersistentBlocks)); }
+inline uint32_t persistentGrid(uint32_t tiles) {
+    return std::max<uint32_t>(1, std::min<uint32_t>(tiles, 4u * (uint32_t)smCount()));
+}
 __device__ __forceinline__ uint32_t liveCount(const uint32_t *d_n, uint32_t cap) {
     if (!d_n) return cap;
     const uint32_t n = *d_n;
@@ -245,7 +262,7 @@ void launchRadixSort(K *keys, K *keys_tmp, uint32_t *vals, uint32_t *vals_tmp, c
     uint32_t *sel = ws.sortHist + 256 * 8;
     uint32_t *counters = ws.sortHist + 256 * 8 + 16;
     PE_CHECK(cudaMemsetAsync(ws.sortHist, 0, sizeof(uint32_t) * (256 * 8 + 16), s));
-    const uint32_t hb = std::max<uint32_t>(1, std::min<uint32_t>((max_n + 255) / 256, 4 * 152));
+    const uint32_t hb = std::max<uint32_t>(1, std::min<uint32_t>((max_n + 255) / 256, 4u * (uint32_t)smCount()));
     k_radix_hist<K><<<hb, 256, 0, s>>>(keys, d_n, max_n, bit_begin, passes, ws.sortHist, ws.sortState, passStride,
                                        counters);
     PE_LAUNCHED();

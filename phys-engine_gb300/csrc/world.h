@@ -192,7 +192,7 @@ class World {
     void wakeContacts(uint32_t index, uint32_t generation);
 
     int device_;
-    int smCount_ = 152;
+    int smCount_ = 0;
     cudaStream_t stream_ = nullptr;
     bool hostDirty_ = true;
     bool deviceNewer_ = false;

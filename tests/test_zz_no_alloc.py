@@ -57,11 +57,19 @@ def noalloc_pairs(engine, mins, maxs, capacity, out=None):
 def test_noalloc_matches_find_pairs_on_two_calls_in_a_row(gpu):
     # Call 1: a dense cloud (many pairs); call 2: a smaller, sparser one run on
     # the scratch call 1 left behind, into the same output buffer.
+    from oracle import cpu
+
     a_min, a_max = random_boxes(11, 6000, 20.0, 0.2, 1.2)
     b_min, b_max = random_boxes(12, 1500, 30.0, 0.1, 0.8)
     want_a, _ = gpu.broadphase(a_min, a_max, gpu.SAP)
     want_b, _ = gpu.broadphase(b_min, b_max, gpu.SAP)
     assert 1000 < len(want_a) <= MAX_PAIRS and 0 < len(want_b) < len(want_a)
+    # The oracle's sweep (the reference's algorithm on the CPU) pins both
+    # expectations independently of the device-wide GPU path.
+    oracle_a, _ = cpu.broadphase("oracle", a_min, a_max, 0)
+    oracle_b, _ = cpu.broadphase("oracle", b_min, b_max, 0)
+    np.testing.assert_array_equal(want_a, oracle_a)
+    np.testing.assert_array_equal(want_b, oracle_b)
 
     got_a, count_a, status_a, out = noalloc_pairs(gpu, a_min, a_max, MAX_PAIRS)
     assert (count_a, status_a) == (len(want_a), 0)
@@ -112,3 +120,22 @@ def test_noalloc_limits(gpu):
     maxs = np.ones((300, 3), np.float32)  # every box overlaps every other: 44,850 pairs
     got, count, status, _ = noalloc_pairs(gpu, mins, maxs, 16)
     assert (count, status) == (300 * 299 // 2, 2)
+
+
+def test_noalloc_keeps_the_callers_current_device(gpu):
+    # The call selects its device to enqueue the kernel and puts the caller's
+    # current device back, on success and on a rejected call alike.
+    import torch
+
+    lib = gpu.lib()
+    torch.cuda.set_device(0)
+    before = torch.cuda.current_device()
+    mins, maxs = random_boxes(21, 200, 5.0, 0.2, 0.6)
+    noalloc_pairs(gpu, mins, maxs, MAX_PAIRS)
+    assert torch.cuda.current_device() == before
+    words = torch.zeros(4, dtype=torch.int32, device="cuda:0")
+    ptr = ctypes.c_void_p
+    rc = lib.pe_broadphase_find_pairs_noalloc(0, ptr(words.data_ptr()), ptr(words.data_ptr()), MAX_BOXES + 1,
+                                              ptr(words.data_ptr()), 1, ptr(words.data_ptr()), None)
+    assert rc != 0
+    assert torch.cuda.current_device() == before
