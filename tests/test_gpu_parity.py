@@ -619,3 +619,108 @@ def test_step_io_equals_separate_calls(gpu):
         assert_bit_equal(pa, pb, f"step {s} positions")
         assert_bit_equal(qa, qb, f"step {s} rotations")
     compare_worlds(a, b, "after step_io")
+
+
+# ------------------------------------------- benchmarked configurations ---
+def _bench_cell(sc):
+    """The benchmark's grid cell: 2 x the largest collider extent (sphere
+    radius, box half diagonal)."""
+    sph = sc.shape == 0
+    ext = np.where(sph, sc.dims[:, 0], np.linalg.norm(sc.dims * 0.5, axis=1))
+    return float(2.0 * ext.max())
+
+
+def _run_pair(gw, ow, steps, dt, check, statics=None):
+    for s in range(steps):
+        gw.step(dt)
+        ow.step(dt)
+        if check(s):
+            compare_worlds(gw, ow, f"step {s}")
+            order, colors = gw.solve_order()
+            oorder, ocolors = ow.solve_order()
+            assert np.array_equal(order, oorder) and np.array_equal(colors, ocolors), f"step {s} colour order"
+            if statics is not None:
+                assert colors_valid(gw.contacts(), colors, statics)
+            st, ost = gw.stats(), ow.stats()
+            for f in ("candidate_pairs", "contact_count", "prepared_points", "warm_start_matches", "np_candidates",
+                      "np_contacts", "color_count", "x_window_comparisons", "grid_comparisons"):
+                assert np.array_equal(st[f], ost[f]), f"step {s} {f}: {st[f]} != {ost[f]}"
+
+
+def test_mixed_100k_bench_config_matches_oracle(gpu):
+    """The benchmark world itself: 100,000 spheres and boxes, the bench's grid
+    cell (2 x the largest extent), 10 iterations, dt 1/60, against the oracle
+    in colour order: every one of the first 5 steps, then every 10th step up
+    to step 60 (pairs, manifolds with feature ids, poses, colour order,
+    counters)."""
+    import os
+
+    sc = scenes.generate(scenes.MIXED_VOLUME, 100_000, 42)
+    cell = _bench_cell(sc)
+    assert abs(cell - 2.055892) < 1e-5
+    gw = gpu.GpuWorld(algo=1, cell_size=cell, iterations=10, order=gpu.ORDER_COLOR)
+    ow = cpu.OracleWorld(algo=1, cell_size=cell, iterations=10, order_mode=1, threads=os.cpu_count() or 1)
+    gw.load_scene(sc)
+    ow.load_scene(sc)
+    _run_pair(gw, ow, 60, 1 / 60, lambda s: s < 5 or s % 10 == 9, sc.is_static.astype(bool))
+    assert gw.stats()["contact_count"] > 200
+
+
+def test_spheres_1000_all_300_steps_match_oracle(gpu):
+    """Config 1 in full: 1,000 spheres dropped on a static floor, SAP, 10
+    iterations, 300 steps at dt 1/60, every step against the oracle."""
+    sc = scenes.generate(scenes.SPHERES_ON_FLOOR, 1000, 42)
+    gw = gpu.GpuWorld(algo=0, iterations=10, order=gpu.ORDER_COLOR)
+    ow = cpu.OracleWorld(algo=0, iterations=10, order_mode=1)
+    gw.load_scene(sc)
+    ow.load_scene(sc)
+    _run_pair(gw, ow, 300, 1 / 60, lambda s: True, sc.is_static.astype(bool))
+    assert gw.stats()["contact_count"] > 500
+
+
+def _lowered_pyramids(per_side, drop):
+    sc = scenes.generate(scenes.PYRAMIDS, per_side, 42)
+    sc.pos[sc.shape == 2, 1] -= np.float32(drop)
+    return sc
+
+
+def test_stacking_convex_16_pyramids_match_oracle(gpu):
+    """Config 3 at 16 pyramids (3,360 boxes) with the proportional 1,250
+    hulls, lowered 28 m so that they reach the pyramids and the floor within
+    the run (GJK/EPA contacts, deep first contacts included), 20 iterations
+    with warm start, 40 steps against the oracle in colour order."""
+    import os
+
+    sc = _lowered_pyramids(4, 28.0)
+    assert int((sc.shape == 2).sum()) == 1250
+    gw = gpu.GpuWorld(algo=0, iterations=20, order=gpu.ORDER_COLOR)
+    ow = cpu.OracleWorld(algo=0, iterations=20, order_mode=1, threads=os.cpu_count() or 1)
+    gw.load_scene(sc)
+    ow.load_scene(sc)
+    hull_contacts = 0
+    for s in range(40):
+        gw.step(1 / 60)
+        ow.step(1 / 60)
+        hull_contacts += int(gw.stats()["np_contacts"][3])
+        if s < 3 or s % 8 == 7:
+            compare_worlds(gw, ow, f"step {s}")
+            assert np.array_equal(gw.solve_order()[1], ow.solve_order()[1]), f"step {s} colours"
+    assert hull_contacts > 100
+    for f in ("contact_count", "prepared_points", "warm_start_matches", "np_contacts", "color_count"):
+        assert np.array_equal(gw.stats()[f], ow.stats()[f]), f
+
+
+def test_stacking_convex_full_config_matches_oracle(gpu):
+    """Config 3 at its full size: 256 pyramids (53,760 boxes) and 20,000
+    hulls, 20 iterations, the first 3 steps against the oracle in colour
+    order (about 130,000 manifolds a step)."""
+    import os
+
+    sc = scenes.generate(scenes.PYRAMIDS, 16, 42)
+    assert int((sc.shape == 1).sum() - sc.is_static.sum()) == 53_760 and int((sc.shape == 2).sum()) == 20_000
+    gw = gpu.GpuWorld(algo=0, iterations=20, order=gpu.ORDER_COLOR)
+    ow = cpu.OracleWorld(algo=0, iterations=20, order_mode=1, threads=os.cpu_count() or 1)
+    gw.load_scene(sc)
+    ow.load_scene(sc)
+    _run_pair(gw, ow, 3, 1 / 60, lambda s: s == 0 or s == 2)
+    assert gw.stats()["contact_count"] > 100_000
