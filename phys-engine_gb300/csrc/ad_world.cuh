@@ -31,7 +31,7 @@
 namespace pe {
 namespace ad {
 
-constexpr uint32_t kAdMaxColors = 128;
+constexpr uint32_t kAdMaxColors = 128;  // colours per window of the per-body colour masks
 constexpr int kDualChunk = 4;
 constexpr int kDualInputs = 29;  // xA 3, qA 4, xB 3, qB 4, v1A 3, w1A 3, v1B 3, w1B 3, mA, mB, restitution
 constexpr int kTapeScalars = 24; // vA, wA, vB, wB, then 4 x (n, t1, t2)
@@ -163,7 +163,7 @@ template <class S> struct StepScratch {
     uint32_t *color, *order;        // maxManifolds
     unsigned long long *sortKeys;   // maxManifolds
     unsigned long long *bodyUsed;   // 2 per body
-    uint32_t *colorStart;           // kAdMaxColors + 1
+    uint32_t *colorStart;           // maxManifolds + 1 (colours <= manifolds)
     S *pp;                          // kPreparedScalars per (k, p)
     S *pm;                          // kPmScalars per k
     S *lam;                         // 3 per (k, p)
@@ -540,35 +540,50 @@ AD_HD void forwardStep(const WorldParams<S> &W, const StateView<S> &in, const Ca
     T::sortU64(sc.sortKeys, M2);
     T::sync();
     if (tid == 0) {
-        uint32_t colors = 0;
-        for (uint32_t r = 0; r < M; ++r) {
-            const uint32_t m = (uint32_t)sc.sortKeys[r];
-            const uint32_t a = sc.mA[m], b = sc.mB[m];
-            const bool da = !W.isStatic[a], db = !W.isStatic[b];
-            unsigned long long u0 = 0, u1 = 0;
-            if (da) {
-                u0 |= sc.bodyUsed[2 * a];
-                u1 |= sc.bodyUsed[2 * a + 1];
-            }
-            if (db) {
-                u0 |= sc.bodyUsed[2 * b];
-                u1 |= sc.bodyUsed[2 * b + 1];
-            }
-            uint32_t c = kAdMaxColors - 1;
-            bool found = false;
-            for (uint32_t k = 0; k < kAdMaxColors && !found; ++k) {
-                const unsigned long long w = k < 64 ? u0 : u1;
-                if (!((w >> (k & 63)) & 1ull)) {
-                    c = k;
-                    found = true;
+        // Colour windows of kAdMaxColors: a manifold whose higher-priority
+        // neighbours use the whole window waits for the next window, in which
+        // only the waiting manifolds take colours (the engine's rule, so the
+        // same colouring); no colour limit.
+        constexpr uint32_t kWaiting = 0xFFFFFFFFu;
+        for (uint32_t r = 0; r < M; ++r) sc.color[(uint32_t)sc.sortKeys[r]] = kWaiting;
+        uint32_t colors = 0, base = 0, waiting = M;
+        while (waiting) {
+            uint32_t deferred = 0;
+            for (uint32_t r = 0; r < M; ++r) {
+                const uint32_t m = (uint32_t)sc.sortKeys[r];
+                if (sc.color[m] != kWaiting) continue;
+                const uint32_t a = sc.mA[m], b = sc.mB[m];
+                const bool da = !W.isStatic[a], db = !W.isStatic[b];
+                unsigned long long u0 = 0, u1 = 0;
+                if (da) {
+                    u0 |= sc.bodyUsed[2 * a];
+                    u1 |= sc.bodyUsed[2 * a + 1];
                 }
+                if (db) {
+                    u0 |= sc.bodyUsed[2 * b];
+                    u1 |= sc.bodyUsed[2 * b + 1];
+                }
+                uint32_t local = kAdMaxColors;
+                for (uint32_t k = 0; k < kAdMaxColors && local == kAdMaxColors; ++k) {
+                    const unsigned long long w = k < 64 ? u0 : u1;
+                    if (!((w >> (k & 63)) & 1ull)) local = k;
+                }
+                if (local == kAdMaxColors) {
+                    ++deferred;
+                    continue;
+                }
+                const uint32_t c = base + local;
+                sc.color[m] = c;
+                const unsigned long long bit = 1ull << (local & 63);
+                if (da) sc.bodyUsed[2 * a + (local >> 6)] |= bit;
+                if (db) sc.bodyUsed[2 * b + (local >> 6)] |= bit;
+                if (c + 1 > colors) colors = c + 1;
             }
-            if (!found) sc.counts[3] |= kAdErrColors;
-            sc.color[m] = c;
-            const unsigned long long bit = 1ull << (c & 63);
-            if (da) sc.bodyUsed[2 * a + (c >> 6)] |= bit;
-            if (db) sc.bodyUsed[2 * b + (c >> 6)] |= bit;
-            if (c + 1 > colors) colors = c + 1;
+            waiting = deferred;
+            if (waiting) {
+                base += kAdMaxColors;
+                for (uint32_t i = 0; i < 2 * n; ++i) sc.bodyUsed[i] = 0ull;
+            }
         }
         sc.counts[2] = colors;
     }

@@ -213,6 +213,7 @@ void Batch::layout(const std::vector<uint32_t> &pairCap, const std::vector<uint3
     color_.reserve(mb);
     dyn_.reserve(mb);
     order_.reserve(mb);
+    colorStart_.reserve(mb);
     pm_.reserve(mb);
     pmInertia_.reserve(6 * mb);
     pp_.reserve((size_t)kPreparedVec4 * 4 * mb);
@@ -328,6 +329,7 @@ BatchView Batch::view(const BatchBucket &bk, float dt, uint32_t parity) const {
     v.sb.color = color_.ptr;
     v.sb.dyn = dyn_.ptr;
     v.sb.order = order_.ptr;
+    v.sb.colorStart = colorStart_.ptr;
     v.sb.pm = pm_.ptr;
     v.sb.pmInertia = pmInertia_.ptr;
     v.sb.pp = pp_.ptr;
@@ -444,7 +446,8 @@ bool Batch::finishStep() {
     PE_CHECK(cudaMemcpy(h.data(), stats_.ptr, W * sizeof(DevStats), cudaMemcpyDeviceToHost));
     for (uint32_t w = 0; w < W; ++w) {
         if (h[w].err & kErrTimeout) throw std::runtime_error("world " + std::to_string(w) + ": a bounded wait timed out");
-        if (h[w].err & kErrColors) throw std::runtime_error("world " + std::to_string(w) + ": more than 128 solver colours");
+        if (h[w].err & kErrColors)
+            throw std::runtime_error("world " + std::to_string(w) + ": the solver colouring exceeded its round limit");
     }
     if (!(err & (kErrPairCapacity | kErrManifoldCapacity | kErrSmallPath)))
         throw std::runtime_error("batched step failed on the device (error bits " + std::to_string(err) + ")");

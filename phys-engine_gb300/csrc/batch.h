@@ -155,7 +155,7 @@ class Batch {
     DeviceArray<float4> mNormal_, mAnchorA_, mAnchorB_, mImpulse_;
     DeviceArray<float> mRest_;
     DeviceArray<unsigned long long> bodyBest_, bodyUsed_, epoch_;
-    DeviceArray<uint32_t> color_, dyn_, colorCount_, order_;
+    DeviceArray<uint32_t> color_, dyn_, colorCount_, order_, colorStart_;
     DeviceArray<float4> pm_, pmInertia_, pp_, pimp_, pn_;
     DeviceArray<uint2> pbody_;
     DeviceArray<uint32_t> pcount_;

@@ -103,6 +103,7 @@ __device__ __forceinline__ SolverBuffers solverSlice(const BatchView &b, const W
     sb.dyn = b.sb.dyn + mb;
     sb.colorCount = b.colorCount + (size_t)wi * kMaxColors;
     sb.order = b.sb.order + mb;
+    sb.colorStart = b.sb.colorStart + mb;
     sb.pm = b.sb.pm + mb;
     sb.pmInertia = b.sb.pmInertia + 6ull * mb;
     sb.pp = b.sb.pp + (size_t)kPreparedVec4 * 4 * mb;

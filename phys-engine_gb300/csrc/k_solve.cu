@@ -122,57 +122,102 @@ __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
         aggregatedMax32(&a.st->colorRounds, pass);
         return;
     }
+    // Jones-Plassmann rounds in colour windows of kMaxColors (see kDeferred):
+    // counters[0] counts manifolds done in the window (coloured or deferred),
+    // counters[2] the deferred ones.
     const unsigned long long epoch0 = __ldcg(sb.epoch);
-    uint32_t round = 0;
-    for (; round < kMaxRounds; ++round) {
-        const unsigned long long stamp = (epoch0 + round + 1) << 32;
-        for (uint32_t m = gtid; m < M; m += gstride) {
-            if (sb.color[m] != kUncolored) continue;
-            const unsigned long long p = stamp | colorPriority(m);
-            const uint32_t d = sb.dyn[m];
-            if (d & 1u) atomicMax(&sb.bodyBest[a.mv.bodyA[m]], p);
-            if (d & 2u) atomicMax(&sb.bodyBest[a.mv.bodyB[m]], p);
+    uint32_t rounds = 0, base = 0;
+    bool exhausted = false;
+    for (;;) {
+        uint32_t round = 0;
+        for (; round < kMaxRounds; ++round) {
+            const unsigned long long stamp = (epoch0 + rounds + round + 1) << 32;
+            for (uint32_t m = gtid; m < M; m += gstride) {
+                if (sb.color[m] != kUncolored) continue;
+                const unsigned long long p = stamp | colorPriority(m);
+                const uint32_t d = sb.dyn[m];
+                if (d & 1u) atomicMax(&sb.bodyBest[a.mv.bodyA[m]], p);
+                if (d & 2u) atomicMax(&sb.bodyBest[a.mv.bodyB[m]], p);
+            }
+            gridBarrier(sb.bar, &a.st->err);
+            for (uint32_t m = gtid; m < M; m += gstride) {
+                if (sb.color[m] != kUncolored) continue;
+                const unsigned long long p = stamp | colorPriority(m);
+                const uint32_t d = sb.dyn[m];
+                const uint32_t ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
+                if ((d & 1u) && __ldcg(&sb.bodyBest[ba]) != p) continue;
+                if ((d & 2u) && __ldcg(&sb.bodyBest[bb]) != p) continue;
+                unsigned long long u0 = 0, u1 = 0;
+                if (d & 1u) {
+                    u0 |= __ldcg(&sb.bodyUsed[2 * ba]);
+                    u1 |= __ldcg(&sb.bodyUsed[2 * ba + 1]);
+                }
+                if (d & 2u) {
+                    u0 |= __ldcg(&sb.bodyUsed[2 * bb]);
+                    u1 |= __ldcg(&sb.bodyUsed[2 * bb + 1]);
+                }
+                uint32_t local = kDeferred;
+                if (~u0) local = __ffsll((long long)~u0) - 1;
+                else if (~u1) local = 64 + __ffsll((long long)~u1) - 1;
+                if (local == kDeferred) {
+                    sb.color[m] = kDeferred;
+                    aggregatedAppend(&sb.counters[2]);
+                } else {
+                    const uint32_t c = base + local;
+                    sb.color[m] = c;
+                    const unsigned long long bit = 1ull << (local & 63);
+                    const uint32_t word = local >> 6;
+                    if (d & 1u) __stcg(&sb.bodyUsed[2 * ba + word], __ldcg(&sb.bodyUsed[2 * ba + word]) | bit);
+                    if (d & 2u) __stcg(&sb.bodyUsed[2 * bb + word], __ldcg(&sb.bodyUsed[2 * bb + word]) | bit);
+                    if (c < (uint32_t)kMaxColors) aggregatedAppendKeyed(sb.colorCount, c);
+                    aggregatedMax32(&a.st->colors, c + 1);
+                }
+                aggregatedAppend(&sb.counters[0]);
+            }
+            gridBarrier(sb.bar, &a.st->err);
+            if (__ldcg(&sb.counters[0]) >= M) break;
         }
-        gridBarrier(sb.bar, &a.st->err);
+        rounds += round + 1;
+        if (round >= kMaxRounds) {
+            exhausted = true;
+            break;
+        }
+        const uint32_t deferred = __ldcg(&sb.counters[2]);
+        if (deferred == 0) break;
+        // next window: deferred manifolds uncoloured again, their bodies'
+        // masks empty
+        base += kMaxColors;
         for (uint32_t m = gtid; m < M; m += gstride) {
-            if (sb.color[m] != kUncolored) continue;
-            const unsigned long long p = stamp | colorPriority(m);
+            if (sb.color[m] != kDeferred) continue;
+            sb.color[m] = kUncolored;
             const uint32_t d = sb.dyn[m];
-            const uint32_t ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
-            if ((d & 1u) && __ldcg(&sb.bodyBest[ba]) != p) continue;
-            if ((d & 2u) && __ldcg(&sb.bodyBest[bb]) != p) continue;
-            unsigned long long u0 = 0, u1 = 0;
             if (d & 1u) {
-                u0 |= __ldcg(&sb.bodyUsed[2 * ba]);
-                u1 |= __ldcg(&sb.bodyUsed[2 * ba + 1]);
+                __stcg(&sb.bodyUsed[2 * a.mv.bodyA[m]], 0ull);
+                __stcg(&sb.bodyUsed[2 * a.mv.bodyA[m] + 1], 0ull);
             }
             if (d & 2u) {
-                u0 |= __ldcg(&sb.bodyUsed[2 * bb]);
-                u1 |= __ldcg(&sb.bodyUsed[2 * bb + 1]);
+                __stcg(&sb.bodyUsed[2 * a.mv.bodyB[m]], 0ull);
+                __stcg(&sb.bodyUsed[2 * a.mv.bodyB[m] + 1], 0ull);
             }
-            uint32_t c;
-            if (~u0) c = __ffsll((long long)~u0) - 1;
-            else if (~u1) c = 64 + __ffsll((long long)~u1) - 1;
-            else {
-                atomicOr(&a.st->err, kErrColors);
-                c = kMaxColors - 1;
-            }
-            sb.color[m] = c;
-            const unsigned long long bit = 1ull << (c & 63);
-            const uint32_t word = c >> 6;
-            if (d & 1u) __stcg(&sb.bodyUsed[2 * ba + word], __ldcg(&sb.bodyUsed[2 * ba + word]) | bit);
-            if (d & 2u) __stcg(&sb.bodyUsed[2 * bb + word], __ldcg(&sb.bodyUsed[2 * bb + word]) | bit);
-            aggregatedAppendKeyed(sb.colorCount, c);
-            aggregatedMax32(&a.st->colors, c + 1);
-            aggregatedAppend(&sb.counters[0]);
         }
         gridBarrier(sb.bar, &a.st->err);
-        if (__ldcg(&sb.counters[0]) >= M) break;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            sb.counters[0] = M - deferred;
+            sb.counters[2] = 0;
+        }
+        gridBarrier(sb.bar, &a.st->err);
+    }
+    if (exhausted) {
+        // The step fails (kErrColors); colour 0 for what is left keeps every
+        // colour index in range.
+        for (uint32_t m = gtid; m < M; m += gstride)
+            if (sb.color[m] >= kDeferred) sb.color[m] = 0;
+        aggregatedMax32(&a.st->colors, 1u);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        *sb.epoch = epoch0 + round + 2;
-        a.st->colorRounds = round + 1;
-        if (round >= kMaxRounds) atomicOr(&a.st->err, kErrColors);
+        *sb.epoch = epoch0 + rounds + 2;
+        a.st->colorRounds = rounds;
+        if (exhausted) atomicOr(&a.st->err, kErrColors);
     }
 }
 
@@ -369,8 +414,10 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
     if (serial || !pairOrderCache) {
         k_order_init<<<gridFor(mcap), 256, 0, s>>>(a, serial ? 1 : 0);
         PE_LAUNCHED();
+        // colours may exceed 255 (colour windows); passes over constant
+        // digits are skipped on the device
         if (!serial)
-            launchRadixSort<uint32_t>(sb.orderKeys, sb.orderKeysTmp, sb.order, sb.orderTmp, a.count, mcap, 0, 8,
+            launchRadixSort<uint32_t>(sb.orderKeys, sb.orderKeysTmp, sb.order, sb.orderTmp, a.count, mcap, 0, 32,
                                       ws, err, s);
     }
     k_prepare<<<gridFor(mcap, kPrepareThreads), kPrepareThreads, kPrepareKeyCap * sizeof(unsigned long long), s>>>(

@@ -544,6 +544,13 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
     }
     __threadfence();
     cluster.sync();
+    if (__ldcg(&a.st->colors) > (uint32_t)kMaxColors) {
+        // More colours than the cluster's shared colour ranges hold (a body
+        // touching more than ~64 others): the step is re-run on the
+        // multi-kernel path.  Every rank reads the same count.
+        if (rank == 0 && tid == 0) atomicOr(&a.st->err, kErrSmallPath);
+        return;
+    }
 
     // ---- 2. this rank's share of every colour and of the staging slots ----
     if (tid == 0) {

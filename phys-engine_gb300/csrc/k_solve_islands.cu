@@ -87,6 +87,14 @@ __device__ __forceinline__ void islUnite(uint32_t *par, uint32_t a, uint32_t b, 
     atomicOr(err, kErrTimeout);
 }
 
+// More colours than the per-colour counters hold (colour windows): every
+// island goes to the grid-wide sweeps, with its per-colour counts and fill
+// cursors in sb.colorStart.
+__device__ __forceinline__ uint32_t islWideColors(const SolveArgs &a, uint32_t M) {
+    const uint32_t C = __ldcg(&a.st->colors);
+    return C > (uint32_t)kMaxColors ? (C < M ? C : M) : 0u;
+}
+
 __device__ __forceinline__ uint32_t *islPar(const SolveArgs &a) { return a.sb.islPar; }
 __device__ __forceinline__ uint32_t *islCnt(const SolveArgs &a) { return a.sb.islPar + a.w.nb; }
 
@@ -100,6 +108,8 @@ __global__ void k_isl_init(SolveArgs a) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
     for (uint32_t i = t; i < kIslCounterWords; i += stride) a.sb.islCounters[i] = 0u;
     for (uint32_t i = t; i < a.w.nb; i += stride) cnt[i] = 0u;
+    const uint32_t wideC = islWideColors(a, M);
+    for (uint32_t i = t; i < wideC; i += stride) a.sb.colorStart[i] = 0u;
     for (uint32_t m = t; m < M; m += stride) {
         const uint32_t fl = a.sb.dyn[m];
         if (fl & kFlagDynA) par[a.mv.bodyA[m]] = a.mv.bodyA[m];
@@ -137,21 +147,24 @@ __global__ void k_isl_count(SolveArgs a) {
 }
 
 // Islands of at least this many manifolds go to the grid-wide sweeps: all
-// once some island is large, none otherwise.
-__device__ __forceinline__ uint32_t islSweepFrom(const SolveArgs &a) {
-    return a.sb.islCounters[7] ? 1u : kIslNone;
+// once some island is large or the colours exceed kMaxColors, none otherwise.
+__device__ __forceinline__ uint32_t islSweepFrom(const SolveArgs &a, uint32_t M) {
+    return (a.sb.islCounters[7] || islWideColors(a, M)) ? 1u : kIslNone;
 }
 
 __global__ void k_isl_fill(SolveArgs a) {
     const uint32_t M = min(*a.count, a.mcap);
     const uint32_t *cnt = islCnt(a);
-    const uint32_t sweepFrom = islSweepFrom(a);
+    const uint32_t sweepFrom = islSweepFrom(a, M), wideC = islWideColors(a, M);
+    uint32_t *colorCounts = wideC ? a.sb.colorStart : a.sb.islCounters + kIslColorCount;
+    const uint32_t colorLimit = wideC ? wideC : (uint32_t)kMaxColors;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
     for (uint32_t m = t; m < M; m += stride) {
         const uint32_t r = a.sb.islRoot[m];
         if (r == kIslNone) continue;
         a.sb.islList[a.sb.islOff[r] + a.sb.islSlot[m]] = m;
-        if (cnt[r] >= sweepFrom) aggregatedAppendKeyed(a.sb.islCounters + kIslColorCount, a.sb.color[m]);
+        const uint32_t c = a.sb.color[m];
+        if (cnt[r] >= sweepFrom && c < colorLimit) aggregatedAppendKeyed(colorCounts, c);
     }
     // the warp queue: islands of 32 manifolds or more at the front (a warp's
     // lanes all busy; they bound the sweep), those of kIslThread to 31 from
@@ -279,8 +292,58 @@ __global__ void __launch_bounds__(kIslThreads) k_isl_solve(SolveArgs a) {
 // bucket lists live in islKeysTmp), then warm start and iterations colour by
 // colour with a grid barrier after each colour.  Every block reads the same
 // counts, so with no large island all return before the first barrier.
+// More than kMaxColors colours: every island in grid-wide sweeps, the
+// per-colour counts in sb.colorStart scanned into starts by block 0, then used
+// as fill cursors (after the fill, colorStart[c] is the end of colour c).
+__device__ void islSolveWide(const SolveArgs &a, uint32_t M, uint32_t C) {
+    __shared__ uint32_t s_scan[9], s_carry;
+    uint32_t *cur = a.sb.colorStart;
+    if (blockIdx.x == 0) {
+        if (threadIdx.x == 0) s_carry = 0;
+        __syncthreads();
+        for (uint32_t c0 = 0; c0 < C; c0 += blockDim.x) {
+            const uint32_t c = c0 + threadIdx.x;
+            const uint32_t v = c < C ? __ldcg(&cur[c]) : 0u;
+            uint32_t total;
+            const uint32_t ex = blockExclusiveScan(v, total, s_scan);
+            if (c < C) __stcg(&cur[c], s_carry + ex);
+            __syncthreads();
+            if (threadIdx.x == 0) s_carry += total;
+            __syncthreads();
+        }
+    }
+    gridBarrier(a.sb.bar, &a.st->err);
+    const uint32_t *cnt = islCnt(a);
+    uint32_t *list = reinterpret_cast<uint32_t *>(a.sb.islKeysTmp);
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
+    for (uint32_t m = gtid; m < M; m += gstride) {
+        const uint32_t r = a.sb.islRoot[m];
+        const uint32_t c = a.sb.color[m];
+        if (r == kIslNone || cnt[r] == 0 || c >= C) continue;
+        list[aggregatedAppendKeyed(cur, c)] = m;
+    }
+    gridBarrier(a.sb.bar, &a.st->err);
+    for (int pass = 0; pass <= a.iterations; ++pass)
+        for (uint32_t c = 0; c < C; ++c) {
+            const uint32_t lo = c ? __ldcg(&cur[c - 1]) : 0u, hi = __ldcg(&cur[c]);
+            for (uint32_t k = lo + gtid; k < hi; k += gstride) {
+                if (pass == 0) warmStartOne(a, k, list[k]);
+                else solveOne(a, k, list[k]);
+            }
+            gridBarrier(a.sb.bar, &a.st->err);
+        }
+}
+
 __global__ void __launch_bounds__(kSolveThreads) k_isl_solve_large(SolveArgs a) {
     __shared__ uint32_t s_start[kMaxColors + 1];
+    {
+        const uint32_t M = min(*a.count, a.mcap);
+        const uint32_t wideC = islWideColors(a, M);
+        if (wideC) {  // every block sees the same colour count
+            islSolveWide(a, M, wideC);
+            return;
+        }
+    }
     const uint32_t *count = a.sb.islCounters + kIslColorCount;
     uint32_t *fill = a.sb.islCounters + kIslColorFill;
     if (threadIdx.x == 0) {
@@ -295,7 +358,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_isl_solve_large(SolveArgs a) 
     if (s_start[kMaxColors] == 0) return;
     const uint32_t M = min(*a.count, a.mcap);
     const uint32_t *cnt = islCnt(a);
-    const uint32_t sweepFrom = islSweepFrom(a);
+    const uint32_t sweepFrom = islSweepFrom(a, M);
     uint32_t *list = reinterpret_cast<uint32_t *>(a.sb.islKeysTmp);
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
     for (uint32_t m = gtid; m < M; m += gstride) {

@@ -8,6 +8,16 @@
 namespace pe {
 
 constexpr uint32_t kUncolored = 0xFFFFFFFFu;
+// Colour windows.  The per-body masks of the Jones-Plassmann colouring hold
+// kMaxColors colours: the window [base, base + kMaxColors).  A manifold whose
+// higher-priority neighbours already use every colour of the window is
+// deferred (kDeferred): its greedy colour lies above the window and depends
+// only on the colours of its deferred higher-priority neighbours, so the
+// deferred manifolds are coloured again, by the same rule, in the next window
+// (masks cleared, colours offset by kMaxColors).  There is no colour limit.
+constexpr uint32_t kDeferred = 0xFFFFFFFEu;
+// Rounds of one colour window (a window takes at least as many rounds as the
+// largest number of its manifolds at one body).
 constexpr uint32_t kMaxRounds = 4096;
 constexpr int kSolveThreads = 256;
 constexpr int kBlockSolveThreads = 512;
@@ -75,7 +85,16 @@ struct BlockSolveShared {
     uint32_t colored;
     uint32_t colors;
     uint32_t slots;
+    uint32_t deferred;  // manifolds deferred to the next colour window
 };
+
+// Solve-index range [first, end) of colour c: from the shared ranges, or
+// from sb.colorStart when the step has more than kMaxColors colours.
+__device__ __forceinline__ uint2 colorRange(const BlockSolveShared &sh, const SolverBuffers &sb, uint32_t c,
+                                            uint32_t C, uint32_t M) {
+    if (C <= (uint32_t)kMaxColors) return make_uint2(sh.start[c], sh.start[c + 1]);
+    return make_uint2(__ldcg(&sb.colorStart[c]), c + 1 < C ? __ldcg(&sb.colorStart[c + 1]) : M);
+}
 
 // Shared-memory copies of the velocities of the bodies the manifolds touch,
 // used by the single-block solver for the warm start and the iterations.
@@ -636,12 +655,14 @@ __device__ inline bool solveBlockFront(const SolveArgs &a, uint32_t M, int seria
             }
             __syncthreads();
         }
-        // --- colouring (Jones-Plassmann rounds, as k_color); per-body arrays in
-        // shared memory by slot when slotted, else in global memory by body ---
+        // --- colouring (Jones-Plassmann rounds in colour windows, as k_color);
+        // per-body arrays in shared memory by slot when slotted, else in global
+        // memory by body ---
         for (uint32_t c = tid; c < kMaxColors; c += nt) s_count[c] = 0;
         if (tid == 0) {
             s_colored = 0;
             s_colors = 0;
+            sh.deferred = 0;
         }
         unsigned long long *cBest = sb.bodyBest, *cUsed = sb.bodyUsed;
         if (slotted) {
@@ -676,80 +697,126 @@ __device__ inline bool solveBlockFront(const SolveArgs &a, uint32_t M, int seria
         }
         __syncthreads();
         const unsigned long long epoch0 = __ldcg(sb.epoch);
-        uint32_t round = 0;
-        for (; round < kMaxRounds; ++round) {
-            const unsigned long long stamp = (epoch0 + round + 1) << 32;
-            for (uint32_t m = tid; m < M; m += nt) {
-                if (s_color[m] != kUncolored) continue;
-                const unsigned long long p = stamp | colorPriority(m);
-                if (s_dyn[m] & 1u) atomicMax(&cBest[cid(m, 0)], p);
-                if (s_dyn[m] & 2u) atomicMax(&cBest[cid(m, 1)], p);
-            }
-            __syncthreads();
-            // (m0 advances uniformly so that whole warps aggregate the counters)
-            for (uint32_t m0 = 0; m0 < M; m0 += nt) {
-                const uint32_t m = m0 + tid;
-                uint32_t c = kUncolored;
-                if (m < M && s_color[m] == kUncolored) {
+        uint32_t rounds = 0, base = 0;
+        bool exhausted = false;
+        for (;;) {  // one colour window [base, base + kMaxColors) per pass
+            uint32_t round = 0;
+            for (; round < kMaxRounds; ++round) {
+                const unsigned long long stamp = (epoch0 + rounds + round + 1) << 32;
+                for (uint32_t m = tid; m < M; m += nt) {
+                    if (s_color[m] != kUncolored) continue;
                     const unsigned long long p = stamp | colorPriority(m);
-                    const uint32_t d = s_dyn[m], ba = cid(m, 0), bb = cid(m, 1);
-                    const bool wins = (!(d & 1u) || ldc(&cBest[ba]) == p) && (!(d & 2u) || ldc(&cBest[bb]) == p);
-                    if (wins) {
-                        unsigned long long u0 = 0, u1 = 0;
-                        if (d & 1u) {
-                            u0 |= ldc(&cUsed[2 * ba]);
-                            u1 |= ldc(&cUsed[2 * ba + 1]);
+                    if (s_dyn[m] & 1u) atomicMax(&cBest[cid(m, 0)], p);
+                    if (s_dyn[m] & 2u) atomicMax(&cBest[cid(m, 1)], p);
+                }
+                __syncthreads();
+                // (m0 advances uniformly so that whole warps aggregate the counters)
+                for (uint32_t m0 = 0; m0 < M; m0 += nt) {
+                    const uint32_t m = m0 + tid;
+                    uint32_t c = kUncolored;
+                    if (m < M && s_color[m] == kUncolored) {
+                        const unsigned long long p = stamp | colorPriority(m);
+                        const uint32_t d = s_dyn[m], ba = cid(m, 0), bb = cid(m, 1);
+                        const bool wins =
+                            (!(d & 1u) || ldc(&cBest[ba]) == p) && (!(d & 2u) || ldc(&cBest[bb]) == p);
+                        if (wins) {
+                            unsigned long long u0 = 0, u1 = 0;
+                            if (d & 1u) {
+                                u0 |= ldc(&cUsed[2 * ba]);
+                                u1 |= ldc(&cUsed[2 * ba + 1]);
+                            }
+                            if (d & 2u) {
+                                u0 |= ldc(&cUsed[2 * bb]);
+                                u1 |= ldc(&cUsed[2 * bb + 1]);
+                            }
+                            uint32_t local = kDeferred;
+                            if (~u0) local = __ffsll((long long)~u0) - 1;
+                            else if (~u1) local = 64 + __ffsll((long long)~u1) - 1;
+                            if (local != kDeferred) {
+                                c = base + local;
+                                const unsigned long long bit = 1ull << (local & 63);
+                                if (d & 1u) stc(&cUsed[2 * ba + (local >> 6)], ldc(&cUsed[2 * ba + (local >> 6)]) | bit);
+                                if (d & 2u) stc(&cUsed[2 * bb + (local >> 6)], ldc(&cUsed[2 * bb + (local >> 6)]) | bit);
+                            } else {
+                                c = kDeferred;
+                            }
+                            s_color[m] = c;
                         }
-                        if (d & 2u) {
-                            u0 |= ldc(&cUsed[2 * bb]);
-                            u1 |= ldc(&cUsed[2 * bb + 1]);
-                        }
-                        if (~u0) c = __ffsll((long long)~u0) - 1;
-                        else if (~u1) c = 64 + __ffsll((long long)~u1) - 1;
-                        else {
-                            atomicOr(&a.st->err, kErrColors);
-                            c = kMaxColors - 1;
-                        }
-                        s_color[m] = c;
-                        const unsigned long long bit = 1ull << (c & 63);
-                        if (d & 1u) stc(&cUsed[2 * ba + (c >> 6)], ldc(&cUsed[2 * ba + (c >> 6)]) | bit);
-                        if (d & 2u) stc(&cUsed[2 * bb + (c >> 6)], ldc(&cUsed[2 * bb + (c >> 6)]) | bit);
                     }
+                    // one shared-memory atomic per warp and counter
+                    const uint32_t lane = tid & 31;
+                    const bool done = c != kUncolored, got = done && c != kDeferred;
+                    const uint32_t doneMask = __ballot_sync(0xffffffffu, done);
+                    const uint32_t gotMask = __ballot_sync(0xffffffffu, got);
+                    const uint32_t top = __reduce_max_sync(0xffffffffu, got ? c + 1 : 0u);
+                    if (lane == 0 && doneMask) {
+                        atomicAdd(&s_colored, (uint32_t)__popc(doneMask));
+                        if (doneMask != gotMask) atomicAdd(&sh.deferred, (uint32_t)__popc(doneMask & ~gotMask));
+                        if (gotMask) atomicMax(&s_colors, top);
+                    }
+                    const uint32_t peers = __match_any_sync(0xffffffffu, c);
+                    if (got && c < (uint32_t)kMaxColors && (peers & ((1u << lane) - 1u)) == 0)
+                        atomicAdd(&s_count[c], (uint32_t)__popc(peers));
                 }
-                // one shared-memory atomic per warp and counter
-                const uint32_t lane = tid & 31;
-                const bool got = c != kUncolored;
-                const uint32_t gotMask = __ballot_sync(0xffffffffu, got);
-                const uint32_t top = __reduce_max_sync(0xffffffffu, got ? c + 1 : 0u);
-                if (lane == 0 && gotMask) {
-                    atomicAdd(&s_colored, (uint32_t)__popc(gotMask));
-                    atomicMax(&s_colors, top);
-                }
-                const uint32_t peers = __match_any_sync(0xffffffffu, c);
-                if (got && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&s_count[c], (uint32_t)__popc(peers));
+                __syncthreads();
+                if (s_colored >= M) break;
+                __syncthreads();
+            }
+            rounds += round + 1;
+            if (round >= kMaxRounds) {
+                exhausted = true;
+                break;
+            }
+            const uint32_t deferred = sh.deferred;
+            __syncthreads();
+            if (deferred == 0) break;
+            // next window: the deferred manifolds become uncoloured again and
+            // the masks of their bodies start empty
+            base += kMaxColors;
+            for (uint32_t m = tid; m < M; m += nt) {
+                if (s_color[m] != kDeferred) continue;
+                s_color[m] = kUncolored;
+                const uint32_t d = s_dyn[m];
+                for (int e = 0; e < 2; ++e)
+                    if (d & (1u << e)) {
+                        stc(&cUsed[2 * cid(m, e)], 0ull);
+                        stc(&cUsed[2 * cid(m, e) + 1], 0ull);
+                    }
+            }
+            if (tid == 0) {
+                s_colored = M - deferred;
+                sh.deferred = 0;
             }
             __syncthreads();
-            if (s_colored >= M) break;
+        }
+        if (exhausted) {
+            // The step fails (kErrColors); colour 0 for what is left keeps every
+            // index below in range.
+            for (uint32_t m = tid; m < M; m += nt)
+                if (s_color[m] >= kDeferred) s_color[m] = 0;
+            if (tid == 0 && s_colors == 0) s_colors = 1;
             __syncthreads();
         }
         if (tid == 0) {
-            *sb.epoch = epoch0 + round + 2;
-            a.st->colorRounds = round + 1;
+            *sb.epoch = epoch0 + rounds + 2;
+            a.st->colorRounds = rounds;
             a.st->colors = s_colors;
-            if (round >= kMaxRounds) atomicOr(&a.st->err, kErrColors);
-            uint32_t acc = 0;
-            for (uint32_t c = 0; c < s_colors; ++c) {
-                s_start[c] = acc;
-                sb.colorCount[c] = s_count[c];
-                acc += s_count[c];
+            if (exhausted) atomicOr(&a.st->err, kErrColors);
+            if (s_colors <= (uint32_t)kMaxColors) {
+                uint32_t acc = 0;
+                for (uint32_t c = 0; c < s_colors; ++c) {
+                    s_start[c] = acc;
+                    sb.colorCount[c] = s_count[c];
+                    acc += s_count[c];
+                }
+                s_start[s_colors] = acc;
             }
-            s_start[s_colors] = acc;
         }
         // colours to global (pair order) and the (colour, index) order
         for (uint32_t m = tid; m < M; m += nt) sb.color[m] = s_color[m];
         __syncthreads();
         const uint32_t nw = nt >> 5, Cc = s_colors;
-        if (nw * Cc <= 2 * maxM) {
+        if (Cc <= (uint32_t)kMaxColors && nw * Cc <= 2 * maxM) {
             // Stable placement: a manifold goes to the start of its colour plus
             // the number of earlier manifolds of that colour (warp ranks from
             // match_any, per-warp colour counts scanned across warps).
@@ -792,6 +859,12 @@ __device__ inline bool solveBlockFront(const SolveArgs &a, uint32_t M, int seria
             for (uint32_t k = tid; k < M; k += nt) {
                 sb.order[k] = keys[k] & 0xFFFu;
                 s_dyn[k] = keys[k] & 0xFFFu;
+                // more colours than the shared ranges hold: colour c starts at
+                // sb.colorStart[c] (every colour below the last is used, so
+                // each has a first solve index)
+                if (Cc > (uint32_t)kMaxColors && (k == 0 || (keys[k] >> 12) != (keys[k - 1] >> 12)) &&
+                    (keys[k] >> 12) < M)
+                    sb.colorStart[keys[k] >> 12] = k;
             }
         }
         __syncthreads();
@@ -894,22 +967,26 @@ __device__ inline void solveBlockSweeps(const SolveArgs &a, uint32_t M, int seri
     } else if (staged) {
         const SharedVel sv{vs->v, vs->slot};
         for (uint32_t c = 0; c < C; ++c) {
-            for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) warmStartOne(a, k, s_dyn[k], sv);
+            const uint2 r = colorRange(sh, sb, c, C, M);
+            for (uint32_t k = r.x + tid; k < r.y; k += nt) warmStartOne(a, k, s_dyn[k], sv);
             __syncthreads();
         }
         for (int it = 0; it < a.iterations; ++it)
             for (uint32_t c = 0; c < C; ++c) {
-                for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) solveOne(a, k, s_dyn[k], sv);
+                const uint2 r = colorRange(sh, sb, c, C, M);
+                for (uint32_t k = r.x + tid; k < r.y; k += nt) solveOne(a, k, s_dyn[k], sv);
                 __syncthreads();
             }
     } else {
         for (uint32_t c = 0; c < C; ++c) {
-            for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) warmStartOne(a, k, s_dyn[k]);
+            const uint2 r = colorRange(sh, sb, c, C, M);
+            for (uint32_t k = r.x + tid; k < r.y; k += nt) warmStartOne(a, k, s_dyn[k]);
             __syncthreads();
         }
         for (int it = 0; it < a.iterations; ++it)
             for (uint32_t c = 0; c < C; ++c) {
-                for (uint32_t k = s_start[c] + tid; k < s_start[c + 1]; k += nt) solveOne(a, k, s_dyn[k]);
+                const uint2 r = colorRange(sh, sb, c, C, M);
+                for (uint32_t k = r.x + tid; k < r.y; k += nt) solveOne(a, k, s_dyn[k]);
                 __syncthreads();
             }
     }

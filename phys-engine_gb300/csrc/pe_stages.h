@@ -71,11 +71,13 @@ struct SolverBuffers {
     uint32_t mcap;
     // colouring
     unsigned long long *bodyBest;   // [nb] round-stamped max priority
-    unsigned long long *bodyUsed;   // [2 * nb] colour masks (128 colours)
+    unsigned long long *bodyUsed;   // [2 * nb] colour masks of the current window of kMaxColors colours
     unsigned long long *epoch;      // [1] persistent round stamp
     uint32_t *color;                // [mcap]
     uint32_t *dyn;                  // [mcap] bit0 A dynamic, bit1 B dynamic
     uint32_t *colorCount;           // [kMaxColors]
+    uint32_t *colorStart;           // [mcap] steps with more than kMaxColors colours: first solve index
+                                    // (block paths), or counts then fill cursors (multi-kernel path) per colour
     uint32_t *orderKeys, *orderKeysTmp, *order, *orderTmp;  // [mcap]
     // prepared data, in solve order k (structure of arrays)
     float4 *pm;                     // [mcap] invMassA, staticA, invMassB, staticB

@@ -64,7 +64,7 @@ Layout makeLayout(uint32_t nMax, uint32_t maxPairs, uint32_t maxM, int iteration
     L.order = take(4ull * maxM);
     L.sortKeys = take(8ull * maxM);
     L.bodyUsed = take(16ull * nMax);
-    L.colorStart = take(4ull * (kAdMaxColors + 1));
+    L.colorStart = take(4ull * (maxM + 1));
     L.pp = take(sizeof(F) * 4 * maxM * kPreparedScalars);
     L.pm = take(sizeof(F) * maxM * kPmScalars);
     L.lam = take(sizeof(F) * 12 * maxM);
@@ -435,7 +435,7 @@ void Rollout::checkErrors(cudaStream_t s, const char *what) {
             const uint32_t b = e[w];
             const char *m = (b & kAdErrPairs)       ? "candidate pairs exceed the world's capacity"
                             : (b & kAdErrManifolds) ? "contact manifolds exceed the world's capacity"
-                            : (b & kAdErrColors)    ? "more than 128 solver colours"
+                            : (b & kAdErrColors)    ? "solver colouring failed"
                             : (b & kAdErrCache)     ? "warm-start cache overflow"
                                                     : "the adjoint's replay of a contact differed from the forward";
             throw std::runtime_error(std::string(what) + ": world " + std::to_string(w) + ": " + m);

@@ -47,7 +47,7 @@ struct ScratchMem {
           mDepth(4 * maxM), pp((size_t)4 * maxM * kPreparedScalars), pm((size_t)maxM * kPmScalars), lam(12 * maxM),
           lamInit(12 * maxM), tape((size_t)(iterations > 0 ? iterations : 1) * maxM * kTapeScalars), pairA(maxPairs),
           pairB(maxPairs), mA(maxM), mB(maxM), mCount(maxM), mFeature(4 * maxM), color(maxM), order(maxM),
-          colorStart(kAdMaxColors + 1), cacheSrc(4 * maxM), counts(4), sortKeys(maxM), bodyUsed(2 * n),
+          colorStart(maxM + 1), cacheSrc(4 * maxM), counts(4), sortKeys(maxM), bodyUsed(2 * n),
           match(4 * maxM) {}
     StepScratch<S> view() {
         StepScratch<S> s;

@@ -533,6 +533,7 @@ void World::ensureCapacity() {
     sColor_.reserve(m);
     sDyn_.reserve(m);
     sColorCount_.reserve(kMaxColors);
+    sColorStart_.reserve(m);
     sOrderKeys_.reserve(m);
     sOrderKeysTmp_.reserve(m);
     sOrder_.reserve(m);
@@ -573,6 +574,7 @@ void World::ensureCapacity() {
                         sColor_.ptr,
                         sDyn_.ptr,
                         sColorCount_.ptr,
+                        sColorStart_.ptr,
                         sOrderKeys_.ptr,
                         sOrderKeysTmp_.ptr,
                         sOrder_.ptr,
@@ -787,7 +789,7 @@ bool World::finishStep() {
     if (h.err & (kErrTimeout | kErrColors | kErrEntryCapacity | kErrTreeDepth)) {
         throw std::runtime_error(std::string("step failed on the device: ") +
                                  ((h.err & kErrTimeout) ? "a bounded wait timed out" :
-                                  (h.err & kErrColors) ? "more than 128 solver colours" :
+                                  (h.err & kErrColors) ? "the solver colouring exceeded its round limit" :
                                   (h.err & kErrTreeDepth) ? "a bounding-volume tree traversal outgrew its stack" :
                                                             "grid cell range exceeds 64 key bits"));
     }
@@ -814,6 +816,9 @@ bool World::finishStep() {
         // the sizes this attempt measured.
         lastMEstimate_ = std::max(lastMEstimate_, h.manifolds);
         lastRawEstimate_ = std::max(lastRawEstimate_, h.rawPairs);
+        // the cluster solver holds kMaxColors colour ranges: more colours take
+        // the multi-kernel path
+        if (h.colors > (uint32_t)kMaxColors) wideColors_ = true;
         if (h.cellKeyBits > gridKeyBits_) gridKeyBits_ = std::min<uint32_t>(64, 8 * ((h.cellKeyBits + 9) / 8));
         retry = true;
     }
@@ -867,6 +872,7 @@ bool World::finishStep() {
     lastManifolds_ = h.manifolds;
     lastMEstimate_ = h.manifolds;
     lastRawEstimate_ = h.rawPairs;
+    wideColors_ = orderMode != 0 && !solveSkipped_ && h.colors > (uint32_t)kMaxColors;
     // Cell-key width: whole bytes with at least two bits of slack, widened
     // early so the captured graph rarely changes.
     if (algorithm == 1) {
@@ -943,7 +949,8 @@ unsigned long long World::launchStep(float dt) {
     coopBlocks_ = (int)std::min<uint32_t>(blocks, (uint32_t)maxCooperativeBlocks(smCount_));
     // Small manifold counts run the single-block solver (with headroom over
     // the last step's count; an overflow re-runs the step on the full path).
-    blockSolver_ = lastMEstimate_ + lastMEstimate_ / 4 + 64 <= kBlockMaxManifolds && nb_ <= kBlockMaxBodies;
+    blockSolver_ = lastMEstimate_ + lastMEstimate_ / 4 + 64 <= kBlockMaxManifolds && nb_ <= kBlockMaxBodies &&
+                   !wideColors_;
     blockM_ = 64;
     while (blockM_ < lastMEstimate_ + lastMEstimate_ / 4 + 64 && blockM_ < kBlockMaxManifolds) blockM_ <<= 1;
     // Pair keys need bits for input indices < nc; the small finalize path is

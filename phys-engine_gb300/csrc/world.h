@@ -205,6 +205,9 @@ class World {
     uint64_t steps_ = 0;
     uint32_t lastErr_ = 0;
     uint32_t lastPairs_ = 0, lastManifolds_ = 0, lastMEstimate_ = 0, lastRawEstimate_ = 0;
+    // the last step needed more than kMaxColors solver colours: solve on the
+    // multi-kernel path (the cluster solver's colour ranges hold kMaxColors)
+    bool wideColors_ = false;
     uint32_t gridKeyBits_ = 64;
     uint64_t possiblePairs_ = 0, dynamicAlive_ = 0;
     StepCounters counters_;
@@ -270,7 +273,7 @@ class World {
     // solver
     SolverBuffers sb_{};
     DeviceArray<unsigned long long> sBest_, sUsed_, sEpoch_, sCacheKeys_, sCacheKeysTmp_;
-    DeviceArray<uint32_t> sColor_, sDyn_, sColorCount_, sOrderKeys_, sOrderKeysTmp_, sOrder_, sOrderTmp_, sPcount_,
+    DeviceArray<uint32_t> sColor_, sDyn_, sColorCount_, sColorStart_, sOrderKeys_, sOrderKeysTmp_, sOrder_, sOrderTmp_, sPcount_,
         sCacheVals_, sCacheValsTmp_, sCacheCounts_, sCacheOff_, sBar_, sCounters_, sStageBody_, sIslandList_;
     DeviceArray<uint32_t> sIslPar_, sIslOff_, sIslRoot_, sIslSlot_, sIslList_, sIslRoots_, sIslLone_, sIslCounters_;
     DeviceArray<unsigned long long> sIslKeys_, sIslKeysTmp_, sIslSort_;
