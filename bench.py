@@ -89,6 +89,9 @@ class ClockSampler:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            # nvidia-smi's start-up (driver and NVML initialisation) is kept out
+            # of the timed steps that follow
+            time.sleep(0.5)
         except OSError:
             self.proc = None
         return self
@@ -324,6 +327,9 @@ def run_gpu(args, rank, world_size, local_rank):
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
+    if world_size == 1 and not args.no_configs:
+        line["spheres_1k"] = run_spheres_1k(args, local_rank, flush, peak)
+        line["stacking_convex"] = run_stacking_convex(args, local_rank, flush, peak)
     if world_size == 1 and not args.no_batched:
         line["batched"] = run_batched(args, local_rank, flush, peak)
         line["differentiable"] = run_differentiable(args, local_rank)
@@ -349,6 +355,143 @@ SPHERES_STEPS = 300
 STACK_PYRAMIDS = 16
 STACK_ITERATIONS = 20
 STACK_STEPS = 1000
+
+def run_config_leg(args, local_rank, flush, peak, scene, algo, iterations, steps, dt, cpu_budget_s, describe):
+    """One whole run of a configured workload: a fresh world stepped `steps`
+    times from its initial state, every step device-timed (CUDA events on the
+    world's stream, L2 flushed before each step); the same run end to end
+    through pe_world_step_io with host buffers (forces in from pinned memory,
+    poses out); and the oracle port (reference algorithm and order, all host
+    threads) on a bounded sample of the same run's first steps."""
+    import torch
+
+    from oracle import cpu
+    from phys_gb300 import engine
+
+    dev = torch.device("cuda", local_rank)
+    warm = engine.GpuWorld(device=local_rank, algo=algo, iterations=iterations, order=engine.ORDER_COLOR)
+    warm.load_scene(scene)
+    for _ in range(min(steps, 10)):
+        warm.step(dt)
+    warm.close()
+
+    w = engine.GpuWorld(device=local_rank, algo=algo, iterations=iterations, order=engine.ORDER_COLOR)
+    w.load_scene(scene)
+    stream = torch.cuda.ExternalStream(w.stream(), device=dev)
+    bodies = int(scene.count - scene.is_static.sum())
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    stage_ms = {k: 0.0 for k in ("integrate", "broadphase", "narrowphase", "solver", "pose")}
+    stage_b = {k: 0 for k in stage_ms}
+    totals = {"pairs": 0, "manifolds": 0, "points": 0, "hull_contacts": 0}
+    launches = 0
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clocks:
+        for k in range(steps):
+            with torch.cuda.stream(stream):
+                flush.add_(1.0)
+            starts[k].record(stream)
+            w.step(dt)
+            ends[k].record(stream)
+            st = w.stats()
+            for key in stage_ms:
+                stage_ms[key] += float(st[key + "_ms"])
+            for key, v in stage_bytes(st, scene.count, iterations).items():
+                stage_b[key] += v
+            launches += int(st["kernel_launches"])
+            totals["pairs"] += int(st["candidate_pairs"])
+            totals["manifolds"] += int(st["contact_count"])
+            totals["points"] += int(st["contact_points"])
+            totals["hull_contacts"] += int(st["np_contacts"][3])
+        torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends))
+    last = w.stats()
+    w.close()
+
+    # end to end: the same run through the C ABI with host buffers
+    w = engine.GpuWorld(device=local_rank, algo=algo, iterations=iterations, order=engine.ORDER_COLOR)
+    w.load_scene(scene)
+    n = scene.count
+    forces = torch.zeros((n, 3), dtype=torch.float32).pin_memory().numpy()
+    pp = torch.empty((n, 3), dtype=torch.float32).pin_memory().numpy()
+    pq = torch.empty((n, 4), dtype=torch.float32).pin_memory().numpy()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        w.step_io(dt, forces, pp, pq)
+    e2e_s = time.perf_counter() - t0
+    w.close()
+
+    # CPU: the oracle port on the first steps of the same run
+    threads = os.cpu_count() or 1
+    ow = cpu.OracleWorld(algo=algo, iterations=iterations, order_mode=0, threads=threads)
+    ow.load_scene(scene)
+    k, t0 = 0, time.perf_counter()
+    while k < steps and (k == 0 or time.perf_counter() - t0 < cpu_budget_s):
+        ow.step(dt)
+        k += 1
+    cpu_s = time.perf_counter() - t0
+
+    dominant = max(stage_ms, key=stage_ms.get)
+    achieved = stage_b[dominant] / (stage_ms[dominant] / 1000.0) / 1e9 if stage_ms[dominant] > 0 else 0.0
+    step_bytes = sum(stage_b.values())
+    return {
+        "metric": f"body-steps/s, {describe}", "value": bodies * steps / (ms / 1000.0), "unit": UNIT,
+        "bodies": bodies, "steps": steps, "ms_per_step": ms / steps, "gpu_launches": launches,
+        "workload_per_step": {k2: v / steps for k2, v in totals.items()},
+        "last_step": {"candidate_pairs": int(last["candidate_pairs"]), "manifolds": int(last["contact_count"]),
+                      "points": int(last["contact_points"]), "colors": int(last["color_count"]),
+                      "hull_contacts": int(last["np_contacts"][3])},
+        "roofline": {
+            "bound": "hbm", "stage": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "algorithmic_bytes_per_step": stage_b[dominant] / steps,
+            "stage_ms_per_step": {k2: v / steps for k2, v in stage_ms.items()},
+            "whole_step": {"algorithmic_bytes_per_step": step_bytes / steps,
+                           "achieved_gbs": step_bytes / (ms / 1000.0) / 1e9,
+                           "frac": step_bytes / (ms / 1000.0) / 1e9 / peak}},
+        "e2e": {"value": bodies * steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 12 * n,
+                "d2h_bytes_per_step": 28 * n, "steps": steps},
+        "cpu_baseline": {"value": bodies * k / cpu_s, "unit": UNIT, "cores": threads, "kind": "port",
+                         "ms_per_step": 1000.0 * cpu_s / k,
+                         "sample": f"the first {k} of the run's {steps} steps ({cpu_s:.1f} s), oracle restatement "
+                                   f"of the reference algorithm in the reference's manifold order"},
+        "speedup_vs_cpu_baseline": (bodies * steps / (ms / 1000.0)) / (bodies * k / cpu_s),
+        "clocks": clocks.summary(),
+    }
+
+
+def run_spheres_1k(args, local_rank, flush, peak):
+    """Config 1: 1,000 spheres (r U[0.25,0.5], density 1) dropped from a
+    20 x 40 x 20 m box onto a static floor, zero velocity, dt 1/60, 10
+    iterations, friction 0.5, restitution 0, SAP, all 300 steps."""
+    from phys_gb300 import engine, scenes
+
+    sc = scenes.generate(scenes.SPHERES_ON_FLOOR, SPHERES_BODIES, SEED)
+    out = run_config_leg(args, local_rank, flush, peak, sc, engine.SAP, ITERATIONS, args.spheres_steps, DT, 10.0,
+                         "1,000 spheres dropped on a floor")
+    out["config"] = {"workload": "spheres_1k", "bodies": SPHERES_BODIES, "radius_m": "U[0.25,0.5]",
+                     "spawn_m": [20, 40, 20], "broadphase": "SAP", "solver_iterations": ITERATIONS,
+                     "friction": 0.5, "restitution": 0.0, "dt": DT, "steps": args.spheres_steps,
+                     "solver_order": "graph colour", "l2": "flushed before every timed step (512 MiB write)"}
+    return out
+
+
+def run_stacking_convex(args, local_rank, flush, peak):
+    """Config 3: 256 planar box pyramids (16 x 16, rows 20..1, 210 boxes of
+    half extent 0.5 m each, 53,760 boxes) on a tiled static floor, plus 20,000
+    convex hulls (24 points on ellipsoids, semi-axes U[0.3,0.8]) dropped from
+    30-60 m (the GJK/EPA path), 20 iterations with warm start, dt 1/60."""
+    from phys_gb300 import engine, scenes
+
+    sc = scenes.generate(scenes.PYRAMIDS, STACK_PYRAMIDS, SEED)
+    out = run_config_leg(args, local_rank, flush, peak, sc, engine.SAP, STACK_ITERATIONS, args.stack_steps, DT, 15.0,
+                         "256 box pyramids + 20,000 convex hulls")
+    out["config"] = {"workload": "stacking_convex", "pyramids": STACK_PYRAMIDS ** 2, "boxes": 53_760,
+                     "hulls": int((sc.shape == 2).sum()), "hull_points": 24, "broadphase": "SAP",
+                     "solver_iterations": STACK_ITERATIONS, "warm_start": True, "dt": DT, "steps": args.stack_steps,
+                     "solver_order": "graph colour", "l2": "flushed before every timed step (512 MiB write)"}
+    return out
+
 
 BATCH_WORLDS = 4096
 BATCH_MIN, BATCH_MAX = 16, 2048
@@ -812,6 +955,10 @@ def main():
     ap.add_argument("--no-sleeping", action="store_true", help="skip the sleeping-island measurement")
     ap.add_argument("--field-steps", type=int, default=1200, help="timed steps of the reference-scene measurement")
     ap.add_argument("--no-field", action="store_true", help="skip the reference's own benchmark scene")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the 1,000-sphere and the pyramids-with-hulls whole-run measurements")
+    ap.add_argument("--spheres-steps", type=int, default=SPHERES_STEPS, help="steps of the 1,000-sphere run")
+    ap.add_argument("--stack-steps", type=int, default=STACK_STEPS, help="steps of the pyramids-with-hulls run")
     ap.add_argument("--workload", choices=PROFILE_WORKLOADS, default=None,
                     help="step one named workload untimed and print its counters (profiling runs)")
     ap.add_argument("--profile-steps", type=int, default=8, help="steps of the --workload run")
