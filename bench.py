@@ -890,7 +890,8 @@ def run_workload(args):
     `spheres1000` 1,000 spheres dropped on a floor (SAP, 10 iterations, dt 1/60);
     `field` the reference's own benchmark scene (benchmarks/bench_scenes.cpp:11-63,
     SAP, 8 iterations, dt 1/120) with --bodies bodies; `stacking_convex` the 256
-    box pyramids plus 20,000 hulls (20 iterations, dt 1/60), or --pyramids per side.
+    box pyramids plus 20,000 hulls (20 iterations, dt 1/60), or --pyramids per side,
+    with the hulls lowered by --drop metres.
     `launches` (engine kernels over all steps) and `last_step_launches` let a
     profiler skip to the last steps of the run."""
     from phys_gb300 import engine, scenes
@@ -915,6 +916,7 @@ def run_workload(args):
         dt = DT
     elif name == "stacking_convex":
         sc = scenes.generate(scenes.PYRAMIDS, args.pyramids, SEED)
+        sc.pos[sc.shape == 2, 1] -= np.float32(args.drop)
         bp = args.broadphase or "sap"
         w = engine.GpuWorld(device=0, algo=algo[bp], iterations=STACK_ITERATIONS)
         dt = DT
@@ -964,6 +966,8 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=8, help="steps of the --workload run")
     ap.add_argument("--bodies", type=int, default=10000, help="bodies of the --workload field scene")
     ap.add_argument("--pyramids", type=int, default=16, help="pyramids per side of --workload stacking_convex")
+    ap.add_argument("--drop", type=float, default=0.0,
+                    help="--workload stacking_convex: lower the hulls by this many metres (contacts from the first steps)")
     ap.add_argument("--broadphase", choices=("grid", "sap", "tree"), default=None, help="--workload broadphase")
     ap.add_argument("--tiles", type=int, nargs=2, default=(1, 1), help="--workload stacks: copies along x and z")
     ap.add_argument("--sleeping", action="store_true", help="--workload: sleeping islands enabled")
