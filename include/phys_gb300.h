@@ -207,6 +207,42 @@ pe_status pe_world_body_is_sleeping(pe_world *world, pe_handle body, int *sleepi
 pe_status pe_world_body_wake_up(pe_world *world, pe_handle body);
 pe_status pe_world_body_apply_force(pe_world *world, pe_handle body, const float *force);
 pe_status pe_world_body_set_velocity(pe_world *world, pe_handle body, const float *linear, const float *angular);
+/* RigidBody as a value (include/phys/dynamics/rigid_body.hpp:14-140): the public
+   state, the diagonal local inverse inertia (inverseInertiaLocal, private in the
+   reference and set only by its factories) and the sleep flags (sleeping,
+   wakeRequested). */
+typedef struct pe_body_record {
+    pe_body_state state;
+    float inv_inertia[3];
+    int32_t sleeping;
+    int32_t wake_requested;
+} pe_body_record;
+/* RigidBody::createSphere / createBox (src/dynamics/rigid_body.cpp:25-92) on the
+   host, no world involved: validation (PE_ERR_CREATE_FAILED with the reference's
+   message), mass = volume x density, inverse inertia. */
+pe_status pe_body_make_sphere(float radius, const float *position, float density, int is_static, float restitution,
+                              float friction, pe_body_record *out);
+pe_status pe_body_make_box(float width, float height, float depth, const float *position, float density,
+                           int is_static, float restitution, float friction, pe_body_record *out);
+/* RigidBody::integrateVelocity / integratePosition / integrateRotation
+   (rigid_body.cpp:94-125) on a body value; no-ops for static or sleeping bodies. */
+enum { PE_INTEGRATE_VELOCITY = 0, PE_INTEGRATE_POSITION = 1, PE_INTEGRATE_ROTATION = 2 };
+pe_status pe_body_integrate(pe_body_record *body, int stage, const float *gravity, float dt);
+/* PhysicsWorld::addBody (physics_world.cpp:162-179): a body without colliders;
+   it enters awake (the reference calls wakeUp). */
+pe_status pe_world_add_body(pe_world *world, const pe_body_record *body, pe_handle *out);
+/* PhysicsWorld::getBody as a value, sleep flags included. */
+pe_status pe_world_get_body_record(pe_world *world, pe_handle body, pe_body_record *out);
+/* PhysicsWorld::getCollider (physics_world.cpp:315-339): the collider's body,
+   shape, dims (radius / half extents) and local transform; any output may be NULL. */
+pe_status pe_world_get_collider(pe_world *world, pe_handle collider, pe_handle *body, int *shape, float *dims,
+                                float *lpos, float *lrot);
+/* A write through the reference's Collider* (its fields are public): new body,
+   shape and local transform of a live collider.  A change of geometry wakes the
+   old and the new body, as prepareSleeping's collider comparison does
+   (physics_world.cpp:455-465); the device copy is refreshed before the next step. */
+pe_status pe_world_set_collider(pe_world *world, pe_handle collider, pe_handle body, int shape, const float *dims,
+                                const float *lpos, const float *lrot);
 /* isSleeping() of every body slot (0 for empty slots).  No reference counterpart. */
 pe_status pe_world_read_sleeping(pe_world *world, uint8_t *sleeping);
 /* RigidBody::integrateRotation (rigid_body.cpp:110-125) on one body; with
@@ -374,6 +410,14 @@ pe_status pe_rollout_backward(pe_rollout *rollout, const float *d_final_x, const
                               void *stream);
 /* Device time of the last forward and backward calls (ms). */
 pe_status pe_rollout_timings(pe_rollout *rollout, double *forward_ms, double *backward_ms);
+
+/* Failure detection, for tests (no reference counterpart).  Every spin-wait of
+   the step kernels (tile look-back, grid barrier, union retries, colouring
+   passes) is bounded by `limit` iterations on `device` (0 = the default,
+   2^24).  A wait that runs out makes its kernel return at once and the step
+   fail with PE_ERR_DEVICE ("a bounded wait timed out"); the world keeps the
+   state it had before that step. */
+pe_status pe_debug_set_spin_limit(int device, uint32_t limit);
 
 /* Allocation-free sweep-and-prune query.  It has no counterpart in the
    reference: it exists for callers that may not allocate device memory at all

@@ -508,6 +508,133 @@ pe_status pe_world_body_integrate_rotation(pe_world *world, pe_handle h, float d
     });
 }
 
+// ------------------------------------------------ RigidBody as a value ---
+namespace {
+void toRecord(const pe::HostBody &b, pe_body_record *out) {
+    std::memcpy(out->state.position, b.pos, sizeof(b.pos));
+    std::memcpy(out->state.rotation, b.rot, sizeof(b.rot));
+    std::memcpy(out->state.linear_velocity, b.lin, sizeof(b.lin));
+    std::memcpy(out->state.angular_velocity, b.ang, sizeof(b.ang));
+    std::memcpy(out->state.force, b.force, sizeof(b.force));
+    out->state.mass = b.mass;
+    out->state.restitution = b.restitution;
+    out->state.friction = b.friction;
+    out->state.is_static = b.isStatic ? 1 : 0;
+    std::memcpy(out->inv_inertia, b.iinv, sizeof(b.iinv));
+    out->sleeping = b.sleeping ? 1 : 0;
+    out->wake_requested = b.wakeRequested ? 1 : 0;
+}
+void fromRecord(const pe_body_record &r, pe::HostBody &b) {
+    std::memcpy(b.pos, r.state.position, sizeof(b.pos));
+    std::memcpy(b.rot, r.state.rotation, sizeof(b.rot));
+    std::memcpy(b.lin, r.state.linear_velocity, sizeof(b.lin));
+    std::memcpy(b.ang, r.state.angular_velocity, sizeof(b.ang));
+    std::memcpy(b.force, r.state.force, sizeof(b.force));
+    b.mass = r.state.mass;
+    b.restitution = r.state.restitution;
+    b.friction = r.state.friction;
+    b.isStatic = r.state.is_static != 0;
+    std::memcpy(b.iinv, r.inv_inertia, sizeof(b.iinv));
+    b.sleeping = r.sleeping != 0;
+    b.wakeRequested = r.wake_requested != 0;
+}
+pe_status makeRecord(int shape, const float *dims, const float *pos, float density, int isStatic, float restitution,
+                     float friction, pe_body_record *out) {
+    if (!dims || !pos || !out) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    pe::HostBody b;
+    if (const char *err = makeBody(shape, dims, pos, density, isStatic, restitution, friction, b))
+        return fail(PE_ERR_CREATE_FAILED, err);
+    toRecord(b, out);
+    return PE_OK;
+}
+} // namespace
+
+pe_status pe_body_make_sphere(float radius, const float *position, float density, int is_static, float restitution,
+                              float friction, pe_body_record *out) {
+    const float d[3] = {radius, 0.0f, 0.0f};
+    return makeRecord(PE_SHAPE_SPHERE, d, position, density, is_static, restitution, friction, out);
+}
+
+pe_status pe_body_make_box(float width, float height, float depth, const float *position, float density,
+                           int is_static, float restitution, float friction, pe_body_record *out) {
+    const float d[3] = {width, height, depth};
+    return makeRecord(PE_SHAPE_BOX, d, position, density, is_static, restitution, friction, out);
+}
+
+pe_status pe_body_integrate(pe_body_record *body, int stage, const float *gravity, float dt) {
+    if (!body || (stage == PE_INTEGRATE_VELOCITY && !gravity)) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    pe::HostBody b;
+    fromRecord(*body, b);
+    if (b.isStatic || b.sleeping) return PE_OK;
+    if (stage == PE_INTEGRATE_VELOCITY) {
+        // RigidBody::integrateVelocity (rigid_body.cpp:94-101)
+        const float im = b.mass <= 0.0f ? 0.0f : 1.0f / b.mass;
+        for (int k = 0; k < 3; ++k) {
+            const float acc = gravity[k] + b.force[k] * im;
+            b.lin[k] += acc * dt;
+        }
+    } else if (stage == PE_INTEGRATE_POSITION) {
+        // RigidBody::integratePosition (rigid_body.cpp:103-108)
+        for (int k = 0; k < 3; ++k) b.pos[k] += b.lin[k] * dt;
+    } else if (stage == PE_INTEGRATE_ROTATION) {
+        integrateRotation(b, dt);
+    } else {
+        return fail(PE_ERR_INVALID_ARGUMENT, "unknown integration stage");
+    }
+    toRecord(b, body);
+    return PE_OK;
+}
+
+pe_status pe_world_add_body(pe_world *world, const pe_body_record *body, pe_handle *out) {
+    if (!world || !body) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        pe::HostBody b;
+        fromRecord(*body, b);
+        uint32_t g;
+        const uint32_t i = world->w->addBody(b, g);
+        if (out) *out = pe_handle{i, g};
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_get_body_record(pe_world *world, pe_handle h, pe_body_record *out) {
+    if (!world || !out) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    return guarded([&] {
+        world->w->pull();
+        pe::HostBody *b = world->w->body(h.index, h.generation);
+        if (!b) return fail(PE_ERR_STALE_HANDLE, "stale body handle");
+        toRecord(*b, out);
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_get_collider(pe_world *world, pe_handle h, pe_handle *body, int *shape, float *dims, float *lpos,
+                                float *lrot) {
+    if (!world) return fail(PE_ERR_INVALID_ARGUMENT, "null world");
+    return guarded([&] {
+        pe::HostCollider *c = world->w->collider(h.index, h.generation);
+        if (!c) return fail(PE_ERR_STALE_HANDLE, "stale collider handle");
+        if (body) *body = pe_handle{c->body, c->bodyGeneration};
+        if (shape) *shape = (int)c->shape;
+        if (dims) std::memcpy(dims, c->dims, sizeof(c->dims));
+        if (lpos) std::memcpy(lpos, c->lpos, sizeof(c->lpos));
+        if (lrot) std::memcpy(lrot, c->lrot, sizeof(c->lrot));
+        return PE_OK;
+    });
+}
+
+pe_status pe_world_set_collider(pe_world *world, pe_handle h, pe_handle body, int shape, const float *dims,
+                                const float *lpos, const float *lrot) {
+    if (!world || !dims || !lpos || !lrot || (shape != PE_SHAPE_SPHERE && shape != PE_SHAPE_BOX))
+        return fail(PE_ERR_INVALID_ARGUMENT, "sphere or box collider expected");
+    return guarded([&] {
+        if (!world->w->setCollider(h.index, h.generation, body.index, body.generation, (uint32_t)shape, dims, lpos,
+                                   lrot))
+            return fail(PE_ERR_STALE_HANDLE, "stale collider handle");
+        return PE_OK;
+    });
+}
+
 pe_status pe_world_create_bodies(pe_world *world, uint32_t n, const uint8_t *shape, const float *dims,
                                  const float *position, const float *density, const uint8_t *is_static,
                                  const float *restitution, const float *friction, const float *linear_velocity,
@@ -1008,6 +1135,17 @@ pe_status pe_rollout_timings(pe_rollout *rollout, double *fwd, double *bwd) {
 namespace pe {
 void findPairsNoAlloc(int device, const float *mins, const float *maxs, uint32_t n, uint32_t *pairs,
                       uint32_t capacity, uint32_t *result, cudaStream_t s);
+}
+
+pe_status pe_debug_set_spin_limit(int device, uint32_t limit) {
+    return guarded([&] {
+        int previous = 0;
+        PE_CHECK(cudaGetDevice(&previous));
+        PE_CHECK(cudaSetDevice(device));
+        pe::setSpinLimit(limit);
+        PE_CHECK(cudaSetDevice(previous));
+        return PE_OK;
+    });
 }
 
 // Allocation-free SAP query for callers that may not allocate device memory;

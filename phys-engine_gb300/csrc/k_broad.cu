@@ -352,7 +352,7 @@ k_grid_body_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, c
                   const uint32_t *d_entries, uint32_t ecap, const unsigned long long *ekeys, const uint32_t *evals,
                   const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen, uint32_t *pairA,
                   uint32_t *pairB, uint32_t cap, DevStats *st, unsigned long long *state, uint32_t *counter) {
-    __shared__ uint32_t s_tile, s_scan[9], s_prefix;
+    __shared__ uint32_t s_tile, s_scan[9], s_prefix, s_abort;
     // Entries were not written this attempt (key width refused): nothing to scan.
     if (st->err & (kErrSmallPath | kErrEntryCapacity)) return;
     const uint32_t n = *in.d_n;
@@ -443,10 +443,15 @@ k_grid_body_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, c
         uint32_t total;
         const uint32_t local = blockExclusiveScan(kept, total, s_scan);
         if (threadIdx.x < 32) {
-            const uint32_t pre = lookbackExclusiveWarp(state, tile, total, &st->err);
-            if (threadIdx.x == 0) s_prefix = pre;
+            bool timedOut;
+            const uint32_t pre = lookbackExclusiveWarp(state, tile, total, &st->err, &timedOut);
+            if (threadIdx.x == 0) {
+                s_prefix = pre;
+                s_abort = timedOut ? 1u : 0u;
+            }
         }
         __syncthreads();
+        if (s_abort) return;  // a bounded wait ran out: nothing of this tile is written
         uint32_t o = s_prefix + local;
         for (uint32_t j = 0; j < m; ++j) {
             const uint32_t sb = inSlot ? inSlot[part[j]] : part[j];
@@ -595,7 +600,7 @@ k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const
               const uint32_t *evals, const uint32_t *enext, const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen,
               uint32_t *pairA, uint32_t *pairB, uint32_t cap, DevStats *st, unsigned long long *state,
               uint32_t *counter) {
-    __shared__ uint32_t s_tile, s_scan[9], s_prefix;
+    __shared__ uint32_t s_tile, s_scan[9], s_prefix, s_abort;
     // Out-of-range cells or too few entry slots: the host re-runs the step.
     if ((st->err & kErrHashRange) || st->gridEntryCount > ecap) return;
     const uint32_t n = *in.d_n;
@@ -729,10 +734,15 @@ k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const
         uint32_t total;
         const uint32_t local = blockExclusiveScan(kept, total, s_scan);
         if (threadIdx.x < 32) {
-            const uint32_t pre = lookbackExclusiveWarp(state, tile, total, &st->err);
-            if (threadIdx.x == 0) s_prefix = pre;
+            bool timedOut;
+            const uint32_t pre = lookbackExclusiveWarp(state, tile, total, &st->err, &timedOut);
+            if (threadIdx.x == 0) {
+                s_prefix = pre;
+                s_abort = timedOut ? 1u : 0u;
+            }
         }
         __syncthreads();
+        if (s_abort) return;  // a bounded wait ran out: nothing of this tile is written
         uint32_t o = s_prefix + local;
         for (uint32_t j = 0; j < kept; ++j, ++o) {
             if (o < cap) {
@@ -982,5 +992,7 @@ void launchPairsFinalize(const uint32_t *inSlot, const uint32_t *cbody, const ui
                                                     pb.pos, pb.a, pb.b);
     PE_LAUNCHED();
 }
+
+void setSpinLimitBroad(uint32_t limit) { setSpinLimitOfUnit(limit); }
 
 } // namespace pe

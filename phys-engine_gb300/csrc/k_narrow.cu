@@ -22,7 +22,7 @@ __global__ void __launch_bounds__(kNarrowThreads)
 k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *__restrict__ pairB,
               const uint32_t *d_pairs, ManifoldView out, uint32_t mcap, DevStats *st, unsigned long long *state,
               uint32_t *counter) {
-    __shared__ uint32_t s_tile, s_scan[9], s_prefix;
+    __shared__ uint32_t s_tile, s_scan[9], s_prefix, s_abort;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->stamp[2] = globalNs();
     const uint32_t P = min(*d_pairs, mcap);
     const uint32_t ntiles = max((P + kNarrowThreads - 1) / kNarrowThreads, 1u);
@@ -50,10 +50,15 @@ k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *_
     uint32_t total;
     const uint32_t local = blockExclusiveScan(hit ? 1u : 0u, total, s_scan);
     if (threadIdx.x < 32) {
-        const uint32_t pre = lookbackExclusiveWarp(state, tile, total, &st->err);
-        if (threadIdx.x == 0) s_prefix = pre;
+        bool timedOut;
+        const uint32_t pre = lookbackExclusiveWarp(state, tile, total, &st->err, &timedOut);
+        if (threadIdx.x == 0) {
+            s_prefix = pre;
+            s_abort = timedOut ? 1u : 0u;
+        }
     }
     __syncthreads();
+    if (s_abort) return;  // a bounded wait ran out: nothing of this tile is written
     const uint32_t m = s_prefix + local;
     if (hit) {
         if (m < mcap) storeManifold(out, m, w, ca, cb, ba, bb, lm, restitution, friction);
@@ -129,5 +134,7 @@ void launchGeneratePairs(const float4 *in, float4 *out, uint32_t n, cudaStream_t
     k_generate_pairs<<<(n + 127) / 128, 128, 0, s>>>(in, out, n);
     PE_LAUNCHED();
 }
+
+void setSpinLimitNarrow(uint32_t limit) { setSpinLimitOfUnit(limit); }
 
 } // namespace pe

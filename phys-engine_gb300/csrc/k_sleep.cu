@@ -44,7 +44,7 @@ __device__ __forceinline__ uint32_t sleepFind(const uint32_t *parent, uint32_t i
 }
 
 __device__ __forceinline__ void sleepUnite(uint32_t *parent, uint32_t a, uint32_t b, uint32_t nb, uint32_t *err) {
-    for (uint32_t spins = 0; spins < kSpinLimit; ++spins) {
+    for (uint32_t spins = 0; spins < spinLimit(); ++spins) {
         a = sleepFind(parent, a, nb);
         b = sleepFind(parent, b, nb);
         if (a == b) return;
@@ -324,5 +324,7 @@ void launchCacheCarry(const WorldView &w, const CacheView &oldCache, const uint3
                                               newCount, cap, st);
     PE_LAUNCHED();
 }
+
+void setSpinLimitSleep(uint32_t limit) { setSpinLimitOfUnit(limit); }
 
 } // namespace pe

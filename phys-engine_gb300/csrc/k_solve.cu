@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
     }
     if (blockIdx.x == 0)
         for (int c = threadIdx.x; c < kMaxColors; c += blockDim.x) sb.colorCount[c] = 0;
-    gridBarrier(sb.bar, &a.st->err);
+    if (!gridBarrier(sb.bar, &a.st->err)) return;
     // each dynamic body's manifolds
     for (uint32_t m = gtid; m < M; m += gstride) {
         const uint32_t d = sb.dyn[m];
@@ -69,11 +69,11 @@ __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
             else sb.counters[1] = 1u;
         }
     }
-    gridBarrier(sb.bar, &a.st->err);
+    if (!gridBarrier(sb.bar, &a.st->err)) return;
     if (__ldcg(&sb.counters[1]) == 0u) {
         uint32_t pass = 0;
         bool pending = true;
-        for (; pending && pass < kSpinLimit; ++pass) {
+        for (; pending && pass < spinLimit(); ++pass) {
             pending = false;
             for (uint32_t m = gtid; m < M; m += gstride) {
                 if (sb.color[m] != kUncolored) continue;
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
                 if (d & 1u) atomicMax(&sb.bodyBest[a.mv.bodyA[m]], p);
                 if (d & 2u) atomicMax(&sb.bodyBest[a.mv.bodyB[m]], p);
             }
-            gridBarrier(sb.bar, &a.st->err);
+            if (!gridBarrier(sb.bar, &a.st->err)) return;
             for (uint32_t m = gtid; m < M; m += gstride) {
                 if (sb.color[m] != kUncolored) continue;
                 const unsigned long long p = stamp | colorPriority(m);
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
                 }
                 aggregatedAppend(&sb.counters[0]);
             }
-            gridBarrier(sb.bar, &a.st->err);
+            if (!gridBarrier(sb.bar, &a.st->err)) return;
             if (__ldcg(&sb.counters[0]) >= M) break;
         }
         rounds += round + 1;
@@ -200,12 +200,12 @@ __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
                 __stcg(&sb.bodyUsed[2 * a.mv.bodyB[m] + 1], 0ull);
             }
         }
-        gridBarrier(sb.bar, &a.st->err);
+        if (!gridBarrier(sb.bar, &a.st->err)) return;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             sb.counters[0] = M - deferred;
             sb.counters[2] = 0;
         }
-        gridBarrier(sb.bar, &a.st->err);
+        if (!gridBarrier(sb.bar, &a.st->err)) return;
     }
     if (exhausted) {
         // The step fails (kErrColors); colour 0 for what is left keeps every
@@ -297,7 +297,7 @@ __global__ void k_cache_counts(SolveArgs a) {
         const bool valid = ia < w.nb && ib < w.nb && (w.bflags[ia] & kBodyAlive) && (w.bflags[ib] & kBodyAlive) &&
                            w.bgen[ia] == a.mv.genA[m] && w.bgen[ib] == a.mv.genB[m] &&
                            solvedPair(w, w.bflags[ia], w.bflags[ib]);
-        a.sb.cacheCounts[k] = valid ? a.mv.pointCount[m] : 0u;
+        a.sb.cacheCounts[k] = valid ? min(a.mv.pointCount[m], 4u) : 0u;
     }
 }
 // Writes the cache entries of manifold m (npts points) starting at entry base.
@@ -449,5 +449,7 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
     k_cache_write<<<gridFor(mcap), 256, 0, s>>>(a, newCache, cacheCap);
     PE_LAUNCHED();
 }
+
+void setSpinLimitSolve(uint32_t limit) { setSpinLimitOfUnit(limit); }
 
 } // namespace pe

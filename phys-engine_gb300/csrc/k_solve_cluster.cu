@@ -173,7 +173,7 @@ __device__ void solveClusterCache(const SolveArgs &a, const CacheView &nc, uint3
     // order): every rank scans the point counts and writes its share.
     uint32_t *s_cnt = reinterpret_cast<uint32_t *>(smem);
     for (uint32_t i = tid; i < M; i += nt)
-        s_cnt[i] = (__ldcg(&sb.dyn[i]) & kFlagValid) ? a.mv.pointCount[i] : 0u;
+        s_cnt[i] = (__ldcg(&sb.dyn[i]) & kFlagValid) ? min(a.mv.pointCount[i], 4u) : 0u;
     __syncthreads();
     const uint32_t total = blockExclusiveScanArray(s_cnt, M, cs.solve.scan);
     for (uint32_t i = rank + kClusterRanks * tid; i < M; i += kClusterRanks * nt) {

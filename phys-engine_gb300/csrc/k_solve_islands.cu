@@ -13,18 +13,22 @@
 //   k_isl_count : each solved manifold's island and slot in it; islands listed
 //   k_isl_fill  : manifolds into their islands' lists (offsets from a scan);
 //                 islands of 32 manifolds or more queued before the others
-//   k_isl_solve : one warp per island (those of 32 manifolds or more first,
-//                 from a queue): the island's manifolds sorted by (colour,
-//                 index), then warm start and iterations colour by colour with
-//                 __syncwarp; islands of fewer than kIslThread manifolds one
-//                 per thread, manifold after manifold in that order (a stack
-//                 of two boxes would leave 30 lanes idle); manifolds without a
-//                 dynamic body (nothing to share) are solved alone
-//   k_isl_solve_large : when some island has kIslLarge manifolds or more, all
-//                 islands together in grid-wide colour sweeps instead: the
-//                 manifolds bucketed by colour, a grid barrier per colour.
-//                 Manifolds of one colour share no dynamic body, so their
-//                 order inside a colour does not change the result.
+//   k_isl_solve : islands of kIslBlock to kIslBlockMax manifolds one thread
+//                 block each (a pyramid of boxes), sorted by (colour, index) in
+//                 shared memory and swept colour by colour with __syncthreads;
+//                 then one warp per smaller island (those of 32 manifolds or
+//                 more first, from a queue), swept with __syncwarp; islands of
+//                 fewer than kIslThread manifolds one per thread, manifold
+//                 after manifold in that order (a stack of two boxes would
+//                 leave 30 lanes idle); manifolds without a dynamic body
+//                 (nothing to share) are solved alone
+//   k_isl_solve_large : when some island has more than kIslBlockMax
+//                 manifolds (a settled pile), all islands together in
+//                 grid-wide colour sweeps instead: the manifolds bucketed by
+//                 colour, a grid barrier per colour.  Manifolds of one colour
+//                 share no dynamic body, so their order inside a colour does
+//                 not change the result.
+#include "pe_block.cuh"
 #include "pe_kernels.cuh"
 #include "pe_prims.cuh"
 #include "pe_solve.cuh"
@@ -37,19 +41,23 @@ namespace {
 constexpr int kIslThreads = 128;           // four warps per block
 constexpr uint32_t kIslWarpSort = 1024;    // island keys sorted in shared memory up to this size
 constexpr uint32_t kIslNone = 0xFFFFFFFFu;
-// An island of this many manifolds (a settled pile; one warp would take it
-// colour by colour 32 manifolds at a time) sends every island of the step to
-// the grid-wide sweeps: measured on piles of 5,000 and 10,000 bodies, keeping
-// the smaller islands on warps only adds their sweep time to the grid's.
-constexpr uint32_t kIslLarge = 512;
+// Islands of kIslBlock manifolds or more are swept by a whole thread block
+// (one warp would take them colour by colour 32 manifolds at a time), up to
+// kIslBlockMax manifolds (the block's shared key buffer).  An island above
+// that (a settled pile of thousands of bodies) sends every island of the step
+// to the grid-wide sweeps: measured on piles of 5,000 and 10,000 bodies,
+// keeping the smaller islands apart only adds their sweep time to the grid's.
+constexpr uint32_t kIslBlock = 512;
+constexpr uint32_t kIslBlockMax = 4 * kIslWarpSort;
 constexpr uint32_t kIslThread = 8;         // islands of fewer manifolds: one thread each
 // islCounters: [0] islands, [1] lone manifolds (solved, no dynamic body), [2]
-// work queue of k_isl_solve, [3] listed manifolds, [4] / [5] islands of 32
+// work queue of the warp items, [3] listed manifolds, [4] / [5] islands of 32
 // manifolds or more / kIslThread to 31 queued, [6] smaller islands, [7] set
-// when an island reached kIslLarge manifolds; [kIslColorCount + c] manifolds
-// of colour c in the grid-wide sweeps, [kIslColorFill + c] their fill cursors
-constexpr uint32_t kIslColorCount = 8;
-constexpr uint32_t kIslColorFill = 8 + kMaxColors;
+// when an island exceeds kIslBlockMax manifolds, [8] block islands queued,
+// [9] work queue of the block islands; [kIslColorCount + c] manifolds of
+// colour c in the grid-wide sweeps, [kIslColorFill + c] their fill cursors
+constexpr uint32_t kIslColorCount = 10;
+constexpr uint32_t kIslColorFill = 10 + kMaxColors;
 static_assert(kIslColorFill + kMaxColors == kIslCounterWords, "island counter layout");
 
 inline uint32_t islGrid(uint32_t n) {
@@ -74,7 +82,7 @@ __device__ __forceinline__ uint32_t islFind(uint32_t *par, uint32_t i, uint32_t 
 }
 
 __device__ __forceinline__ void islUnite(uint32_t *par, uint32_t a, uint32_t b, uint32_t nb, uint32_t *err) {
-    for (uint32_t spins = 0; spins < kSpinLimit; ++spins) {
+    for (uint32_t spins = 0; spins < spinLimit(); ++spins) {
         a = islFind(par, a, nb);
         b = islFind(par, b, nb);
         if (a == b) return;
@@ -137,7 +145,7 @@ __global__ void k_isl_count(SolveArgs a) {
             root = islFind(par, (fl & kFlagDynA) ? a.mv.bodyA[m] : a.mv.bodyB[m], a.w.nb);
             const uint32_t pos = aggregatedAppendKeyed(cnt, root);
             a.sb.islSlot[m] = pos;
-            if (pos + 1 == kIslLarge) a.sb.islCounters[7] = 1u;
+            if (pos == kIslBlockMax) a.sb.islCounters[7] = 1u;
             if (pos == 0) a.sb.islRoots[aggregatedAppend(&a.sb.islCounters[0])] = root;
         } else if (fl & kFlagValid) {
             a.sb.islLone[aggregatedAppend(&a.sb.islCounters[1])] = m;
@@ -168,13 +176,15 @@ __global__ void k_isl_fill(SolveArgs a) {
     }
     // the warp queue: islands of 32 manifolds or more at the front (a warp's
     // lanes all busy; they bound the sweep), those of kIslThread to 31 from
-    // the back; smaller ones to the per-thread list
+    // the back; smaller ones to the per-thread list, islands of kIslBlock or
+    // more to the block list (the per-thread list's area, from its end)
     uint32_t *queue = reinterpret_cast<uint32_t *>(a.sb.islKeys), *tiny = queue + a.mcap;
     const uint32_t nIsl = a.sb.islCounters[0];
     for (uint32_t i = t; i < nIsl; i += stride) {
         const uint32_t r = a.sb.islRoots[i];
         if (cnt[r] >= sweepFrom) continue;
-        if (cnt[r] >= 32) queue[aggregatedAppend(&a.sb.islCounters[4])] = r;
+        if (cnt[r] >= kIslBlock) tiny[a.mcap - 1 - aggregatedAppend(&a.sb.islCounters[8])] = r;
+        else if (cnt[r] >= 32) queue[aggregatedAppend(&a.sb.islCounters[4])] = r;
         else if (cnt[r] >= kIslThread) queue[nIsl - 1 - aggregatedAppend(&a.sb.islCounters[5])] = r;
         else tiny[aggregatedAppend(&a.sb.islCounters[6])] = r;
     }
@@ -203,7 +213,56 @@ __device__ __forceinline__ void warpBitonicSort(unsigned long long *keys, uint32
 __global__ void __launch_bounds__(kIslThreads) k_isl_solve(SolveArgs a) {
     __shared__ unsigned long long s_keys[kIslThreads / 32][kIslWarpSort];
     __shared__ uint32_t s_start[kIslThreads / 32][kMaxColors + 1];
+    __shared__ uint32_t s_item;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // islands of kIslBlock manifolds or more: one block each
+    {
+        const uint32_t nBlock = a.sb.islCounters[8];
+        const uint32_t *blockList = reinterpret_cast<const uint32_t *>(a.sb.islKeys) + a.mcap;
+        unsigned long long *keys = &s_keys[0][0];  // kIslBlockMax keys
+        uint32_t *start = s_start[0];
+        for (;;) {
+            if (threadIdx.x == 0) s_item = atomicAdd(&a.sb.islCounters[9], 1u);
+            __syncthreads();
+            const uint32_t item = s_item;
+            if (item >= nBlock) break;
+            const uint32_t r = blockList[a.mcap - 1 - item];
+            const uint32_t n = islCnt(a)[r], base = a.sb.islOff[r];
+            const uint32_t n2 = nextPow2(n);
+            for (uint32_t j = threadIdx.x; j < n2; j += blockDim.x) {
+                unsigned long long key = ~0ull;
+                if (j < n) {
+                    const uint32_t m = a.sb.islList[base + j];
+                    key = ((unsigned long long)a.sb.color[m] << 32) | m;
+                }
+                keys[j] = key;
+            }
+            __syncthreads();
+            blockBitonicSort(keys, n2);
+            // colour ranges [start[c], start[c + 1])
+            const uint32_t lastColor = (uint32_t)(keys[n - 1] >> 32);
+            const uint32_t C = lastColor < (uint32_t)kMaxColors ? lastColor + 1 : (uint32_t)kMaxColors;
+            for (uint32_t c = threadIdx.x; c <= C; c += blockDim.x) {
+                uint32_t lo = 0, hi = n;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if ((uint32_t)(keys[mid] >> 32) < c) lo = mid + 1;
+                    else hi = mid;
+                }
+                start[c] = lo;
+            }
+            __syncthreads();
+            for (int pass = 0; pass <= a.iterations; ++pass)
+                for (uint32_t c = 0; c < C; ++c) {
+                    for (uint32_t j = start[c] + threadIdx.x; j < start[c + 1]; j += blockDim.x) {
+                        const uint32_t m = (uint32_t)(keys[j] & 0xFFFFFFFFull);
+                        if (pass == 0) warmStartOne(a, j, m);
+                        else solveOneChained(a, j, m);
+                    }
+                    __syncthreads();
+                }
+        }
+    }
     const uint32_t nIsl = a.sb.islCounters[0];
     const uint32_t nFront = a.sb.islCounters[4], nWarp = nFront + a.sb.islCounters[5], nTiny = a.sb.islCounters[6];
     const uint32_t nItems = nWarp + (nTiny + 31) / 32;
@@ -312,7 +371,7 @@ __device__ void islSolveWide(const SolveArgs &a, uint32_t M, uint32_t C) {
             __syncthreads();
         }
     }
-    gridBarrier(a.sb.bar, &a.st->err);
+    if (!gridBarrier(a.sb.bar, &a.st->err)) return;
     const uint32_t *cnt = islCnt(a);
     uint32_t *list = reinterpret_cast<uint32_t *>(a.sb.islKeysTmp);
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
@@ -322,7 +381,7 @@ __device__ void islSolveWide(const SolveArgs &a, uint32_t M, uint32_t C) {
         if (r == kIslNone || cnt[r] == 0 || c >= C) continue;
         list[aggregatedAppendKeyed(cur, c)] = m;
     }
-    gridBarrier(a.sb.bar, &a.st->err);
+    if (!gridBarrier(a.sb.bar, &a.st->err)) return;
     for (int pass = 0; pass <= a.iterations; ++pass)
         for (uint32_t c = 0; c < C; ++c) {
             const uint32_t lo = c ? __ldcg(&cur[c - 1]) : 0u, hi = __ldcg(&cur[c]);
@@ -330,7 +389,7 @@ __device__ void islSolveWide(const SolveArgs &a, uint32_t M, uint32_t C) {
                 if (pass == 0) warmStartOne(a, k, list[k]);
                 else solveOne(a, k, list[k]);
             }
-            gridBarrier(a.sb.bar, &a.st->err);
+            if (!gridBarrier(a.sb.bar, &a.st->err)) return;
         }
 }
 
@@ -363,11 +422,11 @@ __global__ void __launch_bounds__(kSolveThreads) k_isl_solve_large(SolveArgs a) 
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
     for (uint32_t m = gtid; m < M; m += gstride) {
         const uint32_t r = a.sb.islRoot[m];
-        if (r == kIslNone || cnt[r] < sweepFrom) continue;
         const uint32_t c = a.sb.color[m];
+        if (r == kIslNone || cnt[r] < sweepFrom || c >= (uint32_t)kMaxColors) continue;
         list[s_start[c] + aggregatedAppendKeyed(fill, c)] = m;
     }
-    gridBarrier(a.sb.bar, &a.st->err);
+    if (!gridBarrier(a.sb.bar, &a.st->err)) return;
     for (int pass = 0; pass <= a.iterations; ++pass)
         for (int c = 0; c < kMaxColors; ++c) {
             if (s_start[c] == s_start[c + 1]) continue;
@@ -375,7 +434,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_isl_solve_large(SolveArgs a) 
                 if (pass == 0) warmStartOne(a, k, list[k]);
                 else solveOne(a, k, list[k]);
             }
-            gridBarrier(a.sb.bar, &a.st->err);
+            if (!gridBarrier(a.sb.bar, &a.st->err)) return;
         }
 }
 
@@ -414,5 +473,7 @@ void launchSolveIslands(const SolveArgs &a, int coopBlocks, Scratch &ws, cudaStr
     PE_CHECK(cudaLaunchKernelExC(&cfg, (const void *)k_isl_solve_large, params));
     PE_LAUNCHED();
 }
+
+void setSpinLimitIslands(uint32_t limit) { setSpinLimitOfUnit(limit); }
 
 } // namespace pe

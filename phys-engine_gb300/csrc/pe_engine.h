@@ -24,6 +24,16 @@ struct CudaError : std::runtime_error {
 // launch and counts it (the count is reported per step).
 extern unsigned long long g_kernelLaunches;
 
+// Iteration limit of the bounded waits on the current device (0 = the
+// default); each setSpinLimit* writes one translation unit's copy.
+void setSpinLimit(uint32_t limit);
+void setSpinLimitPrims(uint32_t limit);
+void setSpinLimitBroad(uint32_t limit);
+void setSpinLimitNarrow(uint32_t limit);
+void setSpinLimitSleep(uint32_t limit);
+void setSpinLimitSolve(uint32_t limit);
+void setSpinLimitIslands(uint32_t limit);
+
 // Streaming multiprocessors of the current device (queried once per device and
 // cached); launch sizes of the persistent and grid-stride kernels scale with it.
 int smCount();

@@ -4,8 +4,8 @@
 // already running).  Element counts may live in device memory so that the
 // launches are fixed-size and graph-capturable; blocks past the live count
 // exit at once.  Every spin-wait is bounded: on timeout the kernel records an
-// error flag and finishes without waiting (results are then invalid and the
-// host reports PE_ERR_TIMEOUT).
+// error flag and returns without publishing or writing anything further (the
+// host then fails the step).
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -21,7 +21,22 @@ constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortRounds = 8;
 constexpr int kSortTile = kSortThreads * kSortRounds;      // 2048
-constexpr uint32_t kSpinLimit = 1u << 24;
+// Iteration limit of every bounded wait (tile look-back, grid barrier, union
+// retries, colouring passes).  Each translation unit holds its own
+// __constant__ copy; setSpinLimit (prims.cu) writes all of them on the current
+// device, and the waits read it at run time, so captured graphs see a change.
+// A wait that runs out sets kErrTimeout, publishes nothing and its kernel
+// returns at once; the step then fails with "a bounded wait timed out" and the
+// world keeps its state from before the step.
+constexpr uint32_t kSpinLimitDefault = 1u << 24;
+namespace {
+__constant__ uint32_t c_spinLimit = kSpinLimitDefault;
+// Writes this translation unit's copy of the limit (host side).
+inline void setSpinLimitOfUnit(uint32_t limit) {
+    PE_CHECK(cudaMemcpyToSymbol(c_spinLimit, &limit, sizeof(limit)));
+}
+} // namespace
+__device__ __forceinline__ uint32_t spinLimit() { return c_spinLimit; }
 
 
 __device__ __forceinline__ uint32_t ldvol(const uint32_t *p) { return *(volatile const uint32_t *)p; }
@@ -35,9 +50,12 @@ __device__ __forceinline__ unsigned long long ldvol64(const unsigned long long *
 // 32 predecessors at once (lane i: tile - 1 - base - i) and sums them up to the
 // nearest inclusive prefix, so a walk over many finished tiles costs one
 // memory round trip per 32 tiles.  Publishes the tile's inclusive prefix; every
-// lane returns the exclusive prefix.
+// lane returns the exclusive prefix.  If the wait runs out, *timedOut is set
+// on every lane, kErrTimeout is raised and no prefix is published (the tiles
+// after this one run out as well); the caller's block then returns.
 __device__ __forceinline__ uint32_t lookbackExclusiveWarp(unsigned long long *state, uint32_t tile,
-                                                          uint32_t aggregate, uint32_t *err) {
+                                                          uint32_t aggregate, uint32_t *err, bool *timedOut) {
+    *timedOut = false;
     const uint32_t lane = threadIdx.x & 31;
     if (tile == 0) {
         if (lane == 0) atomicExch(&state[0], (2ull << 32) | aggregate);
@@ -56,9 +74,10 @@ __device__ __forceinline__ uint32_t lookbackExclusiveWarp(unsigned long long *st
         const uint32_t first = done & (0u - done);           // nearest inclusive prefix
         const uint32_t upto = done ? (first << 1) - 1u : 0xffffffffu;
         if (zero & upto) {
-            if (++spins > kSpinLimit) {
+            if (++spins > spinLimit()) {
                 if (lane == 0) atomicOr(err, kErrTimeout);
-                break;
+                *timedOut = true;
+                return 0;
             }
             continue;
         }
@@ -113,11 +132,15 @@ __device__ __forceinline__ uint32_t takeTile(uint32_t *counter, uint32_t *slot) 
 }
 
 // Grid-wide barrier for cooperative launches (all blocks co-resident).  bar[0]
-// counts arrivals, bar[1] is the generation.  Bounded spin; on timeout the
-// error flag is set and the block continues.
-__device__ __forceinline__ void gridBarrier(uint32_t *bar, uint32_t *err) {
+// counts arrivals, bar[1] is the generation.  Bounded spin: returns false on
+// every thread of the block when its wait ran out (kErrTimeout raised), and
+// the caller returns from the kernel at once.  The counters are reset before
+// every launch that uses them.
+__device__ __forceinline__ bool gridBarrier(uint32_t *bar, uint32_t *err) {
+    __shared__ uint32_t s_barrierTimedOut;
     __syncthreads();
     if (threadIdx.x == 0) {
+        s_barrierTimedOut = 0;
         uint32_t gen = ldvol(&bar[1]);
         __threadfence();
         uint32_t arrived = atomicAdd(&bar[0], 1u);
@@ -128,8 +151,9 @@ __device__ __forceinline__ void gridBarrier(uint32_t *bar, uint32_t *err) {
         } else {
             uint32_t spins = 0;
             while (ldvol(&bar[1]) == gen) {
-                if (++spins > kSpinLimit) {
+                if (++spins > spinLimit()) {
                     atomicOr(err, kErrTimeout);
+                    s_barrierTimedOut = 1;
                     break;
                 }
             }
@@ -137,6 +161,7 @@ __device__ __forceinline__ void gridBarrier(uint32_t *bar, uint32_t *err) {
         __threadfence();
     }
     __syncthreads();
+    return s_barrierTimedOut == 0;
 }
 
 } // namespace pe

@@ -139,7 +139,7 @@ __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t
     for (uint32_t q = begin; q < 4 * M; q += stride) {
         const uint32_t p = q / M, m = q - p * M;
         const uint32_t k = m;  // data index
-        const uint32_t npts = a.mv.pointCount[m];
+        const uint32_t npts = min(a.mv.pointCount[m], 4u);
         const uint32_t live = npts < 4u ? npts : 4u;  // live points (at most four)
         if (p > 0 && p >= live) continue;
         const uint32_t ia = a.mv.bodyA[m], ib = a.mv.bodyB[m];
@@ -897,7 +897,7 @@ __device__ inline void solveBlockCache(const SolveArgs &a, const CacheView &nc, 
             const bool valid = ia < w.nb && ib < w.nb && (w.bflags[ia] & kBodyAlive) && (w.bflags[ib] & kBodyAlive) &&
                                w.bgen[ia] == a.mv.genA[i] && w.bgen[ib] == a.mv.genB[i] &&
                                solvedPair(w, w.bflags[ia], w.bflags[ib]);
-            s_dyn[i] = valid ? a.mv.pointCount[i] : 0u;
+            s_dyn[i] = valid ? min(a.mv.pointCount[i], 4u) : 0u;
         }
         __syncthreads();
         const uint32_t total = blockExclusiveScanArray(s_dyn, M, s_scan);
@@ -926,7 +926,7 @@ __device__ inline void solveBlockCache(const SolveArgs &a, const CacheView &nc, 
         const bool valid = ia < w.nb && ib < w.nb && (w.bflags[ia] & kBodyAlive) && (w.bflags[ib] & kBodyAlive) &&
                            w.bgen[ia] == a.mv.genA[m] && w.bgen[ib] == a.mv.genB[m] &&
                            solvedPair(w, w.bflags[ia], w.bflags[ib]);
-        s_dyn[i] = valid ? a.mv.pointCount[m] : 0u;
+        s_dyn[i] = valid ? min(a.mv.pointCount[m], 4u) : 0u;
     }
     __syncthreads();
     const uint32_t total = blockExclusiveScanArray(s_dyn, M, s_scan);

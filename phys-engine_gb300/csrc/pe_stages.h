@@ -147,10 +147,11 @@ void launchExpandForces(const float *f3, const uint32_t *bflags, float4 *force, 
 // warm-start cache from the carried sleeping entries of the old cache and
 // the solver's entries (written to tmp).
 struct SolveArgs;
-// The multi-kernel path's sweeps island by island (after k_color and prepare);
-// islands of kIslLarge manifolds or more in grid-wide colour sweeps (a
-// cooperative launch of at most coopBlocks blocks).
-constexpr uint32_t kIslCounterWords = 8 + 2 * kMaxColors;
+// The multi-kernel path's sweeps island by island (after k_color and prepare):
+// a thread, a warp or a block per island by its size; once an island is too
+// large for a block, every island in grid-wide colour sweeps (a cooperative
+// launch of at most coopBlocks blocks).
+constexpr uint32_t kIslCounterWords = 10 + 2 * kMaxColors;
 void launchSolveIslands(const SolveArgs &a, int coopBlocks, Scratch &ws, cudaStream_t s);
 void launchSleepWake(const WorldView &w, const ManifoldView &mv, uint32_t Mhost, uint32_t mcap, uint32_t *flags,
                      float *quiet, uint32_t *err, cudaStream_t s);

@@ -15,6 +15,18 @@ namespace pe {
 
 unsigned long long g_kernelLaunches = 0;
 
+void setSpinLimitPrims(uint32_t limit) { setSpinLimitOfUnit(limit); }
+
+void setSpinLimit(uint32_t limit) {
+    if (limit == 0) limit = kSpinLimitDefault;
+    setSpinLimitPrims(limit);
+    setSpinLimitBroad(limit);
+    setSpinLimitNarrow(limit);
+    setSpinLimitSleep(limit);
+    setSpinLimitSolve(limit);
+    setSpinLimitIslands(limit);
+}
+
 int smCount() {
     constexpr int kMaxDevices = 64;
     static std::atomic<int> cached[kMaxDevices] = {};
@@ -47,7 +59,7 @@ __device__ __forceinline__ uint32_t liveCount(const uint32_t *d_n, uint32_t cap)
 __global__ void __launch_bounds__(kScanThreads)
 k_scan_exclusive(const uint32_t *in, uint32_t *out, const uint32_t *d_n, uint32_t cap, unsigned long long *state,
                  uint32_t *counter, uint32_t *total, uint32_t *err) {
-    __shared__ uint32_t s_tile, s_scan[9], s_prefix;
+    __shared__ uint32_t s_tile, s_scan[9], s_prefix, s_abort;
     const uint32_t n = liveCount(d_n, cap);
     const uint32_t ntiles = max((n + kScanTile - 1) / kScanTile, 1u);
     for (;;) {
@@ -64,10 +76,15 @@ k_scan_exclusive(const uint32_t *in, uint32_t *out, const uint32_t *d_n, uint32_
         uint32_t agg;
         const uint32_t excl = blockExclusiveScan(sum, agg, s_scan);
         if (threadIdx.x < 32) {
-            const uint32_t pre = lookbackExclusiveWarp(state, tile, agg, err);
-            if (threadIdx.x == 0) s_prefix = pre;
+            bool timedOut;
+            const uint32_t pre = lookbackExclusiveWarp(state, tile, agg, err, &timedOut);
+            if (threadIdx.x == 0) {
+                s_prefix = pre;
+                s_abort = timedOut ? 1u : 0u;
+            }
         }
         __syncthreads();
+        if (s_abort) return;  // a bounded wait ran out: nothing of this tile is written
         uint32_t run = s_prefix + excl;
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k) {
@@ -123,7 +140,7 @@ __global__ void __launch_bounds__(kSortThreads)
 k_radix_pass(K *buf0, K *buf1, uint32_t *vbuf0, uint32_t *vbuf1, const uint32_t *d_n, uint32_t cap, int shift,
              const uint32_t *__restrict__ hist, uint32_t *state, uint32_t *counter, uint32_t *sel, int pass,
              uint32_t *err) {
-    __shared__ uint32_t s_tile, s_trivial;
+    __shared__ uint32_t s_tile, s_trivial, s_abort;
     __shared__ uint32_t s_warp[kSortWarps][256];
     __shared__ uint32_t s_tileStart[256];
     __shared__ uint32_t s_base[256];
@@ -159,6 +176,7 @@ k_radix_pass(K *buf0, K *buf1, uint32_t *vbuf0, uint32_t *vbuf1, const uint32_t 
         if (tile >= ntiles) return;
         const uint32_t base = tile * kSortTile;
         for (int i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads) (&s_warp[0][0])[i] = 0;
+        if (threadIdx.x == 0) s_abort = 0;
         __syncthreads();
 
         K key[kSortRounds];
@@ -198,12 +216,15 @@ k_radix_pass(K *buf0, K *buf1, uint32_t *vbuf0, uint32_t *vbuf1, const uint32_t 
             atomicExch(&state[tile * 256 + d], (1u << 30) | cnt);
             int64_t t = (int64_t)tile - 1;
             uint32_t spins = 0;
+            bool timedOut = false;
             while (t >= 0) {
                 const uint32_t v = ldvol(&state[t * 256 + d]);
                 const uint32_t f = v >> 30;
                 if (f == 0) {
-                    if (++spins > kSpinLimit) {
+                    if (++spins > spinLimit()) {
                         atomicOr(err, kErrTimeout);
+                        s_abort = 1;
+                        timedOut = true;
                         break;
                     }
                     continue;
@@ -212,10 +233,12 @@ k_radix_pass(K *buf0, K *buf1, uint32_t *vbuf0, uint32_t *vbuf1, const uint32_t 
                 if (f == 2) break;
                 --t;
             }
-            atomicExch(&state[tile * 256 + d], (2u << 30) | (prefix + cnt));
+            // a digit whose wait ran out publishes nothing
+            if (!timedOut) atomicExch(&state[tile * 256 + d], (2u << 30) | (prefix + cnt));
         }
         s_base[d] = s_bucket[d] + prefix - tileStart;
         __syncthreads();
+        if (s_abort) return;  // a bounded wait ran out: nothing of this tile is written
 #pragma unroll
         for (int r = 0; r < kSortRounds; ++r) {
             const uint32_t idx = base + warp * (32 * kSortRounds) + r * 32 + lane;

@@ -134,6 +134,30 @@ void World::removeCollider(uint32_t index, uint32_t generation) {
     freeColliders.push_back(index);
 }
 
+bool World::setCollider(uint32_t index, uint32_t generation, uint32_t bodyIndex, uint32_t bodyGeneration,
+                        uint32_t shape, const float *dims, const float *lpos, const float *lrot) {
+    pull();
+    HostCollider *c = collider(index, generation);
+    if (!c) return false;
+    const bool same = c->body == bodyIndex && c->bodyGeneration == bodyGeneration && c->shape == shape &&
+                      std::memcmp(c->dims, dims, sizeof(c->dims)) == 0 &&
+                      std::memcmp(c->lpos, lpos, sizeof(c->lpos)) == 0 &&
+                      std::memcmp(c->lrot, lrot, sizeof(c->lrot)) == 0;
+    if (same) return true;
+    // changed geometry wakes the old and the new body (prepareSleeping's
+    // collider comparison, physics_world.cpp:455-465)
+    if (HostBody *b = body(c->body, c->bodyGeneration)) b->wakeUp();
+    if (HostBody *b = body(bodyIndex, bodyGeneration)) b->wakeUp();
+    c->body = bodyIndex;
+    c->bodyGeneration = bodyGeneration;
+    c->shape = shape;
+    std::memcpy(c->dims, dims, sizeof(c->dims));
+    std::memcpy(c->lpos, lpos, sizeof(c->lpos));
+    std::memcpy(c->lrot, lrot, sizeof(c->lrot));
+    hostDirty_ = true;
+    return true;
+}
+
 HostBody *World::body(uint32_t index, uint32_t generation) {
     if (index >= bodies.size()) return nullptr;
     HostBody &b = bodies[index];

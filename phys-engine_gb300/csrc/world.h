@@ -130,6 +130,10 @@ class World {
     void removeCollider(uint32_t index, uint32_t generation);
     HostBody *body(uint32_t index, uint32_t generation);
     HostCollider *collider(uint32_t index, uint32_t generation);
+    // A write through the reference's public Collider fields: body, shape and
+    // local transform of a live collider.  Returns false for a stale handle.
+    bool setCollider(uint32_t index, uint32_t generation, uint32_t body, uint32_t bodyGeneration, uint32_t shape,
+                     const float *dims, const float *lpos, const float *lrot);
     int addHull(const float *verts, uint32_t count);
 
     // Host-mirror access: pull() refreshes it from the device, touch() marks it

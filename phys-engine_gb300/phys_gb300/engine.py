@@ -88,6 +88,16 @@ SIGNATURES = {
     "pe_world_remove_body": (ctypes.c_int, [_P, Handle]),
     "pe_world_remove_collider": (ctypes.c_int, [_P, Handle]),
     "pe_world_get_body": (ctypes.c_int, [_P, Handle, _P]),
+    "pe_debug_set_spin_limit": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint32]),
+    "pe_body_make_sphere": (ctypes.c_int, [ctypes.c_float, _P, ctypes.c_float, ctypes.c_int, ctypes.c_float,
+                                           ctypes.c_float, _P]),
+    "pe_body_make_box": (ctypes.c_int, [ctypes.c_float, ctypes.c_float, ctypes.c_float, _P, ctypes.c_float,
+                                        ctypes.c_int, ctypes.c_float, ctypes.c_float, _P]),
+    "pe_body_integrate": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_float]),
+    "pe_world_add_body": (ctypes.c_int, [_P, _P, _P]),
+    "pe_world_get_body_record": (ctypes.c_int, [_P, Handle, _P]),
+    "pe_world_get_collider": (ctypes.c_int, [_P, Handle, _P, _P, _P, _P, _P]),
+    "pe_world_set_collider": (ctypes.c_int, [_P, Handle, Handle, ctypes.c_int, _P, _P, _P]),
     "pe_world_set_body": (ctypes.c_int, [_P, Handle, _P]),
     "pe_world_body_integrate_rotation": (ctypes.c_int, [_P, Handle, ctypes.c_float]),
     "pe_world_body_is_sleeping": (ctypes.c_int, [_P, Handle, _P]),
