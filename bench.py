@@ -333,6 +333,7 @@ def run_gpu(args, rank, world_size, local_rank):
     if world_size == 1 and not args.no_batched:
         line["batched"] = run_batched(args, local_rank, flush, peak)
         line["differentiable"] = run_differentiable(args, local_rank)
+        line["differentiable_batched"] = run_differentiable_batched(args, local_rank)
     if world_size == 1 and not args.no_sleeping:
         line["sleeping"] = run_sleeping(args, local_rank, flush)
     if world_size == 1 and not args.no_field:
@@ -736,6 +737,129 @@ def run_differentiable(args, local_rank):
         "plain_loop": {"value": plain, "unit": "world-steps/s",
                        "sample": f"every 32nd world ({len(worlds)} worlds), {plain_steps} forward steps each, "
                                  f"wall clock of the single-world engine's step"},
+        "speedup_vs_plain_loop": value / plain,
+    }
+
+
+DIFF_BATCH_STEPS = 60
+DIFF_BATCH_DT = 1.0 / 60.0
+DIFF_BATCH_CHECKPOINT = 10
+# The mixed-volume worlds are sparse (about one manifold per hundred bodies):
+# a quarter manifold of capacity per body (plus 32 per world) covers them.
+DIFF_BATCH_MANIFOLDS_PER_BODY = 0.25
+
+
+def run_differentiable_batched(args, local_rank):
+    """Forward + adjoint over the 4,096 uneven batched worlds (body counts
+    log-uniform in [16, 2048], each the mixed workload scaled to its size, seed
+    42 + w): a 60-step rollout at dt 1/60 with checkpoints every 10 steps, loss =
+    sum over worlds of the squared distance of the final centre of mass from a
+    seeded target within 5 m, gradients with respect to initial velocities,
+    masses, frictions and restitutions through the autograd harness; against
+    looping the plain single-world GPU step over a sample of the same worlds."""
+    import random
+
+    import torch
+
+    from phys_gb300 import engine, rollout
+
+    sizes = batch_world_sizes(args.batch_worlds)
+    sc = batch_scenes(sizes)
+    W = len(sizes)
+    dev = torch.device("cuda", local_rank)
+    free0, _ = torch.cuda.mem_get_info(dev)
+    roll = rollout.GpuRollout(sc, DIFF_BATCH_STEPS, DIFF_BATCH_DT, iterations=ITERATIONS,
+                              checkpoint_every=DIFF_BATCH_CHECKPOINT, device=local_rank,
+                              manifolds_per_body=DIFF_BATCH_MANIFOLDS_PER_BODY)
+    fn = rollout.rollout_function()
+    r = random.Random(SEED)
+    targets = []
+    for _ in range(W):
+        while True:
+            t = [r.uniform(-5, 5) for _ in range(3)]
+            if sum(c * c for c in t) <= 25.0:
+                break
+        targets.append(t)
+    target = torch.tensor(targets, device=dev)
+    x0n, q0n, v0n, w0n = roll.initial_state()
+    dyn = torch.tensor(~roll.is_static.astype(bool), device=dev)
+    world_of = torch.tensor(np.repeat(np.arange(W), roll.counts), device=dev)
+
+    def one(host):
+        ins = [t.to(dev, non_blocking=True) for t in host]
+        for t in ins[2:]:
+            t.requires_grad_(True)
+        x0, q0, v0, w0, m, f, rs = ins
+        xT, qT, vT, wT = fn.apply(roll, x0, q0, v0, w0, m, f, rs)
+        mw = m * dyn
+        msum = torch.zeros(W, device=dev).index_add_(0, world_of, mw)
+        com = torch.zeros(W, 3, device=dev).index_add_(0, world_of, mw[:, None] * xT) / msum[:, None]
+        loss = ((com - target) ** 2).sum()
+        loss.backward()
+        grads = [v0.grad, m.grad, f.grad, rs.grad]
+        return float(loss.item()), [g.to("cpu", non_blocking=True) for g in grads]
+
+    pin = lambda a: torch.tensor(a).pin_memory()
+    host = [pin(x0n), pin(q0n), pin(v0n), pin(w0n), pin(roll.mass), pin(roll.friction), pin(roll.restitution)]
+    one(host)  # warm-up (lays out the device slots)
+    free1, _ = torch.cuda.mem_get_info(dev)
+    reps = 2
+    fwd_ms = bwd_ms = 0.0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        loss, grads = one(host)
+        f_ms, b_ms = roll.timings()
+        fwd_ms += f_ms
+        bwd_ms += b_ms
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    finite = all(bool(torch.isfinite(g).all()) for g in grads)
+    device_bytes = roll.device_bytes()
+    roll.close()
+    # plain loop: forward steps of the single-world engine over a sample
+    worlds = []
+    for w in range(0, W, 64):
+        gw = engine.GpuWorld(device=local_rank, algo=engine.SAP, iterations=ITERATIONS, order=engine.ORDER_COLOR)
+        gw.load_scene(sc[w])
+        worlds.append(gw)
+    for _ in range(3):
+        for gw in worlds:
+            gw.step(DIFF_BATCH_DT)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    plain_steps = 5
+    for _ in range(plain_steps):
+        for gw in worlds:
+            gw.step(DIFF_BATCH_DT)
+    torch.cuda.synchronize()
+    plain = len(worlds) * plain_steps / (time.perf_counter() - t1)
+    for gw in worlds:
+        gw.close()
+    ws = W * DIFF_BATCH_STEPS * reps
+    value = ws / ((fwd_ms + bwd_ms) / 1000.0)
+    h2d = sum(int(t.numel() * t.element_size()) for t in host)
+    return {
+        "metric": f"world-steps/s, {W} uneven batched worlds forward + adjoint", "value": value,
+        "unit": "world-steps/s", "rollouts": reps, "forward_ms_per_rollout": fwd_ms / reps,
+        "adjoint_ms_per_rollout": bwd_ms / reps,
+        "config": {"workload": f"differentiable_batched_{W}", "worlds": W, "bodies": int(sum(sizes)),
+                   "bodies_per_world": f"log-uniform in [{BATCH_MIN}, {BATCH_MAX}] (seed {SEED})",
+                   "world": "mixed workload scaled to the world's body count, seed 42 + world",
+                   "steps": DIFF_BATCH_STEPS, "dt": DIFF_BATCH_DT, "solver_iterations": ITERATIONS,
+                   "checkpoint_every": DIFF_BATCH_CHECKPOINT,
+                   "manifold_capacity_per_body": DIFF_BATCH_MANIFOLDS_PER_BODY,
+                   "loss": "sum over worlds of |final centre of mass - target|^2, targets seeded within 5 m",
+                   "gradients": "initial velocities, masses, frictions, restitutions (torch.autograd)"},
+        "loss": loss, "gradients_finite": finite,
+        "device_memory": {"rollout_bytes": device_bytes,
+                          "device_bytes_used_after_first_rollout": int(free0 - free1)},
+        "e2e": {"value": ws / e2e_s, "unit": "world-steps/s", "h2d_bytes_per_step": h2d / DIFF_BATCH_STEPS,
+                "d2h_bytes_per_step": (4 * roll.n * 6 + 4) / DIFF_BATCH_STEPS},
+        "gpu_launches": 2 * reps,
+        "plain_loop": {"value": plain, "unit": "world-steps/s",
+                       "sample": f"every 64th world ({len(worlds)} worlds), {plain_steps} forward steps each, wall "
+                                 f"clock of the single-world engine's step"},
         "speedup_vs_plain_loop": value / plain,
     }
 

@@ -375,8 +375,8 @@ pe_status pe_batch_set_graphs(pe_batch *batch, int enabled);
 
 /* ------------------------------------------------------------------------
    Differentiable batched rollout (no reference counterpart; the reference has
-   no differentiation).  Many independent worlds of sphere/box bodies (1 to 256
-   per world, one collider each) are stepped `steps` times with
+   no differentiation).  Many independent worlds of sphere/box bodies (1 to
+   8192 per world, one collider each) are stepped `steps` times with
    PhysicsWorld::step's algorithm (SAP pair set, graph-colour solve order) on
    the GPU; the adjoint returns the gradients of sum(d_final . final state)
    with respect to the initial state and to each body's mass (the RigidBody
@@ -385,7 +385,9 @@ pe_status pe_batch_set_graphs(pe_batch *batch, int enabled);
    contact features, colour order, warm-start matches, clamp branches); contact
    points, normals and depths are differentiated as functions of the poses.
    Memory: states are checkpointed every `checkpoint_every` steps and each
-   segment is recomputed once during the adjoint.
+   segment is recomputed once during the adjoint; each world's device slot
+   (checkpoints, one segment's step scratch and tape, adjoints) is sized by its
+   own body count, and pe_rollout_device_bytes reports the total.
    State arrays are DEVICE pointers holding all worlds' bodies back to back:
    positions / linear / angular velocities 3 floats per body, rotations 4
    (x, y, z, w).  Calls run on `stream` and return when the work is done.
@@ -410,6 +412,12 @@ pe_status pe_rollout_backward(pe_rollout *rollout, const float *d_final_x, const
                               void *stream);
 /* Device time of the last forward and backward calls (ms). */
 pe_status pe_rollout_timings(pe_rollout *rollout, double *forward_ms, double *backward_ms);
+/* Contact-manifold capacity per body of every world (0.25 to 64; default 2,
+   enough for boxes resting on one another).  The device slots are laid out at
+   the next forward call; a world whose manifolds outgrow it fails that call. */
+pe_status pe_rollout_set_manifold_capacity(pe_rollout *rollout, float per_body);
+/* Device memory the rollout holds (bytes; 0 before the first forward call). */
+pe_status pe_rollout_device_bytes(pe_rollout *rollout, uint64_t *bytes);
 
 /* Failure detection, for tests (no reference counterpart).  Every spin-wait of
    the step kernels (tile look-back, grid barrier, union retries, colouring

@@ -26,6 +26,7 @@
 
 #if !defined(__CUDACC__)
 #include <algorithm>
+#include <cstring>
 #endif
 
 namespace pe {
@@ -172,7 +173,18 @@ template <class S> struct StepScratch {
     S *tape;                        // iterations * maxManifolds * kTapeScalars
     uint32_t *cacheSrc;             // per cache-out entry: k * 4 + p
     uint32_t *counts;               // [0] pairs, [1] manifolds, [2] colours, [3] error bits
+    // broadphase scratch (not recorded: it may be shared by the steps of a segment)
+    unsigned long long *bpEntries;  // nextPow2(n): (min.x key << 32) | body
+    unsigned long long *bpPairs;    // nextPow2(maxPairs): (first << 32) | second
 };
+
+// Order-preserving 32-bit key of a float (the sort order of the sweep).
+AD_HD uint32_t adOrderedKey(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+AD_HD uint32_t adOrderedKey(double d) { return adOrderedKey((float)d); }
 
 template <class S> struct AdjointView {
     S *ax, *aq, *av, *aw;        // per body (3, 4, 3, 3)
@@ -457,38 +469,64 @@ AD_HD void forwardStep(const WorldParams<S> &W, const StateView<S> &in, const Ca
         sc.counts[3] = 0;
     }
     T::sync();
-    // 2. all pairs (i < j) with overlapping AABBs in lexicographic order
-    const uint32_t total = n * (n - 1) / 2;
+    // 2. every pair (i < j) with overlapping AABBs (touching counts), in
+    // lexicographic order: sort and sweep along x (broadphase.cpp:195-291) —
+    // bodies sorted by min.x, each tested against the later ones whose min.x
+    // does not exceed its max.x (the one of an overlapping pair sorted first
+    // always meets the other) — then the pairs sorted by (first, second).
+    const uint32_t n2 = nextPow2u(n > 0 ? n : 1);
+    for (uint32_t i = tid; i < n2; i += nt)
+        sc.bpEntries[i] = i < n ? ((unsigned long long)adOrderedKey(val(sc.aabb[6 * i])) << 32) | i : ~0ull;
+    T::sync();
+    T::sortU64(sc.bpEntries, n2);
+    T::sync();
+    auto overlapsYZ = [&](uint32_t a, uint32_t b) {
+        const V3<S> amn = ld3(sc.aabb, 2 * a), amx = ld3(sc.aabb, 2 * a + 1);
+        const V3<S> bmn = ld3(sc.aabb, 2 * b), bmx = ld3(sc.aabb, 2 * b + 1);
+        return val(amn.y) <= val(bmx.y) && val(amx.y) >= val(bmn.y) && val(amn.z) <= val(bmx.z) &&
+               val(amx.z) >= val(bmn.z);
+    };
     uint32_t P = 0;
-    for (uint32_t t0 = 0; t0 < total; t0 += nt) {
-        const uint32_t t = t0 + tid;
-        uint32_t i = 0, j = 0;
-        bool hit = false;
-        if (t < total) {
-            uint32_t lo = 0, hi = n - 1;  // largest i with off(i) <= t, off(i) = i (2n - i - 1) / 2
-            while (lo + 1 < hi) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (mid * (2 * n - mid - 1) / 2 <= t) lo = mid;
-                else hi = mid;
+    for (uint32_t k0 = 0; k0 < n; k0 += nt) {
+        const uint32_t k = k0 + tid;
+        uint32_t hits = 0;
+        uint32_t i = 0;
+        if (k < n) {
+            i = (uint32_t)sc.bpEntries[k];
+            const auto maxX = val(sc.aabb[6 * i + 3]);
+            for (uint32_t kk = k + 1; kk < n; ++kk) {
+                const uint32_t j = (uint32_t)sc.bpEntries[kk];
+                if (val(sc.aabb[6 * j]) > maxX) break;
+                if (overlapsYZ(i, j)) ++hits;
             }
-            i = lo;
-            j = i + 1 + (t - i * (2 * n - i - 1) / 2);
-            const V3<S> amn = ld3(sc.aabb, 2 * i), amx = ld3(sc.aabb, 2 * i + 1);
-            const V3<S> bmn = ld3(sc.aabb, 2 * j), bmx = ld3(sc.aabb, 2 * j + 1);
-            hit = val(amn.x) <= val(bmx.x) && val(amx.x) >= val(bmn.x) && val(amn.y) <= val(bmx.y) &&
-                  val(amx.y) >= val(bmn.y) && val(amn.z) <= val(bmx.z) && val(amx.z) >= val(bmn.z);
         }
         uint32_t cnt;
-        const uint32_t slot = P + T::scan(hit ? 1u : 0u, cnt);
-        if (hit && slot < W.maxPairs) {
-            sc.pairA[slot] = i;
-            sc.pairB[slot] = j;
+        uint32_t slot = P + T::scan(hits, cnt);
+        if (k < n && hits) {
+            const auto maxX = val(sc.aabb[6 * i + 3]);
+            for (uint32_t kk = k + 1; kk < n; ++kk) {
+                const uint32_t j = (uint32_t)sc.bpEntries[kk];
+                if (val(sc.aabb[6 * j]) > maxX) break;
+                if (!overlapsYZ(i, j)) continue;
+                if (slot < W.maxPairs)
+                    sc.bpPairs[slot] = ((unsigned long long)(i < j ? i : j) << 32) | (i < j ? j : i);
+                ++slot;
+            }
         }
         P += cnt;
     }
     if (P > W.maxPairs) {
         if (tid == 0) T::orErr(&sc.counts[3], kAdErrPairs);
         P = W.maxPairs;
+    }
+    const uint32_t P2 = nextPow2u(P > 0 ? P : 1);
+    for (uint32_t p = P + tid; p < P2; p += nt) sc.bpPairs[p] = ~0ull;
+    T::sync();
+    T::sortU64(sc.bpPairs, P2);
+    T::sync();
+    for (uint32_t p = tid; p < P; p += nt) {
+        sc.pairA[p] = (uint32_t)(sc.bpPairs[p] >> 32);
+        sc.pairB[p] = (uint32_t)sc.bpPairs[p];
     }
     if (tid == 0) sc.counts[0] = P;
     T::sync();

@@ -1130,6 +1130,20 @@ pe_status pe_rollout_timings(pe_rollout *rollout, double *fwd, double *bwd) {
     return PE_OK;
 }
 
+pe_status pe_rollout_set_manifold_capacity(pe_rollout *rollout, float per_body) {
+    if (!rollout) return fail(PE_ERR_INVALID_ARGUMENT, "null rollout");
+    return guarded([&] {
+        rollout->r->setManifoldCapacity(per_body);
+        return PE_OK;
+    });
+}
+
+pe_status pe_rollout_device_bytes(pe_rollout *rollout, uint64_t *bytes) {
+    if (!rollout || !bytes) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    *bytes = rollout->r->deviceBytes();
+    return PE_OK;
+}
+
 } // extern "C"
 
 namespace pe {

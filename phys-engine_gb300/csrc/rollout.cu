@@ -14,7 +14,7 @@ namespace {
 using namespace ad;
 using F = float;
 
-constexpr size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
+__host__ __device__ constexpr size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
 
 // Byte offsets inside one world's slot of the arena.
 struct Layout {
@@ -27,10 +27,13 @@ struct Layout {
         order, sortKeys, bodyUsed, colorStart, pp, pm, lam, lamInit, match, tape, cacheSrc, counts;
     // adjoints
     size_t ax, aq, av, aw, alam, app, apm, an, amuM, arestM, acache, amass, amu, arest, v1v, v1w;
+    // broadphase sort buffers, shared by the steps (not part of any record)
+    size_t bpEntries, bpPairs;
     size_t stride;
 };
 
-Layout makeLayout(uint32_t nMax, uint32_t maxPairs, uint32_t maxM, int iterations, uint32_t nSnap, uint32_t nScr) {
+__host__ __device__ Layout makeLayout(uint32_t nMax, uint32_t maxPairs, uint32_t maxM, int iterations, uint32_t nSnap,
+                                      uint32_t nScr) {
     Layout L{};
     const uint32_t cap = 4 * maxM;
     size_t o = 0;
@@ -93,22 +96,53 @@ Layout makeLayout(uint32_t nMax, uint32_t maxPairs, uint32_t maxM, int iteration
     L.arest = take(sizeof(F) * nMax);
     L.v1v = take(sizeof(F) * 3 * nMax);
     L.v1w = take(sizeof(F) * 3 * nMax);
+    L.bpEntries = take(8ull * ad::nextPow2u(nMax > 0 ? nMax : 1));
+    L.bpPairs = take(8ull * ad::nextPow2u(maxPairs > 0 ? maxPairs : 1));
     L.stride = o;
     return L;
 }
 
+// Capacities of a world of n bodies: candidate pairs, manifolds (a power of
+// two), and its slot of the arena, sized for those.
+__host__ __device__ inline uint32_t worldMaxPairs(uint32_t n) { return 8 * n + 64; }
+// quarterPerBody: manifold capacity in quarter manifolds per body (8 = two
+// per body, enough for boxes resting on one another).
+__host__ __device__ inline uint32_t worldMaxManifolds(uint32_t n, uint32_t quarterPerBody) {
+    const uint64_t need = ((uint64_t)quarterPerBody * n + 3) / 4 + 32;
+    uint32_t m = 1;
+    while (m < need) m <<= 1;
+    return m;
+}
+
 struct Args {
-    Layout L;
     unsigned char *arena;
-    const uint32_t *bodyStart;  // worlds + 1
+    const unsigned long long *worldOff;  // byte offset of each world's slot in the arena
+    const uint32_t *order;               // worlds in the order blocks take them (largest first)
+    const uint32_t *bodyStart;           // worlds + 1
     const uint8_t *shape, *isStatic;
     const F *dims, *iinv, *mass, *mu, *rest;
-    uint32_t worlds, nMax, maxPairs, maxM, steps, ckEvery, nCk;
+    uint32_t worlds, steps, ckEvery, nCk, quarterPerBody;
     int iterations;
     F gx, gy, gz, dt;
     uint32_t *queueHead;
     uint32_t *err;  // per world
 };
+
+// One world's slot: its layout (sized by its own body count) and base address.
+struct Slot {
+    Layout L;
+    unsigned char *base;
+    uint32_t maxPairs, maxM;
+};
+__device__ __forceinline__ Slot slotOf(const Args &a, uint32_t w) {
+    const uint32_t n = a.bodyStart[w + 1] - a.bodyStart[w];
+    Slot s;
+    s.maxPairs = worldMaxPairs(n);
+    s.maxM = worldMaxManifolds(n, a.quarterPerBody);
+    s.L = makeLayout(n, s.maxPairs, s.maxM, a.iterations, a.nCk + a.ckEvery + 1, a.ckEvery);
+    s.base = a.arena + a.worldOff[w];
+    return s;
+}
 
 template <class P> __device__ __forceinline__ P *at(unsigned char *base, size_t off) {
     return reinterpret_cast<P *>(base + off);
@@ -118,18 +152,18 @@ struct Snap {
     ad::StateView<F> s;
     ad::CacheView<F> c;
 };
-__device__ __forceinline__ Snap snapshot(const Args &a, unsigned char *base, uint32_t j, uint32_t n) {
-    unsigned char *p = base + a.L.snap0 + a.L.snapStride * j;
-    F *st = at<F>(p, a.L.sState);
+__device__ __forceinline__ Snap snapshot(const Slot &ws, uint32_t j, uint32_t n) {
+    unsigned char *p = ws.base + ws.L.snap0 + ws.L.snapStride * j;
+    F *st = at<F>(p, ws.L.sState);
     Snap r;
     r.s = ad::StateView<F>{st, st + 3 * n, st + 7 * n, st + 10 * n};
-    r.c = ad::CacheView<F>{at<uint32_t>(p, a.L.sCount), at<unsigned long long>(p, a.L.sKey), at<F>(p, a.L.sA),
-                       at<F>(p, a.L.sB), at<F>(p, a.L.sLam), 4 * a.maxM};
+    r.c = ad::CacheView<F>{at<uint32_t>(p, ws.L.sCount), at<unsigned long long>(p, ws.L.sKey), at<F>(p, ws.L.sA),
+                       at<F>(p, ws.L.sB), at<F>(p, ws.L.sLam), 4 * ws.maxM};
     return r;
 }
-__device__ __forceinline__ StepScratch<F> scratch(const Args &a, unsigned char *base, uint32_t j) {
-    unsigned char *p = base + a.L.scr0 + a.L.scrStride * j;
-    const Layout &L = a.L;
+__device__ __forceinline__ StepScratch<F> scratch(const Slot &ws, uint32_t j) {
+    unsigned char *p = ws.base + ws.L.scr0 + ws.L.scrStride * j;
+    const Layout &L = ws.L;
     StepScratch<F> s;
     s.aabb = at<F>(p, L.aabb);
     s.pairA = at<uint32_t>(p, L.pairA);
@@ -157,10 +191,12 @@ __device__ __forceinline__ StepScratch<F> scratch(const Args &a, unsigned char *
     s.tape = at<F>(p, L.tape);
     s.cacheSrc = at<uint32_t>(p, L.cacheSrc);
     s.counts = at<uint32_t>(p, L.counts);
+    s.bpEntries = at<unsigned long long>(ws.base, L.bpEntries);
+    s.bpPairs = at<unsigned long long>(ws.base, L.bpPairs);
     return s;
 }
 
-__device__ __forceinline__ WorldParams<F> params(const Args &a, uint32_t w) {
+__device__ __forceinline__ WorldParams<F> params(const Args &a, uint32_t w, const Slot &ws) {
     const uint32_t b = a.bodyStart[w];
     WorldParams<F> W;
     W.n = a.bodyStart[w + 1] - b;
@@ -176,8 +212,8 @@ __device__ __forceinline__ WorldParams<F> params(const Args &a, uint32_t w) {
     W.gz = a.gz;
     W.dt = a.dt;
     W.iterations = a.iterations;
-    W.maxPairs = a.maxPairs;
-    W.maxManifolds = a.maxM;
+    W.maxPairs = ws.maxPairs;
+    W.maxManifolds = ws.maxM;
     return W;
 }
 
@@ -199,7 +235,10 @@ __device__ void copySnap(const Snap &from, const Snap &to, uint32_t n) {
 __device__ __forceinline__ uint32_t nextWorld(const Args &a) {
     __shared__ uint32_t s_w;
     __syncthreads();
-    if (threadIdx.x == 0) s_w = atomicAdd(a.queueHead, 1u);
+    if (threadIdx.x == 0) {
+        const uint32_t i = atomicAdd(a.queueHead, 1u);
+        s_w = i < a.worlds ? a.order[i] : a.worlds;
+    }
     __syncthreads();
     return s_w;
 }
@@ -211,10 +250,10 @@ __global__ void __launch_bounds__(128) k_rollout_forward(Args a, const F *x0, co
     for (;;) {
         const uint32_t w = nextWorld(a);
         if (w >= a.worlds) return;
-        unsigned char *base = a.arena + a.L.stride * (size_t)w;
-        const WorldParams<F> W = params(a, w);
+        const Slot ws = slotOf(a, w);
+        const WorldParams<F> W = params(a, w, ws);
         const uint32_t n = W.n, b = a.bodyStart[w];
-        Snap ck0 = snapshot(a, base, 0, n);
+        Snap ck0 = snapshot(ws, 0, n);
         for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
             for (int j = 0; j < 3; ++j) {
                 ck0.s.x[3 * i + j] = x0[3 * (b + i) + j];
@@ -227,9 +266,9 @@ __global__ void __launch_bounds__(128) k_rollout_forward(Args a, const F *x0, co
         __syncthreads();
         Snap cur = ck0;
         bool failed = false;
-        const StepScratch<F> sc = scratch(a, base, 0);
+        const StepScratch<F> sc = scratch(ws, 0);
         for (uint32_t t = 0; t < a.steps && !failed; ++t) {
-            Snap out = snapshot(a, base, a.nCk + (t & 1), n);
+            Snap out = snapshot(ws, a.nCk + (t & 1), n);
             forwardStep<F, BlockTeam>(W, cur.s, cur.c, out.s, out.c, sc, false);
             if (sc.counts[3]) {
                 if (threadIdx.x == 0) atomicOr(&a.err[w], sc.counts[3]);
@@ -238,7 +277,7 @@ __global__ void __launch_bounds__(128) k_rollout_forward(Args a, const F *x0, co
             }
             const uint32_t s = t + 1;
             if (s % a.ckEvery == 0 || s == a.steps) {
-                const Snap ck = snapshot(a, base, (s + a.ckEvery - 1) / a.ckEvery, n);
+                const Snap ck = snapshot(ws, (s + a.ckEvery - 1) / a.ckEvery, n);
                 copySnap(out, ck, n);
                 cur = ck;
             } else {
@@ -257,10 +296,10 @@ __global__ void __launch_bounds__(128) k_rollout_forward(Args a, const F *x0, co
     }
 }
 
-__device__ void mapCacheAdjoint(const Args &a, unsigned char *base, const StepScratch<F> &prev, uint32_t count) {
-    F *alam = at<F>(base, a.L.alam);
-    const F *acache = at<F>(base, a.L.acache);
-    for (uint32_t i = threadIdx.x; i < 12 * a.maxM; i += blockDim.x) alam[i] = 0.0f;
+__device__ void mapCacheAdjoint(const Slot &ws, const StepScratch<F> &prev, uint32_t count) {
+    F *alam = at<F>(ws.base, ws.L.alam);
+    const F *acache = at<F>(ws.base, ws.L.acache);
+    for (uint32_t i = threadIdx.x; i < 12 * ws.maxM; i += blockDim.x) alam[i] = 0.0f;
     __syncthreads();
     for (uint32_t e = threadIdx.x; e < count; e += blockDim.x) {
         const uint32_t kp = prev.cacheSrc[e];
@@ -277,14 +316,16 @@ __global__ void __launch_bounds__(128) k_rollout_backward(Args a, const F *gx, c
     for (;;) {
         const uint32_t w = nextWorld(a);
         if (w >= a.worlds) return;
-        unsigned char *base = a.arena + a.L.stride * (size_t)w;
-        const WorldParams<F> W = params(a, w);
+        const Slot ws = slotOf(a, w);
+        unsigned char *base = ws.base;
+        const Layout &L0 = ws.L;
+        const WorldParams<F> W = params(a, w, ws);
         const uint32_t n = W.n, b = a.bodyStart[w];
-        AdjointView<F> adj{at<F>(base, a.L.ax),    at<F>(base, a.L.aq),     at<F>(base, a.L.av),
-                           at<F>(base, a.L.aw),    at<F>(base, a.L.alam),   at<F>(base, a.L.app),
-                           at<F>(base, a.L.apm),   at<F>(base, a.L.an),     at<F>(base, a.L.amuM),
-                           at<F>(base, a.L.arestM), at<F>(base, a.L.acache), at<F>(base, a.L.amass),
-                           at<F>(base, a.L.amu),   at<F>(base, a.L.arest)};
+        AdjointView<F> adj{at<F>(base, L0.ax),     at<F>(base, L0.aq),     at<F>(base, L0.av),
+                           at<F>(base, L0.aw),     at<F>(base, L0.alam),   at<F>(base, L0.app),
+                           at<F>(base, L0.apm),    at<F>(base, L0.an),     at<F>(base, L0.amuM),
+                           at<F>(base, L0.arestM), at<F>(base, L0.acache), at<F>(base, L0.amass),
+                           at<F>(base, L0.amu),    at<F>(base, L0.arest)};
         for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
             for (int j = 0; j < 3; ++j) {
                 adj.ax[3 * i + j] = gx ? gx[3 * (b + i) + j] : 0.0f;
@@ -294,19 +335,19 @@ __global__ void __launch_bounds__(128) k_rollout_backward(Args a, const F *gx, c
             for (int j = 0; j < 4; ++j) adj.aq[4 * i + j] = gq ? gq[4 * (b + i) + j] : 0.0f;
             adj.amass[i] = adj.amu[i] = adj.arest[i] = 0.0f;
         }
-        for (uint32_t i = threadIdx.x; i < 12 * a.maxM; i += blockDim.x) adj.alam[i] = 0.0f;
+        for (uint32_t i = threadIdx.x; i < 12 * ws.maxM; i += blockDim.x) adj.alam[i] = 0.0f;
         __syncthreads();
-        ad::StateView<F> v1{nullptr, nullptr, at<F>(base, a.L.v1v), at<F>(base, a.L.v1w)};
+        ad::StateView<F> v1{nullptr, nullptr, at<F>(base, L0.v1v), at<F>(base, L0.v1w)};
         const uint32_t nSeg = (a.steps + a.ckEvery - 1) / a.ckEvery;
         bool pending = false, failed = false;
         uint32_t pendingCount = 0;
         for (int s = (int)nSeg - 1; s >= 0 && !failed; --s) {
             const uint32_t t0 = (uint32_t)s * a.ckEvery;
             const uint32_t L = min(a.steps, t0 + a.ckEvery) - t0;
-            copySnap(snapshot(a, base, (uint32_t)s, n), snapshot(a, base, a.nCk, n), n);
+            copySnap(snapshot(ws, (uint32_t)s, n), snapshot(ws, a.nCk, n), n);
             for (uint32_t i = 0; i < L; ++i) {
-                const Snap in = snapshot(a, base, a.nCk + i, n), out = snapshot(a, base, a.nCk + i + 1, n);
-                const StepScratch<F> sc = scratch(a, base, i);
+                const Snap in = snapshot(ws, a.nCk + i, n), out = snapshot(ws, a.nCk + i + 1, n);
+                const StepScratch<F> sc = scratch(ws, i);
                 forwardStep<F, BlockTeam>(W, in.s, in.c, out.s, out.c, sc, true);
                 if (sc.counts[3]) {
                     if (threadIdx.x == 0) atomicOr(&a.err[w], sc.counts[3]);
@@ -315,10 +356,10 @@ __global__ void __launch_bounds__(128) k_rollout_backward(Args a, const F *gx, c
                 }
             }
             if (failed) break;
-            if (pending) mapCacheAdjoint(a, base, scratch(a, base, L - 1), pendingCount);
+            if (pending) mapCacheAdjoint(ws, scratch(ws, L - 1), pendingCount);
             for (int i = (int)L - 1; i >= 0; --i) {
-                const Snap in = snapshot(a, base, a.nCk + i, n), out = snapshot(a, base, a.nCk + i + 1, n);
-                const StepScratch<F> sc = scratch(a, base, (uint32_t)i);
+                const Snap in = snapshot(ws, a.nCk + i, n), out = snapshot(ws, a.nCk + i + 1, n);
+                const StepScratch<F> sc = scratch(ws, (uint32_t)i);
                 backwardStep<F, BlockTeam>(W, in.s, in.c, out.s, v1, sc, adj);
                 if (sc.counts[3]) {
                     if (threadIdx.x == 0) atomicOr(&a.err[w], sc.counts[3]);
@@ -327,7 +368,7 @@ __global__ void __launch_bounds__(128) k_rollout_backward(Args a, const F *gx, c
                 }
                 const uint32_t cnt = *in.c.count;
                 if (i > 0) {
-                    mapCacheAdjoint(a, base, scratch(a, base, (uint32_t)i - 1), cnt);
+                    mapCacheAdjoint(ws, scratch(ws, (uint32_t)i - 1), cnt);
                 } else {
                     pending = t0 > 0;
                     pendingCount = cnt;
@@ -357,10 +398,6 @@ template <class T> void uploadVec(DeviceArray<T> &d, const std::vector<T> &h) {
 
 } // namespace
 
-struct RolloutLayout {
-    Layout L;
-};
-
 Rollout::Rollout(int device) : device_(device) {
     PE_CHECK(cudaSetDevice(device_));
     PE_CHECK(cudaEventCreate(&e0_));
@@ -387,8 +424,9 @@ void Rollout::create(const std::vector<uint32_t> &worldBodies, const std::vector
     nMax_ = 0;
     std::vector<uint32_t> start(worldBodies.size() + 1, 0);
     for (size_t w = 0; w < worldBodies.size(); ++w) {
-        if (worldBodies[w] == 0 || worldBodies[w] > 256)
-            throw std::invalid_argument("a differentiable world holds 1 to 256 bodies");
+        if (worldBodies[w] == 0 || worldBodies[w] > kRolloutMaxBodies)
+            throw std::invalid_argument("a differentiable world holds 1 to " + std::to_string(kRolloutMaxBodies) +
+                                        " bodies");
         start[w] = (uint32_t)total;
         total += worldBodies[w];
         nMax_ = std::max(nMax_, worldBodies[w]);
@@ -406,11 +444,12 @@ void Rollout::create(const std::vector<uint32_t> &worldBodies, const std::vector
     iterations_ = iterations;
     ckEvery_ = std::min(checkpointEvery, steps);
     nCk_ = (steps + ckEvery_ - 1) / ckEvery_ + 1;
-    maxPairs_ = 8 * nMax_ + 64;
-    maxM_ = ad::nextPow2u(2 * nMax_ + 32);
-    const Layout L = makeLayout(nMax_, maxPairs_, maxM_, iterations_, nCk_ + ckEvery_ + 1, ckEvery_);
-    worldStride_ = align16(L.stride);
-    layout_.reset(new RolloutLayout{L});
+    // worlds are taken largest first
+    std::vector<uint32_t> order(worldBodies.size());
+    for (size_t w = 0; w < order.size(); ++w) order[w] = (uint32_t)w;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint32_t x, uint32_t y) { return worldBodies[x] > worldBodies[y]; });
+    uploadVec(order_, order);
     uploadVec(bodyStart_, start);
     uploadVec(shape_, shape);
     uploadVec(static_, isStatic);
@@ -419,11 +458,39 @@ void Rollout::create(const std::vector<uint32_t> &worldBodies, const std::vector
     mass_.reserve(total);
     mu_.reserve(total);
     rest_.reserve(total);
-    arena_.reserve(worldStride_ * worldBodies.size());
     queue_.reserve(1);
     err_.reserve(worldBodies.size());
-    bytes_ = worldStride_ * worldBodies.size() + total * 64;
+    arena_.release();
     haveForward_ = false;
+}
+
+void Rollout::setManifoldCapacity(float perBody) {
+    if (!(perBody >= 0.25f && perBody <= 64.0f))
+        throw std::invalid_argument("manifold capacity must be 0.25 to 64 manifolds per body");
+    const uint32_t q = (uint32_t)(perBody * 4.0f + 0.5f);
+    if (q == quarterPerBody_) return;
+    quarterPerBody_ = q;
+    arena_.release();  // laid out again at the next forward call
+    haveForward_ = false;
+}
+
+// Every world's slot is sized by its own body count (checkpoints, one
+// segment's step scratch and tape, adjoints), allocated at the first forward
+// call after creation or a capacity change.
+void Rollout::ensureArena() {
+    if (arena_.ptr) return;
+    std::vector<unsigned long long> off(worldBodies_.size());
+    unsigned long long arenaBytes = 0;
+    for (size_t w = 0; w < worldBodies_.size(); ++w) {
+        const uint32_t n = worldBodies_[w];
+        const Layout L = makeLayout(n, worldMaxPairs(n), worldMaxManifolds(n, quarterPerBody_), iterations_,
+                                    nCk_ + ckEvery_ + 1, ckEvery_);
+        off[w] = arenaBytes;
+        arenaBytes += align16(L.stride);
+    }
+    uploadVec(worldOff_, off);
+    arena_.reserve(arenaBytes);
+    bytes_ = arenaBytes + nb_ * 64;
 }
 
 void Rollout::checkErrors(cudaStream_t s, const char *what) {
@@ -448,14 +515,17 @@ void Rollout::forward(const float *x0, const float *q0, const float *v0, const f
     PE_CHECK(cudaSetDevice(device_));
     if (!x0 || !q0 || !v0 || !w0 || !mass || !friction || !restitution || !xT || !qT || !vT || !wT)
         throw std::invalid_argument("null argument");
+    ensureArena();
     PE_CHECK(cudaMemcpyAsync(mass_.ptr, mass, nb_ * 4, cudaMemcpyDeviceToDevice, s));
     PE_CHECK(cudaMemcpyAsync(mu_.ptr, friction, nb_ * 4, cudaMemcpyDeviceToDevice, s));
     PE_CHECK(cudaMemcpyAsync(rest_.ptr, restitution, nb_ * 4, cudaMemcpyDeviceToDevice, s));
     PE_CHECK(cudaMemsetAsync(queue_.ptr, 0, 4, s));
     PE_CHECK(cudaMemsetAsync(err_.ptr, 0, worldBodies_.size() * 4, s));
     Args a{};
-    a.L = layout_->L;
     a.arena = arena_.ptr;
+    a.quarterPerBody = quarterPerBody_;
+    a.worldOff = worldOff_.ptr;
+    a.order = order_.ptr;
     a.bodyStart = bodyStart_.ptr;
     a.shape = shape_.ptr;
     a.isStatic = static_.ptr;
@@ -465,9 +535,6 @@ void Rollout::forward(const float *x0, const float *q0, const float *v0, const f
     a.mu = mu_.ptr;
     a.rest = rest_.ptr;
     a.worlds = (uint32_t)worldBodies_.size();
-    a.nMax = nMax_;
-    a.maxPairs = maxPairs_;
-    a.maxM = maxM_;
     a.steps = steps_;
     a.ckEvery = ckEvery_;
     a.nCk = nCk_;
@@ -501,8 +568,10 @@ void Rollout::backward(const float *gx, const float *gq, const float *gv, const 
     PE_CHECK(cudaMemsetAsync(queue_.ptr, 0, 4, s));
     PE_CHECK(cudaMemsetAsync(err_.ptr, 0, worldBodies_.size() * 4, s));
     Args a{};
-    a.L = layout_->L;
     a.arena = arena_.ptr;
+    a.quarterPerBody = quarterPerBody_;
+    a.worldOff = worldOff_.ptr;
+    a.order = order_.ptr;
     a.bodyStart = bodyStart_.ptr;
     a.shape = shape_.ptr;
     a.isStatic = static_.ptr;
@@ -512,9 +581,6 @@ void Rollout::backward(const float *gx, const float *gq, const float *gv, const 
     a.mu = mu_.ptr;
     a.rest = rest_.ptr;
     a.worlds = (uint32_t)worldBodies_.size();
-    a.nMax = nMax_;
-    a.maxPairs = maxPairs_;
-    a.maxM = maxM_;
     a.steps = steps_;
     a.ckEvery = ckEvery_;
     a.nCk = nCk_;

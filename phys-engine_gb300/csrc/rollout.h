@@ -13,7 +13,8 @@
 
 namespace pe {
 
-struct RolloutLayout;
+// Largest world of a rollout (bodies); the batched engine has the same limit.
+constexpr uint32_t kRolloutMaxBodies = 8192;
 
 class Rollout {
   public:
@@ -38,6 +39,10 @@ class Rollout {
     void backward(const float *gx, const float *gq, const float *gv, const float *gw, float *gx0, float *gq0,
                   float *gv0, float *gw0, float *gmass, float *gfriction, float *grestitution, cudaStream_t s);
 
+    // Manifold capacity per body (default 2: boxes resting on one another);
+    // sparse worlds need far less.  A world that outgrows it fails the call.
+    void setManifoldCapacity(float perBody);
+
     uint64_t bodyCount() const { return nb_; }
     uint32_t worldCount() const { return (uint32_t)worldBodies_.size(); }
     uint32_t steps() const { return steps_; }
@@ -48,10 +53,12 @@ class Rollout {
 
   private:
     void checkErrors(cudaStream_t s, const char *what);
+    void ensureArena();
+    uint32_t quarterPerBody_ = 8;
 
     int device_;
     uint64_t nb_ = 0;
-    uint32_t steps_ = 0, ckEvery_ = 10, nMax_ = 0, maxPairs_ = 0, maxM_ = 0, nCk_ = 0;
+    uint32_t steps_ = 0, ckEvery_ = 10, nMax_ = 0, nCk_ = 0;
     float dt_ = 1.0f / 120.0f;
     int iterations_ = 10;
     bool haveForward_ = false;
@@ -64,11 +71,11 @@ class Rollout {
     DeviceArray<uint32_t> bodyStart_;
     DeviceArray<uint8_t> shape_, static_;
     DeviceArray<float> dims_, iinv_, mass_, mu_, rest_;
-    // per world slots
+    // per world slots, each sized by its world's body count
     DeviceArray<unsigned char> arena_;
-    size_t worldStride_ = 0;
+    DeviceArray<unsigned long long> worldOff_;
+    DeviceArray<uint32_t> order_;
     DeviceArray<uint32_t> queue_, err_;
-    std::unique_ptr<RolloutLayout> layout_;
 };
 
 } // namespace pe

@@ -40,7 +40,7 @@ struct CacheMem {
 struct ScratchMem {
     std::vector<S> aabb, mNormal, mMu, mRest, mAnchorA, mAnchorB, mDepth, pp, pm, lam, lamInit, tape;
     std::vector<uint32_t> pairA, pairB, mA, mB, mCount, mFeature, color, order, colorStart, cacheSrc, counts;
-    std::vector<unsigned long long> sortKeys, bodyUsed;
+    std::vector<unsigned long long> sortKeys, bodyUsed, bpEntries, bpPairs;
     std::vector<int32_t> match;
     ScratchMem(uint32_t n, uint32_t maxPairs, uint32_t maxM, int iterations)
         : aabb(6 * n), mNormal(3 * maxM), mMu(maxM), mRest(maxM), mAnchorA(12 * maxM), mAnchorB(12 * maxM),
@@ -48,7 +48,7 @@ struct ScratchMem {
           lamInit(12 * maxM), tape((size_t)(iterations > 0 ? iterations : 1) * maxM * kTapeScalars), pairA(maxPairs),
           pairB(maxPairs), mA(maxM), mB(maxM), mCount(maxM), mFeature(4 * maxM), color(maxM), order(maxM),
           colorStart(maxM + 1), cacheSrc(4 * maxM), counts(4), sortKeys(maxM), bodyUsed(2 * n),
-          match(4 * maxM) {}
+          bpEntries(nextPow2u(n > 0 ? n : 1)), bpPairs(nextPow2u(maxPairs > 0 ? maxPairs : 1)), match(4 * maxM) {}
     StepScratch<S> view() {
         StepScratch<S> s;
         s.aabb = aabb.data();
@@ -77,6 +77,8 @@ struct ScratchMem {
         s.tape = tape.data();
         s.cacheSrc = cacheSrc.data();
         s.counts = counts.data();
+        s.bpEntries = bpEntries.data();
+        s.bpPairs = bpPairs.data();
         return s;
     }
 };

@@ -89,6 +89,8 @@ SIGNATURES = {
     "pe_world_remove_collider": (ctypes.c_int, [_P, Handle]),
     "pe_world_get_body": (ctypes.c_int, [_P, Handle, _P]),
     "pe_debug_set_spin_limit": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint32]),
+    "pe_rollout_device_bytes": (ctypes.c_int, [_P, _P]),
+    "pe_rollout_set_manifold_capacity": (ctypes.c_int, [_P, ctypes.c_float]),
     "pe_body_make_sphere": (ctypes.c_int, [ctypes.c_float, _P, ctypes.c_float, ctypes.c_int, ctypes.c_float,
                                            ctypes.c_float, _P]),
     "pe_body_make_box": (ctypes.c_int, [ctypes.c_float, ctypes.c_float, ctypes.c_float, _P, ctypes.c_float,

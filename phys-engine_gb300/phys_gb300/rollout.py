@@ -126,7 +126,8 @@ class GpuRollout:
     parameters, as numpy arrays; ``forward`` / ``backward`` take torch CUDA
     tensors."""
 
-    def __init__(self, scenes, steps, dt, iterations=10, checkpoint_every=10, device=0, gravity=(0.0, -9.81, 0.0)):
+    def __init__(self, scenes, steps, dt, iterations=10, checkpoint_every=10, device=0, gravity=(0.0, -9.81, 0.0),
+                 manifolds_per_body=None):
         from . import engine
 
         self.lib = engine.lib()
@@ -149,6 +150,8 @@ class GpuRollout:
             int(checkpoint_every), ctypes.byref(h), _ptr(mass)))
         self.h = h
         engine.check(self.lib.pe_rollout_set_gravity(self.h, *[float(g) for g in gravity]))
+        if manifolds_per_body is not None:
+            engine.check(self.lib.pe_rollout_set_manifold_capacity(self.h, float(manifolds_per_body)))
         self.mass = mass
         self.friction = np.maximum(cat("friction", np.float32), 0).astype(np.float32)
         self.restitution = np.clip(cat("restitution", np.float32), 0, 1).astype(np.float32)
@@ -205,6 +208,11 @@ class GpuRollout:
         engine.check(self.lib.pe_rollout_backward(self.h, *[self._p(a) for a in g], *[self._p(o) for o in outs],
                                                   self._stream()))
         return outs
+
+    def device_bytes(self) -> int:
+        b = ctypes.c_uint64()
+        self.lib.pe_rollout_device_bytes(self.h, ctypes.byref(b))
+        return int(b.value)
 
     def timings(self):
         f, b = ctypes.c_double(), ctypes.c_double()
