@@ -16,10 +16,87 @@
 #include <numeric>
 #include <string>
 #include <atomic>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
 #include <thread>
 #include <vector>
 
 namespace oracle {
+
+// Persistent worker threads shared by every world, the calling thread joining
+// in (the reference keeps a world-owned pool that includes the caller,
+// src/world/step_workspace.hpp:24-172).  run() hands out jobs [0, jobs) from
+// an atomic counter to `workers` threads and returns when all are done.
+class Pool {
+  public:
+    static Pool &instance() {
+        static Pool pool;
+        return pool;
+    }
+    void run(int workers, size_t jobs, const std::function<void(size_t)> &fn) {
+        if (workers <= 1 || jobs <= 1) {
+            for (size_t j = 0; j < jobs; ++j) fn(j);
+            return;
+        }
+        std::lock_guard<std::mutex> serial(runMutex_);
+        const int helpers = workers - 1;
+        while ((int)threads_.size() < helpers) {
+            const size_t id = threads_.size();
+            threads_.emplace_back([this, id] { loop(id); });
+        }
+        {
+            std::lock_guard<std::mutex> l(m_);
+            fn_ = &fn;
+            jobs_ = jobs;
+            next_.store(0);
+            participants_ = helpers;
+            active_ = helpers;
+            ++generation_;
+        }
+        wake_.notify_all();
+        work();
+        std::unique_lock<std::mutex> l(m_);
+        done_.wait(l, [&] { return active_ == 0; });
+        fn_ = nullptr;
+    }
+    ~Pool() {
+        {
+            std::lock_guard<std::mutex> l(m_);
+            stop_ = true;
+        }
+        wake_.notify_all();
+        for (auto &t : threads_) t.join();
+    }
+
+  private:
+    void work() {
+        for (size_t j; (j = next_.fetch_add(1)) < jobs_;) (*fn_)(j);
+    }
+    void loop(size_t id) {
+        uint64_t seen = 0;
+        std::unique_lock<std::mutex> l(m_);
+        for (;;) {
+            wake_.wait(l, [&] { return stop_ || generation_ != seen; });
+            if (stop_) return;
+            seen = generation_;
+            if ((int)id >= participants_) continue;  // not needed this round
+            l.unlock();
+            work();
+            l.lock();
+            if (--active_ == 0) done_.notify_one();
+        }
+    }
+    std::mutex runMutex_, m_;
+    std::condition_variable wake_, done_;
+    std::vector<std::thread> threads_;
+    const std::function<void(size_t)> *fn_ = nullptr;
+    size_t jobs_ = 0;
+    std::atomic<size_t> next_{0};
+    int participants_ = 0, active_ = 0;
+    uint64_t generation_ = 0;
+    bool stop_ = false;
+};
 
 // ---------------------------------------------------------------------------
 // Math (include/phys/math/vec3.hpp, quaternion.hpp, mat3.hpp, math_utils.hpp,
@@ -285,14 +362,9 @@ void sapPairs(const std::vector<Aabb<T>> &bounds, std::vector<Pair> &pairs, ow_s
         size_t ranges = (size_t)threads * 16;
         std::vector<std::vector<Pair>> outs(ranges);
         std::vector<uint64_t> cmps(ranges, 0);
-        std::vector<std::thread> pool;
-        std::atomic<size_t> next{0};
-        for (int t = 0; t < threads; ++t)
-            pool.emplace_back([&] {
-                for (size_t r; (r = next.fetch_add(1)) < ranges;)
-                    sweep(entries.size() * r / ranges, entries.size() * (r + 1) / ranges, outs[r], cmps[r]);
-            });
-        for (auto &th : pool) th.join();
+        Pool::instance().run(threads, ranges, [&](size_t r) {
+            sweep(entries.size() * r / ranges, entries.size() * (r + 1) / ranges, outs[r], cmps[r]);
+        });
         for (size_t r = 0; r < ranges; ++r) {
             pairs.insert(pairs.end(), outs[r].begin(), outs[r].end());
             cmp += cmps[r];
@@ -1356,10 +1428,54 @@ template <class T> struct World : WorldBase {
             b->ang += resp;
         };
 
+        // Islands (sequential_impulse_solver.cpp:366-442): with more than one
+        // worker and at least 4,096 solved contacts the reference solves the
+        // islands (contacts joined by shared non-static bodies) in parallel,
+        // each in solve order; islands share no moving body, so the result is
+        // the serial one.
+        std::vector<uint32_t> islandStart, islandItems, islandJobs;
+        const bool parallelIslands = threads > 1 && pc.size() >= 4096;
+        if (parallelIslands) {
+            std::vector<uint32_t> parent(bodies.size());
+            std::iota(parent.begin(), parent.end(), 0u);
+            auto root = [&](uint32_t i) {
+                while (parent[i] != i) i = parent[i] = parent[parent[i]];
+                return i;
+            };
+            for (const PManifold &p : pc) {
+                if (p.a->body->isStatic || p.b->body->isStatic) continue;
+                const uint32_t ra = root(p.m->aIdx), rb = root(p.m->bIdx);
+                if (ra != rb) parent[std::max(ra, rb)] = std::min(ra, rb);
+            }
+            const uint32_t none = 0xFFFFFFFFu;
+            std::vector<uint32_t> lookup(bodies.size(), none), islandOf(pc.size()), counts, points;
+            for (size_t k = 0; k < pc.size(); ++k) {
+                const PManifold &p = pc[k];
+                const uint32_t r = root(p.a->body->isStatic ? p.m->bIdx : p.m->aIdx);
+                if (lookup[r] == none) {
+                    lookup[r] = (uint32_t)counts.size();
+                    counts.push_back(0);
+                    points.push_back(0);
+                }
+                islandOf[k] = lookup[r];
+                ++counts[lookup[r]];
+                points[lookup[r]] += p.m->pointCount;
+            }
+            islandStart.assign(counts.size() + 1, 0);
+            for (size_t i = 0; i < counts.size(); ++i) islandStart[i + 1] = islandStart[i] + counts[i];
+            std::vector<uint32_t> fill(islandStart.begin(), islandStart.end() - 1);
+            islandItems.resize(pc.size());
+            for (size_t k = 0; k < pc.size(); ++k) islandItems[fill[islandOf[k]]++] = (uint32_t)k;
+            // largest islands first (load balance only)
+            islandJobs.resize(counts.size());
+            std::iota(islandJobs.begin(), islandJobs.end(), 0u);
+            std::stable_sort(islandJobs.begin(), islandJobs.end(),
+                             [&](uint32_t x, uint32_t y) { return points[x] > points[y]; });
+        }
+
         // warmStartPrepared (sequential_impulse_solver.cpp:448-490)
         const T matchSq = T(0.05f) * T(0.05f);
-        uint64_t cmp = 0, matches = 0;
-        for (PManifold &p : pc) {
+        auto warmStartOne = [&](PManifold &p, uint64_t &cmp, uint64_t &matches) {
             Manifold<T> &m = *p.m;
             auto lo = std::lower_bound(cache.begin(), cache.end(), m, [](const Cached<T> &c, const Manifold<T> &k) {
                 return cacheLess(c.aIdx, c.aGen, c.bIdx, c.bGen, k.aIdx, k.aGen, k.bIdx, k.bGen);
@@ -1388,6 +1504,21 @@ template <class T> struct World : WorldBase {
                     break;
                 }
             }
+        };
+        uint64_t cmp = 0, matches = 0;
+        if (parallelIslands) {
+            std::vector<uint64_t> icmp(islandJobs.size(), 0), imatch(islandJobs.size(), 0);
+            Pool::instance().run(threads, islandJobs.size(), [&](size_t job) {
+                const uint32_t isl = islandJobs[job];
+                for (uint32_t o = islandStart[isl]; o < islandStart[isl + 1]; ++o)
+                    warmStartOne(pc[islandItems[o]], icmp[job], imatch[job]);
+            });
+            for (size_t j = 0; j < islandJobs.size(); ++j) {
+                cmp += icmp[j];
+                matches += imatch[j];
+            }
+        } else {
+            for (PManifold &p : pc) warmStartOne(p, cmp, matches);
         }
         ss.warm_start_comparisons = cmp;
         ss.warm_start_matches = matches;
@@ -1435,8 +1566,16 @@ template <class T> struct World : WorldBase {
                 applyTangent(*p.b, ti, rB);
             }
         };
-        for (int it = 0; it < iters; ++it)
-            for (PManifold &p : pc) solveOne(p);
+        if (parallelIslands) {
+            Pool::instance().run(threads, islandJobs.size(), [&](size_t job) {
+                const uint32_t isl = islandJobs[job];
+                for (int it = 0; it < iters; ++it)
+                    for (uint32_t o = islandStart[isl]; o < islandStart[isl + 1]; ++o) solveOne(pc[islandItems[o]]);
+            });
+        } else {
+            for (int it = 0; it < iters; ++it)
+                for (PManifold &p : pc) solveOne(p);
+        }
         ss.velocity_point_visits = prepared * (uint64_t)iters;
 
         // Cache update (sequential_impulse_solver.cpp:623-681): with sleeping
@@ -1585,14 +1724,9 @@ template <class T> struct World : WorldBase {
             results[k] = m;
         };
         if (threads > 1 && pairs.size() >= 4096) {
-            std::vector<std::thread> pool;
-            std::atomic<size_t> next{0};
-            for (int t = 0; t < threads; ++t)
-                pool.emplace_back([&] {
-                    for (size_t k; (k = next.fetch_add(64)) < pairs.size();)
-                        for (size_t e = std::min(pairs.size(), k + 64); k < e; ++k) gen(k);
-                });
-            for (auto &th : pool) th.join();
+            Pool::instance().run(threads, (pairs.size() + 63) / 64, [&](size_t chunk) {
+                for (size_t k = 64 * chunk, e = std::min(pairs.size(), k + 64); k < e; ++k) gen(k);
+            });
         } else {
             for (size_t k = 0; k < pairs.size(); ++k) gen(k);
         }

@@ -241,6 +241,17 @@ void rw_step(rw_world *w, float dt) { w->world.step(dt); }
 
 void rw_get_stats(const rw_world *w, ow_step_stats *s) { fillStats(w->world.lastStepStats(), s); }
 
+// The reference's own stage timings of its last step (ms): integrate velocity,
+// broadphase, narrowphase, solver (prepare, warm start, velocity iterations,
+// cache update), integrate pose, total.
+void rw_get_stage_ms(const rw_world *w, double *ms) {
+    const phys::StepStats &s = w->world.lastStepStats();
+    const double v[9] = {s.integrateVelocityMs,        s.broadPhaseMs,                s.narrowPhaseMs,
+                         s.solverDetails.prepareMs,    s.solverDetails.warmStartMs,   s.solverDetails.velocityIterationsMs,
+                         s.solverDetails.cacheUpdateMs, s.integratePoseMs,            s.totalMs};
+    for (int i = 0; i < 9; ++i) ms[i] = v[i];
+}
+
 uint32_t rw_contact_count(const rw_world *w) { return (uint32_t)w->world.contacts().size(); }
 void rw_get_contacts(const rw_world *w, ow_manifold *out) {
     const auto &cs = w->world.contacts();
