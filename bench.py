@@ -251,6 +251,7 @@ def run_gpu(args, rank, world_size, local_rank):
     stage_b = {k: 0 for k in ("integrate", "broadphase", "narrowphase", "solver", "pose")}
     launches = 0
     totals = {"pairs": 0, "manifolds": 0, "points": 0}
+    phases = np.zeros(7)
     if world_size > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -270,6 +271,7 @@ def run_gpu(args, rank, world_size, local_rank):
             totals["pairs"] += int(st["candidate_pairs"])
             totals["manifolds"] += int(st["contact_count"])
             totals["points"] += int(st["contact_points"])
+            phases += w.solver_phases()
         torch.cuda.synchronize()
     elapsed_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
     max_ms = max_over_ranks(elapsed_ms, world_size, f"cuda:{local_rank}")
@@ -316,6 +318,10 @@ def run_gpu(args, rank, world_size, local_rank):
             "traffic_source": traffic["source"] if traffic else None,
             "algorithmic_bytes_per_launch": stage_b[dominant] / args.steps,
             "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()},
+            # the one-cluster solver's phases (global-timer stamps of its rank 0)
+            "solver_phases_us_per_step": dict(zip(
+                ("prepare", "island_union", "island_lists", "plan_and_stage", "sweeps", "write_back", "cache"),
+                (float(x) for x in phases * 1000.0 / args.steps))),
             "whole_step": {"algorithmic_bytes_per_step": step_bytes / args.steps,
                            "achieved_gbs": step_bytes / (max_ms / 1000.0) / 1e9 / world_size,
                            "frac": step_bytes / (max_ms / 1000.0) / 1e9 / world_size / peak},

@@ -283,6 +283,12 @@ const char *pe_world_graph_error(pe_world *world);
 pe_status pe_world_step(pe_world *world, float dt);
 /* lastStepStats (physics_world.hpp:77) */
 pe_status pe_world_get_step_stats(const pe_world *world, pe_step_stats *out);
+/* Device time (ms) of the phases of the last step's one-cluster contact
+   solver, 7 values: prepare, island union, island lists, island plan +
+   staging (colouring on the colour-phase path), sweeps, write-back, cache
+   rebuild; zeros when the step solved on another path.  No reference
+   counterpart (profiling). */
+pe_status pe_world_get_solver_phases(const pe_world *world, double *ms);
 /* contacts() (physics_world.hpp:61): manifolds of the last step in candidate
    pair order with their solved impulses. */
 pe_status pe_world_get_contacts(pe_world *world, pe_contact_manifold *out, uint32_t capacity, uint32_t *count);

@@ -744,6 +744,12 @@ pe_status pe_world_get_step_stats(const pe_world *world, pe_step_stats *out) {
     return PE_OK;
 }
 
+pe_status pe_world_get_solver_phases(const pe_world *world, double *ms) {
+    if (!world || !ms) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
+    for (int k = 0; k < 7; ++k) ms[k] = world->w->counters().solverPhaseMs[k];
+    return PE_OK;
+}
+
 pe_status pe_world_get_contacts(pe_world *world, pe_contact_manifold *out, uint32_t capacity, uint32_t *count) {
     if (!world || !count) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
     return guarded([&] {

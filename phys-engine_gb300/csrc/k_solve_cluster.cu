@@ -317,7 +317,7 @@ __device__ void solveIslandAlone(const SolveArgs &a, const IslandPlan &P) {
 constexpr uint32_t kIslandUnits = 32;  // warp units per rank
 
 __device__ void solveIslandsRank(const SolveArgs &a, const ClusterSolveLayout &lay, unsigned char *smem, uint32_t ownRoot,
-                                 IslandShared &is) {
+                                 IslandShared &is, bool stamper) {
     const SolverBuffers &sb = a.sb;
     const WorldView &w = a.w;
     const uint32_t tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
@@ -394,6 +394,7 @@ __device__ void solveIslandsRank(const SolveArgs &a, const ClusterSolveLayout &l
         if (!packed) solveIslandAlone(a, P);
     }
     __syncthreads();
+    if (stamper) a.st->solverStamp[4] = globalNs();
     // warp units: pass by pass (pass 0: warm start), colour by colour
     const LocalOnlyPrep pr{a, spm, spn, sm, scnt, soff, spt, lay.pointCap};
     const SharedVel v{sv, sslot};
@@ -410,6 +411,7 @@ __device__ void solveIslandsRank(const SolveArgs &a, const ClusterSolveLayout &l
             }
     }
     __syncthreads();
+    if (stamper) a.st->solverStamp[5] = globalNs();
     if (packed) {
         for (uint32_t t = 0; t < P.n; ++t) {
             const uint32_t m = P.ks[t], L = L0 + t;
@@ -446,6 +448,11 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
         if (rank == 0 && tid == 0) atomicOr(&a.st->err, kErrSmallPath);
         return;
     }
+    const bool stamper = rank == 0 && tid == 0;
+    auto stamp = [&](int k) {
+        if (stamper) a.st->solverStamp[k] = globalNs();
+    };
+    stamp(0);
 
     // ---- 0. all ranks: manifold flags, island sets, prepare ----
     // (manifolds spread over all SMs: their scattered loads are what costs time)
@@ -481,6 +488,7 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
     }
     __threadfence();
     cluster.sync();
+    stamp(1);
     // ---- 1. islands: union of the two dynamic bodies of every solved manifold ----
     for (uint32_t m = g; m < M; m += G) {
         const uint32_t fl = __ldcg(&sb.dyn[m]);
@@ -489,6 +497,7 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
     }
     __threadfence();
     cluster.sync();
+    stamp(2);
     // ---- 2. each solved manifold joins its island's list; the first to join
     // owns the island (M <= blockM <= threads of the cluster: one manifold per
     // thread) ----
@@ -512,16 +521,19 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
     }
     __threadfence();
     cluster.sync();
+    stamp(3);
     // The island path needs the cache in manifold order (one manifold per body
     // pair): a cache sorted over the solve order needs the order, which only
     // the colour-phase path materialises.
     if (__ldcg(&sb.counters[2]) == 0 && G >= M && a.pairOrderCache) {
         // ---- island path ----
         if (g == 0) atomicMax(&a.st->colorRounds, 1u);  // one round when nothing is coloured
-        solveIslandsRank(a, lay, smem, ownRoot, cs.island);
+        solveIslandsRank(a, lay, smem, ownRoot, cs.island, stamper);
         __threadfence();
         cluster.sync();
+        stamp(6);
         solveClusterCache(a, nc, cacheCap, newCount, M, rank, smem, s_sort, s_dyn, cs);
+        stamp(7);
         return;
     }
 
@@ -544,6 +556,7 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
     }
     __threadfence();
     cluster.sync();
+    stamp(4);
     if (__ldcg(&a.st->colors) > (uint32_t)kMaxColors) {
         // More colours than the cluster's shared colour ranges hold (a body
         // touching more than ~64 others): the step is re-run on the
@@ -638,6 +651,7 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
             for (uint32_t L = cs.lstart[c] + tid; L < cs.lstart[c + 1]; L += nt) solveOne(pr, L, L, cv);
             cluster.sync();
         }
+    stamp(5);
 
     // ---- 4. velocities and impulses back; the warm-start cache ----
     for (uint32_t i = tid; rank + kClusterRanks * i < S; i += nt) {
@@ -655,7 +669,9 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
     }
     __threadfence();
     cluster.sync();
+    stamp(6);
     solveClusterCache(a, nc, cacheCap, newCount, M, rank, smem, s_sort, s_dyn, cs);
+    stamp(7);
 }
 
 // Layout of one rank's dynamic shared memory (kClusterSmemMax bytes): the

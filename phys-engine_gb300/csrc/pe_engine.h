@@ -123,6 +123,10 @@ struct DevStats {
     uint32_t pad0;
     int32_t cellLo[3];
     int32_t cellHi[3];
+    // Phase boundaries of the one-cluster solver (global timer, ns; zero when
+    // it did not run): start, prepare done, islands united, island lists,
+    // islands planned and staged, sweeps done, results written, cache rebuilt.
+    unsigned long long solverStamp[8];
     // Stage boundaries (global timer, ns), written by the stage kernels
     // themselves instead of event nodes in the step graph: integrate start,
     // integrate end (latest block), narrowphase start, narrowphase end (last

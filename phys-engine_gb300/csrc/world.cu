@@ -890,6 +890,10 @@ bool World::finishStep() {
     solveSkipped_ = sleepingEnabled && h.solveCount == 0;
     c.colors = orderMode == 0 ? h.manifolds : solveSkipped_ ? (h.manifolds ? 1u : 0u) : h.colors;
     c.colorRounds = h.colorRounds;
+    for (int k = 0; k < 7; ++k) {
+        const unsigned long long t0 = h.solverStamp[k], t1 = h.solverStamp[k + 1];
+        c.solverPhaseMs[k] = (h.solverStamp[0] && t0 && t1 > t0) ? (t1 - t0) * 1e-6 : 0.0;
+    }
     c.epaFailures = h.epaFailures;
     c.points = h.points;
     lastPairs_ = h.pairs;

@@ -95,6 +95,10 @@ struct StepCounters {
     double integrateMs = 0, broadphaseMs = 0, narrowphaseMs = 0, solverMs = 0, poseMs = 0;
     uint64_t kernelLaunches = 0;
     bool graphed = false;  // the step ran from a captured CUDA graph
+    // device time of the one-cluster solver's phases (ms; zero when it did not
+    // run): prepare, island union, island lists, plan + staging (or colouring),
+    // sweeps, write-back, cache rebuild
+    double solverPhaseMs[7] = {0, 0, 0, 0, 0, 0, 0};
 };
 
 // Copies M manifolds of a device manifold view into pe_contact_manifold records.

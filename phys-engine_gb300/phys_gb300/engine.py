@@ -90,6 +90,7 @@ SIGNATURES = {
     "pe_world_get_body": (ctypes.c_int, [_P, Handle, _P]),
     "pe_debug_set_spin_limit": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint32]),
     "pe_rollout_device_bytes": (ctypes.c_int, [_P, _P]),
+    "pe_world_get_solver_phases": (ctypes.c_int, [_P, _P]),
     "pe_rollout_set_manifold_capacity": (ctypes.c_int, [_P, ctypes.c_float]),
     "pe_body_make_sphere": (ctypes.c_int, [ctypes.c_float, _P, ctypes.c_float, ctypes.c_int, ctypes.c_float,
                                            ctypes.c_float, _P]),
@@ -412,6 +413,13 @@ class GpuWorld:
         s = _P()
         check(self.lib.pe_world_get_stream(self.h, ctypes.byref(s)))
         return s.value or 0
+
+    def solver_phases(self):
+        """Device ms of the one-cluster solver's phases in the last step:
+        prepare, union, lists, plan + staging, sweeps, write-back, cache."""
+        ms = np.zeros(7, np.float64)
+        check(self.lib.pe_world_get_solver_phases(self.h, _ptr(ms)))
+        return ms
 
     def stats(self):
         s = np.zeros(1, STATS_DTYPE)
