@@ -49,6 +49,14 @@ __device__ __forceinline__ void integrateAabbOne(const WorldView &w, uint32_t *s
         colliderAabb(w, i, t, mn, mx);
         w.aabbMin[i] = make4(mn, 0.0f);
         w.aabbMax[i] = make4(mx, 0.0f);
+        if (w.npRec) {
+            const float4 s = w.cshape[i], m = w.mat[b];
+            float4 *r = w.npRec + 4 * (size_t)i;
+            r[0] = make_float4(t.p.x, t.p.y, t.p.z, s.x);
+            r[1] = make_float4(t.q.x, t.q.y, t.q.z, t.q.w);
+            r[2] = make_float4(s.y, s.z, s.w, __uint_as_float(cf));
+            r[3] = make_float4(m.y, m.z, __uint_as_float(b), __uint_as_float(w.cbgen[i]));
+        }
         if (sapKeys) {
             sapKeys[i] = orderedFloatKey(mn.x);
             if (sapVals) sapVals[i] = i;

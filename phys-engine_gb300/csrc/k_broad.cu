@@ -504,8 +504,8 @@ __device__ __forceinline__ bool cellFloorFast(float x, float invf, int &cellOut)
 
 __global__ void __launch_bounds__(256)
 k_hgrid_insert(BroadInput in, DevStats *st, int4 *firstCell, uint8_t *inGrid, uint32_t *overflow, double cell,
-               float inv, uint32_t *bucketHead, uint32_t logB, unsigned long long *keys, uint32_t *vals,
-               uint32_t *next, uint32_t ecap, unsigned long long *zeroState, uint32_t nZeroState) {
+               float inv, uint32_t *bucketHead, uint32_t logB, uint4 *entryRec, float4 *cand, uint32_t ecap,
+               unsigned long long *zeroState, uint32_t nZeroState) {
     __shared__ uint32_t s_scan[9], s_base;
     const uint32_t n = *in.d_n;
     // look-back states of the kernels that follow (cleared here, not by memsets)
@@ -571,6 +571,8 @@ k_hgrid_insert(BroadInput in, DevStats *st, int4 *firstCell, uint8_t *inGrid, ui
                 firstCell[i] = make_int4(first[0], first[1], first[2], counts[0] | (counts[1] << 8) | (counts[2] << 16));
                 inGrid[i] = 1;
                 total = cells;
+                cand[2 * i] = make_float4(mn.x, mn.y, mn.z, __uint_as_float((uint32_t)k0));
+                cand[2 * i + 1] = make_float4(mx.x, mx.y, mx.z, __uint_as_float((uint32_t)(k0 >> 32)));
             }
         }
         // entry slots: block scan of the cell counts, one atomic per block
@@ -586,9 +588,8 @@ k_hgrid_insert(BroadInput in, DevStats *st, int4 *firstCell, uint8_t *inGrid, ui
                     if (e >= ecap) continue;  // the host re-runs the step with more entry slots
                     unsigned long long key;
                     cellKey21(first[0] + x, first[1] + y, first[2] + z, key);
-                    keys[e] = key;
-                    vals[e] = i;
-                    next[e] = atomicExch(&bucketHead[bucketOf(key, logB)], e);
+                    const uint32_t nx = atomicExch(&bucketHead[bucketOf(key, logB)], e);
+                    entryRec[e] = make_uint4((uint32_t)key, (uint32_t)(key >> 32), i, nx);
                 }
     }
 }
@@ -596,8 +597,8 @@ k_hgrid_insert(BroadInput in, DevStats *st, int4 *firstCell, uint8_t *inGrid, ui
 // Per-body pairs from the buckets (the counterpart of k_grid_body_pairs).
 __global__ void __launch_bounds__(kBodyPairThreads)
 k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const uint32_t *overflow,
-              const uint32_t *bucketHead, uint32_t logB, uint32_t ecap, const unsigned long long *ekeys,
-              const uint32_t *evals, const uint32_t *enext, const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen,
+              const uint32_t *bucketHead, uint32_t logB, uint32_t ecap, const uint4 *__restrict__ entryRec,
+              const float4 *__restrict__ cand, const uint32_t *inSlot, const uint32_t *cbody, const uint32_t *cbgen,
               uint32_t *pairA, uint32_t *pairB, uint32_t cap, DevStats *st, unsigned long long *state,
               uint32_t *counter) {
     __shared__ uint32_t s_tile, s_scan[9], s_prefix, s_abort;
@@ -626,6 +627,8 @@ k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const
             if (inGrid[a]) {
                 const int cx = fa.w & 0xFF, cy = (fa.w >> 8) & 0xFF, cz = (fa.w >> 16) & 0xFF;
                 const int cells = cx * cy * cz;
+                unsigned long long faKey;
+                cellKey21(fa.x, fa.y, fa.z, faKey);
                 // The list heads of four cells are requested together; then each
                 // list node's key, body and link in one round trip, and a
                 // candidate's box and cell range in one more.  Partners are
@@ -652,7 +655,7 @@ k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const
                         }
                     }
                     // the four lists are walked side by side: one round trip
-                    // per hop for all of them
+                    // (one 16-byte record per list) per hop for all of them
                     uint32_t e[4] = {head[0], head[1], head[2], head[3]};
                     for (uint32_t hops = 0; hops < ecap; ++hops) {
                         unsigned long long k2[4];
@@ -663,9 +666,10 @@ k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const
                             k2[j] = 0;
                             bv[j] = 0;
                             if (e[j] < ecap) {
-                                k2[j] = ekeys[e[j]];
-                                bv[j] = evals[e[j]];
-                                e[j] = enext[e[j]];
+                                const uint4 r = entryRec[e[j]];
+                                k2[j] = ((unsigned long long)r.y << 32) | r.x;
+                                bv[j] = r.z;
+                                e[j] = r.w;
                                 live = true;
                             } else {
                                 k2[j] = ~key[j];  // no match
@@ -675,14 +679,19 @@ k_hgrid_pairs(BroadInput in, const int4 *firstCell, const uint8_t *inGrid, const
 #pragma unroll
                         for (int j = 0; j < 4; ++j) {
                             const uint32_t b = bv[j];
-                            if (k2[j] != key[j] || b <= a) continue;
+                            if (k2[j] != key[j] || b <= a || b >= n) continue;
                             ++cmp;
-                            const float4 bmn = in.mn[b], bmx = in.mx[b];
-                            const int4 fb = firstCell[b];
-                            if (!overlaps(amn, amx, bmn, bmx)) continue;
-                            unsigned long long low;
-                            cellKey21(max(fa.x, fb.x), max(fa.y, fb.y), max(fa.z, fb.z), low);
-                            if (low == key[j]) add(b);
+                            // the candidate's box and first cell: one sector
+                            const float4 c0 = cand[2 * b], c1 = cand[2 * b + 1];
+                            if (!overlaps(amn, amx, c0, c1)) continue;
+                            const unsigned long long fbKey =
+                                ((unsigned long long)__float_as_uint(c1.w) << 32) | __float_as_uint(c0.w);
+                            // the lowest cell both boxes cover: per-axis maxima
+                            // of the biased 21-bit coordinate fields
+                            const unsigned long long fx = max(faKey >> 42, fbKey >> 42);
+                            const unsigned long long fy = max((faKey >> 21) & 0x1FFFFFull, (fbKey >> 21) & 0x1FFFFFull);
+                            const unsigned long long fz = max(faKey & 0x1FFFFFull, fbKey & 0x1FFFFFull);
+                            if (((fx << 42) | (fy << 21) | fz) == key[j]) add(b);
                         }
                     }
                 }
@@ -765,8 +774,7 @@ void launchGridBodyPairs(const BroadInput &in, const BroadBuffers &bb, PairBuffe
     const uint32_t grid = tiles < maxGrid ? tiles : maxGrid;
     if (bb.hashed) {
         k_hgrid_pairs<<<grid, kBodyPairThreads, 0, s>>>(in, bb.firstCell, bb.inGrid, bb.overflow, bb.bucketHead,
-                                                         bb.logBuckets, bb.entryCap, bb.entryKeys, bb.entryVals,
-                                                         bb.entryNext, inSlot,
+                                                         bb.logBuckets, bb.entryCap, bb.entryRec, bb.cand, inSlot,
                                                          cbody, cbgen, pb.a, pb.b, pb.cap, st, ws.scanState,
                                                          (uint32_t *)(ws.scanState + tiles));
         PE_LAUNCHED();
@@ -882,8 +890,8 @@ void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBu
         if (!bb.headsCleared) PE_CHECK(cudaMemsetAsync(bb.bucketHead, 0xFF, B * sizeof(uint32_t), s));
         k_hgrid_insert<<<gridFor(in.maxN), 256, 0, s>>>(in, st, bb.firstCell, bb.inGrid, bb.overflow, fixedCell,
                                                         (float)(1.0 / fixedCell), bb.bucketHead, bb.logBuckets,
-                                                        bb.entryKeys, bb.entryVals, bb.entryNext, bb.entryCap,
-                                                        bb.zeroState, bb.nZeroState);
+                                                        bb.entryRec, bb.cand, bb.entryCap, bb.zeroState,
+                                                        bb.nZeroState);
         PE_LAUNCHED();
         return;
     }

@@ -34,15 +34,32 @@ k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *_
     LocalManifold lm;
     lm.count = 0;
     bool hit = false;
-    uint32_t ca = 0, cb = 0, ba = 0, bb = 0, category = 0;
+    uint32_t ca = 0, cb = 0, ba = 0, bb = 0, ga = 0, gb = 0, category = 0;
     float restitution = 0.0f, friction = 0.0f;
     if (p < P) {
         ca = pairA[p];
         cb = pairB[p];
-        ba = w.cbody[ca];
-        bb = w.cbody[cb];
         bool epaFailed;
-        hit = narrowphasePair(w, ca, cb, ba, bb, lm, restitution, friction, category, epaFailed);
+        if (w.npRec) {
+            // both colliders' packed records: one 64-byte line each
+            float4 ra[4], rb[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                ra[k] = w.npRec[4 * (size_t)ca + k];
+                rb[k] = w.npRec[4 * (size_t)cb + k];
+            }
+            ba = __float_as_uint(ra[3].z);
+            bb = __float_as_uint(rb[3].z);
+            ga = __float_as_uint(ra[3].w);
+            gb = __float_as_uint(rb[3].w);
+            hit = narrowphasePairRec(w, ca, cb, ra, rb, lm, restitution, friction, category, epaFailed);
+        } else {
+            ba = w.cbody[ca];
+            bb = w.cbody[cb];
+            ga = w.cbgen[ca];
+            gb = w.cbgen[cb];
+            hit = narrowphasePair(w, ca, cb, ba, bb, lm, restitution, friction, category, epaFailed);
+        }
         if (epaFailed) atomicAdd(&st->epaFailures, 1ull);
         aggregatedCount(st->npCandidates, category);
         if (hit) aggregatedCount(st->npContacts, category);
@@ -61,7 +78,7 @@ k_narrowphase(WorldView w, const uint32_t *__restrict__ pairA, const uint32_t *_
     if (s_abort) return;  // a bounded wait ran out: nothing of this tile is written
     const uint32_t m = s_prefix + local;
     if (hit) {
-        if (m < mcap) storeManifold(out, m, w, ca, cb, ba, bb, lm, restitution, friction);
+        if (m < mcap) storeManifoldGen(out, m, ba, ga, bb, gb, lm, restitution, friction);
         aggregatedAdd32(&st->points, (uint32_t)lm.count);
     }
     if (threadIdx.x == 0 && tile + 1 == ntiles) {

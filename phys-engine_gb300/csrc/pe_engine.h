@@ -160,6 +160,12 @@ struct WorldView {
     const float4 *hullVerts;
     float4 *aabbMin;
     float4 *aabbMax;
+    // nullable: per collider slot c, the narrowphase's view of the collider in
+    // one 64-byte line, written with its box by the integrate kernel:
+    // [4c] world position, dims.x; [4c+1] world rotation; [4c+2] dims.y,
+    // dims.z, dims.w (hull index bits), collider flags (bits); [4c+3] the
+    // body's restitution, friction, body index (bits), body generation (bits)
+    float4 *npRec;
     float gx, gy, gz, dt;
     // Sleeping (zero / null when off).  Sleep flags and quiet times are read
     // from the step's input copy and written to its output copy; parent,

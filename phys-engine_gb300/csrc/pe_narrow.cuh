@@ -562,15 +562,86 @@ __device__ inline bool narrowphasePair(const WorldView &w, uint32_t ca, uint32_t
     return hit;
 }
 
-// Writes one manifold record in pair order: body handles from the colliders,
-// collider-space anchors already moved to body space, zero impulses.
-__device__ __forceinline__ void storeManifold(const ManifoldView &out, uint32_t m, const WorldView &w, uint32_t ca,
-                                              uint32_t cb, uint32_t ba, uint32_t bb, const LocalManifold &lm,
-                                              float restitution, float friction) {
+// narrowphasePair with both colliders read from their packed records
+// (WorldView::npRec, written by the integrate kernel with the same world
+// transforms, shapes and materials): one 64-byte line per collider instead of
+// a gather from a dozen arrays.  ra / rb: the four float4 of each record.
+__device__ inline bool narrowphasePairRec(const WorldView &w, uint32_t ca, uint32_t cb, const float4 *ra,
+                                          const float4 *rb, LocalManifold &lm, float &restitution, float &friction,
+                                          uint32_t &category, bool &epaFailed) {
+    epaFailed = false;
+    lm.count = 0;
+    const uint32_t sa = colliderShape(__float_as_uint(ra[2].w)), sb = colliderShape(__float_as_uint(rb[2].w));
+    const Tf tA{V3{ra[0].x, ra[0].y, ra[0].z}, Q{ra[1].x, ra[1].y, ra[1].z, ra[1].w}};
+    const Tf tB{V3{rb[0].x, rb[0].y, rb[0].z}, Q{rb[1].x, rb[1].y, rb[1].z, rb[1].w}};
+    const float4 sha = make_float4(ra[0].w, ra[2].x, ra[2].y, ra[2].z);
+    const float4 shb = make_float4(rb[0].w, rb[2].x, rb[2].y, rb[2].z);
+    bool hit;
+    if (sa == kShapeHull || sb == kShapeHull) {
+        category = 3;
+        auto support = [&](uint32_t shape, const float4 &sh, const Tf &t) {
+            SupportShape s;
+            s.shape = shape;
+            s.radius = sh.x;
+            s.he = V3{sh.x, sh.y, sh.z};
+            s.tf = t;
+            s.verts = nullptr;
+            s.nverts = 0;
+            if (shape == kShapeHull) {
+                const uint32_t h = __float_as_uint(sh.w);
+                const uint32_t b = w.hullOffset[h];
+                s.verts = w.hullVerts + b;
+                s.nverts = w.hullOffset[h + 1] - b;
+            }
+            return s;
+        };
+        hit = hullContact(support(sa, sha, tA), support(sb, shb, tB), lm, epaFailed);
+    } else {
+        category = sa + sb;
+        if (sa == kShapeSphere && sb == kShapeSphere) {
+            hit = sphereSphere(sha.x, tA, shb.x, tB, lm);
+        } else if (sa == kShapeSphere) {
+            hit = sphereBox(sha.x, tA, V3{shb.x, shb.y, shb.z}, tB, lm);
+        } else if (sb == kShapeSphere) {
+            hit = sphereBox(shb.x, tB, V3{sha.x, sha.y, sha.z}, tA, lm);
+            if (hit) {
+                lm.normal = -lm.normal;
+                for (uint32_t k = 0; k < lm.count; ++k) {
+                    V3 t = lm.anchorA[k];
+                    lm.anchorA[k] = lm.anchorB[k];
+                    lm.anchorB[k] = t;
+                }
+            }
+        } else {
+            hit = boxBox(V3{sha.x, sha.y, sha.z}, tA, V3{shb.x, shb.y, shb.z}, tB, lm);
+        }
+    }
+    if (hit) {
+        // anchors from collider space to body space (local transforms only
+        // when some collider has one)
+        const V3 lpa = w.clpos ? f4xyz(w.clpos[ca]) : V3{0.0f, 0.0f, 0.0f};
+        const Q lqa = w.clrot ? f4q(w.clrot[ca]) : qidentity();
+        const V3 lpb = w.clpos ? f4xyz(w.clpos[cb]) : V3{0.0f, 0.0f, 0.0f};
+        const Q lqb = w.clrot ? f4q(w.clrot[cb]) : qidentity();
+        for (uint32_t k = 0; k < lm.count; ++k) {
+            lm.anchorA[k] = lpa + rotate(lqa, lm.anchorA[k]);
+            lm.anchorB[k] = lpb + rotate(lqb, lm.anchorB[k]);
+        }
+        restitution = smax(ra[3].x, rb[3].x);
+        friction = sqrtf(smax(ra[3].y, 0.0f) * smax(rb[3].y, 0.0f));
+    }
+    return hit;
+}
+
+// Writes one manifold record in pair order: body handles, collider-space
+// anchors already moved to body space, zero impulses.
+__device__ __forceinline__ void storeManifoldGen(const ManifoldView &out, uint32_t m, uint32_t ba, uint32_t genA,
+                                                 uint32_t bb, uint32_t genB, const LocalManifold &lm,
+                                                 float restitution, float friction) {
     out.bodyA[m] = ba;
-    out.genA[m] = w.cbgen[ca];
+    out.genA[m] = genA;
     out.bodyB[m] = bb;
-    out.genB[m] = w.cbgen[cb];
+    out.genB[m] = genB;
     out.normalFriction[m] = make4(lm.normal, friction);
     out.restitution[m] = restitution;
     out.pointCount[m] = lm.count;
@@ -581,6 +652,13 @@ __device__ __forceinline__ void storeManifold(const ManifoldView &out, uint32_t 
         out.impulse[4 * m + k] = make_float4(0, 0, 0, 0);
         out.feature[4 * m + k] = live ? lm.feature[k] : 0u;
     }
+}
+
+// storeManifold with the body handles taken from the colliders.
+__device__ __forceinline__ void storeManifold(const ManifoldView &out, uint32_t m, const WorldView &w, uint32_t ca,
+                                              uint32_t cb, uint32_t ba, uint32_t bb, const LocalManifold &lm,
+                                              float restitution, float friction) {
+    storeManifoldGen(out, m, ba, w.cbgen[ca], bb, w.cbgen[cb], lm, restitution, friction);
 }
 
 } // namespace pe

@@ -44,6 +44,12 @@ struct BroadBuffers {
     uint32_t nZeroState;
     uint32_t logBuckets;
     bool hashed;
+    // hashed grid, packed for the pair walk: entry e = (cell key low, cell key
+    // high, body, next entry) in one 16-byte record; body i's candidate record
+    // = (min.xyz, first-cell key low) and (max.xyz, first-cell key high), one
+    // 32-byte sector
+    uint4 *entryRec;   // [entryCap]
+    float4 *cand;      // [2 * maxN]
 };
 
 // Linear BVH of the DynamicTree selector (k_lbvh.cu), sized for maxN leaves.

@@ -483,6 +483,7 @@ void World::ensureCapacity() {
     }
     aabbMin_.reserve(nc);
     aabbMax_.reserve(nc);
+    npRec_.reserve(4 * (size_t)nc);
     collectFlags_.reserve(nc);
     collectPos_.reserve(nc);
     inSlot_.reserve(nc);
@@ -518,11 +519,13 @@ void World::ensureCapacity() {
     while ((1u << logB) < 2u * nc && logB < 30) ++logB;
     bbBucketHead_.reserve(1u << logB);
     bbEntryNext_.reserve(entryCap_);
+    bbEntryRec_.reserve(entryCap_);
+    bbCand_.reserve(2 * (size_t)nc);
     bb_ = BroadBuffers{bbKeyTmp32_.ptr, bbValTmp_.ptr, bbMinX_.ptr, bbMaxX_.ptr, bbYZ_.ptr, bbIdx_.ptr, bbLen_.ptr,
                        bbOff_.ptr, bbWidth_.ptr, bbWidthTmp_.ptr, bbFirst_.ptr, bbCellCount_.ptr, bbInGrid_.ptr,
                        bbOverflow_.ptr, bbEntryOff_.ptr, bbEntryKeys_.ptr, bbEntryKeysTmp_.ptr, bbEntryVals_.ptr,
                        bbEntryValsTmp_.ptr, entryCap_, gridKeyBits_, bbCounters_.ptr, bbBucketHead_.ptr,
-                       bbEntryNext_.ptr, false, nullptr, 0, logB, false};
+                       bbEntryNext_.ptr, false, nullptr, 0, logB, false, bbEntryRec_.ptr, bbCand_.ptr};
 
     if (pairCap_ < 4u * nc) pairCap_ = std::max<uint32_t>(65536, 4u * nc);
     pairKeys_.reserve(pairCap_);
@@ -724,6 +727,7 @@ WorldView World::view(float dt) {
     w.hullVerts = hullVerts_.ptr;
     w.aabbMin = aabbMin_.ptr;
     w.aabbMax = aabbMax_.ptr;
+    w.npRec = npRec_.ptr;
     w.gx = gravity[0];
     w.gy = gravity[1];
     w.gz = gravity[2];

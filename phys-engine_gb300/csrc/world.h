@@ -245,7 +245,7 @@ class World {
     bool solveSkipped_ = false;  // the last step solved nothing: every body asleep
     float sleepGravity_[3] = {0, 0, 0};  // PhysicsWorld::sleepGravity
     DeviceArray<uint32_t> cbody_, cbgen_, cflags_;
-    DeviceArray<float4> cshape_, clpos_, clrot_, aabbMin_, aabbMax_;
+    DeviceArray<float4> cshape_, clpos_, clrot_, aabbMin_, aabbMax_, npRec_;
     DeviceArray<uint32_t> hullOffset_;
     DeviceArray<float4> hullVerts_;
     // broadphase input compaction
@@ -255,6 +255,8 @@ class World {
     // broadphase / pairs
     BroadBuffers bb_{};
     DeviceArray<uint32_t> bbBucketHead_, bbEntryNext_;
+    DeviceArray<uint4> bbEntryRec_;
+    DeviceArray<float4> bbCand_;
     DeviceArray<uint32_t> bbKeyTmp32_, bbValTmp_, bbIdx_, bbLen_, bbOff_, bbCellCount_, bbOverflow_, bbEntryOff_,
         bbEntryVals_, bbEntryValsTmp_, bbCounters_;
     DeviceArray<float> bbMinX_, bbMaxX_;
