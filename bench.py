@@ -251,7 +251,7 @@ def run_gpu(args, rank, world_size, local_rank):
     stage_b = {k: 0 for k in ("integrate", "broadphase", "narrowphase", "solver", "pose")}
     launches = 0
     totals = {"pairs": 0, "manifolds": 0, "points": 0}
-    phases = np.zeros(7)
+    phases = np.zeros(8)
     if world_size > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -320,7 +320,8 @@ def run_gpu(args, rank, world_size, local_rank):
             "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()},
             # the one-cluster solver's phases (global-timer stamps of its rank 0)
             "solver_phases_us_per_step": dict(zip(
-                ("prepare", "island_union", "island_lists", "plan_and_stage", "sweeps", "write_back", "cache"),
+                ("gap_after_narrowphase", "prepare_kernel", "gap_to_cluster", "island_lists", "plan_and_stage",
+                 "sweeps", "write_back_and_cache", "gap_to_pose"),
                 (float(x) for x in phases * 1000.0 / args.steps))),
             "whole_step": {"algorithmic_bytes_per_step": step_bytes / args.steps,
                            "achieved_gbs": step_bytes / (max_ms / 1000.0) / 1e9 / world_size,

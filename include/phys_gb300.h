@@ -284,10 +284,14 @@ pe_status pe_world_step(pe_world *world, float dt);
 /* lastStepStats (physics_world.hpp:77) */
 pe_status pe_world_get_step_stats(const pe_world *world, pe_step_stats *out);
 /* Device time (ms) of the phases of the last step's one-cluster contact
-   solver, 7 values: prepare, island union, island lists, island plan +
-   staging (colouring on the colour-phase path), sweeps, write-back, cache
-   rebuild; zeros when the step solved on another path.  No reference
-   counterpart (profiling). */
+   solver, 8 values: the gap from the narrowphase's end to the prepare
+   kernel's start, the prepare kernel (prepare, manifold flags, island
+   unions), the gap to the cluster kernel's start, island lists, island plan +
+   staging (colouring on the colour-phase path), sweeps (island path: with
+   each warp's results and cache entries; colour-phase path: with the
+   staging), write-back and cache rebuild (colour-phase path only), the gap
+   from the solver's end to the pose kernel's start; zeros when the step
+   solved on another path.  No reference counterpart (profiling). */
 pe_status pe_world_get_solver_phases(const pe_world *world, double *ms);
 /* contacts() (physics_world.hpp:61): manifolds of the last step in candidate
    pair order with their solved impulses. */

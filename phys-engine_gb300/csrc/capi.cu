@@ -746,7 +746,7 @@ pe_status pe_world_get_step_stats(const pe_world *world, pe_step_stats *out) {
 
 pe_status pe_world_get_solver_phases(const pe_world *world, double *ms) {
     if (!world || !ms) return fail(PE_ERR_INVALID_ARGUMENT, "null argument");
-    for (int k = 0; k < 7; ++k) ms[k] = world->w->counters().solverPhaseMs[k];
+    for (int k = 0; k < 8; ++k) ms[k] = world->w->counters().solverPhaseMs[k];
     return PE_OK;
 }
 

@@ -120,12 +120,14 @@ struct DevStats {
     uint32_t carried;        // sleeping on: warm-start entries carried for sleeping contacts
     uint32_t awakeInStep;    // sleeping on: live dynamic bodies awake after the contact wake pass
     uint32_t solveCount;     // sleeping on: manifolds handed to the solver (0 when no body is awake)
-    uint32_t pad0;
+    uint32_t islandRefused;  // one-cluster solver: the island path cannot take this step
     int32_t cellLo[3];
     int32_t cellHi[3];
     // Phase boundaries of the one-cluster solver (global timer, ns; zero when
-    // it did not run): start, prepare done, islands united, island lists,
-    // islands planned and staged, sweeps done, results written, cache rebuilt.
+    // it did not run): prepare kernel start, its end (last block), cluster
+    // kernel start, island lists done, planned (coloured) and staged, sweeps
+    // done (island path: with the results and the cache, on the last rank),
+    // then on the colour-phase path results written, cache rebuilt.
     unsigned long long solverStamp[8];
     // Stage boundaries (global timer, ns), written by the stage kernels
     // themselves instead of event nodes in the step graph: integrate start,

@@ -116,168 +116,220 @@ __device__ __forceinline__ bool solvedPair(const WorldView &w, uint32_t flA, uin
 // prepareBody (:275-287) + prepareContactPoints (:101-214) + the cache lookup
 // of warmStartPrepared (:448-490).  Data are written by manifold index m (no
 // dependence on the solve order, so prepare may run before the colouring).
+// Work items are (manifold, point) pairs q = p M + m (all point-0 items first,
+// so consecutive threads take consecutive manifolds): a manifold's points are
+// independent here, so the slowest point, not the sum of a manifold's points,
+// bounds the pass.  Each item reads its manifold's data; point 0's item also
+// writes the per-manifold outputs.
+
+// One item's manifold data.  Every field is requested at once (the point's
+// anchors and impulse are in bounds for any p < 4), before the item is known
+// to be live.
+struct PrepItem {
+    uint32_t m, p, npts, ia, ib, gA, gB;
+    float4 nf, aa, ab, imp;
+    float rest;
+};
+__device__ __forceinline__ PrepItem loadPrepItemAt(const SolveArgs &a, uint32_t m, uint32_t p) {
+    PrepItem t;
+    t.m = m;
+    t.p = p;
+    t.npts = a.mv.pointCount[m];
+    t.ia = a.mv.bodyA[m];
+    t.ib = a.mv.bodyB[m];
+    t.gA = a.mv.genA[m];
+    t.gB = a.mv.genB[m];
+    t.nf = a.mv.normalFriction[m];
+    t.rest = a.mv.restitution[m];
+    t.aa = a.mv.anchorA[4 * m + p];
+    t.ab = a.mv.anchorB[4 * m + p];
+    t.imp = a.mv.impulse[4 * m + p];
+    return t;
+}
+__device__ __forceinline__ PrepItem loadPrepItem(const SolveArgs &a, uint32_t q, uint32_t M) {
+    const uint32_t p = q / M;
+    return loadPrepItemAt(a, q - p * M, p);
+}
+
+struct PrepTally {
+    uint64_t prepared = 0, comparisons = 0, matches = 0;
+    uint32_t solved = 0;
+};
+__device__ __forceinline__ void flushPrepTally(const SolveArgs &a, const PrepTally &t) {
+    aggregatedAdd32(&a.st->solved, t.solved);
+    aggregatedAdd64(&a.st->preparedPoints, t.prepared);
+    aggregatedAdd64(&a.st->warmComparisons, t.comparisons);
+    aggregatedAdd64(&a.st->warmMatches, t.matches);
+}
+
+// Prepares one item.  The bodies' data are requested first (indices clamped to
+// a live entry); the cache range is searched while they are on their way, and
+// the range's first four entries are requested before the body data are used,
+// so an item costs two dependent memory round trips after its manifold data.
 // cacheKeys: the old cache's keys (a shared-memory copy when they fit; the
-// global array otherwise).
+// global array otherwise), cacheN of them.
+__device__ __forceinline__ void prepareItem(const SolveArgs &a, const PrepItem &t,
+                                            const unsigned long long *cacheKeys, uint32_t cacheN, PrepTally &tally) {
+    const uint32_t mcap = a.mcap;
+    const WorldView &w = a.w;
+    const uint32_t m = t.m, p = t.p, k = m;  // k: data index
+    const uint32_t live = t.npts < 4u ? t.npts : 4u;  // live points (at most four)
+    if (p > 0 && p >= live) return;
+    const uint32_t ia = t.ia, ib = t.ib;
+    const uint32_t ca = ia < w.nb ? ia : 0u, cb = ib < w.nb ? ib : 0u;
+    const uint32_t flA = w.bflags[ca], flB = w.bflags[cb], bgA = w.bgen[ca], bgB = w.bgen[cb];
+    const float imA = w.mat[ca].x, imB = w.mat[cb].x;
+    const float4 iA = w.iinv[ca], iB = w.iinv[cb];
+    const float4 qA4 = w.cur.rot[ca], qB4 = w.cur.rot[cb];
+    const float4 lA4 = w.nxt.lin[ca], aA4 = w.nxt.ang[ca], lB4 = w.nxt.lin[cb], aB4 = w.nxt.ang[cb];
+
+    // Cache range for (bodyA, bodyB); generations must match.
+    const unsigned long long key = ((unsigned long long)ia << 32) | ib;
+    const unsigned long long gens = ((unsigned long long)t.gA << 32) | t.gB;
+    uint32_t lo = 0, hi = cacheN;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (cacheKeys[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    uint32_t rb = lo, re = lo;
+    while (re < cacheN && cacheKeys[re] == key) ++re;
+    float4 preA[4], preB[4];
+    float preT[4];
+    unsigned long long gen0 = 0;
+    if (rb < re) gen0 = a.oldCache.gens[rb];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (rb + j < re) {
+            preA[j] = a.oldCache.anchorA[rb + j];
+            preB[j] = a.oldCache.anchorB[rb + j];
+            preT[j] = a.oldCache.tangent2[rb + j];
+        }
+
+    const float4 nf = t.nf;
+    const V3 n{nf.x, nf.y, nf.z};
+    // A manifold whose body handles are stale is not solved and not cached
+    // (sequential_impulse_solver.cpp:317-320).
+    const bool valid = ia < w.nb && ib < w.nb && (flA & kBodyAlive) && (flB & kBodyAlive) && bgA == t.gA &&
+                       bgB == t.gB && solvedPair(w, flA, flB);
+    const bool sA = (flA & kBodyStatic) != 0, sB = (flB & kBodyStatic) != 0;
+    const Q qA = f4q(qA4), qB = f4q(qB4);
+    const M3 IA = inverseInertiaWorld(qA, iA.x, iA.y, iA.z);
+    const M3 IB = inverseInertiaWorld(qB, iB.x, iB.y, iB.z);
+    if (p == 0) {
+        a.sb.pbody[k] = make_uint2(valid ? ia : 0u, valid ? ib : 0u);
+        a.sb.pn[k] = nf;
+        if (!valid) {
+            a.sb.pcount[k] = 0;
+            a.sb.pm[k] = make_float4(0.0f, 1.0f, 0.0f, 1.0f);
+            return;  // no live points: nothing is solved or written back
+        }
+        ++tally.solved;
+        a.sb.pcount[k] = live;
+        a.sb.pm[k] = make_float4(imA, sA ? 1.0f : 0.0f, imB, sB ? 1.0f : 0.0f);
+        a.sb.pmInertia[0 * mcap + k] = make_float4(IA.m00, IA.m01, IA.m02, 0.0f);
+        a.sb.pmInertia[1 * mcap + k] = make_float4(IA.m10, IA.m11, IA.m12, 0.0f);
+        a.sb.pmInertia[2 * mcap + k] = make_float4(IA.m20, IA.m21, IA.m22, 0.0f);
+        a.sb.pmInertia[3 * mcap + k] = make_float4(IB.m00, IB.m01, IB.m02, 0.0f);
+        a.sb.pmInertia[4 * mcap + k] = make_float4(IB.m10, IB.m11, IB.m12, 0.0f);
+        a.sb.pmInertia[5 * mcap + k] = make_float4(IB.m20, IB.m21, IB.m22, 0.0f);
+        if (live == 0) return;
+    } else if (!valid) {
+        return;
+    }
+    if (rb < re && gen0 != gens) re = rb;
+    const V3 linA = f4xyz(lA4), angA = f4xyz(aA4);
+    const V3 linB = f4xyz(lB4), angB = f4xyz(aB4);
+
+    float4 out[kPreparedVec4];
+    for (int v = 0; v < kPreparedVec4; ++v) out[v] = make_float4(0, 0, 0, 0);
+    float4 imp = t.imp;
+    imp.w = 0.0f;
+    const V3 anchorA{t.aa.x, t.aa.y, t.aa.z}, anchorB{t.ab.x, t.ab.y, t.ab.z};
+    const float penetration = t.aa.w;
+    V3 offA = rotate(qA, anchorA), offB = rotate(qB, anchorB);
+    out[0] = make4(offA, 0.0f);
+    out[1] = make4(offB, 0.0f);
+    V3 tref = fabsf(n.x) < 0.9f ? V3{1.0f, 0.0f, 0.0f} : V3{0.0f, 1.0f, 0.0f};
+    V3 t1 = cross(n, tref);
+    float tl = sqrtf(dot(t1, t1));
+    if (tl > 1e-6f) {
+        t1 = t1 / tl;
+        V3 t2 = cross(n, t1);
+        V3 vA = linA + cross(angA, offA), vB = linB + cross(angB, offB);
+        float vin = dot(vB - vA, n);
+        V3 jA = cross(offA, n), jB = cross(offB, n);
+        V3 nrA = mul(IA, jA), nrB = mul(IB, jB);
+        float ims = imA + imB;
+        float iem = ims + dot(jA, nrA) + dot(jB, nrB);
+        V3 tjA = cross(offA, t1), tjB = cross(offB, t1);
+        V3 trA1 = mul(IA, tjA), trB1 = mul(IB, tjB);
+        float tm00 = ims + dot(tjA, trA1) + dot(tjB, trB1);
+        float ntr1 = ims * dot(n, t1) + dot(tjA, nrA) + dot(tjB, nrB);
+        tjA = cross(offA, t2);
+        tjB = cross(offB, t2);
+        V3 trA2 = mul(IA, tjA), trB2 = mul(IB, tjB);
+        float tm11 = ims + dot(tjA, trA2) + dot(tjB, trB2);
+        float ntr2 = ims * dot(n, t2) + dot(tjA, nrA) + dot(tjB, nrB);
+        float tm01 = dot(tjA, trA1) + dot(tjB, trB1);
+        float det = tm00 * tm11 - tm01 * tm01;
+        float itm00 = 0.0f, itm01 = 0.0f, itm11 = 0.0f;
+        if (det > 0.0f) {
+            float inv = 1.0f / det;
+            itm00 = tm11 * inv;
+            itm01 = -tm01 * inv;
+            itm11 = tm00 * inv;
+        }
+        float bias = 0.0f, rv = 0.0f;
+        if (!(iem <= 0.0f)) {
+            ++tally.prepared;
+            bias = smax(penetration - 0.005f, 0.0f) * (0.2f * (1.0f / smax(w.dt, 1e-6f)));
+            rv = vin < -1.0f ? t.rest * vin : 0.0f;
+        }
+        out[0].w = iem;
+        out[1].w = bias;
+        out[2] = make4(t1, rv);
+        out[3] = make4(t2, itm00);
+        out[4] = make4(nrA, itm01);
+        out[5] = make4(nrB, itm11);
+        out[6] = make4(trA1, ntr1);
+        out[7] = make4(trB1, ntr2);
+        out[8] = make4(trA2, 0.0f);
+        out[9] = make4(trB2, 0.0f);
+        if (!(iem <= 0.0f)) {
+            // first entry within 0.05 of both anchors (the range in cache order)
+            const float matchSq = 0.05f * 0.05f;
+            bool found = false;
+            auto tryEntry = [&](const float4 &ca, const float4 &cb, float t2c) {
+                ++tally.comparisons;
+                V3 da = V3{ca.x, ca.y, ca.z} - anchorA, db = V3{cb.x, cb.y, cb.z} - anchorB;
+                if (dot(da, da) > matchSq || dot(db, db) > matchSq) return;
+                float ni = smax(ca.w, 0.0f);
+                float limit = smax(nf.w, 0.0f) * ni;
+                float tlsq = cb.w * cb.w + t2c * t2c;
+                float scale = tlsq > limit * limit ? limit / sqrtf(tlsq) : 1.0f;
+                imp = make_float4(ni, cb.w * scale, t2c * scale, 1.0f);
+                ++tally.matches;
+                found = true;
+            };
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (!found && rb + j < re) tryEntry(preA[j], preB[j], preT[j]);
+            for (uint32_t c = rb + 4; !found && c < re; ++c)
+                tryEntry(a.oldCache.anchorA[c], a.oldCache.anchorB[c], a.oldCache.tangent2[c]);
+        }
+    }
+    for (int v = 0; v < kPreparedVec4; ++v) a.sb.pp[(size_t)(v * 4 + p) * mcap + k] = out[v];
+    a.sb.pimp[(size_t)p * mcap + k] = imp;
+}
+
 __device__ inline void prepareRange(const SolveArgs &a, uint32_t begin, uint32_t stride, uint32_t M,
                                     const unsigned long long *cacheKeys = nullptr) {
     if (!cacheKeys) cacheKeys = a.oldCache.key;
-    const uint32_t mcap = a.mcap;
-    const WorldView &w = a.w;
-    const float inverseDt = 1.0f / smax(w.dt, 1e-6f);
     const uint32_t cacheN = *a.oldCount;
-    const float matchSq = 0.05f * 0.05f;
-    uint64_t prepared = 0, comparisons = 0, matches = 0;
-    uint32_t solved = 0;
-    // Work items are (manifold, point) pairs q = p M + m (all point-0 items
-    // first, so consecutive threads take consecutive manifolds): a manifold's
-    // points are independent here, so the slowest point, not the sum of a
-    // manifold's points, bounds the pass.  Each item reads its manifold's data;
-    // point 0's item also writes the per-manifold outputs.  Everything indexed
-    // by m and the bodies' data (indices clamped to a live entry) are requested
-    // at once: an item costs three dependent memory round trips (manifold,
-    // bodies, warm-start cache).
-    for (uint32_t q = begin; q < 4 * M; q += stride) {
-        const uint32_t p = q / M, m = q - p * M;
-        const uint32_t k = m;  // data index
-        const uint32_t npts = min(a.mv.pointCount[m], 4u);
-        const uint32_t live = npts < 4u ? npts : 4u;  // live points (at most four)
-        if (p > 0 && p >= live) continue;
-        const uint32_t ia = a.mv.bodyA[m], ib = a.mv.bodyB[m];
-        const uint32_t gA = a.mv.genA[m], gB = a.mv.genB[m];
-        const float4 nf = a.mv.normalFriction[m];
-        const float rest = a.mv.restitution[m];
-        const float4 aa = a.mv.anchorA[4 * m + p], ab = a.mv.anchorB[4 * m + p];
-        float4 imp = a.mv.impulse[4 * m + p];
-        const uint32_t ca = ia < w.nb ? ia : 0u, cb = ib < w.nb ? ib : 0u;
-        const uint32_t flA = w.bflags[ca], flB = w.bflags[cb], bgA = w.bgen[ca], bgB = w.bgen[cb];
-        const float imA = w.mat[ca].x, imB = w.mat[cb].x;
-        const float4 iA = w.iinv[ca], iB = w.iinv[cb];
-        const float4 qA4 = w.cur.rot[ca], qB4 = w.cur.rot[cb];
-        const float4 lA4 = w.nxt.lin[ca], aA4 = w.nxt.ang[ca], lB4 = w.nxt.lin[cb], aB4 = w.nxt.ang[cb];
-        const V3 n{nf.x, nf.y, nf.z};
-        // A manifold whose body handles are stale is not solved and not cached
-        // (sequential_impulse_solver.cpp:317-320).
-        const bool valid = ia < w.nb && ib < w.nb && (flA & kBodyAlive) && (flB & kBodyAlive) && bgA == gA &&
-                           bgB == gB && solvedPair(w, flA, flB);
-        const bool sA = (flA & kBodyStatic) != 0, sB = (flB & kBodyStatic) != 0;
-        const Q qA = f4q(qA4), qB = f4q(qB4);
-        const M3 IA = inverseInertiaWorld(qA, iA.x, iA.y, iA.z);
-        const M3 IB = inverseInertiaWorld(qB, iB.x, iB.y, iB.z);
-        if (p == 0) {
-            a.sb.pbody[k] = make_uint2(valid ? ia : 0u, valid ? ib : 0u);
-            a.sb.pn[k] = nf;
-            if (!valid) {
-                a.sb.pcount[k] = 0;
-                a.sb.pm[k] = make_float4(0.0f, 1.0f, 0.0f, 1.0f);
-                continue;  // no live points: nothing is solved or written back
-            }
-            ++solved;
-            a.sb.pcount[k] = live;
-            a.sb.pm[k] = make_float4(imA, sA ? 1.0f : 0.0f, imB, sB ? 1.0f : 0.0f);
-            a.sb.pmInertia[0 * mcap + k] = make_float4(IA.m00, IA.m01, IA.m02, 0.0f);
-            a.sb.pmInertia[1 * mcap + k] = make_float4(IA.m10, IA.m11, IA.m12, 0.0f);
-            a.sb.pmInertia[2 * mcap + k] = make_float4(IA.m20, IA.m21, IA.m22, 0.0f);
-            a.sb.pmInertia[3 * mcap + k] = make_float4(IB.m00, IB.m01, IB.m02, 0.0f);
-            a.sb.pmInertia[4 * mcap + k] = make_float4(IB.m10, IB.m11, IB.m12, 0.0f);
-            a.sb.pmInertia[5 * mcap + k] = make_float4(IB.m20, IB.m21, IB.m22, 0.0f);
-            if (live == 0) continue;
-        } else if (!valid) {
-            continue;
-        }
-        const V3 linA = f4xyz(lA4), angA = f4xyz(aA4);
-        const V3 linB = f4xyz(lB4), angB = f4xyz(aB4);
-
-        // Cache range for (bodyA, bodyB); generations must match.
-        const unsigned long long key = ((unsigned long long)ia << 32) | ib;
-        const unsigned long long gens = ((unsigned long long)gA << 32) | gB;
-        uint32_t lo = 0, hi = cacheN;
-        while (lo < hi) {
-            uint32_t mid = (lo + hi) >> 1;
-            if (cacheKeys[mid] < key) lo = mid + 1;
-            else hi = mid;
-        }
-        uint32_t rb = lo, re = lo;
-        while (re < cacheN && cacheKeys[re] == key) ++re;
-        if (rb < re && a.oldCache.gens[rb] != gens) re = rb;
-
-        float4 out[kPreparedVec4];
-        for (int v = 0; v < kPreparedVec4; ++v) out[v] = make_float4(0, 0, 0, 0);
-        imp.w = 0.0f;
-        const V3 anchorA{aa.x, aa.y, aa.z}, anchorB{ab.x, ab.y, ab.z};
-        const float penetration = aa.w;
-        V3 offA = rotate(qA, anchorA), offB = rotate(qB, anchorB);
-        out[0] = make4(offA, 0.0f);
-        out[1] = make4(offB, 0.0f);
-        V3 tref = fabsf(n.x) < 0.9f ? V3{1.0f, 0.0f, 0.0f} : V3{0.0f, 1.0f, 0.0f};
-        V3 t1 = cross(n, tref);
-        float tl = sqrtf(dot(t1, t1));
-        if (tl > 1e-6f) {
-            t1 = t1 / tl;
-            V3 t2 = cross(n, t1);
-            V3 vA = linA + cross(angA, offA), vB = linB + cross(angB, offB);
-            float vin = dot(vB - vA, n);
-            V3 jA = cross(offA, n), jB = cross(offB, n);
-            V3 nrA = mul(IA, jA), nrB = mul(IB, jB);
-            float ims = imA + imB;
-            float iem = ims + dot(jA, nrA) + dot(jB, nrB);
-            V3 tjA = cross(offA, t1), tjB = cross(offB, t1);
-            V3 trA1 = mul(IA, tjA), trB1 = mul(IB, tjB);
-            float tm00 = ims + dot(tjA, trA1) + dot(tjB, trB1);
-            float ntr1 = ims * dot(n, t1) + dot(tjA, nrA) + dot(tjB, nrB);
-            tjA = cross(offA, t2);
-            tjB = cross(offB, t2);
-            V3 trA2 = mul(IA, tjA), trB2 = mul(IB, tjB);
-            float tm11 = ims + dot(tjA, trA2) + dot(tjB, trB2);
-            float ntr2 = ims * dot(n, t2) + dot(tjA, nrA) + dot(tjB, nrB);
-            float tm01 = dot(tjA, trA1) + dot(tjB, trB1);
-            float det = tm00 * tm11 - tm01 * tm01;
-            float itm00 = 0.0f, itm01 = 0.0f, itm11 = 0.0f;
-            if (det > 0.0f) {
-                float inv = 1.0f / det;
-                itm00 = tm11 * inv;
-                itm01 = -tm01 * inv;
-                itm11 = tm00 * inv;
-            }
-            float bias = 0.0f, rv = 0.0f;
-            if (!(iem <= 0.0f)) {
-                ++prepared;
-                bias = smax(penetration - 0.005f, 0.0f) * (0.2f * inverseDt);
-                rv = vin < -1.0f ? rest * vin : 0.0f;
-            }
-            out[0].w = iem;
-            out[1].w = bias;
-            out[2] = make4(t1, rv);
-            out[3] = make4(t2, itm00);
-            out[4] = make4(nrA, itm01);
-            out[5] = make4(nrB, itm11);
-            out[6] = make4(trA1, ntr1);
-            out[7] = make4(trB1, ntr2);
-            out[8] = make4(trA2, 0.0f);
-            out[9] = make4(trB2, 0.0f);
-            if (!(iem <= 0.0f)) {
-                for (uint32_t c = rb; c < re; ++c) {
-                    ++comparisons;
-                    const float4 ca = a.oldCache.anchorA[c], cb = a.oldCache.anchorB[c];
-                    V3 da = V3{ca.x, ca.y, ca.z} - anchorA, db = V3{cb.x, cb.y, cb.z} - anchorB;
-                    if (dot(da, da) > matchSq || dot(db, db) > matchSq) continue;
-                    const float t2c = a.oldCache.tangent2[c];
-                    float ni = smax(ca.w, 0.0f);
-                    float limit = smax(nf.w, 0.0f) * ni;
-                    float tlsq = cb.w * cb.w + t2c * t2c;
-                    float scale = tlsq > limit * limit ? limit / sqrtf(tlsq) : 1.0f;
-                    imp = make_float4(ni, cb.w * scale, t2c * scale, 1.0f);
-                    ++matches;
-                    break;
-                }
-            }
-        }
-        for (int v = 0; v < kPreparedVec4; ++v) a.sb.pp[(size_t)(v * 4 + p) * mcap + k] = out[v];
-        a.sb.pimp[(size_t)p * mcap + k] = imp;
-    }
-    aggregatedAdd32(&a.st->solved, solved);
-    aggregatedAdd64(&a.st->preparedPoints, prepared);
-    aggregatedAdd64(&a.st->warmComparisons, comparisons);
-    aggregatedAdd64(&a.st->warmMatches, matches);
+    PrepTally tally;
+    for (uint32_t q = begin; q < 4 * M; q += stride) prepareItem(a, loadPrepItem(a, q, M), cacheKeys, cacheN, tally);
+    flushPrepTally(a, tally);
 }
 
 
@@ -559,15 +611,17 @@ __device__ __forceinline__ bool manifoldBodiesValid(const SolveArgs &a, uint32_t
 // generation and dynamic (the colouring's "dynamic side"); bit 2 both handles
 // live (the manifold is solved).
 constexpr uint32_t kFlagDynA = 1u, kFlagDynB = 2u, kFlagValid = 4u;
-__device__ __forceinline__ uint32_t manifoldFlags(const SolveArgs &a, uint32_t m) {
-    const uint32_t ba = a.mv.bodyA[m], bb = a.mv.bodyB[m];
-    const WorldView &w = a.w;
-    const bool okA = ba < w.nb && (w.bflags[ba] & kBodyAlive) && w.bgen[ba] == a.mv.genA[m];
-    const bool okB = bb < w.nb && (w.bflags[bb] & kBodyAlive) && w.bgen[bb] == a.mv.genB[m];
+__device__ __forceinline__ uint32_t manifoldFlagsOf(const WorldView &w, uint32_t ba, uint32_t bb, uint32_t genA,
+                                                    uint32_t genB) {
+    const bool okA = ba < w.nb && (w.bflags[ba] & kBodyAlive) && w.bgen[ba] == genA;
+    const bool okB = bb < w.nb && (w.bflags[bb] & kBodyAlive) && w.bgen[bb] == genB;
     const bool dA = okA && !(w.bflags[ba] & (kBodyStatic | kBodySleeping));
     const bool dB = okB && !(w.bflags[bb] & (kBodyStatic | kBodySleeping));
     return (dA ? kFlagDynA : 0u) | (dB ? kFlagDynB : 0u) |
            (okA && okB && (!w.sleepMode || dA || dB) ? kFlagValid : 0u);
+}
+__device__ __forceinline__ uint32_t manifoldFlags(const SolveArgs &a, uint32_t m) {
+    return manifoldFlagsOf(a.w, a.mv.bodyA[m], a.mv.bodyB[m], a.mv.genA[m], a.mv.genB[m]);
 }
 
 // Front of the single-block solver: staging slots, colouring and the solve

@@ -115,6 +115,14 @@ struct SolverBuffers {
     unsigned long long *islSort;    // [2 * mcap] sort scratch of large islands
     uint32_t *islCounters;          // [kIslCounterWords] islands, lone manifolds, work queue, listed manifolds,
                                     // queue fills; large islands' manifolds per colour and fill cursors
+    // island path of the cluster solver: union-find links stored as parent XOR
+    // body (0 at a root, so the zero-filled array is every body on its own) and
+    // the manifolds listed at each root; the solver returns both to zero before
+    // it ends.  islandRec: kIslandMax records per root body, one per manifold
+    // {manifold | flags << 13 | points << 16, body A, body B, spare}.
+    uint32_t *islLink;              // [nb]
+    uint32_t *islSize;              // [nb]
+    uint4 *islandRec;               // [kIslandMax * nb]
 };
 
 constexpr int kMaxColors = 128;
@@ -215,6 +223,8 @@ struct ClusterSolveLayout {
     uint32_t localCap, pointCap;   // manifolds / prepared points held per rank
     uint32_t islandBodies;         // island path: body slots per rank
     uint32_t offVel, offPm, offPn, offSlot, offM, offCnt, offOff, offPt;
+    uint32_t offCacheOff;          // island path: warm-start cache offset of every manifold [blockM]
+    uint32_t offPtL;               // island path: local manifold of every staged point [pointCap]
     uint32_t smemBytes;
 };
 constexpr uint32_t kBlockMaxBodies = 1u << 20;

@@ -594,6 +594,9 @@ void World::ensureCapacity() {
     sIslKeys_.reserve(m);
     sIslKeysTmp_.reserve(m);
     sIslSort_.reserve(2 * (size_t)m);
+    sIslLink_.reserve(nb);
+    sIslSize_.reserve(nb);
+    sIslandRec_.reserve((size_t)kIslandMax * nb);
     sb_ = SolverBuffers{m,
                         sBest_.ptr,
                         sUsed_.ptr,
@@ -634,7 +637,10 @@ void World::ensureCapacity() {
                         sIslKeys_.ptr,
                         sIslKeysTmp_.ptr,
                         sIslSort_.ptr,
-                        sIslCounters_.ptr};
+                        sIslCounters_.ptr,
+                        sIslLink_.ptr,
+                        sIslSize_.ptr,
+                        sIslandRec_.ptr};
 
     // Warm-start caches keep their contents when they grow.
     const uint32_t needCache = std::max(4 * m, cacheNeed_);
@@ -894,9 +900,18 @@ bool World::finishStep() {
     solveSkipped_ = sleepingEnabled && h.solveCount == 0;
     c.colors = orderMode == 0 ? h.manifolds : solveSkipped_ ? (h.manifolds ? 1u : 0u) : h.colors;
     c.colorRounds = h.colorRounds;
-    for (int k = 0; k < 7; ++k) {
-        const unsigned long long t0 = h.solverStamp[k], t1 = h.solverStamp[k + 1];
-        c.solverPhaseMs[k] = (h.solverStamp[0] && t0 && t1 > t0) ? (t1 - t0) * 1e-6 : 0.0;
+    // gap after the narrowphase, prepare kernel, gap, cluster kernel phases,
+    // gap before the pose kernel (zeros when the one-cluster solver did not run)
+    {
+        const unsigned long long *t = h.solverStamp;
+        auto span = [&](unsigned long long t0, unsigned long long t1) {
+            return (t[0] && t0 && t1 > t0) ? (t1 - t0) * 1e-6 : 0.0;
+        };
+        const unsigned long long last = t[7] ? t[7] : t[5];
+        c.solverPhaseMs[0] = span(h.stamp[3], t[0]);
+        for (int k = 0; k < 5; ++k) c.solverPhaseMs[k + 1] = span(t[k], t[k + 1]);
+        c.solverPhaseMs[6] = span(t[5], t[7]);
+        c.solverPhaseMs[7] = span(last, h.stamp[4]);
     }
     c.epaFailures = h.epaFailures;
     c.points = h.points;

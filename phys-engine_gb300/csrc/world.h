@@ -98,7 +98,7 @@ struct StepCounters {
     // device time of the one-cluster solver's phases (ms; zero when it did not
     // run): prepare, island union, island lists, plan + staging (or colouring),
     // sweeps, write-back, cache rebuild
-    double solverPhaseMs[7] = {0, 0, 0, 0, 0, 0, 0};
+    double solverPhaseMs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 // Copies M manifolds of a device manifold view into pe_contact_manifold records.
@@ -286,6 +286,8 @@ class World {
     DeviceArray<uint32_t> sColor_, sDyn_, sColorCount_, sColorStart_, sOrderKeys_, sOrderKeysTmp_, sOrder_, sOrderTmp_, sPcount_,
         sCacheVals_, sCacheValsTmp_, sCacheCounts_, sCacheOff_, sBar_, sCounters_, sStageBody_, sIslandList_;
     DeviceArray<uint32_t> sIslPar_, sIslOff_, sIslRoot_, sIslSlot_, sIslList_, sIslRoots_, sIslLone_, sIslCounters_;
+    DeviceArray<uint32_t> sIslLink_, sIslSize_;
+    DeviceArray<uint4> sIslandRec_;
     DeviceArray<unsigned long long> sIslKeys_, sIslKeysTmp_, sIslSort_;
     DeviceArray<float4> sPm_, sPmI_, sPp_, sPimp_, sPn_;
     DeviceArray<uint2> sPbody_, sStageSlot_;

@@ -416,8 +416,11 @@ class GpuWorld:
 
     def solver_phases(self):
         """Device ms of the one-cluster solver's phases in the last step:
-        prepare, union, lists, plan + staging, sweeps, write-back, cache."""
-        ms = np.zeros(7, np.float64)
+        gap after the narrowphase, prepare kernel (prepare + flags + unions),
+        gap, island lists, plan + staging, sweeps (island path: with the
+        results and the cache), write-back + cache (colour-phase path), gap to
+        the pose kernel."""
+        ms = np.zeros(8, np.float64)
         check(self.lib.pe_world_get_solver_phases(self.h, _ptr(ms)))
         return ms
 
