@@ -249,6 +249,23 @@ __device__ __forceinline__ uint2 planSlots(uint32_t meta) { return make_uint2((m
 // priority hash is a bijection of the manifold index).
 __device__ void planIsland(const SolveArgs &a, const uint4 *rec, uint32_t n, IslandPlan &P) {
     const SolverBuffers &sb = a.sb;
+    if (n == 1) {
+        // one manifold: colour 0, one round, bodies A and B
+        const uint4 r0 = __ldcg(&rec[0]);
+        const uint32_t m = r0.x & kRecManifoldMask, fl = (r0.x >> 13) & 7u, pts = (r0.x >> 16) & 7u;
+        P.n = 1;
+        P.nbody = 2;
+        P.body[0] = r0.y;
+        P.body[1] = r0.z;
+        P.dynMask = ((fl & kFlagDynA) ? 1u : 0u) | ((fl & kFlagDynB) ? 2u : 0u);
+        P.ks[0] = m;
+        P.meta[0] = pts << 8 | 1u << 24;
+        P.points = pts;
+        P.colors = 1;
+        sb.color[m] = 0;
+        atomicMax(&a.st->colors, 1u);
+        return;
+    }
     uint4 r[kIslandMax];
 #pragma unroll
     for (uint32_t j = 0; j < kIslandMax; ++j)
@@ -613,7 +630,7 @@ constexpr uint32_t kIslPrepKeyCap = 2048;  // old cache keys copied to shared me
 
 __global__ void __launch_bounds__(kIslPrepThreads) k_prepare_islands(SolveArgs a, uint32_t blockM,
                                                                      uint32_t itemBlocks) {
-    __shared__ unsigned long long s_keys[kIslPrepKeyCap];
+    __shared__ __align__(16) unsigned long long s_keys[kIslPrepKeyCap];
     const uint32_t tid = threadIdx.x;
     if (blockIdx.x == 0 && tid == 0) a.st->solverStamp[0] = globalNs();
     if (blockIdx.x >= itemBlocks) {
@@ -640,8 +657,27 @@ __global__ void __launch_bounds__(kIslPrepThreads) k_prepare_islands(SolveArgs a
         const uint32_t M = min(*a.count, a.mcap), cacheN = *a.oldCount;
         const bool work = M <= blockM && blockIdx.x < 4 * M;  // some item of this block is live
         const bool inShared = cacheN <= kIslPrepKeyCap;
-        if (work && inShared)
-            for (uint32_t i = tid; i < cacheN; i += kIslPrepThreads) s_keys[i] = a.oldCache.key[i];
+        if (work && inShared) {
+            // 16-byte loads, every one of a thread's requested before any store
+            constexpr uint32_t kPer = kIslPrepKeyCap / 2 / kIslPrepThreads;
+            const ulonglong2 *src = reinterpret_cast<const ulonglong2 *>(a.oldCache.key);
+            ulonglong2 *dst = reinterpret_cast<ulonglong2 *>(s_keys);
+            const uint32_t pairs = cacheN / 2;
+            ulonglong2 v[kPer];
+#pragma unroll
+            for (uint32_t j = 0; j < kPer; ++j) {
+                const uint32_t i = tid + j * kIslPrepThreads;
+                if (i < pairs) v[j] = __ldcg(&src[i]);
+            }
+            unsigned long long last = 0;
+            if (tid == 0 && (cacheN & 1u)) last = __ldcg(&a.oldCache.key[cacheN - 1]);
+#pragma unroll
+            for (uint32_t j = 0; j < kPer; ++j) {
+                const uint32_t i = tid + j * kIslPrepThreads;
+                if (i < pairs) dst[i] = v[j];
+            }
+            if (tid == 0 && (cacheN & 1u)) s_keys[cacheN - 1] = last;
+        }
         __syncthreads();
         if (work && m < M) {
             PrepTally tally;
