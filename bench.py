@@ -297,12 +297,13 @@ def run_gpu(args, rank, world_size, local_rank):
         return
     peak, peak_kind = measured_peaks()
     stage_ms = {k[:-3]: v for k, v in acc.items()}
-    # The top kernel of the step is the contact solver on one thread-block
-    # cluster (one launch per step whenever the manifold count fits the block
-    # capacity); the solver stage's events then time exactly that kernel.
+    # The top stage of the step is the contact solver: the prepare kernel over
+    # the whole GPU and the solver on one thread-block cluster (two launches per
+    # step whenever the manifold count fits the cluster's capacity); the solver
+    # stage's stamps time exactly those two kernels.
     block_solver = totals["manifolds"] / args.steps < 3000
     dominant = "solver" if block_solver else max(stage_ms, key=stage_ms.get)
-    kernel = "k_solve_cluster" if block_solver else f"{dominant} stage"
+    kernel = "k_prepare_islands + k_solve_cluster" if block_solver else f"{dominant} stage"
     achieved = stage_b[dominant] / (stage_ms[dominant] / 1000.0) / 1e9 if stage_ms[dominant] > 0 else 0.0
     step_bytes = sum(stage_b.values())
     traffic = profiled_traffic(kernel, stage_b[dominant] / args.steps)
