@@ -147,6 +147,118 @@ __global__ void k_sap_emit(const uint32_t *d_n, const uint32_t *off, const uint3
     }
 }
 
+// ------------------------------------------------------ SAP, one block ------
+// The whole sweep of a small world in one thread block: (min.x key, index)
+// bitonic-sorted in shared memory, each sorted entry's window by binary search,
+// the windows flattened by a block scan and dealt out in equal chunks (a floor
+// box's window holds every body: one thread per entry would walk it alone).
+// The sorted order, the windows, the window and pair counters and the pair keys
+// are those of the multi-kernel sweep above (one launch instead of a dozen; at
+// a thousand boxes the launches, not the work, set the sweep's time).
+constexpr uint32_t kSapBlockMax = 4096;
+constexpr int kSapBlockThreads = 1024;
+constexpr size_t kSapBlockSmem = (size_t)kSapBlockMax * (8 + 16 + 4 + 4 + 4 + 4);
+
+__global__ void __launch_bounds__(kSapBlockThreads)
+k_sap_block(BroadInput in, uint32_t *sapKeys, uint32_t *sapVals, uint32_t *unsorted, unsigned long long *keys,
+            uint32_t cap, uint32_t bits, DevStats *st) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned long long *sk = reinterpret_cast<unsigned long long *>(smem);  // key << 32 | index
+    float4 *sYZ = reinterpret_cast<float4 *>(smem + (size_t)kSapBlockMax * 8);
+    float *sMinX = reinterpret_cast<float *>(smem + (size_t)kSapBlockMax * 24);
+    float *sMaxX = sMinX + kSapBlockMax;
+    uint32_t *sIdx = reinterpret_cast<uint32_t *>(sMaxX + kSapBlockMax);
+    uint32_t *sOff = sIdx + kSapBlockMax;  // window lengths, then their exclusive scan
+    __shared__ uint32_t s_count, s_scan[40];
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t n = min(*in.d_n, kSapBlockMax);  // the host launches this for at most kSapBlockMax boxes
+    uint32_t N = 1;
+    while (N < n) N <<= 1;
+    for (uint32_t i = tid; i < N; i += nt)
+        sk[i] = i < n ? ((unsigned long long)orderedFloatKey(in.mn[i].x) << 32 | i) : ~0ull;
+    if (tid == 0) {
+        s_count = 0;
+        if (unsorted) *unsorted = 0u;  // as after the multi-kernel sweep
+    }
+    __syncthreads();
+    for (uint32_t k = 2; k <= N; k <<= 1)
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = tid; i < N; i += nt) {
+                const uint32_t l = i ^ j;
+                if (l > i) {
+                    const unsigned long long a = sk[i], b = sk[l];
+                    if ((a > b) == ((i & k) == 0)) {
+                        sk[i] = b;
+                        sk[l] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (uint32_t i = tid; i < n; i += nt) {
+        const uint32_t idx = (uint32_t)sk[i];
+        const float4 mn = in.mn[idx], mx = in.mx[idx];
+        sMinX[i] = mn.x;
+        sMaxX[i] = mx.x;
+        sYZ[i] = make_float4(mn.y, mx.y, mn.z, mx.z);
+        sIdx[i] = idx;
+        sapKeys[i] = (uint32_t)(sk[i] >> 32);
+        sapVals[i] = idx;
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < n; i += nt) {
+        // window: entries i+1 .. lo-1 with min.x <= max.x(i) (k_sap_window)
+        const float x = sMaxX[i];
+        uint32_t lo = i + 1, hi = n;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (sMinX[mid] > x) hi = mid;
+            else lo = mid + 1;
+        }
+        sOff[i] = lo - i - 1;
+    }
+    __syncthreads();
+    const uint32_t W = blockExclusiveScanArray(sOff, n, s_scan);  // ends with a barrier
+    // thread t: flattened items [t C, (t + 1) C) of the windows, in order
+    const uint32_t C = (W + nt - 1) / nt;
+    const uint32_t w0 = tid * C, wEnd = min(W, w0 + C);
+    if (w0 < wEnd) {
+        uint32_t lo = 0, hi = n;  // i = last entry with off[i] <= w0
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (sOff[mid] > w0) hi = mid;
+            else lo = mid + 1;
+        }
+        uint32_t i = lo - 1;
+        uint32_t j = i + 1 + (w0 - sOff[i]);
+        uint32_t end = i + 1 + ((i + 1 < n ? sOff[i + 1] : W) - sOff[i]);  // i has a non-empty window
+        float4 f = sYZ[i];
+        uint32_t fi = sIdx[i];
+        for (uint32_t w = w0; w < wEnd; ++w) {
+            if (overlapYZ(f, sYZ[j])) {
+                const uint32_t a = fi, b = sIdx[j];
+                const uint32_t slot = atomicAdd(&s_count, 1u);
+                if (slot < cap) keys[slot] = ((unsigned long long)(a < b ? a : b) << bits) | (a < b ? b : a);
+            }
+            if (++j == end && w + 1 < wEnd) {
+                do {
+                    ++i;
+                } while (i + 1 < n && (sOff[i + 1] - sOff[i]) == 0);
+                j = i + 1;
+                end = i + 1 + ((i + 1 < n ? sOff[i + 1] : W) - sOff[i]);
+                f = sYZ[i];
+                fi = sIdx[i];
+            }
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        atomicAdd(&st->xWindow, (unsigned long long)W);
+        st->windowWork = W;
+        atomicAdd(&st->rawPairs, s_count);
+    }
+}
+
 // --------------------------------------------------------------- grid ------
 // Widths for the median cell size (broadphase.cpp:94-110).
 __global__ void k_grid_widths(BroadInput in, unsigned long long *keys, uint32_t *count) {
@@ -861,6 +973,18 @@ void launchSapKeys(const BroadInput &in, uint32_t *keys, uint32_t *vals, cudaStr
 void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, BroadBuffers &bb, PairBuffers &pb,
                DevStats *st, Scratch &ws, cudaStream_t s, const SapCoherence *coh) {
     uint32_t *err = &st->err;
+    if (in.maxN <= kSapBlockMax) {
+        static bool configured = false;
+        if (!configured) {
+            PE_CHECK(cudaFuncSetAttribute(k_sap_block, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)kSapBlockSmem));
+            configured = true;
+        }
+        k_sap_block<<<1, kSapBlockThreads, kSapBlockSmem, s>>>(in, sapKeys, sapVals, coh ? coh->unsorted : nullptr,
+                                                                pb.keys, pb.cap, pb.bits, st);
+        PE_LAUNCHED();
+        return;
+    }
     const uint32_t *sortN = in.d_n;
     if (coh) {
         k_sap_presort<<<gridFor(in.maxN), 256, 0, s>>>(in.d_n, coh->keyOf, sapKeys, sapVals, coh->unsorted);
