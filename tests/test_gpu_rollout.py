@@ -1,8 +1,11 @@
 """GPU tests of the differentiable rollout: the forward pass equals the batched
 engine bit for bit; the FP32 adjoint matches the FP64 CPU adjoint within 1e-3
-(relative to the larger of the entry and 1 % of the largest gradient); the
-torch.autograd.Function harness gives the gradients of a centre-of-mass loss
-that match central finite differences through the oracle's FP64 step."""
+relative (entries below a millionth of the largest gradient, true zeros, are
+held to 1e-9 of it); the torch.autograd.Function harness gives the gradients of
+a centre-of-mass loss — initial velocities, masses, frictions and, on worlds
+with impacts, restitutions — that match central finite differences through the
+oracle's FP64 step within 1e-3 relative.  (Measured: at most 2.2e-4 against the
+FP64 adjoint, at most 1e-5 against finite differences.)"""
 import numpy as np
 import pytest
 
@@ -88,7 +91,7 @@ def test_rollout_gradients_match_fp64_adjoint(gpu):
             if scale == 0:
                 assert np.abs(g).max() < 1e-5, (w, name)
                 continue
-            err = np.abs(g - r) / np.maximum(np.abs(r), 1e-2 * scale)
+            err = np.abs(g - r) / np.maximum(np.abs(r), 1e-6 * scale)
             assert err.max() <= 1e-3, (w, name, float(err.max()), g.ravel()[:6], r.ravel()[:6])
 
 
@@ -148,7 +151,80 @@ def test_rollout_autograd_com_loss_matches_oracle_fd(gpu):
     scale = max(abs(c[4]) for c in checks)
     for w, which, i, j, a in checks:
         ref = fd(w, which, i, j)
-        assert abs(a - ref) <= 1e-3 * max(abs(ref), 1e-2 * scale), (w, which, i, j, a, ref)
+        assert abs(a - ref) <= 1e-3 * max(abs(ref), 1e-6 * scale), (w, which, i, j, a, ref)
+
+
+def com_loss_and_oracle(sc, steps, roll, target):
+    """Centre-of-mass loss of every world through the autograd harness, and the
+    same loss of one world through the oracle's FP64 step with one input
+    perturbed (velocity component j of body i, or its mass / friction /
+    restitution)."""
+    import torch
+
+    fn = rollout.rollout_function()
+    x0, q0, v0, w0, m, f, r = (t.requires_grad_(True) for t in torch_state(roll))
+    xT, qT, vT, wT = fn.apply(roll, x0, q0, v0, w0, m, f, r)
+    dyn = torch.tensor(~np.concatenate([s.is_static for s in sc]).astype(bool), device="cuda:0")
+    loss = 0
+    for w in range(len(sc)):
+        s0, s1 = int(roll.starts[w]), int(roll.starts[w + 1])
+        mw = m[s0:s1] * dyn[s0:s1]
+        com = (mw[:, None] * xT[s0:s1]).sum(0) / mw.sum()
+        loss = loss + ((com - target[w]) ** 2).sum()
+    loss.backward()
+
+    def oracle_loss(w, which, i, j, eps):
+        s = sc[w]
+        ow = cpu.OracleWorld(fp64=True, algo=0, iterations=ITERS, order_mode=1)
+        ow.load_scene(s)
+        mat = np.array([ow.material(k) for k in range(s.count)])
+        if which == "v":
+            b = ow.bodies_f64()
+            v = b["lin"][i].copy()
+            v[j] += eps
+            ow.set_velocity_f64(i, v, b["ang"][i])
+        else:
+            mm, ff, rr = mat[i]
+            mm, ff, rr = mm + eps * (which == "m"), ff + eps * (which == "f"), rr + eps * (which == "r")
+            ow.set_material(i, mm, ff, rr)
+            mat[i] = (mm, ff, rr)
+        for _ in range(steps):
+            ow.step(DT)
+        x = ow.bodies_f64()["pos"]
+        mw = mat[:, 0] * (~s.is_static.astype(bool))
+        com = (mw[:, None] * x).sum(0) / mw.sum()
+        return float(((com - target[w].cpu().numpy().astype(np.float64)) ** 2).sum())
+
+    grads = {"v": v0.grad.cpu().numpy(), "m": m.grad.cpu().numpy(), "f": f.grad.cpu().numpy(),
+             "r": r.grad.cpu().numpy()}
+    return grads, oracle_loss
+
+
+def test_rollout_autograd_restitution_matches_oracle_fd(gpu):
+    """Restitution enters only through an approach faster than 1 m/s
+    (sequential_impulse_solver.cpp:101-214): boxes driven into the plane at
+    2 m/s, 8 steps, two worlds; the gradients of the centre-of-mass loss with
+    respect to every dynamic box's restitution, mass and vertical velocity
+    against central differences (eps 1e-4) through the oracle's FP64 step."""
+    import torch
+
+    sc = [sliding_boxes(6, 13, impact=True), sliding_boxes(6, 14, impact=True)]
+    steps = 8
+    roll = rollout.GpuRollout(sc, steps, DT, iterations=ITERS, checkpoint_every=4)
+    target = torch.tensor([[1.0, 0.5, -2.0], [-3.0, 0.2, 1.0]], device="cuda:0")
+    grads, oracle_loss = com_loss_and_oracle(sc, steps, roll, target)
+    checks = []
+    for w in range(2):
+        base = int(roll.starts[w])
+        for i in range(1, 7):
+            checks += [(w, "r", i, 1, grads["r"][base + i]), (w, "m", i, 1, grads["m"][base + i]),
+                       (w, "v", i, 1, grads["v"][base + i, 1])]
+    assert max(abs(c[4]) for c in checks if c[1] == "r") > 1e-3  # restitution matters here
+    scale = max(abs(c[4]) for c in checks)
+    eps = 1e-4
+    for w, which, i, j, a in checks:
+        ref = (oracle_loss(w, which, i, j, eps) - oracle_loss(w, which, i, j, -eps)) / (2 * eps)
+        assert abs(a - ref) <= 1e-3 * max(abs(ref), 1e-6 * scale), (w, which, i, a, ref)
 
 
 def test_rollout_uneven_mixed_batch_matches_batch_engine(gpu):
