@@ -108,7 +108,7 @@ typedef struct pe_step_stats {
     uint64_t color_rounds;
     uint64_t epa_failures;
     uint64_t contact_points;
-    double total_ms; /* device time of the step */
+    double total_ms; /* device time of the step: integrate kernel start to pose kernel end */
     /* device time per stage, the GPU counterpart of StepStats::integrateVelocityMs,
        broadPhaseMs, narrowPhaseMs, solverMs, integratePoseMs */
     double integrate_ms;

@@ -32,8 +32,10 @@ __device__ __forceinline__ void integrateAabbOne(const WorldView &w, uint32_t *s
             w.sleepQuietMin[i] = 0x7F800000u;  // +inf: no quiet time folded in yet
         }
         if (integrate) {
-            const V3 force = w.force3 ? (i < w.force3n ? V3{w.force3[3 * i], w.force3[3 * i + 1], w.force3[3 * i + 2]}
-                                                       : V3{0.0f, 0.0f, 0.0f})
+            const float *force3 = w.io ? w.io->force3 : w.force3;
+            const uint32_t force3n = w.io ? w.io->force3n : w.force3n;
+            const V3 force = force3 ? (i < force3n ? V3{force3[3 * i], force3[3 * i + 1], force3[3 * i + 2]}
+                                                   : V3{0.0f, 0.0f, 0.0f})
                              : w.force ? f4xyz(w.force[i]) : V3{0.0f, 0.0f, 0.0f};
             lin = integrateVelocity(lin, V3{w.gx, w.gy, w.gz}, force, w.mat[i].x, w.dt);
         }
@@ -126,11 +128,13 @@ __global__ void k_integrate_pose(WorldView w, DevStats *st, DevStats *hostOut, u
         }
         w.nxt.pos[i] = p4;
         w.nxt.rot[i] = q4;
-        if (w.pos3) {
-            w.pos3[3 * i] = p4.x;
-            w.pos3[3 * i + 1] = p4.y;
-            w.pos3[3 * i + 2] = p4.z;
+        float *pos3 = w.io ? w.io->pos3 : w.pos3;
+        if (pos3) {
+            pos3[3 * i] = p4.x;
+            pos3[3 * i + 1] = p4.y;
+            pos3[3 * i + 2] = p4.z;
         }
+        if (w.io && w.io->rot4) w.io->rot4[i] = q4;
         if (w.sleepMode && dyn) {
             // finishSleeping's first loop (physics_world.cpp:474-490): the quiet
             // time of an awake body, folded into its island's minimum.

@@ -138,9 +138,23 @@ struct DevStats {
 };
 static_assert(sizeof(DevStats) % 8 == 0, "DevStats is copied in 8-byte words");
 
+// A step's I/O in the caller's own memory (pinned host or device memory, which
+// the kernels address directly: on GB300 the host arrays are read and written
+// over NVLink-C2C inside the step, with no copy operations).  The host rewrites
+// it before each step; the step reads it at run time, so one captured graph
+// serves every call.
+struct StepIo {
+    const float *force3;  // xyz per body for bodies [0, force3n), zero beyond (null: none)
+    float *pos3;          // xyz per body, written by the pose kernel (null: none)
+    float4 *rot4;         // quaternion per body, written by the pose kernel (null: none)
+    uint32_t force3n;
+    uint32_t pad;
+};
+
 struct WorldView {
     uint32_t nb, nc;
     BodyState cur, nxt;
+    const StepIo *io;        // nullable: the step's I/O descriptor (in place of force3 / pos3)
     const float4 *force;     // nullable: all forces zero
     // nullable: the caller's forces as they were handed over (xyz for bodies
     // [0, force3n), zero beyond), read in place of `force`

@@ -33,10 +33,11 @@ World::World(int device) : device_(device) {
     PE_CHECK(cudaSetDevice(device_));
     PE_CHECK(cudaDeviceGetAttribute(&smCount_, cudaDevAttrMultiProcessorCount, device_));
     PE_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
-    PE_CHECK(cudaEventCreate(&evStart_));
-    PE_CHECK(cudaEventCreate(&evEnd_));
     PE_CHECK(cudaMallocHost(&hostStats_, sizeof(DevStats)));
     std::memset(hostStats_, 0, sizeof(DevStats));
+    PE_CHECK(cudaHostAlloc(reinterpret_cast<void **>(&ioHost_), sizeof(StepIo), cudaHostAllocMapped));
+    std::memset(ioHost_, 0, sizeof(StepIo));
+    PE_CHECK(cudaHostGetDevicePointer(reinterpret_cast<void **>(&ioDev_), ioHost_, 0));
     stats_.reserve(1);
     poseDone_.reserve(1);
     cCount_.reserve(2);
@@ -47,13 +48,30 @@ World::~World() {
     if (stream_) cudaStreamSynchronize(stream_);
     dropGraphs();
     if (hostStats_) cudaFreeHost(hostStats_);
+    if (ioHost_) cudaFreeHost(ioHost_);
     if (pinned_) cudaFreeHost(pinned_);
-    if (evStart_) cudaEventDestroy(evStart_);
-    if (evEnd_) cudaEventDestroy(evEnd_);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
 void World::syncDevice() { PE_CHECK(cudaStreamSynchronize(stream_)); }
+
+// The device address of a caller's array when this world's kernels can read
+// and write it in place — pinned host memory (mapped into every device's
+// address space under unified addressing; on GB300 reached over NVLink-C2C) or
+// memory of this device — aligned to `align` bytes; nullptr otherwise
+// (pageable host memory goes through copies).
+void *World::deviceAddress(const void *p, size_t align) const {
+    if (reinterpret_cast<uintptr_t>(p) % align) return nullptr;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();  // not a CUDA allocation: no sticky error
+        return nullptr;
+    }
+    if (at.type == cudaMemoryTypeHost) return at.devicePointer;
+    if ((at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) && at.device == device_)
+        return at.devicePointer;
+    return nullptr;
+}
 
 // ---------------------------------------------------------------- slots ----
 uint32_t World::addBody(const HostBody &b, uint32_t &generation) {
@@ -719,6 +737,7 @@ WorldView World::view(float dt) {
     w.force3 = rawForces_ ? xfer3_.ptr : nullptr;
     w.force3n = rawForces_ ? force3n_ : 0u;
     w.pos3 = packPoses_ ? posOut_.ptr : nullptr;
+    w.io = ioMode_ ? ioDev_ : nullptr;
     w.mat = mat_.ptr;
     w.iinv = iinv_.ptr;
     w.bflags = bflags_.ptr;
@@ -940,7 +959,8 @@ bool World::GraphKey::operator==(const GraphKey &o) const {
            coopBlocks == o.coopBlocks && blockSolver == o.blockSolver && blockM == o.blockM && pairBits == o.pairBits &&
            blockPairs == o.blockPairs && bodyPairs == o.bodyPairs && hashed == o.hashed && gridKeyBits == o.gridKeyBits && cellSize == o.cellSize && dense == o.dense &&
            localIdentity == o.localIdentity && forces == o.forces && identityColliders == o.identityColliders &&
-           sleeping == o.sleeping && rawForces == o.rawForces && packPoses == o.packPoses && force3n == o.force3n;
+           sleeping == o.sleeping && rawForces == o.rawForces && packPoses == o.packPoses && ioMode == o.ioMode &&
+           force3n == o.force3n;
 }
 
 World::GraphKey World::currentKey(float dt) const {
@@ -974,6 +994,7 @@ World::GraphKey World::currentKey(float dt) const {
     k.sleeping = sleepingEnabled;
     k.rawForces = rawForces_;
     k.packPoses = packPoses_;
+    k.ioMode = ioMode_;
     k.force3n = rawForces_ ? force3n_ : 0u;
     return k;
 }
@@ -1079,8 +1100,29 @@ void World::runStep(float dt, const float *forces, uint32_t nForces, float *posi
     // Step I/O without extra kernels: the step reads the caller's forces where
     // they land and writes packed positions from its pose kernel.  With
     // sleeping on, forces go through the expanding kernel (it wakes bodies).
-    rawForces_ = packPoses_ = false;
+    // When every array the caller hands over is addressable by the device
+    // (pinned host memory, or device memory of this device), the step reads and
+    // writes them in place through the I/O descriptor: no copy operations.
+    rawForces_ = packPoses_ = ioMode_ = false;
     force3n_ = 0;
+    {
+        const bool staged = forces && nForces && (sleepingEnabled || forces_);
+        const void *fDev = nullptr;
+        void *pDev = nullptr, *rDev = nullptr;
+        bool direct = !staged;
+        if (direct && forces && nForces) direct = (fDev = deviceAddress(forces, 4)) != nullptr;
+        if (direct && positions && nb_) direct = (pDev = deviceAddress(positions, 4)) != nullptr;
+        if (direct && rotations && nb_) direct = (rDev = deviceAddress(rotations, 16)) != nullptr;
+        if (direct && (fDev || pDev || rDev)) {
+            ioHost_->force3 = static_cast<const float *>(fDev);
+            ioHost_->force3n = fDev ? std::min<uint32_t>(nForces, nb_) : 0u;
+            ioHost_->pos3 = static_cast<float *>(pDev);
+            ioHost_->rot4 = static_cast<float4 *>(rDev);
+            ioMode_ = true;
+            forces = nullptr;  // handled in place
+            nForces = 0;
+        }
+    }
     if (forces && nForces) {
         if (sleepingEnabled || forces_) {  // forces_: forces written earlier for this step
             stageForces(forces, nForces);
@@ -1093,7 +1135,7 @@ void World::runStep(float dt, const float *forces, uint32_t nForces, float *posi
             rawForces_ = force3n_ > 0;
         }
     }
-    if (positions && nb_) {
+    if (positions && nb_ && !ioMode_) {
         posOut_.reserve(3 * (size_t)nb_);
         packPoses_ = true;
     }
@@ -1111,24 +1153,22 @@ void World::runStep(float dt, const float *forces, uint32_t nForces, float *posi
         wakeCheck_ = false;
     }
     for (int attempt = 0; attempt < 8; ++attempt) {
-        PE_CHECK(cudaEventRecord(evStart_, stream_));
         const unsigned long long launches = launchStep(dt);
-        PE_CHECK(cudaEventRecord(evEnd_, stream_));
         // poses of this attempt's output copy, read back under the same
         // synchronisation as the step (a re-run attempt copies them again)
-        if (nb_ && positions)
+        if (nb_ && positions && !ioMode_)
             PE_CHECK(cudaMemcpyAsync(positions, posOut_.ptr, 3 * (size_t)nb_ * sizeof(float), cudaMemcpyDeviceToHost,
                                      stream_));
-        if (nb_ && rotations) enqueuePoses(1 - cur_, nullptr, rotations);
+        if (nb_ && rotations && !ioMode_) enqueuePoses(1 - cur_, nullptr, rotations);
         if (finishStep()) {
-            rawForces_ = packPoses_ = false;
-            float ms = 0, st[5] = {0, 0, 0, 0, 0};
-            PE_CHECK(cudaEventElapsedTime(&ms, evStart_, evEnd_));
-            // stage times from the stamps the stage kernels wrote (0 when a
-            // stage ran no stamping kernel this step)
+            rawForces_ = packPoses_ = ioMode_ = false;
+            // device and stage times from the stamps the stage kernels wrote
+            // (no event nodes or queries on the step's path; 0 when a stage ran
+            // no stamping kernel this step): integrate start to pose end
+            float st[5] = {0, 0, 0, 0, 0};
             const unsigned long long *t = hostStats_->stamp;
             for (int k = 0; k < 5; ++k) st[k] = t[k + 1] > t[k] ? (float)((t[k + 1] - t[k]) * 1e-6) : 0.0f;
-            counters_.gpuMs = ms;
+            counters_.gpuMs = t[0] && t[5] > t[0] ? (t[5] - t[0]) * 1e-6 : 0.0;
             counters_.integrateMs = st[0];
             counters_.broadphaseMs = st[1];
             counters_.narrowphaseMs = st[2];

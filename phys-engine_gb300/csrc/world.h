@@ -304,7 +304,6 @@ class World {
     uint32_t scratchN_ = 0;
     DeviceArray<DevStats> stats_;
     DevStats *hostStats_ = nullptr;
-    cudaEvent_t evStart_ = nullptr, evEnd_ = nullptr;
     // Captured step pipelines, one per ping-pong parity, valid for graphKey_.
     struct GraphKey {
         uint32_t nb, nc, pairCap, entryCap, mcap, cacheCap;
@@ -314,7 +313,7 @@ class World {
         uint32_t blockM;
         uint32_t pairBits, gridKeyBits;
         double cellSize;
-        bool dense, localIdentity, forces, identityColliders, sleeping, rawForces, packPoses;
+        bool dense, localIdentity, forces, identityColliders, sleeping, rawForces, packPoses, ioMode;
         uint32_t force3n;
         bool operator==(const GraphKey &o) const;
     };
@@ -336,6 +335,12 @@ class World {
     float4 *pinned_ = nullptr;
     size_t pinnedCount_ = 0;
     float4 *pinnedBuffer(size_t n);
+    // Step I/O descriptor in mapped pinned memory (host and device addresses);
+    // ioMode_: this step reads and writes the caller's arrays through it.
+    StepIo *ioHost_ = nullptr;
+    StepIo *ioDev_ = nullptr;
+    bool ioMode_ = false;
+    void *deviceAddress(const void *p, size_t align) const;
 };
 
 } // namespace pe

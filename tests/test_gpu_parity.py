@@ -621,6 +621,43 @@ def test_step_io_equals_separate_calls(gpu):
     compare_worlds(a, b, "after step_io")
 
 
+def test_step_io_in_place_with_pinned_arrays(gpu):
+    """With pinned host arrays the step reads the forces and writes the poses in
+    place (the pose kernel writes the caller's memory through the step's I/O
+    descriptor, no copy operations); the results equal separate calls bit for
+    bit, also on steps where one array is pageable or the rotation array is not
+    16-byte aligned (those go through copies)."""
+    torch = pytest.importorskip("torch")
+    sc = scenes.generate(scenes.MIXED_VOLUME, 5000, 3)
+    a = gpu.GpuWorld(algo=1, cell_size=2.2, iterations=10)
+    b = gpu.GpuWorld(algo=1, cell_size=2.2, iterations=10)
+    a.load_scene(sc)
+    b.load_scene(sc)
+    rng = np.random.default_rng(2)
+    n = sc.count
+
+    def pinned(count):
+        return torch.zeros(count, dtype=torch.float32).pin_memory().numpy()
+
+    for s in range(10):
+        f = pinned(3 * n).reshape(n, 3)
+        f[:] = rng.normal(size=(n, 3)).astype(np.float32) * (s % 3)
+        pa = pinned(3 * n).reshape(n, 3)
+        qa = pinned(4 * n).reshape(n, 4)
+        if s == 4:
+            pa = np.zeros((n, 3), np.float32)  # pageable: this step copies
+        if s == 6:
+            qa = pinned(4 * n + 1)[1:].reshape(n, 4)  # 4 bytes off 16-byte alignment
+        pb, qb = np.zeros((n, 3), np.float32), np.zeros((n, 4), np.float32)
+        a.step_io(1 / 60, f, pa, qa)
+        b.write_forces(np.array(f))
+        b.step(1 / 60)
+        b.read_poses(pb, qb)
+        assert_bit_equal(np.array(pa), pb, f"step {s} positions")
+        assert_bit_equal(np.array(qa), qb, f"step {s} rotations")
+    compare_worlds(a, b, "after in-place step_io")
+
+
 # ------------------------------------------- benchmarked configurations ---
 def _bench_cell(sc):
     """The benchmark's grid cell: 2 x the largest collider extent (sphere
