@@ -621,7 +621,7 @@ def run_batched(args, local_rank, flush, peak):
                      "traffic_source": (profiled_traffic("k_batch_step", algo_bytes) or {}).get("source"),
                      "algorithmic_bytes_per_step": algo_bytes},
         "e2e": {"value": len(sizes) * e2e_steps / e2e_s, "unit": "world-steps/s",
-                "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 32 * n, "steps": e2e_steps},
+                "h2d_bytes_per_step": 12 * n, "d2h_bytes_per_step": 28 * n, "steps": e2e_steps},
         "gpu_launches": int(steps * len(buckets)),
         "autotune": [{"bodies": [int(b["min_bodies"]), int(min(b["max_bodies"], BATCH_MAX))],
                       "worlds": int(b["world_count"]), "threads": int(b["threads"]),

@@ -68,7 +68,6 @@ Batch::~Batch() {
     if (stream_) cudaStreamSynchronize(stream_);
     dropGraphs();
     if (hostErr_) cudaFreeHost(hostErr_);
-    if (hostStage_) cudaFreeHost(hostStage_);
     for (auto s : side_) cudaStreamDestroy(s);
     for (auto e : joins_) cudaEventDestroy(e);
     if (fork_) cudaEventDestroy(fork_);
@@ -556,42 +555,64 @@ void Batch::writeBodies(const float *pos, const float *rot, const float *lin, co
     }
 }
 
+// Forces in and poses out are repacked on the device (xyz per body <-> the
+// engine's float4 arrays), reading and writing the caller's arrays in place
+// when they are device-addressable (pinned host memory: over NVLink-C2C on
+// GB300), through one plain copy each way otherwise.
+__global__ void k_batch_forces_in(const float *f3, float4 *force, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        force[i] = make_float4(f3[3 * i], f3[3 * i + 1], f3[3 * i + 2], 0.0f);
+}
+
+__global__ void k_batch_poses_out(const float4 *pos, const float4 *rot, float *p3, float *q4, bool q4Vector,
+                                  uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float4 p = pos[i], q = rot[i];
+        p3[3 * i] = p.x;
+        p3[3 * i + 1] = p.y;
+        p3[3 * i + 2] = p.z;
+        if (q4Vector) {
+            reinterpret_cast<float4 *>(q4)[i] = q;
+        } else {
+            q4[4 * i] = q.x;
+            q4[4 * i + 1] = q.y;
+            q4[4 * i + 2] = q.z;
+            q4[4 * i + 3] = q.w;
+        }
+    }
+}
+
 void Batch::writeForces(const float *forces) {
     PE_CHECK(cudaSetDevice(device_));
-    if (hostStageCount_ < 2 * nb_) {
-        if (hostStage_) cudaFreeHost(hostStage_);
-        hostStage_ = nullptr;
-        PE_CHECK(cudaMallocHost(&hostStage_, 2 * nb_ * sizeof(float4)));
-        hostStageCount_ = 2 * nb_;
+    const float *src = static_cast<const float *>(deviceAddress(forces, 4, device_));
+    if (!src) {
+        xfer_.reserve(4 * (size_t)nb_);
+        PE_CHECK(cudaMemcpyAsync(xfer_.ptr, forces, 3 * (size_t)nb_ * sizeof(float), cudaMemcpyHostToDevice, stream_));
+        src = xfer_.ptr;
     }
-    for (uint64_t i = 0; i < nb_; ++i)
-        hostStage_[i] = make_float4(forces[3 * i], forces[3 * i + 1], forces[3 * i + 2], 0.0f);
-    PE_CHECK(cudaMemcpyAsync(force_.ptr, hostStage_, nb_ * sizeof(float4), cudaMemcpyHostToDevice, stream_));
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((nb_ + 255) / 256, 8ull * smCount());
+    k_batch_forces_in<<<std::max(grid, 1u), 256, 0, stream_>>>(src, force_.ptr, nb_);
+    PE_LAUNCHED();
+    // read in place: the caller's array is free again when this returns
+    if (src != xfer_.ptr) PE_CHECK(cudaStreamSynchronize(stream_));
     forces_ = true;
 }
 
 void Batch::readPoses(float *pos, float *rot) {
     PE_CHECK(cudaSetDevice(device_));
-    if (hostStageCount_ < 2 * nb_) {
-        if (hostStage_) cudaFreeHost(hostStage_);
-        hostStage_ = nullptr;
-        PE_CHECK(cudaMallocHost(&hostStage_, 2 * nb_ * sizeof(float4)));
-        hostStageCount_ = 2 * nb_;
-    }
-    PE_CHECK(cudaMemcpyAsync(hostStage_, pos_[parity_].ptr, nb_ * sizeof(float4), cudaMemcpyDeviceToHost, stream_));
-    PE_CHECK(cudaMemcpyAsync(hostStage_ + nb_, rot_[parity_].ptr, nb_ * sizeof(float4), cudaMemcpyDeviceToHost,
-                             stream_));
+    float *p = static_cast<float *>(deviceAddress(pos, 4, device_));
+    float *q = static_cast<float *>(deviceAddress(rot, 4, device_));
+    float *pd = p, *qd = q;
+    if (!p || !q) xfer_.reserve(7 * (size_t)nb_);
+    if (!p) pd = xfer_.ptr;
+    if (!q) qd = xfer_.ptr + 3 * (size_t)nb_;
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((nb_ + 255) / 256, 8ull * smCount());
+    k_batch_poses_out<<<std::max(grid, 1u), 256, 0, stream_>>>(pos_[parity_].ptr, rot_[parity_].ptr, pd, qd,
+                                                                reinterpret_cast<uintptr_t>(qd) % 16 == 0, nb_);
+    PE_LAUNCHED();
+    if (!p) PE_CHECK(cudaMemcpyAsync(pos, pd, 3 * (size_t)nb_ * sizeof(float), cudaMemcpyDeviceToHost, stream_));
+    if (!q) PE_CHECK(cudaMemcpyAsync(rot, qd, 4 * (size_t)nb_ * sizeof(float), cudaMemcpyDeviceToHost, stream_));
     PE_CHECK(cudaStreamSynchronize(stream_));
-    for (uint64_t i = 0; i < nb_; ++i) {
-        const float4 p = hostStage_[i], q = hostStage_[nb_ + i];
-        pos[3 * i] = p.x;
-        pos[3 * i + 1] = p.y;
-        pos[3 * i + 2] = p.z;
-        rot[4 * i] = q.x;
-        rot[4 * i + 1] = q.y;
-        rot[4 * i + 2] = q.z;
-        rot[4 * i + 3] = q.w;
-    }
 }
 
 void Batch::worldCounters(uint32_t w, StepCounters &c) {

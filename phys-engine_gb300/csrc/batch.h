@@ -167,8 +167,7 @@ class Batch {
     DeviceArray<WorldDesc> descDev_;
     DeviceArray<uint32_t> queue_, queueHead_, batchErr_;
     uint32_t *hostErr_ = nullptr;
-    float4 *hostStage_ = nullptr;
-    size_t hostStageCount_ = 0;
+    DeviceArray<float> xfer_;  // forces in / poses out when the caller's arrays are pageable
     uint64_t pairTotal_ = 0, mTotal_ = 0, cacheTotal_ = 0;
     size_t deviceBytes_ = 0;
 

@@ -37,6 +37,13 @@ void setSpinLimitIslands(uint32_t limit);
 // Streaming multiprocessors of the current device (queried once per device and
 // cached); launch sizes of the persistent and grid-stride kernels scale with it.
 int smCount();
+
+// The device address of a caller's array when kernels on `device` can read and
+// write it in place — pinned host memory (mapped into every device's address
+// space under unified addressing; on GB300 reached over NVLink-C2C) or memory
+// of that device — aligned to `align` bytes; nullptr otherwise (pageable host
+// memory goes through copies).
+void *deviceAddress(const void *p, size_t align, int device);
 #define PE_LAUNCHED()                                                                               \
     do {                                                                                            \
         PE_CHECK(cudaGetLastError());                                                               \

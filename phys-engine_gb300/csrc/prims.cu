@@ -42,6 +42,19 @@ int smCount() {
     return n;
 }
 
+void *deviceAddress(const void *p, size_t align, int device) {
+    if (!p || reinterpret_cast<uintptr_t>(p) % align) return nullptr;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();  // not a CUDA allocation: no sticky error
+        return nullptr;
+    }
+    if (at.type == cudaMemoryTypeHost) return at.devicePointer;
+    if ((at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) && at.device == device)
+        return at.devicePointer;
+    return nullptr;
+}
+
 namespace {
 inline uint32_t persistentGrid(uint32_t tiles) {
     return std::max<uint32_t>(1, std::min<uint32_t>(tiles, 4u * (uint32_t)smCount()));

@@ -55,23 +55,7 @@ World::~World() {
 
 void World::syncDevice() { PE_CHECK(cudaStreamSynchronize(stream_)); }
 
-// The device address of a caller's array when this world's kernels can read
-// and write it in place — pinned host memory (mapped into every device's
-// address space under unified addressing; on GB300 reached over NVLink-C2C) or
-// memory of this device — aligned to `align` bytes; nullptr otherwise
-// (pageable host memory goes through copies).
-void *World::deviceAddress(const void *p, size_t align) const {
-    if (reinterpret_cast<uintptr_t>(p) % align) return nullptr;
-    cudaPointerAttributes at{};
-    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-        cudaGetLastError();  // not a CUDA allocation: no sticky error
-        return nullptr;
-    }
-    if (at.type == cudaMemoryTypeHost) return at.devicePointer;
-    if ((at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) && at.device == device_)
-        return at.devicePointer;
-    return nullptr;
-}
+void *World::deviceAddress(const void *p, size_t align) const { return pe::deviceAddress(p, align, device_); }
 
 // ---------------------------------------------------------------- slots ----
 uint32_t World::addBody(const HostBody &b, uint32_t &generation) {

@@ -124,6 +124,24 @@ def test_batch_forces_and_body_writes(gpu):
     batch.read_poses(pos, rot)
     assert_bit_equal(pos, batch.bodies()[0], "read_poses positions")
     assert_bit_equal(rot, batch.bodies()[1], "read_poses rotations")
+    # pinned host arrays are read and written in place by the repacking kernels
+    torch = pytest.importorskip("torch")
+    pin = lambda count: torch.zeros(count, dtype=torch.float32).pin_memory().numpy()
+    pf = pin(3 * batch.n).reshape(batch.n, 3)
+    pf[:] = forces
+    batch.write_forces(pf)
+    for w, gw in enumerate(worlds):
+        gw.write_forces(forces[batch.starts[w]:batch.starts[w + 1]])
+    batch.step(DT)
+    for gw in worlds:
+        gw.step(DT)
+    for w, gw in enumerate(worlds):
+        compare(batch, w, gw, f"pinned forces world {w}")
+    pp = pin(3 * batch.n).reshape(batch.n, 3)
+    pq = pin(4 * batch.n + 1)[1:].reshape(batch.n, 4)  # not 16-byte aligned: written per float
+    batch.read_poses(pp, pq)
+    assert_bit_equal(np.array(pp), batch.bodies()[0], "pinned read_poses positions")
+    assert_bit_equal(np.array(pq), batch.bodies()[1], "pinned read_poses rotations")
     # writing the state back unchanged leaves the next step identical
     p, q, l, a = batch.bodies()
     batch.write_bodies(p, q, l, a)
