@@ -28,6 +28,8 @@
 //                 colour, a grid barrier per colour.  Manifolds of one colour
 //                 share no dynamic body, so their order inside a colour does
 //                 not change the result.
+#include <stdexcept>
+
 #include "pe_block.cuh"
 #include "pe_kernels.cuh"
 #include "pe_prims.cuh"
@@ -393,8 +395,82 @@ __device__ void islSolveWide(const SolveArgs &a, uint32_t M, uint32_t C) {
         }
 }
 
+// GlobalVel with the manifold's bodies already loaded.
+struct BodiesGiven {
+    const SolveArgs &a;
+    uint2 b;
+    __device__ __forceinline__ uint2 bodies(uint32_t, uint32_t) const { return b; }
+    __device__ __forceinline__ V3 lin(uint32_t i) const { return f4xyz(ld4(&a.w.nxt.lin[i])); }
+    __device__ __forceinline__ V3 ang(uint32_t i) const { return f4xyz(ld4(&a.w.nxt.ang[i])); }
+    __device__ __forceinline__ void store(uint32_t i, const V3 &l, const V3 &w) const {
+        st4(&a.w.nxt.lin[i], make4(l, 0.0f));
+        st4(&a.w.nxt.ang[i], make4(w, 0.0f));
+    }
+};
+
+// Grid-wide sweeps: each thread keeps one shared-memory slot holding the
+// prepared data of its manifold of the coming colour step (the manifold's
+// normal and masses, then per point the ten prepared vectors and the
+// impulse), laid out field-major across the block's threads.  The copy is
+// issued (cp.async) as soon as the thread has finished its manifold of the
+// current step, so it lands while the grid waits at the colour barrier; after
+// the barrier only the body velocities are loaded from memory.
+constexpr uint32_t kSlotPoint = kPreparedVec4 + 1;                 // prepared vectors + impulse
+constexpr uint32_t kSlotVec4 = 2 + 4 * kSlotPoint;                 // pm, pn, 4 points
+constexpr size_t kLargeSmem = (size_t)kSlotVec4 * kSolveThreads * sizeof(float4);  // 188,416 bytes
+// List entries of the grid-wide sweeps: manifold index | solved points << 29.
+constexpr uint32_t kEntryShift = 29;
+constexpr uint32_t kEntryMask = (1u << kEntryShift) - 1u;
+
+__device__ __forceinline__ void cpAsync16(float4 *dst, const float4 *src) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cpAsyncWaitAll() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// slot: this thread's column (s_slot + threadIdx.x), stride kSolveThreads.
+__device__ __forceinline__ void fetchSlot(const SolveArgs &a, float4 *slot, uint32_t m, uint32_t npts) {
+    const uint32_t mcap = a.mcap;
+    cpAsync16(slot, &a.sb.pm[m]);
+    cpAsync16(slot + kSolveThreads, &a.sb.pn[m]);
+    for (uint32_t p = 0; p < npts; ++p) {
+        float4 *d = slot + (size_t)(2 + p * kSlotPoint) * kSolveThreads;
+#pragma unroll
+        for (uint32_t v = 0; v < (uint32_t)kPreparedVec4; ++v)
+            cpAsync16(d + (size_t)v * kSolveThreads, &a.sb.pp[(size_t)(v * 4 + p) * mcap + m]);
+        cpAsync16(d + (size_t)kPreparedVec4 * kSolveThreads, &a.sb.pimp[(size_t)p * mcap + m]);
+    }
+    cpAsyncCommit();
+}
+
+// Prepared data of one manifold from this thread's slot; impulses are written
+// back to the solver arrays (the slot is refilled for every colour step).
+struct SlotPrep {
+    const SolveArgs &a;
+    const float4 *slot;
+    uint32_t m, npts;
+    __device__ __forceinline__ float4 pm(uint32_t) const { return slot[0]; }
+    __device__ __forceinline__ float4 pn(uint32_t) const { return slot[kSolveThreads]; }
+    __device__ __forceinline__ uint32_t count(uint32_t) const { return npts; }
+    __device__ __forceinline__ float4 inertia(int r, uint32_t) const {
+        return a.sb.pmInertia[(size_t)r * a.mcap + m];
+    }
+    __device__ __forceinline__ float4 pt(int v, uint32_t p, uint32_t) const {
+        return slot[(size_t)(2 + p * kSlotPoint + v) * kSolveThreads];
+    }
+    __device__ __forceinline__ float4 imp(uint32_t p, uint32_t) const {
+        return slot[(size_t)(2 + p * kSlotPoint + kPreparedVec4) * kSolveThreads];
+    }
+    __device__ __forceinline__ void setImp(uint32_t p, uint32_t, const float4 &v) const {
+        a.sb.pimp[(size_t)p * a.mcap + m] = v;
+    }
+};
+
 __global__ void __launch_bounds__(kSolveThreads) k_isl_solve_large(SolveArgs a) {
     __shared__ uint32_t s_start[kMaxColors + 1];
+    __shared__ uint32_t s_colors[kMaxColors], s_colorN;
+    extern __shared__ float4 s_slot[];
     {
         const uint32_t M = min(*a.count, a.mcap);
         const uint32_t wideC = islWideColors(a, M);
@@ -424,23 +500,87 @@ __global__ void __launch_bounds__(kSolveThreads) k_isl_solve_large(SolveArgs a) 
         const uint32_t r = a.sb.islRoot[m];
         const uint32_t c = a.sb.color[m];
         if (r == kIslNone || cnt[r] < sweepFrom || c >= (uint32_t)kMaxColors) continue;
-        list[s_start[c] + aggregatedAppendKeyed(fill, c)] = m;
+        list[s_start[c] + aggregatedAppendKeyed(fill, c)] = m | min(a.sb.pcount[m], 4u) << kEntryShift;
+    }
+    // the non-empty colours, in order
+    if (threadIdx.x == 0) {
+        uint32_t n = 0;
+        for (int c = 0; c < kMaxColors; ++c)
+            if (s_start[c] != s_start[c + 1]) s_colors[n++] = (uint32_t)c;
+        s_colorN = n;
     }
     if (!gridBarrier(a.sb.bar, &a.st->err)) return;
-    for (int pass = 0; pass <= a.iterations; ++pass)
-        for (int c = 0; c < kMaxColors; ++c) {
-            if (s_start[c] == s_start[c + 1]) continue;
-            for (uint32_t k = s_start[c] + gtid; k < s_start[c + 1]; k += gstride) {
-                if (pass == 0) warmStartOne(a, k, list[k]);
-                else solveOne(a, k, list[k]);
+    // Colour steps in (pass, colour) order.  A thread's first manifold of a
+    // step is the same in every pass.  Its
+    // list entry is loaded while the step before is solved, its bodies and
+    // (passes after the warm start) its slot right after that step, before
+    // the barrier; further manifolds of the step (more than one per thread)
+    // read the solver arrays.
+    // Solve index j of a colour goes to block j % gridDim.x, thread j /
+    // gridDim.x: a colour's manifolds are spread over every SM of the grid
+    // (a thin colour keeps one warp per block busy, not a few full blocks).
+    const uint32_t nC = s_colorN;
+    const uint32_t nSteps = nC * (uint32_t)(a.iterations + 1);
+    const uint32_t lane = threadIdx.x * gridDim.x + blockIdx.x;
+    float4 *slot = s_slot + threadIdx.x;
+    const GlobalPrep gp{a};
+    auto firstIndex = [&](uint32_t step) { return s_start[s_colors[step % nC]] + lane; };
+    auto stepEnd = [&](uint32_t step) { return s_start[s_colors[step % nC] + 1]; };
+    uint32_t e = 0;
+    uint2 b = make_uint2(0u, 0u);
+    if (firstIndex(0) < stepEnd(0)) {
+        e = __ldcg(&list[firstIndex(0)]);
+        b = __ldcg(&a.sb.pbody[e & kEntryMask]);
+    }
+    for (uint32_t step = 0; step < nSteps; ++step) {
+        const uint32_t pass = step / nC;
+        const uint32_t k0 = firstIndex(step), end = stepEnd(step);
+        const bool next = step + 1 < nSteps && firstIndex(step + 1) < stepEnd(step + 1);
+        const uint32_t eNext = next ? __ldcg(&list[firstIndex(step + 1)]) : 0u;
+        if (k0 < end) {
+            const uint32_t m = e & kEntryMask;
+            const BodiesGiven v{a, b};
+            if (pass == 0) {
+                warmStartOne(gp, k0, m, v);
+            } else {
+                cpAsyncWaitAll();
+                solveOne(SlotPrep{a, slot, m, e >> kEntryShift}, k0, m, v);
             }
-            if (!gridBarrier(a.sb.bar, &a.st->err)) return;
+            for (uint32_t k = k0 + gstride; k < end; k += gstride) {
+                const uint32_t mk = __ldcg(&list[k]) & kEntryMask;
+                const BodiesGiven vk{a, __ldcg(&a.sb.pbody[mk])};
+                if (pass == 0) warmStartOne(gp, k, mk, vk);
+                else solveOneChained(gp, k, mk, vk);
+            }
         }
+        if (next) {
+            e = eNext;
+            b = __ldcg(&a.sb.pbody[e & kEntryMask]);
+            if ((step + 1) / nC > 0) fetchSlot(a, slot, e & kEntryMask, e >> kEntryShift);
+        }
+        if (!gridBarrier(a.sb.bar, &a.st->err)) {
+            cpAsyncWaitAll();  // no copy into shared memory outlives the block
+            return;
+        }
+    }
+    cpAsyncWaitAll();
 }
 
+namespace {
+void configureLargeSweeps() {
+    static bool configured = false;
+    if (!configured) {
+        PE_CHECK(cudaFuncSetAttribute(k_isl_solve_large, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kLargeSmem));
+        configured = true;
+    }
+}
+} // namespace
+
 int solveIslandsBlocksPerSm() {
+    configureLargeSweeps();
     int b = 0;
-    PE_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_isl_solve_large, kSolveThreads, 0));
+    PE_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_isl_solve_large, kSolveThreads, kLargeSmem));
     return b;
 }
 
@@ -459,11 +599,15 @@ void launchSolveIslands(const SolveArgs &a, int coopBlocks, Scratch &ws, cudaStr
     PE_LAUNCHED();
     k_isl_solve<<<4 * smCount(), kIslThreads, 0, s>>>(a);
     PE_LAUNCHED();
+    // list entries carry the manifold index in kEntryShift bits
+    if (mcap > kEntryMask) throw std::length_error("manifold capacity beyond the grid-wide sweeps' index range");
+    configureLargeSweeps();
     SolveArgs args = a;
     void *params[] = {&args};
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(coopBlocks);
     cfg.blockDim = dim3(kSolveThreads);
+    cfg.dynamicSmemBytes = kLargeSmem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;

@@ -132,30 +132,28 @@ __device__ __forceinline__ uint32_t takeTile(uint32_t *counter, uint32_t *slot) 
 }
 
 // Grid-wide barrier for cooperative launches (all blocks co-resident).  bar[0]
-// counts arrivals, bar[1] is the generation.  Bounded spin: returns false on
-// every thread of the block when its wait ran out (kErrTimeout raised), and
-// the caller returns from the kernel at once.  The counters are reset before
-// every launch that uses them.
+// only ever counts arrivals: the barrier a block arrives at ends when the
+// count reaches the next multiple of the grid size, so the last block's
+// arrival is the release (one atomic per block, no reset or generation word
+// on the path).  Every kernel that shares the counter between two resets runs
+// the same grid size and passes every barrier on every block.  Bounded spin:
+// returns false on every thread of the block when its wait ran out
+// (kErrTimeout raised), and the caller returns from the kernel at once.  The
+// counter is reset before every solver pass that uses it.
 __device__ __forceinline__ bool gridBarrier(uint32_t *bar, uint32_t *err) {
     __shared__ uint32_t s_barrierTimedOut;
     __syncthreads();
     if (threadIdx.x == 0) {
         s_barrierTimedOut = 0;
-        uint32_t gen = ldvol(&bar[1]);
         __threadfence();
-        uint32_t arrived = atomicAdd(&bar[0], 1u);
-        if (arrived == gridDim.x - 1) {
-            atomicExch(&bar[0], 0u);
-            __threadfence();
-            atomicAdd(&bar[1], 1u);
-        } else {
-            uint32_t spins = 0;
-            while (ldvol(&bar[1]) == gen) {
-                if (++spins > spinLimit()) {
-                    atomicOr(err, kErrTimeout);
-                    s_barrierTimedOut = 1;
-                    break;
-                }
+        const uint32_t arrived = atomicAdd(&bar[0], 1u);
+        const uint32_t target = (arrived / gridDim.x + 1u) * gridDim.x;
+        uint32_t spins = 0;
+        while ((int32_t)(ldvol(&bar[0]) - target) < 0) {
+            if (++spins > spinLimit()) {
+                atomicOr(err, kErrTimeout);
+                s_barrierTimedOut = 1;
+                break;
             }
         }
         __threadfence();

@@ -994,11 +994,12 @@ void World::dropGraphs() {
 // Enqueues one step: through a captured graph when possible, else directly.
 // Returns the number of engine kernels the step launches.
 unsigned long long World::launchStep(float dt) {
-    // Cooperative solver grid from the last step's manifold count, in powers of
-    // two so the captured graph rarely changes.
-    uint32_t want = (lastMEstimate_ + 1023) / 1024, blocks = 1;
-    while (blocks < want) blocks <<= 1;
-    coopBlocks_ = (int)std::min<uint32_t>(blocks, (uint32_t)maxCooperativeBlocks(smCount_));
+    // Cooperative solver grid: every block the device holds at once.  The
+    // grid-wide colour sweeps deal each colour's manifolds over all blocks, so
+    // a colour of a few thousand manifolds keeps a warp or two busy on every
+    // SM rather than filling a few SMs (measured: 0.80 -> 0.58 ms per step on
+    // the 10,000-body field, grids sized by manifold count before).
+    coopBlocks_ = maxCooperativeBlocks(smCount_);
     // Small manifold counts run the single-block solver (with headroom over
     // the last step's count; an overflow re-runs the step on the full path).
     blockSolver_ = lastMEstimate_ + lastMEstimate_ / 4 + 64 <= kBlockMaxManifolds && nb_ <= kBlockMaxBodies &&
