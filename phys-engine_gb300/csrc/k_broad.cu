@@ -148,64 +148,88 @@ __global__ void k_sap_emit(const uint32_t *d_n, const uint32_t *off, const uint3
 }
 
 // ------------------------------------------------------ SAP, one block ------
-// The whole sweep of a small world in one thread block: (min.x key, index)
-// bitonic-sorted in shared memory, each sorted entry's window by binary search,
-// the windows flattened by a block scan and dealt out in equal chunks (a floor
-// box's window holds every body: one thread per entry would walk it alone).
-// The sorted order, the windows, the window and pair counters and the pair keys
-// are those of the multi-kernel sweep above (one launch instead of a dozen; at
-// a thousand boxes the launches, not the work, set the sweep's time).
+// The whole sweep of a small world in one thread block: the (min.x key,
+// index) keys sorted in registers (blockRegisterSort), each sorted entry's
+// window by binary search, the windows flattened by a block scan and dealt out
+// in equal chunks (a floor box's window holds every body: one thread per entry
+// would walk it alone).  The sorted order, the windows, the window and pair
+// counters and the pair keys are those of the multi-kernel sweep above (one
+// launch instead of a dozen; at a thousand boxes the launches, not the work,
+// set the sweep's time).
+//
+// With `finalize` set the block also does what k_pairs_block does for the
+// step: the raw pairs stay in shared memory as 32-bit keys (first << bits |
+// second, 2 bits <= 32) and are put in order by their first index (counts per
+// first index taken during the sweep, a scan, a scatter), then each first
+// index's partners by second index (a thread per short list, a warp and a
+// bitmap of the second indices per long one: a floor box's list holds every
+// body); then mapped to collider slots, filtered of same-body pairs and
+// written in order.  The sweep emits each overlapping pair once, so there are
+// no duplicates to drop.  More raw pairs than kSapBlockPairs raise
+// kErrSmallPath (the step is re-run with the separate finalize).
 constexpr uint32_t kSapBlockMax = 4096;
-constexpr int kSapBlockThreads = 1024;
-constexpr size_t kSapBlockSmem = (size_t)kSapBlockMax * (8 + 16 + 4 + 4 + 4 + 4);
+constexpr uint32_t kSapBlockPairs = 8192;
+constexpr int kSapBlockThreads = (int)kRegSortThreads;
+// Shared memory: two sort buffers of kSapBlockMax u64 keys (the second also
+// holds the pair flags of the finalize), y/z bounds, min.x, max.x, entry
+// index, window offsets, then kSapBlockPairs u32 pair keys.
+constexpr size_t kSapBlockSmem = (size_t)kSapBlockMax * (8 + 8 + 16 + 4 + 4 + 4 + 4) + (size_t)kSapBlockPairs * 4;
+static_assert(kSapBlockPairs * 4 <= kSapBlockMax * 8, "pair flags fit one key buffer");
 
-__global__ void __launch_bounds__(kSapBlockThreads)
-k_sap_block(BroadInput in, uint32_t *sapKeys, uint32_t *sapVals, uint32_t *unsorted, unsigned long long *keys,
-            uint32_t cap, uint32_t bits, DevStats *st) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    unsigned long long *sk = reinterpret_cast<unsigned long long *>(smem);  // key << 32 | index
-    float4 *sYZ = reinterpret_cast<float4 *>(smem + (size_t)kSapBlockMax * 8);
-    float *sMinX = reinterpret_cast<float *>(smem + (size_t)kSapBlockMax * 24);
-    float *sMaxX = sMinX + kSapBlockMax;
-    uint32_t *sIdx = reinterpret_cast<uint32_t *>(sMaxX + kSapBlockMax);
-    uint32_t *sOff = sIdx + kSapBlockMax;  // window lengths, then their exclusive scan
-    __shared__ uint32_t s_count, s_scan[40];
-    const uint32_t tid = threadIdx.x, nt = blockDim.x;
-    const uint32_t n = min(*in.d_n, kSapBlockMax);  // the host launches this for at most kSapBlockMax boxes
-    uint32_t N = 1;
-    while (N < n) N <<= 1;
-    for (uint32_t i = tid; i < N; i += nt)
-        sk[i] = i < n ? ((unsigned long long)orderedFloatKey(in.mn[i].x) << 32 | i) : ~0ull;
-    if (tid == 0) {
-        s_count = 0;
-        if (unsorted) *unsorted = 0u;  // as after the multi-kernel sweep
+template <int E>
+__device__ __forceinline__ void sapSortKeys(const BroadInput &in, uint32_t n, unsigned long long *bufA,
+                                            unsigned long long *bufB, uint32_t *sapKeys, uint32_t *sapVals,
+                                            float *sMinX, float *sMaxX, float4 *sYZ, uint32_t *sIdx) {
+    const uint32_t tid = threadIdx.x;
+    unsigned long long v[E];
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+        const uint32_t i = tid * E + r;
+        v[r] = i < n ? ((unsigned long long)orderedFloatKey(in.mn[i].x) << 32 | i) : ~0ull;
     }
-    __syncthreads();
-    for (uint32_t k = 2; k <= N; k <<= 1)
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = tid; i < N; i += nt) {
-                const uint32_t l = i ^ j;
-                if (l > i) {
-                    const unsigned long long a = sk[i], b = sk[l];
-                    if ((a > b) == ((i & k) == 0)) {
-                        sk[i] = b;
-                        sk[l] = a;
-                    }
-                }
-            }
-            __syncthreads();
-        }
-    for (uint32_t i = tid; i < n; i += nt) {
-        const uint32_t idx = (uint32_t)sk[i];
+    blockRegisterSort<unsigned long long, E>(v, bufA, bufB);
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+        const uint32_t i = tid * E + r;
+        if (i >= n) continue;
+        const uint32_t idx = (uint32_t)v[r];
         const float4 mn = in.mn[idx], mx = in.mx[idx];
         sMinX[i] = mn.x;
         sMaxX[i] = mx.x;
         sYZ[i] = make_float4(mn.y, mx.y, mn.z, mx.z);
         sIdx[i] = idx;
-        sapKeys[i] = (uint32_t)(sk[i] >> 32);
+        sapKeys[i] = (uint32_t)(v[r] >> 32);
         sapVals[i] = idx;
     }
+}
+
+__global__ void __launch_bounds__(kSapBlockThreads)
+k_sap_block(BroadInput in, uint32_t *sapKeys, uint32_t *sapVals, uint32_t *unsorted, unsigned long long *keys,
+            uint32_t cap, uint32_t bits, DevStats *st, int finalize, const uint32_t *inSlot, const uint32_t *cbody,
+            const uint32_t *cbgen, uint32_t *pairA, uint32_t *pairB) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned long long *bufA = reinterpret_cast<unsigned long long *>(smem);
+    unsigned long long *bufB = bufA + kSapBlockMax;
+    float4 *sYZ = reinterpret_cast<float4 *>(bufB + kSapBlockMax);
+    float *sMinX = reinterpret_cast<float *>(sYZ + kSapBlockMax);
+    float *sMaxX = sMinX + kSapBlockMax;
+    uint32_t *sIdx = reinterpret_cast<uint32_t *>(sMaxX + kSapBlockMax);
+    uint32_t *sOff = sIdx + kSapBlockMax;  // window lengths, then their exclusive scan
+    uint32_t *sPairs = sOff + kSapBlockMax;
+    __shared__ uint32_t s_count, s_scan[40];
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t n = min(*in.d_n, kSapBlockMax);  // the host launches this for at most kSapBlockMax boxes
+    if (tid == 0) {
+        s_count = 0;
+        if (unsorted) *unsorted = 0u;  // as after the multi-kernel sweep
+    }
+    if (n <= kRegSortThreads) sapSortKeys<1>(in, n, bufA, bufB, sapKeys, sapVals, sMinX, sMaxX, sYZ, sIdx);
+    else if (n <= 2 * kRegSortThreads) sapSortKeys<2>(in, n, bufA, bufB, sapKeys, sapVals, sMinX, sMaxX, sYZ, sIdx);
+    else sapSortKeys<4>(in, n, bufA, bufB, sapKeys, sapVals, sMinX, sMaxX, sYZ, sIdx);
     __syncthreads();
+    uint32_t *sCnt = reinterpret_cast<uint32_t *>(bufA);  // pairs per first index (finalize), n entries
+    if (finalize)
+        for (uint32_t i = tid; i < n; i += nt) sCnt[i] = 0u;
     for (uint32_t i = tid; i < n; i += nt) {
         // window: entries i+1 .. lo-1 with min.x <= max.x(i) (k_sap_window)
         const float x = sMaxX[i];
@@ -222,6 +246,7 @@ k_sap_block(BroadInput in, uint32_t *sapKeys, uint32_t *sapVals, uint32_t *unsor
     // thread t: flattened items [t C, (t + 1) C) of the windows, in order
     const uint32_t C = (W + nt - 1) / nt;
     const uint32_t w0 = tid * C, wEnd = min(W, w0 + C);
+    const uint32_t pairCap = finalize ? kSapBlockPairs : cap;
     if (w0 < wEnd) {
         uint32_t lo = 0, hi = n;  // i = last entry with off[i] <= w0
         while (lo < hi) {
@@ -236,9 +261,17 @@ k_sap_block(BroadInput in, uint32_t *sapKeys, uint32_t *sapVals, uint32_t *unsor
         uint32_t fi = sIdx[i];
         for (uint32_t w = w0; w < wEnd; ++w) {
             if (overlapYZ(f, sYZ[j])) {
-                const uint32_t a = fi, b = sIdx[j];
-                const uint32_t slot = atomicAdd(&s_count, 1u);
-                if (slot < cap) keys[slot] = ((unsigned long long)(a < b ? a : b) << bits) | (a < b ? b : a);
+                const uint32_t b = sIdx[j];
+                const uint32_t lo2 = fi < b ? fi : b, hi2 = fi < b ? b : fi;
+                const uint32_t slot = aggregatedAppend(&s_count);
+                if (slot < pairCap) {
+                    if (finalize) {
+                        sPairs[slot] = lo2 << bits | hi2;
+                        atomicAdd(&sCnt[lo2], 1u);
+                    } else {
+                        keys[slot] = ((unsigned long long)lo2 << bits) | hi2;
+                    }
+                }
             }
             if (++j == end && w + 1 < wEnd) {
                 do {
@@ -252,11 +285,116 @@ k_sap_block(BroadInput in, uint32_t *sapKeys, uint32_t *sapVals, uint32_t *unsor
         }
     }
     __syncthreads();
+    const uint32_t P = s_count;
     if (tid == 0) {
         atomicAdd(&st->xWindow, (unsigned long long)W);
         st->windowWork = W;
-        atomicAdd(&st->rawPairs, s_count);
+        atomicAdd(&st->rawPairs, P);
     }
+    if (!finalize) return;
+    if (P > kSapBlockPairs) {
+        if (tid == 0) atomicOr(&st->err, kErrSmallPath);
+        return;
+    }
+    const uint32_t mask = (1u << bits) - 1u;
+    // Pairs in order of their first index: list offsets, then a scatter with
+    // the counters as cursors (afterwards sCnt[f] is the end of f's list).
+    uint32_t *sSec = reinterpret_cast<uint32_t *>(bufB);      // second indices by list
+    uint32_t *sLong = sOff;                                   // first indices with long lists
+    uint32_t *sBits = reinterpret_cast<uint32_t *>(sYZ);      // a bitmap of kSapBlockMax bits per warp
+    blockExclusiveScanArray(sCnt, n, s_scan);  // ends with a barrier
+    if (tid == 0) s_count = 0;                 // now counts the long lists
+    for (uint32_t k = tid; k < P; k += nt) {
+        const uint32_t key = sPairs[k];
+        sSec[atomicAdd(&sCnt[key >> bits], 1u)] = key & mask;
+    }
+    __syncthreads();
+    // Short lists: one thread sorts its list (insertion) and writes the full
+    // keys back in order; long ones are queued for a warp.
+    constexpr uint32_t kShortList = 32;
+    for (uint32_t f = tid; f < n; f += nt) {
+        const uint32_t begin = f ? sCnt[f - 1] : 0u, end = sCnt[f];
+        if (end - begin > kShortList) {
+            sLong[aggregatedAppend(&s_count)] = f;
+            continue;
+        }
+        for (uint32_t x = begin + 1; x < end; ++x) {
+            const uint32_t v = sSec[x];
+            uint32_t y = x;
+            for (; y > begin && sSec[y - 1] > v; --y) sSec[y] = sSec[y - 1];
+            sSec[y] = v;
+        }
+        for (uint32_t x = begin; x < end; ++x) sPairs[x] = f << bits | sSec[x];
+    }
+    __syncthreads();
+    {
+        const uint32_t lane = tid & 31, warp = tid >> 5, nLong = s_count;
+        constexpr uint32_t kWords = kSapBlockMax / 32, kPerLane = kWords / 32;
+        uint32_t *bm = sBits + warp * kWords;
+        for (uint32_t q = warp; q < nLong; q += nt / 32) {
+            const uint32_t f = sLong[q];
+            const uint32_t begin = f ? sCnt[f - 1] : 0u, end = sCnt[f];
+#pragma unroll
+            for (uint32_t r = 0; r < kPerLane; ++r) bm[lane * kPerLane + r] = 0u;
+            __syncwarp();
+            for (uint32_t x = begin + lane; x < end; x += 32) atomicOr(&bm[sSec[x] >> 5], 1u << (sSec[x] & 31u));
+            __syncwarp();
+            // lane l owns words [l kPerLane, (l + 1) kPerLane): its set bits
+            // come after those of the lanes before it
+            uint32_t words[kPerLane], cnt = 0;
+#pragma unroll
+            for (uint32_t r = 0; r < kPerLane; ++r) {
+                words[r] = bm[lane * kPerLane + r];
+                cnt += __popc(words[r]);
+            }
+            uint32_t incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                if ((int)lane >= o) incl += t;
+            }
+            uint32_t out = begin + incl - cnt;
+#pragma unroll
+            for (uint32_t r = 0; r < kPerLane; ++r)
+                for (uint32_t wbits = words[r]; wbits; wbits &= wbits - 1u)
+                    sPairs[out++] = f << bits | ((lane * kPerLane + r) * 32u + (uint32_t)(__ffs(wbits) - 1));
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    // slot mapping, same-body filter, compaction (k_pairs_block)
+    uint32_t *sFlag = reinterpret_cast<uint32_t *>(bufB);
+    uint32_t unique = 0;
+    for (uint32_t k = tid; k < P; k += nt) {
+        const uint32_t key = sPairs[k];
+        bool keep = !(k > 0 && sPairs[k - 1] == key);
+        if (keep) {
+            ++unique;
+            uint32_t a = key >> bits, b = key & mask;
+            if (inSlot) {
+                a = inSlot[a];
+                b = inSlot[b];
+            }
+            if (cbody && cbody[a] == cbody[b] && cbgen[a] == cbgen[b]) keep = false;
+        }
+        sFlag[k] = keep ? 1u : 0u;
+    }
+    if (unique) atomicAdd(&st->uniquePairs, unique);
+    __syncthreads();
+    const uint32_t total = blockExclusiveScanArray(sFlag, P, s_scan);
+    for (uint32_t k = tid; k < P; k += nt) {
+        const uint32_t next = k + 1 < P ? sFlag[k + 1] : total;
+        if (next == sFlag[k]) continue;
+        const uint32_t key = sPairs[k];
+        uint32_t a = key >> bits, b = key & mask;
+        if (inSlot) {
+            a = inSlot[a];
+            b = inSlot[b];
+        }
+        pairA[sFlag[k]] = a;
+        pairB[sFlag[k]] = b;
+    }
+    if (tid == 0) st->pairs = total;
 }
 
 // --------------------------------------------------------------- grid ------
@@ -970,8 +1108,12 @@ void launchSapKeys(const BroadInput &in, uint32_t *keys, uint32_t *vals, cudaStr
     PE_LAUNCHED();
 }
 
-void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, BroadBuffers &bb, PairBuffers &pb,
-               DevStats *st, Scratch &ws, cudaStream_t s, const SapCoherence *coh) {
+bool sapFinalizesPairs(const BroadInput &in, const PairBuffers &pb) {
+    return in.maxN <= kSapBlockMax && pb.blockPath && 2 * pb.bits <= 32;
+}
+
+bool launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, BroadBuffers &bb, PairBuffers &pb,
+               DevStats *st, Scratch &ws, cudaStream_t s, const SapCoherence *coh, const PairMapping *finalize) {
     uint32_t *err = &st->err;
     if (in.maxN <= kSapBlockMax) {
         static bool configured = false;
@@ -980,10 +1122,13 @@ void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, Broad
                                           (int)kSapBlockSmem));
             configured = true;
         }
-        k_sap_block<<<1, kSapBlockThreads, kSapBlockSmem, s>>>(in, sapKeys, sapVals, coh ? coh->unsorted : nullptr,
-                                                                pb.keys, pb.cap, pb.bits, st);
+        const bool fin = finalize && sapFinalizesPairs(in, pb);
+        k_sap_block<<<1, kSapBlockThreads, kSapBlockSmem, s>>>(
+            in, sapKeys, sapVals, coh ? coh->unsorted : nullptr, pb.keys, pb.cap, pb.bits, st, fin ? 1 : 0,
+            fin ? finalize->inSlot : nullptr, fin ? finalize->cbody : nullptr, fin ? finalize->cbgen : nullptr, pb.a,
+            pb.b);
         PE_LAUNCHED();
-        return;
+        return fin;
     }
     const uint32_t *sortN = in.d_n;
     if (coh) {
@@ -1003,6 +1148,7 @@ void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, Broad
     launchScanExclusive(bb.len, bb.off, in.d_n, in.maxN, &st->windowWork, ws, err, s);
     k_sap_emit<<<8 * smCount(), 256, 0, s>>>(in.d_n, bb.off, bb.len, bb.sYZ, bb.sIdx, pb.keys, pb.cap, pb.bits, st);
     PE_LAUNCHED();
+    return false;
 }
 
 void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBuffers &pb, DevStats *st, Scratch &ws,
@@ -1049,6 +1195,27 @@ void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBu
     PE_LAUNCHED();
 }
 
+// The n raw pair keys, sorted in registers (blockRegisterSort), into s_buf[0, n);
+// s_buf holds 2 kBlockMaxPairs keys (the sort's two buffers).
+template <int E>
+__device__ __forceinline__ void pairsSortKeys(const unsigned long long *keys, uint32_t n, unsigned long long *s_buf) {
+    static_assert(kRegSortThreads * E <= kBlockMaxPairs, "sort buffers hold the keys");
+    unsigned long long v[E];
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+        const uint32_t i = threadIdx.x * E + r;
+        v[r] = i < n ? keys[i] : ~0ull;
+    }
+    blockRegisterSort<unsigned long long, E>(v, s_buf, s_buf + kBlockMaxPairs);
+    __syncthreads();  // the last shared-memory stage's reads are done
+#pragma unroll
+    for (int r = 0; r < E; ++r) {
+        const uint32_t i = threadIdx.x * E + r;
+        if (i < n) s_buf[i] = v[r];
+    }
+    __syncthreads();
+}
+
 // Single-block finalize for up to kBlockMaxPairs raw pairs: sort, dedup, slot
 // mapping, same-body filter and order-preserving compaction in shared memory.
 __global__ void __launch_bounds__(1024)
@@ -1062,10 +1229,18 @@ k_pairs_block(const unsigned long long *keys, uint32_t bits, const uint32_t *inS
         if (threadIdx.x == 0) atomicOr(&st->err, kErrSmallPath);
         return;
     }
-    const uint32_t n2 = nextPow2(n > 0 ? n : 1);
-    for (uint32_t i = threadIdx.x; i < n2; i += blockDim.x) s_buf[i] = i < n ? keys[i] : ~0ull;
-    __syncthreads();
-    const unsigned long long *s_keys = blockMergeSort<unsigned long long>(s_buf, s_buf + kBlockMaxPairs, n2);
+    // up to 4096 keys sorted in registers; more (eight 64-bit keys a thread
+    // would not stay in registers) by the shared-memory merge sort
+    const unsigned long long *s_keys = s_buf;
+    if (n <= kRegSortThreads) pairsSortKeys<1>(keys, n, s_buf);
+    else if (n <= 2 * kRegSortThreads) pairsSortKeys<2>(keys, n, s_buf);
+    else if (n <= 4 * kRegSortThreads) pairsSortKeys<4>(keys, n, s_buf);
+    else {
+        const uint32_t n2 = nextPow2(n);
+        for (uint32_t i = threadIdx.x; i < n2; i += blockDim.x) s_buf[i] = i < n ? keys[i] : ~0ull;
+        __syncthreads();
+        s_keys = blockMergeSort<unsigned long long>(s_buf, s_buf + kBlockMaxPairs, n2);
+    }
     const unsigned long long mask = (1ull << bits) - 1ull;
     uint32_t unique = 0;
     for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {

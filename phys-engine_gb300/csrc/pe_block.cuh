@@ -82,6 +82,59 @@ template <class K> __device__ __forceinline__ K *blockMergeSort(K *a, K *b, uint
     return src;
 }
 
+// Bitonic sort of N = kRegSortThreads * E keys held in registers, ascending;
+// thread t holds positions [t E, t E + E) before and after.  Compare-exchange
+// stages whose partner is in the same thread run in registers, those whose
+// partner is in the same warp through shuffles, and only the stages with
+// partners in other warps (j >= 32 E) through shared memory: bufA and bufB
+// (N keys each) are used in turn, so one barrier per such stage suffices.
+// All kRegSortThreads threads of the block call it (blockDim.x must be that).
+constexpr uint32_t kRegSortThreads = 1024;
+template <class K, int E> __device__ __forceinline__ void blockRegisterSort(K (&v)[E], K *bufA, K *bufB) {
+    constexpr uint32_t N = kRegSortThreads * E;
+    const uint32_t t = threadIdx.x;
+    bool useA = true;
+#pragma unroll
+    for (uint32_t k = 2; k <= N; k <<= 1) {
+#pragma unroll
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32u * E) {
+                K *buf = useA ? bufA : bufB;
+                useA = !useA;
+#pragma unroll
+                for (int r = 0; r < E; ++r) buf[t * E + r] = v[r];
+                __syncthreads();
+#pragma unroll
+                for (int r = 0; r < E; ++r) {
+                    const uint32_t i = t * E + r;
+                    const K p = buf[i ^ j];
+                    const bool keepMin = ((i & j) == 0) == ((i & k) == 0);
+                    v[r] = keepMin ? (p < v[r] ? p : v[r]) : (p > v[r] ? p : v[r]);
+                }
+            } else if (j >= (uint32_t)E) {
+#pragma unroll
+                for (int r = 0; r < E; ++r) {
+                    const uint32_t i = t * E + r;
+                    const K p = __shfl_xor_sync(0xffffffffu, v[r], j / E);
+                    const bool keepMin = ((i & j) == 0) == ((i & k) == 0);
+                    v[r] = keepMin ? (p < v[r] ? p : v[r]) : (p > v[r] ? p : v[r]);
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < E; ++r) {
+                    if ((r & j) != 0) continue;
+                    const uint32_t i = t * E + r;
+                    const K x = v[r], y = v[r ^ j];
+                    if ((x > y) == ((i & k) == 0)) {
+                        v[r] = y;
+                        v[r ^ j] = x;
+                    }
+                }
+            }
+        }
+    }
+}
+
 __device__ __forceinline__ uint32_t nextPow2(uint32_t v) {
     uint32_t p = 1;
     while (p < v) p <<= 1;

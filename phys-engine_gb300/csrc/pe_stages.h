@@ -185,8 +185,17 @@ struct SapCoherence {
     uint32_t *unsorted;
     uint32_t *sortCount;
 };
-void launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, BroadBuffers &bb, PairBuffers &pb,
-               DevStats *st, Scratch &ws, cudaStream_t s, const SapCoherence *coh = nullptr);
+// Collider slot of each broadphase input (null: the input index is the slot)
+// and the body / generation of each slot, for the pair finalize.
+struct PairMapping {
+    const uint32_t *inSlot, *cbody, *cbgen;
+};
+// Returns true when the sweep also finalized the pairs (one-block sweep with
+// `finalize` given and the raw pairs expected to fit it): the caller then
+// launches no separate finalize.
+bool launchSap(const BroadInput &in, uint32_t *sapKeys, uint32_t *sapVals, BroadBuffers &bb, PairBuffers &pb,
+               DevStats *st, Scratch &ws, cudaStream_t s, const SapCoherence *coh = nullptr,
+               const PairMapping *finalize = nullptr);
 void launchGrid(const BroadInput &in, double fixedCell, BroadBuffers &bb, PairBuffers &pb, DevStats *st, Scratch &ws,
                 cudaStream_t s);
 // DynamicTree: every overlapping pair through a linear BVH (pair keys for

@@ -788,13 +788,16 @@ void World::runPipeline(float dt) {
                       sap ? sapKeys_.ptr : nullptr, sapVals_.ptr, &st->inputCount, ws_, &st->err, s);
     }
     BroadInput in{dense_ ? aabbMin_.ptr : inMin_.ptr, dense_ ? aabbMax_.ptr : inMax_.ptr, &st->inputCount, nc_};
-    if (sap) launchSap(in, sapKeys_.ptr, sapVals_.ptr, bb_, pb_, st, ws_, s, dense_ ? &coh : nullptr);
+    const PairMapping mapping{dense_ ? nullptr : inSlot_.ptr, cbody_.ptr, cbgen_.ptr};
+    bool finalized = false;
+    if (sap) finalized = launchSap(in, sapKeys_.ptr, sapVals_.ptr, bb_, pb_, st, ws_, s, dense_ ? &coh : nullptr,
+                                   &mapping);
     else if (algorithm == 2) launchLbvh(in, lb_, pb_, st, ws_, s);
     else launchGrid(in, cellSize, bb_, pb_, st, ws_, s);
     if (!sap && pb_.bodyPath)
-        launchGridBodyPairs(in, bb_, pb_, dense_ ? nullptr : inSlot_.ptr, cbody_.ptr, cbgen_.ptr, st, ws_, s, fused);
-    else
-        launchPairsFinalize(dense_ ? nullptr : inSlot_.ptr, cbody_.ptr, cbgen_.ptr, pb_, st, ws_, s);
+        launchGridBodyPairs(in, bb_, pb_, mapping.inSlot, cbody_.ptr, cbgen_.ptr, st, ws_, s, fused);
+    else if (!finalized)
+        launchPairsFinalize(mapping.inSlot, cbody_.ptr, cbgen_.ptr, pb_, st, ws_, s);
     ManifoldView mv = manifoldView();
     launchNarrowphase(w, pb_, mv, mcap_, st, ws_, s, fused ? ws_.scanState + narrowOff : nullptr, fused);
     const bool sleeping = sleepingEnabled;
