@@ -643,10 +643,12 @@ __global__ void __launch_bounds__(kIslPrepThreads) k_prepare_islands(SolveArgs a
             gB = a.mv.genB[m];
         }
         const uint32_t M = min(*a.count, a.mcap);
+        // no unions while the solver skips the island attempt (the links stay 0)
+        const bool unite = __ldcg(a.sb.pathHint) == 0u;
         if (M <= blockM && m < M) {
             const uint32_t fl = manifoldFlagsOf(a.w, ba, bb, gA, gB);
             a.sb.dyn[m] = fl;
-            if ((fl & (kFlagValid | kFlagDynA | kFlagDynB)) == (kFlagValid | kFlagDynA | kFlagDynB) &&
+            if (unite && (fl & (kFlagValid | kFlagDynA | kFlagDynB)) == (kFlagValid | kFlagDynA | kFlagDynB) &&
                 !islandUnite(a.sb.islLink, ba, bb))
                 atomicOr(&a.st->islandRefused, 1u);
         }
@@ -657,6 +659,12 @@ __global__ void __launch_bounds__(kIslPrepThreads) k_prepare_islands(SolveArgs a
         const uint32_t M = min(*a.count, a.mcap), cacheN = *a.oldCount;
         const bool work = M <= blockM && blockIdx.x < 4 * M;  // some item of this block is live
         const bool inShared = cacheN <= kIslPrepKeyCap;
+        // a larger cache: every stride-th key in shared memory (two-level search)
+        const uint32_t stride = inShared ? 1u : (cacheN + kIslPrepKeyCap - 1) / kIslPrepKeyCap;
+        const bool sampled = !inShared && stride <= kCacheSampleStride;
+        const uint32_t nS = sampled ? (cacheN + stride - 1) / stride : 0u;
+        if (work && sampled)
+            for (uint32_t i = tid; i < nS; i += kIslPrepThreads) s_keys[i] = __ldcg(&a.oldCache.key[i * stride]);
         if (work && inShared) {
             // 16-byte loads, every one of a thread's requested before any store
             constexpr uint32_t kPer = kIslPrepKeyCap / 2 / kIslPrepThreads;
@@ -681,7 +689,12 @@ __global__ void __launch_bounds__(kIslPrepThreads) k_prepare_islands(SolveArgs a
         __syncthreads();
         if (work && m < M) {
             PrepTally tally;
-            prepareItem(a, it, inShared ? s_keys : a.oldCache.key, cacheN, tally);
+            if (sampled) {
+                const uint2 range = cacheRangeSampled(s_keys, nS, stride, a.oldCache.key, cacheN, it.ia, it.ib);
+                prepareItem(a, it, a.oldCache.key, cacheN, tally, &range);
+            } else {
+                prepareItem(a, it, inShared ? s_keys : a.oldCache.key, cacheN, tally);
+            }
             flushPrepTally(a, tally);
         }
     }
@@ -721,6 +734,12 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
     }
     const bool hasU = um < M;
     if (!hasU) ufl = 0;
+    // A recent step found islands the island path cannot take (a pile): go
+    // straight to the colour-phase path for a few steps (both paths give the
+    // same result; this one skips the records and finds).  Every rank reads
+    // the hint here, the prepare kernel read it before; rank 0 updates it
+    // after the first cluster barrier.
+    const uint32_t hint = __ldcg(sb.pathHint);
     uint32_t *link = sb.islLink;   // island links of the bodies (0 between steps)
     uint32_t *isize = sb.islSize;  // manifolds listed at an island root (0 between steps)
     unsigned long long *s_sort = reinterpret_cast<unsigned long long *>(smem);
@@ -730,8 +749,8 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
     // join owns the island (M <= blockM <= threads of the cluster: one
     // manifold per thread) ----
     uint32_t ownRoot = kNoIsland;
-    bool refuse = false;
-    if (hasU) {
+    bool refuse = hint != 0u;
+    if (hasU && !refuse) {
         if (!(ufl & kFlagValid)) {
             // an unsolved manifold that still shapes the colouring: colour-phase path
             if (ufl & (kFlagDynA | kFlagDynB)) refuse = true;
@@ -746,12 +765,16 @@ k_solve_cluster(SolveArgs a, CacheView nc, uint32_t cacheCap, uint32_t *newCount
             if (pos == 0) ownRoot = r;
         }
     }
-    if (refuse) atomicOr(&a.st->islandRefused, 1u);
+    if (refuse && (hint == 0u || (rank == 0 && tid == 0))) atomicOr(&a.st->islandRefused, 1u);
     if (tid == 0) cs.island.plans = 0;
     // The cluster barriers have release / acquire semantics at cluster scope:
     // what one rank wrote before a barrier, any rank reads after it.
     cluster.sync();
     stamp(3);
+    if (rank == 0 && tid == 0) {
+        const bool refused = __ldcg(&a.st->islandRefused) != 0u;
+        *sb.pathHint = hint ? hint - 1u : (refused ? kPathHintSteps : 0u);
+    }
     // Every find is done: the links and the island sizes go back to 0.
     uint32_t ownN = 0;
     if (ownRoot != kNoIsland) {

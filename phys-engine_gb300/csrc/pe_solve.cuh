@@ -168,8 +168,58 @@ __device__ __forceinline__ void flushPrepTally(const SolveArgs &a, const PrepTal
 // so an item costs two dependent memory round trips after its manifold data.
 // cacheKeys: the old cache's keys (a shared-memory copy when they fit; the
 // global array otherwise), cacheN of them.
+// Cache entries [rb, re) of the body pair (ia, ib) in the sorted cache keys:
+// the reference's equal_range (sequential_impulse_solver.cpp:448-456).
+__device__ __forceinline__ uint2 cacheRange(const unsigned long long *cacheKeys, uint32_t cacheN, uint32_t ia,
+                                            uint32_t ib) {
+    const unsigned long long key = ((unsigned long long)ia << 32) | ib;
+    uint32_t lo = 0, hi = cacheN;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (cacheKeys[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    uint32_t re = lo;
+    while (re < cacheN && cacheKeys[re] == key) ++re;
+    return make_uint2(lo, re);
+}
+
+// cacheRange for a cache larger than shared memory holds: `sample` holds every
+// stride-th key (sample[i] = key[i stride], nS entries, stride <= kCacheSampleStride)
+// in shared memory; the search there leaves a window of stride keys that holds the
+// range's start, which is read from memory in one round trip with the entries
+// after it.  Same result as cacheRange on the whole array.
+constexpr uint32_t kCacheSampleStride = 8;
+__device__ __forceinline__ uint2 cacheRangeSampled(const unsigned long long *sample, uint32_t nS, uint32_t stride,
+                                                   const unsigned long long *cacheKeys, uint32_t cacheN,
+                                                   uint32_t ia, uint32_t ib) {
+    const unsigned long long key = ((unsigned long long)ia << 32) | ib;
+    uint32_t lo = 0, hi = nS;  // first sample >= key
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (sample[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    // the first key >= key lies in [base, base + stride)
+    const uint32_t base = lo ? (lo - 1) * stride + 1 : 0u;
+    constexpr uint32_t W = kCacheSampleStride + 4;
+    unsigned long long v[W];
+#pragma unroll
+    for (uint32_t j = 0; j < W; ++j) v[j] = base + j < cacheN ? __ldcg(&cacheKeys[base + j]) : ~0ull;
+    uint32_t rb = base, re = base;
+#pragma unroll
+    for (uint32_t j = 0; j < W; ++j) {
+        rb += (base + j < cacheN && v[j] < key) ? 1u : 0u;
+        re += (base + j < cacheN && v[j] <= key) ? 1u : 0u;
+    }
+    // a run of equal keys longer than the window continues in memory
+    while (re < cacheN && re == base + W && __ldcg(&cacheKeys[re]) == key) ++re;
+    return make_uint2(rb, re);
+}
+
 __device__ __forceinline__ void prepareItem(const SolveArgs &a, const PrepItem &t,
-                                            const unsigned long long *cacheKeys, uint32_t cacheN, PrepTally &tally) {
+                                            const unsigned long long *cacheKeys, uint32_t cacheN, PrepTally &tally,
+                                            const uint2 *range = nullptr) {
     const uint32_t mcap = a.mcap;
     const WorldView &w = a.w;
     const uint32_t m = t.m, p = t.p, k = m;  // k: data index
@@ -184,16 +234,9 @@ __device__ __forceinline__ void prepareItem(const SolveArgs &a, const PrepItem &
     const float4 lA4 = w.nxt.lin[ca], aA4 = w.nxt.ang[ca], lB4 = w.nxt.lin[cb], aB4 = w.nxt.ang[cb];
 
     // Cache range for (bodyA, bodyB); generations must match.
-    const unsigned long long key = ((unsigned long long)ia << 32) | ib;
     const unsigned long long gens = ((unsigned long long)t.gA << 32) | t.gB;
-    uint32_t lo = 0, hi = cacheN;
-    while (lo < hi) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (cacheKeys[mid] < key) lo = mid + 1;
-        else hi = mid;
-    }
-    uint32_t rb = lo, re = lo;
-    while (re < cacheN && cacheKeys[re] == key) ++re;
+    const uint2 rr = range ? *range : cacheRange(cacheKeys, cacheN, ia, ib);
+    uint32_t rb = rr.x, re = rr.y;
     float4 preA[4], preB[4];
     float preT[4];
     unsigned long long gen0 = 0;

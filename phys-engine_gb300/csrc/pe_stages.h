@@ -123,7 +123,14 @@ struct SolverBuffers {
     uint32_t *islLink;              // [nb]
     uint32_t *islSize;              // [nb]
     uint4 *islandRec;               // [kIslandMax * nb]
+    // [1] steps in which the cluster solver goes straight to its colour-phase
+    // path without the island attempt (set when an attempt was refused; kept
+    // by the device across steps, zero in a new world)
+    uint32_t *pathHint;
 };
+// Steps the cluster solver skips the island attempt after one was refused (a
+// pile persists for many steps; the attempt is retried when this runs out).
+constexpr uint32_t kPathHintSteps = 16;
 
 constexpr int kMaxColors = 128;
 constexpr uint32_t kBlockMaxPairs = 8192;

@@ -599,6 +599,7 @@ void World::ensureCapacity() {
     sIslLink_.reserve(nb);
     sIslSize_.reserve(nb);
     sIslandRec_.reserve((size_t)kIslandMax * nb);
+    sPathHint_.reserve(1);
     sb_ = SolverBuffers{m,
                         sBest_.ptr,
                         sUsed_.ptr,
@@ -642,7 +643,8 @@ void World::ensureCapacity() {
                         sIslCounters_.ptr,
                         sIslLink_.ptr,
                         sIslSize_.ptr,
-                        sIslandRec_.ptr};
+                        sIslandRec_.ptr,
+                        sPathHint_.ptr};
 
     // Warm-start caches keep their contents when they grow.
     const uint32_t needCache = std::max(4 * m, cacheNeed_);

@@ -286,7 +286,7 @@ class World {
     DeviceArray<uint32_t> sColor_, sDyn_, sColorCount_, sColorStart_, sOrderKeys_, sOrderKeysTmp_, sOrder_, sOrderTmp_, sPcount_,
         sCacheVals_, sCacheValsTmp_, sCacheCounts_, sCacheOff_, sBar_, sCounters_, sStageBody_, sIslandList_;
     DeviceArray<uint32_t> sIslPar_, sIslOff_, sIslRoot_, sIslSlot_, sIslList_, sIslRoots_, sIslLone_, sIslCounters_;
-    DeviceArray<uint32_t> sIslLink_, sIslSize_;
+    DeviceArray<uint32_t> sIslLink_, sIslSize_, sPathHint_;
     DeviceArray<uint4> sIslandRec_;
     DeviceArray<unsigned long long> sIslKeys_, sIslKeysTmp_, sIslSort_;
     DeviceArray<float4> sPm_, sPmI_, sPp_, sPimp_, sPn_;
