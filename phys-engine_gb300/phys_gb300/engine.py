@@ -177,7 +177,15 @@ def lib():
 
 
 def _ptr(a):
+    # a ctypes pointer object: it keeps the array alive for the call, so a
+    # temporary array may be passed
     return None if a is None else a.ctypes.data_as(_P)
+
+
+def _addr(a):
+    # the buffer address as an int (cheaper per call than _ptr); only for
+    # arrays that a name holds for the whole call
+    return None if a is None else a.ctypes.data
 
 
 def _f32(a):
@@ -406,8 +414,8 @@ class GpuWorld:
     def step_io(self, dt, forces=None, positions=None, rotations=None):
         """write_forces + step + read_poses with one synchronisation."""
         f = None if forces is None else _f32(forces)
-        check(self.lib.pe_world_step_io(self.h, _ptr(f), 0 if f is None else len(f), float(dt), _ptr(positions),
-                                        _ptr(rotations)))
+        check(self.lib.pe_world_step_io(self.h, _addr(f), 0 if f is None else len(f), float(dt), _addr(positions),
+                                        _addr(rotations)))
 
     def stream(self) -> int:
         s = _P()

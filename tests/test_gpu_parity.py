@@ -263,6 +263,24 @@ def test_pair_buffer_growth(gpu):
     assert gw.stats()["candidate_pairs"] > 65536
 
 
+def test_one_block_sweep_pair_overflow_reruns(gpu):
+    """A world small enough for the one-block sweep whose raw pairs outgrow the
+    sweep's own finalize (more than 8,192): the step is re-run with the
+    separate finalize and still matches, step after step."""
+    n = 2000
+    rng = np.random.default_rng(3)
+    sc = scenes.generate(scenes.SPHERES_ON_FLOOR, n, 5)
+    sc.pos[1:] = (rng.uniform(-6, 6, (n, 3)) * np.float32([1, 0.25, 1])).astype(np.float32) + np.float32([0, 4, 0])
+    gw, ow = gpu.GpuWorld(order=gpu.ORDER_COLOR), cpu.OracleWorld(order_mode=1)
+    gw.load_scene(sc)
+    ow.load_scene(sc)
+    for s in range(3):
+        gw.step(1 / 60)
+        ow.step(1 / 60)
+        compare_worlds(gw, ow, f"step {s}")
+    assert gw.stats()["candidate_pairs"] > 8192
+
+
 def test_world_read_poses_matches_bodies(gpu):
     """read_poses (positions packed on the device, rotations copied as they
     are) returns the state pe_world_read_bodies reports, and forces written
