@@ -25,7 +25,15 @@
 namespace pe {
 
 // ------------------------------------------------------------- colouring ---
+// Manifolds per thread whose higher-priority neighbours the colouring keeps
+// in shared memory (32 slots each: two bodies x kIslandMax list entries).
+constexpr uint32_t kColorCached = 6;
+constexpr uint32_t kColorSlots = 2 * kIslandMax;
+constexpr uint32_t kNoNeighbour = 0xFFFFFFFFu;
+constexpr size_t kColorSmem = (size_t)kColorCached * kColorSlots * kSolveThreads * sizeof(uint32_t);  // 196,608 bytes
+
 __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
+    extern __shared__ uint32_t s_hp[];  // [kColorCached][kColorSlots][blockDim.x]
     const uint32_t M = min(*a.count, a.mcap);
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
     const WorldView &w = a.w;
@@ -70,6 +78,73 @@ __global__ void __launch_bounds__(kSolveThreads) k_color(SolveArgs a) {
         }
     }
     if (!gridBarrier(sb.bar, &a.st->err)) return;
+    if (__ldcg(&sb.counters[1]) == 0u && (M + gstride - 1) / gstride <= kColorCached) {
+        // Each thread reads its manifolds' neighbour lists once and keeps the
+        // higher-priority neighbours in shared memory; every pass then asks
+        // for all of a manifold's neighbour colours in one round trip.
+        const uint32_t T = blockDim.x, R = (M + gstride - 1) / gstride;
+        uint32_t pendingMask = 0;
+        for (uint32_t k = 0; k < R; ++k) {
+            const uint32_t m = gtid + k * gstride;
+            if (m >= M) continue;
+            pendingMask |= 1u << k;
+            uint32_t *row = s_hp + (size_t)k * kColorSlots * T + threadIdx.x;
+            const uint32_t p = colorPriority(m), d = sb.dyn[m];
+            uint32_t n[2], bs[2];
+            for (int e = 0; e < 2; ++e) {
+                bs[e] = e ? a.mv.bodyB[m] : a.mv.bodyA[m];
+                n[e] = (d & (1u << e)) ? min(__ldcg(&incCount[bs[e]]), kIslandMax) : 0u;
+            }
+            uint32_t o[kColorSlots];
+#pragma unroll
+            for (uint32_t i = 0; i < kColorSlots; ++i) {
+                const uint32_t e = i / kIslandMax, j = i % kIslandMax;
+                o[i] = j < n[e] ? __ldcg(&inc[(size_t)bs[e] * kIslandMax + j]) : kNoNeighbour;
+            }
+#pragma unroll
+            for (uint32_t i = 0; i < kColorSlots; ++i)
+                row[(size_t)i * T] = (o[i] != kNoNeighbour && o[i] != m && colorPriority(o[i]) > p) ? o[i]
+                                                                                                  : kNoNeighbour;
+        }
+        uint32_t pass = 0;
+        for (; pendingMask && pass < spinLimit(); ++pass) {
+            for (uint32_t k = 0; k < R; ++k) {
+                if (!(pendingMask >> k & 1u)) continue;
+                const uint32_t m = gtid + k * gstride;
+                const uint32_t *row = s_hp + (size_t)k * kColorSlots * T + threadIdx.x;
+                uint32_t cs[kColorSlots];
+#pragma unroll
+                for (uint32_t i = 0; i < kColorSlots; ++i) {
+                    const uint32_t o = row[(size_t)i * T];
+                    cs[i] = o != kNoNeighbour ? ldvol(&sb.color[o]) : 0xFFFFFFFEu;
+                }
+                unsigned long long u0 = 0, u1 = 0;
+                bool ready = true;
+#pragma unroll
+                for (uint32_t i = 0; i < kColorSlots; ++i) {
+                    if (cs[i] == 0xFFFFFFFEu) continue;
+                    if (cs[i] == kUncolored) ready = false;
+                    else if (cs[i] < 64) u0 |= 1ull << cs[i];
+                    else u1 |= 1ull << (cs[i] - 64);
+                }
+                if (!ready) continue;
+                uint32_t c;
+                if (~u0) c = __ffsll((long long)~u0) - 1;
+                else if (~u1) c = 64 + __ffsll((long long)~u1) - 1;
+                else {
+                    atomicOr(&a.st->err, kErrColors);
+                    c = kMaxColors - 1;
+                }
+                *(volatile uint32_t *)&sb.color[m] = c;
+                aggregatedAppendKeyed(sb.colorCount, c);
+                aggregatedMax32(&a.st->colors, c + 1);
+                pendingMask &= ~(1u << k);
+            }
+        }
+        if (pendingMask) atomicOr(&a.st->err, kErrTimeout);
+        aggregatedMax32(&a.st->colorRounds, pass);
+        return;
+    }
     if (__ldcg(&sb.counters[1]) == 0u) {
         uint32_t pass = 0;
         bool pending = true;
@@ -343,11 +418,12 @@ static int gridFor(uint32_t n, int threads = 256, int maxBlocks = 0) {
     return (int)(b < (uint32_t)maxBlocks ? b : (uint32_t)maxBlocks);
 }
 
-static void launchCooperative(const void *fn, int blocks, SolveArgs &args, cudaStream_t s) {
+static void launchCooperative(const void *fn, int blocks, SolveArgs &args, cudaStream_t s, size_t smem = 0) {
     void *params[] = {&args};
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(blocks);
     cfg.blockDim = dim3(kSolveThreads);
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
@@ -358,11 +434,20 @@ static void launchCooperative(const void *fn, int blocks, SolveArgs &args, cudaS
     ++g_kernelLaunches;
 }
 
+static void configureColor() {
+    static bool configured = false;
+    if (!configured) {
+        PE_CHECK(cudaFuncSetAttribute(k_color, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kColorSmem));
+        configured = true;
+    }
+}
+
 int maxCooperativeBlocks(int smCount) {
     static int perSm = -1;
     if (perSm < 0) {
+        configureColor();
         int a = 0;
-        PE_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_color, kSolveThreads, 0));
+        PE_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_color, kSolveThreads, kColorSmem));
         const int b = solveIslandsBlocksPerSm();
         perSm = a < b ? a : b;
         if (perSm < 1) perSm = 1;
@@ -408,7 +493,10 @@ void launchSolver(const WorldView &w, const ManifoldView &mv, const CacheView &o
     PE_CHECK(cudaMemsetAsync(sb.counters, 0, 4 * sizeof(uint32_t), s));
     PE_CHECK(cudaMemsetAsync(sb.bar, 0, 2 * sizeof(uint32_t), s));
     const bool serial = orderMode == 0;
-    if (!serial) launchCooperative((const void *)k_color, coopBlocks, a, s);
+    if (!serial) {
+        configureColor();
+        launchCooperative((const void *)k_color, coopBlocks, a, s, kColorSmem);
+    }
     // the solve order itself is needed by the serial sweep and by a cache
     // rebuilt in solve order; the island sweeps order each island themselves
     if (serial || !pairOrderCache) {
