@@ -1,5 +1,6 @@
 // Block-level primitives for work that fits one thread block (shared-memory
-// bitonic sort, block-wide exclusive scan over many items).
+// bitonic and merge sorts, a bitonic sort in registers, block-wide exclusive
+// scan over many items).
 #pragma once
 #include <cstdint>
 

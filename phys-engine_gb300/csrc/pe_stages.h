@@ -134,8 +134,10 @@ constexpr uint32_t kPathHintSteps = 16;
 
 constexpr int kMaxColors = 128;
 constexpr uint32_t kBlockMaxPairs = 8192;
-// The single-block finalize (a shared-memory merge sort) is chosen while the
-// expected raw pair count is at most this.
+// The single-block finalize (keys sorted in registers up to 4,096, a
+// shared-memory merge sort above) — or, for the one-block SAP sweep, the
+// sweep's own finalize — is chosen while the expected raw pair count is at
+// most this.
 constexpr uint32_t kBlockPreferredPairs = 6144;
 constexpr int kPreparedVec4 = 10;
 
