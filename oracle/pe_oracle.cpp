@@ -16,6 +16,7 @@
 #include <numeric>
 #include <string>
 #include <atomic>
+#include <chrono>
 #include <condition_variable>
 #include <functional>
 #include <mutex>
@@ -1012,7 +1013,16 @@ inline uint32_t colorPriority(uint32_t m) {
 struct WorldBase {
     virtual ~WorldBase() = default;
     virtual WorldBase *clone() const = 0;
+    // wall time of the last step's stages (ms): integrate + bounds, broadphase,
+    // narrowphase, colouring / order, solve, pose, total
+    double stageMs[7] = {0, 0, 0, 0, 0, 0, 0};
 };
+inline double msSince(std::chrono::steady_clock::time_point &t) {
+    const auto now = std::chrono::steady_clock::now();
+    const double ms = std::chrono::duration<double, std::milli>(now - t).count();
+    t = now;
+    return ms;
+}
 
 template <class T> struct World : WorldBase {
     V3<T> gravity{T(0), T(-9.81f), T(0)};
@@ -1393,6 +1403,11 @@ template <class T> struct World : WorldBase {
         std::vector<PManifold> pc;
         pc.reserve(cs.size());
         size_t prepared = 0;
+        // With more than one worker and at least 4,096 contacts the reference
+        // prepares the contact points on its workers after the bodies
+        // (sequential_impulse_solver.cpp:312-350); each manifold's points
+        // depend only on it and its two prepared bodies.
+        const bool deferPreparation = threads > 1 && cs.size() >= 4096;
         for (size_t k = 0; k < cs.size(); ++k) {
             Manifold<T> &m = cs[ord ? ord[k] : k];
             Body<T> *A = getBody(m.aIdx, m.aGen), *B = getBody(m.bIdx, m.bGen);
@@ -1403,8 +1418,16 @@ template <class T> struct World : WorldBase {
             p.m = &m;
             p.a = prepareBody(A, m.aIdx);
             p.b = prepareBody(B, m.bIdx);
-            prepared += preparePoints(p, inverseDt);
+            if (!deferPreparation) prepared += preparePoints(p, inverseDt);
             pc.push_back(p);
+        }
+        if (deferPreparation) {
+            std::vector<size_t> counts((pc.size() + 63) / 64, 0);
+            Pool::instance().run(threads, counts.size(), [&](size_t chunk) {
+                for (size_t k = 64 * chunk, e = std::min(pc.size(), k + 64); k < e; ++k)
+                    counts[chunk] += preparePoints(pc[k], inverseDt);
+            });
+            for (size_t c : counts) prepared += c;
         }
         ss.solved_contact_count = pc.size();
         ss.prepared_points = prepared;
@@ -1642,6 +1665,8 @@ template <class T> struct World : WorldBase {
 
     // PhysicsWorld::step (physics_world.cpp:518-782)
     void step(T dt) {
+        auto clk = std::chrono::steady_clock::now();
+        const auto start = clk;
         if (sleepingEnabled) prepareSleeping();
         for (uint32_t i = 0; i < bodies.size(); ++i) {
             Body<T> &b = bodies[i];
@@ -1655,6 +1680,7 @@ template <class T> struct World : WorldBase {
             if (!b) continue;
             c.bounds = aabbFromCollider(c, Tf<T>{b->pos, b->rot}, hulls);
         }
+        stageMs[0] = msSince(clk);
         std::vector<Aabb<T>> bounds;
         std::vector<uint32_t> slots;
         std::vector<uint64_t> perBody(bodies.size(), 0);
@@ -1695,6 +1721,7 @@ template <class T> struct World : WorldBase {
                     pairs.end());
         stats.possible_pairs = possible;
         stats.candidate_pairs = pairs.size();
+        stageMs[1] = msSince(clk);
 
         // Narrowphase driver (physics_world.cpp:645-736); results kept in pair order.
         contacts.clear();
@@ -1748,6 +1775,7 @@ template <class T> struct World : WorldBase {
                     integrateVelocity(bodies[i], dt);
         }
 
+        stageMs[2] = msSince(clk);
         if (orderMode == 1) {
             stats.color_count = colorManifolds(contacts, order, colors);
         } else {
@@ -1757,17 +1785,21 @@ template <class T> struct World : WorldBase {
             for (uint32_t i = 0; i < colors.size(); ++i) colors[i] = i;
             stats.color_count = contacts.size();
         }
+        stageMs[3] = msSince(clk);
         solve(contacts, dt, iterations, order.data());
+        stageMs[4] = msSince(clk);
 
         for (auto &b : bodies) {
             if (!b.alive) continue;
             integratePose(b, dt);
             b.force = {};
         }
+        stageMs[5] = msSince(clk);
         if (sleepingEnabled) finishSleeping(dt);
         stats.awake_body_count = stats.sleeping_body_count = 0;
         for (auto &b : bodies)
             if (b.alive && !b.isStatic) ++(b.isSleeping() ? stats.sleeping_body_count : stats.awake_body_count);
+        stageMs[6] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - start).count();
     }
 };
 
@@ -2132,6 +2164,10 @@ int ow_step(ow_world *world, float dt) {
     });
     return 0;
 }
+void ow_get_stage_ms(const ow_world *world, double *ms) {
+    for (int i = 0; i < 7; ++i) ms[i] = world->w->stageMs[i];
+}
+
 void ow_get_stats(const ow_world *world, ow_step_stats *s) {
     dispatch(world, [&](auto &w) { *s = w.stats; });
 }
