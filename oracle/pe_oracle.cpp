@@ -1318,6 +1318,17 @@ template <class T> struct World : WorldBase {
         PBody *a, *b;
         PPoint p[4];
     };
+    // Per-step work arrays kept between steps (the reference keeps its step
+    // workspace the same way, step_workspace.hpp): re-allocating megabytes a
+    // step would touch fresh pages every step.
+    std::vector<PBody> wsBodies;
+    std::vector<uint8_t> wsBodyDone;
+    std::vector<PManifold> wsManifolds;
+    std::vector<Aabb<T>> wsBounds;
+    std::vector<uint32_t> wsSlots;
+    std::vector<uint64_t> wsPerBody;
+    std::vector<Manifold<T>> wsResults;
+    std::vector<int8_t> wsHit;
 
     // prepareContactPoints (sequential_impulse_solver.cpp:101-214)
     static size_t preparePoints(PManifold &pm, T inverseDt) {
@@ -1387,8 +1398,10 @@ template <class T> struct World : WorldBase {
         auto &ss = stats;
         ss.prepared_points = ss.warm_start_comparisons = ss.warm_start_matches = ss.velocity_point_visits = 0;
         const T inverseDt = T(1) / smax(dt, T(1e-6f));
-        std::vector<PBody> pbodies(bodies.size());
-        std::vector<uint8_t> pdone(bodies.size(), 0);
+        std::vector<PBody> &pbodies = wsBodies;
+        std::vector<uint8_t> &pdone = wsBodyDone;
+        pbodies.resize(bodies.size());
+        pdone.assign(bodies.size(), 0);
         auto prepareBody = [&](Body<T> *b, uint32_t idx) -> PBody * {
             PBody &p = pbodies[idx];
             if (!pdone[idx]) {
@@ -1400,7 +1413,8 @@ template <class T> struct World : WorldBase {
             }
             return &p;
         };
-        std::vector<PManifold> pc;
+        std::vector<PManifold> &pc = wsManifolds;
+        pc.clear();
         pc.reserve(cs.size());
         size_t prepared = 0;
         // With more than one worker and at least 4,096 contacts the reference
@@ -1681,9 +1695,12 @@ template <class T> struct World : WorldBase {
             c.bounds = aabbFromCollider(c, Tf<T>{b->pos, b->rot}, hulls);
         }
         stageMs[0] = msSince(clk);
-        std::vector<Aabb<T>> bounds;
-        std::vector<uint32_t> slots;
-        std::vector<uint64_t> perBody(bodies.size(), 0);
+        std::vector<Aabb<T>> &bounds = wsBounds;
+        std::vector<uint32_t> &slots = wsSlots;
+        std::vector<uint64_t> &perBody = wsPerBody;
+        bounds.clear();
+        slots.clear();
+        perBody.assign(bodies.size(), 0);
         uint64_t possible = 0;
         for (uint32_t i = 0; i < colliders.size(); ++i) {
             const Collider<T> &c = colliders[i];
@@ -1725,8 +1742,10 @@ template <class T> struct World : WorldBase {
 
         // Narrowphase driver (physics_world.cpp:645-736); results kept in pair order.
         contacts.clear();
-        std::vector<Manifold<T>> results(pairs.size());
-        std::vector<int8_t> hit(pairs.size(), -1);
+        std::vector<Manifold<T>> &results = wsResults;
+        std::vector<int8_t> &hit = wsHit;
+        results.resize(pairs.size());
+        hit.assign(pairs.size(), -1);
         auto gen = [&](size_t k) {
             const Collider<T> &ca = colliders[pairs[k].first], &cb = colliders[pairs[k].second];
             Body<T> *A = getBody(ca.bodyIndex, ca.bodyGeneration), *B = getBody(cb.bodyIndex, cb.bodyGeneration);
