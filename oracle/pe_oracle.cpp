@@ -329,6 +329,30 @@ using Pair = std::pair<uint32_t, uint32_t>;
 // (first, second) order; a stable sort on the pair reproduces either.
 inline void sortPairsLex(std::vector<Pair> &pairs) { std::sort(pairs.begin(), pairs.end()); }
 
+// The sweep's pair sort (broadphase.cpp:27-60): with at least as many pairs
+// as boxes, two stable counting passes (by second, then by first) in linear
+// time; otherwise a comparison sort.  Either gives the lexicographic order.
+inline void sortPairsLinear(std::vector<Pair> &pairs, size_t keyCount) {
+    if (pairs.size() < 2) return;
+    if (pairs.size() < keyCount) return sortPairsLex(pairs);
+    thread_local std::vector<Pair> buffer;
+    thread_local std::vector<size_t> counts;
+    buffer.resize(pairs.size());
+    auto pass = [&](const std::vector<Pair> &in, std::vector<Pair> &out, auto key) {
+        counts.assign(keyCount, 0);
+        for (const Pair &p : in) ++counts[key(p)];
+        size_t offset = 0;
+        for (size_t &c : counts) {
+            const size_t n = c;
+            c = offset;
+            offset += n;
+        }
+        for (const Pair &p : in) out[counts[key(p)]++] = p;
+    };
+    pass(pairs, buffer, [](const Pair &p) { return p.second; });
+    pass(buffer, pairs, [](const Pair &p) { return p.first; });
+}
+
 // SAP: detail::findCandidatePairs (broadphase.cpp:205-290)
 template <class T>
 void sapPairs(const std::vector<Aabb<T>> &bounds, std::vector<Pair> &pairs, ow_step_stats &st, int threads) {
@@ -336,7 +360,12 @@ void sapPairs(const std::vector<Aabb<T>> &bounds, std::vector<Pair> &pairs, ow_s
         Aabb<T> b;
         uint32_t idx;
     };
-    std::vector<Entry> entries(bounds.size());
+    // kept between calls (the reference's workspace); the pool's threads reach
+    // the caller's copies through these references
+    thread_local std::vector<Entry> entriesStore;
+    thread_local std::vector<std::vector<Pair>> outsStore;
+    std::vector<Entry> &entries = entriesStore;
+    entries.resize(bounds.size());
     for (uint32_t i = 0; i < bounds.size(); ++i) entries[i] = {bounds[i], i};
     std::sort(entries.begin(), entries.end(), [](const Entry &l, const Entry &r) {
         if (l.b.min.x != r.b.min.x) return l.b.min.x < r.b.min.x;
@@ -361,7 +390,9 @@ void sapPairs(const std::vector<Aabb<T>> &bounds, std::vector<Pair> &pairs, ow_s
     if (threads > 1 && entries.size() >= 4096) {
         // Parallel sweep over contiguous ranges (broadphase.cpp:244-274).
         size_t ranges = (size_t)threads * 16;
-        std::vector<std::vector<Pair>> outs(ranges);
+        std::vector<std::vector<Pair>> &outs = outsStore;
+        outs.resize(ranges);
+        for (auto &o : outs) o.clear();
         std::vector<uint64_t> cmps(ranges, 0);
         Pool::instance().run(threads, ranges, [&](size_t r) {
             sweep(entries.size() * r / ranges, entries.size() * (r + 1) / ranges, outs[r], cmps[r]);
@@ -373,7 +404,7 @@ void sapPairs(const std::vector<Aabb<T>> &bounds, std::vector<Pair> &pairs, ow_s
     } else {
         sweep(0, entries.size(), pairs, cmp);
     }
-    sortPairsLex(pairs);
+    sortPairsLinear(pairs, bounds.size());
     st.x_window_comparisons = cmp;
     st.aabb_pairs = pairs.size();
     st.grid_comparisons = st.grid_entries = st.grid_overflow_aabbs = 0;
@@ -1014,8 +1045,9 @@ struct WorldBase {
     virtual ~WorldBase() = default;
     virtual WorldBase *clone() const = 0;
     // wall time of the last step's stages (ms): integrate + bounds, broadphase,
-    // narrowphase, colouring / order, solve, pose, total
-    double stageMs[7] = {0, 0, 0, 0, 0, 0, 0};
+    // narrowphase, colouring / order, solve, pose, total; then the solve's
+    // prepare, warm start, velocity iterations and cache update
+    double stageMs[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 };
 inline double msSince(std::chrono::steady_clock::time_point &t) {
     const auto now = std::chrono::steady_clock::now();
@@ -1039,6 +1071,7 @@ template <class T> struct World : WorldBase {
     std::vector<Manifold<T>> contacts;
     std::vector<Pair> pairs;
     std::vector<Cached<T>> cache;
+    std::vector<Cached<T>> wsNextCache;  // the next cache's storage, kept between steps
     std::vector<uint32_t> order, colors;
     ow_step_stats stats{};
 
@@ -1329,6 +1362,8 @@ template <class T> struct World : WorldBase {
     std::vector<uint64_t> wsPerBody;
     std::vector<Manifold<T>> wsResults;
     std::vector<int8_t> wsHit;
+    std::vector<uint32_t> wsIslandStart, wsIslandItems, wsIslandJobs, wsParent, wsLookup, wsIslandOf, wsCounts,
+        wsPoints, wsFill;
 
     // prepareContactPoints (sequential_impulse_solver.cpp:101-214)
     static size_t preparePoints(PManifold &pm, T inverseDt) {
@@ -1396,6 +1431,7 @@ template <class T> struct World : WorldBase {
     // serial path, iteration count and order as parameters.
     void solve(std::vector<Manifold<T>> &cs, T dt, int iters, const uint32_t *ord) {
         auto &ss = stats;
+        auto sclk = std::chrono::steady_clock::now();
         ss.prepared_points = ss.warm_start_comparisons = ss.warm_start_matches = ss.velocity_point_visits = 0;
         const T inverseDt = T(1) / smax(dt, T(1e-6f));
         std::vector<PBody> &pbodies = wsBodies;
@@ -1445,6 +1481,7 @@ template <class T> struct World : WorldBase {
         }
         ss.solved_contact_count = pc.size();
         ss.prepared_points = prepared;
+        stageMs[7] = msSince(sclk);
 
         auto applyCached = [](const PBody &p, const V3<T> &imp, const V3<T> &off) {
             Body<T> *b = p.body;
@@ -1470,10 +1507,11 @@ template <class T> struct World : WorldBase {
         // islands (contacts joined by shared non-static bodies) in parallel,
         // each in solve order; islands share no moving body, so the result is
         // the serial one.
-        std::vector<uint32_t> islandStart, islandItems, islandJobs;
+        std::vector<uint32_t> &islandStart = wsIslandStart, &islandItems = wsIslandItems, &islandJobs = wsIslandJobs;
         const bool parallelIslands = threads > 1 && pc.size() >= 4096;
         if (parallelIslands) {
-            std::vector<uint32_t> parent(bodies.size());
+            std::vector<uint32_t> &parent = wsParent;
+            parent.resize(bodies.size());
             std::iota(parent.begin(), parent.end(), 0u);
             auto root = [&](uint32_t i) {
                 while (parent[i] != i) i = parent[i] = parent[parent[i]];
@@ -1485,7 +1523,11 @@ template <class T> struct World : WorldBase {
                 if (ra != rb) parent[std::max(ra, rb)] = std::min(ra, rb);
             }
             const uint32_t none = 0xFFFFFFFFu;
-            std::vector<uint32_t> lookup(bodies.size(), none), islandOf(pc.size()), counts, points;
+            std::vector<uint32_t> &lookup = wsLookup, &islandOf = wsIslandOf, &counts = wsCounts, &points = wsPoints;
+            lookup.assign(bodies.size(), none);
+            islandOf.resize(pc.size());
+            counts.clear();
+            points.clear();
             for (size_t k = 0; k < pc.size(); ++k) {
                 const PManifold &p = pc[k];
                 const uint32_t r = root(p.a->body->isStatic ? p.m->bIdx : p.m->aIdx);
@@ -1500,7 +1542,8 @@ template <class T> struct World : WorldBase {
             }
             islandStart.assign(counts.size() + 1, 0);
             for (size_t i = 0; i < counts.size(); ++i) islandStart[i + 1] = islandStart[i] + counts[i];
-            std::vector<uint32_t> fill(islandStart.begin(), islandStart.end() - 1);
+            std::vector<uint32_t> &fill = wsFill;
+            fill.assign(islandStart.begin(), islandStart.end() - 1);
             islandItems.resize(pc.size());
             for (size_t k = 0; k < pc.size(); ++k) islandItems[fill[islandOf[k]]++] = (uint32_t)k;
             // largest islands first (load balance only)
@@ -1514,12 +1557,17 @@ template <class T> struct World : WorldBase {
         const T matchSq = T(0.05f) * T(0.05f);
         auto warmStartOne = [&](PManifold &p, uint64_t &cmp, uint64_t &matches) {
             Manifold<T> &m = *p.m;
-            auto lo = std::lower_bound(cache.begin(), cache.end(), m, [](const Cached<T> &c, const Manifold<T> &k) {
-                return cacheLess(c.aIdx, c.aGen, c.bIdx, c.bGen, k.aIdx, k.aGen, k.bIdx, k.bGen);
-            });
-            auto hi = std::upper_bound(cache.begin(), cache.end(), m, [](const Manifold<T> &k, const Cached<T> &c) {
-                return cacheLess(k.aIdx, k.aGen, k.bIdx, k.bGen, c.aIdx, c.aGen, c.bIdx, c.bGen);
-            });
+            // the pair's entries (std::equal_range, as the reference searches)
+            struct PairOrder {
+                bool operator()(const Cached<T> &c, const Manifold<T> &k) const {
+                    return cacheLess(c.aIdx, c.aGen, c.bIdx, c.bGen, k.aIdx, k.aGen, k.bIdx, k.bGen);
+                }
+                bool operator()(const Manifold<T> &k, const Cached<T> &c) const {
+                    return cacheLess(k.aIdx, k.aGen, k.bIdx, k.bGen, c.aIdx, c.aGen, c.bIdx, c.bGen);
+                }
+            };
+            const auto range = std::equal_range(cache.begin(), cache.end(), m, PairOrder{});
+            const auto lo = range.first, hi = range.second;
             for (uint32_t i = 0; i < m.pointCount; ++i) {
                 Point<T> &pt = m.points[i];
                 PPoint &pp = p.p[i];
@@ -1559,6 +1607,7 @@ template <class T> struct World : WorldBase {
         }
         ss.warm_start_comparisons = cmp;
         ss.warm_start_matches = matches;
+        stageMs[8] = msSince(sclk);
 
         // solvePrepared (sequential_impulse_solver.cpp:520-603)
         auto solveOne = [&](PManifold &p) {
@@ -1614,10 +1663,15 @@ template <class T> struct World : WorldBase {
                 for (PManifold &p : pc) solveOne(p);
         }
         ss.velocity_point_visits = prepared * (uint64_t)iters;
+        stageMs[9] = msSince(sclk);
 
         // Cache update (sequential_impulse_solver.cpp:623-681): with sleeping
-        // on, the entries of sleeping contacts are carried over first.
-        std::vector<Cached<T>> next;
+        // on, the entries of sleeping contacts are carried over first.  The
+        // next cache's storage is kept between steps, and a cache that comes
+        // out already in pair order (manifolds in pair order) needs no sort,
+        // as in the reference.
+        std::vector<Cached<T>> &next = wsNextCache;
+        next.clear();
         if (sleepingEnabled)
             for (const Cached<T> &c : cache) {
                 const Body<T> *A = getBody(c.aIdx, c.aGen), *B = getBody(c.bIdx, c.bGen);
@@ -1633,10 +1687,12 @@ template <class T> struct World : WorldBase {
                                 pt.tangentImpulse1, pt.tangentImpulse2});
             }
         }
-        std::stable_sort(next.begin(), next.end(), [](const Cached<T> &l, const Cached<T> &r) {
+        auto pairLess = [](const Cached<T> &l, const Cached<T> &r) {
             return cacheLess(l.aIdx, l.aGen, l.bIdx, l.bGen, r.aIdx, r.aGen, r.bIdx, r.bGen);
-        });
+        };
+        if (!std::is_sorted(next.begin(), next.end(), pairLess)) std::stable_sort(next.begin(), next.end(), pairLess);
         cache.swap(next);
+        stageMs[10] = msSince(sclk);
     }
 
     uint32_t colorManifolds(const std::vector<Manifold<T>> &cs, std::vector<uint32_t> &ord,
@@ -1746,20 +1802,19 @@ template <class T> struct World : WorldBase {
         std::vector<int8_t> &hit = wsHit;
         results.resize(pairs.size());
         hit.assign(pairs.size(), -1);
-        auto gen = [&](size_t k) {
+        // pair k's manifold into m; -1: a body is gone, 0: no contact, 1: contact
+        auto gen = [&](size_t k, Manifold<T> &m) -> int8_t {
             const Collider<T> &ca = colliders[pairs[k].first], &cb = colliders[pairs[k].second];
             Body<T> *A = getBody(ca.bodyIndex, ca.bodyGeneration), *B = getBody(cb.bodyIndex, cb.bodyGeneration);
-            if (!A || !B) return;
+            if (!A || !B) return -1;
             Tf<T> tA = colliderWorld(ca, Tf<T>{A->pos, A->rot});
             Tf<T> tB = colliderWorld(cb, Tf<T>{B->pos, B->rot});
-            Manifold<T> m{};
+            m = Manifold<T>{};
             m.aIdx = ca.bodyIndex;
             m.aGen = ca.bodyGeneration;
             m.bIdx = cb.bodyIndex;
             m.bGen = cb.bodyGeneration;
-            bool h = generateContact(ca, tA, cb, tB, hulls, m);
-            hit[k] = h ? 1 : 0;
-            if (!h) return;
+            if (!generateContact(ca, tA, cb, tB, hulls, m)) return 0;
             for (uint32_t i = 0; i < m.pointCount; ++i) {
                 Point<T> &pt = m.points[i];
                 pt.anchorA = ca.local.p + rotate(ca.local.q, pt.anchorA);
@@ -1767,23 +1822,36 @@ template <class T> struct World : WorldBase {
             }
             m.restitution = smax(A->restitution, B->restitution);
             m.friction = std::sqrt(smax(A->friction, T(0)) * smax(B->friction, T(0)));
-            results[k] = m;
+            return 1;
+        };
+        auto category = [&](size_t k) {
+            const Collider<T> &ca = colliders[pairs[k].first], &cb = colliders[pairs[k].second];
+            return (ca.shape == kHull || cb.shape == kHull) ? 3 : ca.shape + cb.shape;
         };
         if (threads > 1 && pairs.size() >= 4096) {
             Pool::instance().run(threads, (pairs.size() + 63) / 64, [&](size_t chunk) {
-                for (size_t k = 64 * chunk, e = std::min(pairs.size(), k + 64); k < e; ++k) gen(k);
+                for (size_t k = 64 * chunk, e = std::min(pairs.size(), k + 64); k < e; ++k) hit[k] = gen(k, results[k]);
             });
+            for (size_t k = 0; k < pairs.size(); ++k) {
+                if (hit[k] < 0) continue;
+                const int cat = category(k);
+                ++stats.np_candidates[cat];
+                if (!hit[k]) continue;
+                ++stats.np_contacts[cat];
+                contacts.push_back(results[k]);
+            }
         } else {
-            for (size_t k = 0; k < pairs.size(); ++k) gen(k);
-        }
-        for (size_t k = 0; k < pairs.size(); ++k) {
-            if (hit[k] < 0) continue;
-            const Collider<T> &ca = colliders[pairs[k].first], &cb = colliders[pairs[k].second];
-            int cat = (ca.shape == kHull || cb.shape == kHull) ? 3 : ca.shape + cb.shape;
-            ++stats.np_candidates[cat];
-            if (!hit[k]) continue;
-            ++stats.np_contacts[cat];
-            contacts.push_back(results[k]);
+            // one pass in pair order, each manifold built in place
+            contacts.reserve(pairs.size());
+            for (size_t k = 0; k < pairs.size(); ++k) {
+                contacts.emplace_back();
+                const int8_t h = gen(k, contacts.back());
+                if (h != 1) contacts.pop_back();
+                if (h < 0) continue;
+                const int cat = category(k);
+                ++stats.np_candidates[cat];
+                if (h) ++stats.np_contacts[cat];
+            }
         }
         stats.contact_count = contacts.size();
         if (sleepingEnabled) {
@@ -2184,7 +2252,7 @@ int ow_step(ow_world *world, float dt) {
     return 0;
 }
 void ow_get_stage_ms(const ow_world *world, double *ms) {
-    for (int i = 0; i < 7; ++i) ms[i] = world->w->stageMs[i];
+    for (int i = 0; i < 11; ++i) ms[i] = world->w->stageMs[i];
 }
 
 void ow_get_stats(const ow_world *world, ow_step_stats *s) {

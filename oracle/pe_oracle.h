@@ -134,8 +134,9 @@ void ow_get_material(const ow_world *world, uint32_t index, double *mass,
 
 int ow_step(ow_world *world, float dt);
 void ow_get_stats(const ow_world *world, ow_step_stats *stats);
-/* Wall time of the last step's stages (ms): integrate + bounds, broadphase,
-   narrowphase, colouring / order, solve, pose, total. */
+/* Wall time of the last step's stages (ms, 11 values): integrate + bounds,
+   broadphase, narrowphase, colouring / order, solve, pose, total; then the
+   solve's prepare, warm start, velocity iterations and cache update. */
 void ow_get_stage_ms(const ow_world *world, double *ms);
 uint32_t ow_pair_count(const ow_world *world);
 void ow_get_pairs(const ow_world *world, uint32_t *pairs);

@@ -292,8 +292,8 @@ def test_port_threads_like_the_reference(workers):
     solve on a persistent pool with the caller included) and stays bit-identical
     to the unmodified reference; its step time is measured beside the
     reference's on the reference's own 10k-body benchmark scene and must stay
-    within a factor of 1.6 (measured on an 8-core x86 host: 1.15x at 1
-    worker, 1.21x at 8, the port the slower)."""
+    within a factor of 1.3 (measured on an 8-core x86 host: 1.02x at 1
+    worker, 1.03x at 8; the margin is for a loaded host)."""
     import time
 
     sc = scenes.mixed_field(10000, 42)
@@ -318,4 +318,4 @@ def test_port_threads_like_the_reference(workers):
         return min(t)
 
     ratio = best(o) / best(r)
-    assert 1 / 1.6 < ratio < 1.6, ratio
+    assert 1 / 1.3 < ratio < 1.3, ratio
